@@ -1,0 +1,274 @@
+"""Benchmark of the 2D particle-in-cell step (particle-updates/s).
+
+Default workload: the 2D Weibel configuration at scale -- 2048 x 2048 cells,
+64 particles per cell per species (536,870,912 particles), beams +-0.3c,
+u_th = 0.1c, c dt/dx = 0.5 -- loaded on the device from a seeded Philox
+stream.  One step = push + deposition + implicit field solve + particle
+boundaries + bucket sort, i.e. one pass of the reference driver loop body.
+
+Prints one JSON line.  ``--impl reference`` times the CPU restatement of the
+reference (oracle/, OpenMP over all host cores) on the same metric instead.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-updates/s on 1 GB300: mixed vs FP64 path at <=1% growth-rate error"
+UNIT = "particle-updates/s"
+
+# algorithmic bytes per particle for the FP64 kernels (compulsory state traffic)
+BYTES_PUSH_FP64 = 96       # read x,y,ux,uy,uz,id (48 B) + write the same (48 B)
+BYTES_DEPOSIT_FP64 = 56    # read old x,y (16 B) + new x,y,ux,uy,uz (40 B)
+BYTES_DEPOSIT_CELL = 600   # per cell: one 5x5x3 FP64 tile written
+
+
+def config(name):
+    from wumingpic_gb300.loader import Plasma2D
+    if name == "cfg1":
+        return Plasma2D(nx=2048, ny=2048, ppc=64, drift=0.3, u_the=0.1, seed=20261203, np_slack=1.25)
+    if name == "cfg0":
+        return Plasma2D(nx=256, ny=256, ppc=16, drift=0.5, u_the=0.05, seed=20261203)
+    if name.startswith("sq"):  # sqN_PPC: N x N cells, PPC per species, cfg1 physics
+        n, ppc = name[2:].split("_")
+        return Plasma2D(nx=int(n), ny=int(n), ppc=int(ppc), drift=0.3, u_the=0.1, seed=20261203, np_slack=1.25)
+    raise ValueError(name)
+
+
+def workload_desc(p, name):
+    return {"workload": f"2D Weibel {p.nx}x{p.ny} cells, {p.ppc} ppc/species, {p.n_particles} particles, "
+                        f"drift +-{p.drift}c, u_th {p.u_the}c, c*dt/dx={p.c * p.delt / p.delx}",
+            "name": name, "nx": p.nx, "ny": p.ny, "ppc_per_species": p.ppc, "particles": p.n_particles,
+            "l2": "inputs larger than L2 (particle state >> 129 MB)", "parallelism": "replicas"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.rows.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:  # noqa: BLE001
+                pass
+            self._stop.wait(0.2)
+
+    def start(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = sorted(float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit())
+        smax = max((float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()), default=None)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 5 + k and r[5 + k] == "Active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:  # noqa: BLE001
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(name, threads=None, budget_s=20.0):
+    """Oracle (C++ restatement of the reference, OpenMP) on a bounded sample of the
+    workload: same physics and particles per cell, a 256 x 256 grid, as many steps as
+    fit in about budget_s seconds."""
+    from oracle.oracle import Oracle2D
+    from wumingpic_gb300.loader import Plasma2D, load_weibel2d
+    full = config(name)
+    p = Plasma2D(nx=256, ny=256, ppc=full.ppc, drift=full.drift, u_the=full.u_the, seed=full.seed, np_slack=1.25)
+    st = load_weibel2d(p)
+    q, r = p.charges()
+    threads = threads or os.cpu_count() or 1
+    o = Oracle2D(nx=p.nx, ny=p.ny, np_cap=p.np_cap, q=q, r=r, delt=p.delt, gfac=p.gfac, threads=threads)
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        rc = o.step(st)
+        if rc:
+            raise RuntimeError(f"oracle status {rc}")
+        steps += 1
+        if time.perf_counter() - t0 > budget_s or steps >= 50:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": p.n_particles * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} steps of {p.nx}x{p.ny} cells x {p.ppc} ppc/species ({p.n_particles} particles), "
+                      f"same physics as the workload, {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    name = args.config
+    full = config(name)
+    cores = os.cpu_count() or 1
+    vals = []
+    base = None
+    for k in range(args.warmup + args.steps):
+        b = cpu_baseline(name, threads=cores, budget_s=max(2.0, 60.0 / max(1, args.warmup + args.steps)))
+        if k >= args.warmup:
+            vals.append(b["value"])
+            base = b
+    v = sum(vals) / len(vals)
+    base["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": full.n_particles / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_desc(full, name), "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cfg1")
+    ap.add_argument("--precision", default="fp64")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--stages", action="store_true", help="print the per-stage breakdown to stderr")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from wumingpic_gb300.pic2d import Pic2D
+    p = config(args.config)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    g = Pic2D(p, precision=args.precision, stream=stream.cuda_stream)
+    g.load_weibel(seed=p.seed + 7919 * rank)
+    npart = g.num_particles()
+    for _ in range(args.warmup):
+        g.step(1)
+    g.timing(True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        g.step(1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    stages = g.stage_times()
+    g.timing(False)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = npart * world * args.steps / (ms / 1e3)
+
+    # roofline of the dominant kernel, from CUDA events around its launches
+    peak, peak_kind = measured_peaks()
+    dom = max(("push", "deposit"), key=lambda k: stages[k][0])
+    dms, dl = stages[dom]
+    per_launch_ms = dms / max(1, dl if dom == "push" else dl // 2)
+    if dom == "push":
+        alg = BYTES_PUSH_FP64 * npart
+    else:
+        alg = BYTES_DEPOSIT_FP64 * npart + BYTES_DEPOSIT_CELL * p.nx * p.ny
+    achieved = alg / (per_launch_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_push2d" if dom == "push" else "k_deposit2d", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": peak_kind, "note": "FP64 kernels are bound by the FP64 pipe, not by HBM"}
+    launches = int(sum(v[1] for v in stages.values()))
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(g, p, args)
+    base = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            base = cpu_baseline(args.config)
+        except Exception as ex:  # noqa: BLE001
+            base = {"error": str(ex)}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": workload_desc(p, args.config), "precision": args.precision,
+                "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clocks,
+                "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()}}
+        print(json.dumps(line), flush=True)
+        if args.stages:
+            for k, (t, n) in stages.items():
+                print(f"{k:16s} {t / args.steps:10.3f} ms/step {n:8d} launches", file=sys.stderr)
+    g.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def measure_e2e(g, p, args):
+    """The same step through the C ABI with the reference-layout state in host memory:
+    every step copies the state in (host -> device), runs the step and copies it back."""
+    import numpy as np
+    st = g.get_state()
+    steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g.put_state(st)
+        g.step(1)
+        g.get_state(st)
+    dt = time.perf_counter() - t0
+    n = int(st.np2.sum())
+    bytes_state = st.up.nbytes + st.uf.nbytes + st.np2.nbytes + st.cumcnt.nbytes
+    return {"value": n * steps / dt, "unit": UNIT, "h2d_bytes_per_step": int(bytes_state),
+            "d2h_bytes_per_step": int(bytes_state + st.gp.nbytes), "steps": steps,
+            "note": "host arrays in the reference layout, pageable memory"}
+
+
+if __name__ == "__main__":
+    main()

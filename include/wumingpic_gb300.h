@@ -1,0 +1,142 @@
+/*
+ * wumingpic_gb300.h -- C ABI of the GB300 (sm_103a) implementation of WumingPIC's
+ * particle-in-cell time step.
+ *
+ * The library replaces, for one GPU holding the whole domain, the module
+ * procedures that WumingPIC's Fortran drivers ({2d,3d}/proj/STAR/app.f90) call every
+ * step.  Each entry point below names the reference procedure it stands in for.
+ * All arrays passed across this boundary use the reference's own layout
+ * (Fortran column-major, the lower bounds of the Fortran declarations):
+ *
+ *   2D  up, gp     real(8) (ndim, np, nys:nye, nsp)              ndim = 6: x, y, ux, uy, uz, id
+ *       uf         real(8) (6, nxgs-2:nxge+2, nys-2:nye+2)        Bx, By, Bz, Ex, Ey, Ez
+ *       uj         real(8) (3, nxgs-2:nxge+2, nys-2:nye+2)
+ *       df         real(8) (6, nxgs-2:nxge+2, nys-2:nye+2)        CG warm start / field increment
+ *       cumcnt     integer (nxgs:nxge+1, nys:nye, nsp)
+ *       np2        integer (nys:nye, nsp)
+ *
+ * The particle id slot holds the 64-bit integer id bit-cast into a real(8)
+ * (2d/proj/weibel/app.f90:468) and is carried bit for bit.
+ *
+ * State lives on the device between calls (the caller's arrays are read by
+ * wpic_put_* and written by wpic_get_*).  Every function returns a status code
+ * instead of stopping the program as the reference does; none of them aborts.
+ * One host thread per context; all work is ordered on the context's stream.
+ */
+#ifndef WUMINGPIC_GB300_H
+#define WUMINGPIC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define WPIC_OK 0
+#define WPIC_CG_NOT_CONVERGED 1 /* reference: 'stop at cgm after ite_max' (2d/common/field.f90:427-430) */
+#define WPIC_CAPACITY 2         /* reference: 'memory over (np2 > np)' (2d/common/boundary_periodic.f90:231-234) */
+#define WPIC_OUT_OF_RANGE 3     /* a particle outside the domain where the reference indexes out of bounds */
+#define WPIC_MOVED_TOO_FAR 4    /* a particle crossed more than one cell in one step (c*dt >= dx) */
+#define WPIC_NONFINITE 5
+#define WPIC_BAD_ARGUMENT 6
+#define WPIC_CUDA_ERROR 7
+#define WPIC_NOT_INITIALISED 8
+
+/* boundary kinds: replace the procedure arguments of field__fdtd_i
+ * (2d/common/field.f90:66-89) and the driver's choice of boundary module */
+#define WPIC_BC_PERIODIC 0     /* boundary_periodic (2d/common/boundary_periodic.f90) */
+#define WPIC_BC_RECONNECTION 1 /* boundary_reconnection: conducting walls in x
+                                  (2d/proj/reconnection/boundary_reconnection.f90) */
+
+/* arithmetic of the particle and field kernels */
+#define WPIC_FP64 0       /* FP64, fused multiply-add allowed */
+#define WPIC_FP64_EXACT 1 /* FP64 in the reference's operation order (bit-exact parity mode) */
+
+typedef struct wpic_ctx wpic_ctx;
+
+/* The scalar arguments of particle__init (2d/common/particle.f90:18-45),
+ * field__init (2d/common/field.f90:22-63), sort__init (2d/common/sort.f90:16-33)
+ * and bc__init (2d/common/boundary_periodic.f90:26-58), merged.  With one GPU
+ * holding the whole domain nys = nygs and nye = nyge. */
+typedef struct wpic_params {
+  int ndim;                 /* 6 in 2D */
+  int np;                   /* per-row capacity of the caller's particle arrays */
+  int nsp;                  /* number of species, 1 or 2 */
+  int nxgs, nxge, nygs, nyge, nys, nye;
+  double delx, delt, c, gfac;
+  double q[2], r[2];        /* charge and mass of each species */
+  int bc_kind;              /* WPIC_BC_* */
+  int precision;            /* WPIC_FP64 or WPIC_FP64_EXACT */
+  int device_cap;           /* device particle slots per row per species; 0 = np */
+} wpic_params;
+
+/* particle__init + field__init + sort__init + bc__init for a 2D run.
+ * cuda_stream: a cudaStream_t to order all work on, or NULL for a private stream. */
+int wpic_init_2d(wpic_ctx** ctx, const wpic_params* p, void* cuda_stream);
+int wpic_finalize(wpic_ctx* ctx);
+
+/* State exchange in the reference layout.  which = 0: the sorted state 'up'
+ * with its cumcnt; which = 1: the scratch/new state 'gp' (cumcnt ignored).
+ * np2 is shared by both.  put validates np2 <= device capacity and the cumcnt
+ * prefix sums. */
+int wpic_put_particles(wpic_ctx* ctx, int which, const double* up, const int* np2, const int* cumcnt);
+int wpic_get_particles(wpic_ctx* ctx, int which, double* up, int* np2, int* cumcnt);
+int wpic_put_fields(wpic_ctx* ctx, const double* uf);
+int wpic_get_fields(wpic_ctx* ctx, double* uf);
+/* The SAVEd field__fdtd_i arrays (2d/common/field.f90:98): df is the CG warm
+ * start carried from step to step; uj is the current after the boundary fold. */
+int wpic_put_df(wpic_ctx* ctx, const double* df);
+int wpic_get_df(wpic_ctx* ctx, double* df);
+int wpic_get_uj(wpic_ctx* ctx, double* uj);
+
+/* particle__solv(gp, up, uf, cumcnt, nxs, nxe)      2d/common/particle.f90:48-179 */
+int wpic_particle_solv(wpic_ctx* ctx);
+/* field__fdtd_i(uf, up, gp, cumcnt, nxs, nxe, bc__dfield, bc__curre, bc__phi)
+ *                                                   2d/common/field.f90:66-186 */
+int wpic_field_fdtd_i(wpic_ctx* ctx);
+/* ele_cur + bc__curre only (the current that field__fdtd_i deposits), for checks
+ *                                                   2d/common/field.f90:189-316 */
+int wpic_ele_cur(wpic_ctx* ctx);
+/* bc__particle_x(gp, np2)                           2d/common/boundary_periodic.f90:61-96
+ *                                                   2d/proj/reconnection/boundary_reconnection.f90:61-99 */
+int wpic_bc_particle_x(wpic_ctx* ctx);
+/* bc__particle_y(gp, np2)                           2d/common/boundary_periodic.f90:99-248 */
+int wpic_bc_particle_y(wpic_ctx* ctx);
+/* sort__bucket(up, gp, cumcnt, np2, nxs, nxe)       2d/common/sort.f90:36-82 */
+int wpic_sort_bucket(wpic_ctx* ctx);
+/* nsteps iterations of the driver loop body (2d/proj/weibel/app.f90:102-107;
+ * reconnection order 2d/proj/reconnection/app.f90:101-106), fused. */
+int wpic_step(wpic_ctx* ctx, int nsteps);
+
+/* energy_history sums (2d/proj/weibel/app.f90:502-534):
+ * out[0..nsp-1] = sum r (gamma-1) per species, out[nsp] = sum E^2 / 8pi, out[nsp+1] = sum B^2 / 8pi */
+int wpic_energy(wpic_ctx* ctx, double* out);
+
+/* CG control: fixed3[l] >= 0 runs exactly that many iterations for component l
+ * (parity mode), < 0 or fixed3 == NULL uses the reference stopping rule;
+ * ite_max as in cgm (2d/common/field.f90:337).  cg_iters returns the last counts. */
+int wpic_cg_control(wpic_ctx* ctx, const int* fixed3, int ite_max);
+int wpic_cg_iters(wpic_ctx* ctx, int* out3);
+
+/* Device-side seeded loader of a 2D Weibel plasma (no reference counterpart:
+ * the reference loads on the host from an unseeded RNG, 2d/proj/weibel/app.f90:380-437). */
+int wpic_load_weibel_2d(wpic_ctx* ctx, int ppc, uint64_t seed, double drift, int drift_axis, double u_thi,
+                        double u_the, const double* b0);
+
+/* Stage timing with CUDA events on the context stream: enable != 0 starts
+ * accumulating; times returns ms per stage and launch counts (see wpic_stage_name). */
+int wpic_timing_enable(wpic_ctx* ctx, int enable);
+int wpic_timing_get(wpic_ctx* ctx, double* ms, long long* launches, int n);
+const char* wpic_stage_name(int stage);
+int wpic_num_stages(void);
+
+int wpic_synchronize(wpic_ctx* ctx);
+long long wpic_num_particles(wpic_ctx* ctx);
+const char* wpic_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WUMINGPIC_GB300_H */

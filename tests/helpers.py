@@ -1,0 +1,147 @@
+"""Shared test helpers: small seeded cases, an independent charge-density
+routine, and a literal pure-Python restatement of the reference's particle
+migration used to cross-check both the C++ oracle and the closed-form plan the
+GPU kernels implement."""
+import numpy as np
+
+from wumingpic_gb300.loader import Plasma2D, load_weibel2d
+
+
+def small_plasma(nx=16, ny=12, ppc=6, seed=3, **kw):
+    kw.setdefault("drift", 0.5)
+    kw.setdefault("u_the", 0.05)
+    return Plasma2D(nx=nx, ny=ny, ppc=ppc, seed=seed, **kw)
+
+
+def small_case(**kw):
+    p = small_plasma(**kw)
+    return p, load_weibel2d(p)
+
+
+def rho2d(p, up, np2, q):
+    """Charge density sum_p q S(x_p) on the periodic interior grid (nx, ny),
+    with the reference's quadratic spline and cell index int(x)."""
+    R = np.zeros((p.nx, p.ny))
+    for isp in range(p.nsp):
+        for jj in range(p.ny):
+            n = np2[jj, isp]
+            x = up[0, :n, jj, isp] / p.delx
+            y = up[1, :n, jj, isp] / p.delx
+            i = np.floor(x).astype(int)
+            j = np.floor(y).astype(int)
+            dx = x - 0.5 - i
+            dy = y - 0.5 - j
+            sx = [0.5 * (0.5 - dx) ** 2, 0.75 - dx ** 2, 0.5 * (0.5 + dx) ** 2]
+            sy = [0.5 * (0.5 - dy) ** 2, 0.75 - dy ** 2, 0.5 * (0.5 + dy) ** 2]
+            for a in range(3):
+                for b in range(3):
+                    np.add.at(R, ((i + a - 1 - p.nxgs) % p.nx, (j + b - 1 - p.nygs) % p.ny), q[isp] * sx[a] * sy[b])
+    return R
+
+
+def continuity_residual(p, q, up0, gp1, np2, uj):
+    """(rho1 - rho0) dx/dt + div J on the periodic interior; uj already folded."""
+    r0 = rho2d(p, up0, np2, q)
+    r1 = rho2d(p, gp1, np2, q)
+    J = uj[:, 2:-2, 2:-2]
+    res = (r1 - r0) * p.delx / p.delt + (np.roll(J[0], -1, 0) - J[0]) + (np.roll(J[1], -1, 1) - J[1])
+    return np.abs(res).max(), np.abs(r1 - r0).max() * p.delx / p.delt
+
+
+def literal_particle_y(up, np2, nys, nye, nygs, nyge, delx, ndim, npcap):
+    """Pure-Python restatement of boundary_periodic__particle_y with one rank
+    and one thread (2d/common/boundary_periodic.f90:99-248), round-down wraps
+    omitted (callers use positions where the wrap is exact).  up is modified in
+    place (Fortran layout (ndim, np, ny, nsp), 0-based here)."""
+    ny = nye - nys + 1
+    nsp = up.shape[3]
+    for isp in range(nsp):
+        bff = {j: [] for j in range(nys - 1, nye + 2)}
+        flag = {j: [] for j in range(nys, nye + 1)}
+        for j in range(nys, nye + 1):
+            jj = j - nys
+            for ii in range(np2[jj, isp]):
+                jpos = int(up[1, ii, jj, isp] / delx)
+                if jpos != j:
+                    if jpos <= nygs - 1:
+                        up[1, ii, jj, isp] += ny * delx
+                    elif jpos >= nyge + 1:
+                        up[1, ii, jj, isp] -= ny * delx
+                    bff[jpos].append(up[:, ii, jj, isp].copy())
+                    flag[j].append(ii)
+        bff[nye] = bff[nye] + bff[nys - 1]
+        bff[nys] = bff[nys] + bff[nye + 1]
+        for j in range(nys, nye + 1):
+            jj = j - nys
+            n2 = int(np2[jj, isp])
+            fl = flag[j]
+            buf = bff[j]
+            iii = 0
+            cnt = len(buf)
+            cnt_tmp = len(fl) - 1
+            k = 0
+            done = False
+            while k < len(fl) and not done:
+                if cnt == 0:
+                    if n2 - 1 < fl[k]:
+                        break
+                    while n2 - 1 == fl[cnt_tmp]:
+                        n2 -= 1
+                        if n2 - 1 < fl[k]:
+                            done = True
+                            break
+                        cnt_tmp -= 1
+                    if done:
+                        break
+                    up[:, fl[k], jj, isp] = up[:, n2 - 1, jj, isp]
+                    n2 -= 1
+                else:
+                    up[:, fl[k], jj, isp] = buf[iii]
+                    iii += 1
+                    cnt -= 1
+                k += 1
+            for m in range(cnt):
+                up[:, n2 + m, jj, isp] = buf[iii + m]
+            n2 += cnt
+            if n2 > npcap:
+                raise RuntimeError("capacity")
+            np2[jj, isp] = n2
+    return up, np2
+
+
+def closed_form_plan(dirs, ny):
+    """The closed-form post-migration order the GPU implements (see
+    wumingpic_gb300/csrc/kernels_common.cu, k_migrate_plan), for one species.
+    dirs[jj] = int array (n,) of 0 stay / 1 up / 2 down.  Returns, per row, the
+    list of (source row, source slot)."""
+    up = [np.nonzero(d == 1)[0] for d in dirs]
+    dn = [np.nonzero(d == 2)[0] for d in dirs]
+    out = []
+    for jj in range(ny):
+        d = dirs[jj]
+        n = len(d)
+        holes = np.nonzero(d != 0)[0]
+        h = len(holes)
+        if ny == 1:
+            arr = [(jj, s) for s in dn[jj]] + [(jj, s) for s in up[jj]]
+        elif jj == 0:
+            arr = [(1, s) for s in dn[1]] + [(ny - 1, s) for s in up[ny - 1]]
+        elif jj == ny - 1:
+            arr = [(jj - 1, s) for s in up[jj - 1]] + [(0, s) for s in dn[0]]
+        else:
+            arr = [(jj - 1, s) for s in up[jj - 1]] + [(jj + 1, s) for s in dn[jj + 1]]
+        b = len(arr)
+        nn = n - h + b
+        seq = []
+        tail = [t for t in range(n - 1, nn - 1, -1) if d[t] == 0] if b < h else []
+        m = 0
+        for t in range(nn):
+            if t >= n:
+                seq.append(arr[h + t - n])
+            elif d[t] == 0:
+                seq.append((jj, t))
+            else:
+                seq.append(arr[m] if m < b else (jj, tail[m - b]))
+                m += 1
+        out.append(seq)
+    return out

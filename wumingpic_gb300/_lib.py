@@ -1,0 +1,97 @@
+"""ctypes binding of libwumingpic_gb300.so (the C ABI in include/wumingpic_gb300.h).
+
+The library is built in-tree by ``__graft_entry__.build()``.  There is no CPU
+fallback: if the shared library is missing, or no CUDA device is usable, the
+calls fail with an exception.
+"""
+import ctypes
+import os
+
+from . import _build
+
+LIB_PATH = _build.LIB_PATH
+
+# status codes (include/wumingpic_gb300.h)
+OK = 0
+CG_NOT_CONVERGED = 1
+CAPACITY = 2
+OUT_OF_RANGE = 3
+MOVED_TOO_FAR = 4
+NONFINITE = 5
+BAD_ARGUMENT = 6
+CUDA_ERROR = 7
+NOT_INITIALISED = 8
+
+BC_PERIODIC = 0
+BC_RECONNECTION = 1
+FP64 = 0
+FP64_EXACT = 1
+
+
+class WpicParams(ctypes.Structure):
+    _fields_ = [
+        ("ndim", ctypes.c_int), ("np", ctypes.c_int), ("nsp", ctypes.c_int),
+        ("nxgs", ctypes.c_int), ("nxge", ctypes.c_int), ("nygs", ctypes.c_int), ("nyge", ctypes.c_int),
+        ("nys", ctypes.c_int), ("nye", ctypes.c_int),
+        ("delx", ctypes.c_double), ("delt", ctypes.c_double), ("c", ctypes.c_double), ("gfac", ctypes.c_double),
+        ("q", ctypes.c_double * 2), ("r", ctypes.c_double * 2),
+        ("bc_kind", ctypes.c_int), ("precision", ctypes.c_int), ("device_cap", ctypes.c_int),
+    ]
+
+
+class WpicError(RuntimeError):
+    def __init__(self, status, where=""):
+        self.status = status
+        msg = status_string(status)
+        super().__init__(f"{where}: wpic status {status} ({msg})" if where else f"wpic status {status} ({msg})")
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"CUDA library not built: {LIB_PATH}; run __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i, d, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+        L.wpic_init_2d.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(WpicParams), vp]
+        L.wpic_finalize.argtypes = [vp]
+        L.wpic_put_particles.argtypes = [vp, i, vp, vp, vp]
+        L.wpic_get_particles.argtypes = [vp, i, vp, vp, vp]
+        for n in ("wpic_put_fields", "wpic_get_fields", "wpic_put_df", "wpic_get_df", "wpic_get_uj"):
+            getattr(L, n).argtypes = [vp, vp]
+        for n in ("wpic_particle_solv", "wpic_field_fdtd_i", "wpic_ele_cur", "wpic_bc_particle_x",
+                  "wpic_bc_particle_y", "wpic_sort_bucket", "wpic_synchronize"):
+            getattr(L, n).argtypes = [vp]
+        L.wpic_step.argtypes = [vp, i]
+        L.wpic_energy.argtypes = [vp, vp]
+        L.wpic_cg_control.argtypes = [vp, vp, i]
+        L.wpic_cg_iters.argtypes = [vp, vp]
+        L.wpic_load_weibel_2d.argtypes = [vp, i, ctypes.c_uint64, d, i, d, d, vp]
+        L.wpic_timing_enable.argtypes = [vp, i]
+        L.wpic_timing_get.argtypes = [vp, vp, vp, i]
+        L.wpic_stage_name.argtypes = [i]
+        L.wpic_stage_name.restype = ctypes.c_char_p
+        L.wpic_num_stages.argtypes = []
+        L.wpic_num_particles.argtypes = [vp]
+        L.wpic_num_particles.restype = ll
+        L.wpic_status_string.argtypes = [i]
+        L.wpic_status_string.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def status_string(status):
+    try:
+        return lib().wpic_status_string(int(status)).decode()
+    except ImportError:
+        return "library not built"
+
+
+def check(status, where=""):
+    if status != OK:
+        raise WpicError(status, where)
+    return status

@@ -1,0 +1,618 @@
+// C ABI of the library (declared in include/wumingpic_gb300.h): context
+// creation, device memory, reference-layout state exchange, and the host-side
+// sequencing of the kernels of one time step.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "wumingpic_gb300.h"
+#include "wpic_internal.h"
+
+using namespace wpic;
+
+namespace {
+
+enum Stage { SG_PUSH, SG_DEPOSIT, SG_JREDUCE, SG_FIELD, SG_CG, SG_PBC, SG_SORT, SG_COUNT };
+const char* kStageNames[SG_COUNT] = {"push", "deposit", "current_reduce", "field", "cg", "particle_bc", "sort"};
+
+constexpr int CG_CHECK_EVERY = 4;  // CG iterations enqueued between host checks of the active flags
+
+}  // namespace
+
+struct wpic_ctx {
+  wpic_params prm;
+  Dev2D d;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  CGState* h_cg = nullptr;  // pinned mirror of the CG states
+  int* h_err = nullptr;     // pinned mirror of the error word
+  int cg_fixed[3] = {-1, -1, -1};
+  int cg_iters[3] = {0, 0, 0};
+  std::vector<void*> allocs;
+  double* staging = nullptr;
+  size_t staging_bytes = 0;
+  bool have_C = false;
+  bool timing = false;
+  cudaEvent_t ev0[SG_COUNT], ev1[SG_COUNT];
+  bool pending[SG_COUNT] = {};
+  double stage_ms[SG_COUNT] = {};
+  long long stage_launches[SG_COUNT] = {};
+  int sticky_status = WPIC_OK;
+};
+
+namespace {
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return WPIC_OK;
+  fprintf(stderr, "wumingpic_gb300: CUDA error %s\n", cudaGetErrorString(e));
+  return WPIC_CUDA_ERROR;
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+template <typename T>
+int dalloc(wpic_ctx* c, T** p, size_t n) {
+  void* v = nullptr;
+  cudaError_t e = cudaMalloc(&v, n * sizeof(T) + 16);
+  if (e != cudaSuccess) return cuda_status(e);
+  c->allocs.push_back(v);
+  e = cudaMemsetAsync(v, 0, n * sizeof(T) + 16, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  *p = (T*)v;
+  return WPIC_OK;
+}
+
+int alloc_parts(wpic_ctx* c, Parts64* P, size_t n) {
+  int st;
+  if ((st = dalloc(c, &P->x, n))) return st;
+  if ((st = dalloc(c, &P->y, n))) return st;
+  if ((st = dalloc(c, &P->ux, n))) return st;
+  if ((st = dalloc(c, &P->uy, n))) return st;
+  if ((st = dalloc(c, &P->uz, n))) return st;
+  if ((st = dalloc(c, &P->id, n))) return st;
+  return WPIC_OK;
+}
+
+void stage_begin(wpic_ctx* c, int s) {
+  if (c->timing) cudaEventRecord(c->ev0[s], c->stream);
+}
+void stage_end(wpic_ctx* c, int s, int launches) {
+  c->stage_launches[s] += launches;
+  if (c->timing) {
+    cudaEventRecord(c->ev1[s], c->stream);
+    c->pending[s] = true;
+  }
+}
+// Resolve recorded stage events; call after the stream has been synchronised.
+void stage_collect(wpic_ctx* c) {
+  if (!c->timing) return;
+  for (int s = 0; s < SG_COUNT; ++s)
+    if (c->pending[s]) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, c->ev0[s], c->ev1[s]) == cudaSuccess) c->stage_ms[s] += ms;
+      c->pending[s] = false;
+    }
+}
+
+// Synchronise, fold the device error word into a status, clear it.
+int finish(wpic_ctx* c) {
+  cudaError_t e = cudaMemcpyAsync(c->h_err, c->d.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e);
+  stage_collect(c);
+  const int bits = *c->h_err;
+  if (bits) cudaMemsetAsync(c->d.err, 0, sizeof(int), c->stream);
+  if (bits & EB_MOVED_TOO_FAR) return WPIC_MOVED_TOO_FAR;
+  if (bits & EB_OUT_OF_RANGE) return WPIC_OUT_OF_RANGE;
+  if (bits & EB_CAPACITY) return WPIC_CAPACITY;
+  if (bits & EB_CG) return WPIC_CG_NOT_CONVERGED;
+  return WPIC_OK;
+}
+
+bool exact_mode(const wpic_ctx* c) { return c->prm.precision == WPIC_FP64_EXACT; }
+
+#define FP(fn, ...)                       \
+  do {                                    \
+    if (exact_mode(c)) exact::fn(__VA_ARGS__); \
+    else fast::fn(__VA_ARGS__);           \
+  } while (0)
+
+int ensure_staging(wpic_ctx* c, size_t bytes) {
+  if (c->staging_bytes >= bytes) return WPIC_OK;
+  if (c->staging) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->staging);
+    c->staging = nullptr;
+    c->staging_bytes = 0;
+  }
+  CK(cudaMalloc(&c->staging, bytes));
+  c->staging_bytes = bytes;
+  return WPIC_OK;
+}
+
+// ---- the stages of one step ----
+
+void do_push(wpic_ctx* c) {
+  stage_begin(c, SG_PUSH);
+  FP(push2d, c->d, c->stream);
+  stage_end(c, SG_PUSH, 1);
+}
+
+void do_ele_cur(wpic_ctx* c) {
+  stage_begin(c, SG_DEPOSIT);
+  FP(deposit2d, c->d, c->stream);  // k_deposit2d + k_jgather2d
+  stage_end(c, SG_DEPOSIT, 2);
+  stage_begin(c, SG_JREDUCE);
+  curre_fold2d(c->d, c->stream);
+  stage_end(c, SG_JREDUCE, c->d.ph.bc == BC_PERIODIC ? 2 : 1);
+}
+
+int do_cg(wpic_ctx* c) {
+  stage_begin(c, SG_CG);
+  for (int l = 0; l < 3; ++l) c->h_cg[l].fixed = c->cg_fixed[l];
+  // publish the fixed counts; the rest of the state is (re)initialised by the init kernels
+  for (int l = 0; l < 3; ++l)
+    CK(cudaMemcpyAsync(&c->d.cg[l].fixed, &c->h_cg[l].fixed, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  FP(cg_init2d, c->d, c->stream);
+  int launches = 2;
+  for (int guard = 0; guard < 100000; ++guard) {
+    CK(cudaMemcpyAsync(c->h_cg, c->d.cg, 3 * sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (!c->h_cg[0].active && !c->h_cg[1].active && !c->h_cg[2].active) break;
+    for (int k = 0; k < CG_CHECK_EVERY; ++k) {
+      FP(cg_iter_ap2d, c->d, c->stream);
+      FP(cg_iter_update2d, c->d, c->stream);
+      FP(cg_iter_p2d, c->d, c->stream);
+      launches += 6;
+    }
+  }
+  for (int l = 0; l < 3; ++l) c->cg_iters[l] = c->h_cg[l].ite;
+  FP(cg_store2d, c->d, c->stream);
+  stage_end(c, SG_CG, launches + 1);
+  return WPIC_OK;
+}
+
+int do_field(wpic_ctx* c) {
+  do_ele_cur(c);
+  stage_begin(c, SG_FIELD);
+  FP(gkl2d, c->d, c->stream);
+  stage_end(c, SG_FIELD, 1);
+  int st = do_cg(c);
+  if (st) return st;
+  stage_begin(c, SG_FIELD);
+  dfield_ghost2d(c->d, c->stream);
+  FP(efield2d, c->d, c->stream);
+  dfield_ghost2d(c->d, c->stream);
+  uf_add2d(c->d, c->stream);
+  stage_end(c, SG_FIELD, 6);
+  return WPIC_OK;
+}
+
+void do_particle_x(wpic_ctx* c) {
+  stage_begin(c, SG_PBC);
+  particle_x2d(c->d, c->d.B, c->stream);
+  stage_end(c, SG_PBC, 1);
+}
+
+int ensure_C(wpic_ctx* c) {
+  if (c->have_C) return WPIC_OK;
+  int st = alloc_parts(c, &c->d.C, (size_t)c->d.nrowjob * c->d.cap);
+  if (st) return st;
+  c->have_C = true;
+  return WPIC_OK;
+}
+
+// fused migration + bucket sort: B (post-push, post-x-boundary) -> A sorted
+void do_migrate_sort(wpic_ctx* c) {
+  stage_begin(c, SG_PBC);
+  migrate_scan2d(c->d, c->d.B, c->stream);
+  migrate_plan2d(c->d, c->stream);
+  stage_end(c, SG_PBC, 2);
+  stage_begin(c, SG_SORT);
+  sort_rank2d(c->d, c->d.B, c->d.slist, c->stream);
+  gather2d(c->d, c->d.B, c->d.A, c->d.map, c->d.np2new, c->stream);
+  cudaMemcpyAsync(c->d.np2, c->d.np2new, sizeof(int) * c->d.nrowjob, cudaMemcpyDeviceToDevice, c->stream);
+  stage_end(c, SG_SORT, 2);
+}
+
+int one_step(wpic_ctx* c) {
+  do_push(c);
+  if (c->d.ph.bc == BC_RECONNECTION) do_particle_x(c);
+  int st = do_field(c);
+  if (st) return st;
+  if (c->d.ph.bc == BC_PERIODIC) do_particle_x(c);
+  do_migrate_sort(c);
+  return WPIC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
+  if (!out || !p) return WPIC_BAD_ARGUMENT;
+  *out = nullptr;
+  const int nx = p->nxge - p->nxgs + 1, ny = p->nyge - p->nygs + 1;
+  if (p->ndim != 6 || p->nsp < 1 || p->nsp > 2 || nx < 4 || ny < 4 || p->np < 1) return WPIC_BAD_ARGUMENT;
+  if (p->nys != p->nygs || p->nye != p->nyge) return WPIC_BAD_ARGUMENT;  // one device holds the whole domain
+  if (!(p->delx > 0) || !(p->delt > 0) || !(p->c > 0)) return WPIC_BAD_ARGUMENT;
+  if (p->bc_kind != WPIC_BC_PERIODIC && p->bc_kind != WPIC_BC_RECONNECTION) return WPIC_BAD_ARGUMENT;
+  if (p->precision != WPIC_FP64 && p->precision != WPIC_FP64_EXACT) return WPIC_BAD_ARGUMENT;
+  wpic_ctx* c = new wpic_ctx();
+  c->prm = *p;
+  Dev2D& d = c->d;
+  d.g.nx = nx;
+  d.g.ny = ny;
+  d.g.nxgs = p->nxgs;
+  d.g.nygs = p->nygs;
+  d.g.fp = nx + 4;
+  d.g.fplane = (nx + 4) * (ny + 4);
+  d.g.ncell = nx * ny;
+  Phys& ph = d.ph;
+  ph.delx = p->delx;
+  ph.delt = p->delt;
+  ph.c = p->c;
+  ph.gfac = p->gfac;
+  ph.nsp = p->nsp;
+  ph.bc = p->bc_kind;
+  for (int k = 0; k < 2; ++k) {
+    ph.q[k] = k < p->nsp ? p->q[k] : 0.0;
+    ph.r[k] = k < p->nsp ? p->r[k] : 1.0;
+  }
+  // field__init constants (2d/common/field.f90:53-59), same operation order
+  ph.pi = 4.0 * std::atan(1.0);
+  ph.f1 = p->c * p->delt / p->delx;
+  ph.f2 = p->gfac * ph.f1 * ph.f1;
+  ph.f3 = 4.0 * ph.pi * p->delx / p->c;
+  const double t = p->delx / (p->c * p->delt * p->gfac);
+  ph.f4 = 4.0 + t * t;
+  ph.f5 = t * t;
+  ph.d_delx = 1. / p->delx;
+  ph.d_delt = 1. / p->delt;
+  ph.p_d_delx = 1. / p->delx;
+  d.cap = p->device_cap > 0 ? p->device_cap : p->np;
+  d.nrowjob = p->nsp * ny;
+  d.nred = (d.g.ncell + 255) / 256;
+  if (d.nred > 1216) d.nred = 1216;
+  d.ite_max = 100;
+
+  int st = WPIC_OK;
+  if (cuda_stream) {
+    c->stream = (cudaStream_t)cuda_stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete c;
+      return WPIC_CUDA_ERROR;
+    }
+    c->own_stream = true;
+  }
+  const size_t slots = (size_t)d.nrowjob * d.cap;
+  const size_t ncell = d.g.ncell, fplane = d.g.fplane;
+  do {
+    if ((st = alloc_parts(c, &d.A, slots))) break;
+    if ((st = alloc_parts(c, &d.B, slots))) break;
+    if ((st = dalloc(c, &d.cc, (size_t)d.nrowjob * (nx + 1)))) break;
+    if ((st = dalloc(c, &d.np2, d.nrowjob))) break;
+    if ((st = dalloc(c, &d.np2new, d.nrowjob))) break;
+    if ((st = dalloc(c, &d.nup, d.nrowjob))) break;
+    if ((st = dalloc(c, &d.ndown, d.nrowjob))) break;
+    if ((st = dalloc(c, &d.uf, 6 * fplane))) break;
+    if ((st = dalloc(c, &d.df, 6 * fplane))) break;
+    if ((st = dalloc(c, &d.uj, 3 * fplane))) break;
+    if ((st = dalloc(c, &d.gkl, 3 * ncell))) break;
+    if ((st = dalloc(c, &d.cellJ, 75 * ncell))) break;
+    if ((st = dalloc(c, &d.phi, 3 * ncell))) break;
+    if ((st = dalloc(c, &d.p, 3 * ncell))) break;
+    if ((st = dalloc(c, &d.r, 3 * ncell))) break;
+    if ((st = dalloc(c, &d.ap, 3 * ncell))) break;
+    if ((st = dalloc(c, &d.b, 3 * ncell))) break;
+    if ((st = dalloc(c, &d.partials, (size_t)3 * d.nred * 2))) break;
+    if ((st = dalloc(c, &d.cg, 3))) break;
+    if ((st = dalloc(c, &d.err, 1))) break;
+    if ((st = dalloc(c, &d.red_out, 8))) break;
+    if ((st = dalloc(c, &d.mig, slots))) break;
+    if ((st = dalloc(c, &d.ulist, slots))) break;
+    if ((st = dalloc(c, &d.dlist, slots))) break;
+    if ((st = dalloc(c, &d.tlist, slots))) break;
+    if ((st = dalloc(c, &d.slist, slots))) break;
+    if ((st = dalloc(c, &d.map, slots))) break;
+    if (cudaMallocHost(&c->h_cg, 3 * sizeof(CGState)) != cudaSuccess) { st = WPIC_CUDA_ERROR; break; }
+    if (cudaMallocHost(&c->h_err, sizeof(int)) != cudaSuccess) { st = WPIC_CUDA_ERROR; break; }
+    for (int s = 0; s < SG_COUNT; ++s) {
+      cudaEventCreate(&c->ev0[s]);
+      cudaEventCreate(&c->ev1[s]);
+    }
+  } while (0);
+  if (st == WPIC_OK) st = cuda_status(cudaStreamSynchronize(c->stream));
+  if (st != WPIC_OK) {
+    wpic_finalize(c);
+    return st;
+  }
+  *out = c;
+  return WPIC_OK;
+}
+
+int wpic_finalize(wpic_ctx* c) {
+  if (!c) return WPIC_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->staging) cudaFree(c->staging);
+  if (c->h_cg) cudaFreeHost(c->h_cg);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  for (int s = 0; s < SG_COUNT; ++s) {
+    if (c->ev0[s]) cudaEventDestroy(c->ev0[s]);
+    if (c->ev1[s]) cudaEventDestroy(c->ev1[s]);
+  }
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return WPIC_OK;
+}
+
+int wpic_put_particles(wpic_ctx* c, int which, const double* up, const int* np2, const int* cumcnt) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!up || !np2 || (which == 0 && !cumcnt) || (which != 0 && which != 1)) return WPIC_BAD_ARGUMENT;
+  Dev2D& d = c->d;
+  const int nx = d.g.nx, ndim = c->prm.ndim, nph = c->prm.np;
+  for (int r = 0; r < d.nrowjob; ++r) {
+    if (np2[r] < 0 || np2[r] > d.cap || np2[r] > nph) return WPIC_CAPACITY;
+    if (which == 0) {
+      const int* cc = cumcnt + (size_t)r * (nx + 1);
+      if (cc[0] != 0 || cc[nx] != np2[r]) return WPIC_BAD_ARGUMENT;
+      for (int i = 0; i < nx; ++i)
+        if (cc[i + 1] < cc[i]) return WPIC_BAD_ARGUMENT;
+    }
+  }
+  CK(cudaMemcpyAsync(d.np2, np2, sizeof(int) * d.nrowjob, cudaMemcpyHostToDevice, c->stream));
+  if (which == 0)
+    CK(cudaMemcpyAsync(d.cc, cumcnt, sizeof(int) * (size_t)d.nrowjob * (nx + 1), cudaMemcpyHostToDevice,
+                       c->stream));
+  const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
+  size_t rows_per = ((size_t)1 << 30) / row_bytes;
+  if (rows_per < 1) rows_per = 1;
+  if (rows_per > (size_t)d.nrowjob) rows_per = d.nrowjob;
+  int st = ensure_staging(c, rows_per * row_bytes);
+  if (st) return st;
+  const Parts64& P = which == 0 ? d.A : d.B;
+  for (int r0 = 0; r0 < d.nrowjob; r0 += (int)rows_per) {
+    const int nr = (int)((size_t)(d.nrowjob - r0) < rows_per ? d.nrowjob - r0 : rows_per);
+    CK(cudaMemcpyAsync(c->staging, up + (size_t)r0 * ndim * nph, nr * row_bytes, cudaMemcpyHostToDevice,
+                       c->stream));
+    aos_to_soa2d(d, c->staging, ndim, nph, r0, nr, P, c->stream);
+  }
+  return finish(c);
+}
+
+int wpic_get_particles(wpic_ctx* c, int which, double* up, int* np2, int* cumcnt) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!up || (which != 0 && which != 1)) return WPIC_BAD_ARGUMENT;
+  Dev2D& d = c->d;
+  const int nx = d.g.nx, ndim = c->prm.ndim, nph = c->prm.np;
+  if (np2) CK(cudaMemcpyAsync(np2, d.np2, sizeof(int) * d.nrowjob, cudaMemcpyDeviceToHost, c->stream));
+  if (cumcnt && which == 0)
+    CK(cudaMemcpyAsync(cumcnt, d.cc, sizeof(int) * (size_t)d.nrowjob * (nx + 1), cudaMemcpyDeviceToHost,
+                       c->stream));
+  const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
+  size_t rows_per = ((size_t)1 << 30) / row_bytes;
+  if (rows_per < 1) rows_per = 1;
+  if (rows_per > (size_t)d.nrowjob) rows_per = d.nrowjob;
+  int st = ensure_staging(c, rows_per * row_bytes);
+  if (st) return st;
+  const Parts64& P = which == 0 ? d.A : d.B;
+  for (int r0 = 0; r0 < d.nrowjob; r0 += (int)rows_per) {
+    const int nr = (int)((size_t)(d.nrowjob - r0) < rows_per ? d.nrowjob - r0 : rows_per);
+    soa_to_aos2d(d, c->staging, ndim, nph, r0, nr, P, c->stream);
+    CK(cudaMemcpyAsync(up + (size_t)r0 * ndim * nph, c->staging, nr * row_bytes, cudaMemcpyDeviceToHost,
+                       c->stream));
+  }
+  return finish(c);
+}
+
+static int put_field(wpic_ctx* c, const double* ref, double* dst, int ncomp) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!ref) return WPIC_BAD_ARGUMENT;
+  const size_t n = (size_t)ncomp * c->d.g.fplane;
+  int st = ensure_staging(c, n * sizeof(double));
+  if (st) return st;
+  CK(cudaMemcpyAsync(c->staging, ref, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  field_ref_to_soa(c->staging, dst, ncomp, c->d.g.fplane, c->stream);
+  return finish(c);
+}
+
+static int get_field(wpic_ctx* c, double* ref, const double* src, int ncomp) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!ref) return WPIC_BAD_ARGUMENT;
+  const size_t n = (size_t)ncomp * c->d.g.fplane;
+  int st = ensure_staging(c, n * sizeof(double));
+  if (st) return st;
+  field_soa_to_ref(src, c->staging, ncomp, c->d.g.fplane, c->stream);
+  CK(cudaMemcpyAsync(ref, c->staging, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+int wpic_put_fields(wpic_ctx* c, const double* uf) { return c ? put_field(c, uf, c->d.uf, 6) : WPIC_NOT_INITIALISED; }
+int wpic_get_fields(wpic_ctx* c, double* uf) { return c ? get_field(c, uf, c->d.uf, 6) : WPIC_NOT_INITIALISED; }
+int wpic_put_df(wpic_ctx* c, const double* df) { return c ? put_field(c, df, c->d.df, 6) : WPIC_NOT_INITIALISED; }
+int wpic_get_df(wpic_ctx* c, double* df) { return c ? get_field(c, df, c->d.df, 6) : WPIC_NOT_INITIALISED; }
+int wpic_get_uj(wpic_ctx* c, double* uj) { return c ? get_field(c, uj, c->d.uj, 3) : WPIC_NOT_INITIALISED; }
+
+int wpic_particle_solv(wpic_ctx* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  do_push(c);
+  return finish(c);
+}
+
+int wpic_field_fdtd_i(wpic_ctx* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  int st = do_field(c);
+  int st2 = finish(c);
+  return st ? st : st2;
+}
+
+int wpic_ele_cur(wpic_ctx* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  do_ele_cur(c);
+  return finish(c);
+}
+
+int wpic_bc_particle_x(wpic_ctx* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  do_particle_x(c);
+  return finish(c);
+}
+
+int wpic_bc_particle_y(wpic_ctx* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  int st = ensure_C(c);
+  if (st) return st;
+  Dev2D& d = c->d;
+  stage_begin(c, SG_PBC);
+  migrate_scan2d(d, d.B, c->stream);
+  migrate_plan2d(d, c->stream);
+  gather2d(d, d.B, d.C, d.slist, d.np2new, c->stream);
+  CK(cudaMemcpyAsync(d.np2, d.np2new, sizeof(int) * d.nrowjob, cudaMemcpyDeviceToDevice, c->stream));
+  stage_end(c, SG_PBC, 3);
+  const Parts64 t = d.B;
+  d.B = d.C;
+  d.C = t;
+  return finish(c);
+}
+
+int wpic_sort_bucket(wpic_ctx* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  Dev2D& d = c->d;
+  stage_begin(c, SG_SORT);
+  sort_rank2d(d, d.B, nullptr, c->stream);
+  gather2d(d, d.B, d.A, d.map, d.np2, c->stream);
+  stage_end(c, SG_SORT, 2);
+  return finish(c);
+}
+
+int wpic_step(wpic_ctx* c, int nsteps) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  for (int it = 0; it < nsteps; ++it) {
+    int st = one_step(c);
+    int st2 = finish(c);
+    if (st) return st;
+    if (st2) return st2;
+  }
+  return WPIC_OK;
+}
+
+int wpic_energy(wpic_ctx* c, double* out) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!out) return WPIC_BAD_ARGUMENT;
+  FP(energy2d, c->d, c->stream);
+  double h[4];
+  CK(cudaMemcpyAsync(h, c->d.red_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  int st = finish(c);
+  if (st) return st;
+  const int nsp = c->prm.nsp;
+  for (int k = 0; k < nsp; ++k) out[k] = h[k];
+  out[nsp] = h[2] / (8 * c->d.ph.pi);
+  out[nsp + 1] = h[3] / (8 * c->d.ph.pi);
+  return WPIC_OK;
+}
+
+int wpic_cg_control(wpic_ctx* c, const int* fixed3, int ite_max) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  for (int l = 0; l < 3; ++l) c->cg_fixed[l] = fixed3 ? fixed3[l] : -1;
+  c->d.ite_max = ite_max > 0 ? ite_max : 100;
+  return WPIC_OK;
+}
+
+int wpic_cg_iters(wpic_ctx* c, int* out3) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!out3) return WPIC_BAD_ARGUMENT;
+  for (int l = 0; l < 3; ++l) out3[l] = c->cg_iters[l];
+  return WPIC_OK;
+}
+
+int wpic_load_weibel_2d(wpic_ctx* c, int ppc, uint64_t seed, double drift, int drift_axis, double u_thi,
+                        double u_the, const double* b0) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  Dev2D& d = c->d;
+  if (ppc < 1 || (long long)ppc * d.g.nx > d.cap || drift_axis < 0 || drift_axis > 2) return WPIC_BAD_ARGUMENT;
+  load_weibel2d_ppc(d, ppc, seed, drift, drift_axis, u_thi, u_the, c->stream);
+  const size_t fplane = d.g.fplane;
+  CK(cudaMemsetAsync(d.uf, 0, 6 * fplane * sizeof(double), c->stream));
+  CK(cudaMemsetAsync(d.df, 0, 6 * fplane * sizeof(double), c->stream));
+  CK(cudaMemsetAsync(d.uj, 0, 3 * fplane * sizeof(double), c->stream));
+  if (b0) {
+    std::vector<double> plane(fplane);
+    for (int k = 0; k < 3; ++k) {
+      if (b0[k] == 0.0) continue;
+      for (size_t i = 0; i < fplane; ++i) plane[i] = b0[k];
+      CK(cudaMemcpyAsync(d.uf + k * fplane, plane.data(), fplane * sizeof(double), cudaMemcpyHostToDevice,
+                         c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+    }
+  }
+  return finish(c);
+}
+
+int wpic_timing_enable(wpic_ctx* c, int enable) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  cudaStreamSynchronize(c->stream);
+  stage_collect(c);
+  c->timing = enable != 0;
+  for (int s = 0; s < SG_COUNT; ++s) {
+    c->stage_ms[s] = 0.0;
+    c->stage_launches[s] = 0;
+    c->pending[s] = false;
+  }
+  return WPIC_OK;
+}
+
+int wpic_timing_get(wpic_ctx* c, double* ms, long long* launches, int n) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  cudaStreamSynchronize(c->stream);
+  stage_collect(c);
+  for (int s = 0; s < n && s < SG_COUNT; ++s) {
+    if (ms) ms[s] = c->stage_ms[s];
+    if (launches) launches[s] = c->stage_launches[s];
+  }
+  return WPIC_OK;
+}
+
+const char* wpic_stage_name(int s) { return (s >= 0 && s < SG_COUNT) ? kStageNames[s] : "?"; }
+int wpic_num_stages(void) { return SG_COUNT; }
+
+int wpic_synchronize(wpic_ctx* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  return finish(c);
+}
+
+long long wpic_num_particles(wpic_ctx* c) {
+  if (!c) return -1;
+  std::vector<int> h(c->d.nrowjob);
+  if (cudaMemcpyAsync(h.data(), c->d.np2, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, c->stream) !=
+      cudaSuccess)
+    return -1;
+  cudaStreamSynchronize(c->stream);
+  long long n = 0;
+  for (int v : h) n += v;
+  return n;
+}
+
+const char* wpic_status_string(int s) {
+  switch (s) {
+    case WPIC_OK: return "ok";
+    case WPIC_CG_NOT_CONVERGED: return "CG did not converge within ite_max iterations";
+    case WPIC_CAPACITY: return "particle capacity of a row exceeded";
+    case WPIC_OUT_OF_RANGE: return "particle outside the domain";
+    case WPIC_MOVED_TOO_FAR: return "particle moved more than one cell in one step";
+    case WPIC_NONFINITE: return "non-finite value";
+    case WPIC_BAD_ARGUMENT: return "bad argument";
+    case WPIC_CUDA_ERROR: return "CUDA error";
+    case WPIC_NOT_INITIALISED: return "context not initialised";
+    default: return "unknown status";
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,629 @@
+// Precision-dependent 2D kernels of the FP64 path.  Included twice, inside
+// namespace wpic::exact (compiled with -fmad=false: every operation rounded
+// separately, in the reference's evaluation order, so the single-thread
+// Fortran results are reproduced bit for bit where no reduction intervenes) and
+// inside namespace wpic::fast (FMA contraction allowed; results within a few
+// ulp of the exact build).
+//
+// Requires: wpic_internal.h, common.cuh included before.
+
+// ---------------------------------------------------------------------------
+// particle__solv  (2d/common/particle.f90:48-179)
+// One CTA per (tile of PUSH_TW cells of a bucket row, species).  The E/B values
+// at cell centres, tmp(1:6, i-1:i+1, j-1:j+1) of the reference, are formed once
+// per tile in shared memory; every particle of the tile then gathers from there.
+// ---------------------------------------------------------------------------
+constexpr int PUSH_TW = 32;
+constexpr int PUSH_THREADS = 128;
+
+__global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
+  const Grid2D g = d.g;
+  const int c0 = blockIdx.x * PUSH_TW;
+  const int jj = blockIdx.y, isp = blockIdx.z;
+  if (c0 >= g.nx) return;
+  const int nc = min(PUSH_TW, g.nx - c0);
+  __shared__ double tmp[6][3][PUSH_TW + 2];
+  __shared__ int scc[PUSH_TW + 1];
+  const int row = isp * g.ny + jj;
+  for (int idx = threadIdx.x; idx < 3 * (nc + 2); idx += blockDim.x) {
+    const int rj = idx / (nc + 2), ci = idx - rj * (nc + 2);
+    const int fi = c0 + ci + 1, fj = jj + rj + 1;  // field index of cell (c0+ci-1, jj+rj-1)
+    const double* U = d.uf;
+    const size_t b0 = (size_t)fj * g.fp + fi;
+#define UF(c, di, dj) U[(size_t)(c) * g.fplane + b0 + (size_t)(dj) * g.fp + (di)]
+    tmp[0][rj][ci] = 0.5 * (+UF(0, 0, 0) + UF(0, 0, 1));
+    tmp[1][rj][ci] = 0.5 * (+UF(1, 0, 0) + UF(1, 1, 0));
+    tmp[2][rj][ci] = 0.25 * (+UF(2, 0, 0) + UF(2, 1, 0) + UF(2, 0, 1) + UF(2, 1, 1));
+    tmp[3][rj][ci] = 0.5 * (+UF(3, 0, 0) + UF(3, 1, 0));
+    tmp[4][rj][ci] = 0.5 * (+UF(4, 0, 0) + UF(4, 0, 1));
+    tmp[5][rj][ci] = UF(5, 0, 0);
+#undef UF
+  }
+  for (int idx = threadIdx.x; idx <= nc; idx += blockDim.x) scc[idx] = d.cc[(size_t)row * (g.nx + 1) + c0 + idx];
+  __syncthreads();
+
+  const double dxi = d.ph.p_d_delx, delt = d.ph.delt, c = d.ph.c;
+  const double fac1 = d.ph.q[isp] / d.ph.r[isp] * 0.5 * delt;
+  const double txxx = fac1 * fac1;
+  const double fac2 = d.ph.q[isp] * delt / d.ph.r[isp];
+  const int jabs = g.nygs + jj;
+  const size_t rbase = (size_t)row * d.cap;
+  const int s_end = scc[nc];
+  for (int s = scc[0] + threadIdx.x; s < s_end; s += blockDim.x) {
+    int lo = 0, hi = nc;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (scc[mid] <= s) lo = mid; else hi = mid;
+    }
+    const int iabs = g.nxgs + c0 + lo;
+    const size_t k = rbase + s;
+    const double x = d.A.x[k], y = d.A.y[k];
+    double dh = x * dxi - 0.5 - (double)iabs;
+    const double sx0 = 0.5 * (0.5 - dh) * (0.5 - dh);
+    const double sx1 = 0.75 - dh * dh;
+    const double sx2 = 0.5 * (0.5 + dh) * (0.5 + dh);
+    dh = y * dxi - 0.5 - (double)jabs;
+    const double sy0 = 0.5 * (0.5 - dh) * (0.5 - dh);
+    const double sy1 = 0.75 - dh * dh;
+    const double sy2 = 0.5 * (0.5 + dh) * (0.5 + dh);
+    double f[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      f[m] = +(+tmp[m][0][lo] * sx0 + tmp[m][0][lo + 1] * sx1 + tmp[m][0][lo + 2] * sx2) * sy0
+             + (+tmp[m][1][lo] * sx0 + tmp[m][1][lo + 1] * sx1 + tmp[m][1][lo + 2] * sx2) * sy1
+             + (+tmp[m][2][lo] * sx0 + tmp[m][2][lo + 1] * sx1 + tmp[m][2][lo + 2] * sx2) * sy2;
+    }
+    const double bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
+    double uvm1 = d.A.ux[k] + fac1 * epx;
+    double uvm2 = d.A.uy[k] + fac1 * epy;
+    double uvm3 = d.A.uz[k] + fac1 * epz;
+    double gam = sqrt(c * c + uvm1 * uvm1 + uvm2 * uvm2 + uvm3 * uvm3);
+    const double igam = 1. / gam;
+    const double fac1r = fac1 * igam;
+    const double fac2r = fac2 / (gam + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
+    const double uvm4 = uvm1 + fac1r * (+uvm2 * bpz - uvm3 * bpy);
+    const double uvm5 = uvm2 + fac1r * (+uvm3 * bpx - uvm1 * bpz);
+    const double uvm6 = uvm3 + fac1r * (+uvm1 * bpy - uvm2 * bpx);
+    uvm1 = uvm1 + fac2r * (+uvm5 * bpz - uvm6 * bpy);
+    uvm2 = uvm2 + fac2r * (+uvm6 * bpx - uvm4 * bpz);
+    uvm3 = uvm3 + fac2r * (+uvm4 * bpy - uvm5 * bpx);
+    const double g3 = uvm1 + fac1 * epx;
+    const double g4 = uvm2 + fac1 * epy;
+    const double g5 = uvm3 + fac1 * epz;
+    gam = 1.0 / sqrt(1.0 + (+g3 * g3 + g4 * g4 + g5 * g5) / (c * c));
+    d.B.ux[k] = g3;
+    d.B.uy[k] = g4;
+    d.B.uz[k] = g5;
+    d.B.x[k] = x + g3 * delt * gam;
+    d.B.y[k] = y + g4 * delt * gam;
+    d.B.id[k] = d.A.id[k];
+  }
+}
+
+void push2d(const Dev2D& d, cudaStream_t s) {
+  dim3 grid((d.g.nx + PUSH_TW - 1) / PUSH_TW, d.g.ny, d.ph.nsp);
+  k_push2d<<<grid, PUSH_THREADS, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// ele_cur  (2d/common/field.f90:189-316)
+// One thread per cell walks the cell's particles of both species in bucket
+// order and accumulates the cell's 5x5 Esirkepov tiles pjx/pjy/pjz exactly as
+// the reference does (shared memory, one column per thread); the tiles go to
+// cellJ and k_jgather2d adds them into uj in the reference's (j, i) cell order,
+// which is the single-thread OpenMP reduction order.
+// ---------------------------------------------------------------------------
+constexpr int DEP_THREADS = 64;
+
+__global__ void __launch_bounds__(DEP_THREADS) k_deposit2d(Dev2D d) {
+  extern __shared__ double acc[];  // [75][DEP_THREADS]: pjx(ip,jp) at (ip+2)+5*(jp+2), pjy at 25+, pjz at 50+
+  const Grid2D g = d.g;
+  const int cx = blockIdx.x * DEP_THREADS + threadIdx.x;
+  const int jj = blockIdx.y;
+  if (cx >= g.nx) return;
+  double* a = acc + threadIdx.x;
+#pragma unroll 5
+  for (int e = 0; e < 75; ++e) a[e * DEP_THREADS] = 0.0;
+  const double d_delx = d.ph.d_delx, d_delt = d.ph.d_delt, delx = d.ph.delx, c = d.ph.c;
+  const double fac = 1.0 / 3.0;
+  const int iabs = g.nxgs + cx, jabs = g.nygs + jj;
+  for (int isp = 0; isp < d.ph.nsp; ++isp) {
+    const int row = isp * g.ny + jj;
+    const int* ccr = d.cc + (size_t)row * (g.nx + 1);
+    const int s0i = ccr[cx], s1i = ccr[cx + 1];
+    const double qs = d.ph.q[isp];
+    const double qdd = qs * delx * d_delt;
+    const size_t rbase = (size_t)row * d.cap;
+    for (int s = s0i; s < s1i; ++s) {
+      const size_t k = rbase + s;
+      double s0x[5], s0y[5], dsx[5], dsy[5];
+      double dh = d.A.x[k] * d_delx - 0.5 - (double)iabs;
+      s0x[0] = 0.0;
+      s0x[1] = 0.5 * (0.5 - dh) * (0.5 - dh);
+      s0x[2] = 0.75 - dh * dh;
+      s0x[3] = 0.5 * (0.5 + dh) * (0.5 + dh);
+      s0x[4] = 0.0;
+      dh = d.A.y[k] * d_delx - 0.5 - (double)jabs;
+      s0y[0] = 0.0;
+      s0y[1] = 0.5 * (0.5 - dh) * (0.5 - dh);
+      s0y[2] = 0.75 - dh * dh;
+      s0y[3] = 0.5 * (0.5 + dh) * (0.5 + dh);
+      s0y[4] = 0.0;
+      const double xn = d.B.x[k], yn = d.B.y[k];
+#pragma unroll
+      for (int dim = 0; dim < 2; ++dim) {
+        const double pn = dim == 0 ? xn : yn;
+        const int i2 = (int)(pn * d_delx);
+        const double dh1 = pn * d_delx - 0.5 - (double)i2;
+        const int inc = i2 - (dim == 0 ? iabs : jabs);
+        if (inc < -1 || inc > 1) atomicOr(d.err, EB_MOVED_TOO_FAR);
+        const double s1_1 = 0.5 * (0.5 - dh1) * (0.5 - dh1);
+        const double s1_2 = 0.75 - dh1 * dh1;
+        const double s1_3 = 0.5 * (0.5 + dh1) * (0.5 + dh1);
+        const int ainc = inc < 0 ? -inc : inc;
+        const double smo_1 = (double)(-(inc - ainc)) * 0.5;
+        const double smo_2 = (double)(-ainc + 1);
+        const double smo_3 = (double)(inc + ainc) * 0.5;
+        double* ds = dim == 0 ? dsx : dsy;
+        const double* s0 = dim == 0 ? s0x : s0y;
+        ds[0] = s1_1 * smo_1 - s0[0];
+        ds[1] = s1_1 * smo_2 + s1_2 * smo_1 - s0[1];
+        ds[2] = s1_2 * smo_2 + s1_3 * smo_1 + s1_1 * smo_3 - s0[2];
+        ds[3] = s1_3 * smo_2 + s1_2 * smo_3 - s0[3];
+        ds[4] = s1_3 * smo_3 - s0[4];
+      }
+      const double g3 = d.B.ux[k], g4 = d.B.uy[k], g5 = d.B.uz[k];
+      const double gvz = g5 / sqrt(1. + (+g3 * g3 + g4 * g4 + g5 * g5) / (c * c));
+      // pjx: prefix along x, pjtmp(ip+1,jp) = pjtmp(ip,jp) - q*delx/dt*ds_x(ip)*(s0_y(jp)+ds_y(jp)/2)
+#pragma unroll
+      for (int jp = 0; jp < 5; ++jp) {
+        const double wy = s0y[jp] + 0.5 * dsy[jp];
+        double t = 0.0;
+#pragma unroll
+        for (int ip = 0; ip < 4; ++ip) {
+          t = t - qdd * dsx[ip] * wy;
+          double* e = a + ((ip + 1) + 5 * jp) * DEP_THREADS;
+          *e = *e + t;
+        }
+      }
+      // pjy: prefix along y
+#pragma unroll
+      for (int ip = 0; ip < 5; ++ip) {
+        const double wx = s0x[ip] + 0.5 * dsx[ip];
+        double t = 0.0;
+#pragma unroll
+        for (int jp = 0; jp < 4; ++jp) {
+          t = t - qdd * dsy[jp] * wx;
+          double* e = a + (25 + ip + 5 * (jp + 1)) * DEP_THREADS;
+          *e = *e + t;
+        }
+      }
+      // pjz: out-of-plane current with the 1/3 cross term
+      const double qg = qs * gvz;
+#pragma unroll
+      for (int jp = 0; jp < 5; ++jp) {
+#pragma unroll
+        for (int ip = 0; ip < 5; ++ip) {
+          double* e = a + (50 + ip + 5 * jp) * DEP_THREADS;
+          *e = *e + qg * (+s0x[ip] * s0y[jp] + 0.5 * dsx[ip] * s0y[jp] + 0.5 * s0x[ip] * dsy[jp]
+                          + fac * dsx[ip] * dsy[jp]);
+        }
+      }
+    }
+  }
+  const size_t cell = (size_t)jj * g.nx + cx;
+#pragma unroll 5
+  for (int e = 0; e < 75; ++e) d.cellJ[(size_t)e * g.ncell + cell] = a[e * DEP_THREADS];
+}
+
+// uj(node) = sum over the 25 neighbouring cells, in the reference's cell loop
+// order (j ascending, then i ascending), of that cell's tile entry.
+__global__ void k_jgather2d(Dev2D d) {
+  const Grid2D g = d.g;
+  const int ii = blockIdx.x * blockDim.x + threadIdx.x;  // field column 0..nx+3
+  const int jf = blockIdx.y;                              // field row 0..ny+3
+  if (ii >= g.nx + 4) return;
+  double sx = 0.0, sy = 0.0, sz = 0.0;
+  for (int jp = 2; jp >= -2; --jp) {
+    const int cy = jf - 2 - jp;
+    if (cy < 0 || cy >= g.ny) continue;
+    for (int ip = 2; ip >= -2; --ip) {
+      const int cx = ii - 2 - ip;
+      if (cx < 0 || cx >= g.nx) continue;
+      const size_t cell = (size_t)cy * g.nx + cx;
+      const int e = (ip + 2) + 5 * (jp + 2);
+      sx = sx + d.cellJ[(size_t)e * g.ncell + cell];
+      sy = sy + d.cellJ[(size_t)(25 + e) * g.ncell + cell];
+      sz = sz + d.cellJ[(size_t)(50 + e) * g.ncell + cell];
+    }
+  }
+  const size_t f = (size_t)jf * g.fp + ii;
+  d.uj[f] = sx;
+  d.uj[(size_t)g.fplane + f] = sy;
+  d.uj[2 * (size_t)g.fplane + f] = sz;
+}
+
+void deposit2d(const Dev2D& d, cudaStream_t s) {
+  dim3 grid((d.g.nx + DEP_THREADS - 1) / DEP_THREADS, d.g.ny);
+  const size_t shm = (size_t)75 * DEP_THREADS * sizeof(double);
+  k_deposit2d<<<grid, DEP_THREADS, shm, s>>>(d);
+  dim3 g2((d.g.nx + 4 + 127) / 128, d.g.ny + 4);
+  k_jgather2d<<<g2, 128, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// RHS gkl of the implicit B solve  (2d/common/field.f90:125-146)
+// ---------------------------------------------------------------------------
+__global__ void k_gkl2d(Dev2D d) {
+  const Grid2D g = d.g;
+  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
+  if (cx >= g.nx) return;
+  const size_t f = (size_t)(cy + 2) * g.fp + (cx + 2);
+  const size_t P = g.fplane;
+  const double* uf = d.uf;
+  const double* uj = d.uj;
+  const double f1 = d.ph.f1, f2 = d.ph.f2, f3 = d.ph.f3;
+  const size_t S = f - g.fp, W = f - 1, E = f + 1, N = f + g.fp;
+#define U(c, at) uf[(c) * P + (at)]
+#define J(c, at) uj[(c) * P + (at)]
+  const double g1 = +f2 * (+U(0, S) + U(0, W) - 4. * U(0, f) + U(0, E) + U(0, N) + f3 * (-J(2, S) + J(2, f)))
+                    - f1 * (-U(5, S) + U(5, f));
+  const double g2 = +f2 * (+U(1, S) + U(1, W) - 4. * U(1, f) + U(1, E) + U(1, N) - f3 * (-J(2, W) + J(2, f)))
+                    + f1 * (-U(5, W) + U(5, f));
+  const double g3 = +f2 * (+U(2, S) + U(2, W) - 4. * U(2, f) + U(2, E) + U(2, N)
+                           + f3 * (-J(1, W) + J(1, f) + J(0, S) - J(0, f)))
+                    - f1 * (-U(4, W) + U(4, f) + U(3, S) - U(3, f));
+#undef U
+#undef J
+  const size_t c = (size_t)cy * g.nx + cx;
+  d.gkl[c] = g1;
+  d.gkl[(size_t)g.ncell + c] = g2;
+  d.gkl[2 * (size_t)g.ncell + c] = g3;
+}
+
+void gkl2d(const Dev2D& d, cudaStream_t s) {
+  dim3 grid((d.g.nx + 127) / 128, d.g.ny);
+  k_gkl2d<<<grid, 128, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// cgm  (2d/common/field.f90:319-461), the three components solved side by side
+// (blockIdx.y = component).  Dot products are reduced deterministically: fixed
+// per-block tree, then a fixed-order sum of the block partials.  The stopping
+// rule is the reference's, quirks included: the first loop test compares
+// ||b||^2 with eps, and ||r|| is taken before the update, so one extra
+// iteration runs after convergence.
+// ---------------------------------------------------------------------------
+constexpr int CG_THREADS = 256;
+
+// phi(cx, cy) of component l with the boundary_*__phi ghost rules applied by
+// index arithmetic (periodic y; periodic or conducting-wall x).
+__device__ __forceinline__ double phi_at(const double* v, const Grid2D& g, int bc, int l, int cx, int cy) {
+  if (cy < 0) cy += g.ny; else if (cy >= g.ny) cy -= g.ny;
+  double sgn = 1.0;
+  if (cx < 0) {
+    if (bc == BC_PERIODIC) cx += g.nx;
+    else if (l == 0) { cx = 0; sgn = -1.0; }
+    else cx = 1;
+  } else if (cx >= g.nx) {
+    if (bc == BC_PERIODIC) cx -= g.nx;
+    else if (l == 0) { cx = g.nx - 3; sgn = -1.0; }
+    else cx = g.nx - 2;
+  }
+  const double val = v[(size_t)cy * g.nx + cx];
+  return sgn < 0.0 ? -val : val;
+}
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int w = CG_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// phase 0: phi = db(l), b = f5*gkl(l), r = b + N(phi) - f4 phi, p = r; partials of b.b and r.r
+__global__ void __launch_bounds__(CG_THREADS) k_cg_init(Dev2D d) {
+  __shared__ double sh[CG_THREADS];
+  const Grid2D g = d.g;
+  const int l = blockIdx.y;
+  const size_t off = (size_t)l * g.ncell;
+  const double f4 = d.ph.f4, f5 = d.ph.f5;
+  double sb = 0.0, sr = 0.0;
+  for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS) {
+    const int cy = c / g.nx, cx = c - cy * g.nx;
+    // db interior viewed as a [ny][nx] array with pitch fp
+    const double* db = d.df + (size_t)l * g.fplane + 2 * (size_t)g.fp + 2;
+    auto ph = [&](int x, int y) {
+      if (y < 0) y += g.ny; else if (y >= g.ny) y -= g.ny;
+      double sgn = 1.0;
+      if (x < 0) {
+        if (d.ph.bc == BC_PERIODIC) x += g.nx; else if (l == 0) { x = 0; sgn = -1.0; } else x = 1;
+      } else if (x >= g.nx) {
+        if (d.ph.bc == BC_PERIODIC) x -= g.nx; else if (l == 0) { x = g.nx - 3; sgn = -1.0; } else x = g.nx - 2;
+      }
+      const double v = db[(size_t)y * g.fp + x];
+      return sgn < 0.0 ? -v : v;
+    };
+    const double pc = ph(cx, cy);
+    const double b = f5 * d.gkl[off + c];
+    const double r = b + ph(cx, cy - 1) + ph(cx - 1, cy) - f4 * pc + ph(cx + 1, cy) + ph(cx, cy + 1);
+    d.phi[off + c] = pc;
+    d.b[off + c] = b;
+    d.r[off + c] = r;
+    d.p[off + c] = r;
+    sb = sb + b * b;
+    sr = sr + r * r;
+  }
+  sb = block_sum(sb, sh);
+  sr = block_sum(sr, sh);
+  if (threadIdx.x == 0) {
+    d.partials[((size_t)l * d.nred + blockIdx.x) * 2 + 0] = sb;
+    d.partials[((size_t)l * d.nred + blockIdx.x) * 2 + 1] = sr;
+  }
+}
+
+__device__ __forceinline__ void final_sums(const Dev2D& d, int l, double* sh, double* out0, double* out1) {
+  double a = 0.0, b = 0.0;
+  for (int k = threadIdx.x; k < d.nred; k += CG_THREADS) {
+    a = a + d.partials[((size_t)l * d.nred + k) * 2 + 0];
+    b = b + d.partials[((size_t)l * d.nred + k) * 2 + 1];
+  }
+  a = block_sum(a, sh);
+  b = block_sum(b, sh);
+  *out0 = a;
+  *out1 = b;
+}
+
+__global__ void __launch_bounds__(CG_THREADS) k_cg_init_fin(Dev2D d) {
+  __shared__ double sh[CG_THREADS];
+  const int l = blockIdx.x;
+  double sb, sr;
+  final_sums(d, l, sh, &sb, &sr);
+  if (threadIdx.x == 0) {
+    CGState& st = d.cg[l];
+    st.sum_g = sb;
+    st.eps = sqrt(sb) * 1e-6;
+    st.sumr_g = sr;
+    st.ite = 0;
+    if (st.fixed >= 0) st.active = st.fixed > 0;
+    else st.active = (sqrt(sr) > st.eps) && (st.sum_g > st.eps);
+  }
+}
+
+// ap = (f4 - N) p ; partials of r.r and p.ap
+__global__ void __launch_bounds__(CG_THREADS) k_cg_ap(Dev2D d) {
+  __shared__ double sh[CG_THREADS];
+  const Grid2D g = d.g;
+  const int l = blockIdx.y;
+  if (!d.cg[l].active) return;
+  const size_t off = (size_t)l * g.ncell;
+  const double f4 = d.ph.f4;
+  const double* p = d.p + off;
+  const int bc = d.ph.bc;
+  double sr = 0.0, s2 = 0.0;
+  for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS) {
+    const int cy = c / g.nx, cx = c - cy * g.nx;
+    const double pc = p[c];
+    const double ap = -phi_at(p, g, bc, l, cx, cy - 1) - phi_at(p, g, bc, l, cx - 1, cy) + f4 * pc
+                      - phi_at(p, g, bc, l, cx + 1, cy) - phi_at(p, g, bc, l, cx, cy + 1);
+    d.ap[off + c] = ap;
+    const double r = d.r[off + c];
+    sr = sr + r * r;
+    s2 = s2 + pc * ap;
+  }
+  sr = block_sum(sr, sh);
+  s2 = block_sum(s2, sh);
+  if (threadIdx.x == 0) {
+    d.partials[((size_t)l * d.nred + blockIdx.x) * 2 + 0] = sr;
+    d.partials[((size_t)l * d.nred + blockIdx.x) * 2 + 1] = s2;
+  }
+}
+
+__global__ void __launch_bounds__(CG_THREADS) k_cg_ap_fin(Dev2D d) {
+  __shared__ double sh[CG_THREADS];
+  const int l = blockIdx.x;
+  if (!d.cg[l].active) return;
+  double sr, s2;
+  final_sums(d, l, sh, &sr, &s2);
+  if (threadIdx.x == 0) {
+    CGState& st = d.cg[l];
+    st.sumr_g = sr;
+    st.sum2_g = s2;
+    st.av = sr / s2;
+  }
+}
+
+// phi += av p ; r -= av ap ; partial of r.r
+__global__ void __launch_bounds__(CG_THREADS) k_cg_update(Dev2D d) {
+  __shared__ double sh[CG_THREADS];
+  const Grid2D g = d.g;
+  const int l = blockIdx.y;
+  if (!d.cg[l].active) return;
+  const size_t off = (size_t)l * g.ncell;
+  const double av = d.cg[l].av;
+  double s1 = 0.0;
+  for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS) {
+    d.phi[off + c] = d.phi[off + c] + av * d.p[off + c];
+    const double r = d.r[off + c] - av * d.ap[off + c];
+    d.r[off + c] = r;
+    s1 = s1 + r * r;
+  }
+  s1 = block_sum(s1, sh);
+  if (threadIdx.x == 0) {
+    d.partials[((size_t)l * d.nred + blockIdx.x) * 2 + 0] = s1;
+    d.partials[((size_t)l * d.nred + blockIdx.x) * 2 + 1] = 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(CG_THREADS) k_cg_update_fin(Dev2D d) {
+  __shared__ double sh[CG_THREADS];
+  const int l = blockIdx.x;
+  if (!d.cg[l].active) return;
+  double s1, dummy;
+  final_sums(d, l, sh, &s1, &dummy);
+  if (threadIdx.x == 0) {
+    CGState& st = d.cg[l];
+    st.sum_g = sqrt(st.sumr_g);
+    st.ite = st.ite + 1;
+    st.sum1_g = s1;
+    st.bv = s1 / st.sumr_g;
+    bool cont = st.fixed >= 0 ? (st.ite < st.fixed) : (st.sum_g > st.eps);
+    if (st.fixed < 0 && st.ite >= d.ite_max) {  // reference: write + stop (field.f90:427-430)
+      atomicOr(d.err, EB_CG);
+      cont = false;
+    }
+    // the active flag is cleared only after k_cg_p has consumed bv for a continuing component
+    st.active = cont ? 1 : 2;
+  }
+}
+
+// p = r + bv p, for components that continue; finishing components drop to inactive
+__global__ void __launch_bounds__(CG_THREADS) k_cg_p(Dev2D d) {
+  const Grid2D g = d.g;
+  const int l = blockIdx.y;
+  const int act = d.cg[l].active;
+  if (act != 1) return;
+  const size_t off = (size_t)l * g.ncell;
+  const double bv = d.cg[l].bv;
+  for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS)
+    d.p[off + c] = d.r[off + c] + bv * d.p[off + c];
+}
+
+__global__ void k_cg_settle(Dev2D d) {
+  if (threadIdx.x < 3 && d.cg[threadIdx.x].active == 2) d.cg[threadIdx.x].active = 0;
+}
+
+void cg_init2d(const Dev2D& d, cudaStream_t s) {
+  k_cg_init<<<dim3(d.nred, 3), CG_THREADS, 0, s>>>(d);
+  k_cg_init_fin<<<3, CG_THREADS, 0, s>>>(d);
+}
+void cg_iter_ap2d(const Dev2D& d, cudaStream_t s) {
+  k_cg_ap<<<dim3(d.nred, 3), CG_THREADS, 0, s>>>(d);
+  k_cg_ap_fin<<<3, CG_THREADS, 0, s>>>(d);
+}
+void cg_iter_update2d(const Dev2D& d, cudaStream_t s) {
+  k_cg_update<<<dim3(d.nred, 3), CG_THREADS, 0, s>>>(d);
+  k_cg_update_fin<<<3, CG_THREADS, 0, s>>>(d);
+}
+void cg_iter_p2d(const Dev2D& d, cudaStream_t s) {
+  k_cg_p<<<dim3(d.nred, 3), CG_THREADS, 0, s>>>(d);
+  k_cg_settle<<<1, 32, 0, s>>>(d);
+}
+
+// db(l, interior) = phi  (field.f90:455-457)
+__global__ void k_cg_store(Dev2D d) {
+  const Grid2D g = d.g;
+  const int l = blockIdx.y;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < g.ncell; c += gridDim.x * blockDim.x) {
+    const int cy = c / g.nx, cx = c - cy * g.nx;
+    d.df[(size_t)l * g.fplane + (size_t)(cy + 2) * g.fp + cx + 2] = d.phi[(size_t)l * g.ncell + c];
+  }
+}
+void cg_store2d(const Dev2D& d, cudaStream_t s) { k_cg_store<<<dim3(d.nred, 3), CG_THREADS, 0, s>>>(d); }
+
+// ---------------------------------------------------------------------------
+// E increment  (2d/common/field.f90:153-171)
+// ---------------------------------------------------------------------------
+__global__ void k_efield2d(Dev2D d) {
+  const Grid2D g = d.g;
+  const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
+  if (cx >= g.nx) return;
+  const size_t f = (size_t)(cy + 2) * g.fp + (cx + 2);
+  const size_t P = g.fplane;
+  const size_t E = f + 1, N = f + g.fp;
+  const double f1 = d.ph.f1, gfac = d.ph.gfac, pi = d.ph.pi, delt = d.ph.delt;
+  const double* uf = d.uf;
+  const double* df = d.df;
+  const double* uj = d.uj;
+#define U(c, at) uf[(c) * P + (at)]
+#define D(c, at) df[(c) * P + (at)]
+#define J(c, at) uj[(c) * P + (at)]
+  const double d4 = +f1 * (+gfac * (-D(2, f) + D(2, N)) + (-U(2, f) + U(2, N))) - 4. * pi * delt * J(0, f);
+  const double d5 = -f1 * (+gfac * (-D(2, f) + D(2, E)) + (-U(2, f) + U(2, E))) - 4. * pi * delt * J(1, f);
+  const double d6 = +f1 * (+gfac * (-D(1, f) + D(1, E) + D(0, f) - D(0, N)) + (-U(1, f) + U(1, E) + U(0, f) - U(0, N)))
+                    - 4. * pi * delt * J(2, f);
+#undef U
+#undef D
+#undef J
+  d.df[3 * P + f] = d4;
+  d.df[4 * P + f] = d5;
+  d.df[5 * P + f] = d6;
+}
+
+void efield2d(const Dev2D& d, cudaStream_t s) {
+  dim3 grid((d.g.nx + 127) / 128, d.g.ny);
+  k_efield2d<<<grid, 128, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// energy_history sums (2d/proj/weibel/app.f90:502-534), deterministic reductions.
+// red_out = [vene(1), vene(2), sum E^2, sum B^2]
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(CG_THREADS) k_energy_parts(Dev2D d) {
+  __shared__ double sh[CG_THREADS];
+  const Grid2D g = d.g;
+  const int isp = blockIdx.y;
+  const double c = d.ph.c, rr = d.ph.r[isp];
+  double v = 0.0;
+  for (int jj = 0; jj < g.ny; ++jj) {
+    const int row = isp * g.ny + jj;
+    const int n = d.np2[row];
+    const size_t rb = (size_t)row * d.cap;
+    for (int s = blockIdx.x * CG_THREADS + threadIdx.x; s < n; s += gridDim.x * CG_THREADS) {
+      const double a = d.A.ux[rb + s], b = d.A.uy[rb + s], e = d.A.uz[rb + s];
+      const double u2 = a * a + b * b + e * e;
+      const double gam = sqrt(1 + u2 / (c * c));
+      v = v + rr * (gam - 1);
+    }
+  }
+  v = block_sum(v, sh);
+  if (threadIdx.x == 0) d.partials[((size_t)isp * d.nred + blockIdx.x) * 2] = v;
+}
+
+__global__ void __launch_bounds__(CG_THREADS) k_energy_fields(Dev2D d) {
+  __shared__ double sh[CG_THREADS];
+  const Grid2D g = d.g;
+  double be = 0.0, ee = 0.0;
+  for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS) {
+    const int cy = c / g.nx, cx = c - cy * g.nx;
+    const size_t f = (size_t)(cy + 2) * g.fp + cx + 2;
+    const size_t P = g.fplane;
+    const double b1 = d.uf[f], b2 = d.uf[P + f], b3 = d.uf[2 * P + f];
+    const double e1 = d.uf[3 * P + f], e2 = d.uf[4 * P + f], e3 = d.uf[5 * P + f];
+    be = be + b1 * b1 + b2 * b2 + b3 * b3;
+    ee = ee + e1 * e1 + e2 * e2 + e3 * e3;
+  }
+  be = block_sum(be, sh);
+  ee = block_sum(ee, sh);
+  if (threadIdx.x == 0) {
+    d.partials[((size_t)2 * d.nred + blockIdx.x) * 2 + 0] = ee;
+    d.partials[((size_t)2 * d.nred + blockIdx.x) * 2 + 1] = be;
+  }
+}
+
+__global__ void __launch_bounds__(CG_THREADS) k_energy_fin(Dev2D d) {
+  __shared__ double sh[CG_THREADS];
+  double a, b;
+  final_sums(d, 0, sh, &a, &b);
+  if (threadIdx.x == 0) d.red_out[0] = a;
+  final_sums(d, 1, sh, &a, &b);
+  if (threadIdx.x == 0) d.red_out[1] = a;
+  final_sums(d, 2, sh, &a, &b);
+  if (threadIdx.x == 0) {
+    d.red_out[2] = a;
+    d.red_out[3] = b;
+  }
+}
+
+void energy2d(const Dev2D& d, cudaStream_t s) {
+  // partial slots [l][k][2]: l = 0,1 species kinetic (slot 0); l = 2 fields
+  cudaMemsetAsync(d.partials, 0, sizeof(double) * 2 * 3 * (size_t)d.nred, s);
+  k_energy_parts<<<dim3(d.nred, d.ph.nsp), CG_THREADS, 0, s>>>(d);
+  k_energy_fields<<<d.nred, CG_THREADS, 0, s>>>(d);
+  k_energy_fin<<<1, CG_THREADS, 0, s>>>(d);
+}

@@ -1,0 +1,532 @@
+// Precision-independent 2D kernels: ghost fills and current folds (exact adds
+// and copies), particle boundaries (round-toward-minus-infinity arithmetic as
+// in the reference), particle migration between bucket rows, the bucket sort,
+// gathers, layout conversions and the device-side synthetic loader.
+#include "common.cuh"
+
+namespace wpic {
+
+// ---------------------------------------------------------------------------
+// boundary_periodic__curre (2d/common/boundary_periodic.f90:357-508) with one
+// rank: fold rows nys-2,nys-1 into nye-1,nye and nye+1,nye+2 into nys,nys+1,
+// refresh the ghost rows, then (periodic x only) fold and refresh the ghost
+// columns.  boundary_reconnection__curre has no x part
+// (2d/proj/reconnection/boundary_reconnection.f90:364-502).
+// Field rows: nys-2 -> 0, nys -> 2, nye -> ny+1, nye+2 -> ny+3 (same for x).
+// ---------------------------------------------------------------------------
+__global__ void k_curre_y(Dev2D d) {
+  const Grid2D g = d.g;
+  const int ii = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ii >= g.nx + 4) return;
+  const int ny = g.ny;
+  for (int k = 0; k < 3; ++k) {
+    double* u = d.uj + (size_t)k * g.fplane + ii;
+    const size_t fp = g.fp;
+    u[ny * fp] = u[ny * fp] + u[0];
+    u[(ny + 1) * fp] = u[(ny + 1) * fp] + u[fp];
+    u[2 * fp] = u[2 * fp] + u[(ny + 2) * fp];
+    u[3 * fp] = u[3 * fp] + u[(ny + 3) * fp];
+    u[(ny + 2) * fp] = u[2 * fp];
+    u[(ny + 3) * fp] = u[3 * fp];
+    u[0] = u[ny * fp];
+    u[fp] = u[(ny + 1) * fp];
+  }
+}
+
+__global__ void k_curre_x(Dev2D d) {
+  const Grid2D g = d.g;
+  const int jf = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jf >= g.ny + 4) return;
+  const int nx = g.nx;
+  for (int k = 0; k < 3; ++k) {
+    double* u = d.uj + (size_t)k * g.fplane + (size_t)jf * g.fp;
+    u[nx] = u[nx] + u[0];
+    u[nx + 1] = u[nx + 1] + u[1];
+    u[2] = u[2] + u[nx + 2];
+    u[3] = u[3] + u[nx + 3];
+    u[0] = u[nx];
+    u[1] = u[nx + 1];
+    u[nx + 2] = u[2];
+    u[nx + 3] = u[3];
+  }
+}
+
+void curre_fold2d(const Dev2D& d, cudaStream_t s) {
+  k_curre_y<<<(d.g.nx + 4 + 127) / 128, 128, 0, s>>>(d);
+  if (d.ph.bc == BC_PERIODIC) k_curre_x<<<(d.g.ny + 4 + 127) / 128, 128, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// boundary_*__dfield (2d/common/boundary_periodic.f90:251-354;
+// 2d/proj/reconnection/boundary_reconnection.f90:254-361): two-deep ghosts of df.
+// ---------------------------------------------------------------------------
+__global__ void k_dfield_y(Dev2D d) {
+  const Grid2D g = d.g;
+  const int ii = 2 + blockIdx.x * blockDim.x + threadIdx.x;  // interior columns nxs..nxe
+  if (ii >= g.nx + 2) return;
+  const int ny = g.ny;
+  const size_t fp = g.fp;
+  for (int k = 0; k < 6; ++k) {
+    double* u = d.df + (size_t)k * g.fplane + ii;
+    u[(ny + 2) * fp] = u[2 * fp];
+    u[(ny + 3) * fp] = u[3 * fp];
+    u[0] = u[ny * fp];
+    u[fp] = u[(ny + 1) * fp];
+  }
+}
+
+__global__ void k_dfield_x(Dev2D d) {
+  const Grid2D g = d.g;
+  const int jf = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jf >= g.ny + 4) return;
+  const int nx = g.nx;
+  double* u[6];
+  for (int k = 0; k < 6; ++k) u[k] = d.df + (size_t)k * g.fplane + (size_t)jf * g.fp;
+  if (d.ph.bc == BC_PERIODIC) {
+    for (int k = 0; k < 6; ++k) u[k][0] = u[k][nx];
+    for (int k = 0; k < 6; ++k) u[k][1] = u[k][nx + 1];
+    for (int k = 0; k < 6; ++k) u[k][nx + 2] = u[k][2];
+    for (int k = 0; k < 6; ++k) u[k][nx + 3] = u[k][3];
+  } else {
+    // nxs-1 -> 1, nxs -> 2, nxs+1 -> 3, nxe-1 -> nx, nxe -> nx+1, nxe+1 -> nx+2
+    u[0][1] = -u[0][2];
+    for (int k = 1; k <= 3; ++k) u[k][1] = u[k][3];
+    for (int k = 4; k <= 5; ++k) u[k][1] = -u[k][2];
+    u[0][nx + 1] = -u[0][nx];
+    for (int k = 1; k <= 3; ++k) u[k][nx + 2] = u[k][nx];
+    for (int k = 4; k <= 5; ++k) u[k][nx + 1] = -u[k][nx];
+  }
+}
+
+void dfield_ghost2d(const Dev2D& d, cudaStream_t s) {
+  k_dfield_y<<<(d.g.nx + 127) / 128, 128, 0, s>>>(d);
+  k_dfield_x<<<(d.g.ny + 4 + 127) / 128, 128, 0, s>>>(d);
+}
+
+// uf = uf + df over the whole ghosted extent (2d/common/field.f90:175-184)
+__global__ void k_uf_add(Dev2D d) {
+  const size_t n = (size_t)6 * d.g.fplane;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    d.uf[k] = d.uf[k] + d.df[k];
+}
+void uf_add2d(const Dev2D& d, cudaStream_t s) { k_uf_add<<<4 * 152, 256, 0, s>>>(d); }
+
+// ---------------------------------------------------------------------------
+// particle boundaries in x
+//  periodic:     boundary_periodic__particle_x (2d/common/boundary_periodic.f90:61-96),
+//                evaluated with round-toward-minus-infinity as the reference sets it (line 74)
+//  reconnection: boundary_reconnection__particle_x (boundary_reconnection.f90:61-99),
+//                reflection at x walls, all three momentum components reversed
+// ---------------------------------------------------------------------------
+__global__ void k_particle_x(Dev2D d, Parts64 P) {
+  const int row = blockIdx.y;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.np2[row]) return;
+  const size_t k = (size_t)row * d.cap + s;
+  const Grid2D g = d.g;
+  const double delx = d.ph.delx;
+  double x = P.x[k];
+  const int nxge = g.nxgs + g.nx - 1;
+  if (d.ph.bc == BC_PERIODIC) {
+    const int ipos = (int)__ddiv_rd(x, delx);
+    const double L = __dmul_rd((double)g.nx, delx);
+    if (ipos < g.nxgs) x = __dadd_rd(x, L);
+    else if (ipos >= nxge + 1) x = __dsub_rd(x, L);
+    P.x[k] = x;
+  } else {
+    const int nxs = g.nxgs, nxe = nxge;
+    const int ipos = (int)(x / delx);
+    bool flip = false;
+    if (ipos < nxs + 1) {
+      x = (double)(2.0f * (float)(nxs + 1)) * delx - x;
+      flip = true;
+    } else if (ipos >= nxe - 1) {
+      x = (double)(2.0f * (float)(nxe - 1)) * delx - x;
+      flip = true;
+    }
+    if (flip) {
+      P.x[k] = x;
+      P.ux[k] = -P.ux[k];
+      P.uy[k] = -P.uy[k];
+      P.uz[k] = -P.uz[k];
+    }
+  }
+}
+
+void particle_x2d(const Dev2D& d, const Parts64& P, cudaStream_t s) {
+  dim3 grid((d.cap + 255) / 256, d.nrowjob);
+  k_particle_x<<<grid, 256, 0, s>>>(d, P);
+}
+
+// ---------------------------------------------------------------------------
+// boundary_periodic__particle_y (2d/common/boundary_periodic.f90:99-248),
+// first phase: classify every particle of a bucket row as staying, moving up
+// (+y) or down (-y); wrap y with round-toward-minus-infinity as the reference
+// does (line 124); record the up- and down-movers in slot order.  One CTA per
+// (species, row).
+// ---------------------------------------------------------------------------
+constexpr int MIG_THREADS = 256;
+
+__global__ void __launch_bounds__(MIG_THREADS) k_migrate_scan(Dev2D d, Parts64 P) {
+  const Grid2D g = d.g;
+  const int row = blockIdx.x;
+  const int jj = row % g.ny;
+  const int j = g.nygs + jj;
+  const int nyge = g.nygs + g.ny - 1;
+  const int n = d.np2[row];
+  const size_t rb = (size_t)row * d.cap;
+  const double delx = d.ph.delx;
+  const double L = __dmul_rd((double)g.ny, delx);
+  __shared__ int wu[MIG_THREADS / 32], wd[MIG_THREADS / 32];
+  __shared__ int base_u, base_d;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) base_u = base_d = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < n; c0 += MIG_THREADS) {
+    const int s = c0 + threadIdx.x;
+    int dir = 0;
+    if (s < n) {
+      double y = P.y[rb + s];
+      const int jpos = (int)__ddiv_rd(y, delx);
+      if (jpos != j) {
+        if (jpos == j + 1) dir = 1;
+        else if (jpos == j - 1) dir = 2;
+        else atomicOr(d.err, EB_MOVED_TOO_FAR);
+        if (dir != 0) {
+          if (jpos <= g.nygs - 1) y = __dadd_rd(y, L);
+          else if (jpos >= nyge + 1) y = __dsub_rd(y, L);
+          P.y[rb + s] = y;
+        }
+      }
+      d.mig[rb + s] = (int8_t)dir;
+    }
+    const unsigned bu = __ballot_sync(0xffffffffu, dir == 1);
+    const unsigned bd = __ballot_sync(0xffffffffu, dir == 2);
+    if (lane == 0) {
+      wu[warp] = __popc(bu);
+      wd[warp] = __popc(bd);
+    }
+    __syncthreads();
+    int ou = base_u, od = base_d;
+    for (int w = 0; w < warp; ++w) {
+      ou += wu[w];
+      od += wd[w];
+    }
+    const unsigned lt = lanemask_lt();
+    if (dir == 1) d.ulist[rb + ou + __popc(bu & lt)] = s;
+    if (dir == 2) d.dlist[rb + od + __popc(bd & lt)] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 0; w < MIG_THREADS / 32; ++w) {
+        base_u += wu[w];
+        base_d += wd[w];
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    d.nup[row] = base_u;
+    d.ndown[row] = base_d;
+  }
+}
+
+void migrate_scan2d(const Dev2D& d, const Parts64& P, cudaStream_t s) {
+  k_migrate_scan<<<d.nrowjob, MIG_THREADS, 0, s>>>(d, P);
+}
+
+// ---------------------------------------------------------------------------
+// Second phase of particle_y: the post-migration slot order of every row, in
+// closed form.  The reference (boundary_periodic.f90:173-236, one rank, one
+// thread) builds for each row an arrival buffer -- movers from the neighbouring
+// rows in source order, then the ones wrapped through the periodic ghost row --
+// and fills the row's holes in ascending slot order: first from the buffer;
+// once the buffer is empty, from the tail of the row, taking the non-hole
+// particles from the end downwards and dropping holes that the shrinking tail
+// passes; leftover arrivals are appended.  Equivalently, with h holes, b
+// arrivals and n particles:
+//   b >= h : hole m <- arrival m ; slot n+k <- arrival h+k
+//   b <  h : hole m (m < b) <- arrival m ; holes m >= b below n' = n-(h-b) <- the
+//            non-hole slots of [n', n) in descending order ; the row ends at n'.
+// One warp per (species, row) writes slist[t] = source slot of post-migration slot t.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(32) k_migrate_plan(Dev2D d) {
+  const Grid2D g = d.g;
+  const int row = blockIdx.x;
+  const int isp = row / g.ny, jj = row - isp * g.ny;
+  const int rowS = isp * g.ny;
+  const int lane = threadIdx.x;
+  const size_t cap = d.cap;
+  const int n = d.np2[row];
+  const int h = d.nup[row] + d.ndown[row];
+  int r1, r2, c1, c2;
+  const int *l1, *l2;
+  if (g.ny == 1) {
+    r1 = row; l1 = d.dlist + r1 * cap; c1 = d.ndown[r1];
+    r2 = row; l2 = d.ulist + r2 * cap; c2 = d.nup[r2];
+  } else if (jj == 0) {
+    r1 = row + 1; l1 = d.dlist + r1 * cap; c1 = d.ndown[r1];
+    r2 = rowS + g.ny - 1; l2 = d.ulist + r2 * cap; c2 = d.nup[r2];
+  } else if (jj == g.ny - 1) {
+    r1 = row - 1; l1 = d.ulist + r1 * cap; c1 = d.nup[r1];
+    r2 = rowS; l2 = d.dlist + r2 * cap; c2 = d.ndown[r2];
+  } else {
+    r1 = row - 1; l1 = d.ulist + r1 * cap; c1 = d.nup[r1];
+    r2 = row + 1; l2 = d.dlist + r2 * cap; c2 = d.ndown[r2];
+  }
+  const int b = c1 + c2;
+  int nn = n - h + b;
+  if (nn > (int)cap) {
+    if (lane == 0) atomicOr(d.err, EB_CAPACITY);
+    nn = (int)cap;
+  }
+  if (lane == 0) d.np2new[row] = nn;
+  const size_t rb = (size_t)row * cap;
+  const unsigned lt = lanemask_lt();
+  if (b < h) {
+    int k = 0;
+    for (int t0 = n - 1; t0 >= nn; t0 -= 32) {
+      const int t = t0 - lane;
+      const bool st = t >= nn && d.mig[rb + t] == 0;
+      const unsigned bal = __ballot_sync(0xffffffffu, st);
+      if (st) d.tlist[rb + k + __popc(bal & lt)] = t;
+      k += __popc(bal);
+    }
+  }
+  __syncwarp();
+  int m0 = 0;
+  for (int t0 = 0; t0 < nn; t0 += 32) {
+    const int t = t0 + lane;
+    const bool act = t < nn;
+    const bool hole = act && t < n && d.mig[rb + t] != 0;
+    const unsigned hb = __ballot_sync(0xffffffffu, hole);
+    const int m = m0 + __popc(hb & lt);
+    if (act) {
+      int src;
+      int a = -1;  // arrival index
+      if (t >= n) a = h + (t - n);
+      else if (!hole) src = (int)(rb + t);
+      else if (m < b) a = m;
+      else src = (int)(rb + d.tlist[rb + (m - b)]);
+      if (a >= 0) src = a < c1 ? (int)((size_t)r1 * cap + l1[a]) : (int)((size_t)r2 * cap + l2[a - c1]);
+      d.slist[rb + t] = src;
+    }
+    m0 += __popc(hb);
+  }
+}
+
+void migrate_plan2d(const Dev2D& d, cudaStream_t s) { k_migrate_plan<<<d.nrowjob, 32, 0, s>>>(d); }
+
+// ---------------------------------------------------------------------------
+// sort__bucket (2d/common/sort.f90:36-82): stable counting sort of each row by
+// the x cell i = int(x) (no division by delx, as in the reference).  One warp
+// per (species, row): histogram in shared memory, exclusive scan -> cumcnt,
+// then a rank pass in slot order where lanes with equal cells are ordered by
+// __match_any_sync, which keeps the sort stable.  map[pos] = source slot.
+// The input sequence is slist (post-migration order) or, if null, the row itself.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(32) k_sort_rank(Dev2D d, Parts64 P, const int* slist, const int* counts) {
+  extern __shared__ int off[];
+  const Grid2D g = d.g;
+  const int row = blockIdx.x;
+  const int lane = threadIdx.x;
+  const int n = counts[row];
+  const int nx = g.nx;
+  const size_t rb = (size_t)row * d.cap;
+  for (int k = lane; k <= nx; k += 32) off[k] = 0;
+  __syncwarp();
+  for (int t0 = 0; t0 < n; t0 += 32) {
+    const int t = t0 + lane;
+    if (t < n) {
+      const int src = slist ? slist[rb + t] : (int)(rb + t);
+      int cell = (int)P.x[src] - g.nxgs;
+      if (cell < 0 || cell >= nx) {
+        atomicOr(d.err, EB_OUT_OF_RANGE);
+        cell = cell < 0 ? 0 : nx - 1;
+      }
+      atomicAdd(&off[cell], 1);
+    }
+  }
+  __syncwarp();
+  int* ccr = d.cc + (size_t)row * (nx + 1);
+  int carry = 0;
+  for (int k0 = 0; k0 < nx; k0 += 32) {
+    const int k = k0 + lane;
+    const int v = k < nx ? off[k] : 0;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int excl = incl - v + carry;
+    if (k < nx) {
+      off[k] = excl;
+      ccr[k] = excl;
+    }
+    carry += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (lane == 0) ccr[nx] = carry;
+  __syncwarp();
+  const unsigned lt = lanemask_lt();
+  for (int t0 = 0; t0 < n; t0 += 32) {
+    const int t = t0 + lane;
+    const bool act = t < n;
+    int src = 0, cell = -1 - lane;
+    if (act) {
+      src = slist ? slist[rb + t] : (int)(rb + t);
+      cell = (int)P.x[src] - g.nxgs;
+      cell = cell < 0 ? 0 : (cell >= nx ? nx - 1 : cell);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, cell);
+    int base = 0;
+    if (act) base = off[cell];
+    __syncwarp();
+    if (act && lane == __ffs(peers) - 1) off[cell] = base + __popc(peers);
+    __syncwarp();
+    if (act) d.map[rb + base + __popc(peers & lt)] = src;
+  }
+}
+
+void sort_rank2d(const Dev2D& d, const Parts64& P, const int* slist, cudaStream_t s) {
+  const int* counts = slist ? d.np2new : d.np2;
+  k_sort_rank<<<d.nrowjob, 32, (d.g.nx + 1) * sizeof(int), s>>>(d, P, slist, counts);
+}
+
+// dst[row][pos] = src[map[row][pos]] for pos < counts[row]
+__global__ void k_gather(Dev2D d, Parts64 S, Parts64 D, const int* map, const int* counts) {
+  const int row = blockIdx.y;
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= counts[row]) return;
+  const size_t k = (size_t)row * d.cap + pos;
+  const size_t m = (size_t)map[k];
+  D.x[k] = S.x[m];
+  D.y[k] = S.y[m];
+  D.ux[k] = S.ux[m];
+  D.uy[k] = S.uy[m];
+  D.uz[k] = S.uz[m];
+  D.id[k] = S.id[m];
+}
+
+void gather2d(const Dev2D& d, const Parts64& src, const Parts64& dst, const int* map, const int* counts,
+              cudaStream_t s) {
+  dim3 grid((d.cap + 255) / 256, d.nrowjob);
+  k_gather<<<grid, 256, 0, s>>>(d, src, dst, map, counts);
+}
+
+// ---------------------------------------------------------------------------
+// layout conversions between the reference's particle layout up(ndim, np, ny, nsp)
+// (AoS inside each row) and the device SoA; rows [row0, row0+nrows) of a staging block
+// ---------------------------------------------------------------------------
+__global__ void k_aos_to_soa(Dev2D d, const double* aos, int ndim, int np_host, int row0, Parts64 P) {
+  const int row = row0 + blockIdx.y;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.np2[row]) return;
+  const double* a = aos + ((size_t)blockIdx.y * np_host + s) * ndim;
+  const size_t k = (size_t)row * d.cap + s;
+  P.x[k] = a[0];
+  P.y[k] = a[1];
+  P.ux[k] = a[2];
+  P.uy[k] = a[3];
+  P.uz[k] = a[4];
+  P.id[k] = ndim > 5 ? __double_as_longlong(a[5]) : 0;
+}
+
+__global__ void k_soa_to_aos(Dev2D d, double* aos, int ndim, int np_host, int row0, Parts64 P) {
+  const int row = row0 + blockIdx.y;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= np_host) return;
+  double* a = aos + ((size_t)blockIdx.y * np_host + s) * ndim;
+  if (s >= d.np2[row] || s >= d.cap) {
+    for (int c = 0; c < ndim; ++c) a[c] = 0.0;
+    return;
+  }
+  const size_t k = (size_t)row * d.cap + s;
+  a[0] = P.x[k];
+  a[1] = P.y[k];
+  a[2] = P.ux[k];
+  a[3] = P.uy[k];
+  a[4] = P.uz[k];
+  if (ndim > 5) a[5] = __longlong_as_double(P.id[k]);
+}
+
+void aos_to_soa2d(const Dev2D& d, const double* aos, int ndim, int np_host, int row0, int nrows,
+                  const Parts64& P, cudaStream_t s) {
+  dim3 grid((np_host + 255) / 256, nrows);
+  k_aos_to_soa<<<grid, 256, 0, s>>>(d, aos, ndim, np_host, row0, P);
+}
+
+void soa_to_aos2d(const Dev2D& d, double* aos, int ndim, int np_host, int row0, int nrows, const Parts64& P,
+                  cudaStream_t s) {
+  dim3 grid((np_host + 255) / 256, nrows);
+  k_soa_to_aos<<<grid, 256, 0, s>>>(d, aos, ndim, np_host, row0, P);
+}
+
+__global__ void k_ref_to_soa(const double* ref, double* soa, int ncomp, int nslab) {
+  const size_t n = (size_t)ncomp * nslab;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t cell = k / ncomp, c = k - cell * ncomp;
+    soa[c * nslab + cell] = ref[k];
+  }
+}
+__global__ void k_soa_to_ref(const double* soa, double* ref, int ncomp, int nslab) {
+  const size_t n = (size_t)ncomp * nslab;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t cell = k / ncomp, c = k - cell * ncomp;
+    ref[k] = soa[c * nslab + cell];
+  }
+}
+void field_ref_to_soa(const double* ref, double* soa, int ncomp, int nslab, cudaStream_t s) {
+  k_ref_to_soa<<<4 * 152, 256, 0, s>>>(ref, soa, ncomp, nslab);
+}
+void field_soa_to_ref(const double* soa, double* ref, int ncomp, int nslab, cudaStream_t s) {
+  k_soa_to_ref<<<4 * 152, 256, 0, s>>>(soa, ref, ncomp, nslab);
+}
+
+// ---------------------------------------------------------------------------
+// Device-side synthetic Weibel loader (same conventions as loader.py: species
+// 0 = ions, 1 = electrons; co-located pairs; n0 = ppc per cell, uniform in the
+// cell; electron beams +-drift alternating by particle; Philox4x32-10 streams).
+// ---------------------------------------------------------------------------
+__global__ void k_load_weibel2d(Dev2D d, int ppc, unsigned long long seed, double drift, int axis, double u_thi,
+                                double u_the) {
+  const Grid2D g = d.g;
+  const int jj = blockIdx.y, isp = blockIdx.z;
+  const int npr = g.nx * ppc;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = isp * g.ny + jj;
+  if (k < npr && k < d.cap) {
+    const uint2 key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
+    const uint4 rp = philox4x32(make_uint4((unsigned)k, (unsigned)jj, 0u, 0u), key);
+    const uint4 r1 = philox4x32(make_uint4((unsigned)k, (unsigned)jj, 1u + 2u * isp, 0u), key);
+    const uint4 r2 = philox4x32(make_uint4((unsigned)k, (unsigned)jj, 2u + 2u * isp, 0u), key);
+    const int cx = k / ppc;
+    const size_t idx = (size_t)row * d.cap + k;
+    d.A.x[idx] = ((double)(g.nxgs + cx) + (1.0 - u01(rp.x, rp.y))) * d.ph.delx;
+    d.A.y[idx] = ((double)(g.nygs + jj) + (1.0 - u01(rp.z, rp.w))) * d.ph.delx;
+    const double sd = isp == 0 ? u_thi : u_the;
+    const double twopi = 6.283185307179586;
+    const double a1 = u01(r1.x, r1.y), b1 = u01(r1.z, r1.w), a2 = u01(r2.x, r2.y), b2 = u01(r2.z, r2.w);
+    double u[3];
+    const double rad1 = sqrt(-2.0 * log(a1)), rad2 = sqrt(-2.0 * log(a2));
+    u[0] = sd * rad1 * cos(twopi * b1);
+    u[1] = sd * rad1 * sin(twopi * b1);
+    u[2] = sd * rad2 * cos(twopi * b2);
+    if (isp == 1 && drift != 0.0) u[axis] += (k % 2 == 0) ? drift : -drift;
+    d.A.ux[idx] = u[0];
+    d.A.uy[idx] = u[1];
+    d.A.uz[idx] = u[2];
+    d.A.id[idx] = -((long long)jj * npr + k + 1);
+  }
+  if (k <= g.nx && blockIdx.x == 0) {
+    for (int kk = threadIdx.x; kk <= g.nx; kk += blockDim.x) d.cc[(size_t)row * (g.nx + 1) + kk] = kk * ppc;
+  }
+  if (k == 0) d.np2[row] = npr < d.cap ? npr : d.cap;
+}
+
+void load_weibel2d_ppc(const Dev2D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
+                       double u_thi, double u_the, cudaStream_t s) {
+  dim3 grid((d.g.nx * ppc + 255) / 256, d.g.ny, d.ph.nsp);
+  k_load_weibel2d<<<grid, 256, 0, s>>>(d, ppc, seed, drift, drift_axis, u_thi, u_the);
+}
+
+}  // namespace wpic

@@ -1,0 +1,8 @@
+// FP64 kernels with fused multiply-add contraction: the production FP64 build.
+#include "common.cuh"
+
+namespace wpic {
+namespace fast {
+#include "fp2d.cuh"
+}  // namespace fast
+}  // namespace wpic

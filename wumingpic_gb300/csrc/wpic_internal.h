@@ -1,0 +1,127 @@
+// Internal declarations shared by the C-ABI unit (capi.cu) and the kernel units.
+//
+// Device data layout (2D; one GPU holds the whole domain):
+//   fields   SoA, component-major, with the reference's +-2 ghost layers:
+//            F[c][jj][ii], jj = j-(nys-2) in [0,ny+4), ii = i-(nxgs-2) in [0,nx+4)
+//   particles SoA per species and row ("bucket row" = the reference's storage row j),
+//            slot s of row jj of species isp at ((isp*ny)+jj)*cap + s; inside a row the
+//            particles are bucket-sorted by x cell, cumcnt giving the cell offsets
+//   cumcnt   [isp][jj][0..nx]  (cumcnt(nxgs+ii, j, isp))
+//   np2      [isp][jj]
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace wpic {
+
+enum Status : int {
+  ST_OK = 0,
+  ST_CG_NOT_CONVERGED = 1,
+  ST_CAPACITY = 2,
+  ST_OUT_OF_RANGE = 3,
+  ST_MOVED_TOO_FAR = 4,
+  ST_NONFINITE = 5,
+  ST_BAD_ARGUMENT = 6,
+  ST_CUDA = 7,
+  ST_NOT_INITIALISED = 8,
+};
+
+// device error word bits
+enum ErrBit : int {
+  EB_CAPACITY = 1,
+  EB_OUT_OF_RANGE = 2,
+  EB_MOVED_TOO_FAR = 4,
+  EB_CG = 8,
+};
+
+enum Bc : int { BC_PERIODIC = 0, BC_RECONNECTION = 1 };
+
+struct Grid2D {
+  int nx, ny;       // interior cells
+  int nxgs, nygs;   // reference index of the first interior cell (nxgs, nys)
+  int fp;           // field row pitch = nx + 4
+  int fplane;       // (nx + 4) * (ny + 4)
+  int ncell;        // nx * ny
+};
+
+struct Phys {
+  double delx, delt, c, gfac;
+  double q[2], r[2];
+  double p_d_delx;  // particle__init:  1./delx        (2d/common/particle.f90:41)
+  double d_delx;    // field__init:     1./delx        (2d/common/field.f90:58)
+  double d_delt;    // field__init:     1./delt        (2d/common/field.f90:59)
+  double f1, f2, f3, f4, f5, pi;
+  int nsp;
+  int bc;
+};
+
+struct Parts64 {
+  double *x, *y, *ux, *uy, *uz;
+  long long* id;
+};
+
+struct CGState {
+  double sum_g, eps, sumr_g, sum2_g, sum1_g, av, bv;
+  int ite, active, fixed, pad;
+};
+
+struct Dev2D {
+  Grid2D g;
+  Phys ph;
+  int cap;          // device slots per row per species
+  int nrowjob;      // nsp * ny
+  Parts64 A, B, C;  // A = "up" (sorted state), B = "gp" (scratch / new state), C = migration staging
+  int* cc;          // cumcnt [nsp][ny][nx+1]
+  int* np2;         // [nsp][ny]
+  double *uf, *df, *uj;  // [6|6|3][ny+4][nx+4]
+  double* gkl;           // [3][ny][nx]
+  double* cellJ;         // [75][ny][nx]  per-cell 5x5 current tiles (3 components)
+  double *phi, *p, *r, *ap, *b;  // [3][ny][nx]
+  double* partials;      // reduction partials
+  int nred;              // number of reduction blocks per component
+  CGState* cg;           // [3]
+  int ite_max;
+  // migration / sort scratch
+  int8_t* mig;           // per slot: 0 stay, 1 up (+y), 2 down (-y)
+  int *ulist, *dlist, *tlist, *slist, *map;  // per slot
+  int *nup, *ndown, *np2new;                 // per row job
+  int* err;              // device error word
+  double* red_out;       // misc reduction output (energy)
+};
+
+// ---- launchers: precision-dependent kernels exist in two builds ----
+#define WPIC_DECLARE_FP_LAUNCHERS                                                          \
+  void push2d(const Dev2D& d, cudaStream_t s);                                             \
+  void deposit2d(const Dev2D& d, cudaStream_t s);                                          \
+  void gkl2d(const Dev2D& d, cudaStream_t s);                                              \
+  void cg_init2d(const Dev2D& d, cudaStream_t s);                                          \
+  void cg_iter_ap2d(const Dev2D& d, cudaStream_t s);                                       \
+  void cg_iter_update2d(const Dev2D& d, cudaStream_t s);                                   \
+  void cg_iter_p2d(const Dev2D& d, cudaStream_t s);                                        \
+  void cg_store2d(const Dev2D& d, cudaStream_t s);                                         \
+  void efield2d(const Dev2D& d, cudaStream_t s);                                           \
+  void energy2d(const Dev2D& d, cudaStream_t s);
+
+namespace exact { WPIC_DECLARE_FP_LAUNCHERS }
+namespace fast { WPIC_DECLARE_FP_LAUNCHERS }
+
+// ---- precision-independent kernels (integer work, copies, exact adds) ----
+void curre_fold2d(const Dev2D& d, cudaStream_t s);
+void dfield_ghost2d(const Dev2D& d, cudaStream_t s);
+void uf_add2d(const Dev2D& d, cudaStream_t s);
+void particle_x2d(const Dev2D& d, const Parts64& P, cudaStream_t s);
+void migrate_scan2d(const Dev2D& d, const Parts64& P, cudaStream_t s);
+void migrate_plan2d(const Dev2D& d, cudaStream_t s);
+void sort_rank2d(const Dev2D& d, const Parts64& P, const int* slist, cudaStream_t s);
+void gather2d(const Dev2D& d, const Parts64& src, const Parts64& dst, const int* map, const int* counts,
+              cudaStream_t s);
+void aos_to_soa2d(const Dev2D& d, const double* aos, int ndim, int np_host, int row0, int nrows,
+                  const Parts64& P, cudaStream_t s);
+void soa_to_aos2d(const Dev2D& d, double* aos, int ndim, int np_host, int row0, int nrows, const Parts64& P,
+                  cudaStream_t s);
+void field_ref_to_soa(const double* ref, double* soa, int ncomp, int nslab, cudaStream_t s);
+void field_soa_to_ref(const double* soa, double* ref, int ncomp, int nslab, cudaStream_t s);
+void load_weibel2d_ppc(const Dev2D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
+                       double u_thi, double u_the, cudaStream_t s);
+
+}  // namespace wpic

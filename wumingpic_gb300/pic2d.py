@@ -1,0 +1,167 @@
+"""Host-side mirror of WumingPIC's 2D module interface over the C ABI.
+
+``Pic2D`` holds one device context and exposes the reference's procedure
+names (particle__solv, field__fdtd_i, bc__particle_x, bc__particle_y,
+sort__bucket) acting on device-resident state, plus the reference-layout state
+exchange a Fortran driver needs at its I/O points.  Errors that the reference
+reports with ``stop`` raise ``WpicError`` carrying the status code.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+from .loader import Plasma2D, State2D, empty_state2d
+
+
+def _ptr(a, dtype):
+    assert a.dtype == dtype and (a.flags.f_contiguous or a.ndim == 1), (a.dtype, a.flags)
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Pic2D:
+    def __init__(self, plasma: Plasma2D, precision="fp64", stream=None, device_cap=0):
+        self.p = plasma
+        q, r = plasma.charges()
+        prm = _lib.WpicParams()
+        prm.ndim, prm.np, prm.nsp = plasma.ndim, plasma.np_cap, plasma.nsp
+        prm.nxgs, prm.nxge = plasma.nxgs, plasma.nxge
+        prm.nygs, prm.nyge = plasma.nygs, plasma.nyge
+        prm.nys, prm.nye = plasma.nygs, plasma.nyge
+        prm.delx, prm.delt, prm.c, prm.gfac = plasma.delx, plasma.delt, plasma.c, plasma.gfac
+        prm.q[0], prm.q[1] = q[0], q[1]
+        prm.r[0], prm.r[1] = r[0], r[1]
+        prm.bc_kind = _lib.BC_PERIODIC if plasma.bc == "periodic" else _lib.BC_RECONNECTION
+        prm.precision = {"fp64": _lib.FP64, "fp64_exact": _lib.FP64_EXACT}[precision]
+        prm.device_cap = int(device_cap)
+        self.precision = precision
+        h = ctypes.c_void_p()
+        check(lib().wpic_init_2d(ctypes.byref(h), ctypes.byref(prm), ctypes.c_void_p(stream or 0)), "wpic_init_2d")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().wpic_finalize(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    # ---- state exchange (reference layout) ----
+    def put_state(self, st: State2D, gp=False):
+        check(lib().wpic_put_particles(self._h, 0, _ptr(st.up, np.float64), _ptr(st.np2, np.int32),
+                                       _ptr(st.cumcnt, np.int32)), "put up")
+        if gp:
+            check(lib().wpic_put_particles(self._h, 1, _ptr(st.gp, np.float64), _ptr(st.np2, np.int32), None),
+                  "put gp")
+        check(lib().wpic_put_fields(self._h, _ptr(st.uf, np.float64)), "put uf")
+
+    def get_state(self, st: State2D = None) -> State2D:
+        if st is None:
+            st = empty_state2d(self.p)
+        check(lib().wpic_get_particles(self._h, 0, _ptr(st.up, np.float64), _ptr(st.np2, np.int32),
+                                       _ptr(st.cumcnt, np.int32)), "get up")
+        check(lib().wpic_get_particles(self._h, 1, _ptr(st.gp, np.float64), None, None), "get gp")
+        check(lib().wpic_get_fields(self._h, _ptr(st.uf, np.float64)), "get uf")
+        return st
+
+    def put_particles(self, which, up, np2, cumcnt=None):
+        check(lib().wpic_put_particles(self._h, which, _ptr(up, np.float64), _ptr(np2, np.int32),
+                                       None if cumcnt is None else _ptr(cumcnt, np.int32)), "put particles")
+
+    def get_particles(self, which):
+        p = self.p
+        up = np.zeros((p.ndim, p.np_cap, p.ny, p.nsp), order="F")
+        np2 = np.zeros((p.ny, p.nsp), np.int32, order="F")
+        cc = np.zeros((p.nx + 1, p.ny, p.nsp), np.int32, order="F")
+        check(lib().wpic_get_particles(self._h, which, _ptr(up, np.float64), _ptr(np2, np.int32),
+                                       _ptr(cc, np.int32)), "get particles")
+        return up, np2, cc
+
+    def put_fields(self, uf):
+        check(lib().wpic_put_fields(self._h, _ptr(np.asfortranarray(uf), np.float64)), "put uf")
+
+    def get_fields(self):
+        uf = np.zeros((6, self.p.nx + 4, self.p.ny + 4), order="F")
+        check(lib().wpic_get_fields(self._h, _ptr(uf, np.float64)), "get uf")
+        return uf
+
+    def get_df(self):
+        df = np.zeros((6, self.p.nx + 4, self.p.ny + 4), order="F")
+        check(lib().wpic_get_df(self._h, _ptr(df, np.float64)), "get df")
+        return df
+
+    def put_df(self, df):
+        check(lib().wpic_put_df(self._h, _ptr(np.asfortranarray(df), np.float64)), "put df")
+
+    def get_uj(self):
+        uj = np.zeros((3, self.p.nx + 4, self.p.ny + 4), order="F")
+        check(lib().wpic_get_uj(self._h, _ptr(uj, np.float64)), "get uj")
+        return uj
+
+    # ---- the module procedures ----
+    def particle__solv(self):
+        check(lib().wpic_particle_solv(self._h), "particle__solv")
+
+    def field__fdtd_i(self):
+        check(lib().wpic_field_fdtd_i(self._h), "field__fdtd_i")
+
+    def ele_cur(self):
+        check(lib().wpic_ele_cur(self._h), "ele_cur")
+
+    def bc__particle_x(self):
+        check(lib().wpic_bc_particle_x(self._h), "bc__particle_x")
+
+    def bc__particle_y(self):
+        check(lib().wpic_bc_particle_y(self._h), "bc__particle_y")
+
+    def sort__bucket(self):
+        check(lib().wpic_sort_bucket(self._h), "sort__bucket")
+
+    def step(self, nsteps=1):
+        check(lib().wpic_step(self._h, int(nsteps)), "step")
+
+    def energy(self):
+        out = np.zeros(self.p.nsp + 2)
+        check(lib().wpic_energy(self._h, _ptr(out, np.float64)), "energy")
+        return out
+
+    def cg_control(self, fixed=None, ite_max=100):
+        if fixed is None:
+            check(lib().wpic_cg_control(self._h, None, ite_max))
+        else:
+            f = np.ascontiguousarray(fixed, dtype=np.int32)
+            check(lib().wpic_cg_control(self._h, _ptr(f, np.int32), ite_max))
+
+    def cg_iters(self):
+        out = np.zeros(3, np.int32)
+        check(lib().wpic_cg_iters(self._h, _ptr(out, np.int32)))
+        return out
+
+    def load_weibel(self, seed=None):
+        """Device-side seeded loading of the plasma described by self.p."""
+        p = self.p
+        b0 = np.ascontiguousarray(p.b0, dtype=np.float64)
+        check(lib().wpic_load_weibel_2d(self._h, p.ppc, int(p.seed if seed is None else seed), p.drift,
+                                        p.drift_axis, p.u_thi, p.u_the, _ptr(b0, np.float64)), "load")
+
+    def num_particles(self):
+        return lib().wpic_num_particles(self._h)
+
+    def synchronize(self):
+        check(lib().wpic_synchronize(self._h))
+
+    # ---- stage timing ----
+    def timing(self, enable=True):
+        check(lib().wpic_timing_enable(self._h, 1 if enable else 0))
+
+    def stage_times(self):
+        n = lib().wpic_num_stages()
+        ms = np.zeros(n)
+        ln = np.zeros(n, np.int64)
+        check(lib().wpic_timing_get(self._h, _ptr(ms, np.float64), _ptr(ln, np.int64), n))
+        return {lib().wpic_stage_name(k).decode(): (float(ms[k]), int(ln[k])) for k in range(n)}
