@@ -286,7 +286,7 @@ def test_status_codes_instead_of_stop(gpu_lib):
     assert e.value.status == _lib.CG_NOT_CONVERGED
     # bad cumcnt is rejected at the boundary
     bad = st.copy()
-    bad.cumcnt[3, 0, 0] += 1
+    bad.cumcnt[-1, 0, 0] += 1  # last prefix sum no longer equals np2
     g4 = make_gpu(p, "fp64", gpu_lib)
     with pytest.raises(WpicError) as e:
         g4.put_state(bad)
