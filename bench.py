@@ -3,15 +3,17 @@
 Default workload: the 2D Weibel configuration at scale -- 2048 x 2048 cells,
 64 particles per cell per species (536,870,912 particles), beams +-0.3c,
 u_th = 0.1c, c dt/dx = 0.5 -- loaded on the device from a seeded Philox
-stream.  One step = push + deposition + implicit field solve + particle
-boundaries + bucket sort, i.e. one pass of the reference driver loop body.
+stream (synthetic data).  One step = push + deposition + implicit field solve
+(CG) + particle boundaries + bucket sort/migration: one pass of the reference
+driver loop body (2d/proj/weibel/app.f90:102-107).
 
-Prints one JSON line.  ``--impl reference`` times the CPU restatement of the
-reference (oracle/, OpenMP over all host cores) on the same metric instead.
+The headline value is the mixed-precision path (FP32 particles, FP64 fields);
+the FP64 path is timed beside it on the same workload.  Prints one JSON line.
+``--impl reference`` times the CPU restatement of the reference (oracle/,
+OpenMP over all host cores) on the same metric instead.
 """
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
@@ -24,10 +26,21 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-updates/s on 1 GB300: mixed vs FP64 path at <=1% growth-rate error"
 UNIT = "particle-updates/s"
 
-# algorithmic bytes per particle for the FP64 kernels (compulsory state traffic)
-BYTES_PUSH_FP64 = 96       # read x,y,ux,uy,uz,id (48 B) + write the same (48 B)
-BYTES_DEPOSIT_FP64 = 56    # read old x,y (16 B) + new x,y,ux,uy,uz (40 B)
-BYTES_DEPOSIT_CELL = 600   # per cell: one 5x5x3 FP64 tile written
+# Algorithmic bytes of the dominant kernels (compulsory traffic, one launch):
+#  k_mix_push (mixed push + deposit): per particle read cell (4 B) + x/y offsets (8 B) +
+#    ux, uy, uz (12 B) and write them back = 48 B; the id (8 B) is not touched by the push.
+#  k_push2d (FP64 push): per particle read x, y, ux, uy, uz, id (48 B) + write them (48 B) = 96 B.
+#  k_deposit2d (FP64 deposit): per particle read old x, y (16 B) + new x, y, ux, uy, uz (40 B)
+#    = 56 B, plus 600 B per cell for the cell's 5x5x3 current tile.
+BYTES_MIX_PUSH = 48
+BYTES_PUSH_FP64 = 96
+BYTES_DEPOSIT_FP64 = 56
+BYTES_DEPOSIT_CELL = 600
+# FP64 floating-point operations per particle of the FP64 kernels, counted from the
+# reference's statements (2d/common/particle.f90:99-163, 2d/common/field.f90:224-298) with
+# each sqrt and divide counted as one operation
+FLOP_PUSH_FP64 = 215
+FLOP_DEPOSIT_FP64 = 600
 
 
 def config(name):
@@ -36,7 +49,7 @@ def config(name):
         return Plasma2D(nx=2048, ny=2048, ppc=64, drift=0.3, u_the=0.1, seed=20261203, np_slack=1.25)
     if name == "cfg0":
         return Plasma2D(nx=256, ny=256, ppc=16, drift=0.5, u_the=0.05, seed=20261203)
-    if name.startswith("sq"):  # sqN_PPC: N x N cells, PPC per species, cfg1 physics
+    if name.startswith("sq"):  # sqN_PPC: N x N cells, PPC per species, the cfg1 physics
         n, ppc = name[2:].split("_")
         return Plasma2D(nx=int(n), ny=int(n), ppc=int(ppc), drift=0.3, u_the=0.1, seed=20261203, np_slack=1.25)
     raise ValueError(name)
@@ -90,7 +103,7 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def measured_peaks():
+def measured_hbm_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
@@ -118,25 +131,25 @@ def cpu_baseline(name, threads=None, budget_s=20.0):
         if rc:
             raise RuntimeError(f"oracle status {rc}")
         steps += 1
-        if time.perf_counter() - t0 > budget_s or steps >= 50:
+        if time.perf_counter() - t0 > budget_s or steps >= 200:
             break
     dt = time.perf_counter() - t0
     return {"value": p.n_particles * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{steps} steps of {p.nx}x{p.ny} cells x {p.ppc} ppc/species ({p.n_particles} particles), "
-                      f"same physics as the workload, {dt:.1f} s"}
+                      f"same physics as the workload, {dt:.1f} s, OpenMP threads = host cores"}
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's step on the host cores."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     name = args.config
     full = config(name)
     cores = os.cpu_count() or 1
-    vals = []
-    base = None
+    vals, base = [], None
     for k in range(args.warmup + args.steps):
-        b = cpu_baseline(name, threads=cores, budget_s=max(2.0, 60.0 / max(1, args.warmup + args.steps)))
+        b = cpu_baseline(name, threads=cores, budget_s=max(2.0, 90.0 / max(1, args.warmup + args.steps)))
         if k >= args.warmup:
             vals.append(b["value"])
             base = b
@@ -150,41 +163,15 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cfg1")
-    ap.add_argument("--precision", default="fp64")
-    ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--stages", action="store_true", help="print the per-stage breakdown to stderr")
-    args = ap.parse_args()
-    if args.impl == "reference":
-        return run_reference(args)
-
-    import numpy as np
-    import torch
-
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-
+def time_path(p, precision, steps, warmup, rank, torch, dist, local):
+    """Device-resident timing of `steps` fused steps on one context."""
     from wumingpic_gb300.pic2d import Pic2D
-    p = config(args.config)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    g = Pic2D(p, precision=args.precision, stream=stream.cuda_stream)
+    g = Pic2D(p, precision=precision, stream=stream.cuda_stream)
     g.load_weibel(seed=p.seed + 7919 * rank)
     npart = g.num_particles()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         g.step(1)
     g.timing(True)
     sampler = ClockSampler(local)
@@ -194,7 +181,7 @@ def main():
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         g.step(1)
     e1.record(stream)
     torch.cuda.synchronize()
@@ -208,26 +195,78 @@ def main():
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
+    return g, npart, ms, stages, clocks
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cfg1")
+    ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the FP64 path (0 = skip)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--stages", action="store_true", help="print the per-stage breakdown to stderr")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from wumingpic_gb300 import _lib
+
+    p = config(args.config)
+    hbm_peak, hbm_src = measured_hbm_peak()
+
+    # ---- mixed path: the headline ----
+    g, npart, ms, stages, clocks = time_path(p, "mixed", args.steps, args.warmup, rank, torch, dist, local)
     value = npart * world * args.steps / (ms / 1e3)
-
-    # roofline of the dominant kernel, from CUDA events around its launches
-    peak, peak_kind = measured_peaks()
-    dom = max(("push", "deposit"), key=lambda k: stages[k][0])
-    dms, dl = stages[dom]
-    per_launch_ms = dms / max(1, dl if dom == "push" else dl // 2)
-    if dom == "push":
-        alg = BYTES_PUSH_FP64 * npart
-    else:
-        alg = BYTES_DEPOSIT_FP64 * npart + BYTES_DEPOSIT_CELL * p.nx * p.ny
-    achieved = alg / (per_launch_ms / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "k_push2d" if dom == "push" else "k_deposit2d", "achieved": achieved,
-                "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                "peak_source": peak_kind, "note": "FP64 kernels are bound by the FP64 pipe, not by HBM"}
+    push_ms, push_n = stages["push"]
+    per_launch = push_ms / max(1, push_n)
+    achieved = BYTES_MIX_PUSH * npart / (per_launch / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_mix_push (fused push + deposit, mixed precision)",
+                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": None, "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "bytes_per_particle": BYTES_MIX_PUSH, "launch_ms": per_launch}
     launches = int(sum(v[1] for v in stages.values()))
+    e2e = None if args.no_e2e else measure_e2e(g, p)
+    g.close()
 
-    e2e = None
-    if not args.no_e2e:
-        e2e = measure_e2e(g, p, args)
+    # ---- FP64 path on the same workload ----
+    fp64 = None
+    if args.fp64_steps > 0:
+        g64, n64, ms64, st64, clk64 = time_path(p, "fp64", args.fp64_steps, 1, rank, torch, dist, local)
+        v64 = n64 * world * args.fp64_steps / (ms64 / 1e3)
+        peak64 = _lib.fma_peak_gflops(True)
+        dep_ms = st64["deposit"][0] / max(1, st64["deposit"][1] // 2)
+        push64_ms = st64["push"][0] / max(1, st64["push"][1])
+        fp64 = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps,
+                "warmup": 1, "mixed_over_fp64": value / v64 if v64 else None,
+                "fp64_fma_peak_gflops": peak64,
+                "kernels": {
+                    "k_deposit2d": {"launch_ms": dep_ms,
+                                    "hbm_gbs": (BYTES_DEPOSIT_FP64 * n64 + BYTES_DEPOSIT_CELL * p.nx * p.ny)
+                                    / (dep_ms / 1e3) / 1e9,
+                                    "fp64_gflops": FLOP_DEPOSIT_FP64 * n64 / (dep_ms / 1e3) / 1e9},
+                    "k_push2d": {"launch_ms": push64_ms,
+                                 "hbm_gbs": BYTES_PUSH_FP64 * n64 / (push64_ms / 1e3) / 1e9,
+                                 "fp64_gflops": FLOP_PUSH_FP64 * n64 / (push64_ms / 1e3) / 1e9}},
+                "stages_ms_per_step": {k: v[0] / args.fp64_steps for k, v in st64.items()}, "clocks": clk64}
+        for k in fp64["kernels"].values():
+            k["hbm_frac"] = k["hbm_gbs"] / hbm_peak
+            k["fp64_pipe_frac"] = k["fp64_gflops"] / peak64
+        g64.close()
+
     base = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -237,26 +276,32 @@ def main():
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": workload_desc(p, args.config), "precision": args.precision,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "config": workload_desc(p, args.config),
+                "path": "mixed: integer cell + FP32 offset, FP32 push/gather/deposition, FP64 fields and CG",
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clocks,
-                "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()}}
+                "clocks": clocks, "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()},
+                "fp64_path": fp64}
         print(json.dumps(line), flush=True)
         if args.stages:
             for k, (t, n) in stages.items():
-                print(f"{k:16s} {t / args.steps:10.3f} ms/step {n:8d} launches", file=sys.stderr)
-    g.close()
+                print(f"mixed {k:16s} {t / args.steps:10.3f} ms/step {n:8d} launches", file=sys.stderr)
+            if fp64:
+                for k, t in fp64["stages_ms_per_step"].items():
+                    print(f"fp64  {k:16s} {t:10.3f} ms/step", file=sys.stderr)
     if dist:
         dist.destroy_process_group()
 
 
-def measure_e2e(g, p, args):
+def measure_e2e(g, p):
     """The same step through the C ABI with the reference-layout state in host memory:
-    every step copies the state in (host -> device), runs the step and copies it back."""
-    import numpy as np
+    every step copies the state in (host -> device), runs the step and copies the new
+    state back (device -> host)."""
     st = g.get_state()
-    steps = max(1, min(args.steps, 3))
+    steps = 2
+    g.put_state(st)
+    g.step(1)
+    g.get_state(st)
     t0 = time.perf_counter()
     for _ in range(steps):
         g.put_state(st)
@@ -266,8 +311,8 @@ def measure_e2e(g, p, args):
     n = int(st.np2.sum())
     bytes_state = st.up.nbytes + st.uf.nbytes + st.np2.nbytes + st.cumcnt.nbytes
     return {"value": n * steps / dt, "unit": UNIT, "h2d_bytes_per_step": int(bytes_state),
-            "d2h_bytes_per_step": int(bytes_state + st.gp.nbytes), "steps": steps,
-            "note": "host arrays in the reference layout, pageable memory"}
+            "d2h_bytes_per_step": int(bytes_state), "steps": steps,
+            "note": "reference-layout host arrays (pageable), full state in and out every step"}
 
 
 if __name__ == "__main__":

@@ -52,6 +52,12 @@ extern "C" {
 /* arithmetic of the particle and field kernels */
 #define WPIC_FP64 0       /* FP64, fused multiply-add allowed */
 #define WPIC_FP64_EXACT 1 /* FP64 in the reference's operation order (bit-exact parity mode) */
+#define WPIC_MIXED 2      /* positions as integer cell + FP32 offset, FP32 push / gather / deposition
+                             weights, FP32 tile currents flushed into FP64 J, FP64 field solve.
+                             Requires nx and ny to be multiples of 16; particles live in 16 x 16-cell
+                             tile bins whose capacity is np * 256 / nx slots per species.  Only the fused
+                             wpic_step, the state exchange (which = 0), the loader and the
+                             diagnostics are available in this mode. */
 
 typedef struct wpic_ctx wpic_ctx;
 
@@ -67,7 +73,7 @@ typedef struct wpic_params {
   double delx, delt, c, gfac;
   double q[2], r[2];        /* charge and mass of each species */
   int bc_kind;              /* WPIC_BC_* */
-  int precision;            /* WPIC_FP64 or WPIC_FP64_EXACT */
+  int precision;            /* WPIC_FP64, WPIC_FP64_EXACT or WPIC_MIXED */
   int device_cap;           /* device particle slots per row per species; 0 = np */
 } wpic_params;
 
@@ -130,6 +136,10 @@ int wpic_timing_enable(wpic_ctx* ctx, int enable);
 int wpic_timing_get(wpic_ctx* ctx, double* ms, long long* launches, int n);
 const char* wpic_stage_name(int stage);
 int wpic_num_stages(void);
+
+/* FMA throughput of the device in GFLOP/s (fp64 != 0: FP64, else FP32), measured by a
+ * register-only kernel; the compute roof the FP64 kernels are reported against. */
+int wpic_measure_fma_peak(int fp64, double* gflops);
 
 int wpic_synchronize(wpic_ctx* ctx);
 long long wpic_num_particles(wpic_ctx* ctx);

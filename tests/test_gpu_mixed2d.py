@@ -1,0 +1,165 @@
+"""GPU tests of the mixed-precision 2D path (integer cell + FP32 offset,
+FP32 push/gather/deposition, FP64 fields), through the C ABI.
+
+Every result is stated as an error against the FP64 path:
+  * one step from the same state: momenta and positions within 1e-5 relative to
+    their scale, fields within 1e-4 of max|B, E|;
+  * charge conservation |d rho/dt + div J| <= 1e-6 of max |d rho/dt|, rho computed in
+    FP64 from the exact stored positions;
+  * bookkeeping exact: particle count and the set of IDs conserved, every
+    particle inside the cell its bin records.
+"""
+import numpy as np
+import pytest
+
+from tests.helpers import continuity_residual, small_case, small_plasma
+from wumingpic_gb300.loader import load_weibel2d
+
+pytestmark = pytest.mark.gpu
+
+
+def make(p, precision, gpu_lib):
+    from wumingpic_gb300.pic2d import Pic2D
+    return Pic2D(p, precision=precision)
+
+
+def by_id(st, p):
+    """dict id -> (x, y, ux, uy, uz) over all valid particles, plus species index"""
+    out = {}
+    for isp in range(p.nsp):
+        for jj in range(p.ny):
+            n = st.np2[jj, isp]
+            a = st.up[:, :n, jj, isp]
+            ids = a[5].view(np.int64)
+            for k in range(n):
+                out[(isp, int(ids[k]))] = a[:5, k]
+    return out
+
+
+def test_put_get_round_trip(gpu_lib):
+    p, st = small_case(nx=32, ny=32, ppc=5, seed=4)
+    g = make(p, "mixed", gpu_lib)
+    g.put_state(st)
+    out = g.get_state()
+    np.testing.assert_array_equal(out.np2, st.np2)
+    np.testing.assert_array_equal(out.cumcnt, st.cumcnt)
+    for isp in range(p.nsp):
+        for jj in range(p.ny):
+            n = st.np2[jj, isp]
+            np.testing.assert_array_equal(out.up[5, :n, jj, isp].view(np.int64), st.up[5, :n, jj, isp].view(np.int64))
+            np.testing.assert_allclose(out.up[0:2, :n, jj, isp], st.up[0:2, :n, jj, isp], rtol=0, atol=2 ** -22)
+            np.testing.assert_allclose(out.up[2:5, :n, jj, isp], st.up[2:5, :n, jj, isp], rtol=2 ** -23, atol=1e-30)
+
+
+def test_one_step_against_fp64(gpu_lib):
+    p, st = small_case(nx=32, ny=32, ppc=8, seed=6)
+    rng = np.random.default_rng(6)
+    st.uf[...] = 0.02 * rng.standard_normal(st.uf.shape)
+    st.uf[:, :2, :] = st.uf[:, p.nx:p.nx + 2, :]
+    st.uf[:, p.nx + 2:, :] = st.uf[:, 2:4, :]
+    st.uf[:, :, :2] = st.uf[:, :, p.ny:p.ny + 2]
+    st.uf[:, :, p.ny + 2:] = st.uf[:, :, 2:4]
+    gm, gd = make(p, "mixed", gpu_lib), make(p, "fp64", gpu_lib)
+    gm.put_state(st)
+    gd.put_state(st)
+    gm.step(1)
+    gd.step(1)
+    a, b = gm.get_state(), gd.get_state()
+    assert a.np2.sum() == b.np2.sum() == p.n_particles
+    pa, pb = by_id(a, p), by_id(b, p)
+    assert pa.keys() == pb.keys()
+    xa = np.array([pa[k] for k in sorted(pa)])
+    xb = np.array([pb[k] for k in sorted(pb)])
+    np.testing.assert_allclose(xa[:, :2], xb[:, :2], rtol=0, atol=1e-5)
+    uscale = np.abs(xb[:, 2:]).max()
+    np.testing.assert_allclose(xa[:, 2:], xb[:, 2:], rtol=0, atol=1e-5 * uscale)
+    fscale = np.abs(b.uf).max()
+    np.testing.assert_allclose(a.uf, b.uf, rtol=0, atol=1e-4 * fscale)
+
+
+def test_charge_conservation_fp32_deposit(gpu_lib):
+    p, st = small_case(nx=32, ny=32, ppc=16, seed=8)
+    q, _ = p.charges()
+    g = make(p, "mixed", gpu_lib)
+    g.put_state(st)
+    for _ in range(3):
+        before = g.get_state()
+        g.step(1)
+        after = g.get_state()
+        # positions after the step are the new positions (no x/y wrap issue: rho2d wraps periodically)
+        res, scale = continuity_residual(p, q, before.up, _match_order(before, after, p), before.np2,
+                                         g.get_uj())
+        assert res <= 1e-6 * scale, (res, scale)
+
+
+def _match_order(before, after, p):
+    """after-step positions arranged in the before-step slot order (by id)"""
+    m = by_id(after, p)
+    out = np.array(before.up, order="F", copy=True)
+    for isp in range(p.nsp):
+        for jj in range(p.ny):
+            n = before.np2[jj, isp]
+            ids = before.up[5, :n, jj, isp].view(np.int64)
+            for k in range(n):
+                out[:5, k, jj, isp] = m[(isp, int(ids[k]))]
+    # undo the periodic wrap so that positions are continuous with the old ones
+    for dim, L in ((0, p.nx), (1, p.ny)):
+        d = out[dim] - before.up[dim]
+        out[dim] -= np.round(d / L) * L
+    return out
+
+
+def test_migration_bookkeeping_many_steps(gpu_lib):
+    """Thirty steps of a hot plasma on a 64 x 48 grid (4 x 3 tiles): count and ID set
+    conserved, every particle inside the cell its bucket says, cumcnt consistent."""
+    p = small_plasma(nx=64, ny=48, ppc=6, seed=12, u_the=0.3, drift=0.5)
+    g = make(p, "mixed", gpu_lib)
+    st = load_weibel2d(p)
+    g.put_state(st)
+    ids0 = np.sort(np.concatenate([st.up[5, :st.np2[jj, s], jj, s].view(np.int64)
+                                   for s in range(p.nsp) for jj in range(p.ny)]))
+    g.step(30)
+    out = g.get_state()
+    ids = np.sort(np.concatenate([out.up[5, :out.np2[jj, s], jj, s].view(np.int64)
+                                  for s in range(p.nsp) for jj in range(p.ny)]))
+    np.testing.assert_array_equal(ids, ids0)
+    for s in range(p.nsp):
+        for jj in range(p.ny):
+            n = out.np2[jj, s]
+            x = out.up[0, :n, jj, s]
+            y = out.up[1, :n, jj, s]
+            cell = np.floor(x).astype(int) - p.nxgs
+            assert (np.floor(y).astype(int) == p.nygs + jj).all()
+            assert (np.diff(cell) >= 0).all()
+            np.testing.assert_array_equal(out.cumcnt[:, jj, s],
+                                          np.concatenate([[0], np.cumsum(np.bincount(cell, minlength=p.nx))]))
+
+
+def test_device_loader_matches_fp64_loader(gpu_lib):
+    """The mixed and FP64 device loaders draw the same plasma (same Philox counters)."""
+    p = small_plasma(nx=32, ny=32, ppc=4, seed=77)
+    gm, gd = make(p, "mixed", gpu_lib), make(p, "fp64", gpu_lib)
+    gm.load_weibel()
+    gd.load_weibel()
+    a, b = gm.get_state(), gd.get_state()
+    pa, pb = by_id(a, p), by_id(b, p)
+    assert pa.keys() == pb.keys()
+    xa = np.array([pa[k] for k in sorted(pa)])
+    xb = np.array([pb[k] for k in sorted(pb)])
+    np.testing.assert_allclose(xa, xb, rtol=2 ** -23, atol=2 ** -22)
+    np.testing.assert_allclose(gm.energy(), gd.energy(), rtol=1e-6)
+
+
+def test_reconnection_walls_mixed(gpu_lib):
+    """Conducting walls in x: after 20 steps every particle is still between the walls."""
+    p = small_plasma(nx=32, ny=32, ppc=6, seed=5, bc="reconnection", u_the=0.3)
+    st = load_weibel2d(p)
+    g = make(p, "mixed", gpu_lib)
+    g.put_state(st)
+    g.step(20)
+    out = g.get_state()
+    assert out.np2.sum() == st.np2.sum()
+    for s in range(p.nsp):
+        for jj in range(p.ny):
+            x = out.up[0, :out.np2[jj, s], jj, s]
+            assert (x >= p.nxgs + 1 - 1e-6).all() and (x <= p.nxge - 1 + 1e-6).all()

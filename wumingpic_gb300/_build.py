@@ -31,6 +31,8 @@ CUDA_UNITS = {
     "kernels_fast.cu": [],
     "kernels_exact.cu": ["-fmad=false"],
     "kernels_common.cu": [],
+    "mixed2d.cu": [],
+    "probe.cu": [],
 }
 
 

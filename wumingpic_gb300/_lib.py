@@ -26,6 +26,7 @@ BC_PERIODIC = 0
 BC_RECONNECTION = 1
 FP64 = 0
 FP64_EXACT = 1
+MIXED = 2
 
 
 class WpicParams(ctypes.Structure):
@@ -78,10 +79,17 @@ def lib():
         L.wpic_num_stages.argtypes = []
         L.wpic_num_particles.argtypes = [vp]
         L.wpic_num_particles.restype = ll
+        L.wpic_measure_fma_peak.argtypes = [i, vp]
         L.wpic_status_string.argtypes = [i]
         L.wpic_status_string.restype = ctypes.c_char_p
         _lib = L
     return _lib
+
+
+def fma_peak_gflops(fp64=True):
+    out = ctypes.c_double()
+    check(lib().wpic_measure_fma_peak(1 if fp64 else 0, ctypes.byref(out)), "fma peak")
+    return out.value
 
 
 def status_string(status):

@@ -39,6 +39,8 @@ struct wpic_ctx {
   double stage_ms[SG_COUNT] = {};
   long long stage_launches[SG_COUNT] = {};
   int sticky_status = WPIC_OK;
+  bool mixed = false;
+  alignas(128) unsigned char tmap[128];  // CUtensorMap of uf (mixed path TMA loads)
 };
 
 namespace {
@@ -221,7 +223,33 @@ void do_migrate_sort(wpic_ctx* c) {
   stage_end(c, SG_SORT, 2);
 }
 
+int mixed_step(wpic_ctx* c) {
+  Dev2D& d = c->d;
+  stage_begin(c, SG_PUSH);
+  mix_push_deposit2d(d, c->tmap, c->stream);
+  stage_end(c, SG_PUSH, 1);
+  stage_begin(c, SG_JREDUCE);
+  mix_curre_refresh2d(d, c->stream);
+  stage_end(c, SG_JREDUCE, d.ph.bc == BC_PERIODIC ? 2 : 1);
+  stage_begin(c, SG_FIELD);
+  fast::gkl2d(d, c->stream);
+  stage_end(c, SG_FIELD, 1);
+  int st = do_cg(c);
+  if (st) return st;
+  stage_begin(c, SG_FIELD);
+  dfield_ghost2d(d, c->stream);
+  fast::efield2d(d, c->stream);
+  dfield_ghost2d(d, c->stream);
+  uf_add2d(d, c->stream);
+  stage_end(c, SG_FIELD, 6);
+  stage_begin(c, SG_PBC);
+  mix_migrate2d(d, c->stream);
+  stage_end(c, SG_PBC, 2);
+  return WPIC_OK;
+}
+
 int one_step(wpic_ctx* c) {
+  if (c->mixed) return mixed_step(c);
   do_push(c);
   if (c->d.ph.bc == BC_RECONNECTION) do_particle_x(c);
   int st = do_field(c);
@@ -243,9 +271,12 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
   if (p->nys != p->nygs || p->nye != p->nyge) return WPIC_BAD_ARGUMENT;  // one device holds the whole domain
   if (!(p->delx > 0) || !(p->delt > 0) || !(p->c > 0)) return WPIC_BAD_ARGUMENT;
   if (p->bc_kind != WPIC_BC_PERIODIC && p->bc_kind != WPIC_BC_RECONNECTION) return WPIC_BAD_ARGUMENT;
-  if (p->precision != WPIC_FP64 && p->precision != WPIC_FP64_EXACT) return WPIC_BAD_ARGUMENT;
+  if (p->precision != WPIC_FP64 && p->precision != WPIC_FP64_EXACT && p->precision != WPIC_MIXED)
+    return WPIC_BAD_ARGUMENT;
+  if (p->precision == WPIC_MIXED && (nx % MIX_TS != 0 || ny % MIX_TS != 0)) return WPIC_BAD_ARGUMENT;
   wpic_ctx* c = new wpic_ctx();
   c->prm = *p;
+  c->mixed = p->precision == WPIC_MIXED;
   Dev2D& d = c->d;
   d.g.nx = nx;
   d.g.ny = ny;
@@ -292,11 +323,35 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
     }
     c->own_stream = true;
   }
-  const size_t slots = (size_t)d.nrowjob * d.cap;
+  const size_t slots = c->mixed ? 0 : (size_t)d.nrowjob * d.cap;
   const size_t ncell = d.g.ncell, fplane = d.g.fplane;
+  d.mixed = c->mixed ? 1 : 0;
   do {
-    if ((st = alloc_parts(c, &d.A, slots))) break;
-    if ((st = alloc_parts(c, &d.B, slots))) break;
+    if (c->mixed) {
+      Mix2D& m = d.m;
+      m.ntx = nx / MIX_TS;
+      m.nty = ny / MIX_TS;
+      m.ntile = m.ntx * m.nty;
+      m.nbin = m.ntile * p->nsp;
+      m.bcap = (int)(((long long)p->np * MIX_TC + nx - 1) / nx);
+      m.lcap = m.bcap / 4 > 256 ? m.bcap / 4 : 256;
+      const size_t nb = (size_t)m.nbin * m.bcap, nl = (size_t)m.nbin * m.lcap;
+      if ((st = dalloc(c, &m.P.cell, nb)) || (st = dalloc(c, &m.P.ox, nb)) || (st = dalloc(c, &m.P.oy, nb)) ||
+          (st = dalloc(c, &m.P.ux, nb)) || (st = dalloc(c, &m.P.uy, nb)) || (st = dalloc(c, &m.P.uz, nb)) ||
+          (st = dalloc(c, &m.P.id, nb)))
+        break;
+      if ((st = dalloc(c, &m.L.cell, nl)) || (st = dalloc(c, &m.L.ox, nl)) || (st = dalloc(c, &m.L.oy, nl)) ||
+          (st = dalloc(c, &m.L.ux, nl)) || (st = dalloc(c, &m.L.uy, nl)) || (st = dalloc(c, &m.L.uz, nl)) ||
+          (st = dalloc(c, &m.L.id, nl)))
+        break;
+      if ((st = dalloc(c, &m.cnt, m.nbin)) || (st = dalloc(c, &m.lcnt, (size_t)m.nbin * 9)) ||
+          (st = dalloc(c, &m.lofs, (size_t)m.nbin * 9)) || (st = dalloc(c, &m.holes, nl)) ||
+          (st = dalloc(c, &m.tails, nl)) || (st = dalloc(c, &m.cellcnt, (size_t)d.nrowjob * nx)))
+        break;
+    } else {
+      if ((st = alloc_parts(c, &d.A, slots))) break;
+      if ((st = alloc_parts(c, &d.B, slots))) break;
+    }
     if ((st = dalloc(c, &d.cc, (size_t)d.nrowjob * (nx + 1)))) break;
     if ((st = dalloc(c, &d.np2, d.nrowjob))) break;
     if ((st = dalloc(c, &d.np2new, d.nrowjob))) break;
@@ -306,7 +361,7 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
     if ((st = dalloc(c, &d.df, 6 * fplane))) break;
     if ((st = dalloc(c, &d.uj, 3 * fplane))) break;
     if ((st = dalloc(c, &d.gkl, 3 * ncell))) break;
-    if ((st = dalloc(c, &d.cellJ, 75 * ncell))) break;
+    if (!c->mixed && (st = dalloc(c, &d.cellJ, 75 * ncell))) break;
     if ((st = dalloc(c, &d.phi, 3 * ncell))) break;
     if ((st = dalloc(c, &d.p, 3 * ncell))) break;
     if ((st = dalloc(c, &d.r, 3 * ncell))) break;
@@ -316,12 +371,17 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
     if ((st = dalloc(c, &d.cg, 3))) break;
     if ((st = dalloc(c, &d.err, 1))) break;
     if ((st = dalloc(c, &d.red_out, 8))) break;
-    if ((st = dalloc(c, &d.mig, slots))) break;
-    if ((st = dalloc(c, &d.ulist, slots))) break;
-    if ((st = dalloc(c, &d.dlist, slots))) break;
-    if ((st = dalloc(c, &d.tlist, slots))) break;
-    if ((st = dalloc(c, &d.slist, slots))) break;
-    if ((st = dalloc(c, &d.map, slots))) break;
+    if (!c->mixed) {
+      if ((st = dalloc(c, &d.mig, slots))) break;
+      if ((st = dalloc(c, &d.ulist, slots))) break;
+      if ((st = dalloc(c, &d.dlist, slots))) break;
+      if ((st = dalloc(c, &d.tlist, slots))) break;
+      if ((st = dalloc(c, &d.slist, slots))) break;
+      if ((st = dalloc(c, &d.map, slots))) break;
+    } else if (mix_make_tensor_map(d, c->tmap) != 0) {
+      st = WPIC_CUDA_ERROR;
+      break;
+    }
     if (cudaMallocHost(&c->h_cg, 3 * sizeof(CGState)) != cudaSuccess) { st = WPIC_CUDA_ERROR; break; }
     if (cudaMallocHost(&c->h_err, sizeof(int)) != cudaSuccess) { st = WPIC_CUDA_ERROR; break; }
     for (int s = 0; s < SG_COUNT; ++s) {
@@ -368,11 +428,29 @@ int wpic_put_particles(wpic_ctx* c, int which, const double* up, const int* np2,
         if (cc[i + 1] < cc[i]) return WPIC_BAD_ARGUMENT;
     }
   }
+  if (c->mixed && which != 0) return WPIC_BAD_ARGUMENT;
   CK(cudaMemcpyAsync(d.np2, np2, sizeof(int) * d.nrowjob, cudaMemcpyHostToDevice, c->stream));
   if (which == 0)
     CK(cudaMemcpyAsync(d.cc, cumcnt, sizeof(int) * (size_t)d.nrowjob * (nx + 1), cudaMemcpyHostToDevice,
                        c->stream));
   const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
+  if (c->mixed) {
+    // stage whole tile rows (16 bucket rows) of one species at a time
+    size_t trows = ((size_t)1 << 30) / (row_bytes * MIX_TS);
+    if (trows < 1) trows = 1;
+    if (trows > (size_t)d.m.nty) trows = d.m.nty;
+    int st = ensure_staging(c, trows * MIX_TS * row_bytes);
+    if (st) return st;
+    for (int isp = 0; isp < c->prm.nsp; ++isp)
+      for (int ty0 = 0; ty0 < d.m.nty; ty0 += (int)trows) {
+        const int nt = (int)((size_t)(d.m.nty - ty0) < trows ? d.m.nty - ty0 : trows);
+        const size_t r0 = (size_t)isp * d.g.ny + (size_t)ty0 * MIX_TS;
+        CK(cudaMemcpyAsync(c->staging, up + r0 * ndim * nph, (size_t)nt * MIX_TS * row_bytes,
+                           cudaMemcpyHostToDevice, c->stream));
+        mix_put2d(d, c->staging, ndim, nph, isp, ty0, nt, c->stream);
+      }
+    return finish(c);
+  }
   size_t rows_per = ((size_t)1 << 30) / row_bytes;
   if (rows_per < 1) rows_per = 1;
   if (rows_per > (size_t)d.nrowjob) rows_per = d.nrowjob;
@@ -393,6 +471,30 @@ int wpic_get_particles(wpic_ctx* c, int which, double* up, int* np2, int* cumcnt
   if (!up || (which != 0 && which != 1)) return WPIC_BAD_ARGUMENT;
   Dev2D& d = c->d;
   const int nx = d.g.nx, ndim = c->prm.ndim, nph = c->prm.np;
+  if (c->mixed) {
+    if (which != 0) return WPIC_BAD_ARGUMENT;
+    mix_count_rows2d(d, c->stream);
+    if (np2) CK(cudaMemcpyAsync(np2, d.np2, sizeof(int) * d.nrowjob, cudaMemcpyDeviceToHost, c->stream));
+    if (cumcnt)
+      CK(cudaMemcpyAsync(cumcnt, d.cc, sizeof(int) * (size_t)d.nrowjob * (nx + 1), cudaMemcpyDeviceToHost,
+                         c->stream));
+    const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
+    size_t trows = ((size_t)1 << 30) / (row_bytes * MIX_TS);
+    if (trows < 1) trows = 1;
+    if (trows > (size_t)d.m.nty) trows = d.m.nty;
+    int st = ensure_staging(c, trows * MIX_TS * row_bytes);
+    if (st) return st;
+    for (int isp = 0; isp < c->prm.nsp; ++isp)
+      for (int ty0 = 0; ty0 < d.m.nty; ty0 += (int)trows) {
+        const int nt = (int)((size_t)(d.m.nty - ty0) < trows ? d.m.nty - ty0 : trows);
+        const size_t r0 = (size_t)isp * d.g.ny + (size_t)ty0 * MIX_TS;
+        CK(cudaMemsetAsync(c->staging, 0, (size_t)nt * MIX_TS * row_bytes, c->stream));
+        mix_get2d(d, c->staging, ndim, nph, isp, ty0, nt, c->stream);
+        CK(cudaMemcpyAsync(up + r0 * ndim * nph, c->staging, (size_t)nt * MIX_TS * row_bytes,
+                           cudaMemcpyDeviceToHost, c->stream));
+      }
+    return finish(c);
+  }
   if (np2) CK(cudaMemcpyAsync(np2, d.np2, sizeof(int) * d.nrowjob, cudaMemcpyDeviceToHost, c->stream));
   if (cumcnt && which == 0)
     CK(cudaMemcpyAsync(cumcnt, d.cc, sizeof(int) * (size_t)d.nrowjob * (nx + 1), cudaMemcpyDeviceToHost,
@@ -443,12 +545,14 @@ int wpic_get_uj(wpic_ctx* c, double* uj) { return c ? get_field(c, uj, c->d.uj, 
 
 int wpic_particle_solv(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;
   do_push(c);
   return finish(c);
 }
 
 int wpic_field_fdtd_i(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;
   int st = do_field(c);
   int st2 = finish(c);
   return st ? st : st2;
@@ -456,18 +560,21 @@ int wpic_field_fdtd_i(wpic_ctx* c) {
 
 int wpic_ele_cur(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;
   do_ele_cur(c);
   return finish(c);
 }
 
 int wpic_bc_particle_x(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;
   do_particle_x(c);
   return finish(c);
 }
 
 int wpic_bc_particle_y(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;
   int st = ensure_C(c);
   if (st) return st;
   Dev2D& d = c->d;
@@ -485,6 +592,7 @@ int wpic_bc_particle_y(wpic_ctx* c) {
 
 int wpic_sort_bucket(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;
   Dev2D& d = c->d;
   stage_begin(c, SG_SORT);
   sort_rank2d(d, d.B, nullptr, c->stream);
@@ -507,7 +615,8 @@ int wpic_step(wpic_ctx* c, int nsteps) {
 int wpic_energy(wpic_ctx* c, double* out) {
   if (!c) return WPIC_NOT_INITIALISED;
   if (!out) return WPIC_BAD_ARGUMENT;
-  FP(energy2d, c->d, c->stream);
+  if (c->mixed) mix_energy2d(c->d, c->stream);
+  else FP(energy2d, c->d, c->stream);
   double h[4];
   CK(cudaMemcpyAsync(h, c->d.red_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   int st = finish(c);
@@ -537,8 +646,14 @@ int wpic_load_weibel_2d(wpic_ctx* c, int ppc, uint64_t seed, double drift, int d
                         double u_the, const double* b0) {
   if (!c) return WPIC_NOT_INITIALISED;
   Dev2D& d = c->d;
-  if (ppc < 1 || (long long)ppc * d.g.nx > d.cap || drift_axis < 0 || drift_axis > 2) return WPIC_BAD_ARGUMENT;
-  load_weibel2d_ppc(d, ppc, seed, drift, drift_axis, u_thi, u_the, c->stream);
+  if (drift_axis < 0 || drift_axis > 2 || ppc < 1) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) {
+    if ((long long)ppc * MIX_TC > d.m.bcap) return WPIC_CAPACITY;
+    mix_load_weibel2d(d, ppc, seed, drift, drift_axis, u_thi, u_the, c->stream);
+  } else {
+    if ((long long)ppc * d.g.nx > d.cap) return WPIC_CAPACITY;
+    load_weibel2d_ppc(d, ppc, seed, drift, drift_axis, u_thi, u_the, c->stream);
+  }
   const size_t fplane = d.g.fplane;
   CK(cudaMemsetAsync(d.uf, 0, 6 * fplane * sizeof(double), c->stream));
   CK(cudaMemsetAsync(d.df, 0, 6 * fplane * sizeof(double), c->stream));
@@ -590,8 +705,10 @@ int wpic_synchronize(wpic_ctx* c) {
 
 long long wpic_num_particles(wpic_ctx* c) {
   if (!c) return -1;
-  std::vector<int> h(c->d.nrowjob);
-  if (cudaMemcpyAsync(h.data(), c->d.np2, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, c->stream) !=
+  const bool mx = c->mixed;
+  std::vector<int> h(mx ? c->d.m.nbin : c->d.nrowjob);
+  if (cudaMemcpyAsync(h.data(), mx ? c->d.m.cnt : c->d.np2, sizeof(int) * h.size(), cudaMemcpyDeviceToHost,
+                      c->stream) !=
       cudaSuccess)
     return -1;
   cudaStreamSynchronize(c->stream);

@@ -620,10 +620,13 @@ __global__ void __launch_bounds__(CG_THREADS) k_energy_fin(Dev2D d) {
   }
 }
 
+// partial slots [l][k][2]: l = 0,1 species kinetic (slot 0); l = 2 fields
 void energy2d(const Dev2D& d, cudaStream_t s) {
-  // partial slots [l][k][2]: l = 0,1 species kinetic (slot 0); l = 2 fields
   cudaMemsetAsync(d.partials, 0, sizeof(double) * 2 * 3 * (size_t)d.nred, s);
   k_energy_parts<<<dim3(d.nred, d.ph.nsp), CG_THREADS, 0, s>>>(d);
+  energy_fields_fin2d(d, s);
+}
+void energy_fields_fin2d(const Dev2D& d, cudaStream_t s) {
   k_energy_fields<<<d.nred, CG_THREADS, 0, s>>>(d);
   k_energy_fin<<<1, CG_THREADS, 0, s>>>(d);
 }

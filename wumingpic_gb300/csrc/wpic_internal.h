@@ -60,6 +60,34 @@ struct Parts64 {
   long long* id;
 };
 
+// ---- mixed-precision particle storage (2D) ----
+// Particles live in bins of one 16 x 16-cell tile and one species, bin = tile * nsp + isp,
+// tile = ty * ntx + tx.  Position = integer cell (local index ly*16+lx inside the tile)
+// plus an FP32 offset in [0, 1) per dimension; momenta FP32; 64-bit id.  Inside a bin the
+// order is interleaved over cells, so that the lanes of a warp rarely share a cell.
+constexpr int MIX_TS = 16;
+constexpr int MIX_TC = MIX_TS * MIX_TS;
+
+struct PartsMix {
+  int* cell;  // < 256: local cell; >= 256: leaver, (dir+1)*256 + local cell in the destination tile
+  float *ox, *oy, *ux, *uy, *uz;
+  long long* id;
+};
+
+struct Mix2D {
+  int ntx, nty, ntile, nbin;
+  int bcap;          // slots per bin
+  int lcap;          // leaver slots per bin
+  PartsMix P;        // [nbin][bcap]
+  PartsMix L;        // [nbin][lcap] leavers grouped by direction
+  int* cnt;          // [nbin]
+  int* lcnt;         // [nbin][9] leavers per direction (index 4 unused)
+  int* lofs;         // [nbin][9] offset of each direction's group inside the bin's leaver region
+  int* holes;        // [nbin][lcap] slots vacated by leavers, ascending
+  int* tails;        // [nbin][lcap] scratch for the tail compaction
+  int* cellcnt;      // [nsp][ny][nx] per-cell counts (reference-layout export)
+};
+
 struct CGState {
   double sum_g, eps, sumr_g, sum2_g, sum1_g, av, bv;
   int ite, active, fixed, pad;
@@ -87,6 +115,8 @@ struct Dev2D {
   int *nup, *ndown, *np2new;                 // per row job
   int* err;              // device error word
   double* red_out;       // misc reduction output (energy)
+  int mixed;             // 1: particles in the mixed-precision bins below
+  Mix2D m;
 };
 
 // ---- launchers: precision-dependent kernels exist in two builds ----
@@ -100,7 +130,8 @@ struct Dev2D {
   void cg_iter_p2d(const Dev2D& d, cudaStream_t s);                                        \
   void cg_store2d(const Dev2D& d, cudaStream_t s);                                         \
   void efield2d(const Dev2D& d, cudaStream_t s);                                           \
-  void energy2d(const Dev2D& d, cudaStream_t s);
+  void energy2d(const Dev2D& d, cudaStream_t s);                                           \
+  void energy_fields_fin2d(const Dev2D& d, cudaStream_t s);
 
 namespace exact { WPIC_DECLARE_FP_LAUNCHERS }
 namespace fast { WPIC_DECLARE_FP_LAUNCHERS }
@@ -121,6 +152,18 @@ void soa_to_aos2d(const Dev2D& d, double* aos, int ndim, int np_host, int row0, 
                   cudaStream_t s);
 void field_ref_to_soa(const double* ref, double* soa, int ncomp, int nslab, cudaStream_t s);
 void field_soa_to_ref(const double* soa, double* ref, int ncomp, int nslab, cudaStream_t s);
+// ---- mixed-precision path (mixed2d.cu) ----
+int mix_make_tensor_map(const Dev2D& d, void* tmap_out);  // CUtensorMap of uf for the TMA tile loads
+void mix_push_deposit2d(const Dev2D& d, const void* tmap, cudaStream_t s);
+void mix_curre_refresh2d(const Dev2D& d, cudaStream_t s);
+void mix_migrate2d(const Dev2D& d, cudaStream_t s);
+void mix_put2d(const Dev2D& d, const double* aos, int ndim, int np_host, int isp, int ty0, int nty, cudaStream_t s);
+void mix_count_rows2d(const Dev2D& d, cudaStream_t s);
+void mix_get2d(const Dev2D& d, double* aos, int ndim, int np_host, int isp, int ty0, int nty, cudaStream_t s);
+void mix_load_weibel2d(const Dev2D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
+                       double u_thi, double u_the, cudaStream_t s);
+void mix_energy2d(const Dev2D& d, cudaStream_t s);
+
 void load_weibel2d_ppc(const Dev2D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
                        double u_thi, double u_the, cudaStream_t s);
 

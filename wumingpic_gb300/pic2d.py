@@ -33,7 +33,7 @@ class Pic2D:
         prm.q[0], prm.q[1] = q[0], q[1]
         prm.r[0], prm.r[1] = r[0], r[1]
         prm.bc_kind = _lib.BC_PERIODIC if plasma.bc == "periodic" else _lib.BC_RECONNECTION
-        prm.precision = {"fp64": _lib.FP64, "fp64_exact": _lib.FP64_EXACT}[precision]
+        prm.precision = {"fp64": _lib.FP64, "fp64_exact": _lib.FP64_EXACT, "mixed": _lib.MIXED}[precision]
         prm.device_cap = int(device_cap)
         self.precision = precision
         h = ctypes.c_void_p()
@@ -65,7 +65,8 @@ class Pic2D:
             st = empty_state2d(self.p)
         check(lib().wpic_get_particles(self._h, 0, _ptr(st.up, np.float64), _ptr(st.np2, np.int32),
                                        _ptr(st.cumcnt, np.int32)), "get up")
-        check(lib().wpic_get_particles(self._h, 1, _ptr(st.gp, np.float64), None, None), "get gp")
+        if self.precision != "mixed":
+            check(lib().wpic_get_particles(self._h, 1, _ptr(st.gp, np.float64), None, None), "get gp")
         check(lib().wpic_get_fields(self._h, _ptr(st.uf, np.float64)), "get uf")
         return st
 
