@@ -26,6 +26,7 @@
 #ifndef WUMINGPIC_GB300_H
 #define WUMINGPIC_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -140,6 +141,11 @@ int wpic_num_stages(void);
 /* FMA throughput of the device in GFLOP/s (fp64 != 0: FP64, else FP32), measured by a
  * register-only kernel; the compute roof the FP64 kernels are reported against. */
 int wpic_measure_fma_peak(int fp64, double* gflops);
+
+/* Page-lock (and release) a caller's host array, e.g. the reference-layout up/uf arrays,
+ * so that wpic_put_* / wpic_get_* copy at full host-link bandwidth. */
+int wpic_host_register(void* ptr, size_t bytes);
+int wpic_host_unregister(void* ptr);
 
 int wpic_synchronize(wpic_ctx* ctx);
 long long wpic_num_particles(wpic_ctx* ctx);

@@ -80,6 +80,8 @@ def lib():
         L.wpic_num_particles.argtypes = [vp]
         L.wpic_num_particles.restype = ll
         L.wpic_measure_fma_peak.argtypes = [i, vp]
+        L.wpic_host_register.argtypes = [vp, ctypes.c_size_t]
+        L.wpic_host_unregister.argtypes = [vp]
         L.wpic_status_string.argtypes = [i]
         L.wpic_status_string.restype = ctypes.c_char_p
         _lib = L
@@ -90,6 +92,15 @@ def fma_peak_gflops(fp64=True):
     out = ctypes.c_double()
     check(lib().wpic_measure_fma_peak(1 if fp64 else 0, ctypes.byref(out)), "fma peak")
     return out.value
+
+
+def host_register(arr):
+    """Page-lock a numpy array's buffer for fast host<->device copies."""
+    check(lib().wpic_host_register(arr.ctypes.data_as(ctypes.c_void_p), arr.nbytes), "host_register")
+
+
+def host_unregister(arr):
+    check(lib().wpic_host_unregister(arr.ctypes.data_as(ctypes.c_void_p)), "host_unregister")
 
 
 def status_string(status):

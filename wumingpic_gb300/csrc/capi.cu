@@ -698,6 +698,16 @@ int wpic_timing_get(wpic_ctx* c, double* ms, long long* launches, int n) {
 const char* wpic_stage_name(int s) { return (s >= 0 && s < SG_COUNT) ? kStageNames[s] : "?"; }
 int wpic_num_stages(void) { return SG_COUNT; }
 
+int wpic_host_register(void* ptr, size_t bytes) {
+  if (!ptr || !bytes) return WPIC_BAD_ARGUMENT;
+  return cuda_status(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+}
+
+int wpic_host_unregister(void* ptr) {
+  if (!ptr) return WPIC_BAD_ARGUMENT;
+  return cuda_status(cudaHostUnregister(ptr));
+}
+
 int wpic_synchronize(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
   return finish(c);

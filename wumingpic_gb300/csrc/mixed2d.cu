@@ -24,6 +24,7 @@ namespace wpic {
 namespace {
 
 constexpr int MP_THREADS = 256;
+constexpr int MP_ROUND = 4;  // particles per thread between folds of the FP32 tile into FP64
 constexpr int TW = MIX_TS + 4;   // staged field nodes per tile edge (cells -2 .. 17)
 constexpr int TT = MIX_TS + 2;   // cell-centred values per tile edge (cells -1 .. 16)
 constexpr unsigned long long kSpinLimit = 1ull << 22;  // a few seconds at most
@@ -98,7 +99,8 @@ int mix_make_tensor_map(const Dev2D& d, void* out) {
 __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_constant__ CUtensorMap tm) {
   __shared__ __align__(128) double suf[6][TW][TW];
   __shared__ __align__(16) float stmp[TT * TT][8];
-  __shared__ float sJ[3][TW][TW];
+  __shared__ float sJ[3][TW][TW];     // FP32 current of the particles of one round
+  __shared__ double sJ64[3][TW][TW];  // FP64 sum over rounds
   __shared__ __align__(8) unsigned long long bar;
   const Mix2D& m = d.m;
   const int tile = blockIdx.x;
@@ -112,7 +114,10 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
     mbar_expect_tx(&bar, (unsigned)sizeof(suf));
     tma_load_3d(&suf[0][0][0], &tm, tx * MIX_TS, ty * MIX_TS, 0, &bar);
   }
-  for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) (&sJ[0][0][0])[k] = 0.f;
+  for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) {
+    (&sJ[0][0][0])[k] = 0.f;
+    (&sJ64[0][0][0])[k] = 0.0;
+  }
   if (!mbar_wait_bounded(&bar)) {
     atomicOr(d.err, EB_OUT_OF_RANGE);
     mbar_wait_bounded(&bar);  // second bounded wait for the copy in flight
@@ -147,7 +152,10 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
     const float fac2 = (float)(d.ph.q[isp] * d.ph.delt / d.ph.r[isp]);
     const float qdd = (float)(d.ph.q[isp] * d.ph.delx * d.ph.d_delt);
     const float qs = (float)d.ph.q[isp];
-    for (int s = threadIdx.x; s < n; s += MP_THREADS) {
+    for (int s0 = 0; s0 < n; s0 += MP_THREADS * MP_ROUND) {
+    for (int rr = 0; rr < MP_ROUND; ++rr) {
+      const int s = s0 + rr * MP_THREADS + threadIdx.x;
+      if (s >= n) break;
       const size_t k = base + s;
       const int cl = m.P.cell[k];
       const int lx = cl & (MIX_TS - 1), ly = cl >> 4;
@@ -281,19 +289,29 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
       m.P.uy[k] = uy;
       m.P.uz[k] = uz;
     }
+    // fold the round's FP32 sums into the FP64 tile: each FP32 sum has few terms
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) {
+      const float v = (&sJ[0][0][0])[k];
+      if (v != 0.f) {
+        (&sJ64[0][0][0])[k] += (double)v;
+        (&sJ[0][0][0])[k] = 0.f;
+      }
+    }
+    __syncthreads();
+    }
   }
-  __syncthreads();
-  // one flush of the FP32 tile into FP64 global J; nodes wrap periodically in y, and in x unless walls
+  // one flush of the tile into FP64 global J; nodes wrap periodically in y, and in x unless walls
   for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) {
-    const float v = (&sJ[0][0][0])[k];
-    if (v == 0.f) continue;
+    const double v = (&sJ64[0][0][0])[k];
+    if (v == 0.0) continue;
     const int comp = k / (TW * TW), r = (k / TW) % TW, cc = k % TW;
     int gx = tx * MIX_TS + cc - 2, gy = ty * MIX_TS + r - 2;
     if (gy < 0) gy += g.ny; else if (gy >= g.ny) gy -= g.ny;
     if (!walls) {
       if (gx < 0) gx += g.nx; else if (gx >= g.nx) gx -= g.nx;
     }
-    atomicAdd(&d.uj[(size_t)comp * g.fplane + (size_t)(gy + 2) * g.fp + gx + 2], (double)v);
+    atomicAdd(&d.uj[(size_t)comp * g.fplane + (size_t)(gy + 2) * g.fp + gx + 2], v);
   }
 }
 
