@@ -298,20 +298,21 @@ constexpr int CG_THREADS = 256;
 
 // phi(cx, cy) of component l with the boundary_*__phi ghost rules applied by
 // index arithmetic (periodic y; periodic or conducting-wall x).
+// The sign flip is an integer flag so that no FP64 compare is issued.
 __device__ __forceinline__ double phi_at(const double* v, const Grid2D& g, int bc, int l, int cx, int cy) {
   if (cy < 0) cy += g.ny; else if (cy >= g.ny) cy -= g.ny;
-  double sgn = 1.0;
+  bool neg = false;
   if (cx < 0) {
     if (bc == BC_PERIODIC) cx += g.nx;
-    else if (l == 0) { cx = 0; sgn = -1.0; }
+    else if (l == 0) { cx = 0; neg = true; }
     else cx = 1;
   } else if (cx >= g.nx) {
     if (bc == BC_PERIODIC) cx -= g.nx;
-    else if (l == 0) { cx = g.nx - 3; sgn = -1.0; }
+    else if (l == 0) { cx = g.nx - 3; neg = true; }
     else cx = g.nx - 2;
   }
   const double val = v[(size_t)cy * g.nx + cx];
-  return sgn < 0.0 ? -val : val;
+  return neg ? -val : val;
 }
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -340,14 +341,14 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_init(Dev2D d) {
     const double* db = d.df + (size_t)l * g.fplane + 2 * (size_t)g.fp + 2;
     auto ph = [&](int x, int y) {
       if (y < 0) y += g.ny; else if (y >= g.ny) y -= g.ny;
-      double sgn = 1.0;
+      bool neg = false;
       if (x < 0) {
-        if (d.ph.bc == BC_PERIODIC) x += g.nx; else if (l == 0) { x = 0; sgn = -1.0; } else x = 1;
+        if (d.ph.bc == BC_PERIODIC) x += g.nx; else if (l == 0) { x = 0; neg = true; } else x = 1;
       } else if (x >= g.nx) {
-        if (d.ph.bc == BC_PERIODIC) x -= g.nx; else if (l == 0) { x = g.nx - 3; sgn = -1.0; } else x = g.nx - 2;
+        if (d.ph.bc == BC_PERIODIC) x -= g.nx; else if (l == 0) { x = g.nx - 3; neg = true; } else x = g.nx - 2;
       }
       const double v = db[(size_t)y * g.fp + x];
-      return sgn < 0.0 ? -v : v;
+      return neg ? -v : v;
     };
     const double pc = ph(cx, cy);
     const double b = f5 * d.gkl[off + c];
@@ -395,7 +396,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_init_fin(Dev2D d) {
   }
 }
 
-// ap = (f4 - N) p ; partials of r.r and p.ap
+// ap = (f4 - N) p ; partial of p.ap.  The reference also sums r.r here (field.f90:403);
+// r has not changed since the previous iteration's r.r (or the initial one), which was
+// reduced in this same deterministic order, so that sum is carried instead of recomputed.
 __global__ void __launch_bounds__(CG_THREADS) k_cg_ap(Dev2D d) {
   __shared__ double sh[CG_THREADS];
   const Grid2D g = d.g;
@@ -405,21 +408,18 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_ap(Dev2D d) {
   const double f4 = d.ph.f4;
   const double* p = d.p + off;
   const int bc = d.ph.bc;
-  double sr = 0.0, s2 = 0.0;
+  double s2 = 0.0;
   for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS) {
     const int cy = c / g.nx, cx = c - cy * g.nx;
     const double pc = p[c];
     const double ap = -phi_at(p, g, bc, l, cx, cy - 1) - phi_at(p, g, bc, l, cx - 1, cy) + f4 * pc
                       - phi_at(p, g, bc, l, cx + 1, cy) - phi_at(p, g, bc, l, cx, cy + 1);
     d.ap[off + c] = ap;
-    const double r = d.r[off + c];
-    sr = sr + r * r;
     s2 = s2 + pc * ap;
   }
-  sr = block_sum(sr, sh);
   s2 = block_sum(s2, sh);
   if (threadIdx.x == 0) {
-    d.partials[((size_t)l * d.nred + blockIdx.x) * 2 + 0] = sr;
+    d.partials[((size_t)l * d.nred + blockIdx.x) * 2 + 0] = 0.0;
     d.partials[((size_t)l * d.nred + blockIdx.x) * 2 + 1] = s2;
   }
 }
@@ -428,13 +428,12 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_ap_fin(Dev2D d) {
   __shared__ double sh[CG_THREADS];
   const int l = blockIdx.x;
   if (!d.cg[l].active) return;
-  double sr, s2;
-  final_sums(d, l, sh, &sr, &s2);
+  double dummy, s2;
+  final_sums(d, l, sh, &dummy, &s2);
   if (threadIdx.x == 0) {
     CGState& st = d.cg[l];
-    st.sumr_g = sr;
     st.sum2_g = s2;
-    st.av = sr / s2;
+    st.av = st.sumr_g / s2;  // sumr_g: r.r of the current r (initial sum or the last sum1)
   }
 }
 
@@ -472,6 +471,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_update_fin(Dev2D d) {
     st.ite = st.ite + 1;
     st.sum1_g = s1;
     st.bv = s1 / st.sumr_g;
+    st.sumr_g = s1;  // r.r of the updated r: the next iteration's sumr
     bool cont = st.fixed >= 0 ? (st.ite < st.fixed) : (st.sum_g > st.eps);
     if (st.fixed < 0 && st.ite >= d.ite_max) {  // reference: write + stop (field.f90:427-430)
       atomicOr(d.err, EB_CG);

@@ -27,6 +27,10 @@ constexpr int MP_THREADS = 256;
 constexpr int MP_ROUND = 4;  // particles per thread between folds of the FP32 tile into FP64
 constexpr int TW = MIX_TS + 4;   // staged field nodes per tile edge (cells -2 .. 17)
 constexpr int TT = MIX_TS + 2;   // cell-centred values per tile edge (cells -1 .. 16)
+// Row pitch of the FP32 current tile.  The lanes of a warp sit in two consecutive cell rows
+// (bins are filled round-robin over the 256 cells); a pitch of 16 (mod 32) words puts the
+// two rows on disjoint banks, so the deposit atomics of such a warp are conflict-free.
+constexpr int JP = 48;
 constexpr unsigned long long kSpinLimit = 1ull << 22;  // a few seconds at most
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -70,6 +74,34 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar) {
 }
 
 __device__ __forceinline__ int dir_dx(int d) { return d % 3 - 1; }
+
+// s1 - s0 of the quadratic spline on the 4-node window of the deposit, in factored form.
+// o = old offset in the old cell, p = new offset in the new cell, inc = new cell - old cell.
+// Written as products of small exact-ish factors (differences of offsets, distances to the
+// cell faces) instead of differences of O(1) spline values, so each entry keeps FP32
+// relative accuracy for small displacements: Esirkepov's charge conservation then holds to
+// ~1e-7 relative in FP32.  Window: offsets -1..2 (inc >= 0) or -2..1 (inc < 0).
+__device__ __forceinline__ void shape_diff(float o, float p, int inc, float ds[4]) {
+  if (inc == 0) {
+    const float dl = p - o;
+    ds[0] = -0.5f * dl * (2.f - o - p);
+    ds[1] = -dl * (o + p - 1.f);
+    ds[2] = 0.5f * dl * (o + p);
+    ds[3] = 0.f;
+  } else if (inc > 0) {
+    const float q = 1.f - o;
+    ds[0] = -0.5f * q * q;
+    ds[1] = -p * (1.f - 0.5f * p) - o * q;
+    ds[2] = p * (1.f - p) + 0.5f * q * (1.f + o);
+    ds[3] = 0.5f * p * p;
+  } else {
+    const float q = 1.f - p;
+    ds[0] = 0.5f * q * q;
+    ds[1] = p * q + o * (1.f - 0.5f * o);
+    ds[2] = -0.5f * q * (1.f + p) - o * (1.f - o);
+    ds[3] = -0.5f * o * o;
+  }
+}
 __device__ __forceinline__ int dir_dy(int d) { return d / 3 - 1; }
 
 }  // namespace
@@ -98,8 +130,8 @@ int mix_make_tensor_map(const Dev2D& d, void* out) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_constant__ CUtensorMap tm) {
   __shared__ __align__(128) double suf[6][TW][TW];
-  __shared__ __align__(16) float stmp[TT * TT][8];
-  __shared__ float sJ[3][TW][TW];     // FP32 current of the particles of one round
+  __shared__ __align__(16) float2 stmp[3][TT * TT];  // (Bx,By), (Bz,Ex), (Ey,Ez) at cell centres
+  __shared__ float sJ[3][TW][JP];     // FP32 current of the particles of one round
   __shared__ double sJ64[3][TW][TW];  // FP64 sum over rounds
   __shared__ __align__(8) unsigned long long bar;
   const Mix2D& m = d.m;
@@ -114,10 +146,8 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
     mbar_expect_tx(&bar, (unsigned)sizeof(suf));
     tma_load_3d(&suf[0][0][0], &tm, tx * MIX_TS, ty * MIX_TS, 0, &bar);
   }
-  for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) {
-    (&sJ[0][0][0])[k] = 0.f;
-    (&sJ64[0][0][0])[k] = 0.0;
-  }
+  for (int k = threadIdx.x; k < 3 * TW * JP; k += MP_THREADS) (&sJ[0][0][0])[k] = 0.f;
+  for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) (&sJ64[0][0][0])[k] = 0.0;
   if (!mbar_wait_bounded(&bar)) {
     atomicOr(d.err, EB_OUT_OF_RANGE);
     mbar_wait_bounded(&bar);  // second bounded wait for the copy in flight
@@ -126,15 +156,11 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
   // cell-centred fields for local cells -1..16 (2d/common/particle.f90:70-83), FP64 sums rounded to FP32
   for (int k = threadIdx.x; k < TT * TT; k += MP_THREADS) {
     const int r = k / TT + 1, c = k % TT + 1;  // staged node of local cell (c-2, r-2) ... origin at cell -2
-    float* o = stmp[k];
-    o[0] = (float)(0.5 * (suf[0][r][c] + suf[0][r + 1][c]));
-    o[1] = (float)(0.5 * (suf[1][r][c] + suf[1][r][c + 1]));
-    o[2] = (float)(0.25 * (suf[2][r][c] + suf[2][r][c + 1] + suf[2][r + 1][c] + suf[2][r + 1][c + 1]));
-    o[3] = (float)(0.5 * (suf[3][r][c] + suf[3][r][c + 1]));
-    o[4] = (float)(0.5 * (suf[4][r][c] + suf[4][r + 1][c]));
-    o[5] = (float)suf[5][r][c];
-    o[6] = 0.f;
-    o[7] = 0.f;
+    stmp[0][k] = make_float2((float)(0.5 * (suf[0][r][c] + suf[0][r + 1][c])),
+                             (float)(0.5 * (suf[1][r][c] + suf[1][r][c + 1])));
+    stmp[1][k] = make_float2((float)(0.25 * (suf[2][r][c] + suf[2][r][c + 1] + suf[2][r + 1][c] + suf[2][r + 1][c + 1])),
+                             (float)(0.5 * (suf[3][r][c] + suf[3][r][c + 1])));
+    stmp[2][k] = make_float2((float)(0.5 * (suf[4][r][c] + suf[4][r + 1][c])), (float)suf[5][r][c]);
   }
   __syncthreads();
 
@@ -172,14 +198,14 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
 #pragma unroll
         for (int jx = 0; jx < 3; ++jx) {
           const float wx = jx == 0 ? sx0 : (jx == 1 ? sx1 : sx2);
-          const float4 a = *reinterpret_cast<const float4*>(&stmp[(ly + jy) * TT + lx + jx][0]);
-          const float2 b = *reinterpret_cast<const float2*>(&stmp[(ly + jy) * TT + lx + jx][4]);
+          const int ci = (ly + jy) * TT + lx + jx;
+          const float2 a = stmp[0][ci], b = stmp[1][ci], e = stmp[2][ci];
           fr[0] = fmaf(wx, a.x, fr[0]);
           fr[1] = fmaf(wx, a.y, fr[1]);
-          fr[2] = fmaf(wx, a.z, fr[2]);
-          fr[3] = fmaf(wx, a.w, fr[3]);
-          fr[4] = fmaf(wx, b.x, fr[4]);
-          fr[5] = fmaf(wx, b.y, fr[5]);
+          fr[2] = fmaf(wx, b.x, fr[2]);
+          fr[3] = fmaf(wx, b.y, fr[3]);
+          fr[4] = fmaf(wx, e.x, fr[4]);
+          fr[5] = fmaf(wx, e.y, fr[5]);
         }
 #pragma unroll
         for (int q = 0; q < 6; ++q) f[q] = fmaf(wy, fr[q], f[q]);
@@ -187,10 +213,11 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
       const float bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
       // Buneman-Boris (2d/common/particle.f90:133-155)
       float u1 = ux + fac1 * epx, u2 = uy + fac1 * epy, u3 = uz + fac1 * epz;
-      const float gm = sqrtf(c * c + u1 * u1 + u2 * u2 + u3 * u3);
-      const float igam = 1.f / gm;
+      const float g2 = c * c + u1 * u1 + u2 * u2 + u3 * u3;
+      const float igam = rsqrtf(g2);
+      const float gm = g2 * igam;
       const float fac1r = fac1 * igam;
-      const float fac2r = fac2 / (gm + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
+      const float fac2r = __fdividef(fac2, gm + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
       const float u4 = u1 + fac1r * (u2 * bpz - u3 * bpy);
       const float u5 = u2 + fac1r * (u3 * bpx - u1 * bpz);
       const float u6 = u3 + fac1r * (u1 * bpy - u2 * bpx);
@@ -233,15 +260,11 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
       // ---- Esirkepov deposition on 4-wide windows (2d/common/field.f90:223-298) ----
       // window origin (node index space 0..4 = offsets -2..2): 0 if the particle moved to -1, else 1
       const int xa = incx < 0 ? 0 : 1, ya = incy < 0 ? 0 : 1;
-      const float a1x = 0.5f * (1.f - nx_) * (1.f - nx_), b1x = 0.75f - (nx_ - 0.5f) * (nx_ - 0.5f), c1x = 0.5f * nx_ * nx_;
-      const float a1y = 0.5f * (1.f - ny_) * (1.f - ny_), b1y = 0.75f - (ny_ - 0.5f) * (ny_ - 0.5f), c1y = 0.5f * ny_ * ny_;
       float s0x[4], s0y[4], dsx[4], dsy[4];
       s0x[0] = incx < 0 ? 0.f : sx0; s0x[1] = incx < 0 ? sx0 : sx1; s0x[2] = incx < 0 ? sx1 : sx2; s0x[3] = incx < 0 ? sx2 : 0.f;
       s0y[0] = incy < 0 ? 0.f : sy0; s0y[1] = incy < 0 ? sy0 : sy1; s0y[2] = incy < 0 ? sy1 : sy2; s0y[3] = incy < 0 ? sy2 : 0.f;
-      dsx[0] = (incx > 0 ? 0.f : a1x) - s0x[0]; dsx[1] = (incx > 0 ? a1x : b1x) - s0x[1];
-      dsx[2] = (incx > 0 ? b1x : c1x) - s0x[2]; dsx[3] = (incx > 0 ? c1x : 0.f) - s0x[3];
-      dsy[0] = (incy > 0 ? 0.f : a1y) - s0y[0]; dsy[1] = (incy > 0 ? a1y : b1y) - s0y[1];
-      dsy[2] = (incy > 0 ? b1y : c1y) - s0y[2]; dsy[3] = (incy > 0 ? c1y : 0.f) - s0y[3];
+      shape_diff(ox, nx_, incx, dsx);
+      shape_diff(oy, ny_, incy, dsy);
       const float gvz = uz * ig;
       const float qg = qs * gvz;
       float wy[4], wx[4], vy[4];
@@ -292,10 +315,11 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
     // fold the round's FP32 sums into the FP64 tile: each FP32 sum has few terms
     __syncthreads();
     for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) {
-      const float v = (&sJ[0][0][0])[k];
+      float* f = &sJ[0][0][0] + (k / TW) * JP + k % TW;
+      const float v = *f;
       if (v != 0.f) {
         (&sJ64[0][0][0])[k] += (double)v;
-        (&sJ[0][0][0])[k] = 0.f;
+        *f = 0.f;
       }
     }
     __syncthreads();
@@ -365,74 +389,87 @@ __global__ void __launch_bounds__(MG_THREADS) k_mix_mig1(Dev2D d) {
   const int bin = blockIdx.x;
   const int n = m.cnt[bin];
   const size_t base = (size_t)bin * m.bcap, lbase = (size_t)bin * m.lcap;
-  __shared__ int cnt9[9], off9[9], run9[10];
-  __shared__ int wcnt[MG_WARPS][10];
+  // each warp owns a contiguous segment of the bin: count, then write in slot order
+  __shared__ int wc[MG_WARPS][10];   // per warp: leavers per direction, [9] = all leavers
+  __shared__ int wo[MG_WARPS][10];   // per warp: first output position per direction / hole list
+  __shared__ int off9[9];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x < 9) cnt9[threadIdx.x] = 0;
+  const int seg = ((n + MG_WARPS - 1) / MG_WARPS + 31) & ~31;
+  const int s_lo = min(n, warp * seg), s_hi = min(n, s_lo + seg);
+  const unsigned lt = lanemask_lt();
+  int cnt[10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q) cnt[q] = 0;
+  for (int s0 = s_lo; s0 < s_hi; s0 += 32) {
+    const int s = s0 + lane;
+    const int code = s < s_hi ? m.P.cell[base + s] : 0;
+    const int q = code >= MIX_TC ? code / MIX_TC - 1 : -1;
+    const unsigned any = __ballot_sync(0xffffffffu, q >= 0);
+    if (!any) continue;
+    cnt[9] += __popc(any);
+#pragma unroll
+    for (int dd = 0; dd < 9; ++dd) cnt[dd] += __popc(__ballot_sync(0xffffffffu, q == dd));
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < 10; ++q) wc[warp][q] = cnt[q];
+  }
   __syncthreads();
-  for (int s = threadIdx.x; s < n; s += MG_THREADS) {
-    const int code = m.P.cell[base + s];
-    if (code >= MIX_TC) atomicAdd(&cnt9[code / MIX_TC - 1], 1);
+  if (threadIdx.x < 10) {
+    const int q = threadIdx.x;
+    int acc = 0;
+    for (int w = 0; w < MG_WARPS; ++w) {
+      wo[w][q] = acc;
+      acc += wc[w][q];
+    }
+    if (q < 9) {
+      m.lcnt[bin * 9 + q] = acc;
+      off9[q] = acc;  // totals, turned into offsets below
+    } else if (acc > m.lcap) {
+      atomicOr(d.err, EB_CAPACITY);
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     int acc = 0;
     for (int q = 0; q < 9; ++q) {
+      const int t = off9[q];
       off9[q] = acc;
-      acc += cnt9[q];
-      m.lcnt[bin * 9 + q] = cnt9[q];
-      m.lofs[bin * 9 + q] = off9[q];
-      run9[q] = 0;
+      m.lofs[bin * 9 + q] = acc;
+      acc += t;
     }
-    run9[9] = 0;  // holes
-    if (acc > m.lcap) atomicOr(d.err, EB_CAPACITY);
   }
   __syncthreads();
-  const unsigned lt = lanemask_lt();
-  for (int s0 = 0; s0 < n; s0 += MG_THREADS) {
-    const int s = s0 + threadIdx.x;
-    const int code = s < n ? m.P.cell[base + s] : 0;
+  int run[10];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) run[q] = off9[q] + wo[warp][q];
+  run[9] = wo[warp][9];
+  for (int s0 = s_lo; s0 < s_hi; s0 += 32) {
+    const int s = s0 + lane;
+    const int code = s < s_hi ? m.P.cell[base + s] : 0;
     const int q = code >= MIX_TC ? code / MIX_TC - 1 : -1;
-    // per-warp counts for the 9 directions and the hole list (index 9)
-    int myrank = 0, hrank = 0;
+    const unsigned any = __ballot_sync(0xffffffffu, q >= 0);
+    if (!any) continue;
+    int lpos = 0;
 #pragma unroll
     for (int dd = 0; dd < 9; ++dd) {
       const unsigned b = __ballot_sync(0xffffffffu, q == dd);
-      if (q == dd) myrank = __popc(b & lt);
-      if (lane == 0) wcnt[warp][dd] = __popc(b);
+      if (q == dd) lpos = run[dd] + __popc(b & lt);
+      run[dd] += __popc(b);
     }
-    const unsigned bh = __ballot_sync(0xffffffffu, q >= 0);
-    hrank = __popc(bh & lt);
-    if (lane == 0) wcnt[warp][9] = __popc(bh);
-    __syncthreads();
-    if (q >= 0) {
-      int pos = run9[q], hpos = run9[9];
-      for (int w = 0; w < warp; ++w) {
-        pos += wcnt[w][q];
-        hpos += wcnt[w][9];
-      }
-      pos += myrank;
-      hpos += hrank;
-      const int lpos = off9[q] + pos;
-      if (lpos < m.lcap && hpos < m.lcap) {
-        const size_t k = base + s, l = lbase + lpos;
-        m.L.cell[l] = code % MIX_TC;
-        m.L.ox[l] = m.P.ox[k];
-        m.L.oy[l] = m.P.oy[k];
-        m.L.ux[l] = m.P.ux[k];
-        m.L.uy[l] = m.P.uy[k];
-        m.L.uz[l] = m.P.uz[k];
-        m.L.id[l] = m.P.id[k];
-        m.holes[lbase + hpos] = s;
-      }
+    const int hpos = run[9] + __popc(any & lt);
+    run[9] += __popc(any);
+    if (q >= 0 && lpos < m.lcap && hpos < m.lcap) {
+      const size_t k = base + s, l = lbase + lpos;
+      m.L.cell[l] = code % MIX_TC;
+      m.L.ox[l] = m.P.ox[k];
+      m.L.oy[l] = m.P.oy[k];
+      m.L.ux[l] = m.P.ux[k];
+      m.L.uy[l] = m.P.uy[k];
+      m.L.uz[l] = m.P.uz[k];
+      m.L.id[l] = m.P.id[k];
+      m.holes[lbase + hpos] = s;
     }
-    __syncthreads();
-    if (threadIdx.x < 10) {
-      int add = 0;
-      for (int w = 0; w < MG_WARPS; ++w) add += wcnt[w][threadIdx.x];
-      run9[threadIdx.x] += add;
-    }
-    __syncthreads();
   }
 }
 
