@@ -163,3 +163,20 @@ def test_reconnection_walls_mixed(gpu_lib):
         for jj in range(p.ny):
             x = out.up[0, :out.np2[jj, s], jj, s]
             assert (x >= p.nxgs + 1 - 1e-6).all() and (x <= p.nxge - 1 + 1e-6).all()
+
+
+def test_mixed_path_is_bitwise_reproducible(gpu_lib):
+    """Integer (fixed-point) current sums, deterministic reductions and deterministic
+    migration: two runs from the same state agree bit for bit."""
+    p, st = small_case(nx=32, ny=32, ppc=8, seed=23)
+    outs = []
+    for _ in range(2):
+        g = make(p, "mixed", gpu_lib)
+        g.put_state(st)
+        g.step(5)
+        outs.append((g.get_state(), g.energy()))
+    (a, ea), (b, eb) = outs
+    np.testing.assert_array_equal(a.np2, b.np2)
+    np.testing.assert_array_equal(a.up.view(np.int64), b.up.view(np.int64))
+    np.testing.assert_array_equal(a.uf.view(np.int64), b.uf.view(np.int64))
+    np.testing.assert_array_equal(ea, eb)

@@ -230,7 +230,7 @@ int mixed_step(wpic_ctx* c) {
   stage_end(c, SG_PUSH, 1);
   stage_begin(c, SG_JREDUCE);
   mix_curre_refresh2d(d, c->stream);
-  stage_end(c, SG_JREDUCE, d.ph.bc == BC_PERIODIC ? 2 : 1);
+  stage_end(c, SG_JREDUCE, d.ph.bc == BC_PERIODIC ? 3 : 2);
   stage_begin(c, SG_FIELD);
   fast::gkl2d(d, c->stream);
   stage_end(c, SG_FIELD, 1);
@@ -335,6 +335,26 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
       m.nbin = m.ntile * p->nsp;
       m.bcap = (int)(((long long)p->np * MIX_TC + nx - 1) / nx);
       m.lcap = m.bcap / 4 > 256 ? m.bcap / 4 : 256;
+      // fixed-point scales of the deposit: every contribution is bounded by
+      // vmax = max(|q| dx/dt, 2 |q| c); a tile pass adds at most nsp * bcap of them to a node.
+      double vmax = 0.0;
+      for (int k = 0; k < p->nsp; ++k) {
+        const double a = std::fabs(p->q[k]) * p->delx / p->delt, b = 2.0 * std::fabs(p->q[k]) * p->c;
+        vmax = std::fmax(vmax, std::fmax(a, b));
+      }
+      double s1 = std::ldexp(1.0, 21) / std::fmax(vmax, 1e-30);  // |v s1| < 2^21: magic-number rounding exact
+      const double lim = std::ldexp(1.0, 30) / ((double)p->nsp * m.bcap * std::fmax(vmax, 1e-30));
+      if (lim < s1) s1 = lim;
+      s1 = std::ldexp(1.0, (int)std::floor(std::log2(s1)));
+      // lo plane: each contribution |lo| <= 2^14, at most nsp * bcap of them per node
+      if (!(s1 >= 1.0) || s1 > std::ldexp(1.0, 60) || (double)p->nsp * m.bcap * 16384.0 >= std::ldexp(1.0, 31)) {
+        st = WPIC_BAD_ARGUMENT;
+        break;
+      }
+      m.fx_s1 = (float)s1;
+      m.fx_s2 = (float)(s1 * 32768.0);
+      m.fx_is1 = 1.0 / s1;
+      m.fx_is2 = 1.0 / (s1 * 32768.0);
       const size_t nb = (size_t)m.nbin * m.bcap, nl = (size_t)m.nbin * m.lcap;
       if ((st = dalloc(c, &m.P.cell, nb)) || (st = dalloc(c, &m.P.ox, nb)) || (st = dalloc(c, &m.P.oy, nb)) ||
           (st = dalloc(c, &m.P.ux, nb)) || (st = dalloc(c, &m.P.uy, nb)) || (st = dalloc(c, &m.P.uz, nb)) ||
@@ -346,7 +366,8 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
         break;
       if ((st = dalloc(c, &m.cnt, m.nbin)) || (st = dalloc(c, &m.lcnt, (size_t)m.nbin * 9)) ||
           (st = dalloc(c, &m.lofs, (size_t)m.nbin * 9)) || (st = dalloc(c, &m.holes, nl)) ||
-          (st = dalloc(c, &m.tails, nl)) || (st = dalloc(c, &m.cellcnt, (size_t)d.nrowjob * nx)))
+          (st = dalloc(c, &m.tails, nl)) || (st = dalloc(c, &m.cellcnt, (size_t)d.nrowjob * nx)) ||
+          (st = dalloc(c, &m.ujx, 3 * (size_t)(nx + 4) * (ny + 4))))
         break;
     } else {
       if ((st = alloc_parts(c, &d.A, slots))) break;

@@ -24,7 +24,6 @@ namespace wpic {
 namespace {
 
 constexpr int MP_THREADS = 256;
-constexpr int MP_ROUND = 4;  // particles per thread between folds of the FP32 tile into FP64
 constexpr int TW = MIX_TS + 4;   // staged field nodes per tile edge (cells -2 .. 17)
 constexpr int TT = MIX_TS + 2;   // cell-centred values per tile edge (cells -1 .. 16)
 // Row pitch of the FP32 current tile.  The lanes of a warp sit in two consecutive cell rows
@@ -74,6 +73,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar) {
 }
 
 __device__ __forceinline__ int dir_dx(int d) { return d % 3 - 1; }
+__device__ __forceinline__ int dir_dy(int d) { return d / 3 - 1; }
 
 // s1 - s0 of the quadratic spline on the 4-node window of the deposit, in factored form.
 // o = old offset in the old cell, p = new offset in the new cell, inc = new cell - old cell.
@@ -82,27 +82,19 @@ __device__ __forceinline__ int dir_dx(int d) { return d % 3 - 1; }
 // relative accuracy for small displacements: Esirkepov's charge conservation then holds to
 // ~1e-7 relative in FP32.  Window: offsets -1..2 (inc >= 0) or -2..1 (inc < 0).
 __device__ __forceinline__ void shape_diff(float o, float p, int inc, float ds[4]) {
-  if (inc == 0) {
-    const float dl = p - o;
-    ds[0] = -0.5f * dl * (2.f - o - p);
-    ds[1] = -dl * (o + p - 1.f);
-    ds[2] = 0.5f * dl * (o + p);
-    ds[3] = 0.f;
-  } else if (inc > 0) {
-    const float q = 1.f - o;
-    ds[0] = -0.5f * q * q;
-    ds[1] = -p * (1.f - 0.5f * p) - o * q;
-    ds[2] = p * (1.f - p) + 0.5f * q * (1.f + o);
-    ds[3] = 0.5f * p * p;
-  } else {
-    const float q = 1.f - p;
-    ds[0] = 0.5f * q * q;
-    ds[1] = p * q + o * (1.f - 0.5f * o);
-    ds[2] = -0.5f * q * (1.f + p) - o * (1.f - o);
-    ds[3] = -0.5f * o * o;
-  }
+  // the three cases are evaluated and selected, so the warp does not diverge
+  const float dl = p - o, sp = o + p;
+  const float z0 = -0.5f * dl * (2.f - sp), z1 = -dl * (sp - 1.f), z2 = 0.5f * dl * sp;
+  const float qo = 1.f - o, qp = 1.f - p;
+  const float a0 = -0.5f * qo * qo, a1 = -p * (1.f - 0.5f * p) - o * qo, a2 = p * qp + 0.5f * qo * (1.f + o),
+              a3 = 0.5f * p * p;
+  const float b0 = 0.5f * qp * qp, b1 = p * qp + o * (1.f - 0.5f * o), b2 = -0.5f * qp * (1.f + p) - o * qo,
+              b3 = -0.5f * o * o;
+  ds[0] = inc == 0 ? z0 : (inc > 0 ? a0 : b0);
+  ds[1] = inc == 0 ? z1 : (inc > 0 ? a1 : b1);
+  ds[2] = inc == 0 ? z2 : (inc > 0 ? a2 : b2);
+  ds[3] = inc == 0 ? 0.f : (inc > 0 ? a3 : b3);
 }
-__device__ __forceinline__ int dir_dy(int d) { return d / 3 - 1; }
 
 }  // namespace
 
@@ -128,11 +120,29 @@ int mix_make_tensor_map(const Dev2D& d, void* out) {
 // ---------------------------------------------------------------------------
 // fused push + deposit, one CTA per tile
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_constant__ CUtensorMap tm) {
-  __shared__ __align__(128) double suf[6][TW][TW];
+// Two-plane fixed-point split of an FP32 contribution v: hi = round(v s1), lo = round((v - hi/s1) s2),
+// with s2 = 2^15 s1.  Rounding by the magic-number addition (1.5 * 2^23): exact for |v s1| < 2^22,
+// and v - hi/s1 is exact (Sterbenz), so hi/s1 + lo/s2 equals v to within 1/(2 s2).  Both planes are
+// summed with native 32-bit shared-memory integer atomics: exact, hence order independent.
+__device__ __forceinline__ void fx_add(int* hi, int* lo, float v, float s1, float is1, float s2) {
+  const float M = 12582912.0f;  // 1.5 * 2^23
+  const float t = fmaf(v, s1, M);
+  const float hf = t - M;
+  const float r = fmaf(-hf, is1, v);
+  const float u = fmaf(r, s2, M);
+  atomicAdd(hi, __float_as_int(t) - 0x4B400000);
+  atomicAdd(lo, __float_as_int(u) - 0x4B400000);
+}
+
+__global__ void __launch_bounds__(MP_THREADS, 4) k_mix_push(Dev2D d, const __grid_constant__ CUtensorMap tm) {
+  // the TMA staging of uf is dead once the cell-centred values exist; its bytes then hold the
+  // fixed-point current planes of the tile
+  __shared__ __align__(128) unsigned char sbuf[(6 * TW * TW * 8 > 2 * 3 * TW * JP * 4) ? 6 * TW * TW * 8
+                                                                                     : 2 * 3 * TW * JP * 4];
+  double(*suf)[TW][TW] = reinterpret_cast<double(*)[TW][TW]>(sbuf);
+  int(*jhi)[TW][JP] = reinterpret_cast<int(*)[TW][JP]>(sbuf);
+  int(*jlo)[TW][JP] = reinterpret_cast<int(*)[TW][JP]>(sbuf + 3 * TW * JP * 4);
   __shared__ __align__(16) float2 stmp[3][TT * TT];  // (Bx,By), (Bz,Ex), (Ey,Ez) at cell centres
-  __shared__ float sJ[3][TW][JP];     // FP32 current of the particles of one round
-  __shared__ double sJ64[3][TW][TW];  // FP64 sum over rounds
   __shared__ __align__(8) unsigned long long bar;
   const Mix2D& m = d.m;
   const int tile = blockIdx.x;
@@ -143,11 +153,9 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    mbar_expect_tx(&bar, (unsigned)sizeof(suf));
+    mbar_expect_tx(&bar, (unsigned)(6 * TW * TW * sizeof(double)));
     tma_load_3d(&suf[0][0][0], &tm, tx * MIX_TS, ty * MIX_TS, 0, &bar);
   }
-  for (int k = threadIdx.x; k < 3 * TW * JP; k += MP_THREADS) (&sJ[0][0][0])[k] = 0.f;
-  for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) (&sJ64[0][0][0])[k] = 0.0;
   if (!mbar_wait_bounded(&bar)) {
     atomicOr(d.err, EB_OUT_OF_RANGE);
     mbar_wait_bounded(&bar);  // second bounded wait for the copy in flight
@@ -163,6 +171,9 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
     stmp[2][k] = make_float2((float)(0.5 * (suf[4][r][c] + suf[4][r + 1][c])), (float)suf[5][r][c]);
   }
   __syncthreads();
+  for (int k = threadIdx.x; k < 2 * 3 * TW * JP; k += MP_THREADS) (&jhi[0][0][0])[k] = 0;
+  __syncthreads();
+  const float fs1 = m.fx_s1, fs2 = m.fx_s2, fis1 = 1.0f / m.fx_s1;
 
   const float dtdx = (float)(d.ph.delt * d.ph.d_delx);
   const float c = (float)d.ph.c;
@@ -178,10 +189,7 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
     const float fac2 = (float)(d.ph.q[isp] * d.ph.delt / d.ph.r[isp]);
     const float qdd = (float)(d.ph.q[isp] * d.ph.delx * d.ph.d_delt);
     const float qs = (float)d.ph.q[isp];
-    for (int s0 = 0; s0 < n; s0 += MP_THREADS * MP_ROUND) {
-    for (int rr = 0; rr < MP_ROUND; ++rr) {
-      const int s = s0 + rr * MP_THREADS + threadIdx.x;
-      if (s >= n) break;
+    for (int s = threadIdx.x; s < n; s += MP_THREADS) {
       const size_t k = base + s;
       const int cl = m.P.cell[k];
       const int lx = cl & (MIX_TS - 1), ly = cl >> 4;
@@ -276,16 +284,16 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
       }
       const int nx0 = lx + xa, ny0 = ly + ya;  // sJ index of window node 0 (sJ origin = local cell -2)
       float px = 0.f, py = 0.f;
+      const int b0 = ny0 * JP + nx0;  // word offset of window node (0, 0) in a plane
 #pragma unroll
       for (int t = 0; t < 3; ++t) {
         px += dsx[t];
         py += dsy[t];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-          const float jx = px * wy[v];
-          if (jx != 0.f) atomicAdd(&sJ[0][ny0 + v][nx0 + t + 1], jx);
-          const float jy = py * wx[v];
-          if (jy != 0.f) atomicAdd(&sJ[1][ny0 + t + 1][nx0 + v], jy);
+          const int ox_ = b0 + v * JP + t + 1, oy_ = b0 + (t + 1) * JP + v;
+          fx_add(&jhi[0][0][0] + ox_, &jlo[0][0][0] + ox_, px * wy[v], fs1, fis1, fs2);
+          fx_add(&jhi[1][0][0] + oy_, &jlo[1][0][0] + oy_, py * wx[v], fs1, fis1, fs2);
         }
       }
 #pragma unroll
@@ -293,8 +301,8 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
         const float zy = qg * (s0y[v] + 0.5f * dsy[v]);
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
-          const float jz = s0x[t] * zy + dsx[t] * vy[v];
-          if (jz != 0.f) atomicAdd(&sJ[2][ny0 + v][nx0 + t], jz);
+          const int oz_ = b0 + v * JP + t;
+          fx_add(&jhi[2][0][0] + oz_, &jlo[2][0][0] + oz_, s0x[t] * zy + dsx[t] * vy[v], fs1, fis1, fs2);
         }
       }
       // ---- new cell, tile and bin code ----
@@ -312,35 +320,28 @@ __global__ void __launch_bounds__(MP_THREADS) k_mix_push(Dev2D d, const __grid_c
       m.P.uy[k] = uy;
       m.P.uz[k] = uz;
     }
-    // fold the round's FP32 sums into the FP64 tile: each FP32 sum has few terms
-    __syncthreads();
-    for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) {
-      float* f = &sJ[0][0][0] + (k / TW) * JP + k % TW;
-      const float v = *f;
-      if (v != 0.f) {
-        (&sJ64[0][0][0])[k] += (double)v;
-        *f = 0.f;
-      }
-    }
-    __syncthreads();
-    }
   }
-  // one flush of the tile into FP64 global J; nodes wrap periodically in y, and in x unless walls
+  __syncthreads();
+  // one flush of the tile into the global fixed-point current (exact 64-bit integer sums, so the
+  // result does not depend on the order of the tiles); nodes wrap periodically in y, and in x
+  // unless walls
   for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) {
-    const double v = (&sJ64[0][0][0])[k];
-    if (v == 0.0) continue;
+    const int w = (k / TW) * JP + k % TW;
+    const int ih = (&jhi[0][0][0])[w], il = (&jlo[0][0][0])[w];
+    if ((ih | il) == 0) continue;
+    const long long v = (long long)ih * 32768LL + (long long)il;
     const int comp = k / (TW * TW), r = (k / TW) % TW, cc = k % TW;
     int gx = tx * MIX_TS + cc - 2, gy = ty * MIX_TS + r - 2;
     if (gy < 0) gy += g.ny; else if (gy >= g.ny) gy -= g.ny;
     if (!walls) {
       if (gx < 0) gx += g.nx; else if (gx >= g.nx) gx -= g.nx;
     }
-    atomicAdd(&d.uj[(size_t)comp * g.fplane + (size_t)(gy + 2) * g.fp + gx + 2], v);
+    atomicAdd(&m.ujx[(size_t)comp * g.fplane + (size_t)(gy + 2) * g.fp + gx + 2], (unsigned long long)v);
   }
 }
 
 void mix_push_deposit2d(const Dev2D& d, const void* tmap, cudaStream_t s) {
-  cudaMemsetAsync(d.uj, 0, sizeof(double) * 3 * (size_t)d.g.fplane, s);
+  cudaMemsetAsync(d.m.ujx, 0, sizeof(unsigned long long) * 3 * (size_t)d.g.fplane, s);
   k_mix_push<<<d.m.ntile, MP_THREADS, 0, s>>>(d, *(const CUtensorMap*)tmap);
 }
 
@@ -371,7 +372,16 @@ __global__ void k_mix_refresh_x(Dev2D d) {
     u[nx + 3] = u[3];
   }
 }
+// fixed point -> FP64 current over the whole ghosted extent
+__global__ void k_mix_fix2d(Dev2D d) {
+  const size_t n = (size_t)3 * d.g.fplane;
+  const double is2 = d.m.fx_is2;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    d.uj[k] = (double)(long long)d.m.ujx[k] * is2;
+}
+
 void mix_curre_refresh2d(const Dev2D& d, cudaStream_t s) {
+  k_mix_fix2d<<<4 * 152, 256, 0, s>>>(d);
   k_mix_refresh_y<<<(d.g.nx + 4 + 127) / 128, 128, 0, s>>>(d);
   if (d.ph.bc == BC_PERIODIC) k_mix_refresh_x<<<(d.g.ny + 4 + 127) / 128, 128, 0, s>>>(d);
 }

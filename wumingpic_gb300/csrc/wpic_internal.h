@@ -75,6 +75,9 @@ struct PartsMix {
 };
 
 struct Mix2D {
+  // fixed-point current accumulation of the push: v = hi / s1 + lo / s2 with int32 hi, lo
+  float fx_s1, fx_s2;
+  double fx_is1, fx_is2;
   int ntx, nty, ntile, nbin;
   int bcap;          // slots per bin
   int lcap;          // leaver slots per bin
@@ -86,6 +89,7 @@ struct Mix2D {
   int* holes;        // [nbin][lcap] slots vacated by leavers, ascending
   int* tails;        // [nbin][lcap] scratch for the tail compaction
   int* cellcnt;      // [nsp][ny][nx] per-cell counts (reference-layout export)
+  unsigned long long* ujx;  // [3][ny+4][nx+4] current in fixed point (units 1/fx_s2), summed exactly
 };
 
 struct CGState {
