@@ -325,3 +325,24 @@ def test_device_loader_and_moderate_size_properties(gpu_lib):
                                           np.concatenate([[0], np.cumsum(np.bincount(cell, minlength=p.nx))]))
             yj = np.floor(st.up[1, :n, jj, isp]).astype(int)
             assert (yj == p.nygs + jj).all()
+
+
+def test_exact_step_matches_golden_fixture(gpu_lib):
+    """One exact-build step from the golden fixture's initial state reproduces the
+    fixture's particle state bit for bit (fields 1e-12, CG at the fixture's counts)."""
+    import os
+    from tests.golden.make_golden import CASE
+    from wumingpic_gb300.loader import Plasma2D, State2D
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "weibel2d_small.npz"))
+    p = Plasma2D(**CASE)
+    st = State2D(up=np.asfortranarray(ref["up0"]), gp=np.asfortranarray(ref["up0"]).copy(order="F"),
+                 uf=np.asfortranarray(ref["uf0"]), cumcnt=np.asfortranarray(ref["cumcnt0"]),
+                 np2=np.asfortranarray(ref["np20"]))
+    g = make_gpu(p, "fp64_exact", gpu_lib)
+    g.cg_control(fixed=ref["cg1"])
+    g.put_state(st)
+    g.step(1)
+    out = g.get_state()
+    assert_particles(out.up, out.np2, ref["up1"], ref["np21"])
+    np.testing.assert_array_equal(out.cumcnt, ref["cumcnt1"])
+    assert_field(out.uf, ref["uf1"], REL)

@@ -1,0 +1,282 @@
+! wpic_shim2d.f90 -- drop-in replacements for WumingPIC's 2D hot-path modules
+! (particle, field, sort, boundary_periodic) that forward to the GB300 library
+! through ISO_C_BINDING.  Link these objects instead of the corresponding objects
+! of libwuming2d_common.a; the drivers ({2d}/proj/*/app.f90) stay unchanged.
+!
+! Coherence: the first particle__solv uploads the host state (up, uf, cumcnt;
+! np2 = cumcnt(nxe+1,:,:)).  Afterwards the device state is authoritative; with
+! the default sync interval of 1 the host arrays are refreshed every step (uf at
+! the end of field__fdtd_i, up/np2/cumcnt at the end of sort__bucket) so that
+! the drivers' I/O and diagnostics read current values.  A driver that knows its
+! output interval may call wpic_shim_set_sync(n) to refresh only every n steps.
+!
+! The three boundary routines that field__fdtd_i receives as procedure arguments
+! are accepted and ignored: the library applies the boundary of the kind chosen
+! at init (periodic here).
+module wpic_capi
+  use iso_c_binding
+  implicit none
+
+  type, bind(C) :: wpic_params
+     integer(c_int) :: ndim, np, nsp, nxgs, nxge, nygs, nyge, nys, nye
+     real(c_double) :: delx, delt, c, gfac
+     real(c_double) :: q(2), r(2)
+     integer(c_int) :: bc_kind, precision, device_cap
+  end type wpic_params
+
+  interface
+     integer(c_int) function wpic_init_2d(ctx, p, stream) bind(C, name="wpic_init_2d")
+       import :: c_int, c_ptr, wpic_params
+       type(c_ptr), intent(out) :: ctx
+       type(wpic_params), intent(in) :: p
+       type(c_ptr), value :: stream
+     end function wpic_init_2d
+     integer(c_int) function wpic_put_particles(ctx, which, up, np2, cumcnt) bind(C, name="wpic_put_particles")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: which
+       real(c_double), intent(in) :: up(*)
+       integer(c_int), intent(in) :: np2(*), cumcnt(*)
+     end function wpic_put_particles
+     integer(c_int) function wpic_get_particles(ctx, which, up, np2, cumcnt) bind(C, name="wpic_get_particles")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: which
+       real(c_double), intent(inout) :: up(*)
+       integer(c_int), intent(inout) :: np2(*), cumcnt(*)
+     end function wpic_get_particles
+     integer(c_int) function wpic_put_fields(ctx, uf) bind(C, name="wpic_put_fields")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: uf(*)
+     end function wpic_put_fields
+     integer(c_int) function wpic_get_fields(ctx, uf) bind(C, name="wpic_get_fields")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(inout) :: uf(*)
+     end function wpic_get_fields
+     integer(c_int) function wpic_call(ctx) bind(C)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic_call
+  end interface
+
+  ! one device context per process (one MPI rank holding the whole domain)
+  type(c_ptr), save :: wpic_ctx = c_null_ptr
+  type(wpic_params), save :: wpic_prm
+  logical, save :: wpic_uploaded = .false.
+  integer, save :: wpic_sync_every = 1, wpic_step_count = 0
+
+  procedure(wpic_call), pointer :: p_solv => null(), p_fdtd => null(), p_bcx => null(), &
+       p_bcy => null(), p_sort => null()
+
+contains
+
+  subroutine wpic_check(st, where)
+    integer(c_int), intent(in) :: st
+    character(len=*), intent(in) :: where
+    if (st /= 0) then
+       write(0,*) 'wumingpic_gb300: ', where, ' failed with status ', st
+       stop
+    endif
+  end subroutine wpic_check
+
+  subroutine wpic_shim_set_sync(n)
+    integer, intent(in) :: n
+    wpic_sync_every = max(1, n)
+  end subroutine wpic_shim_set_sync
+
+  subroutine wpic_bind_procedures()
+    interface
+       integer(c_int) function wpic_particle_solv(ctx) bind(C, name="wpic_particle_solv")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx
+       end function
+       integer(c_int) function wpic_field_fdtd_i(ctx) bind(C, name="wpic_field_fdtd_i")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx
+       end function
+       integer(c_int) function wpic_bc_particle_x(ctx) bind(C, name="wpic_bc_particle_x")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx
+       end function
+       integer(c_int) function wpic_bc_particle_y(ctx) bind(C, name="wpic_bc_particle_y")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx
+       end function
+       integer(c_int) function wpic_sort_bucket(ctx) bind(C, name="wpic_sort_bucket")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx
+       end function
+    end interface
+    p_solv => wpic_particle_solv
+    p_fdtd => wpic_field_fdtd_i
+    p_bcx => wpic_bc_particle_x
+    p_bcy => wpic_bc_particle_y
+    p_sort => wpic_sort_bucket
+  end subroutine wpic_bind_procedures
+
+  subroutine wpic_ensure_ctx()
+    if (.not. c_associated(wpic_ctx)) then
+       call wpic_check(wpic_init_2d(wpic_ctx, wpic_prm, c_null_ptr), 'wpic_init_2d')
+       call wpic_bind_procedures()
+    endif
+  end subroutine wpic_ensure_ctx
+
+end module wpic_capi
+
+
+module particle
+  use wpic_capi
+  implicit none
+  private
+  public :: particle__init, particle__solv, particle__solv_vay
+contains
+  subroutine particle__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nys_in,nye_in, &
+                            delx_in,delt_in,c_in,q_in,r_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in, nxgs_in, nxge_in, nygs_in, nyge_in, nys_in, nye_in
+    real(8), intent(in) :: delx_in, delt_in, c_in, q_in(nsp_in), r_in(nsp_in)
+    wpic_prm%ndim = ndim_in; wpic_prm%np = np_in; wpic_prm%nsp = nsp_in
+    wpic_prm%nxgs = nxgs_in; wpic_prm%nxge = nxge_in; wpic_prm%nygs = nygs_in; wpic_prm%nyge = nyge_in
+    wpic_prm%nys = nys_in; wpic_prm%nye = nye_in
+    wpic_prm%delx = delx_in; wpic_prm%delt = delt_in; wpic_prm%c = c_in
+    wpic_prm%q(1:nsp_in) = q_in; wpic_prm%r(1:nsp_in) = r_in
+    wpic_prm%bc_kind = 0; wpic_prm%precision = 0; wpic_prm%device_cap = 0
+  end subroutine particle__init
+
+  subroutine particle__solv(gp,up,uf,cumcnt,nxs,nxe)
+    integer, intent(in)  :: nxs, nxe
+    integer, intent(in)  :: cumcnt(wpic_prm%nxgs:wpic_prm%nxge+1,wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    real(8), intent(in)  :: up(*), uf(*)
+    real(8), intent(out) :: gp(*)
+    integer(c_int) :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    call wpic_ensure_ctx()
+    if (.not. wpic_uploaded) then
+       np2(:,:) = cumcnt(nxe+1,:,:)
+       call wpic_check(wpic_put_particles(wpic_ctx, 0_c_int, up, np2, cumcnt), 'put up')
+       call wpic_check(wpic_put_fields(wpic_ctx, uf), 'put uf')
+       wpic_uploaded = .true.
+    endif
+    call wpic_check(p_solv(wpic_ctx), 'particle__solv')
+  end subroutine particle__solv
+
+  subroutine particle__solv_vay(gp,up,uf,cumcnt,nxs,nxe)
+    integer, intent(in) :: nxs, nxe
+    integer, intent(in) :: cumcnt(*)
+    real(8), intent(in) :: up(*), uf(*)
+    real(8), intent(out) :: gp(*)
+    write(0,*) 'wumingpic_gb300: particle__solv_vay is not provided by the GPU library'
+    stop
+  end subroutine particle__solv_vay
+end module particle
+
+
+module field
+  use wpic_capi
+  implicit none
+  private
+  public :: field__init, field__fdtd_i
+contains
+  subroutine field__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nys_in,nye_in, &
+                         mnpr_in,ncomw_in,opsum_in,nerr_in,delx_in,delt_in,c_in,q_in,r_in,gfac_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in, nxgs_in, nxge_in, nygs_in, nyge_in, nys_in, nye_in
+    integer, intent(in) :: mnpr_in, ncomw_in, opsum_in, nerr_in
+    real(8), intent(in) :: delx_in, delt_in, c_in, q_in(nsp_in), r_in(nsp_in), gfac_in
+    wpic_prm%gfac = gfac_in
+  end subroutine field__init
+
+  subroutine field__fdtd_i(uf,up,gp,cumcnt,nxs,nxe,set_boundary_dfield,set_boundary_curre,set_boundary_phi)
+    integer, intent(in)    :: nxs, nxe
+    integer, intent(in)    :: cumcnt(*)
+    real(8), intent(in)    :: up(*), gp(*)
+    real(8), intent(inout) :: uf(*)
+    external :: set_boundary_dfield, set_boundary_curre, set_boundary_phi
+    call wpic_check(p_fdtd(wpic_ctx), 'field__fdtd_i')
+    if (mod(wpic_step_count + 1, wpic_sync_every) == 0) then
+       call wpic_check(wpic_get_fields(wpic_ctx, uf), 'get uf')
+    endif
+  end subroutine field__fdtd_i
+end module field
+
+
+module sort
+  use wpic_capi
+  implicit none
+  private
+  public :: sort__init, sort__bucket
+contains
+  subroutine sort__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nys_in,nye_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in, nxgs_in, nxge_in, nygs_in, nyge_in, nys_in, nye_in
+  end subroutine sort__init
+
+  ! np2 is intent(in) in the reference; here it is refreshed together with the
+  ! sorted state at the sync points, so it is declared intent(inout)
+  subroutine sort__bucket(gp,up,cumcnt,np2,nxs,nxe)
+    integer, intent(in)    :: nxs, nxe
+    integer, intent(inout) :: np2(wpic_prm%nye-wpic_prm%nys+1, wpic_prm%nsp)
+    integer, intent(out)   :: cumcnt(*)
+    real(8), intent(in)    :: up(*)
+    real(8), intent(out)   :: gp(*)
+    integer(c_int) :: np2_dev(wpic_prm%nye-wpic_prm%nys+1, wpic_prm%nsp)
+    call wpic_check(p_sort(wpic_ctx), 'sort__bucket')
+    wpic_step_count = wpic_step_count + 1
+    if (mod(wpic_step_count, wpic_sync_every) == 0) then
+       ! the sorted state ('gp' dummy = the driver's up) with its np2 and cumcnt
+       call wpic_check(wpic_get_particles(wpic_ctx, 0_c_int, gp, np2_dev, cumcnt), 'get up')
+       np2(:,:) = np2_dev(:,:)
+    endif
+  end subroutine sort__bucket
+end module sort
+
+
+module boundary_periodic
+  use wpic_capi
+  implicit none
+  private
+  public :: boundary_periodic__init, boundary_periodic__dfield, boundary_periodic__particle_x, &
+       boundary_periodic__particle_y, boundary_periodic__curre, boundary_periodic__phi, boundary_periodic__mom
+contains
+  subroutine boundary_periodic__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nys_in,nye_in, &
+                                     nup_in,ndown_in,mnpi_in,mnpr_in,ncomw_in,nerr_in,nstat_in,delx_in,delt_in,c_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in, nxgs_in, nxge_in, nygs_in, nyge_in, nys_in, nye_in
+    integer, intent(in) :: nup_in, ndown_in, mnpi_in, mnpr_in, ncomw_in, nerr_in, nstat_in(:)
+    real(8), intent(in) :: delx_in, delt_in, c_in
+  end subroutine boundary_periodic__init
+
+  subroutine boundary_periodic__particle_x(up,np2)
+    real(8), intent(inout) :: up(*)
+    integer, intent(in)    :: np2(*)
+    call wpic_check(p_bcx(wpic_ctx), 'bc__particle_x')
+  end subroutine boundary_periodic__particle_x
+
+  subroutine boundary_periodic__particle_y(up,np2)
+    real(8), intent(inout) :: up(*)
+    integer, intent(inout) :: np2(*)
+    call wpic_check(p_bcy(wpic_ctx), 'bc__particle_y')
+  end subroutine boundary_periodic__particle_y
+
+  ! applied inside the library; present so that field__fdtd_i's arguments type-check
+  subroutine boundary_periodic__dfield(df,nxs,nxe,nys,nye,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nxgs, nxge
+    real(8), intent(inout) :: df(*)
+  end subroutine boundary_periodic__dfield
+  subroutine boundary_periodic__curre(uj,nxs,nxe,nys,nye,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nxgs, nxge
+    real(8), intent(inout) :: uj(*)
+  end subroutine boundary_periodic__curre
+  subroutine boundary_periodic__phi(phi,nxs,nxe,nys,nye,l)
+    integer, intent(in)    :: nxs, nxe, nys, nye, l
+    real(8), intent(inout) :: phi(*)
+  end subroutine boundary_periodic__phi
+
+  ! moments stay on the host: the one-rank periodic fold of the moment array
+  subroutine boundary_periodic__mom(mom)
+    real(8), intent(inout) :: mom(7, wpic_prm%nxgs-1:wpic_prm%nxge+1, wpic_prm%nys-1:wpic_prm%nye+1, wpic_prm%nsp)
+    integer :: gs, ge, ys, ye
+    gs = wpic_prm%nxgs; ge = wpic_prm%nxge; ys = wpic_prm%nys; ye = wpic_prm%nye
+    mom(:, gs, :, :) = mom(:, gs, :, :) + mom(:, ge+1, :, :)
+    mom(:, ge, :, :) = mom(:, ge, :, :) + mom(:, gs-1, :, :)
+    mom(:, :, ye, :) = mom(:, :, ye, :) + mom(:, :, ys-1, :)
+    mom(:, :, ys, :) = mom(:, :, ys, :) + mom(:, :, ye+1, :)
+  end subroutine boundary_periodic__mom
+end module boundary_periodic
