@@ -147,6 +147,28 @@ int wpic_measure_fma_peak(int fp64, double* gflops);
 int wpic_host_register(void* ptr, size_t bytes);
 int wpic_host_unregister(void* ptr);
 
+/* The energy_history sums of wpic_energy, computed from the caller's own device
+ * arrays without allocating anything.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory where they need the diagnostic:
+ * arrays held on the device by another runtime's allocator (OpenACC or CUDA Fortran
+ * data regions, a framework's pool), a time-step loop where cudaMalloc would
+ * synchronise the device, or a run sized to fill HBM.  up (ndim, np, ny, nsp),
+ * np2 (ny, nsp) and uf (6, nx+4, ny+4) are device pointers in the reference layout;
+ * r holds the nsp masses in host memory; out is a device pointer to nsp+2 doubles,
+ * laid out as in wpic_energy.  Work is queued on stream (NULL: the default stream)
+ * and out is valid once the stream reaches it.
+ *
+ * Scratch: a fixed __device__ array of 3 * WPIC_NOALLOC_MAX_ROWS doubles (192 KiB)
+ * that every GPU loading the library holds until the process exits.  Grids with
+ * ny * nsp > WPIC_NOALLOC_MAX_ROWS are refused with WPIC_BAD_ARGUMENT.  All calls
+ * share the array, so calls that overlap on the GPU race.  The first call on each
+ * device looks up the array's device address; make that first call before any
+ * stream capture. */
+#define WPIC_NOALLOC_MAX_ROWS 8192
+int wpic_energy_noalloc(const double* up, const int* np2, const double* uf, int ndim, int np, int nx, int ny,
+                        int nsp, const double* r, double c, double* out, void* stream);
+
 int wpic_synchronize(wpic_ctx* ctx);
 long long wpic_num_particles(wpic_ctx* ctx);
 const char* wpic_status_string(int status);

@@ -33,6 +33,7 @@ CUDA_UNITS = {
     "kernels_common.cu": [],
     "mixed2d.cu": [],
     "probe.cu": [],
+    "no_alloc.cu": [],
 }
 
 
