@@ -27,12 +27,13 @@ METRIC = "particle-updates/s on 1 GB300: mixed vs FP64 path at <=1% growth-rate 
 UNIT = "particle-updates/s"
 
 # Algorithmic bytes of the dominant kernels (compulsory traffic, one launch):
-#  k_mix_push (mixed push + deposit): per particle read cell (4 B) + x/y offsets (8 B) +
-#    ux, uy, uz (12 B) and write them back = 48 B; the id (8 B) is not touched by the push.
+#  k_mix_push (mixed push + deposit): per particle read the x/y offsets (8 B), ux, uy, uz
+#    (12 B) and the id (8 B), and write them back = 56 B (a particle that changes cell is
+#    written to its new cell's inbox instead, plus a 4-byte order key).
 #  k_push2d (FP64 push): per particle read x, y, ux, uy, uz, id (48 B) + write them (48 B) = 96 B.
 #  k_deposit2d (FP64 deposit): per particle read old x, y (16 B) + new x, y, ux, uy, uz (40 B)
 #    = 56 B, plus 600 B per cell for the cell's 5x5x3 current tile.
-BYTES_MIX_PUSH = 48
+BYTES_MIX_PUSH = 56
 BYTES_PUSH_FP64 = 96
 BYTES_DEPOSIT_FP64 = 56
 BYTES_DEPOSIT_CELL = 600

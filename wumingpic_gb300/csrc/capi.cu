@@ -228,6 +228,11 @@ int mixed_step(wpic_ctx* c) {
   stage_begin(c, SG_PUSH);
   mix_push_deposit2d(d, c->tmap, c->stream);
   stage_end(c, SG_PUSH, 1);
+  // the arrivals join their columns right away, so the particle state is whole again before
+  // the field solve (which does not read particles) can return an error
+  stage_begin(c, SG_PBC);
+  mix_migrate2d(d, c->stream);
+  stage_end(c, SG_PBC, 1);
   stage_begin(c, SG_JREDUCE);
   mix_curre_refresh2d(d, c->stream);
   stage_end(c, SG_JREDUCE, d.ph.bc == BC_PERIODIC ? 3 : 2);
@@ -242,9 +247,6 @@ int mixed_step(wpic_ctx* c) {
   dfield_ghost2d(d, c->stream);
   uf_add2d(d, c->stream);
   stage_end(c, SG_FIELD, 6);
-  stage_begin(c, SG_PBC);
-  mix_migrate2d(d, c->stream);
-  stage_end(c, SG_PBC, 2);
   return WPIC_OK;
 }
 
@@ -333,40 +335,67 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
       m.nty = ny / MIX_TS;
       m.ntile = m.ntx * m.nty;
       m.nbin = m.ntile * p->nsp;
-      m.bcap = (int)(((long long)p->np * MIX_TC + nx - 1) / nx);
-      m.lcap = m.bcap / 4 > 256 ? m.bcap / 4 : 256;
-      // fixed-point scales of the deposit: every contribution is bounded by
-      // vmax = max(|q| dx/dt, 2 |q| c); a tile pass adds at most nsp * bcap of them to a node.
+      // column depth: the mean slots per cell the caller allotted (np / nx) plus a
+      // Poisson margin of 6 standard deviations, rounded up to a multiple of 4
+      const double nbar = (double)p->np / nx;
+      m.depth = ((int)std::ceil(nbar + 6.0 * std::sqrt(nbar) + 8.0) + 3) & ~3;
+      if (m.depth > MIX_MAX_DEPTH) {
+        st = WPIC_BAD_ARGUMENT;
+        break;
+      }
+      m.bcap = MIX_TC * m.depth;
+      // arrivals per cell and step: a particle leaves its cell with probability <= (|vx| + |vy|) dt / dx
+      // <= sqrt(2) c dt / dx; the inbox holds 1.5 c dt / dx of the mean column plus a Poisson margin
+      {
+        const double mean = nbar * std::fmin(1.0, 1.5 * p->c * p->delt / p->delx);
+        m.icap = ((int)std::ceil(mean + 6.0 * std::sqrt(mean) + 8.0) + 3) & ~3;
+        if (m.icap > m.depth) m.icap = m.depth;
+      }
+      // fixed-point scales of the deposit.  One particle adds at most vmax = max(|q| dx/dt, 2 |q| c)
+      // to a node; a thread flushes the sum of up to 16 particles at once (|v s1| < 2^22 keeps the
+      // magic-number rounding exact), and at most 25 * nsp * depth particles reach a node in one
+      // tile pass (|sum hi| < 2^30).
       double vmax = 0.0;
       for (int k = 0; k < p->nsp; ++k) {
         const double a = std::fabs(p->q[k]) * p->delx / p->delt, b = 2.0 * std::fabs(p->q[k]) * p->c;
         vmax = std::fmax(vmax, std::fmax(a, b));
       }
-      double s1 = std::ldexp(1.0, 21) / std::fmax(vmax, 1e-30);  // |v s1| < 2^21: magic-number rounding exact
-      const double lim = std::ldexp(1.0, 30) / ((double)p->nsp * m.bcap * std::fmax(vmax, 1e-30));
+      vmax = std::fmax(vmax, 1e-30);
+      double s1 = std::ldexp(1.0, 17) / vmax;
+      const double lim = std::ldexp(1.0, 30) / (25.0 * p->nsp * m.depth * vmax);
       if (lim < s1) s1 = lim;
       s1 = std::ldexp(1.0, (int)std::floor(std::log2(s1)));
-      // lo plane: each contribution |lo| <= 2^14, at most nsp * bcap of them per node
-      if (!(s1 >= 1.0) || s1 > std::ldexp(1.0, 60) || (double)p->nsp * m.bcap * 16384.0 >= std::ldexp(1.0, 31)) {
+      // lo plane: each flush adds |lo| <= 2^14; a node takes at most 25 * ceil(nsp * depth / 16) flushes
+      const double nflush = 25.0 * std::ceil((double)p->nsp * m.depth / 16.0) + 25.0;
+      if (!(s1 >= 1.0) || s1 > std::ldexp(1.0, 60) || nflush * 16384.0 >= std::ldexp(1.0, 31) ||
+          (double)m.nbin * m.bcap >= std::ldexp(1.0, 62)) {
         st = WPIC_BAD_ARGUMENT;
         break;
       }
       m.fx_s1 = (float)s1;
+      m.fx_is1f = (float)(1.0 / s1);
       m.fx_s2 = (float)(s1 * 32768.0);
+      for (int k = 0; k < 2; ++k) {
+        const int is = k < p->nsp ? k : 0;
+        m.k_fac1[k] = (float)(p->q[is] / p->r[is] * 0.5 * p->delt);
+        m.k_fac2[k] = (float)(p->q[is] * p->delt / p->r[is]);
+        m.k_qdd[k] = (float)(p->q[is] * p->delx * (1.0 / p->delt));
+        m.k_q[k] = (float)p->q[is];
+      }
+      m.k_dtdx = (float)(p->delt * (1.0 / p->delx));
+      m.k_c = (float)p->c;
+      m.k_ic2 = (float)(1.0 / (p->c * p->c));
       m.fx_is1 = 1.0 / s1;
       m.fx_is2 = 1.0 / (s1 * 32768.0);
-      const size_t nb = (size_t)m.nbin * m.bcap, nl = (size_t)m.nbin * m.lcap;
-      if ((st = dalloc(c, &m.P.cell, nb)) || (st = dalloc(c, &m.P.ox, nb)) || (st = dalloc(c, &m.P.oy, nb)) ||
-          (st = dalloc(c, &m.P.ux, nb)) || (st = dalloc(c, &m.P.uy, nb)) || (st = dalloc(c, &m.P.uz, nb)) ||
-          (st = dalloc(c, &m.P.id, nb)))
+      const size_t nb = (size_t)m.nbin * m.bcap, ni = (size_t)m.nbin * m.icap * MIX_TC;
+      if ((st = dalloc(c, &m.P.ox, nb)) || (st = dalloc(c, &m.P.oy, nb)) || (st = dalloc(c, &m.P.ux, nb)) ||
+          (st = dalloc(c, &m.P.uy, nb)) || (st = dalloc(c, &m.P.uz, nb)) || (st = dalloc(c, &m.P.id, nb)))
         break;
-      if ((st = dalloc(c, &m.L.cell, nl)) || (st = dalloc(c, &m.L.ox, nl)) || (st = dalloc(c, &m.L.oy, nl)) ||
-          (st = dalloc(c, &m.L.ux, nl)) || (st = dalloc(c, &m.L.uy, nl)) || (st = dalloc(c, &m.L.uz, nl)) ||
-          (st = dalloc(c, &m.L.id, nl)))
+      if ((st = dalloc(c, &m.I.ox, ni)) || (st = dalloc(c, &m.I.oy, ni)) || (st = dalloc(c, &m.I.ux, ni)) ||
+          (st = dalloc(c, &m.I.uy, ni)) || (st = dalloc(c, &m.I.uz, ni)) || (st = dalloc(c, &m.I.id, ni)) ||
+          (st = dalloc(c, &m.ikey, ni)))
         break;
-      if ((st = dalloc(c, &m.cnt, m.nbin)) || (st = dalloc(c, &m.lcnt, (size_t)m.nbin * 9)) ||
-          (st = dalloc(c, &m.lofs, (size_t)m.nbin * 9)) || (st = dalloc(c, &m.holes, nl)) ||
-          (st = dalloc(c, &m.tails, nl)) || (st = dalloc(c, &m.cellcnt, (size_t)d.nrowjob * nx)) ||
+      if ((st = dalloc(c, &m.cnt, (size_t)m.nbin * MIX_TC)) || (st = dalloc(c, &m.icnt, (size_t)m.nbin * MIX_TC)) ||
           (st = dalloc(c, &m.ujx, 3 * (size_t)(nx + 4) * (ny + 4))))
         break;
     } else {
@@ -399,7 +428,7 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
       if ((st = dalloc(c, &d.tlist, slots))) break;
       if ((st = dalloc(c, &d.slist, slots))) break;
       if ((st = dalloc(c, &d.map, slots))) break;
-    } else if (mix_make_tensor_map(d, c->tmap) != 0) {
+    } else if (mix_setup2d(d, c->tmap) != 0) {
       st = WPIC_CUDA_ERROR;
       break;
     }
@@ -669,7 +698,7 @@ int wpic_load_weibel_2d(wpic_ctx* c, int ppc, uint64_t seed, double drift, int d
   Dev2D& d = c->d;
   if (drift_axis < 0 || drift_axis > 2 || ppc < 1) return WPIC_BAD_ARGUMENT;
   if (c->mixed) {
-    if ((long long)ppc * MIX_TC > d.m.bcap) return WPIC_CAPACITY;
+    if (ppc > d.m.depth) return WPIC_CAPACITY;
     mix_load_weibel2d(d, ppc, seed, drift, drift_axis, u_thi, u_the, c->stream);
   } else {
     if ((long long)ppc * d.g.nx > d.cap) return WPIC_CAPACITY;
@@ -737,7 +766,7 @@ int wpic_synchronize(wpic_ctx* c) {
 long long wpic_num_particles(wpic_ctx* c) {
   if (!c) return -1;
   const bool mx = c->mixed;
-  std::vector<int> h(mx ? c->d.m.nbin : c->d.nrowjob);
+  std::vector<int> h(mx ? (size_t)c->d.m.nbin * MIX_TC : (size_t)c->d.nrowjob);
   if (cudaMemcpyAsync(h.data(), mx ? c->d.m.cnt : c->d.np2, sizeof(int) * h.size(), cudaMemcpyDeviceToHost,
                       c->stream) !=
       cudaSuccess)

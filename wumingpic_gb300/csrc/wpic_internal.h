@@ -62,33 +62,37 @@ struct Parts64 {
 
 // ---- mixed-precision particle storage (2D) ----
 // Particles live in bins of one 16 x 16-cell tile and one species, bin = tile * nsp + isp,
-// tile = ty * ntx + tx.  Position = integer cell (local index ly*16+lx inside the tile)
-// plus an FP32 offset in [0, 1) per dimension; momenta FP32; 64-bit id.  Inside a bin the
-// order is interleaved over cells, so that the lanes of a warp rarely share a cell.
+// tile = ty * ntx + tx.  Inside a bin every cell owns a column of `depth` slots:
+// slot (k, c) = k * 256 + c for cell c = ly * 16 + lx, so the cell of a particle is implicit.
+// Position = that cell plus an FP32 offset in [0, 1) per dimension; momenta FP32; 64-bit id.
+// Particles that change cell in a push go to the inbox of their new cell (same [k][256] layout,
+// `icap` slots per cell), tagged with a key that orders a cell's arrivals deterministically.
 constexpr int MIX_TS = 16;
 constexpr int MIX_TC = MIX_TS * MIX_TS;
+constexpr int MIX_MAX_DEPTH = 1024;
 
 struct PartsMix {
-  int* cell;  // < 256: local cell; >= 256: leaver, (dir+1)*256 + local cell in the destination tile
   float *ox, *oy, *ux, *uy, *uz;
   long long* id;
 };
 
 struct Mix2D {
   // fixed-point current accumulation of the push: v = hi / s1 + lo / s2 with int32 hi, lo
-  float fx_s1, fx_s2;
+  float fx_s1, fx_s2, fx_is1f;
   double fx_is1, fx_is2;
+  // FP32 constants of the push and deposit, rounded once from the FP64 parameters:
+  // per species q/r dt/2, q dt/r, q dx/dt, q; then dt/dx, c, 1/c^2
+  float k_fac1[2], k_fac2[2], k_qdd[2], k_q[2];
+  float k_dtdx, k_c, k_ic2;
   int ntx, nty, ntile, nbin;
-  int bcap;          // slots per bin
-  int lcap;          // leaver slots per bin
-  PartsMix P;        // [nbin][bcap]
-  PartsMix L;        // [nbin][lcap] leavers grouped by direction
-  int* cnt;          // [nbin]
-  int* lcnt;         // [nbin][9] leavers per direction (index 4 unused)
-  int* lofs;         // [nbin][9] offset of each direction's group inside the bin's leaver region
-  int* holes;        // [nbin][lcap] slots vacated by leavers, ascending
-  int* tails;        // [nbin][lcap] scratch for the tail compaction
-  int* cellcnt;      // [nsp][ny][nx] per-cell counts (reference-layout export)
+  int depth;         // slots per cell column (<= MIX_MAX_DEPTH)
+  int bcap;          // slots per bin = 256 * depth
+  int icap;          // inbox slots per cell
+  PartsMix P;        // [nbin][depth][256]
+  int* cnt;          // [nbin][256] particles per cell column
+  PartsMix I;        // [nbin][icap][256] arrivals of the last push
+  int* ikey;         // [nbin][icap][256] arrival order key: direction group << 16 | source slot
+  int* icnt;         // [nbin][256] arrivals per cell (zero between steps)
   unsigned long long* ujx;  // [3][ny+4][nx+4] current in fixed point (units 1/fx_s2), summed exactly
 };
 
@@ -157,12 +161,12 @@ void soa_to_aos2d(const Dev2D& d, double* aos, int ndim, int np_host, int row0, 
 void field_ref_to_soa(const double* ref, double* soa, int ncomp, int nslab, cudaStream_t s);
 void field_soa_to_ref(const double* soa, double* ref, int ncomp, int nslab, cudaStream_t s);
 // ---- mixed-precision path (mixed2d.cu) ----
-int mix_make_tensor_map(const Dev2D& d, void* tmap_out);  // CUtensorMap of uf for the TMA tile loads
+int mix_setup2d(const Dev2D& d, void* tmap_out);  // CUtensorMap of uf for the TMA tile loads; kernel attributes
 void mix_push_deposit2d(const Dev2D& d, const void* tmap, cudaStream_t s);
 void mix_curre_refresh2d(const Dev2D& d, cudaStream_t s);
 void mix_migrate2d(const Dev2D& d, cudaStream_t s);
 void mix_put2d(const Dev2D& d, const double* aos, int ndim, int np_host, int isp, int ty0, int nty, cudaStream_t s);
-void mix_count_rows2d(const Dev2D& d, cudaStream_t s);
+void mix_count_rows2d(const Dev2D& d, cudaStream_t s);  // cumcnt and np2 of the reference layout
 void mix_get2d(const Dev2D& d, double* aos, int ndim, int np_host, int isp, int ty0, int nty, cudaStream_t s);
 void mix_load_weibel2d(const Dev2D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
                        double u_thi, double u_the, cudaStream_t s);
