@@ -1,6 +1,7 @@
 // C ABI of the library (declared in include/wumingpic_gb300.h): context
 // creation, device memory, reference-layout state exchange, and the host-side
 // sequencing of the kernels of one time step.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -41,6 +42,12 @@ struct wpic_ctx {
   int sticky_status = WPIC_OK;
   bool mixed = false;
   alignas(128) unsigned char tmap[128];  // CUtensorMap of uf (mixed path TMA loads)
+  // mixed path: the particle layers (reallocated when bins grow) and the host copy of the layout
+  float* mixP = nullptr;
+  std::vector<int> h_dep;
+  std::vector<long long> h_off;
+  int* h_grow = nullptr;  // pinned mirror of the grow flag
+  double mix_vmax = 0.0;  // largest contribution of one particle to one node of the deposit
 };
 
 namespace {
@@ -223,6 +230,90 @@ void do_migrate_sort(wpic_ctx* c) {
   stage_end(c, SG_SORT, 2);
 }
 
+// Fixed-point scales of the mixed deposit for columns of at most maxdep slots.  One particle adds
+// at most vmax = max(|q| dx/dt, 2 |q| c) to a node; a thread flushes the sum of up to 16 particles
+// at once (|v s1| < 2^22 keeps the magic-number rounding exact), and at most 25 * nsp * maxdep
+// particles reach a node in one tile pass (|sum hi| < 2^30).  The current is rebuilt every step,
+// so the scales may change with the layout.
+int mix_set_scales(wpic_ctx* c, int maxdep) {
+  Mix2D& m = c->d.m;
+  const double vmax = c->mix_vmax;
+  const int nsp = c->prm.nsp;
+  double s1 = std::ldexp(1.0, 17) / vmax;
+  const double lim = std::ldexp(1.0, 30) / (25.0 * nsp * maxdep * vmax);
+  if (lim < s1) s1 = lim;
+  s1 = std::ldexp(1.0, (int)std::floor(std::log2(s1)));
+  // lo plane: each flush adds |lo| <= 2^14; a node takes at most 25 * ceil(nsp * maxdep / 16) flushes
+  const double nflush = 25.0 * std::ceil((double)nsp * maxdep / 16.0) + 25.0;
+  if (!(s1 > 0.0) || s1 > std::ldexp(1.0, 100) || nflush * 16384.0 >= std::ldexp(1.0, 31)) return WPIC_BAD_ARGUMENT;
+  m.fx_s1 = (float)s1;
+  m.fx_is1f = (float)(1.0 / s1);
+  m.fx_s2 = (float)(s1 * 32768.0);
+  m.fx_is1 = 1.0 / s1;
+  m.fx_is2 = 1.0 / (s1 * 32768.0);
+  return WPIC_OK;
+}
+
+// Lays the mixed-path bins out with the given depths (slots per column).  keep = true copies
+// the columns of the current layout (counts unchanged); otherwise the new layout starts empty.
+int mix_set_layout(wpic_ctx* c, const std::vector<int>& dep, bool keep) {
+  Mix2D& m = c->d.m;
+  std::vector<long long> off(m.nbin);
+  long long layers = 0;
+  int maxdep = 1;
+  for (int b = 0; b < m.nbin; ++b) {
+    if (dep[b] < 1 || dep[b] > MIX_MAX_DEPTH) return WPIC_CAPACITY;
+    off[b] = layers;
+    layers += dep[b];
+    maxdep = std::max(maxdep, dep[b]);
+  }
+  if (int st = mix_set_scales(c, maxdep)) return st;
+  if (!keep && c->mixP) {
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(c->mixP);
+    c->mixP = nullptr;
+  }
+  float* np_ = nullptr;
+  CK(cudaMalloc(&np_, (size_t)layers * MIX_PL * sizeof(float)));
+  long long* old_off = nullptr;
+  const float* old_P = c->mixP;
+  if (keep && old_P) {
+    // the old offsets stay readable by the copy kernel until it is done
+    CK(cudaMalloc(&old_off, sizeof(long long) * m.nbin));
+    CK(cudaMemcpyAsync(old_off, m.boff, sizeof(long long) * m.nbin, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  CK(cudaMemcpyAsync(m.boff, off.data(), sizeof(long long) * m.nbin, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(m.bdep, dep.data(), sizeof(int) * m.nbin, cudaMemcpyHostToDevice, c->stream));
+  m.P = np_;
+  if (keep && old_P) mix_relayout2d(c->d, old_P, old_off, c->stream);
+  CK(cudaStreamSynchronize(c->stream));  // host vectors and the old buffers are released below
+  if (old_off) cudaFree(old_off);
+  if (keep && old_P) cudaFree(c->mixP);
+  c->mixP = np_;
+  c->h_dep = dep;
+  c->h_off = off;
+  return WPIC_OK;
+}
+
+// grows the bins whose columns came within 1/8 of full in the last step to 1.5 x their need
+int mix_grow(wpic_ctx* c) {
+  Mix2D& m = c->d.m;
+  std::vector<int> need(m.nbin);
+  CK(cudaMemcpyAsync(need.data(), m.bneed, sizeof(int) * m.nbin, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemsetAsync(m.grow, 0, sizeof(int), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *c->h_grow = 0;
+  std::vector<int> dep = c->h_dep;
+  bool any = false;
+  for (int b = 0; b < m.nbin; ++b)
+    if (8LL * need[b] > 7LL * dep[b]) {
+      const long long nd = ((long long)std::ceil(1.5 * need[b] + 16.0) + 7) & ~7LL;
+      dep[b] = (int)(nd > MIX_MAX_DEPTH ? MIX_MAX_DEPTH : nd);
+      any = true;
+    }
+  return any ? mix_set_layout(c, dep, true) : WPIC_OK;
+}
+
 int mixed_step(wpic_ctx* c) {
   Dev2D& d = c->d;
   stage_begin(c, SG_PUSH);
@@ -233,6 +324,7 @@ int mixed_step(wpic_ctx* c) {
   stage_begin(c, SG_PBC);
   mix_migrate2d(d, c->stream);
   stage_end(c, SG_PBC, 1);
+  CK(cudaMemcpyAsync(c->h_grow, d.m.grow, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   stage_begin(c, SG_JREDUCE);
   mix_curre_refresh2d(d, c->stream);
   stage_end(c, SG_JREDUCE, d.ph.bc == BC_PERIODIC ? 3 : 2);
@@ -247,6 +339,8 @@ int mixed_step(wpic_ctx* c) {
   dfield_ghost2d(d, c->stream);
   uf_add2d(d, c->stream);
   stage_end(c, SG_FIELD, 6);
+  // the CG's host checks synchronised the stream, so the grow flag of this step is in h_grow
+  if (*c->h_grow) return mix_grow(c);
   return WPIC_OK;
 }
 
@@ -335,46 +429,14 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
       m.nty = ny / MIX_TS;
       m.ntile = m.ntx * m.nty;
       m.nbin = m.ntile * p->nsp;
-      // column depth: the mean slots per cell the caller allotted (np / nx) plus a
-      // Poisson margin of 6 standard deviations, rounded up to a multiple of 4
-      const double nbar = (double)p->np / nx;
-      m.depth = ((int)std::ceil(nbar + 6.0 * std::sqrt(nbar) + 8.0) + 3) & ~3;
-      if (m.depth > MIX_MAX_DEPTH) {
-        st = WPIC_BAD_ARGUMENT;
-        break;
-      }
-      m.bcap = MIX_TC * m.depth;
-      // arrivals per cell and step: a particle leaves its cell with probability <= (|vx| + |vy|) dt / dx
-      // <= sqrt(2) c dt / dx; the inbox holds 1.5 c dt / dx of the mean column plus a Poisson margin
-      {
-        const double mean = nbar * std::fmin(1.0, 1.5 * p->c * p->delt / p->delx);
-        m.icap = ((int)std::ceil(mean + 6.0 * std::sqrt(mean) + 8.0) + 3) & ~3;
-        if (m.icap > m.depth) m.icap = m.depth;
-      }
-      // fixed-point scales of the deposit.  One particle adds at most vmax = max(|q| dx/dt, 2 |q| c)
-      // to a node; a thread flushes the sum of up to 16 particles at once (|v s1| < 2^22 keeps the
-      // magic-number rounding exact), and at most 25 * nsp * depth particles reach a node in one
-      // tile pass (|sum hi| < 2^30).
+      // largest contribution of one particle to one node of the deposit (sets the fixed-point
+      // scales, see mix_set_scales)
       double vmax = 0.0;
       for (int k = 0; k < p->nsp; ++k) {
         const double a = std::fabs(p->q[k]) * p->delx / p->delt, b = 2.0 * std::fabs(p->q[k]) * p->c;
         vmax = std::fmax(vmax, std::fmax(a, b));
       }
-      vmax = std::fmax(vmax, 1e-30);
-      double s1 = std::ldexp(1.0, 17) / vmax;
-      const double lim = std::ldexp(1.0, 30) / (25.0 * p->nsp * m.depth * vmax);
-      if (lim < s1) s1 = lim;
-      s1 = std::ldexp(1.0, (int)std::floor(std::log2(s1)));
-      // lo plane: each flush adds |lo| <= 2^14; a node takes at most 25 * ceil(nsp * depth / 16) flushes
-      const double nflush = 25.0 * std::ceil((double)p->nsp * m.depth / 16.0) + 25.0;
-      if (!(s1 >= 1.0) || s1 > std::ldexp(1.0, 60) || nflush * 16384.0 >= std::ldexp(1.0, 31) ||
-          (double)m.nbin * m.bcap >= std::ldexp(1.0, 62)) {
-        st = WPIC_BAD_ARGUMENT;
-        break;
-      }
-      m.fx_s1 = (float)s1;
-      m.fx_is1f = (float)(1.0 / s1);
-      m.fx_s2 = (float)(s1 * 32768.0);
+      c->mix_vmax = std::fmax(vmax, 1e-300);
       for (int k = 0; k < 2; ++k) {
         const int is = k < p->nsp ? k : 0;
         m.k_fac1[k] = (float)(p->q[is] / p->r[is] * 0.5 * p->delt);
@@ -385,19 +447,20 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
       m.k_dtdx = (float)(p->delt * (1.0 / p->delx));
       m.k_c = (float)p->c;
       m.k_ic2 = (float)(1.0 / (p->c * p->c));
-      m.fx_is1 = 1.0 / s1;
-      m.fx_is2 = 1.0 / (s1 * 32768.0);
-      const size_t nb = (size_t)m.nbin * m.bcap, ni = (size_t)m.nbin * m.icap * MIX_TC;
-      if ((st = dalloc(c, &m.P.ox, nb)) || (st = dalloc(c, &m.P.oy, nb)) || (st = dalloc(c, &m.P.ux, nb)) ||
-          (st = dalloc(c, &m.P.uy, nb)) || (st = dalloc(c, &m.P.uz, nb)) || (st = dalloc(c, &m.P.id, nb)))
+      const size_t ncol = (size_t)m.nbin * MIX_TC;
+      if ((st = dalloc(c, &m.boff, m.nbin)) || (st = dalloc(c, &m.bdep, m.nbin)) || (st = dalloc(c, &m.cnt, ncol)) ||
+          (st = dalloc(c, &m.ccnt, ncol)) || (st = dalloc(c, &m.acnt, ncol)) || (st = dalloc(c, &m.bneed, m.nbin)) ||
+          (st = dalloc(c, &m.grow, 1)) || (st = dalloc(c, &m.ujx, 3 * (size_t)(nx + 4) * (ny + 4))))
         break;
-      if ((st = dalloc(c, &m.I.ox, ni)) || (st = dalloc(c, &m.I.oy, ni)) || (st = dalloc(c, &m.I.ux, ni)) ||
-          (st = dalloc(c, &m.I.uy, ni)) || (st = dalloc(c, &m.I.uz, ni)) || (st = dalloc(c, &m.I.id, ni)) ||
-          (st = dalloc(c, &m.ikey, ni)))
+      if (cudaMallocHost(&c->h_grow, sizeof(int)) != cudaSuccess) {
+        st = WPIC_CUDA_ERROR;
         break;
-      if ((st = dalloc(c, &m.cnt, (size_t)m.nbin * MIX_TC)) || (st = dalloc(c, &m.icnt, (size_t)m.nbin * MIX_TC)) ||
-          (st = dalloc(c, &m.ujx, 3 * (size_t)(nx + 4) * (ny + 4))))
-        break;
+      }
+      *c->h_grow = 0;
+      // an initial layout for the capacity the caller allotted (np per row); put and load
+      // lay the bins out again for the particles they bring
+      const int dep0 = mix_initial_depth((double)p->np / nx, p->c * p->delt / p->delx);
+      if ((st = mix_set_layout(c, std::vector<int>(m.nbin, dep0), false))) break;
     } else {
       if ((st = alloc_parts(c, &d.A, slots))) break;
       if ((st = alloc_parts(c, &d.B, slots))) break;
@@ -452,6 +515,8 @@ int wpic_finalize(wpic_ctx* c) {
   if (!c) return WPIC_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (void* p : c->allocs) cudaFree(p);
+  if (c->mixP) cudaFree(c->mixP);
+  if (c->h_grow) cudaFreeHost(c->h_grow);
   if (c->staging) cudaFree(c->staging);
   if (c->h_cg) cudaFreeHost(c->h_cg);
   if (c->h_err) cudaFreeHost(c->h_err);
@@ -485,6 +550,24 @@ int wpic_put_particles(wpic_ctx* c, int which, const double* up, const int* np2,
                        c->stream));
   const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
   if (c->mixed) {
+    // lay the bins out for these particles: each bin's depth from its fullest cell
+    {
+      const Mix2D& m = d.m;
+      std::vector<int> dep(m.nbin);
+      const double cdx = c->prm.c * c->prm.delt / c->prm.delx;
+      for (int isp = 0; isp < c->prm.nsp; ++isp)
+        for (int ty = 0; ty < m.nty; ++ty)
+          for (int tx = 0; tx < m.ntx; ++tx) {
+            int mx = 0;
+            for (int ly = 0; ly < MIX_TS; ++ly) {
+              const int* cc = cumcnt + ((size_t)isp * d.g.ny + ty * MIX_TS + ly) * (nx + 1) + tx * MIX_TS;
+              for (int lx = 0; lx < MIX_TS; ++lx) mx = std::max(mx, cc[lx + 1] - cc[lx]);
+            }
+            dep[(ty * m.ntx + tx) * c->prm.nsp + isp] = mix_initial_depth(mx, cdx);
+          }
+      int st = mix_set_layout(c, dep, false);
+      if (st) return st;
+    }
     // stage whole tile rows (16 bucket rows) of one species at a time
     size_t trows = ((size_t)1 << 30) / (row_bytes * MIX_TS);
     if (trows < 1) trows = 1;
@@ -698,7 +781,9 @@ int wpic_load_weibel_2d(wpic_ctx* c, int ppc, uint64_t seed, double drift, int d
   Dev2D& d = c->d;
   if (drift_axis < 0 || drift_axis > 2 || ppc < 1) return WPIC_BAD_ARGUMENT;
   if (c->mixed) {
-    if (ppc > d.m.depth) return WPIC_CAPACITY;
+    const int dep = mix_initial_depth(ppc, c->prm.c * c->prm.delt / c->prm.delx);
+    int st = mix_set_layout(c, std::vector<int>(d.m.nbin, dep), false);
+    if (st) return st;
     mix_load_weibel2d(d, ppc, seed, drift, drift_axis, u_thi, u_the, c->stream);
   } else {
     if ((long long)ppc * d.g.nx > d.cap) return WPIC_CAPACITY;

@@ -26,6 +26,8 @@
 // (2d/common/boundary_periodic.f90:193-225) applied to a cell column.
 #include <cuda.h>
 
+#include <cmath>
+
 #include "common.cuh"
 
 namespace wpic {
@@ -40,7 +42,7 @@ constexpr int TT = MIX_TS + 2;      // cell-centred values per tile edge (cells 
 constexpr int JP = 48;
 constexpr int FLUSH_EVERY = 16;     // particles accumulated in registers between flushes
 constexpr int PF = 8;               // particles in flight per push thread (shared-memory ring)
-constexpr int PF_BYTES = PF * (5 * 4 + 8) * MP_THREADS;
+constexpr int PF_BYTES = PF * 7 * MIX_TC * 4;  // the key plane is not prefetched
 constexpr unsigned long long kSpinLimit = 1ull << 22;  // a few seconds at most
 // resident CTAs per SM asked of the push kernel; at 2 its 128 registers per thread still hold
 // the cell's whole current stencil without spilling
@@ -91,9 +93,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar) {
 // 4-byte asynchronous global -> shared copy, completion tracked per thread by commit groups
 __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async8(long long* dst, const long long* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
@@ -175,28 +174,25 @@ __device__ __forceinline__ void cell_flush(CellCurrent& a, int (*jhi)[TW][JP], i
 
 }  // namespace
 
-// a leaver of the push waiting for its inbox slot (one per thread)
+// a leaver of the push waiting for its slot (one per thread): the top slot of its new column,
+// that column's depth, and the eight 32-bit words of the entry (five FP32 components, the id's
+// two words, the arrival key)
 struct PendingLeaver {
-  size_t ibase[MP_THREADS];
-  long long id[MP_THREADS];
-  float v[5][MP_THREADS];
-  int key[MP_THREADS];
+  float* top[MP_THREADS];
+  int dep[MP_THREADS];
+  float w[8][MP_THREADS];
 };
 constexpr int PUSH_DYN_BYTES = PF_BYTES + (int)sizeof(PendingLeaver);
 
-__device__ __forceinline__ void write_pending(const Mix2D& m, const PendingLeaver* pend, int c, int pos, int* err) {
-  if (pos >= m.icap) {
+// arrival number pos of a column goes to slot depth - 1 - pos
+__device__ __forceinline__ void write_pending(const PendingLeaver* pend, int c, int pos, int* err) {
+  if (pos >= pend->dep[c]) {
     atomicOr(err, EB_CAPACITY);
     return;
   }
-  const size_t io = pend->ibase[c] + (size_t)pos * MIX_TC;
-  m.I.ox[io] = pend->v[0][c];
-  m.I.oy[io] = pend->v[1][c];
-  m.I.ux[io] = pend->v[2][c];
-  m.I.uy[io] = pend->v[3][c];
-  m.I.uz[io] = pend->v[4][c];
-  m.I.id[io] = pend->id[c];
-  m.ikey[io] = pend->key[c];
+  float* io = pend->top[c] - (size_t)pos * MIX_PL;
+#pragma unroll
+  for (int a = 0; a < 8; ++a) io[a * MIX_TC] = pend->w[a][c];
 }
 
 // ---------------------------------------------------------------------------
@@ -213,9 +209,11 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
   __shared__ __align__(16) float4 sfa[TT * TT];  // (Bx, By, Bz, Ex) at cell centres
   __shared__ __align__(8) float2 sfb[TT * TT];   // (Ey, Ez)
   __shared__ __align__(8) unsigned long long bar;
-  extern __shared__ __align__(16) float pfbuf[];  // [PF][5][256] prefetched particles, then [PF][256] ids
-  long long* pfid = reinterpret_cast<long long*>(pfbuf + PF * 5 * MIX_TC);
-  PendingLeaver* pend = reinterpret_cast<PendingLeaver*>(pfid + PF * MIX_TC);
+  // the 3 x 3 neighbourhood of tiles, per species: bin, first layer, depth
+  __shared__ int nb_bin[2][9], nb_dep[2][9];
+  __shared__ long long nb_off[2][9];
+  extern __shared__ __align__(16) float pfbuf[];  // [PF][7][256] prefetched slots
+  PendingLeaver* pend = reinterpret_cast<PendingLeaver*>(pfbuf + PF * 7 * MIX_TC);
   const Mix2D& m = d.m;
   const int tile = blockIdx.x;
   const int tx = tile % m.ntx, ty = tile / m.ntx;
@@ -225,21 +223,27 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
   const int bin0 = tile * nsp;
   const int n0 = m.cnt[bin0 * MIX_TC + c];
   const int ntot = n0 + (nsp > 1 ? m.cnt[(bin0 + 1) * MIX_TC + c] : 0);
-  // slot of flattened item t (species 0 items first): col[t >= n0] + t * 256
-  const size_t col0 = (size_t)bin0 * m.bcap + c;
-  const size_t col1 = (size_t)(bin0 + 1) * m.bcap + c - (size_t)n0 * MIX_TC;
+  if (threadIdx.x < 2 * 9) {
+    const int s = threadIdx.x / 9, q = threadIdx.x % 9;
+    int ntx_ = tx + q % 3 - 1, nty_ = ty + q / 3 - 1;
+    if (ntx_ < 0) ntx_ += m.ntx; else if (ntx_ >= m.ntx) ntx_ -= m.ntx;
+    if (nty_ < 0) nty_ += m.nty; else if (nty_ >= m.nty) nty_ -= m.nty;
+    const int b = (nty_ * m.ntx + ntx_) * nsp + (s < nsp ? s : 0);
+    nb_bin[s][q] = b;
+    nb_dep[s][q] = m.bdep[b];
+    nb_off[s][q] = m.boff[b];
+  }
+  // slot of flattened item t (species 0 items first): col[t >= n0] + t layers
+  float* const col0 = mix_slot(m, bin0, 0, c);
+  float* const col1 = mix_slot(m, bin0 + (nsp > 1 ? 1 : 0), 0, c) - (size_t)n0 * MIX_PL;
   // each thread streams its own column(s) through a ring of PF particles in shared memory
   // (cp.async), so PF particle loads per thread are in flight
   auto issue = [&](int t) {
     if (t < ntot) {
-      const size_t sl = (t < n0 ? col0 : col1) + (size_t)t * MIX_TC;
-      float* s = pfbuf + (t & (PF - 1)) * 5 * MIX_TC + c;
-      cp_async4(s, m.P.ox + sl);
-      cp_async4(s + MIX_TC, m.P.oy + sl);
-      cp_async4(s + 2 * MIX_TC, m.P.ux + sl);
-      cp_async4(s + 3 * MIX_TC, m.P.uy + sl);
-      cp_async4(s + 4 * MIX_TC, m.P.uz + sl);
-      cp_async8(pfid + (t & (PF - 1)) * MIX_TC + c, m.P.id + sl);
+      const float* src = (t < n0 ? col0 : col1) + (size_t)t * MIX_PL;
+      float* dst = pfbuf + (t & (PF - 1)) * 7 * MIX_TC + c;
+#pragma unroll
+      for (int a = 0; a < 7; ++a) cp_async4(dst + a * MIX_TC, src + a * MIX_TC);
     }
     cp_async_commit();
   };
@@ -282,17 +286,17 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
   cell_zero(acc);
   int since = 0;
   // the column is compacted in place: stayer number j goes to slot j (<= its old slot, whose
-  // contents were already read); leavers go to the inbox of their new cell
+  // contents were already read); leavers go to the top of their new cell's column
   int j0 = 0, j1 = 0;
-  int ppos = -1;  // inbox slot of the pending leaver parked in shared memory, -1 if none
+  int ppos = -1;  // arrival number of the pending leaver parked in shared memory, -1 if none
   for (int t = 0; t < ntot; ++t) {
     cp_async_wait<PF - 1>();
     const bool sp1 = t >= n0;
     const int k = sp1 ? t - n0 : t;
-    const float* pb = pfbuf + (t & (PF - 1)) * 5 * MIX_TC + c;
-    const long long pid = pfid[(t & (PF - 1)) * MIX_TC + c];
-    const float ox = pb[0], oy = pb[MIX_TC];
-    float ux = pb[2 * MIX_TC], uy = pb[3 * MIX_TC], uz = pb[4 * MIX_TC];
+    const float* pb = pfbuf + (t & (PF - 1)) * 7 * MIX_TC + c;
+    const float ox = pb[MIX_OX], oy = pb[MIX_OY];
+    float ux = pb[MIX_UX], uy = pb[MIX_UY], uz = pb[MIX_UZ];
+    const float idlo = pb[MIX_IDLO], idhi = pb[MIX_IDHI];  // the id's two words, passed through
     const float fac1 = sp1 ? m.k_fac1[1] : m.k_fac1[0];
     const float fac2 = sp1 ? m.k_fac2[1] : m.k_fac2[0];
     const float qdd = sp1 ? m.k_qdd[1] : m.k_qdd[0];
@@ -305,21 +309,18 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
 #pragma unroll
     for (int jy = 0; jy < 3; ++jy) {
       const float wy = jy == 0 ? sy0 : (jy == 1 ? sy1 : sy2);
-      float fr[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
       for (int jx = 0; jx < 3; ++jx) {
-        const float wx = jx == 0 ? sx0 : (jx == 1 ? sx1 : sx2);
+        const float w = wy * (jx == 0 ? sx0 : (jx == 1 ? sx1 : sx2));
         const float4 a = sfa[f0 + jy * TT + jx];
         const float2 b = sfb[f0 + jy * TT + jx];
-        fr[0] = fmaf(wx, a.x, fr[0]);
-        fr[1] = fmaf(wx, a.y, fr[1]);
-        fr[2] = fmaf(wx, a.z, fr[2]);
-        fr[3] = fmaf(wx, a.w, fr[3]);
-        fr[4] = fmaf(wx, b.x, fr[4]);
-        fr[5] = fmaf(wx, b.y, fr[5]);
+        f[0] = fmaf(w, a.x, f[0]);
+        f[1] = fmaf(w, a.y, f[1]);
+        f[2] = fmaf(w, a.z, f[2]);
+        f[3] = fmaf(w, a.w, f[3]);
+        f[4] = fmaf(w, b.x, f[4]);
+        f[5] = fmaf(w, b.y, f[5]);
       }
-#pragma unroll
-      for (int q = 0; q < 6; ++q) f[q] = fmaf(wy, fr[q], f[q]);
     }
     const float bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
     // Buneman-Boris (2d/common/particle.f90:133-155)
@@ -373,33 +374,37 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
       }
     }
     const bool leaves = (incx | incy) != 0;
-    // the inbox slot of the previous leaver has had a whole iteration to return
-    if (ppos >= 0) write_pending(m, pend, c, ppos, d.err);
+    // the slot of the previous leaver has had a whole iteration to return
+    if (ppos >= 0) write_pending(pend, c, ppos, d.err);
     ppos = -1;
     if (leaves) {
-      // destination cell (periodic in y; in x periodic, or inside the walls)
-      int gxn = tx * MIX_TS + lx + incx, gyn = ty * MIX_TS + ly + incy;
-      if (gxn < 0) gxn += g.nx; else if (gxn >= g.nx) gxn -= g.nx;
-      if (gyn < 0) gyn += g.ny; else if (gyn >= g.ny) gyn -= g.ny;
-      const int dbin = ((gyn >> 4) * m.ntx + (gxn >> 4)) * nsp + (sp1 ? 1 : 0);
-      const int dlc = (gyn & (MIX_TS - 1)) * MIX_TS + (gxn & (MIX_TS - 1));
-      ppos = atomicAdd(&m.icnt[dbin * MIX_TC + dlc], 1);  // used in the next iteration
-      pend->ibase[c] = (size_t)dbin * m.icap * MIX_TC + dlc;
-      pend->v[0][c] = nx_;
-      pend->v[1][c] = ny_;
-      pend->v[2][c] = ux;
-      pend->v[3][c] = uy;
-      pend->v[4][c] = uz;
-      pend->id[c] = pid;
-      pend->key[c] = (dir_group((incy + 1) * 3 + (incx + 1)) << 16) | k;
+      // new cell, and its tile among the 3 x 3 neighbourhood (periodic in y; in x periodic, or
+      // inside the walls)
+      const int nlx = lx + incx, nly = ly + incy;
+      const int q = ((nly >> 4) + 1) * 3 + ((nlx >> 4) + 1);  // >> 4 of -1 is -1
+      const int s = sp1 ? 1 : 0;
+      const int dlc = (nly & (MIX_TS - 1)) * MIX_TS + (nlx & (MIX_TS - 1));
+      const int dep = nb_dep[s][q];
+      ppos = atomicAdd(&m.acnt[nb_bin[s][q] * MIX_TC + dlc], 1);  // used in the next iteration
+      pend->top[c] = m.P + ((size_t)nb_off[s][q] + dep - 1) * MIX_PL + dlc;
+      pend->dep[c] = dep;
+      pend->w[0][c] = nx_;
+      pend->w[1][c] = ny_;
+      pend->w[2][c] = ux;
+      pend->w[3][c] = uy;
+      pend->w[4][c] = uz;
+      pend->w[5][c] = idlo;
+      pend->w[6][c] = idhi;
+      pend->w[7][c] = __int_as_float((dir_group((incy + 1) * 3 + (incx + 1)) << 16) | k);
     } else {
-      const size_t so = (sp1 ? col1 + (size_t)n0 * MIX_TC : col0) + (size_t)(sp1 ? j1 : j0) * MIX_TC;
-      m.P.ox[so] = nx_;
-      m.P.oy[so] = ny_;
-      m.P.ux[so] = ux;
-      m.P.uy[so] = uy;
-      m.P.uz[so] = uz;
-      m.P.id[so] = pid;
+      float* so = (sp1 ? col1 + (size_t)n0 * MIX_PL : col0) + (size_t)(sp1 ? j1 : j0) * MIX_PL;
+      so[MIX_OX] = nx_;
+      so[MIX_OY] = ny_;
+      so[MIX_UX] = ux;
+      so[MIX_UY] = uy;
+      so[MIX_UZ] = uz;
+      so[MIX_IDLO] = idlo;
+      so[MIX_IDHI] = idhi;
       if (sp1) ++j1; else ++j0;
     }
     // ---- Esirkepov deposition on the cell's full 5 x 5 stencil (2d/common/field.f90:223-298) ----
@@ -439,9 +444,9 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
     issue(t + PF);
   }
   cp_async_wait<0>();
-  if (ppos >= 0) write_pending(m, pend, c, ppos, d.err);
-  m.cnt[bin0 * MIX_TC + c] = j0;
-  if (nsp > 1) m.cnt[(bin0 + 1) * MIX_TC + c] = j1;
+  if (ppos >= 0) write_pending(pend, c, ppos, d.err);
+  m.ccnt[bin0 * MIX_TC + c] = j0;
+  if (nsp > 1) m.ccnt[(bin0 + 1) * MIX_TC + c] = j1;
   if (since) cell_flush(acc, jhi, jlo, lx, ly, fs1, fis1, fs2);
   __syncthreads();
   // one flush of the tile into the global fixed-point current (exact 64-bit integer sums, so the
@@ -510,84 +515,124 @@ void mix_curre_refresh2d(const Dev2D& d, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
-// arrivals (per bin, thread = destination cell): the cell's inbox entries are
-// appended to its column in the order of their keys -- direction group, then
-// slot in the source column -- so the result does not depend on the order in
-// which the push's atomics handed out inbox slots.  Appending at the end of the
-// compacted column keeps the reference's hole-filling idea (arrivals take the
-// free slots) without holes: the push already compacted the stayers.
+// arrivals (per bin, thread = destination cell): the push left the cell's j stayers in slots
+// 0 .. j-1 and its b arrivals in slots dep-1 down to dep-b, in the order the push's atomics
+// handed out.  They are moved to slots j .. j+b-1 in the order of their keys -- direction
+// group, then slot in the source column -- so the result does not depend on that order.
+// This keeps the reference's scheme of arrivals taking the free slots of a row
+// (2d/common/boundary_periodic.f90:193-225), applied to a cell column.  The kernel also
+// records, per bin, count + 2 x arrivals of its fullest column, the room the next step may
+// need; past 7/8 of the depth the host grows the bin before the next push.
 // ---------------------------------------------------------------------------
 constexpr int ARR_KEYS_SMEM = 32;  // keys per cell staged in shared memory; more are read from global memory
 constexpr int ARR_BATCH = 4;
 
 __global__ void __launch_bounds__(MIX_TC, 4) k_mix_arrive(Dev2D d) {
   __shared__ int skey[ARR_KEYS_SMEM][MIX_TC];
+  __shared__ int wmax[MIX_TC / 32];
   const Mix2D& m = d.m;
   const int bin = blockIdx.x;
   const int c = threadIdx.x;
-  const int n = m.cnt[bin * MIX_TC + c];
-  int b = m.icnt[bin * MIX_TC + c];
-  if (b > m.icap) b = m.icap;  // the push flagged the overflow
-  const size_t ib = (size_t)bin * m.icap * MIX_TC + c;
-  const int* kg = m.ikey + ib;
+  const int dep = m.bdep[bin];
+  const int nold = m.cnt[bin * MIX_TC + c];
+  const int j = m.ccnt[bin * MIX_TC + c];
+  int b = m.acnt[bin * MIX_TC + c];
+  bool ok = true;
+  // the arrivals must not have reached the slots the push read (nold) or the moved arrivals' range
+  if (b > dep || nold + b > dep || j + 2 * b > dep) {
+    ok = false;
+    atomicOr(d.err, EB_CAPACITY);
+  }
+  if (b > dep) b = dep;
+  float* const col = mix_slot(m, bin, 0, c);
+  const float* top = col + (size_t)(dep - 1) * MIX_PL;  // arrival i in slot dep - 1 - i
   const int ns = b < ARR_KEYS_SMEM ? b : ARR_KEYS_SMEM;
-  for (int j = 0; j < ns; ++j)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(&skey[j][c])), "l"(kg + (size_t)j * MIX_TC)
+  for (int i = 0; i < ns; ++i)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(&skey[i][c])),
+                 "l"(top - (size_t)i * MIX_PL + MIX_KEY)
                  : "memory");
   asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
-  auto key = [&](int j) { return j < ARR_KEYS_SMEM ? skey[j][c] : kg[(size_t)j * MIX_TC]; };
-  const size_t base = (size_t)bin * m.bcap + c;
-  for (int i0 = 0; i0 < b; i0 += ARR_BATCH) {
-    size_t src[ARR_BATCH], dst[ARR_BATCH];
+  auto key = [&](int i) {
+    return i < ARR_KEYS_SMEM ? skey[i][c] : __float_as_int(top[MIX_KEY - (ptrdiff_t)i * MIX_PL]);
+  };
+  for (int i0 = 0; ok && i0 < b; i0 += ARR_BATCH) {
+    const float* src[ARR_BATCH];
+    float* dst[ARR_BATCH];
     bool on[ARR_BATCH];
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u) {
       const int i = i0 + u;
-      on[u] = false;
-      src[u] = dst[u] = 0;
-      if (i < b) {
+      on[u] = i < b;
+      src[u] = top;
+      dst[u] = col;
+      if (on[u]) {
         const int ki = key(i);
         int rank = 0;
-        for (int j = 0; j < b; ++j) rank += key(j) < ki ? 1 : 0;
-        const int slot = n + rank;
-        on[u] = slot < m.depth;
-        src[u] = ib + (size_t)i * MIX_TC;
-        dst[u] = base + (size_t)slot * MIX_TC;
+        for (int l = 0; l < b; ++l) rank += key(l) < ki ? 1 : 0;
+        src[u] = top - (size_t)i * MIX_PL;
+        dst[u] = col + (size_t)(j + rank) * MIX_PL;
       }
     }
-    float a[ARR_BATCH], bb[ARR_BATCH], e[ARR_BATCH], f[ARR_BATCH], h[ARR_BATCH];
-    long long id[ARR_BATCH];
+    float w[ARR_BATCH][7];
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u)
       if (on[u]) {
-        a[u] = m.I.ox[src[u]];
-        bb[u] = m.I.oy[src[u]];
-        e[u] = m.I.ux[src[u]];
-        f[u] = m.I.uy[src[u]];
-        h[u] = m.I.uz[src[u]];
-        id[u] = m.I.id[src[u]];
+#pragma unroll
+        for (int a = 0; a < 7; ++a) w[u][a] = src[u][a * MIX_TC];
       }
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u)
       if (on[u]) {
-        m.P.ox[dst[u]] = a[u];
-        m.P.oy[dst[u]] = bb[u];
-        m.P.ux[dst[u]] = e[u];
-        m.P.uy[dst[u]] = f[u];
-        m.P.uz[dst[u]] = h[u];
-        m.P.id[dst[u]] = id[u];
+#pragma unroll
+        for (int a = 0; a < 7; ++a) dst[u][a * MIX_TC] = w[u][a];
       }
   }
-  int nn = n + b;
-  if (nn > m.depth) {
-    atomicOr(d.err, EB_CAPACITY);
-    nn = m.depth;
-  }
+  const int nn = ok ? j + b : j;
   m.cnt[bin * MIX_TC + c] = nn;
-  m.icnt[bin * MIX_TC + c] = 0;
+  m.acnt[bin * MIX_TC + c] = 0;
+  // room for the next step: count + 2 x arrivals, maximum over the bin
+  int need = nn + 2 * b;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) need = max(need, __shfl_xor_sync(0xffffffffu, need, o));
+  if ((c & 31) == 0) wmax[c >> 5] = need;
+  __syncthreads();
+  if (c == 0) {
+    for (int w = 1; w < MIX_TC / 32; ++w) need = max(need, wmax[w]);
+    m.bneed[bin] = need;
+    if (8 * (long long)need > 7 * (long long)dep) atomicOr(m.grow, 1);
+  }
 }
 
 void mix_migrate2d(const Dev2D& d, cudaStream_t s) { k_mix_arrive<<<d.m.nbin, MIX_TC, 0, s>>>(d); }
+
+// copy of every column (cnt[bin][c] slots, all planes) from another layout into d.m's
+__global__ void __launch_bounds__(MIX_TC) k_mix_relayout(Dev2D d, const float* from_P, const long long* from_boff) {
+  const Mix2D& m = d.m;
+  const int bin = blockIdx.x, c = threadIdx.x;
+  const int n = m.cnt[bin * MIX_TC + c];
+  const float* src = from_P + (size_t)from_boff[bin] * MIX_PL + c;
+  float* dst = mix_slot(m, bin, 0, c);
+  for (int k = 0; k < n; ++k) {
+    float w[7];
+#pragma unroll
+    for (int a = 0; a < 7; ++a) w[a] = src[(size_t)k * MIX_PL + a * MIX_TC];
+#pragma unroll
+    for (int a = 0; a < 7; ++a) dst[(size_t)k * MIX_PL + a * MIX_TC] = w[a];
+  }
+}
+
+void mix_relayout2d(const Dev2D& d, const float* from_P, const long long* from_boff, cudaStream_t s) {
+  k_mix_relayout<<<d.m.nbin, MIX_TC, 0, s>>>(d, from_P, from_boff);
+}
+
+int mix_initial_depth(double n, double c_dt_dx) {
+  // count with a 25 % rise and 6 standard deviations of Poisson noise, plus room for the arrivals
+  // of the first steps (a particle crosses a face with probability <= c dt / dx per dimension)
+  const double arr = 0.5 * n * (c_dt_dx < 1.0 ? c_dt_dx : 1.0) + 4.0 * std::sqrt(n);
+  const double dep = 1.25 * n + 6.0 * std::sqrt(n) + 2.0 * arr + 16.0;
+  int k = ((int)std::ceil(dep) + 7) & ~7;
+  return k > MIX_MAX_DEPTH ? MIX_MAX_DEPTH : k;
+}
 
 // ---------------------------------------------------------------------------
 // reference layout -> columns: thread c copies the particles of cell c, which are
@@ -606,22 +651,24 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_put(Dev2D d, const double* aos, 
   const int* ccr = d.cc + (size_t)row * (g.nx + 1);
   const int first = ccr[gx];
   int n = ccr[gx + 1] - first;
-  if (n > m.depth) {
+  if (n > m.bdep[bin]) {
     atomicOr(d.err, EB_CAPACITY);
-    n = m.depth;
+    n = m.bdep[bin];
   }
   const double* rowp = aos + (size_t)((ty - ty0) * MIX_TS + ly) * np_host * ndim;
   const double dxi = d.ph.d_delx;
-  const size_t base = (size_t)bin * m.bcap + c;
+  float* const col = mix_slot(m, bin, 0, c);
   for (int k = 0; k < n; ++k) {
     const double* a = rowp + (size_t)(first + k) * ndim;
-    const size_t o = base + (size_t)k * MIX_TC;
-    m.P.ox[o] = (float)(a[0] * dxi - (double)(g.nxgs + gx));
-    m.P.oy[o] = (float)(a[1] * dxi - (double)(g.nygs + gy));
-    m.P.ux[o] = (float)a[2];
-    m.P.uy[o] = (float)a[3];
-    m.P.uz[o] = (float)a[4];
-    m.P.id[o] = ndim > 5 ? __double_as_longlong(a[5]) : 0;
+    float* o = col + (size_t)k * MIX_PL;
+    o[MIX_OX] = (float)(a[0] * dxi - (double)(g.nxgs + gx));
+    o[MIX_OY] = (float)(a[1] * dxi - (double)(g.nygs + gy));
+    o[MIX_UX] = (float)a[2];
+    o[MIX_UY] = (float)a[3];
+    o[MIX_UZ] = (float)a[4];
+    const long long id = ndim > 5 ? __double_as_longlong(a[5]) : 0;
+    o[MIX_IDLO] = __int_as_float((int)(unsigned)(id & 0xffffffffll));
+    o[MIX_IDHI] = __int_as_float((int)(unsigned)((unsigned long long)id >> 32));
   }
   m.cnt[bin * MIX_TC + c] = n;
 }
@@ -680,7 +727,7 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_get(Dev2D d, double* aos, int nd
   const int gx = tx * MIX_TS + lx, gy = ty * MIX_TS + ly;
   const int first = d.cc[((size_t)isp * g.ny + gy) * (g.nx + 1) + gx];
   const int n = m.cnt[bin * MIX_TC + c];
-  const size_t base = (size_t)bin * m.bcap + c;
+  const float* col = mix_slot(m, bin, 0, c);
   const double dx = d.ph.delx;
   double* rowp = aos + (size_t)((ty - ty0) * MIX_TS + ly) * np_host * ndim;
   for (int k = 0; k < n; ++k) {
@@ -689,14 +736,18 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_get(Dev2D d, double* aos, int nd
       atomicOr(d.err, EB_CAPACITY);
       break;
     }
-    const size_t o = base + (size_t)k * MIX_TC;
+    const float* o = col + (size_t)k * MIX_PL;
     double* a = rowp + (size_t)pos * ndim;
-    a[0] = ((double)(g.nxgs + gx) + (double)m.P.ox[o]) * dx;
-    a[1] = ((double)(g.nygs + gy) + (double)m.P.oy[o]) * dx;
-    a[2] = (double)m.P.ux[o];
-    a[3] = (double)m.P.uy[o];
-    a[4] = (double)m.P.uz[o];
-    if (ndim > 5) a[5] = __longlong_as_double(m.P.id[o]);
+    a[0] = ((double)(g.nxgs + gx) + (double)o[MIX_OX]) * dx;
+    a[1] = ((double)(g.nygs + gy) + (double)o[MIX_OY]) * dx;
+    a[2] = (double)o[MIX_UX];
+    a[3] = (double)o[MIX_UY];
+    a[4] = (double)o[MIX_UZ];
+    if (ndim > 5) {
+      const unsigned long long id = ((unsigned long long)(unsigned)__float_as_int(o[MIX_IDHI]) << 32) |
+                                    (unsigned)__float_as_int(o[MIX_IDLO]);
+      a[5] = __longlong_as_double((long long)id);
+    }
   }
 }
 
@@ -719,8 +770,9 @@ __global__ void k_mix_load(Dev2D d, int ppc, unsigned long long seed, double dri
   const int tx = tile % m.ntx, ty = tile / m.ntx;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;  // = kk * 256 + c
   const int c = s % MIX_TC, kk = s / MIX_TC;
-  if (kk == 0) m.cnt[bin * MIX_TC + c] = ppc < m.depth ? ppc : m.depth;
-  if (kk >= ppc || kk >= m.depth) return;
+  const int dep = m.bdep[bin];
+  if (kk == 0) m.cnt[bin * MIX_TC + c] = ppc < dep ? ppc : dep;
+  if (kk >= ppc || kk >= dep) return;
   const int lx = c & (MIX_TS - 1), ly = c >> 4;
   const int cx = tx * MIX_TS + lx, jj = ty * MIX_TS + ly;
   const int k = cx * ppc + kk;
@@ -728,22 +780,24 @@ __global__ void k_mix_load(Dev2D d, int ppc, unsigned long long seed, double dri
   const uint4 rp = philox4x32(make_uint4((unsigned)k, (unsigned)jj, 0u, 0u), key);
   const uint4 r1 = philox4x32(make_uint4((unsigned)k, (unsigned)jj, 1u + 2u * isp, 0u), key);
   const uint4 r2 = philox4x32(make_uint4((unsigned)k, (unsigned)jj, 2u + 2u * isp, 0u), key);
-  const size_t o = (size_t)bin * m.bcap + s;
+  float* const o = mix_slot(m, bin, kk, c);
   float ox = (float)(1.0 - u01(rp.x, rp.y)), oy = (float)(1.0 - u01(rp.z, rp.w));
   if (ox >= 1.f) ox = 0.f;
   if (oy >= 1.f) oy = 0.f;
-  m.P.ox[o] = ox;
-  m.P.oy[o] = oy;
+  o[MIX_OX] = ox;
+  o[MIX_OY] = oy;
   const double sd = isp == 0 ? u_thi : u_the;
   const double twopi = 6.283185307179586;
   const double a1 = u01(r1.x, r1.y), b1 = u01(r1.z, r1.w), a2 = u01(r2.x, r2.y), b2 = u01(r2.z, r2.w);
   const double rad1 = sqrt(-2.0 * log(a1)), rad2 = sqrt(-2.0 * log(a2));
   double u[3] = {sd * rad1 * cos(twopi * b1), sd * rad1 * sin(twopi * b1), sd * rad2 * cos(twopi * b2)};
   if (isp == 1 && drift != 0.0) u[axis] += (k % 2 == 0) ? drift : -drift;
-  m.P.ux[o] = (float)u[0];
-  m.P.uy[o] = (float)u[1];
-  m.P.uz[o] = (float)u[2];
-  m.P.id[o] = -((long long)jj * g.nx * ppc + k + 1);
+  o[MIX_UX] = (float)u[0];
+  o[MIX_UY] = (float)u[1];
+  o[MIX_UZ] = (float)u[2];
+  const long long id = -((long long)jj * g.nx * ppc + k + 1);
+  o[MIX_IDLO] = __int_as_float((int)(unsigned)(id & 0xffffffffll));
+  o[MIX_IDHI] = __int_as_float((int)(unsigned)((unsigned long long)id >> 32));
 }
 
 void mix_load_weibel2d(const Dev2D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
@@ -762,10 +816,10 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_energy(Dev2D d) {
   for (int tile = blockIdx.x; tile < m.ntile; tile += gridDim.x) {
     const int bin = tile * d.ph.nsp + isp;
     const int n = m.cnt[bin * MIX_TC + threadIdx.x];
-    const size_t base = (size_t)bin * m.bcap + threadIdx.x;
+    const float* col = mix_slot(m, bin, 0, threadIdx.x);
     for (int k = 0; k < n; ++k) {
-      const size_t o = base + (size_t)k * MIX_TC;
-      const double a = m.P.ux[o], b = m.P.uy[o], e = m.P.uz[o];
+      const float* o = col + (size_t)k * MIX_PL;
+      const double a = o[MIX_UX], b = o[MIX_UY], e = o[MIX_UZ];
       v += rr * (sqrt(1.0 + (a * a + b * b + e * e) / (c * c)) - 1.0);
     }
   }

@@ -62,19 +62,22 @@ struct Parts64 {
 
 // ---- mixed-precision particle storage (2D) ----
 // Particles live in bins of one 16 x 16-cell tile and one species, bin = tile * nsp + isp,
-// tile = ty * ntx + tx.  Inside a bin every cell owns a column of `depth` slots:
-// slot (k, c) = k * 256 + c for cell c = ly * 16 + lx, so the cell of a particle is implicit.
-// Position = that cell plus an FP32 offset in [0, 1) per dimension; momenta FP32; 64-bit id.
-// Particles that change cell in a push go to the inbox of their new cell (same [k][256] layout,
-// `icap` slots per cell), tagged with a key that orders a cell's arrivals deterministically.
+// tile = ty * ntx + tx.  Inside a bin every cell owns a column of bdep[bin] slots:
+// slot (k, c) for cell c = ly * 16 + lx lies in layer boff[bin] + k, so the cell of a particle
+// is implicit.  Position = that cell plus an FP32 offset in [0, 1) per dimension; momenta FP32;
+// 64-bit id.  Each 256-slot layer stores its components one after another as 32-bit planes
+// (ox, oy, ux, uy, uz, id low word, id high word, arrival key), so one address per slot reaches
+// every component through fixed offsets while a warp still reads 128 contiguous bytes.
+// A push compacts each column in place (stayers to the bottom) and writes the particles that
+// change cell to the top of their new cell's column, from slot bdep - 1 downwards; the arrival
+// kernel then moves them, in key order, to just above the stayers.  The depth of a bin grows
+// (the host re-lays out the bins) when its columns come close to full.
 constexpr int MIX_TS = 16;
 constexpr int MIX_TC = MIX_TS * MIX_TS;
-constexpr int MIX_MAX_DEPTH = 1024;
-
-struct PartsMix {
-  float *ox, *oy, *ux, *uy, *uz;
-  long long* id;
-};
+constexpr int MIX_MAX_DEPTH = 32767;  // slot indices fit the 16-bit field of the arrival key
+constexpr int MIX_OX = 0, MIX_OY = MIX_TC, MIX_UX = 2 * MIX_TC, MIX_UY = 3 * MIX_TC, MIX_UZ = 4 * MIX_TC;
+constexpr int MIX_IDLO = 5 * MIX_TC, MIX_IDHI = 6 * MIX_TC, MIX_KEY = 7 * MIX_TC;
+constexpr int MIX_PL = 8 * MIX_TC;   // 32-bit words per layer
 
 struct Mix2D {
   // fixed-point current accumulation of the push: v = hi / s1 + lo / s2 with int32 hi, lo
@@ -85,16 +88,21 @@ struct Mix2D {
   float k_fac1[2], k_fac2[2], k_qdd[2], k_q[2];
   float k_dtdx, k_c, k_ic2;
   int ntx, nty, ntile, nbin;
-  int depth;         // slots per cell column (<= MIX_MAX_DEPTH)
-  int bcap;          // slots per bin = 256 * depth
-  int icap;          // inbox slots per cell
-  PartsMix P;        // [nbin][depth][256]
-  int* cnt;          // [nbin][256] particles per cell column
-  PartsMix I;        // [nbin][icap][256] arrivals of the last push
-  int* ikey;         // [nbin][icap][256] arrival order key: direction group << 16 | source slot
-  int* icnt;         // [nbin][256] arrivals per cell (zero between steps)
+  float* P;            // particle layers, MIX_PL words each
+  long long* boff;     // [nbin] first layer of each bin
+  int* bdep;           // [nbin] slots per cell column of each bin
+  int* cnt;            // [nbin][256] particles per column (the push's input count)
+  int* ccnt;           // [nbin][256] stayers after the push's compaction
+  int* acnt;           // [nbin][256] arrivals written by the push (zero between steps)
+  int* bneed;          // [nbin] largest count + 2 x arrivals over a bin's columns in the last step
+  int* grow;           // nonzero when some bin's need passed 7/8 of its depth
   unsigned long long* ujx;  // [3][ny+4][nx+4] current in fixed point (units 1/fx_s2), summed exactly
 };
+
+// word of slot (k, c) of bin `bin` in the first plane; the other components at + MIX_OY ... + MIX_KEY
+__device__ inline float* mix_slot(const Mix2D& m, int bin, int k, int c) {
+  return m.P + ((size_t)m.boff[bin] + k) * MIX_PL + c;
+}
 
 struct CGState {
   double sum_g, eps, sumr_g, sum2_g, sum1_g, av, bv;
@@ -162,6 +170,10 @@ void field_ref_to_soa(const double* ref, double* soa, int ncomp, int nslab, cuda
 void field_soa_to_ref(const double* soa, double* ref, int ncomp, int nslab, cudaStream_t s);
 // ---- mixed-precision path (mixed2d.cu) ----
 int mix_setup2d(const Dev2D& d, void* tmap_out);  // CUtensorMap of uf for the TMA tile loads; kernel attributes
+// copy every column of the layout `from` (P, boff, bdep) into the layout of d.m (counts unchanged)
+void mix_relayout2d(const Dev2D& d, const float* from_P, const long long* from_boff, cudaStream_t s);
+// initial slots per column for a column of n particles (with the room the first pushes need)
+int mix_initial_depth(double n, double c_dt_dx);
 void mix_push_deposit2d(const Dev2D& d, const void* tmap, cudaStream_t s);
 void mix_curre_refresh2d(const Dev2D& d, cudaStream_t s);
 void mix_migrate2d(const Dev2D& d, cudaStream_t s);
