@@ -54,15 +54,16 @@ def lib():
         L.orc2d_energy.argtypes = [vp, dp, dp, ip, dp]
         if hasattr(L, "orc3d_create"):
             L.orc3d_create.restype = vp
-            L.orc3d_create.argtypes = [i] * 13 + [d, d, d, dp, dp, d, i]
+            L.orc3d_create.argtypes = [i] * 13 + [d, d, d, dp, dp, d]
             L.orc3d_destroy.argtypes = [vp]
             L.orc3d_set_threads.argtypes = [vp, i]
             L.orc3d_cg_control.argtypes = [vp, ip, i]
             L.orc3d_cg_iters.argtypes = [vp, ip]
-            for n in ("orc3d_get_df", "orc3d_set_df", "orc3d_get_uj"):
+            for n in ("orc3d_get_df", "orc3d_get_uj"):
                 getattr(L, n).argtypes = [vp, dp]
             L.orc3d_particle_solv.argtypes = [vp, dp, dp, dp, ip, i, i]
             L.orc3d_ele_cur.argtypes = [vp, dp, dp, dp, ip, i, i]
+            L.orc3d_bc_curre.argtypes = [vp, dp, i, i]
             L.orc3d_field_fdtd_i.argtypes = [vp, dp, dp, dp, ip, i, i]
             L.orc3d_bc_particle_x.argtypes = [vp, dp, ip]
             L.orc3d_bc_particle_yz.argtypes = [vp, dp, ip]
@@ -179,5 +180,98 @@ class Oracle2D:
         if self.bc == BC_PERIODIC:
             rc = rc or self.bc_particle_x(st.gp, st.np2)
         rc = rc or self.bc_particle_y(st.gp, st.np2)
+        rc = rc or self.sort_bucket(st.up, st.gp, st.cumcnt, st.np2)
+        return rc
+
+
+class Oracle3D:
+    """3D oracle instance (periodic boundaries): the SAVEd module state of particle/field/sort/boundary."""
+
+    def __init__(self, *, nx, ny, nz, np_cap, nsp=2, ndim=7, delx=1.0, delt=0.5, c=1.0, q, r, gfac=0.501,
+                 threads=1, nxgs=2, nygs=2, nzgs=2):
+        self.nx, self.ny, self.nz, self.np, self.nsp, self.ndim = nx, ny, nz, np_cap, nsp, ndim
+        self.nxgs, self.nxge = nxgs, nxgs + nx - 1
+        self.nygs, self.nyge = nygs, nygs + ny - 1
+        self.nzgs, self.nzge = nzgs, nzgs + nz - 1
+        self.nxs, self.nxe = self.nxgs, self.nxge
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        self._h = lib().orc3d_create(ndim, np_cap, nsp, self.nxgs, self.nxge, self.nygs, self.nyge, self.nzgs,
+                                     self.nzge, self.nygs, self.nyge, self.nzgs, self.nzge, delx, delt, c,
+                                     _p(q, np.float64), _p(r, np.float64), gfac)
+        lib().orc3d_set_threads(self._h, threads)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().orc3d_destroy(h)
+            self._h = None
+
+    def set_threads(self, n):
+        lib().orc3d_set_threads(self._h, n)
+
+    def cg_control(self, fixed=None, ite_max=100):
+        if fixed is None:
+            lib().orc3d_cg_control(self._h, None, ite_max)
+        else:
+            f = np.ascontiguousarray(fixed, dtype=np.int32)
+            lib().orc3d_cg_control(self._h, _p(f, np.int32), ite_max)
+
+    def cg_iters(self):
+        out = np.zeros(3, np.int32)
+        lib().orc3d_cg_iters(self._h, _p(out, np.int32))
+        return out
+
+    def field_shape(self, ncomp=6):
+        return (ncomp, self.nx + 4, self.ny + 4, self.nz + 4)
+
+    def get_df(self):
+        out = np.zeros(self.field_shape(6), order="F")
+        lib().orc3d_get_df(self._h, _p(out, np.float64))
+        return out
+
+    def get_uj(self):
+        out = np.zeros(self.field_shape(3), order="F")
+        lib().orc3d_get_uj(self._h, _p(out, np.float64))
+        return out
+
+    def particle_solv(self, gp, up, uf, cumcnt):
+        return lib().orc3d_particle_solv(self._h, _p(gp, np.float64), _p(up, np.float64), _p(uf, np.float64),
+                                         _p(cumcnt, np.int32), self.nxs, self.nxe)
+
+    def ele_cur(self, uj, up, gp, cumcnt):
+        return lib().orc3d_ele_cur(self._h, _p(uj, np.float64), _p(up, np.float64), _p(gp, np.float64),
+                                   _p(cumcnt, np.int32), self.nxs, self.nxe)
+
+    def bc_curre(self, uj):
+        return lib().orc3d_bc_curre(self._h, _p(uj, np.float64), self.nxs, self.nxe)
+
+    def field_fdtd_i(self, uf, up, gp, cumcnt):
+        return lib().orc3d_field_fdtd_i(self._h, _p(uf, np.float64), _p(up, np.float64), _p(gp, np.float64),
+                                        _p(cumcnt, np.int32), self.nxs, self.nxe)
+
+    def bc_particle_x(self, up, np2):
+        return lib().orc3d_bc_particle_x(self._h, _p(up, np.float64), _p(np2, np.int32))
+
+    def bc_particle_yz(self, up, np2):
+        return lib().orc3d_bc_particle_yz(self._h, _p(up, np.float64), _p(np2, np.int32))
+
+    def sort_bucket(self, gp, up, cumcnt, np2):
+        return lib().orc3d_sort_bucket(self._h, _p(gp, np.float64), _p(up, np.float64), _p(cumcnt, np.int32),
+                                       _p(np2, np.int32), self.nxs, self.nxe)
+
+    def energy(self, up, uf, np2):
+        out = np.zeros(self.nsp + 2)
+        lib().orc3d_energy(self._h, _p(up, np.float64), _p(uf, np.float64), _p(np2, np.int32),
+                           _p(out, np.float64))
+        return out
+
+    def step(self, st):
+        """One reference time step on a State3D, in the driver's call order
+        (3d/proj/weibel/app.f90:103-108)."""
+        rc = self.particle_solv(st.gp, st.up, st.uf, st.cumcnt)
+        rc = rc or self.field_fdtd_i(st.uf, st.up, st.gp, st.cumcnt)
+        rc = rc or self.bc_particle_x(st.gp, st.np2)
+        rc = rc or self.bc_particle_yz(st.gp, st.np2)
         rc = rc or self.sort_bucket(st.up, st.gp, st.cumcnt, st.np2)
         return rc

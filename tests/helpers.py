@@ -145,3 +145,126 @@ def closed_form_plan(dirs, ny):
                 m += 1
         out.append(seq)
     return out
+
+
+# ---------------------------------------------------------------------------
+# 3D
+# ---------------------------------------------------------------------------
+def small_plasma3d(nx=8, ny=6, nz=5, ppc=4, seed=3, **kw):
+    from wumingpic_gb300.loader import Plasma3D
+    kw.setdefault("drift", 0.5)
+    kw.setdefault("u_the", 0.05)
+    return Plasma3D(nx=nx, ny=ny, nz=nz, ppc=ppc, seed=seed, **kw)
+
+
+def small_case3d(**kw):
+    from wumingpic_gb300.loader import load_weibel3d
+    p = small_plasma3d(**kw)
+    return p, load_weibel3d(p)
+
+
+def rho3d(p, up, np2, q):
+    """Charge density on the periodic interior grid (nx, ny, nz), quadratic spline, cell int(x)."""
+    R = np.zeros((p.nx, p.ny, p.nz))
+    for isp in range(p.nsp):
+        for kk in range(p.nz):
+            for jj in range(p.ny):
+                n = np2[jj, kk, isp]
+                pos = [up[d, :n, jj, kk, isp] / p.delx for d in range(3)]
+                idx = [np.floor(a).astype(int) for a in pos]
+                sh = []
+                for d in range(3):
+                    h = pos[d] - 0.5 - idx[d]
+                    sh.append([0.5 * (0.5 - h) ** 2, 0.75 - h ** 2, 0.5 * (0.5 + h) ** 2])
+                org = (p.nxgs, p.nygs, p.nzgs)
+                dims = (p.nx, p.ny, p.nz)
+                for a in range(3):
+                    for b in range(3):
+                        for c in range(3):
+                            np.add.at(R, tuple((idx[d] + (a, b, c)[d] - 1 - org[d]) % dims[d] for d in range(3)),
+                                      q[isp] * sh[0][a] * sh[1][b] * sh[2][c])
+    return R
+
+
+def continuity_residual3d(p, q, up0, gp1, np2, uj):
+    """(rho1 - rho0) dx/dt + div J on the periodic interior; uj already folded."""
+    r0 = rho3d(p, up0, np2, q)
+    r1 = rho3d(p, gp1, np2, q)
+    J = uj[:, 2:-2, 2:-2, 2:-2]
+    res = (r1 - r0) * p.delx / p.delt
+    for d in range(3):
+        res = res + (np.roll(J[d], -1, d) - J[d])
+    return np.abs(res).max(), np.abs(r1 - r0).max() * p.delx / p.delt
+
+
+def literal_particle_yz(up, np2, p):
+    """Pure-Python restatement of boundary_periodic__particle_yz
+    (3d/common/boundary_periodic.f90:104-455) on one rank, single thread: wrap, buffer per
+    destination row (ghost rows included), y transfers for all z rows, then z transfers,
+    then hole filling.  Operates in place on the reference-layout arrays."""
+    nys, nye, nzs, nze = p.nygs, p.nyge, p.nzgs, p.nzge
+    ndim = up.shape[0]
+    for isp in range(p.nsp):
+        bff = {}
+        flags = {}
+        for k in range(nzs, nze + 1):
+            for j in range(nys, nye + 1):
+                fl = []
+                for ii in range(1, np2[j - nys, k - nzs, isp] + 1):
+                    a = up[:, ii - 1, j - nys, k - nzs, isp]
+                    jpos = int(a[1] / p.delx)
+                    kpos = int(a[2] / p.delx)
+                    if not (jpos == j and kpos == k):
+                        if jpos <= p.nygs - 1:
+                            a[1] = a[1] + (p.nyge - p.nygs + 1) * p.delx
+                        elif jpos >= p.nyge + 1:
+                            a[1] = a[1] - (p.nyge - p.nygs + 1) * p.delx
+                        if kpos <= p.nzgs - 1:
+                            a[2] = a[2] + (p.nzge - p.nzgs + 1) * p.delx
+                        elif kpos >= p.nzge + 1:
+                            a[2] = a[2] - (p.nzge - p.nzgs + 1) * p.delx
+                        bff.setdefault((jpos, kpos), []).append(a.copy())
+                        fl.append(ii)
+                flags[(j, k)] = fl
+        for k in range(nzs - 1, nze + 2):
+            bff.setdefault((nye, k), []).extend(bff.pop((nys - 1, k), []))
+        for k in range(nzs - 1, nze + 2):
+            bff.setdefault((nys, k), []).extend(bff.pop((nye + 1, k), []))
+        for j in range(nys, nye + 1):
+            bff.setdefault((j, nze), []).extend(bff.pop((j, nzs - 1), []))
+        for j in range(nys, nye + 1):
+            bff.setdefault((j, nzs), []).extend(bff.pop((j, nze + 1), []))
+        for k in range(nzs, nze + 1):
+            for j in range(nys, nye + 1):
+                row = up[:, :, j - nys, k - nzs, isp]
+                n2 = int(np2[j - nys, k - nzs, isp])
+                fl = flags[(j, k)]
+                arr = bff.get((j, k), [])
+                iii = 0
+                cnt = len(arr)
+                cnt_tmp = len(fl)
+                ii = 1
+                while ii <= len(fl):
+                    if cnt == 0:
+                        if n2 < fl[ii - 1]:
+                            break
+                        done = False
+                        while n2 == fl[cnt_tmp - 1]:
+                            n2 -= 1
+                            if n2 < fl[ii - 1]:
+                                done = True
+                                break
+                            cnt_tmp -= 1
+                        if done:
+                            break
+                        row[:, fl[ii - 1] - 1] = row[:, n2 - 1]
+                        n2 -= 1
+                    else:
+                        row[:, fl[ii - 1] - 1] = arr[iii]
+                        iii += 1
+                        cnt -= 1
+                    ii += 1
+                for m in range(cnt):
+                    row[:, n2 + m] = arr[iii + m]
+                np2[j - nys, k - nzs, isp] = n2 + cnt
+    return np2

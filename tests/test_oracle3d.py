@@ -1,0 +1,189 @@
+"""CPU tests of the 3D oracle (oracle/oracle3d.cpp) against physical invariants and
+against an independent restatement of the 3D migration.  The reference ships no
+golden vectors for this path, so these invariants are what pins the oracle."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Oracle3D
+from tests.helpers import continuity_residual3d, literal_particle_yz, small_case3d
+
+
+def make_oracle3d(p, **kw):
+    q, r = p.charges()
+    return Oracle3D(nx=p.nx, ny=p.ny, nz=p.nz, np_cap=p.np_cap, q=q, r=r, delt=p.delt, delx=p.delx, c=p.c,
+                    gfac=p.gfac, **kw)
+
+
+def test_charge_conservation_multistep_3d():
+    """Esirkepov deposition in 3D: (rho1 - rho0)/dt + div J = 0 to round-off every step."""
+    p, st = small_case3d(nx=6, ny=5, nz=4, ppc=4, seed=11, u_the=0.2)
+    q, _ = p.charges()
+    o = make_oracle3d(p)
+    for _ in range(4):
+        up0 = st.up.copy(order="F")
+        assert o.particle_solv(st.gp, st.up, st.uf, st.cumcnt) == 0
+        assert o.field_fdtd_i(st.uf, st.up, st.gp, st.cumcnt) == 0
+        res, scale = continuity_residual3d(p, q, up0, st.gp, st.np2, o.get_uj())
+        assert res <= 1e-12 * scale, (res, scale)
+        assert o.bc_particle_x(st.gp, st.np2) == 0
+        assert o.bc_particle_yz(st.gp, st.np2) == 0
+        assert o.sort_bucket(st.up, st.gp, st.cumcnt, st.np2) == 0
+    assert st.np2.sum() == p.n_particles
+
+
+def test_free_streaming_push_is_exact_3d():
+    p, st = small_case3d(seed=5)
+    st.uf[...] = 0.0
+    o = make_oracle3d(p)
+    assert o.particle_solv(st.gp, st.up, st.uf, st.cumcnt) == 0
+    n = st.np2[0, 0, 1]
+    u = st.up[3:6, :n, 0, 0, 1]
+    np.testing.assert_array_equal(st.gp[3:6, :n, 0, 0, 1], u)
+    gam = 1.0 / np.sqrt(1.0 + (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) / (p.c * p.c))
+    for d in range(3):
+        np.testing.assert_array_equal(st.gp[d, :n, 0, 0, 1], st.up[d, :n, 0, 0, 1] + u[d] * p.delt * gam)
+    np.testing.assert_array_equal(st.gp[6].view(np.int64), st.up[6].view(np.int64))
+
+
+def test_gyration_in_uniform_bx_3d():
+    """Uniform Bx, no E: |u| conserved, rotation by 2 atan(q B dt / (2 m gamma c)) about x."""
+    p, st = small_case3d(seed=9, u_the=0.2, u_thi=0.1)
+    q, r = p.charges()
+    bx = 0.3
+    st.uf[...] = 0.0
+    st.uf[0] = bx
+    o = make_oracle3d(p)
+    assert o.particle_solv(st.gp, st.up, st.uf, st.cumcnt) == 0
+    for isp in range(p.nsp):
+        n = st.np2[0, 0, isp]
+        u0 = st.up[3:6, :n, 0, 0, isp]
+        u1 = st.gp[3:6, :n, 0, 0, isp]
+        np.testing.assert_allclose(np.linalg.norm(u1, axis=0), np.linalg.norm(u0, axis=0), rtol=1e-14)
+        gc = np.sqrt(p.c ** 2 + (u0 ** 2).sum(0))
+        theta = 2 * np.arctan(q[isp] / r[isp] * 0.5 * p.delt * bx / gc)
+        ang = np.arctan2(u0[1] * u1[2] - u0[2] * u1[1], u0[1] * u1[1] + u0[2] * u1[2])
+        np.testing.assert_allclose(ang, -theta, rtol=1e-10, atol=1e-14)
+        np.testing.assert_allclose(u1[0], u0[0], rtol=1e-15)
+
+
+def test_cg_solves_the_implicit_system_3d():
+    """After field__fdtd_i the B increment satisfies (f4 - N) dB = f5 gkl to the CG tolerance."""
+    p, st = small_case3d(nx=8, ny=8, nz=6, ppc=4, seed=21, u_the=0.2)
+    o = make_oracle3d(p)
+    uf0 = st.uf.copy(order="F")
+    # a nonzero field so that every term of gkl contributes
+    rng = np.random.default_rng(0)
+    uf0[:, 2:-2, 2:-2, 2:-2] = 1e-3 * rng.standard_normal(uf0[:, 2:-2, 2:-2, 2:-2].shape)
+    # periodic ghosts of the seeded field
+    core = uf0[:, 2:-2, 2:-2, 2:-2]
+    uf0[...] = np.pad(core, ((0, 0), (2, 2), (2, 2), (2, 2)), mode="wrap")
+    st.uf[...] = uf0
+    assert o.particle_solv(st.gp, st.up, st.uf, st.cumcnt) == 0
+    assert o.field_fdtd_i(st.uf, st.up, st.gp, st.cumcnt) == 0
+    uj = o.get_uj()
+    df = o.get_df()
+    f1 = p.c * p.delt / p.delx
+    f2 = p.gfac * f1 * f1
+    f3 = 4 * math.pi * p.delx / p.c
+    f5 = (p.delx / (p.c * p.delt * p.gfac)) ** 2
+    f4 = 6 + f5
+    U = uf0[:, 2:-2, 2:-2, 2:-2]
+    J = uj[:, 2:-2, 2:-2, 2:-2]
+
+    def lap(a):
+        return sum(np.roll(a, s, ax) for ax in range(3) for s in (1, -1)) - 6 * a
+
+    def sm(a, ax):  # a(i-1) along axis ax
+        return np.roll(a, 1, ax)
+    X, Y, Z = 0, 1, 2
+    gkl = np.zeros((3,) + U.shape[1:])
+    gkl[0] = f2 * (lap(U[0]) + f3 * (-sm(J[2], Y) + J[2] + sm(J[1], Z) - J[1])) - f1 * (-sm(U[5], Y) + U[5] + sm(U[4], Z) - U[4])
+    gkl[1] = f2 * (lap(U[1]) + f3 * (-sm(J[0], Z) + J[0] + sm(J[2], X) - J[2])) - f1 * (-sm(U[3], Z) + U[3] + sm(U[5], X) - U[5])
+    gkl[2] = f2 * (lap(U[2]) + f3 * (-sm(J[1], X) + J[1] + sm(J[0], Y) - J[0])) - f1 * (-sm(U[4], X) + U[4] + sm(U[3], Y) - U[3])
+    for l in range(3):
+        b = f5 * gkl[l]
+        x = df[l, 2:-2, 2:-2, 2:-2]
+        res = b - (f4 * x - (lap(x) + 6 * x))
+        assert np.linalg.norm(res) <= 2e-6 * np.linalg.norm(b) + 1e-300
+    assert (o.cg_iters() > 0).all()
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_particle_yz_matches_literal_restatement(seed):
+    """The oracle's 3D migration equals a literal pure-Python restatement, particle by particle."""
+    p, st = small_case3d(nx=5, ny=4, nz=3, ppc=5, seed=seed, u_the=0.6, drift=0.0)
+    o = make_oracle3d(p)
+    # move particles by up to one cell in y and z (and across the periodic faces)
+    rng = np.random.default_rng(seed)
+    for isp in range(p.nsp):
+        for kk in range(p.nz):
+            for jj in range(p.ny):
+                n = st.np2[jj, kk, isp]
+                st.up[1, :n, jj, kk, isp] += rng.uniform(-0.9, 0.9, n)
+                st.up[2, :n, jj, kk, isp] += rng.uniform(-0.9, 0.9, n)
+    a = st.up.copy(order="F")
+    na = st.np2.copy(order="F")
+    assert o.bc_particle_yz(a, na) == 0
+    b = st.up.copy(order="F")
+    nb = st.np2.copy(order="F")
+    literal_particle_yz(b, nb, p)
+    np.testing.assert_array_equal(na, nb)
+    for isp in range(p.nsp):
+        for kk in range(p.nz):
+            for jj in range(p.ny):
+                n = na[jj, kk, isp]
+                np.testing.assert_array_equal(a[:, :n, jj, kk, isp].view(np.int64), b[:, :n, jj, kk, isp].view(np.int64))
+                # every particle now lies in its row
+                assert (np.floor(a[1, :n, jj, kk, isp]).astype(int) == p.nygs + jj).all()
+                assert (np.floor(a[2, :n, jj, kk, isp]).astype(int) == p.nzgs + kk).all()
+    assert na.sum() == st.np2.sum()
+
+
+def test_sort_and_bookkeeping_3d():
+    p, st = small_case3d(nx=6, ny=4, nz=4, ppc=4, seed=7, u_the=0.3)
+    o = make_oracle3d(p)
+    ids0 = np.sort(np.concatenate([st.up[6, :st.np2[j, k, s], j, k, s].view(np.int64)
+                                   for s in range(p.nsp) for k in range(p.nz) for j in range(p.ny)]))
+    for _ in range(5):
+        assert o.step(st) == 0
+    ids = np.sort(np.concatenate([st.up[6, :st.np2[j, k, s], j, k, s].view(np.int64)
+                                  for s in range(p.nsp) for k in range(p.nz) for j in range(p.ny)]))
+    np.testing.assert_array_equal(ids, ids0)
+    for s in range(p.nsp):
+        for k in range(p.nz):
+            for j in range(p.ny):
+                n = st.np2[j, k, s]
+                cell = np.floor(st.up[0, :n, j, k, s]).astype(int)
+                assert (np.diff(cell) >= 0).all()
+                cc = np.searchsorted(cell, np.arange(p.nxgs, p.nxge + 2), side="left")
+                np.testing.assert_array_equal(st.cumcnt[:, j, k, s], cc)
+
+
+def test_energy_sums_3d():
+    p, st = small_case3d(seed=13)
+    rng = np.random.default_rng(1)
+    st.uf[...] = rng.standard_normal(st.uf.shape)
+    o = make_oracle3d(p)
+    e = o.energy(st.up, st.uf, st.np2)
+    q, r = p.charges()
+    for s in range(p.nsp):
+        u = np.concatenate([st.up[3:6, :st.np2[j, k, s], j, k, s] for k in range(p.nz) for j in range(p.ny)], axis=1)
+        ke = (r[s] * (np.sqrt(1 + (u ** 2).sum(0) / p.c ** 2) - 1)).sum()
+        np.testing.assert_allclose(e[s], ke, rtol=1e-12)
+    U = st.uf[:, 2:-2, 2:-2, 2:-2]
+    np.testing.assert_allclose(e[p.nsp], (U[3:] ** 2).sum() / (8 * math.pi), rtol=1e-12)
+    np.testing.assert_allclose(e[p.nsp + 1], (U[:3] ** 2).sum() / (8 * math.pi), rtol=1e-12)
+
+
+def test_threads_do_not_change_push_and_fields_3d():
+    p, st = small_case3d(nx=6, ny=6, nz=4, ppc=4, seed=17, u_the=0.2)
+    s1 = st.copy()
+    o1 = make_oracle3d(p, threads=1)
+    o4 = make_oracle3d(p, threads=4)
+    for _ in range(2):
+        assert o1.step(st) == 0
+        assert o4.step(s1) == 0
+    np.testing.assert_allclose(s1.uf, st.uf, rtol=0, atol=1e-12 * np.abs(st.uf).max())
+    np.testing.assert_array_equal(s1.np2, st.np2)

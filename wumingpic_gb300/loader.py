@@ -157,3 +157,128 @@ def config_weibel2d(size="small", seed=12345):
     if size == "cfg4":
         return Plasma2D(nx=512, ny=512, ppc=32, drift=0.3, u_the=0.05, seed=seed)
     return Plasma2D(nx=16, ny=12, ppc=4, drift=0.5, u_the=0.05, seed=seed)
+
+
+# ---------------------------------------------------------------------------
+# 3D (3d/proj/weibel/app.f90 conventions: ndim = 7, (x, y, z, ux, uy, uz, id),
+# rows (j, k) of x-sorted particles, uf(6, nxgs-2:nxge+2, nys-2:nye+2, nzs-2:nze+2))
+# ---------------------------------------------------------------------------
+@dataclass
+class Plasma3D:
+    """Physics/grid parameters of one 3D run (periodic in x, y, z)."""
+    nx: int
+    ny: int
+    nz: int
+    ppc: int
+    mass_ratio: float = 16.0
+    omega_pe: float = 0.1
+    drift: float = 0.5
+    drift_axis: int = 0           # 0 = x, 1 = y, 2 = z (the 3D Weibel configuration drifts along x)
+    u_the: float = 0.05
+    u_thi: float = 0.0
+    delx: float = 1.0
+    delt: float = 0.5
+    c: float = 1.0
+    gfac: float = 0.501
+    np_slack: float = 1.5
+    nsp: int = 2
+    ndim: int = 7
+    seed: int = 12345
+    nxgs: int = 2
+    nygs: int = 2
+    nzgs: int = 2
+
+    @property
+    def nxge(self):
+        return self.nxgs + self.nx - 1
+
+    @property
+    def nyge(self):
+        return self.nygs + self.ny - 1
+
+    @property
+    def nzge(self):
+        return self.nzgs + self.nz - 1
+
+    @property
+    def np_cap(self):
+        return int(math.ceil(self.np_slack * self.ppc * self.nx))
+
+    def charges(self):
+        r = np.array([self.mass_ratio, 1.0])
+        wpe = self.omega_pe
+        wpi = wpe / math.sqrt(self.mass_ratio)
+        n0 = self.ppc
+        q = np.array([+math.sqrt(r[0] / (4 * PI * n0 / self.delx ** 3)) * wpi,
+                      -math.sqrt(r[1] / (4 * PI * n0 / self.delx ** 3)) * wpe])
+        return q, r
+
+    @property
+    def n_particles(self):
+        return self.nx * self.ny * self.nz * self.ppc * self.nsp
+
+
+@dataclass
+class State3D:
+    """Reference-layout host arrays of the 3D driver (Fortran order)."""
+    up: np.ndarray      # (ndim, np, ny, nz, nsp) float64
+    gp: np.ndarray
+    uf: np.ndarray      # (6, nx+4, ny+4, nz+4) float64
+    cumcnt: np.ndarray  # (nx+1, ny, nz, nsp) int32
+    np2: np.ndarray     # (ny, nz, nsp) int32
+
+    def copy(self):
+        return State3D(*(np.array(a, order="F", copy=True) for a in (self.up, self.gp, self.uf, self.cumcnt,
+                                                                    self.np2)))
+
+
+def empty_state3d(p: Plasma3D) -> State3D:
+    up = np.zeros((p.ndim, p.np_cap, p.ny, p.nz, p.nsp), order="F")
+    return State3D(up=up, gp=np.zeros_like(up, order="F"),
+                   uf=np.zeros((6, p.nx + 4, p.ny + 4, p.nz + 4), order="F"),
+                   cumcnt=np.zeros((p.nx + 1, p.ny, p.nz, p.nsp), dtype=np.int32, order="F"),
+                   np2=np.zeros((p.ny, p.nz, p.nsp), dtype=np.int32, order="F"))
+
+
+def load_weibel3d(p: Plasma3D) -> State3D:
+    """Counter-streaming electron beams (+-drift along drift_axis, alternating sign) with
+    isotropic thermal spread, cold (or warm) ions co-located with the electrons, uniform
+    random positions in each cell, ppc particles per cell per species, zero fields."""
+    rng = np.random.Generator(np.random.Philox(p.seed))
+    st = empty_state3d(p)
+    nx, ny, nz, n0 = p.nx, p.ny, p.nz, p.ppc
+    npr = nx * n0
+    ix = np.repeat(np.arange(nx), n0)
+    rx = rng.random((nz, ny, npr))
+    ry = rng.random((nz, ny, npr))
+    rz = rng.random((nz, ny, npr))
+    xs = (p.nxgs + ix[None, None, :] + rx) * p.delx
+    ys = (p.nygs + np.arange(ny)[None, :, None] + ry) * p.delx
+    zs = (p.nzgs + np.arange(nz)[:, None, None] + rz) * p.delx
+    for isp in range(p.nsp):
+        st.up[0, :npr, :, :, isp] = xs.transpose(2, 1, 0)
+        st.up[1, :npr, :, :, isp] = ys.transpose(2, 1, 0)
+        st.up[2, :npr, :, :, isp] = zs.transpose(2, 1, 0)
+    sd = (p.u_thi, p.u_the)
+    for isp in range(p.nsp):
+        u = rng.standard_normal((3, npr, ny, nz)) * sd[isp]
+        if isp == 1 and p.drift != 0.0:
+            sign = np.where(np.arange(npr) % 2 == 0, 1.0, -1.0)
+            u[p.drift_axis] += p.drift * sign[:, None, None]
+        st.up[3:6, :npr, :, :, isp] = u
+    for isp in range(p.nsp):
+        row = (np.arange(ny)[:, None] + ny * np.arange(nz)[None, :]).astype(np.int64)  # (ny, nz)
+        pid = row[None, :, :] * npr + np.arange(1, npr + 1, dtype=np.int64)[:, None, None]
+        st.up[6, :npr, :, :, isp] = (-pid).view(np.float64)
+    st.np2[:, :, :] = npr
+    st.cumcnt[:, :, :, :] = (np.arange(nx + 1, dtype=np.int32) * n0)[:, None, None, None]
+    st.gp[...] = st.up
+    return st
+
+
+def config_weibel3d(size="small", seed=12345):
+    """The 3D Weibel configuration 'cfg2' (256^3, 16 ppc, m_i/m_e = 16, beams +-0.5c along x,
+    u_th 0.05c), or a small case for tests."""
+    if size == "cfg2":
+        return Plasma3D(nx=256, ny=256, nz=256, ppc=16, drift=0.5, u_the=0.05, seed=seed)
+    return Plasma3D(nx=8, ny=6, nz=5, ppc=3, drift=0.5, u_the=0.05, seed=seed)
