@@ -173,6 +173,61 @@ int wpic_synchronize(wpic_ctx* ctx);
 long long wpic_num_particles(wpic_ctx* ctx);
 const char* wpic_status_string(int status);
 
+/* ------------------------------------------------------------------------- */
+/* 3D (periodic in x, y and z), FP64 path.  The arrays follow the 3D drivers:  */
+/*   up/gp(7, np, nys:nye, nzs:nze, nsp): x, y, z, ux, uy, uz, id (bit-cast)  */
+/*   uf(6, nxgs-2:nxge+2, nys-2:nye+2, nzs-2:nze+2), cumcnt(nxgs:nxge+1,       */
+/*   nys:nye, nzs:nze, nsp), np2(nys:nye, nzs:nze, nsp).                        */
+/* nx, ny, nz >= 4; one device holds the whole domain (nys = nygs, ...).       */
+/* ------------------------------------------------------------------------- */
+typedef struct wpic_ctx3d wpic_ctx3d;
+
+typedef struct wpic_params3d {
+  int ndim;                 /* 7 in 3D */
+  int np;                   /* per-row capacity of the caller's particle arrays */
+  int nsp;                  /* 1 or 2 */
+  int nxgs, nxge, nygs, nyge, nzgs, nzge, nys, nye, nzs, nze;
+  double delx, delt, c, gfac;
+  double q[2], r[2];
+  int precision;            /* WPIC_FP64 or WPIC_FP64_EXACT */
+  int device_cap;           /* device particle slots per row per species; 0 = np */
+} wpic_params3d;
+
+/* particle__init + field__init + sort__init + bc__init of a 3D run
+   (3d/common/particle.f90:18, field.f90:22, sort.f90:18, boundary_periodic.f90:25) */
+int wpic3d_init(wpic_ctx3d** ctx, const wpic_params3d* p, void* cuda_stream);
+int wpic3d_finalize(wpic_ctx3d* ctx);
+/* which = 0: up (with cumcnt), 1: gp */
+int wpic3d_put_particles(wpic_ctx3d* ctx, int which, const double* up, const int* np2, const int* cumcnt);
+int wpic3d_get_particles(wpic_ctx3d* ctx, int which, double* up, int* np2, int* cumcnt);
+int wpic3d_put_fields(wpic_ctx3d* ctx, const double* uf);
+int wpic3d_get_fields(wpic_ctx3d* ctx, double* uf);
+int wpic3d_get_df(wpic_ctx3d* ctx, double* df);   /* the SAVEd dB/dE of field__fdtd_i */
+int wpic3d_get_uj(wpic_ctx3d* ctx, double* uj);   /* the current of the last field__fdtd_i */
+/* particle__solv(gp, up, uf, cumcnt, nxs, nxe)       3d/common/particle.f90:52 */
+int wpic3d_particle_solv(wpic_ctx3d* ctx);
+/* field__fdtd_i(uf, up, gp, cumcnt, nxs, nxe, ...)   3d/common/field.f90:70 */
+int wpic3d_field_fdtd_i(wpic_ctx3d* ctx);
+/* ele_cur + bc__curre, the deposit half of field__fdtd_i (3d/common/field.f90:129-130) */
+int wpic3d_ele_cur(wpic_ctx3d* ctx);
+/* bc__particle_x(gp, np2)                            3d/common/boundary_periodic.f90:68 */
+int wpic3d_bc_particle_x(wpic_ctx3d* ctx);
+/* bc__particle_yz(gp, np2)                           3d/common/boundary_periodic.f90:104 */
+int wpic3d_bc_particle_yz(wpic_ctx3d* ctx);
+/* sort__bucket(up, gp, cumcnt, np2, nxs, nxe)        3d/common/sort.f90:40 */
+int wpic3d_sort_bucket(wpic_ctx3d* ctx);
+/* the driver loop body (3d/proj/weibel/app.f90:103-108), nsteps times */
+int wpic3d_step(wpic_ctx3d* ctx, int nsteps);
+/* energy_history sums (3d/proj/weibel/app.f90:531-566): kinetic per species, E, B */
+int wpic3d_energy(wpic_ctx3d* ctx, double* out);
+int wpic3d_cg_control(wpic_ctx3d* ctx, const int* fixed3, int ite_max);
+int wpic3d_cg_iters(wpic_ctx3d* ctx, int* out3);
+/* seeded synthetic Weibel plasma (no counterpart in the reference: its loader is unseeded) */
+int wpic3d_load_weibel(wpic_ctx3d* ctx, int ppc, uint64_t seed, double drift, int drift_axis, double u_thi,
+                       double u_the);
+long long wpic3d_num_particles(wpic_ctx3d* ctx);
+int wpic3d_synchronize(wpic_ctx3d* ctx);
+
 #ifdef __cplusplus
 }
 #endif

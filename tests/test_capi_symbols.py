@@ -15,7 +15,7 @@ def declared_functions():
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         src = open(h).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(wpic_\w+)\s*\(", src, flags=re.M):
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(wpic(?:3d)?_\w+)\s*\(", src, flags=re.M):
             names.add(m.group(1))
     return names
 
@@ -23,8 +23,10 @@ def declared_functions():
 def test_header_declares_entry_points():
     names = declared_functions()
     for n in ("wpic_init_2d", "wpic_particle_solv", "wpic_field_fdtd_i", "wpic_bc_particle_x",
-              "wpic_bc_particle_y", "wpic_sort_bucket", "wpic_step", "wpic_energy"):
-        assert n in names
+              "wpic_bc_particle_y", "wpic_sort_bucket", "wpic_step", "wpic_energy",
+              "wpic3d_init", "wpic3d_particle_solv", "wpic3d_field_fdtd_i", "wpic3d_bc_particle_x",
+              "wpic3d_bc_particle_yz", "wpic3d_sort_bucket", "wpic3d_step", "wpic3d_energy"):
+        assert n in names, n
 
 
 def test_library_exports_every_declared_symbol():

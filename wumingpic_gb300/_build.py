@@ -34,6 +34,8 @@ CUDA_UNITS = {
     "mixed2d.cu": [],
     "probe.cu": [],
     "no_alloc.cu": [],
+    "capi3d.cu": [],
+    "kernels3d_common.cu": [],
 }
 
 

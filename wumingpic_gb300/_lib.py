@@ -40,6 +40,18 @@ class WpicParams(ctypes.Structure):
     ]
 
 
+class WpicParams3D(ctypes.Structure):
+    _fields_ = [
+        ("ndim", ctypes.c_int), ("np", ctypes.c_int), ("nsp", ctypes.c_int),
+        ("nxgs", ctypes.c_int), ("nxge", ctypes.c_int), ("nygs", ctypes.c_int), ("nyge", ctypes.c_int),
+        ("nzgs", ctypes.c_int), ("nzge", ctypes.c_int),
+        ("nys", ctypes.c_int), ("nye", ctypes.c_int), ("nzs", ctypes.c_int), ("nze", ctypes.c_int),
+        ("delx", ctypes.c_double), ("delt", ctypes.c_double), ("c", ctypes.c_double), ("gfac", ctypes.c_double),
+        ("q", ctypes.c_double * 2), ("r", ctypes.c_double * 2),
+        ("precision", ctypes.c_int), ("device_cap", ctypes.c_int),
+    ]
+
+
 class WpicError(RuntimeError):
     def __init__(self, status, where=""):
         self.status = status
@@ -84,6 +96,24 @@ def lib():
         L.wpic_host_unregister.argtypes = [vp]
         L.wpic_status_string.argtypes = [i]
         L.wpic_status_string.restype = ctypes.c_char_p
+        # 3D
+        L.wpic3d_init.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(WpicParams3D), vp]
+        L.wpic3d_finalize.argtypes = [vp]
+        L.wpic3d_put_particles.argtypes = [vp, i, vp, vp, vp]
+        L.wpic3d_get_particles.argtypes = [vp, i, vp, vp, vp]
+        for n in ("wpic3d_put_fields", "wpic3d_get_fields", "wpic3d_get_df", "wpic3d_get_uj"):
+            getattr(L, n).argtypes = [vp, vp]
+        for n in ("wpic3d_particle_solv", "wpic3d_field_fdtd_i", "wpic3d_ele_cur", "wpic3d_bc_particle_x",
+                  "wpic3d_bc_particle_yz",
+                  "wpic3d_sort_bucket", "wpic3d_synchronize"):
+            getattr(L, n).argtypes = [vp]
+        L.wpic3d_step.argtypes = [vp, i]
+        L.wpic3d_energy.argtypes = [vp, vp]
+        L.wpic3d_cg_control.argtypes = [vp, vp, i]
+        L.wpic3d_cg_iters.argtypes = [vp, vp]
+        L.wpic3d_load_weibel.argtypes = [vp, i, ctypes.c_uint64, d, i, d, d]
+        L.wpic3d_num_particles.argtypes = [vp]
+        L.wpic3d_num_particles.restype = ll
         _lib = L
     return _lib
 

@@ -1,0 +1,467 @@
+// C ABI of the 3D FP64 path (declared in include/wumingpic_gb300.h): context
+// creation, device memory, reference-layout state exchange, and the host-side
+// sequencing of one 3D time step (3d/proj/weibel/app.f90:103-108).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "wumingpic_gb300.h"
+#include "wpic_internal.h"
+
+using namespace wpic;
+
+struct wpic_ctx3d {
+  wpic_params3d prm;
+  Dev3D d;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  CGState* h_cg = nullptr;
+  int* h_err = nullptr;
+  int cg_fixed[3] = {-1, -1, -1};
+  int cg_iters[3] = {0, 0, 0};
+  std::vector<void*> allocs;
+  double* staging = nullptr;
+  size_t staging_bytes = 0;
+};
+
+namespace {
+
+constexpr int CG3_CHECK_EVERY = 4;
+constexpr int CG_THREADS_HOST = 256;  // threads of the CG reduction blocks
+
+int cuda_status3(cudaError_t e) {
+  if (e == cudaSuccess) return WPIC_OK;
+  fprintf(stderr, "wumingpic_gb300: CUDA error %s\n", cudaGetErrorString(e));
+  return WPIC_CUDA_ERROR;
+}
+
+#define CK3(call)                                   \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_status3(e_); \
+  } while (0)
+
+template <typename T>
+int dalloc3(wpic_ctx3d* c, T** p, size_t n) {
+  void* v = nullptr;
+  cudaError_t e = cudaMalloc(&v, n * sizeof(T) + 16);
+  if (e != cudaSuccess) return cuda_status3(e);
+  c->allocs.push_back(v);
+  e = cudaMemsetAsync(v, 0, n * sizeof(T) + 16, c->stream);
+  if (e != cudaSuccess) return cuda_status3(e);
+  *p = (T*)v;
+  return WPIC_OK;
+}
+
+int alloc_parts3(wpic_ctx3d* c, Parts3D* P, size_t n) {
+  int st;
+  if ((st = dalloc3(c, &P->x, n)) || (st = dalloc3(c, &P->y, n)) || (st = dalloc3(c, &P->z, n)) ||
+      (st = dalloc3(c, &P->ux, n)) || (st = dalloc3(c, &P->uy, n)) || (st = dalloc3(c, &P->uz, n)) ||
+      (st = dalloc3(c, &P->id, n)))
+    return st;
+  return WPIC_OK;
+}
+
+int finish3(wpic_ctx3d* c) {
+  cudaError_t e = cudaMemcpyAsync(c->h_err, c->d.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status3(e);
+  const int bits = *c->h_err;
+  if (bits) cudaMemsetAsync(c->d.err, 0, sizeof(int), c->stream);
+  if (bits & EB_MOVED_TOO_FAR) return WPIC_MOVED_TOO_FAR;
+  if (bits & EB_OUT_OF_RANGE) return WPIC_OUT_OF_RANGE;
+  if (bits & EB_CAPACITY) return WPIC_CAPACITY;
+  if (bits & EB_CG) return WPIC_CG_NOT_CONVERGED;
+  return WPIC_OK;
+}
+
+bool exact3(const wpic_ctx3d* c) { return c->prm.precision == WPIC_FP64_EXACT; }
+
+#define FP3(fn, ...)                            \
+  do {                                          \
+    if (exact3(c)) exact::fn(__VA_ARGS__);      \
+    else fast::fn(__VA_ARGS__);                 \
+  } while (0)
+
+int ensure_staging3(wpic_ctx3d* c, size_t bytes) {
+  if (c->staging_bytes >= bytes) return WPIC_OK;
+  if (c->staging) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->staging);
+    c->staging = nullptr;
+    c->staging_bytes = 0;
+  }
+  CK3(cudaMalloc(&c->staging, bytes));
+  c->staging_bytes = bytes;
+  return WPIC_OK;
+}
+
+int do_cg3(wpic_ctx3d* c) {
+  for (int l = 0; l < 3; ++l) c->h_cg[l].fixed = c->cg_fixed[l];
+  for (int l = 0; l < 3; ++l)
+    CK3(cudaMemcpyAsync(&c->d.cg[l].fixed, &c->h_cg[l].fixed, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  FP3(cg_init3d, c->d, c->stream);
+  for (int guard = 0; guard < 100000; ++guard) {
+    CK3(cudaMemcpyAsync(c->h_cg, c->d.cg, 3 * sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
+    CK3(cudaStreamSynchronize(c->stream));
+    if (!c->h_cg[0].active && !c->h_cg[1].active && !c->h_cg[2].active) break;
+    for (int k = 0; k < CG3_CHECK_EVERY; ++k) {
+      FP3(cg_iter_ap3d, c->d, c->stream);
+      FP3(cg_iter_update3d, c->d, c->stream);
+      FP3(cg_iter_p3d, c->d, c->stream);
+    }
+  }
+  for (int l = 0; l < 3; ++l) c->cg_iters[l] = c->h_cg[l].ite;
+  FP3(cg_store3d, c->d, c->stream);
+  return WPIC_OK;
+}
+
+// field__fdtd_i (3d/common/field.f90:70-208)
+int do_field3(wpic_ctx3d* c) {
+  FP3(deposit3d, c->d, c->stream);  // ele_cur
+  curre_fold3d(c->d, c->stream);
+  FP3(gkl3d, c->d, c->stream);
+  int st = do_cg3(c);
+  if (st) return st;
+  dfield_ghost3d(c->d, c->stream);
+  FP3(efield3d, c->d, c->stream);
+  dfield_ghost3d(c->d, c->stream);
+  uf_add3d(c->d, c->stream);
+  return WPIC_OK;
+}
+
+// bc__particle_yz + sort__bucket fused: B (pushed, x-wrapped) -> A (migrated and sorted)
+void do_migrate_sort3(wpic_ctx3d* c) {
+  migrate_scan3d(c->d, c->d.B, c->stream);
+  migrate_plan3d(c->d, c->stream);
+  sort_rank3d(c->d, c->d.B, c->d.slist, c->stream);
+  gather3d(c->d, c->d.B, c->d.A, c->d.map, c->d.np2new, c->stream);
+  cudaMemcpyAsync(c->d.np2, c->d.np2new, sizeof(int) * c->d.nrow, cudaMemcpyDeviceToDevice, c->stream);
+}
+
+int one_step3(wpic_ctx3d* c) {
+  FP3(push3d, c->d, c->stream);
+  int st = do_field3(c);
+  if (st) return st;
+  particle_x3d(c->d, c->d.B, c->stream);
+  do_migrate_sort3(c);
+  return WPIC_OK;
+}
+
+int put_field3(wpic_ctx3d* c, const double* ref, double* dst, int ncomp) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!ref) return WPIC_BAD_ARGUMENT;
+  const size_t n = (size_t)ncomp * c->d.g.fvol;
+  int st = ensure_staging3(c, n * sizeof(double));
+  if (st) return st;
+  CK3(cudaMemcpyAsync(c->staging, ref, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  field_ref_to_soa(c->staging, dst, ncomp, (int)c->d.g.fvol, c->stream);
+  return finish3(c);
+}
+
+int get_field3(wpic_ctx3d* c, double* ref, const double* src, int ncomp) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!ref) return WPIC_BAD_ARGUMENT;
+  const size_t n = (size_t)ncomp * c->d.g.fvol;
+  int st = ensure_staging3(c, n * sizeof(double));
+  if (st) return st;
+  field_soa_to_ref(src, c->staging, ncomp, (int)c->d.g.fvol, c->stream);
+  CK3(cudaMemcpyAsync(ref, c->staging, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return finish3(c);
+}
+
+}  // namespace
+
+extern "C" {
+
+int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
+  if (!out || !p) return WPIC_BAD_ARGUMENT;
+  *out = nullptr;
+  const int nx = p->nxge - p->nxgs + 1, ny = p->nyge - p->nygs + 1, nz = p->nzge - p->nzgs + 1;
+  if (p->ndim != 7 || p->nsp < 1 || p->nsp > 2 || nx < 4 || ny < 4 || nz < 4 || p->np < 1) return WPIC_BAD_ARGUMENT;
+  if (p->nys != p->nygs || p->nye != p->nyge || p->nzs != p->nzgs || p->nze != p->nzge) return WPIC_BAD_ARGUMENT;
+  if (!(p->delx > 0) || !(p->delt > 0) || !(p->c > 0)) return WPIC_BAD_ARGUMENT;
+  if (p->precision != WPIC_FP64 && p->precision != WPIC_FP64_EXACT) return WPIC_BAD_ARGUMENT;
+  if ((double)nx * ny * nz > 2.0e9 || (double)p->nsp * ny * nz * p->np >= 2147483647.0) return WPIC_BAD_ARGUMENT;
+  wpic_ctx3d* c = new wpic_ctx3d();
+  c->prm = *p;
+  Dev3D& d = c->d;
+  d.g.nx = nx;
+  d.g.ny = ny;
+  d.g.nz = nz;
+  d.g.nxgs = p->nxgs;
+  d.g.nygs = p->nygs;
+  d.g.nzgs = p->nzgs;
+  d.g.fp = nx + 4;
+  d.g.fplane = (size_t)(nx + 4) * (ny + 4);
+  d.g.fvol = d.g.fplane * (nz + 4);
+  d.g.ncell = (size_t)nx * ny * nz;
+  Phys& ph = d.ph;
+  ph.delx = p->delx;
+  ph.delt = p->delt;
+  ph.c = p->c;
+  ph.gfac = p->gfac;
+  ph.nsp = p->nsp;
+  ph.bc = BC_PERIODIC;
+  for (int k = 0; k < 2; ++k) {
+    ph.q[k] = k < p->nsp ? p->q[k] : 0.0;
+    ph.r[k] = k < p->nsp ? p->r[k] : 1.0;
+  }
+  // field__init constants (3d/common/field.f90:57-63), same operation order
+  ph.pi = 4.0 * std::atan(1.0);
+  ph.f1 = p->c * p->delt / p->delx;
+  ph.f2 = p->gfac * ph.f1 * ph.f1;
+  ph.f3 = 4.0 * ph.pi * p->delx / p->c;
+  const double t = p->delx / (p->c * p->delt * p->gfac);
+  ph.f4 = 6.0 + t * t;
+  ph.f5 = t * t;
+  ph.p_d_delx = 1.0 / p->delx;
+  ph.d_delx = 1.0 / p->delx;
+  ph.d_delt = 1.0 / p->delt;
+  d.cap = p->device_cap > 0 ? p->device_cap : p->np;
+  d.nrow = p->nsp * ny * nz;
+  d.nred = (int)std::min<size_t>(1216, (d.g.ncell + CG_THREADS_HOST - 1) / CG_THREADS_HOST);
+  if (d.nred < 1) d.nred = 1;
+  d.ite_max = 100;
+  if (cuda_stream) {
+    c->stream = (cudaStream_t)cuda_stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete c;
+      return WPIC_CUDA_ERROR;
+    }
+    c->own_stream = true;
+  }
+  const size_t slots = (size_t)d.nrow * d.cap;
+  int st = WPIC_OK;
+  do {
+    if ((st = alloc_parts3(c, &d.A, slots)) || (st = alloc_parts3(c, &d.B, slots))) break;
+    if ((st = dalloc3(c, &d.cc, (size_t)d.nrow * (nx + 1))) || (st = dalloc3(c, &d.np2, d.nrow)) ||
+        (st = dalloc3(c, &d.np2new, d.nrow)))
+      break;
+    if ((st = dalloc3(c, &d.uf, 6 * d.g.fvol)) || (st = dalloc3(c, &d.df, 6 * d.g.fvol)) ||
+        (st = dalloc3(c, &d.uj, 3 * d.g.fvol)) || (st = dalloc3(c, &d.gkl, 3 * d.g.ncell)))
+      break;
+    if ((st = dalloc3(c, &d.cellJ, (size_t)375 * d.g.ncell))) break;
+    if ((st = dalloc3(c, &d.phi, 3 * d.g.ncell)) || (st = dalloc3(c, &d.p, 3 * d.g.ncell)) ||
+        (st = dalloc3(c, &d.r, 3 * d.g.ncell)) || (st = dalloc3(c, &d.ap, 3 * d.g.ncell)) ||
+        (st = dalloc3(c, &d.b, 3 * d.g.ncell)))
+      break;
+    if ((st = dalloc3(c, &d.partials, (size_t)3 * d.nred * 2)) || (st = dalloc3(c, &d.cg, 3)) ||
+        (st = dalloc3(c, &d.err, 1)) || (st = dalloc3(c, &d.red_out, 8)))
+      break;
+    if ((st = dalloc3(c, &d.mig, slots)) || (st = dalloc3(c, &d.glist, slots)) ||
+        (st = dalloc3(c, &d.gcnt, (size_t)d.nrow * 8)) || (st = dalloc3(c, &d.goff, (size_t)d.nrow * 8)) ||
+        (st = dalloc3(c, &d.tlist, slots)) || (st = dalloc3(c, &d.slist, slots)) || (st = dalloc3(c, &d.map, slots)))
+      break;
+    if (cudaMallocHost(&c->h_cg, 3 * sizeof(CGState)) != cudaSuccess) { st = WPIC_CUDA_ERROR; break; }
+    if (cudaMallocHost(&c->h_err, sizeof(int)) != cudaSuccess) { st = WPIC_CUDA_ERROR; break; }
+    *c->h_err = 0;
+    st = finish3(c);
+  } while (false);
+  if (st) {
+    wpic3d_finalize(c);
+    return st;
+  }
+  *out = c;
+  return WPIC_OK;
+}
+
+int wpic3d_finalize(wpic_ctx3d* c) {
+  if (!c) return WPIC_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->staging) cudaFree(c->staging);
+  if (c->h_cg) cudaFreeHost(c->h_cg);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return WPIC_OK;
+}
+
+int wpic3d_put_particles(wpic_ctx3d* c, int which, const double* up, const int* np2, const int* cumcnt) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!up || !np2 || (which == 0 && !cumcnt) || (which != 0 && which != 1)) return WPIC_BAD_ARGUMENT;
+  Dev3D& d = c->d;
+  const int nx = d.g.nx, ndim = c->prm.ndim, nph = c->prm.np;
+  for (int r = 0; r < d.nrow; ++r) {
+    if (np2[r] < 0 || np2[r] > d.cap || np2[r] > nph) return WPIC_CAPACITY;
+    if (which == 0) {
+      const int* cc = cumcnt + (size_t)r * (nx + 1);
+      if (cc[0] != 0 || cc[nx] != np2[r]) return WPIC_BAD_ARGUMENT;
+      for (int i = 0; i < nx; ++i)
+        if (cc[i + 1] < cc[i]) return WPIC_BAD_ARGUMENT;
+    }
+  }
+  CK3(cudaMemcpyAsync(d.np2, np2, sizeof(int) * d.nrow, cudaMemcpyHostToDevice, c->stream));
+  if (which == 0)
+    CK3(cudaMemcpyAsync(d.cc, cumcnt, sizeof(int) * (size_t)d.nrow * (nx + 1), cudaMemcpyHostToDevice, c->stream));
+  const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
+  size_t rows_per = ((size_t)1 << 30) / row_bytes;
+  if (rows_per < 1) rows_per = 1;
+  if (rows_per > (size_t)d.nrow) rows_per = d.nrow;
+  int st = ensure_staging3(c, rows_per * row_bytes);
+  if (st) return st;
+  const Parts3D& P = which == 0 ? d.A : d.B;
+  for (int r0 = 0; r0 < d.nrow; r0 += (int)rows_per) {
+    const int nr = (int)std::min<size_t>(rows_per, (size_t)(d.nrow - r0));
+    CK3(cudaMemcpyAsync(c->staging, up + (size_t)r0 * ndim * nph, nr * row_bytes, cudaMemcpyHostToDevice, c->stream));
+    aos_to_soa3d(d, c->staging, ndim, nph, r0, nr, P, c->stream);
+  }
+  return finish3(c);
+}
+
+int wpic3d_get_particles(wpic_ctx3d* c, int which, double* up, int* np2, int* cumcnt) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!up || (which != 0 && which != 1)) return WPIC_BAD_ARGUMENT;
+  Dev3D& d = c->d;
+  const int nx = d.g.nx, ndim = c->prm.ndim, nph = c->prm.np;
+  if (np2) CK3(cudaMemcpyAsync(np2, d.np2, sizeof(int) * d.nrow, cudaMemcpyDeviceToHost, c->stream));
+  if (cumcnt && which == 0)
+    CK3(cudaMemcpyAsync(cumcnt, d.cc, sizeof(int) * (size_t)d.nrow * (nx + 1), cudaMemcpyDeviceToHost, c->stream));
+  const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
+  size_t rows_per = ((size_t)1 << 30) / row_bytes;
+  if (rows_per < 1) rows_per = 1;
+  if (rows_per > (size_t)d.nrow) rows_per = d.nrow;
+  int st = ensure_staging3(c, rows_per * row_bytes);
+  if (st) return st;
+  const Parts3D& P = which == 0 ? d.A : d.B;
+  for (int r0 = 0; r0 < d.nrow; r0 += (int)rows_per) {
+    const int nr = (int)std::min<size_t>(rows_per, (size_t)(d.nrow - r0));
+    CK3(cudaMemsetAsync(c->staging, 0, nr * row_bytes, c->stream));
+    soa_to_aos3d(d, c->staging, ndim, nph, r0, nr, P, c->stream);
+    CK3(cudaMemcpyAsync(up + (size_t)r0 * ndim * nph, c->staging, nr * row_bytes, cudaMemcpyDeviceToHost, c->stream));
+  }
+  return finish3(c);
+}
+
+int wpic3d_put_fields(wpic_ctx3d* c, const double* uf) { return c ? put_field3(c, uf, c->d.uf, 6) : WPIC_NOT_INITIALISED; }
+int wpic3d_get_fields(wpic_ctx3d* c, double* uf) { return c ? get_field3(c, uf, c->d.uf, 6) : WPIC_NOT_INITIALISED; }
+int wpic3d_get_df(wpic_ctx3d* c, double* df) { return c ? get_field3(c, df, c->d.df, 6) : WPIC_NOT_INITIALISED; }
+int wpic3d_get_uj(wpic_ctx3d* c, double* uj) { return c ? get_field3(c, uj, c->d.uj, 3) : WPIC_NOT_INITIALISED; }
+
+int wpic3d_particle_solv(wpic_ctx3d* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  FP3(push3d, c->d, c->stream);
+  return finish3(c);
+}
+
+int wpic3d_field_fdtd_i(wpic_ctx3d* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  int st = do_field3(c);
+  if (st) return st;
+  return finish3(c);
+}
+
+// ele_cur + bc__curre of field__fdtd_i (3d/common/field.f90:129-130), for parity checks
+int wpic3d_ele_cur(wpic_ctx3d* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  FP3(deposit3d, c->d, c->stream);
+  curre_fold3d(c->d, c->stream);
+  return finish3(c);
+}
+
+int wpic3d_bc_particle_x(wpic_ctx3d* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  particle_x3d(c->d, c->d.B, c->stream);
+  return finish3(c);
+}
+
+// bc__particle_yz on gp (B) in place: the post-migration order is gathered through map = slist
+int wpic3d_bc_particle_yz(wpic_ctx3d* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  Dev3D& d = c->d;
+  migrate_scan3d(d, d.B, c->stream);
+  migrate_plan3d(d, c->stream);
+  // gather B -> A by slist, then copy back into B (A is the sorted state, rebuilt by sort_bucket)
+  gather3d(d, d.B, d.A, d.slist, d.np2new, c->stream);
+  const size_t slots = (size_t)d.nrow * d.cap;
+  CK3(cudaMemcpyAsync(d.B.x, d.A.x, slots * 8, cudaMemcpyDeviceToDevice, c->stream));
+  CK3(cudaMemcpyAsync(d.B.y, d.A.y, slots * 8, cudaMemcpyDeviceToDevice, c->stream));
+  CK3(cudaMemcpyAsync(d.B.z, d.A.z, slots * 8, cudaMemcpyDeviceToDevice, c->stream));
+  CK3(cudaMemcpyAsync(d.B.ux, d.A.ux, slots * 8, cudaMemcpyDeviceToDevice, c->stream));
+  CK3(cudaMemcpyAsync(d.B.uy, d.A.uy, slots * 8, cudaMemcpyDeviceToDevice, c->stream));
+  CK3(cudaMemcpyAsync(d.B.uz, d.A.uz, slots * 8, cudaMemcpyDeviceToDevice, c->stream));
+  CK3(cudaMemcpyAsync(d.B.id, d.A.id, slots * 8, cudaMemcpyDeviceToDevice, c->stream));
+  CK3(cudaMemcpyAsync(d.np2, d.np2new, sizeof(int) * d.nrow, cudaMemcpyDeviceToDevice, c->stream));
+  return finish3(c);
+}
+
+// sort__bucket: gp (B) -> up (A) with cumcnt
+int wpic3d_sort_bucket(wpic_ctx3d* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  Dev3D& d = c->d;
+  sort_rank3d(d, d.B, nullptr, c->stream);
+  gather3d(d, d.B, d.A, d.map, d.np2, c->stream);
+  return finish3(c);
+}
+
+int wpic3d_step(wpic_ctx3d* c, int nsteps) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  for (int it = 0; it < nsteps; ++it) {
+    int st = one_step3(c);
+    if (st) return st;
+    st = finish3(c);
+    if (st) return st;
+  }
+  return WPIC_OK;
+}
+
+int wpic3d_energy(wpic_ctx3d* c, double* out) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!out) return WPIC_BAD_ARGUMENT;
+  FP3(energy3d, c->d, c->stream);
+  double h[4];
+  CK3(cudaMemcpyAsync(h, c->d.red_out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  int st = finish3(c);
+  if (st) return st;
+  const int nsp = c->prm.nsp;
+  for (int k = 0; k < nsp; ++k) out[k] = h[k];
+  out[nsp] = h[2];
+  out[nsp + 1] = h[3];
+  return WPIC_OK;
+}
+
+int wpic3d_cg_control(wpic_ctx3d* c, const int* fixed3, int ite_max) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  for (int l = 0; l < 3; ++l) c->cg_fixed[l] = fixed3 ? fixed3[l] : -1;
+  c->d.ite_max = ite_max > 0 ? ite_max : 100;
+  return WPIC_OK;
+}
+
+int wpic3d_cg_iters(wpic_ctx3d* c, int* out3) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!out3) return WPIC_BAD_ARGUMENT;
+  for (int l = 0; l < 3; ++l) out3[l] = c->cg_iters[l];
+  return WPIC_OK;
+}
+
+int wpic3d_load_weibel(wpic_ctx3d* c, int ppc, uint64_t seed, double drift, int drift_axis, double u_thi,
+                       double u_the) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  Dev3D& d = c->d;
+  if (drift_axis < 0 || drift_axis > 2 || ppc < 1) return WPIC_BAD_ARGUMENT;
+  if ((long long)ppc * d.g.nx > d.cap) return WPIC_CAPACITY;
+  load_weibel3d_ppc(d, ppc, seed, drift, drift_axis, u_thi, u_the, c->stream);
+  CK3(cudaMemsetAsync(d.uf, 0, 6 * d.g.fvol * sizeof(double), c->stream));
+  CK3(cudaMemsetAsync(d.df, 0, 6 * d.g.fvol * sizeof(double), c->stream));
+  CK3(cudaMemsetAsync(d.uj, 0, 3 * d.g.fvol * sizeof(double), c->stream));
+  return finish3(c);
+}
+
+long long wpic3d_num_particles(wpic_ctx3d* c) {
+  if (!c) return -1;
+  std::vector<int> h(c->d.nrow);
+  if (cudaMemcpyAsync(h.data(), c->d.np2, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+    return -1;
+  cudaStreamSynchronize(c->stream);
+  long long n = 0;
+  for (int v : h) n += v;
+  return n;
+}
+
+int wpic3d_synchronize(wpic_ctx3d* c) { return c ? finish3(c) : WPIC_NOT_INITIALISED; }
+
+}  // extern "C"

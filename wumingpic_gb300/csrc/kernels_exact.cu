@@ -5,5 +5,6 @@
 namespace wpic {
 namespace exact {
 #include "fp2d.cuh"
+#include "fp3d.cuh"
 }  // namespace exact
 }  // namespace wpic

@@ -4,5 +4,6 @@
 namespace wpic {
 namespace fast {
 #include "fp2d.cuh"
+#include "fp3d.cuh"
 }  // namespace fast
 }  // namespace wpic

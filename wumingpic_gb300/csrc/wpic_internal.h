@@ -187,4 +187,75 @@ void mix_energy2d(const Dev2D& d, cudaStream_t s);
 void load_weibel2d_ppc(const Dev2D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
                        double u_thi, double u_the, cudaStream_t s);
 
+// ---- 3D FP64 path ----
+struct Grid3D {
+  int nx, ny, nz;
+  int nxgs, nygs, nzgs;
+  int fp;          // nx + 4: row pitch of a ghosted field
+  size_t fplane;   // (nx + 4)(ny + 4)
+  size_t fvol;     // (nx + 4)(ny + 4)(nz + 4): one component of a ghosted field
+  size_t ncell;    // nx ny nz
+};
+
+struct Parts3D {
+  double *x, *y, *z, *ux, *uy, *uz;
+  long long* id;
+};
+
+struct Dev3D {
+  Grid3D g;
+  Phys ph;
+  int cap;          // device slots per row (j, k) per species
+  int nrow;         // nsp * nz * ny; row = (isp * nz + kk) * ny + jj, the reference's (j, k) loop order
+  Parts3D A, B;     // A = "up" (sorted state), B = "gp" (new state)
+  int* cc;          // cumcnt [row][nx+1]
+  int *np2, *np2new;
+  double *uf, *df, *uj;          // [6|6|3][nz+4][ny+4][nx+4]
+  double* gkl;                   // [3][nz][ny][nx]
+  double* cellJ;                 // [cell][375]: per-cell 5x5x5 current stencils (3 components)
+  double *phi, *p, *r, *ap, *b;  // [3][nz][ny][nx]
+  double* partials;
+  int nred;
+  CGState* cg;
+  int ite_max;
+  // migration / sort scratch
+  int8_t* mig;      // per slot: 0 stay, else 1 + direction code (dz + 1) * 3 + (dy + 1)
+  int* glist;       // per row: movers grouped by direction group (0..7), slot order inside a group
+  int *gcnt, *goff; // [row][8]: movers per direction group and their offset in glist
+  int *tlist, *slist, *map;
+  int* err;
+  double* red_out;
+};
+
+#define WPIC_DECLARE_FP3_LAUNCHERS                       \
+  void push3d(const Dev3D& d, cudaStream_t s);           \
+  void deposit3d(const Dev3D& d, cudaStream_t s);        \
+  void gkl3d(const Dev3D& d, cudaStream_t s);            \
+  void cg_init3d(const Dev3D& d, cudaStream_t s);        \
+  void cg_iter_ap3d(const Dev3D& d, cudaStream_t s);     \
+  void cg_iter_update3d(const Dev3D& d, cudaStream_t s); \
+  void cg_iter_p3d(const Dev3D& d, cudaStream_t s);      \
+  void cg_store3d(const Dev3D& d, cudaStream_t s);       \
+  void efield3d(const Dev3D& d, cudaStream_t s);         \
+  void energy3d(const Dev3D& d, cudaStream_t s);
+
+namespace exact { WPIC_DECLARE_FP3_LAUNCHERS }
+namespace fast { WPIC_DECLARE_FP3_LAUNCHERS }
+
+void curre_fold3d(const Dev3D& d, cudaStream_t s);
+void dfield_ghost3d(const Dev3D& d, cudaStream_t s);
+void uf_add3d(const Dev3D& d, cudaStream_t s);
+void particle_x3d(const Dev3D& d, const Parts3D& P, cudaStream_t s);
+void migrate_scan3d(const Dev3D& d, const Parts3D& P, cudaStream_t s);
+void migrate_plan3d(const Dev3D& d, cudaStream_t s);
+void sort_rank3d(const Dev3D& d, const Parts3D& P, const int* slist, cudaStream_t s);
+void gather3d(const Dev3D& d, const Parts3D& src, const Parts3D& dst, const int* map, const int* counts,
+              cudaStream_t s);
+void aos_to_soa3d(const Dev3D& d, const double* aos, int ndim, int np_host, int row0, int nrows, const Parts3D& P,
+                  cudaStream_t s);
+void soa_to_aos3d(const Dev3D& d, double* aos, int ndim, int np_host, int row0, int nrows, const Parts3D& P,
+                  cudaStream_t s);
+void load_weibel3d_ppc(const Dev3D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
+                       double u_thi, double u_the, cudaStream_t s);
+
 }  // namespace wpic
