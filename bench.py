@@ -199,6 +199,40 @@ def time_path(p, precision, steps, warmup, rank, torch, dist, local):
     return g, npart, ms, stages, clocks
 
 
+def time_path3d(steps, rank, torch, dist, world):
+    """The 3D FP64 path on the 3D Weibel workload (256^3 cells, 16 ppc/species, m_i/m_e = 16,
+    beams +-0.5c along x, u_th 0.05c), state resident in HBM, one warm-up step."""
+    from wumingpic_gb300.loader import Plasma3D
+    from wumingpic_gb300.pic3d import Pic3D
+    p = Plasma3D(nx=256, ny=256, nz=256, ppc=16, mass_ratio=16.0, drift=0.5, drift_axis=0, u_the=0.05,
+                 seed=20261203 + 7919 * rank, np_slack=1.5)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    g = Pic3D(p, precision="fp64", stream=stream.cuda_stream)
+    g.load_weibel()
+    npart = g.num_particles()
+    g.step(1)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    g.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    cg = [int(x) for x in g.cg_iters()]
+    g.close()
+    return {"workload": f"3D Weibel 256^3 cells, 16 ppc/species, {npart} particles, drift +-0.5c along x, "
+                        f"u_th 0.05c, m_i/m_e 16, c*dt/dx=0.5",
+            "value": npart * world * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+            "steps": steps, "warmup": 1, "dtype": "f64", "cg_iterations": cg}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -207,6 +241,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg1")
     ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the FP64 path (0 = skip)")
+    ap.add_argument("--fp64-3d-steps", type=int, default=2,
+                    help="timed steps of the 3D FP64 path on the 256^3 x 16 ppc Weibel workload (0 = skip)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--stages", action="store_true", help="print the per-stage breakdown to stderr")
@@ -268,6 +304,11 @@ def main():
             k["fp64_pipe_frac"] = k["fp64_gflops"] / peak64
         g64.close()
 
+    # ---- 3D FP64 path: 256^3 cells, 16 ppc/species (the 3D Weibel configuration) ----
+    fp64_3d = None
+    if args.fp64_3d_steps > 0:
+        fp64_3d = time_path3d(args.fp64_3d_steps, rank, torch, dist, world)
+
     base = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -282,7 +323,7 @@ def main():
                 "path": "mixed: integer cell + FP32 offset, FP32 push/gather/deposition, FP64 fields and CG",
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks, "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()},
-                "fp64_path": fp64}
+                "fp64_path": fp64, "fp64_3d_path": fp64_3d}
         print(json.dumps(line), flush=True)
         if args.stages:
             for k, (t, n) in stages.items():
