@@ -1,0 +1,262 @@
+! wpic_shim3d.f90 -- drop-in replacements for WumingPIC's 3D hot-path modules
+! (particle, field, sort, boundary_periodic) that forward to the GB300 library's
+! wpic3d_* entry points through ISO_C_BINDING.  Link these objects instead of the
+! corresponding objects of libwuming3d_common.a; the drivers (3d/proj/*/app.f90)
+! stay unchanged.  Coherence follows the 2D shim: the first particle__solv uploads
+! the host state, the device state is authoritative afterwards, and the host arrays
+! are refreshed every wpic3d_shim_set_sync(n) steps (default: every step).
+module wpic3d_capi
+  use iso_c_binding
+  implicit none
+
+  type, bind(C) :: wpic_params3d
+     integer(c_int) :: ndim, np, nsp, nxgs, nxge, nygs, nyge, nzgs, nzge, nys, nye, nzs, nze
+     real(c_double) :: delx, delt, c, gfac
+     real(c_double) :: q(2), r(2)
+     integer(c_int) :: precision, device_cap
+  end type wpic_params3d
+
+  interface
+     integer(c_int) function wpic3d_init(ctx, p, stream) bind(C, name="wpic3d_init")
+       import :: c_int, c_ptr, wpic_params3d
+       type(c_ptr), intent(out) :: ctx
+       type(wpic_params3d), intent(in) :: p
+       type(c_ptr), value :: stream
+     end function wpic3d_init
+     integer(c_int) function wpic3d_put_particles(ctx, which, up, np2, cumcnt) bind(C, name="wpic3d_put_particles")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: which
+       real(c_double), intent(in) :: up(*)
+       integer(c_int), intent(in) :: np2(*), cumcnt(*)
+     end function wpic3d_put_particles
+     integer(c_int) function wpic3d_get_particles(ctx, which, up, np2, cumcnt) bind(C, name="wpic3d_get_particles")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: which
+       real(c_double), intent(inout) :: up(*)
+       integer(c_int), intent(inout) :: np2(*), cumcnt(*)
+     end function wpic3d_get_particles
+     integer(c_int) function wpic3d_put_fields(ctx, uf) bind(C, name="wpic3d_put_fields")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: uf(*)
+     end function wpic3d_put_fields
+     integer(c_int) function wpic3d_get_fields(ctx, uf) bind(C, name="wpic3d_get_fields")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(inout) :: uf(*)
+     end function wpic3d_get_fields
+     integer(c_int) function wpic3d_particle_solv(ctx) bind(C, name="wpic3d_particle_solv")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic3d_particle_solv
+     integer(c_int) function wpic3d_field_fdtd_i(ctx) bind(C, name="wpic3d_field_fdtd_i")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic3d_field_fdtd_i
+     integer(c_int) function wpic3d_bc_particle_x(ctx) bind(C, name="wpic3d_bc_particle_x")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic3d_bc_particle_x
+     integer(c_int) function wpic3d_bc_particle_yz(ctx) bind(C, name="wpic3d_bc_particle_yz")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic3d_bc_particle_yz
+     integer(c_int) function wpic3d_sort_bucket(ctx) bind(C, name="wpic3d_sort_bucket")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic3d_sort_bucket
+  end interface
+
+  type(c_ptr), save :: wpic3_ctx = c_null_ptr
+  type(wpic_params3d), save :: wpic3_prm
+  logical, save :: wpic3_uploaded = .false.
+  integer, save :: wpic3_sync_every = 1, wpic3_step_count = 0
+
+contains
+
+  subroutine wpic3_check(st, where)
+    integer(c_int), intent(in) :: st
+    character(len=*), intent(in) :: where
+    if (st /= 0) then
+       write(0,*) 'wumingpic_gb300: ', where, ' failed with status ', st
+       stop
+    endif
+  end subroutine wpic3_check
+
+  subroutine wpic3d_shim_set_sync(n)
+    integer, intent(in) :: n
+    wpic3_sync_every = max(1, n)
+  end subroutine wpic3d_shim_set_sync
+
+  subroutine wpic3_ensure_ctx()
+    if (.not. c_associated(wpic3_ctx)) call wpic3_check(wpic3d_init(wpic3_ctx, wpic3_prm, c_null_ptr), 'wpic3d_init')
+  end subroutine wpic3_ensure_ctx
+
+end module wpic3d_capi
+
+
+module particle
+  use wpic3d_capi
+  implicit none
+  private
+  public :: particle__init, particle__solv, particle__solv_vay
+contains
+  subroutine particle__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nzgs_in,nzge_in,nys_in,nye_in, &
+                            nzs_in,nze_in,delx_in,delt_in,c_in,q_in,r_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in
+    integer, intent(in) :: nxgs_in, nxge_in, nygs_in, nyge_in, nzgs_in, nzge_in, nys_in, nye_in, nzs_in, nze_in
+    real(8), intent(in) :: delx_in, delt_in, c_in, q_in(nsp_in), r_in(nsp_in)
+    wpic3_prm%ndim = ndim_in; wpic3_prm%np = np_in; wpic3_prm%nsp = nsp_in
+    wpic3_prm%nxgs = nxgs_in; wpic3_prm%nxge = nxge_in; wpic3_prm%nygs = nygs_in; wpic3_prm%nyge = nyge_in
+    wpic3_prm%nzgs = nzgs_in; wpic3_prm%nzge = nzge_in
+    wpic3_prm%nys = nys_in; wpic3_prm%nye = nye_in; wpic3_prm%nzs = nzs_in; wpic3_prm%nze = nze_in
+    wpic3_prm%delx = delx_in; wpic3_prm%delt = delt_in; wpic3_prm%c = c_in
+    wpic3_prm%q(1:nsp_in) = q_in; wpic3_prm%r(1:nsp_in) = r_in
+    wpic3_prm%precision = 0; wpic3_prm%device_cap = 0
+  end subroutine particle__init
+
+  subroutine particle__solv(gp,up,uf,cumcnt,nxs,nxe)
+    integer, intent(in)  :: nxs, nxe
+    integer, intent(in)  :: cumcnt(wpic3_prm%nxgs:wpic3_prm%nxge+1,wpic3_prm%nys:wpic3_prm%nye, &
+                                   wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    real(8), intent(in)  :: up(*), uf(*)
+    real(8), intent(out) :: gp(*)
+    integer(c_int) :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    call wpic3_ensure_ctx()
+    if (.not. wpic3_uploaded) then
+       np2(:,:,:) = cumcnt(nxe+1,:,:,:)
+       call wpic3_check(wpic3d_put_particles(wpic3_ctx, 0_c_int, up, np2, cumcnt), 'put up')
+       call wpic3_check(wpic3d_put_fields(wpic3_ctx, uf), 'put uf')
+       wpic3_uploaded = .true.
+    endif
+    call wpic3_check(wpic3d_particle_solv(wpic3_ctx), 'particle__solv')
+  end subroutine particle__solv
+
+  subroutine particle__solv_vay(gp,up,uf,cumcnt,nxs,nxe)
+    integer, intent(in) :: nxs, nxe
+    integer, intent(in) :: cumcnt(*)
+    real(8), intent(in) :: up(*), uf(*)
+    real(8), intent(out) :: gp(*)
+    write(0,*) 'wumingpic_gb300: particle__solv_vay is not provided by the GPU library in 3D'
+    stop
+  end subroutine particle__solv_vay
+end module particle
+
+
+module field
+  use wpic3d_capi
+  implicit none
+  private
+  public :: field__init, field__fdtd_i
+contains
+  subroutine field__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nzgs_in,nzge_in,nys_in,nye_in, &
+                         nzs_in,nze_in,mnpr_in,ncomw_in,opsum_in,nerr_in,delx_in,delt_in,c_in,q_in,r_in,gfac_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in
+    integer, intent(in) :: nxgs_in, nxge_in, nygs_in, nyge_in, nzgs_in, nzge_in, nys_in, nye_in, nzs_in, nze_in
+    integer, intent(in) :: mnpr_in, ncomw_in, opsum_in, nerr_in
+    real(8), intent(in) :: delx_in, delt_in, c_in, q_in(nsp_in), r_in(nsp_in), gfac_in
+    wpic3_prm%gfac = gfac_in
+  end subroutine field__init
+
+  subroutine field__fdtd_i(uf,up,gp,cumcnt,nxs,nxe,set_boundary_dfield,set_boundary_curre,set_boundary_phi)
+    integer, intent(in)    :: nxs, nxe
+    integer, intent(in)    :: cumcnt(*)
+    real(8), intent(in)    :: up(*), gp(*)
+    real(8), intent(inout) :: uf(*)
+    external :: set_boundary_dfield, set_boundary_curre, set_boundary_phi
+    call wpic3_check(wpic3d_field_fdtd_i(wpic3_ctx), 'field__fdtd_i')
+    if (mod(wpic3_step_count + 1, wpic3_sync_every) == 0) then
+       call wpic3_check(wpic3d_get_fields(wpic3_ctx, uf), 'get uf')
+    endif
+  end subroutine field__fdtd_i
+end module field
+
+
+module sort
+  use wpic3d_capi
+  implicit none
+  private
+  public :: sort__init, sort__bucket
+contains
+  subroutine sort__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nzgs_in,nzge_in,nys_in,nye_in,nzs_in,nze_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in
+    integer, intent(in) :: nxgs_in, nxge_in, nygs_in, nyge_in, nzgs_in, nzge_in, nys_in, nye_in, nzs_in, nze_in
+  end subroutine sort__init
+
+  ! np2 is intent(in) in the reference; it is refreshed with the sorted state at the sync points
+  subroutine sort__bucket(gp,up,cumcnt,np2,nxs,nxe)
+    integer, intent(in)    :: nxs, nxe
+    integer, intent(inout) :: np2(wpic3_prm%nye-wpic3_prm%nys+1, wpic3_prm%nze-wpic3_prm%nzs+1, wpic3_prm%nsp)
+    integer, intent(out)   :: cumcnt(*)
+    real(8), intent(in)    :: up(*)
+    real(8), intent(out)   :: gp(*)
+    integer(c_int) :: np2_dev(wpic3_prm%nye-wpic3_prm%nys+1, wpic3_prm%nze-wpic3_prm%nzs+1, wpic3_prm%nsp)
+    call wpic3_check(wpic3d_sort_bucket(wpic3_ctx), 'sort__bucket')
+    wpic3_step_count = wpic3_step_count + 1
+    if (mod(wpic3_step_count, wpic3_sync_every) == 0) then
+       call wpic3_check(wpic3d_get_particles(wpic3_ctx, 0_c_int, gp, np2_dev, cumcnt), 'get up')
+       np2(:,:,:) = np2_dev(:,:,:)
+    endif
+  end subroutine sort__bucket
+end module sort
+
+
+module boundary_periodic
+  use wpic3d_capi
+  implicit none
+  private
+  public :: boundary_periodic__init, boundary_periodic__dfield, boundary_periodic__particle_x, &
+       boundary_periodic__particle_yz, boundary_periodic__curre, boundary_periodic__phi, boundary_periodic__mom
+contains
+  subroutine boundary_periodic__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nzgs_in, &
+                                     nzge_in,nys_in,nye_in,nzs_in,nze_in,jup_in,jdown_in,kup_in,kdown_in,mnpi_in, &
+                                     mnpr_in,ncomw_in,nerr_in,nstat_in,delx_in,delt_in,c_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in
+    integer, intent(in) :: nxgs_in, nxge_in, nygs_in, nyge_in, nzgs_in, nzge_in, nys_in, nye_in, nzs_in, nze_in
+    integer, intent(in) :: jup_in, jdown_in, kup_in, kdown_in, mnpi_in, mnpr_in, ncomw_in, nerr_in, nstat_in(:)
+    real(8), intent(in) :: delx_in, delt_in, c_in
+  end subroutine boundary_periodic__init
+
+  subroutine boundary_periodic__particle_x(up,np2)
+    real(8), intent(inout) :: up(*)
+    integer, intent(in)    :: np2(*)
+    call wpic3_check(wpic3d_bc_particle_x(wpic3_ctx), 'bc__particle_x')
+  end subroutine boundary_periodic__particle_x
+
+  subroutine boundary_periodic__particle_yz(up,np2)
+    real(8), intent(inout) :: up(*)
+    integer, intent(inout) :: np2(*)
+    call wpic3_check(wpic3d_bc_particle_yz(wpic3_ctx), 'bc__particle_yz')
+  end subroutine boundary_periodic__particle_yz
+
+  ! applied inside the library; present so that field__fdtd_i's arguments type-check
+  subroutine boundary_periodic__dfield(df,nxs,nxe,nys,nye,nzs,nze,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nzs, nze, nxgs, nxge
+    real(8), intent(inout) :: df(*)
+  end subroutine boundary_periodic__dfield
+  subroutine boundary_periodic__curre(uj,nxs,nxe,nys,nye,nzs,nze,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nzs, nze, nxgs, nxge
+    real(8), intent(inout) :: uj(*)
+  end subroutine boundary_periodic__curre
+  subroutine boundary_periodic__phi(phi,nxs,nxe,nys,nye,nzs,nze,l)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nzs, nze, l
+    real(8), intent(inout) :: phi(*)
+  end subroutine boundary_periodic__phi
+
+  ! moments stay on the host: the one-rank periodic fold of the moment array in x, y, z
+  subroutine boundary_periodic__mom(mom)
+    real(8), intent(inout) :: mom(7, wpic3_prm%nxgs-1:wpic3_prm%nxge+1, wpic3_prm%nys-1:wpic3_prm%nye+1, &
+                                  wpic3_prm%nzs-1:wpic3_prm%nze+1, wpic3_prm%nsp)
+    integer :: gs, ge, ys, ye, zs, ze
+    gs = wpic3_prm%nxgs; ge = wpic3_prm%nxge; ys = wpic3_prm%nys; ye = wpic3_prm%nye
+    zs = wpic3_prm%nzs; ze = wpic3_prm%nze
+    mom(:, gs, :, :, :) = mom(:, gs, :, :, :) + mom(:, ge+1, :, :, :)
+    mom(:, ge, :, :, :) = mom(:, ge, :, :, :) + mom(:, gs-1, :, :, :)
+    mom(:, :, ye, :, :) = mom(:, :, ye, :, :) + mom(:, :, ys-1, :, :)
+    mom(:, :, ys, :, :) = mom(:, :, ys, :, :) + mom(:, :, ye+1, :, :)
+    mom(:, :, :, ze, :) = mom(:, :, :, ze, :) + mom(:, :, :, zs-1, :)
+    mom(:, :, :, zs, :) = mom(:, :, :, zs, :) + mom(:, :, :, ze+1, :)
+  end subroutine boundary_periodic__mom
+end module boundary_periodic
