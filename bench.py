@@ -342,7 +342,7 @@ def measure_e2e(g, p):
     from wumingpic_gb300 import _lib
     st = g.get_state()
     pinned = []
-    for a in (st.up, st.uf):
+    for a in (st.up, st.uf, st.cumcnt, st.np2):
         try:
             _lib.host_register(a)
             pinned.append(a)

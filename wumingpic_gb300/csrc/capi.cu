@@ -47,6 +47,15 @@ struct wpic_ctx {
   std::vector<int> h_dep;
   std::vector<long long> h_off;
   int* h_grow = nullptr;  // pinned mirror of the grow flag
+  // mixed path state exchange: a copy stream and two staging buffers used in turn, so that
+  // the host link transfers one chunk while the device converts the other
+  // two copy streams take alternate rows, so that one copy's setup overlaps the other's transfer
+  cudaStream_t xfer[2] = {nullptr, nullptr};
+  double* xstg[2] = {nullptr, nullptr};
+  size_t xstg_bytes = 0;
+  cudaEvent_t ev_copied[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [buffer][copy stream]
+  cudaEvent_t ev_used[2] = {nullptr, nullptr};
+  std::vector<int> h_np2;
   double mix_vmax = 0.0;  // largest contribution of one particle to one node of the deposit
 };
 
@@ -142,6 +151,34 @@ int ensure_staging(wpic_ctx* c, size_t bytes) {
   }
   CK(cudaMalloc(&c->staging, bytes));
   c->staging_bytes = bytes;
+  return WPIC_OK;
+}
+
+// copy streams, events and two staging buffers of `bytes` each for the mixed state exchange
+int ensure_xfer(wpic_ctx* c, size_t bytes) {
+  if (!c->xfer[0]) {
+    for (int k = 0; k < 2; ++k) {
+      CK(cudaStreamCreateWithFlags(&c->xfer[k], cudaStreamNonBlocking));
+      for (int q = 0; q < 2; ++q) CK(cudaEventCreateWithFlags(&c->ev_copied[k][q], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&c->ev_used[k], cudaEventDisableTiming));
+    }
+  }
+  if (c->xstg_bytes < bytes) {
+    for (int k = 0; k < 2; ++k) CK(cudaStreamSynchronize(c->xfer[k]));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < 2; ++k) {
+      if (c->xstg[k]) cudaFree(c->xstg[k]);
+      c->xstg[k] = nullptr;
+    }
+    c->xstg_bytes = 0;
+    for (int k = 0; k < 2; ++k) CK(cudaMalloc(&c->xstg[k], bytes));
+    c->xstg_bytes = bytes;
+  }
+  return WPIC_OK;
+}
+
+int sync_xfer(wpic_ctx* c) {
+  for (int k = 0; k < 2; ++k) CK(cudaStreamSynchronize(c->xfer[k]));
   return WPIC_OK;
 }
 
@@ -517,6 +554,15 @@ int wpic_finalize(wpic_ctx* c) {
   for (void* p : c->allocs) cudaFree(p);
   if (c->mixP) cudaFree(c->mixP);
   if (c->h_grow) cudaFreeHost(c->h_grow);
+  for (int k = 0; k < 2; ++k)
+    if (c->xfer[k]) cudaStreamSynchronize(c->xfer[k]);
+  for (int k = 0; k < 2; ++k) {
+    if (c->xstg[k]) cudaFree(c->xstg[k]);
+    for (int q = 0; q < 2; ++q)
+      if (c->ev_copied[k][q]) cudaEventDestroy(c->ev_copied[k][q]);
+    if (c->ev_used[k]) cudaEventDestroy(c->ev_used[k]);
+    if (c->xfer[k]) cudaStreamDestroy(c->xfer[k]);
+  }
   if (c->staging) cudaFree(c->staging);
   if (c->h_cg) cudaFreeHost(c->h_cg);
   if (c->h_err) cudaFreeHost(c->h_err);
@@ -534,54 +580,86 @@ int wpic_put_particles(wpic_ctx* c, int which, const double* up, const int* np2,
   if (!up || !np2 || (which == 0 && !cumcnt) || (which != 0 && which != 1)) return WPIC_BAD_ARGUMENT;
   Dev2D& d = c->d;
   const int nx = d.g.nx, ndim = c->prm.ndim, nph = c->prm.np;
-  for (int r = 0; r < d.nrowjob; ++r) {
+  for (int r = 0; r < d.nrowjob; ++r)
     if (np2[r] < 0 || np2[r] > d.cap || np2[r] > nph) return WPIC_CAPACITY;
-    if (which == 0) {
+  // cumcnt: prefix sums of the rows' cell counts (checked while the first copies run in the mixed path)
+  auto check_cumcnt = [&]() -> int {
+    if (which != 0) return WPIC_OK;
+    for (int r = 0; r < d.nrowjob; ++r) {
       const int* cc = cumcnt + (size_t)r * (nx + 1);
       if (cc[0] != 0 || cc[nx] != np2[r]) return WPIC_BAD_ARGUMENT;
       for (int i = 0; i < nx; ++i)
         if (cc[i + 1] < cc[i]) return WPIC_BAD_ARGUMENT;
     }
-  }
+    return WPIC_OK;
+  };
   if (c->mixed && which != 0) return WPIC_BAD_ARGUMENT;
+  if (!c->mixed) {
+    const int st = check_cumcnt();
+    if (st) return st;
+  }
   CK(cudaMemcpyAsync(d.np2, np2, sizeof(int) * d.nrowjob, cudaMemcpyHostToDevice, c->stream));
   if (which == 0)
     CK(cudaMemcpyAsync(d.cc, cumcnt, sizeof(int) * (size_t)d.nrowjob * (nx + 1), cudaMemcpyHostToDevice,
                        c->stream));
   const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
   if (c->mixed) {
-    // lay the bins out for these particles: each bin's depth from its fullest cell
+    int st = ensure_xfer(c, (size_t)MIX_TS * row_bytes);
+    if (st) return st;
+    // the first two chunks start crossing the link while the device finds each bin's fullest
+    // cell (the layout check below); their staging buffers are free (the last call finished)
+    auto copy_chunk = [&](int k) -> int {
+      const int isp = k / d.m.nty, ty = k - isp * d.m.nty;
+      const size_t r0 = (size_t)isp * d.g.ny + (size_t)ty * MIX_TS;
+      for (int rr = 0; rr < MIX_TS; ++rr) {
+        const size_t nb = (size_t)np2[r0 + rr] * ndim * sizeof(double);
+        if (nb)
+          CK(cudaMemcpyAsync(c->xstg[k & 1] + (size_t)rr * nph * ndim, up + (r0 + rr) * ndim * nph, nb,
+                             cudaMemcpyHostToDevice, c->xfer[rr & 1]));
+      }
+      for (int q = 0; q < 2; ++q) CK(cudaEventRecord(c->ev_copied[k & 1][q], c->xfer[q]));
+      return WPIC_OK;
+    };
+    const int nchunk = c->prm.nsp * d.m.nty;
+    for (int k = 0; k < 2 && k < nchunk; ++k)
+      if ((st = copy_chunk(k))) return st;
+    if ((st = check_cumcnt())) {
+      sync_xfer(c);
+      return st;
+    }
+    // lay the bins out for these particles unless every bin already has the room: each bin's
+    // depth from its fullest cell
     {
       const Mix2D& m = d.m;
-      std::vector<int> dep(m.nbin);
+      mix_binmax2d(d, c->stream);
+      std::vector<int> mx(m.nbin);
+      CK(cudaMemcpyAsync(mx.data(), m.bneed, sizeof(int) * m.nbin, cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
       const double cdx = c->prm.c * c->prm.delt / c->prm.delx;
-      for (int isp = 0; isp < c->prm.nsp; ++isp)
-        for (int ty = 0; ty < m.nty; ++ty)
-          for (int tx = 0; tx < m.ntx; ++tx) {
-            int mx = 0;
-            for (int ly = 0; ly < MIX_TS; ++ly) {
-              const int* cc = cumcnt + ((size_t)isp * d.g.ny + ty * MIX_TS + ly) * (nx + 1) + tx * MIX_TS;
-              for (int lx = 0; lx < MIX_TS; ++lx) mx = std::max(mx, cc[lx + 1] - cc[lx]);
-            }
-            dep[(ty * m.ntx + tx) * c->prm.nsp + isp] = mix_initial_depth(mx, cdx);
-          }
-      int st = mix_set_layout(c, dep, false);
-      if (st) return st;
-    }
-    // stage whole tile rows (16 bucket rows) of one species at a time
-    size_t trows = ((size_t)1 << 30) / (row_bytes * MIX_TS);
-    if (trows < 1) trows = 1;
-    if (trows > (size_t)d.m.nty) trows = d.m.nty;
-    int st = ensure_staging(c, trows * MIX_TS * row_bytes);
-    if (st) return st;
-    for (int isp = 0; isp < c->prm.nsp; ++isp)
-      for (int ty0 = 0; ty0 < d.m.nty; ty0 += (int)trows) {
-        const int nt = (int)((size_t)(d.m.nty - ty0) < trows ? d.m.nty - ty0 : trows);
-        const size_t r0 = (size_t)isp * d.g.ny + (size_t)ty0 * MIX_TS;
-        CK(cudaMemcpyAsync(c->staging, up + r0 * ndim * nph, (size_t)nt * MIX_TS * row_bytes,
-                           cudaMemcpyHostToDevice, c->stream));
-        mix_put2d(d, c->staging, ndim, nph, isp, ty0, nt, c->stream);
+      // the current layout is kept while every bin keeps 40 % of its depth free above its
+      // fullest cell (room for the arrivals of the next steps; bins grow on demand after that)
+      std::vector<int> dep(m.nbin);
+      bool fits = (int)c->h_dep.size() == m.nbin;
+      for (int b = 0; b < m.nbin; ++b) {
+        dep[b] = mix_initial_depth(mx[b], cdx);
+        if (fits && 5LL * mx[b] > 3LL * c->h_dep[b]) fits = false;
       }
+      if (!fits && (st = mix_set_layout(c, dep, false))) return st;
+    }
+    // one tile row (16 bucket rows) of one species per chunk: the valid prefix of each row is
+    // copied into staging buffer k % 2 on the copy stream while the device converts chunk k - 1
+    for (int k = 0; k < nchunk; ++k) {
+      const int b = k & 1;
+      const int isp = k / d.m.nty, ty = k - isp * d.m.nty;
+      if (k >= 2) {
+        for (int q = 0; q < 2; ++q) CK(cudaStreamWaitEvent(c->xfer[q], c->ev_used[b], 0));
+        if ((st = copy_chunk(k))) return st;
+      }
+      for (int q = 0; q < 2; ++q) CK(cudaStreamWaitEvent(c->stream, c->ev_copied[b][q], 0));
+      mix_put2d(d, c->xstg[b], ndim, nph, isp, ty, 1, c->stream);
+      CK(cudaEventRecord(c->ev_used[b], c->stream));
+    }
+    if ((st = sync_xfer(c))) return st;
     return finish(c);
   }
   size_t rows_per = ((size_t)1 << 30) / row_bytes;
@@ -607,25 +685,39 @@ int wpic_get_particles(wpic_ctx* c, int which, double* up, int* np2, int* cumcnt
   if (c->mixed) {
     if (which != 0) return WPIC_BAD_ARGUMENT;
     mix_count_rows2d(d, c->stream);
-    if (np2) CK(cudaMemcpyAsync(np2, d.np2, sizeof(int) * d.nrowjob, cudaMemcpyDeviceToHost, c->stream));
+    c->h_np2.resize(d.nrowjob);
+    CK(cudaMemcpyAsync(c->h_np2.data(), d.np2, sizeof(int) * d.nrowjob, cudaMemcpyDeviceToHost, c->stream));
     if (cumcnt)
       CK(cudaMemcpyAsync(cumcnt, d.cc, sizeof(int) * (size_t)d.nrowjob * (nx + 1), cudaMemcpyDeviceToHost,
                          c->stream));
+    CK(cudaStreamSynchronize(c->stream));  // the row counts size the copies below
+    for (int r = 0; r < d.nrowjob; ++r)
+      if (c->h_np2[r] > nph) return WPIC_CAPACITY;
+    if (np2) std::copy(c->h_np2.begin(), c->h_np2.end(), np2);
     const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
-    size_t trows = ((size_t)1 << 30) / (row_bytes * MIX_TS);
-    if (trows < 1) trows = 1;
-    if (trows > (size_t)d.m.nty) trows = d.m.nty;
-    int st = ensure_staging(c, trows * MIX_TS * row_bytes);
+    // chunk k is converted into staging buffer k % 2 while the copy stream moves chunk k - 1
+    // to the host; only each row's valid prefix crosses the link
+    int st = ensure_xfer(c, (size_t)MIX_TS * row_bytes);
     if (st) return st;
+    int k = 0;
     for (int isp = 0; isp < c->prm.nsp; ++isp)
-      for (int ty0 = 0; ty0 < d.m.nty; ty0 += (int)trows) {
-        const int nt = (int)((size_t)(d.m.nty - ty0) < trows ? d.m.nty - ty0 : trows);
-        const size_t r0 = (size_t)isp * d.g.ny + (size_t)ty0 * MIX_TS;
-        CK(cudaMemsetAsync(c->staging, 0, (size_t)nt * MIX_TS * row_bytes, c->stream));
-        mix_get2d(d, c->staging, ndim, nph, isp, ty0, nt, c->stream);
-        CK(cudaMemcpyAsync(up + r0 * ndim * nph, c->staging, (size_t)nt * MIX_TS * row_bytes,
-                           cudaMemcpyDeviceToHost, c->stream));
+      for (int ty = 0; ty < d.m.nty; ++ty, ++k) {
+        const int b = k & 1;
+        const size_t r0 = (size_t)isp * d.g.ny + (size_t)ty * MIX_TS;
+        if (k >= 2)
+          for (int q = 0; q < 2; ++q) CK(cudaStreamWaitEvent(c->stream, c->ev_copied[b][q], 0));
+        mix_get2d(d, c->xstg[b], ndim, nph, isp, ty, 1, c->stream);
+        CK(cudaEventRecord(c->ev_used[b], c->stream));
+        for (int q = 0; q < 2; ++q) CK(cudaStreamWaitEvent(c->xfer[q], c->ev_used[b], 0));
+        for (int rr = 0; rr < MIX_TS; ++rr) {
+          const size_t nb = (size_t)c->h_np2[r0 + rr] * ndim * sizeof(double);
+          if (nb)
+            CK(cudaMemcpyAsync(up + (r0 + rr) * ndim * nph, c->xstg[b] + (size_t)rr * nph * ndim, nb,
+                               cudaMemcpyDeviceToHost, c->xfer[rr & 1]));
+        }
+        for (int q = 0; q < 2; ++q) CK(cudaEventRecord(c->ev_copied[b][q], c->xfer[q]));
       }
+    if ((st = sync_xfer(c))) return st;
     return finish(c);
   }
   if (np2) CK(cudaMemcpyAsync(np2, d.np2, sizeof(int) * d.nrowjob, cudaMemcpyDeviceToHost, c->stream));

@@ -638,40 +638,105 @@ int mix_initial_depth(double n, double c_dt_dx) {
 // reference layout -> columns: thread c copies the particles of cell c, which are
 // contiguous in the cell-sorted row (cumcnt gives the range)
 // ---------------------------------------------------------------------------
+// One CTA per tile.  For each of the tile's 16 bucket rows, the 16 cells' particles are one
+// contiguous range of the AoS row; the CTA reads that range with consecutive threads on
+// consecutive words (coalesced), finds each word's cell among the 16 (cumcnt), and stores the
+// converted component into the cell's column.
 __global__ void __launch_bounds__(MIX_TC) k_mix_put(Dev2D d, const double* aos, int ndim, int np_host, int isp,
                                                    int ty0) {
+  __shared__ int scc[MIX_TS][MIX_TS + 1];
   const Mix2D& m = d.m;
   const Grid2D g = d.g;
   const int tx = blockIdx.x, ty = ty0 + blockIdx.y;
   const int bin = (ty * m.ntx + tx) * d.ph.nsp + isp;
   const int c = threadIdx.x;
-  const int lx = c & (MIX_TS - 1), ly = c >> 4;
-  const int gx = tx * MIX_TS + lx, gy = ty * MIX_TS + ly;
-  const int row = isp * g.ny + gy;
-  const int* ccr = d.cc + (size_t)row * (g.nx + 1);
-  const int first = ccr[gx];
-  int n = ccr[gx + 1] - first;
-  if (n > m.bdep[bin]) {
-    atomicOr(d.err, EB_CAPACITY);
-    n = m.bdep[bin];
+  const int dep = m.bdep[bin];
+  for (int t = c; t < MIX_TS * (MIX_TS + 1); t += MIX_TC) {
+    const int ly = t / (MIX_TS + 1), q = t - ly * (MIX_TS + 1);
+    scc[ly][q] = d.cc[((size_t)isp * g.ny + ty * MIX_TS + ly) * (g.nx + 1) + tx * MIX_TS + q];
   }
-  const double* rowp = aos + (size_t)((ty - ty0) * MIX_TS + ly) * np_host * ndim;
+  __syncthreads();
+  {
+    const int lx = c & (MIX_TS - 1), ly = c >> 4;
+    int n = scc[ly][lx + 1] - scc[ly][lx];
+    if (n > dep) {
+      atomicOr(d.err, EB_CAPACITY);
+      n = dep;
+    }
+    m.cnt[bin * MIX_TC + c] = n;
+  }
   const double dxi = d.ph.d_delx;
-  float* const col = mix_slot(m, bin, 0, c);
-  for (int k = 0; k < n; ++k) {
-    const double* a = rowp + (size_t)(first + k) * ndim;
-    float* o = col + (size_t)k * MIX_PL;
-    o[MIX_OX] = (float)(a[0] * dxi - (double)(g.nxgs + gx));
-    o[MIX_OY] = (float)(a[1] * dxi - (double)(g.nygs + gy));
-    o[MIX_UX] = (float)a[2];
-    o[MIX_UY] = (float)a[3];
-    o[MIX_UZ] = (float)a[4];
-    const long long id = ndim > 5 ? __double_as_longlong(a[5]) : 0;
-    o[MIX_IDLO] = __int_as_float((int)(unsigned)(id & 0xffffffffll));
-    o[MIX_IDHI] = __int_as_float((int)(unsigned)((unsigned long long)id >> 32));
+  float* const col0 = mix_slot(m, bin, 0, 0);
+  for (int ly = 0; ly < MIX_TS; ++ly) {
+    const int first = scc[ly][0];
+    const long long nw = (long long)(scc[ly][MIX_TS] - first) * ndim;
+    const double* rowp = aos + ((size_t)((ty - ty0) * MIX_TS + ly) * np_host + first) * ndim;
+    const int gy = ty * MIX_TS + ly;
+    for (long long w = c; w < nw; w += MIX_TC) {
+      const int pl = (int)(w / ndim), comp = (int)(w - (long long)pl * ndim);
+      const int p = first + pl;
+      int lx = 0;
+#pragma unroll
+      for (int step = 8; step > 0; step >>= 1)
+        if (scc[ly][lx + step] <= p) lx += step;
+      const int k = p - scc[ly][lx];
+      if (k >= dep || comp > 5) continue;
+      const double a = rowp[w];
+      float* o = col0 + (size_t)k * MIX_PL + ly * MIX_TS + lx;
+      const int gx = tx * MIX_TS + lx;
+      if (comp == 0) o[MIX_OX] = (float)(a * dxi - (double)(g.nxgs + gx));
+      else if (comp == 1) o[MIX_OY] = (float)(a * dxi - (double)(g.nygs + gy));
+      else if (comp == 2) o[MIX_UX] = (float)a;
+      else if (comp == 3) o[MIX_UY] = (float)a;
+      else if (comp == 4) o[MIX_UZ] = (float)a;
+      else {
+        const long long id = __double_as_longlong(a);
+        o[MIX_IDLO] = __int_as_float((int)(unsigned)(id & 0xffffffffll));
+        o[MIX_IDHI] = __int_as_float((int)(unsigned)((unsigned long long)id >> 32));
+      }
+    }
+    if (ndim <= 5) {  // no id words in the input: ids are zero
+      const int n = scc[ly][MIX_TS] - first;
+      for (int pl = c; pl < n; pl += MIX_TC) {
+        const int p = first + pl;
+        int lx = 0;
+#pragma unroll
+        for (int step = 8; step > 0; step >>= 1)
+          if (scc[ly][lx + step] <= p) lx += step;
+        const int k = p - scc[ly][lx];
+        if (k >= dep) continue;
+        float* o = col0 + (size_t)k * MIX_PL + ly * MIX_TS + lx;
+        o[MIX_IDLO] = 0.f;
+        o[MIX_IDHI] = 0.f;
+      }
+    }
   }
-  m.cnt[bin * MIX_TC + c] = n;
 }
+
+// per bin, the largest particle count of its cells in the reference-layout cumcnt (d.cc)
+__global__ void __launch_bounds__(MIX_TC) k_mix_binmax(Dev2D d) {
+  __shared__ int wmax[MIX_TC / 32];
+  const Mix2D& m = d.m;
+  const Grid2D g = d.g;
+  const int bin = blockIdx.x;
+  const int nsp = d.ph.nsp;
+  const int tile = bin / nsp, isp = bin - tile * nsp;
+  const int tx = tile % m.ntx, ty = tile / m.ntx;
+  const int c = threadIdx.x;
+  const int gx = tx * MIX_TS + (c & (MIX_TS - 1)), gy = ty * MIX_TS + (c >> 4);
+  const int* ccr = d.cc + ((size_t)isp * g.ny + gy) * (g.nx + 1);
+  int v = ccr[gx + 1] - ccr[gx];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((c & 31) == 0) wmax[c >> 5] = v;
+  __syncthreads();
+  if (c == 0) {
+    for (int w = 1; w < MIX_TC / 32; ++w) v = max(v, wmax[w]);
+    m.bneed[bin] = v;
+  }
+}
+
+void mix_binmax2d(const Dev2D& d, cudaStream_t s) { k_mix_binmax<<<d.m.nbin, MIX_TC, 0, s>>>(d); }
 
 void mix_put2d(const Dev2D& d, const double* aos, int ndim, int np_host, int isp, int ty0, int nty,
                cudaStream_t s) {
@@ -717,36 +782,57 @@ __global__ void __launch_bounds__(32) k_mix_rowscan(Dev2D d) {
 
 void mix_count_rows2d(const Dev2D& d, cudaStream_t s) { k_mix_rowscan<<<d.nrowjob, 32, 0, s>>>(d); }
 
+// One CTA per tile, the reverse of k_mix_put: the tile's particles of each bucket row are
+// written as one contiguous AoS range (cumcnt from k_mix_rowscan), consecutive threads on
+// consecutive words.
 __global__ void __launch_bounds__(MIX_TC) k_mix_get(Dev2D d, double* aos, int ndim, int np_host, int isp, int ty0) {
+  __shared__ int scc[MIX_TS][MIX_TS + 1];
   const Mix2D& m = d.m;
   const Grid2D g = d.g;
   const int tx = blockIdx.x, ty = ty0 + blockIdx.y;
   const int bin = (ty * m.ntx + tx) * d.ph.nsp + isp;
   const int c = threadIdx.x;
-  const int lx = c & (MIX_TS - 1), ly = c >> 4;
-  const int gx = tx * MIX_TS + lx, gy = ty * MIX_TS + ly;
-  const int first = d.cc[((size_t)isp * g.ny + gy) * (g.nx + 1) + gx];
-  const int n = m.cnt[bin * MIX_TC + c];
-  const float* col = mix_slot(m, bin, 0, c);
+  for (int t = c; t < MIX_TS * (MIX_TS + 1); t += MIX_TC) {
+    const int ly = t / (MIX_TS + 1), q = t - ly * (MIX_TS + 1);
+    scc[ly][q] = d.cc[((size_t)isp * g.ny + ty * MIX_TS + ly) * (g.nx + 1) + tx * MIX_TS + q];
+  }
+  __syncthreads();
   const double dx = d.ph.delx;
-  double* rowp = aos + (size_t)((ty - ty0) * MIX_TS + ly) * np_host * ndim;
-  for (int k = 0; k < n; ++k) {
-    const int pos = first + k;
-    if (pos >= np_host) {
-      atomicOr(d.err, EB_CAPACITY);
-      break;
+  const float* const col0 = mix_slot(m, bin, 0, 0);
+  for (int ly = 0; ly < MIX_TS; ++ly) {
+    const int first = scc[ly][0];
+    int last = scc[ly][MIX_TS];
+    if (last > np_host) {
+      if (c == 0) atomicOr(d.err, EB_CAPACITY);
+      last = np_host;
     }
-    const float* o = col + (size_t)k * MIX_PL;
-    double* a = rowp + (size_t)pos * ndim;
-    a[0] = ((double)(g.nxgs + gx) + (double)o[MIX_OX]) * dx;
-    a[1] = ((double)(g.nygs + gy) + (double)o[MIX_OY]) * dx;
-    a[2] = (double)o[MIX_UX];
-    a[3] = (double)o[MIX_UY];
-    a[4] = (double)o[MIX_UZ];
-    if (ndim > 5) {
-      const unsigned long long id = ((unsigned long long)(unsigned)__float_as_int(o[MIX_IDHI]) << 32) |
-                                    (unsigned)__float_as_int(o[MIX_IDLO]);
-      a[5] = __longlong_as_double((long long)id);
+    const long long nw = (long long)(last - first) * ndim;
+    double* rowp = aos + ((size_t)((ty - ty0) * MIX_TS + ly) * np_host + (first > 0 ? first : 0)) * ndim;
+    const int gy = ty * MIX_TS + ly;
+    for (long long w = c; w < nw; w += MIX_TC) {
+      const int pl = (int)(w / ndim), comp = (int)(w - (long long)pl * ndim);
+      const int p = first + pl;
+      int lx = 0;
+#pragma unroll
+      for (int step = 8; step > 0; step >>= 1)
+        if (scc[ly][lx + step] <= p) lx += step;
+      const int k = p - scc[ly][lx];
+      const float* o = col0 + (size_t)k * MIX_PL + ly * MIX_TS + lx;
+      const int gx = tx * MIX_TS + lx;
+      double v;
+      if (comp == 0) v = ((double)(g.nxgs + gx) + (double)o[MIX_OX]) * dx;
+      else if (comp == 1) v = ((double)(g.nygs + gy) + (double)o[MIX_OY]) * dx;
+      else if (comp == 2) v = (double)o[MIX_UX];
+      else if (comp == 3) v = (double)o[MIX_UY];
+      else if (comp == 4) v = (double)o[MIX_UZ];
+      else if (comp == 5) {
+        const unsigned long long id = ((unsigned long long)(unsigned)__float_as_int(o[MIX_IDHI]) << 32) |
+                                      (unsigned)__float_as_int(o[MIX_IDLO]);
+        v = __longlong_as_double((long long)id);
+      } else {
+        v = 0.0;
+      }
+      rowp[w] = v;
     }
   }
 }

@@ -178,6 +178,7 @@ void mix_push_deposit2d(const Dev2D& d, const void* tmap, cudaStream_t s);
 void mix_curre_refresh2d(const Dev2D& d, cudaStream_t s);
 void mix_migrate2d(const Dev2D& d, cudaStream_t s);
 void mix_put2d(const Dev2D& d, const double* aos, int ndim, int np_host, int isp, int ty0, int nty, cudaStream_t s);
+void mix_binmax2d(const Dev2D& d, cudaStream_t s);  // bneed[bin] = largest cell count in d.cc
 void mix_count_rows2d(const Dev2D& d, cudaStream_t s);  // cumcnt and np2 of the reference layout
 void mix_get2d(const Dev2D& d, double* aos, int ndim, int np_host, int isp, int ty0, int nty, cudaStream_t s);
 void mix_load_weibel2d(const Dev2D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
