@@ -60,6 +60,10 @@ extern "C" {
                              wpic_step, the state exchange (which = 0), the loader and the
                              diagnostics are available in this mode. */
 
+/* the push of the fused step: particle__solv (Buneman-Boris) or particle__solv_vay */
+#define WPIC_PUSH_BORIS 0
+#define WPIC_PUSH_VAY 1   /* FP64 paths only */
+
 typedef struct wpic_ctx wpic_ctx;
 
 /* The scalar arguments of particle__init (2d/common/particle.f90:18-45),
@@ -99,6 +103,10 @@ int wpic_get_uj(wpic_ctx* ctx, double* uj);
 
 /* particle__solv(gp, up, uf, cumcnt, nxs, nxe)      2d/common/particle.f90:48-179 */
 int wpic_particle_solv(wpic_ctx* ctx);
+/* particle__solv_vay(gp,up,uf,cumcnt,nxs,nxe)  2d/common/particle.f90:182 (FP64 paths) */
+int wpic_particle_solv_vay(wpic_ctx* ctx);
+/* which push the fused step (wpic_step) uses: WPIC_PUSH_BORIS (default) or WPIC_PUSH_VAY */
+int wpic_set_pusher(wpic_ctx* ctx, int pusher);
 /* field__fdtd_i(uf, up, gp, cumcnt, nxs, nxe, bc__dfield, bc__curre, bc__phi)
  *                                                   2d/common/field.f90:66-186 */
 int wpic_field_fdtd_i(wpic_ctx* ctx);
@@ -206,6 +214,9 @@ int wpic3d_get_df(wpic_ctx3d* ctx, double* df);   /* the SAVEd dB/dE of field__f
 int wpic3d_get_uj(wpic_ctx3d* ctx, double* uj);   /* the current of the last field__fdtd_i */
 /* particle__solv(gp, up, uf, cumcnt, nxs, nxe)       3d/common/particle.f90:52 */
 int wpic3d_particle_solv(wpic_ctx3d* ctx);
+/* particle__solv_vay(gp, up, uf, cumcnt, nxs, nxe)   3d/common/particle.f90:236 */
+int wpic3d_particle_solv_vay(wpic_ctx3d* ctx);
+int wpic3d_set_pusher(wpic_ctx3d* ctx, int pusher);
 /* field__fdtd_i(uf, up, gp, cumcnt, nxs, nxe, ...)   3d/common/field.f90:70 */
 int wpic3d_field_fdtd_i(wpic_ctx3d* ctx);
 /* ele_cur + bc__curre, the deposit half of field__fdtd_i (3d/common/field.f90:129-130) */

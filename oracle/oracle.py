@@ -42,6 +42,7 @@ def lib():
         for n in ("orc2d_get_df", "orc2d_set_df", "orc2d_get_uj"):
             getattr(L, n).argtypes = [vp, dp]
         L.orc2d_particle_solv.argtypes = [vp, dp, dp, dp, ip, i, i]
+        L.orc2d_particle_solv_vay.argtypes = [vp, dp, dp, dp, ip, i, i]
         L.orc2d_ele_cur.argtypes = [vp, dp, dp, dp, ip, i, i]
         L.orc2d_bc_curre.argtypes = [vp, dp, i, i]
         L.orc2d_bc_dfield.argtypes = [vp, dp, i, i]
@@ -62,6 +63,7 @@ def lib():
             for n in ("orc3d_get_df", "orc3d_get_uj"):
                 getattr(L, n).argtypes = [vp, dp]
             L.orc3d_particle_solv.argtypes = [vp, dp, dp, dp, ip, i, i]
+            L.orc3d_particle_solv_vay.argtypes = [vp, dp, dp, dp, ip, i, i]
             L.orc3d_ele_cur.argtypes = [vp, dp, dp, dp, ip, i, i]
             L.orc3d_bc_curre.argtypes = [vp, dp, i, i]
             L.orc3d_field_fdtd_i.argtypes = [vp, dp, dp, dp, ip, i, i]
@@ -137,6 +139,10 @@ class Oracle2D:
         return lib().orc2d_particle_solv(self._h, _p(gp, np.float64), _p(up, np.float64), _p(uf, np.float64),
                                          _p(cumcnt, np.int32), self.nxs, self.nxe)
 
+    def particle_solv_vay(self, gp, up, uf, cumcnt):
+        return lib().orc2d_particle_solv_vay(self._h, _p(gp, np.float64), _p(up, np.float64), _p(uf, np.float64),
+                                             _p(cumcnt, np.int32), self.nxs, self.nxe)
+
     def ele_cur(self, uj, up, gp, cumcnt):
         return lib().orc2d_ele_cur(self._h, _p(uj, np.float64), _p(up, np.float64), _p(gp, np.float64),
                                    _p(cumcnt, np.int32), self.nxs, self.nxe)
@@ -170,10 +176,12 @@ class Oracle2D:
                            _p(out, np.float64))
         return out
 
-    def step(self, st):
+    def step(self, st, pusher="boris"):
         """One reference time step on a State2D, in the driver's call order
-        (2d/proj/weibel/app.f90:102-107; reconnection: 2d/proj/reconnection/app.f90:101-106)."""
-        rc = self.particle_solv(st.gp, st.up, st.uf, st.cumcnt)
+        (2d/proj/weibel/app.f90:102-107; reconnection: 2d/proj/reconnection/app.f90:101-106);
+        pusher="vay" calls particle__solv_vay in place of particle__solv."""
+        push = self.particle_solv_vay if pusher == "vay" else self.particle_solv
+        rc = push(st.gp, st.up, st.uf, st.cumcnt)
         if self.bc == BC_RECONNECTION:
             rc = rc or self.bc_particle_x(st.gp, st.np2)
         rc = rc or self.field_fdtd_i(st.uf, st.up, st.gp, st.cumcnt)
@@ -239,6 +247,10 @@ class Oracle3D:
         return lib().orc3d_particle_solv(self._h, _p(gp, np.float64), _p(up, np.float64), _p(uf, np.float64),
                                          _p(cumcnt, np.int32), self.nxs, self.nxe)
 
+    def particle_solv_vay(self, gp, up, uf, cumcnt):
+        return lib().orc3d_particle_solv_vay(self._h, _p(gp, np.float64), _p(up, np.float64), _p(uf, np.float64),
+                                             _p(cumcnt, np.int32), self.nxs, self.nxe)
+
     def ele_cur(self, uj, up, gp, cumcnt):
         return lib().orc3d_ele_cur(self._h, _p(uj, np.float64), _p(up, np.float64), _p(gp, np.float64),
                                    _p(cumcnt, np.int32), self.nxs, self.nxe)
@@ -266,10 +278,11 @@ class Oracle3D:
                            _p(out, np.float64))
         return out
 
-    def step(self, st):
+    def step(self, st, pusher="boris"):
         """One reference time step on a State3D, in the driver's call order
-        (3d/proj/weibel/app.f90:103-108)."""
-        rc = self.particle_solv(st.gp, st.up, st.uf, st.cumcnt)
+        (3d/proj/weibel/app.f90:103-108); pusher="vay" calls particle__solv_vay."""
+        push = self.particle_solv_vay if pusher == "vay" else self.particle_solv
+        rc = push(st.gp, st.up, st.uf, st.cumcnt)
         rc = rc or self.field_fdtd_i(st.uf, st.up, st.gp, st.cumcnt)
         rc = rc or self.bc_particle_x(st.gp, st.np2)
         rc = rc or self.bc_particle_yz(st.gp, st.np2)

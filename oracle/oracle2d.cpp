@@ -113,8 +113,32 @@ struct RoundDown {
 // ---------------------------------------------------------------------------
 // particle__solv  (2d/common/particle.f90:48-179)
 // ---------------------------------------------------------------------------
+// The Vay update (particle.f90:182-315, the gather shared with particle__solv): u' from
+// E and the rotation at the old gamma, then gamma from the quadratic of Vay (2008).
+inline void vay_update(double fac1, double fac2, double c, double bpx, double bpy, double bpz, double epx,
+                       double epy, double epz, double uvm1, double uvm2, double uvm3, double* g, double* gam_out) {
+  double gam = std::sqrt(c * c + uvm1 * uvm1 + uvm2 * uvm2 + uvm3 * uvm3);
+  const double fac1r = fac1 / gam;
+  const double uvm4 = uvm1 + fac2 * epx + fac1r * (+uvm2 * bpz - uvm3 * bpy);
+  const double uvm5 = uvm2 + fac2 * epy + fac1r * (+uvm3 * bpx - uvm1 * bpz);
+  const double uvm6 = uvm3 + fac2 * epz + fac1r * (+uvm1 * bpy - uvm2 * bpx);
+  const double taux = fac1 * bpx / c;
+  const double tauy = fac1 * bpy / c;
+  const double tauz = fac1 * bpz / c;
+  const double tau2 = taux * taux + tauy * tauy + tauz * tauz;
+  const double ua = (uvm4 * taux + uvm5 * tauy + uvm6 * tauz) / c;
+  const double sigma = 1.0 + (uvm4 * uvm4 + uvm5 * uvm5 + uvm6 * uvm6) / (c * c) - tau2;
+  const double gam2 = 0.5 * (sigma + std::sqrt(sigma * sigma + 4.0 * (tau2 + ua * ua)));
+  gam = std::sqrt(gam2);
+  const double txxx = 1.0 / (tau2 + gam2);
+  g[0] = txxx * (gam2 * uvm4 + c * ua * taux + gam * (uvm5 * tauz - uvm6 * tauy));
+  g[1] = txxx * (gam2 * uvm5 + c * ua * tauy + gam * (uvm6 * taux - uvm4 * tauz));
+  g[2] = txxx * (gam2 * uvm6 + c * ua * tauz + gam * (uvm4 * tauy - uvm5 * taux));
+  *gam_out = 1.0 / gam;
+}
+
 int particle_solv(Orc2D* o, double* gp, const double* up, const double* uf, const int* cumcnt,
-                  int nxs, int nxe) {
+                  int nxs, int nxe, bool vay = false) {
   const int nys = o->nys, nye = o->nye;
   const int tw = nxe - nxs + 3;  // tmp(1:6, nxs-1:nxe+1, nys-1:nye+1)
   std::vector<double> tmp((size_t)6 * tw * (nye - nys + 3));
@@ -160,6 +184,17 @@ int particle_solv(Orc2D* o, double* gp, const double* up, const double* uf, cons
                        + (+it(m, i - 1, j) * sh[0][0] + it(m, i, j) * sh[1][0] + it(m, i + 1, j) * sh[2][0]) * sh[1][1]
                        + (+it(m, i - 1, j + 1) * sh[0][0] + it(m, i, j + 1) * sh[1][0] + it(m, i + 1, j + 1) * sh[2][0]) * sh[2][1];
           const double bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
+          if (vay) {
+            double g[3], igam;
+            vay_update(fac1, fac2, c, bpx, bpy, bpz, epx, epy, epz, up[o->iup(3, ii, j, isp)],
+                       up[o->iup(4, ii, j, isp)], up[o->iup(5, ii, j, isp)], g, &igam);
+            gp[o->iup(3, ii, j, isp)] = g[0];
+            gp[o->iup(4, ii, j, isp)] = g[1];
+            gp[o->iup(5, ii, j, isp)] = g[2];
+            gp[o->iup(1, ii, j, isp)] = up[o->iup(1, ii, j, isp)] + g[0] * delt * igam;
+            gp[o->iup(2, ii, j, isp)] = up[o->iup(2, ii, j, isp)] + g[1] * delt * igam;
+            continue;
+          }
           // accel.
           double uvm1 = up[o->iup(3, ii, j, isp)] + fac1 * epx;
           double uvm2 = up[o->iup(4, ii, j, isp)] + fac1 * epy;
@@ -860,6 +895,10 @@ void orc2d_get_uj(void* h, double* out) {
 }
 int orc2d_particle_solv(void* h, double* gp, const double* up, const double* uf, const int* cumcnt, int nxs, int nxe) {
   return particle_solv((Orc2D*)h, gp, up, uf, cumcnt, nxs, nxe);
+}
+int orc2d_particle_solv_vay(void* h, double* gp, const double* up, const double* uf, const int* cumcnt, int nxs,
+                            int nxe) {
+  return particle_solv((Orc2D*)h, gp, up, uf, cumcnt, nxs, nxe, true);
 }
 int orc2d_ele_cur(void* h, double* uj, const double* up, const double* gp, const int* cumcnt, int nxs, int nxe) {
   return ele_cur((Orc2D*)h, uj, up, gp, cumcnt, nxs, nxe);

@@ -88,6 +88,47 @@ def test_push_parity(gpu_lib, precision, rel):
 
 
 @pytest.mark.parametrize("precision,rel", [("fp64_exact", 0.0), ("fp64", REL)])
+def test_push_vay_parity(gpu_lib, precision, rel):
+    """particle__solv_vay (2d/common/particle.f90:182) against the oracle's Vay update."""
+    p, st = perturbed_case(seed=8, u_the=0.3)
+    st.uf[:3] *= 40.0  # magnetic rotation of a few tenths of a radian per step for electrons
+    o = make_oracle(p)
+    g = make_gpu(p, precision, gpu_lib)
+    g.put_state(st)
+    g.particle__solv_vay()
+    gp_gpu, np2, _ = g.get_particles(1)
+    ref = st.copy()
+    assert o.particle_solv_vay(ref.gp, ref.up, ref.uf, ref.cumcnt) == 0
+    assert_particles(gp_gpu, np2, ref.gp, ref.np2, rel)
+
+
+def test_one_step_vay_exact_is_bit_exact_on_particles(gpu_lib):
+    """The fused step with the Vay push selected, exact build: particles bit-identical."""
+    p, st = perturbed_case(seed=33, nx=16, ny=12, ppc=6)
+    g = make_gpu(p, "fp64_exact", gpu_lib)
+    g.set_pusher("vay")
+    g.put_state(st)
+    g.step(1)
+    o = make_oracle(p)
+    o.cg_control(fixed=g.cg_iters())
+    ref = st.copy()
+    assert o.step(ref, pusher="vay") == 0
+    out = g.get_state()
+    assert_particles(out.up, out.np2, ref.up, ref.np2)
+    np.testing.assert_array_equal(out.cumcnt, ref.cumcnt)
+    assert_field(out.uf, ref.uf, REL)
+
+
+def test_vay_is_rejected_on_the_mixed_path(gpu_lib):
+    p, st = perturbed_case(seed=34, nx=16, ny=16)
+    g = make_gpu(p, "mixed", gpu_lib)
+    with pytest.raises(RuntimeError):
+        g.set_pusher("vay")
+    with pytest.raises(RuntimeError):
+        g.particle__solv_vay()
+
+
+@pytest.mark.parametrize("precision,rel", [("fp64_exact", 0.0), ("fp64", REL)])
 def test_deposit_parity(gpu_lib, precision, rel):
     """ele_cur + bc__curre: the exact build reproduces the single-thread reduction order bit for bit."""
     p, st = perturbed_case(seed=12)

@@ -210,3 +210,68 @@ def test_reconnection_walls_reflect():
     assert st.gp[0, 0, 0, 0] == 2 * (p.nxgs + 1) - (p.nxgs + 0.25)
     assert st.gp[0, n - 1, 0, 0] == 2 * (p.nxge - 1) - (p.nxge + 0.5)
     np.testing.assert_array_equal(st.gp[2:5, [0, n - 1], 0, 0], -u0)
+
+
+def _uniform_fields(uf, b, e):
+    uf[...] = 0.0
+    for k in range(3):
+        uf[k] = b[k]
+        uf[3 + k] = e[k]
+
+
+def test_vay_conserves_momentum_magnitude_in_pure_b():
+    """particle__solv_vay with E = 0: gamma' solves the quadratic exactly at gamma, so
+    |u| is conserved for any direction of B (not only u perpendicular to B)."""
+    p, st = small_case(seed=13, u_the=0.3, u_thi=0.2)
+    _uniform_fields(st.uf, (0.2, -0.1, 0.35), (0.0, 0.0, 0.0))
+    o = make_oracle(p)
+    assert o.particle_solv_vay(st.gp, st.up, st.uf, st.cumcnt) == 0
+    for isp in range(p.nsp):
+        for jj in range(p.ny):
+            n = st.np2[jj, isp]
+            u0 = st.up[2:5, :n, jj, isp]
+            u1 = st.gp[2:5, :n, jj, isp]
+            np.testing.assert_allclose(np.linalg.norm(u1, axis=0), np.linalg.norm(u0, axis=0), rtol=1e-13)
+            np.testing.assert_array_equal(st.gp[5, :n, jj, isp].view(np.int64),
+                                          st.up[5, :n, jj, isp].view(np.int64))
+
+
+def test_vay_equals_boris_in_pure_e():
+    """With B = 0 both pushes reduce to u += (q/m) dt E and x += u dt / gamma."""
+    p, st = small_case(seed=17, u_the=0.3)
+    _uniform_fields(st.uf, (0.0, 0.0, 0.0), (0.05, -0.02, 0.03))
+    o = make_oracle(p)
+    gb = st.gp.copy(order="F")
+    assert o.particle_solv(gb, st.up, st.uf, st.cumcnt) == 0
+    assert o.particle_solv_vay(st.gp, st.up, st.uf, st.cumcnt) == 0
+    for isp in range(p.nsp):
+        for jj in range(p.ny):
+            n = st.np2[jj, isp]
+            np.testing.assert_allclose(st.gp[:5, :n, jj, isp], gb[:5, :n, jj, isp], rtol=1e-13, atol=1e-15)
+
+
+def test_vay_keeps_relativistic_exb_drift_force_free():
+    """E = -v x B / c for a particle at gamma ~ 5: the Lorentz force vanishes, and the Vay
+    push leaves u unchanged to round-off; the Boris push does not (the defect the Vay
+    scheme removes)."""
+    p, st = small_case(seed=19)
+    q, r = p.charges()
+    ux = 5.0 * p.c
+    bz = 0.2 / abs(q[1] / r[1] * 0.5 * p.delt)  # electrons turn by ~0.4 rad / gamma per step
+    vx = ux / math.sqrt(1.0 + (ux / p.c) ** 2)
+    _uniform_fields(st.uf, (0.0, 0.0, bz), (0.0, vx * bz / p.c, 0.0))
+    for isp in range(p.nsp):
+        for jj in range(p.ny):
+            n = st.np2[jj, isp]
+            st.up[2, :n, jj, isp] = ux
+            st.up[3:5, :n, jj, isp] = 0.0
+    o = make_oracle(p)
+    gb = st.gp.copy(order="F")
+    assert o.particle_solv(gb, st.up, st.uf, st.cumcnt) == 0
+    assert o.particle_solv_vay(st.gp, st.up, st.uf, st.cumcnt) == 0
+    for isp in range(p.nsp):
+        n = st.np2[0, isp]
+        np.testing.assert_allclose(st.gp[2, :n, 0, isp], ux, rtol=1e-12)
+        np.testing.assert_allclose(st.gp[3:5, :n, 0, isp], 0.0, atol=1e-12 * ux)
+    n = st.np2[0, 1]
+    assert np.abs(gb[2:5, :n, 0, 1] - st.up[2:5, :n, 0, 1]).max() > 1e-5 * ux

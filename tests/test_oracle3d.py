@@ -187,3 +187,40 @@ def test_threads_do_not_change_push_and_fields_3d():
         assert o4.step(s1) == 0
     np.testing.assert_allclose(s1.uf, st.uf, rtol=0, atol=1e-12 * np.abs(st.uf).max())
     np.testing.assert_array_equal(s1.np2, st.np2)
+
+
+def _uniform_fields3d(uf, b, e):
+    uf[...] = 0.0
+    for k in range(3):
+        uf[k] = b[k]
+        uf[3 + k] = e[k]
+
+
+def test_vay_conserves_momentum_magnitude_in_pure_b_3d():
+    """particle__solv_vay (3d/common/particle.f90:236) with E = 0 conserves |u|."""
+    p, st = small_case3d(seed=13, u_the=0.3)
+    _uniform_fields3d(st.uf, (0.2, -0.1, 0.35), (0.0, 0.0, 0.0))
+    o = make_oracle3d(p)
+    assert o.particle_solv_vay(st.gp, st.up, st.uf, st.cumcnt) == 0
+    for isp in range(p.nsp):
+        for kk in range(p.nz):
+            for jj in range(p.ny):
+                n = st.np2[jj, kk, isp]
+                u0 = st.up[3:6, :n, jj, kk, isp]
+                u1 = st.gp[3:6, :n, jj, kk, isp]
+                np.testing.assert_allclose(np.linalg.norm(u1, axis=0), np.linalg.norm(u0, axis=0), rtol=1e-13)
+
+
+def test_vay_equals_boris_in_pure_e_3d():
+    p, st = small_case3d(seed=17, u_the=0.3)
+    _uniform_fields3d(st.uf, (0.0, 0.0, 0.0), (0.05, -0.02, 0.03))
+    o = make_oracle3d(p)
+    gb = st.gp.copy(order="F")
+    assert o.particle_solv(gb, st.up, st.uf, st.cumcnt) == 0
+    assert o.particle_solv_vay(st.gp, st.up, st.uf, st.cumcnt) == 0
+    for isp in range(p.nsp):
+        for kk in range(p.nz):
+            for jj in range(p.ny):
+                n = st.np2[jj, kk, isp]
+                np.testing.assert_allclose(st.gp[:6, :n, jj, kk, isp], gb[:6, :n, jj, kk, isp],
+                                           rtol=1e-13, atol=1e-15)

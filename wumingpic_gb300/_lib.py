@@ -27,6 +27,8 @@ BC_RECONNECTION = 1
 FP64 = 0
 FP64_EXACT = 1
 MIXED = 2
+PUSH_BORIS = 0
+PUSH_VAY = 1
 
 
 class WpicParams(ctypes.Structure):
@@ -76,7 +78,10 @@ def lib():
         L.wpic_get_particles.argtypes = [vp, i, vp, vp, vp]
         for n in ("wpic_put_fields", "wpic_get_fields", "wpic_put_df", "wpic_get_df", "wpic_get_uj"):
             getattr(L, n).argtypes = [vp, vp]
-        for n in ("wpic_particle_solv", "wpic_field_fdtd_i", "wpic_ele_cur", "wpic_bc_particle_x",
+        L.wpic_set_pusher.argtypes = [vp, i]
+        L.wpic3d_set_pusher.argtypes = [vp, i]
+        for n in ("wpic_particle_solv", "wpic_particle_solv_vay", "wpic_field_fdtd_i", "wpic_ele_cur",
+                  "wpic_bc_particle_x",
                   "wpic_bc_particle_y", "wpic_sort_bucket", "wpic_synchronize"):
             getattr(L, n).argtypes = [vp]
         L.wpic_step.argtypes = [vp, i]
@@ -103,7 +108,8 @@ def lib():
         L.wpic3d_get_particles.argtypes = [vp, i, vp, vp, vp]
         for n in ("wpic3d_put_fields", "wpic3d_get_fields", "wpic3d_get_df", "wpic3d_get_uj"):
             getattr(L, n).argtypes = [vp, vp]
-        for n in ("wpic3d_particle_solv", "wpic3d_field_fdtd_i", "wpic3d_ele_cur", "wpic3d_bc_particle_x",
+        for n in ("wpic3d_particle_solv", "wpic3d_particle_solv_vay", "wpic3d_field_fdtd_i", "wpic3d_ele_cur",
+                  "wpic3d_bc_particle_x",
                   "wpic3d_bc_particle_yz",
                   "wpic3d_sort_bucket", "wpic3d_synchronize"):
             getattr(L, n).argtypes = [vp]

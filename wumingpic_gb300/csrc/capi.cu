@@ -57,6 +57,7 @@ struct wpic_ctx {
   cudaEvent_t ev_used[2] = {nullptr, nullptr};
   std::vector<int> h_np2;
   double mix_vmax = 0.0;  // largest contribution of one particle to one node of the deposit
+  int pusher = WPIC_PUSH_BORIS;  // the push of the fused step
 };
 
 namespace {
@@ -186,7 +187,8 @@ int sync_xfer(wpic_ctx* c) {
 
 void do_push(wpic_ctx* c) {
   stage_begin(c, SG_PUSH);
-  FP(push2d, c->d, c->stream);
+  if (c->pusher == WPIC_PUSH_VAY) FP(push_vay2d, c->d, c->stream);
+  else FP(push2d, c->d, c->stream);
   stage_end(c, SG_PUSH, 1);
 }
 
@@ -773,6 +775,21 @@ int wpic_particle_solv(wpic_ctx* c) {
   if (c->mixed) return WPIC_BAD_ARGUMENT;
   do_push(c);
   return finish(c);
+}
+
+int wpic_particle_solv_vay(wpic_ctx* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;
+  FP(push_vay2d, c->d, c->stream);
+  return finish(c);
+}
+
+int wpic_set_pusher(wpic_ctx* c, int pusher) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (pusher != WPIC_PUSH_BORIS && pusher != WPIC_PUSH_VAY) return WPIC_BAD_ARGUMENT;
+  if (c->mixed && pusher != WPIC_PUSH_BORIS) return WPIC_BAD_ARGUMENT;
+  c->pusher = pusher;
+  return WPIC_OK;
 }
 
 int wpic_field_fdtd_i(wpic_ctx* c) {

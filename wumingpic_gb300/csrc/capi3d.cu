@@ -23,6 +23,7 @@ struct wpic_ctx3d {
   std::vector<void*> allocs;
   double* staging = nullptr;
   size_t staging_bytes = 0;
+  int pusher = WPIC_PUSH_BORIS;  // the push of the fused step
 };
 
 namespace {
@@ -142,7 +143,8 @@ void do_migrate_sort3(wpic_ctx3d* c) {
 }
 
 int one_step3(wpic_ctx3d* c) {
-  FP3(push3d, c->d, c->stream);
+  if (c->pusher == WPIC_PUSH_VAY) FP3(push_vay3d, c->d, c->stream);
+  else FP3(push3d, c->d, c->stream);
   int st = do_field3(c);
   if (st) return st;
   particle_x3d(c->d, c->d.B, c->stream);
@@ -346,6 +348,19 @@ int wpic3d_particle_solv(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
   FP3(push3d, c->d, c->stream);
   return finish3(c);
+}
+
+int wpic3d_particle_solv_vay(wpic_ctx3d* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  FP3(push_vay3d, c->d, c->stream);
+  return finish3(c);
+}
+
+int wpic3d_set_pusher(wpic_ctx3d* c, int pusher) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (pusher != WPIC_PUSH_BORIS && pusher != WPIC_PUSH_VAY) return WPIC_BAD_ARGUMENT;
+  c->pusher = pusher;
+  return WPIC_OK;
 }
 
 int wpic3d_field_fdtd_i(wpic_ctx3d* c) {

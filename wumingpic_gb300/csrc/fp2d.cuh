@@ -16,6 +16,33 @@
 constexpr int PUSH_TW = 32;
 constexpr int PUSH_THREADS = 128;
 
+// particle__solv_vay's momentum update (2d/common/particle.f90:182-315; the same in 3D,
+// 3d/common/particle.f90:236-419), Vay, Phys. Plasmas 15, 056701 (2008): u' from E and the
+// rotation at the old gamma, then the new gamma from Vay's quadratic.  Returns 1/gamma.
+__device__ __forceinline__ double vay_update(double fac1, double fac2, double c, double bpx, double bpy, double bpz,
+                                             double epx, double epy, double epz, double uvm1, double uvm2, double uvm3,
+                                             double* g) {
+  double gam = sqrt(c * c + uvm1 * uvm1 + uvm2 * uvm2 + uvm3 * uvm3);
+  const double fac1r = fac1 / gam;
+  const double uvm4 = uvm1 + fac2 * epx + fac1r * (+uvm2 * bpz - uvm3 * bpy);
+  const double uvm5 = uvm2 + fac2 * epy + fac1r * (+uvm3 * bpx - uvm1 * bpz);
+  const double uvm6 = uvm3 + fac2 * epz + fac1r * (+uvm1 * bpy - uvm2 * bpx);
+  const double taux = fac1 * bpx / c;
+  const double tauy = fac1 * bpy / c;
+  const double tauz = fac1 * bpz / c;
+  const double tau2 = taux * taux + tauy * tauy + tauz * tauz;
+  const double ua = (uvm4 * taux + uvm5 * tauy + uvm6 * tauz) / c;
+  const double sigma = 1.0 + (uvm4 * uvm4 + uvm5 * uvm5 + uvm6 * uvm6) / (c * c) - tau2;
+  const double gam2 = 0.5 * (sigma + sqrt(sigma * sigma + 4.0 * (tau2 + ua * ua)));
+  gam = sqrt(gam2);
+  const double txxx = 1.0 / (tau2 + gam2);
+  g[0] = txxx * (gam2 * uvm4 + c * ua * taux + gam * (uvm5 * tauz - uvm6 * tauy));
+  g[1] = txxx * (gam2 * uvm5 + c * ua * tauy + gam * (uvm6 * taux - uvm4 * tauz));
+  g[2] = txxx * (gam2 * uvm6 + c * ua * tauz + gam * (uvm4 * tauy - uvm5 * taux));
+  return 1.0 / gam;
+}
+
+template <bool VAY>
 __global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
   const Grid2D g = d.g;
   const int c0 = blockIdx.x * PUSH_TW;
@@ -74,6 +101,17 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
              + (+tmp[m][2][lo] * sx0 + tmp[m][2][lo + 1] * sx1 + tmp[m][2][lo + 2] * sx2) * sy2;
     }
     const double bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
+    if (VAY) {
+      double gv[3];
+      const double ig = vay_update(fac1, fac2, c, bpx, bpy, bpz, epx, epy, epz, d.A.ux[k], d.A.uy[k], d.A.uz[k], gv);
+      d.B.ux[k] = gv[0];
+      d.B.uy[k] = gv[1];
+      d.B.uz[k] = gv[2];
+      d.B.x[k] = x + gv[0] * delt * ig;
+      d.B.y[k] = y + gv[1] * delt * ig;
+      d.B.id[k] = d.A.id[k];
+      continue;
+    }
     double uvm1 = d.A.ux[k] + fac1 * epx;
     double uvm2 = d.A.uy[k] + fac1 * epy;
     double uvm3 = d.A.uz[k] + fac1 * epz;
@@ -102,7 +140,12 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
 
 void push2d(const Dev2D& d, cudaStream_t s) {
   dim3 grid((d.g.nx + PUSH_TW - 1) / PUSH_TW, d.g.ny, d.ph.nsp);
-  k_push2d<<<grid, PUSH_THREADS, 0, s>>>(d);
+  k_push2d<false><<<grid, PUSH_THREADS, 0, s>>>(d);
+}
+
+void push_vay2d(const Dev2D& d, cudaStream_t s) {
+  dim3 grid((d.g.nx + PUSH_TW - 1) / PUSH_TW, d.g.ny, d.ph.nsp);
+  k_push2d<true><<<grid, PUSH_THREADS, 0, s>>>(d);
 }
 
 // ---------------------------------------------------------------------------

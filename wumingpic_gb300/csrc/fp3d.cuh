@@ -15,6 +15,7 @@ __device__ __forceinline__ size_t f3(const Grid3D& g, int fi, int fj, int fk) { 
 // shared memory (particle.f90:75-92); each particle then gathers 27 points per
 // component in the reference's nesting order.
 // ---------------------------------------------------------------------------
+template <bool VAY>
 __global__ void __launch_bounds__(PUSH_THREADS) k_push3d(Dev3D d) {
   const Grid3D g = d.g;
   // blockIdx.x = x tile + tiles per row * (row of the species), blockIdx.y = species
@@ -81,6 +82,18 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push3d(Dev3D d) {
       f[m] = +pl[0] * shzm + pl[1] * shz + pl[2] * shzp;
     }
     const double bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
+    if (VAY) {
+      double gv[3];
+      const double ig = vay_update(fac1, fac2, c, bpx, bpy, bpz, epx, epy, epz, d.A.ux[k], d.A.uy[k], d.A.uz[k], gv);
+      d.B.ux[k] = gv[0];
+      d.B.uy[k] = gv[1];
+      d.B.uz[k] = gv[2];
+      d.B.x[k] = x + gv[0] * delt * ig;
+      d.B.y[k] = y + gv[1] * delt * ig;
+      d.B.z[k] = z + gv[2] * delt * ig;
+      d.B.id[k] = d.A.id[k];
+      continue;
+    }
     double uvm1 = d.A.ux[k] + fac1 * epx;
     double uvm2 = d.A.uy[k] + fac1 * epy;
     double uvm3 = d.A.uz[k] + fac1 * epz;
@@ -110,7 +123,12 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push3d(Dev3D d) {
 
 void push3d(const Dev3D& d, cudaStream_t s) {
   dim3 grid(((d.g.nx + PUSH_TW - 1) / PUSH_TW) * d.g.ny * d.g.nz, d.ph.nsp);
-  k_push3d<<<grid, PUSH_THREADS, 0, s>>>(d);
+  k_push3d<false><<<grid, PUSH_THREADS, 0, s>>>(d);
+}
+
+void push_vay3d(const Dev3D& d, cudaStream_t s) {
+  dim3 grid(((d.g.nx + PUSH_TW - 1) / PUSH_TW) * d.g.ny * d.g.nz, d.ph.nsp);
+  k_push3d<true><<<grid, PUSH_THREADS, 0, s>>>(d);
 }
 
 // ---------------------------------------------------------------------------

@@ -138,6 +138,7 @@ struct Dev2D {
 // ---- launchers: precision-dependent kernels exist in two builds ----
 #define WPIC_DECLARE_FP_LAUNCHERS                                                          \
   void push2d(const Dev2D& d, cudaStream_t s);                                             \
+  void push_vay2d(const Dev2D& d, cudaStream_t s);                                         \
   void deposit2d(const Dev2D& d, cudaStream_t s);                                          \
   void gkl2d(const Dev2D& d, cudaStream_t s);                                              \
   void cg_init2d(const Dev2D& d, cudaStream_t s);                                          \
@@ -230,6 +231,7 @@ struct Dev3D {
 
 #define WPIC_DECLARE_FP3_LAUNCHERS                       \
   void push3d(const Dev3D& d, cudaStream_t s);           \
+  void push_vay3d(const Dev3D& d, cudaStream_t s);       \
   void deposit3d(const Dev3D& d, cudaStream_t s);        \
   void gkl3d(const Dev3D& d, cudaStream_t s);            \
   void cg_init3d(const Dev3D& d, cudaStream_t s);        \

@@ -68,7 +68,7 @@ module wpic_capi
   integer, save :: wpic_sync_every = 1, wpic_step_count = 0
 
   procedure(wpic_call), pointer :: p_solv => null(), p_fdtd => null(), p_bcx => null(), &
-       p_bcy => null(), p_sort => null()
+       p_bcy => null(), p_sort => null(), p_solv_vay => null()
 
 contains
 
@@ -92,6 +92,10 @@ contains
          import :: c_int, c_ptr
          type(c_ptr), value :: ctx
        end function
+       integer(c_int) function wpic_particle_solv_vay(ctx) bind(C, name="wpic_particle_solv_vay")
+         import :: c_int, c_ptr
+         type(c_ptr), value :: ctx
+       end function
        integer(c_int) function wpic_field_fdtd_i(ctx) bind(C, name="wpic_field_fdtd_i")
          import :: c_int, c_ptr
          type(c_ptr), value :: ctx
@@ -110,6 +114,7 @@ contains
        end function
     end interface
     p_solv => wpic_particle_solv
+    p_solv_vay => wpic_particle_solv_vay
     p_fdtd => wpic_field_fdtd_i
     p_bcx => wpic_bc_particle_x
     p_bcy => wpic_bc_particle_y
@@ -161,12 +166,19 @@ contains
   end subroutine particle__solv
 
   subroutine particle__solv_vay(gp,up,uf,cumcnt,nxs,nxe)
-    integer, intent(in) :: nxs, nxe
-    integer, intent(in) :: cumcnt(*)
-    real(8), intent(in) :: up(*), uf(*)
+    integer, intent(in)  :: nxs, nxe
+    integer, intent(in)  :: cumcnt(wpic_prm%nxgs:wpic_prm%nxge+1,wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    real(8), intent(in)  :: up(*), uf(*)
     real(8), intent(out) :: gp(*)
-    write(0,*) 'wumingpic_gb300: particle__solv_vay is not provided by the GPU library'
-    stop
+    integer(c_int) :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    call wpic_ensure_ctx()
+    if (.not. wpic_uploaded) then
+       np2(:,:) = cumcnt(nxe+1,:,:)
+       call wpic_check(wpic_put_particles(wpic_ctx, 0_c_int, up, np2, cumcnt), 'put up')
+       call wpic_check(wpic_put_fields(wpic_ctx, uf), 'put uf')
+       wpic_uploaded = .true.
+    endif
+    call wpic_check(p_solv_vay(wpic_ctx), 'particle__solv_vay')
   end subroutine particle__solv_vay
 end module particle
 

@@ -51,6 +51,10 @@ module wpic3d_capi
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx
      end function wpic3d_particle_solv
+     integer(c_int) function wpic3d_particle_solv_vay(ctx) bind(C, name="wpic3d_particle_solv_vay")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic3d_particle_solv_vay
      integer(c_int) function wpic3d_field_fdtd_i(ctx) bind(C, name="wpic3d_field_fdtd_i")
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx
@@ -135,12 +139,20 @@ contains
   end subroutine particle__solv
 
   subroutine particle__solv_vay(gp,up,uf,cumcnt,nxs,nxe)
-    integer, intent(in) :: nxs, nxe
-    integer, intent(in) :: cumcnt(*)
-    real(8), intent(in) :: up(*), uf(*)
+    integer, intent(in)  :: nxs, nxe
+    integer, intent(in)  :: cumcnt(wpic3_prm%nxgs:wpic3_prm%nxge+1,wpic3_prm%nys:wpic3_prm%nye, &
+                                   wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    real(8), intent(in)  :: up(*), uf(*)
     real(8), intent(out) :: gp(*)
-    write(0,*) 'wumingpic_gb300: particle__solv_vay is not provided by the GPU library in 3D'
-    stop
+    integer(c_int) :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    call wpic3_ensure_ctx()
+    if (.not. wpic3_uploaded) then
+       np2(:,:,:) = cumcnt(nxe+1,:,:,:)
+       call wpic3_check(wpic3d_put_particles(wpic3_ctx, 0_c_int, up, np2, cumcnt), 'put up')
+       call wpic3_check(wpic3d_put_fields(wpic3_ctx, uf), 'put uf')
+       wpic3_uploaded = .true.
+    endif
+    call wpic3_check(wpic3d_particle_solv_vay(wpic3_ctx), 'particle__solv_vay')
   end subroutine particle__solv_vay
 end module particle
 

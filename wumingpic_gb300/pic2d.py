@@ -108,6 +108,13 @@ class Pic2D:
     def particle__solv(self):
         check(lib().wpic_particle_solv(self._h), "particle__solv")
 
+    def particle__solv_vay(self):
+        check(lib().wpic_particle_solv_vay(self._h), "particle__solv_vay")
+
+    def set_pusher(self, name):
+        """the push of the fused step: "boris" (particle__solv) or "vay" (particle__solv_vay)"""
+        check(lib().wpic_set_pusher(self._h, {"boris": _lib.PUSH_BORIS, "vay": _lib.PUSH_VAY}[name]), "set_pusher")
+
     def field__fdtd_i(self):
         check(lib().wpic_field_fdtd_i(self._h), "field__fdtd_i")
 
