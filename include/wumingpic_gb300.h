@@ -107,6 +107,23 @@ int wpic_particle_solv(wpic_ctx* ctx);
 int wpic_particle_solv_vay(wpic_ctx* ctx);
 /* which push the fused step (wpic_step) uses: WPIC_PUSH_BORIS (default) or WPIC_PUSH_VAY */
 int wpic_set_pusher(wpic_ctx* ctx, int pusher);
+
+/* Moments (the driver's diagnostic block, 2d/proj/weibel/app.f90:121-123).  The device keeps
+ * mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp) in the reference's layout: number density, the three
+ * velocity components and the diagonal of u v at the half-integer nodes, per species.
+ * mom_calc__accl(gp,up,uf,cumcnt,nxs,nxe)   2d/common/mom_calc.f90:48   (FP64 paths): writes gp */
+int wpic_mom_calc_accl(wpic_ctx* ctx);
+/* mom_calc__nvt(mom,gp,np2)   2d/common/mom_calc.f90:164; from_gp = 1 reads gp (after
+ * wpic_mom_calc_accl), 0 reads up.  The particles must be bucket-sorted (cumcnt). */
+int wpic_mom_calc_nvt(wpic_ctx* ctx, int from_gp);
+/* bc__mom(mom): boundary_periodic__mom 2d/common/boundary_periodic.f90:571,
+ * boundary_reconnection__mom 2d/proj/reconnection/boundary_reconnection.f90:582 */
+int wpic_bc_mom(wpic_ctx* ctx);
+/* the device moments to a host array of 7*(nx+2)*(ny+2)*nsp doubles */
+int wpic_get_mom(wpic_ctx* ctx, double* mom);
+/* accl + nvt + bc__mom in one call (all paths; the mixed path computes the half-step push in
+ * FP32 and leaves the particle state untouched); mom may be NULL to keep the result on the device */
+int wpic_moments(wpic_ctx* ctx, double* mom);
 /* field__fdtd_i(uf, up, gp, cumcnt, nxs, nxe, bc__dfield, bc__curre, bc__phi)
  *                                                   2d/common/field.f90:66-186 */
 int wpic_field_fdtd_i(wpic_ctx* ctx);
@@ -217,6 +234,14 @@ int wpic3d_particle_solv(wpic_ctx3d* ctx);
 /* particle__solv_vay(gp, up, uf, cumcnt, nxs, nxe)   3d/common/particle.f90:236 */
 int wpic3d_particle_solv_vay(wpic_ctx3d* ctx);
 int wpic3d_set_pusher(wpic_ctx3d* ctx, int pusher);
+/* mom_calc__accl  3d/common/mom_calc.f90:49; mom_calc__nvt  3d/common/mom_calc.f90:219;
+ * bc__mom = boundary_periodic__mom  3d/common/boundary_periodic.f90:1102;
+ * mom(7, nxgs-1:nxge+1, nys-1:nye+1, nzs-1:nze+1, nsp) */
+int wpic3d_mom_calc_accl(wpic_ctx3d* ctx);
+int wpic3d_mom_calc_nvt(wpic_ctx3d* ctx, int from_gp);
+int wpic3d_bc_mom(wpic_ctx3d* ctx);
+int wpic3d_get_mom(wpic_ctx3d* ctx, double* mom);
+int wpic3d_moments(wpic_ctx3d* ctx, double* mom);
 /* field__fdtd_i(uf, up, gp, cumcnt, nxs, nxe, ...)   3d/common/field.f90:70 */
 int wpic3d_field_fdtd_i(wpic_ctx3d* ctx);
 /* ele_cur + bc__curre, the deposit half of field__fdtd_i (3d/common/field.f90:129-130) */

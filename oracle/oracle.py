@@ -43,6 +43,9 @@ def lib():
             getattr(L, n).argtypes = [vp, dp]
         L.orc2d_particle_solv.argtypes = [vp, dp, dp, dp, ip, i, i]
         L.orc2d_particle_solv_vay.argtypes = [vp, dp, dp, dp, ip, i, i]
+        L.orc2d_mom_calc_accl.argtypes = [vp, dp, dp, dp, ip, i, i]
+        L.orc2d_mom_calc_nvt.argtypes = [vp, dp, dp, ip]
+        L.orc2d_bc_mom.argtypes = [vp, dp]
         L.orc2d_ele_cur.argtypes = [vp, dp, dp, dp, ip, i, i]
         L.orc2d_bc_curre.argtypes = [vp, dp, i, i]
         L.orc2d_bc_dfield.argtypes = [vp, dp, i, i]
@@ -64,6 +67,9 @@ def lib():
                 getattr(L, n).argtypes = [vp, dp]
             L.orc3d_particle_solv.argtypes = [vp, dp, dp, dp, ip, i, i]
             L.orc3d_particle_solv_vay.argtypes = [vp, dp, dp, dp, ip, i, i]
+            L.orc3d_mom_calc_accl.argtypes = [vp, dp, dp, dp, ip, i, i]
+            L.orc3d_mom_calc_nvt.argtypes = [vp, dp, dp, ip]
+            L.orc3d_bc_mom.argtypes = [vp, dp]
             L.orc3d_ele_cur.argtypes = [vp, dp, dp, dp, ip, i, i]
             L.orc3d_bc_curre.argtypes = [vp, dp, i, i]
             L.orc3d_field_fdtd_i.argtypes = [vp, dp, dp, dp, ip, i, i]
@@ -142,6 +148,29 @@ class Oracle2D:
     def particle_solv_vay(self, gp, up, uf, cumcnt):
         return lib().orc2d_particle_solv_vay(self._h, _p(gp, np.float64), _p(up, np.float64), _p(uf, np.float64),
                                              _p(cumcnt, np.int32), self.nxs, self.nxe)
+
+    def mom_shape(self):
+        """mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp)"""
+        return (7, self.nx + 2, self.ny + 2, self.nsp)
+
+    def mom_calc_accl(self, gp, up, uf, cumcnt):
+        return lib().orc2d_mom_calc_accl(self._h, _p(gp, np.float64), _p(up, np.float64), _p(uf, np.float64),
+                                         _p(cumcnt, np.int32), self.nxs, self.nxe)
+
+    def mom_calc_nvt(self, mom, up, np2):
+        return lib().orc2d_mom_calc_nvt(self._h, _p(mom, np.float64), _p(up, np.float64), _p(np2, np.int32))
+
+    def bc_mom(self, mom):
+        return lib().orc2d_bc_mom(self._h, _p(mom, np.float64))
+
+    def moments(self, st):
+        """The driver's diagnostic block (2d/proj/weibel/app.f90:121-123) on a State2D:
+        mom_calc__accl into st.gp, mom_calc__nvt from st.gp, bc__mom.  Returns (status, mom)."""
+        mom = np.zeros(self.mom_shape(), order="F")
+        rc = self.mom_calc_accl(st.gp, st.up, st.uf, st.cumcnt)
+        rc = rc or self.mom_calc_nvt(mom, st.gp, st.np2)
+        rc = rc or self.bc_mom(mom)
+        return rc, mom
 
     def ele_cur(self, uj, up, gp, cumcnt):
         return lib().orc2d_ele_cur(self._h, _p(uj, np.float64), _p(up, np.float64), _p(gp, np.float64),
@@ -250,6 +279,29 @@ class Oracle3D:
     def particle_solv_vay(self, gp, up, uf, cumcnt):
         return lib().orc3d_particle_solv_vay(self._h, _p(gp, np.float64), _p(up, np.float64), _p(uf, np.float64),
                                              _p(cumcnt, np.int32), self.nxs, self.nxe)
+
+    def mom_shape(self):
+        """mom(7, nxgs-1:nxge+1, nys-1:nye+1, nzs-1:nze+1, nsp)"""
+        return (7, self.nx + 2, self.ny + 2, self.nz + 2, self.nsp)
+
+    def mom_calc_accl(self, gp, up, uf, cumcnt):
+        return lib().orc3d_mom_calc_accl(self._h, _p(gp, np.float64), _p(up, np.float64), _p(uf, np.float64),
+                                         _p(cumcnt, np.int32), self.nxs, self.nxe)
+
+    def mom_calc_nvt(self, mom, up, np2):
+        return lib().orc3d_mom_calc_nvt(self._h, _p(mom, np.float64), _p(up, np.float64), _p(np2, np.int32))
+
+    def bc_mom(self, mom):
+        return lib().orc3d_bc_mom(self._h, _p(mom, np.float64))
+
+    def moments(self, st):
+        """The 3D driver's diagnostic block (3d/proj/weibel/app.f90:122-124) on a State3D.
+        Returns (status, mom)."""
+        mom = np.zeros(self.mom_shape(), order="F")
+        rc = self.mom_calc_accl(st.gp, st.up, st.uf, st.cumcnt)
+        rc = rc or self.mom_calc_nvt(mom, st.gp, st.np2)
+        rc = rc or self.bc_mom(mom)
+        return rc, mom
 
     def ele_cur(self, uj, up, gp, cumcnt):
         return lib().orc3d_ele_cur(self._h, _p(uj, np.float64), _p(up, np.float64), _p(gp, np.float64),

@@ -17,6 +17,10 @@
 //   boundary_reconnection__particle_x/dfield/curre/phi (conducting walls in x)
 //                             2d/proj/reconnection/boundary_reconnection.f90:61-99,254-579
 //   energy_history sums       2d/proj/weibel/app.f90:479-545
+//   particle__solv_vay        2d/common/particle.f90:182-315
+//   mom_calc__accl / __nvt    2d/common/mom_calc.f90:48-249
+//   boundary_periodic__mom    2d/common/boundary_periodic.f90:571-636
+//   boundary_reconnection__mom 2d/proj/reconnection/boundary_reconnection.f90:582-647
 //
 // Parity status: UNPINNED.  The reference ships no golden vectors or
 // known-answer tests for this path and cannot be compiled in this image (no
@@ -137,8 +141,14 @@ inline void vay_update(double fac1, double fac2, double c, double bpx, double bp
   *gam_out = 1.0 / gam;
 }
 
+// mode: PUSH_BORIS = particle__solv, PUSH_VAY = particle__solv_vay, PUSH_MOM = mom_calc__accl
+// (2d/common/mom_calc.f90:48-161: the same gather and Boris rotation at half the time step,
+// mom_calc__init halves delt at :36; positions copied, no move, IDs untouched).
+enum { PUSH_BORIS = 0, PUSH_VAY = 1, PUSH_MOM = 2 };
+
 int particle_solv(Orc2D* o, double* gp, const double* up, const double* uf, const int* cumcnt,
-                  int nxs, int nxe, bool vay = false) {
+                  int nxs, int nxe, int mode = PUSH_BORIS) {
+  const bool vay = mode == PUSH_VAY;
   const int nys = o->nys, nye = o->nye;
   const int tw = nxe - nxs + 3;  // tmp(1:6, nxs-1:nxe+1, nys-1:nye+1)
   std::vector<double> tmp((size_t)6 * tw * (nye - nys + 3));
@@ -159,7 +169,7 @@ int particle_solv(Orc2D* o, double* gp, const double* up, const double* uf, cons
       it(6, i, j) = uf[o->iuf(6, i, j)];
     }
 
-  const double d_delx = o->p_d_delx, delt = o->delt, c = o->c;
+  const double d_delx = o->p_d_delx, delt = mode == PUSH_MOM ? o->delt * 0.5 : o->delt, c = o->c;
   // particle loop  (particle.f90:85-171)
 #pragma omp parallel for
   for (int j = nys; j <= nye; ++j)
@@ -214,9 +224,14 @@ int particle_solv(Orc2D* o, double* gp, const double* up, const double* uf, cons
           const double g3 = uvm1 + fac1 * epx;
           const double g4 = uvm2 + fac1 * epy;
           const double g5 = uvm3 + fac1 * epz;
+          if (mode == PUSH_MOM) {  // mom_calc.f90:154-159
+            gp[o->iup(1, ii, j, isp)] = up[o->iup(1, ii, j, isp)];
+            gp[o->iup(2, ii, j, isp)] = up[o->iup(2, ii, j, isp)];
+          }
           gp[o->iup(3, ii, j, isp)] = g3;
           gp[o->iup(4, ii, j, isp)] = g4;
           gp[o->iup(5, ii, j, isp)] = g5;
+          if (mode == PUSH_MOM) continue;
           // move
           gam = 1.0 / std::sqrt(1.0 + (+g3 * g3 + g4 * g4 + g5 * g5) / (c * c));
           gp[o->iup(1, ii, j, isp)] = up[o->iup(1, ii, j, isp)] + g3 * delt * gam;
@@ -224,7 +239,7 @@ int particle_solv(Orc2D* o, double* gp, const double* up, const double* uf, cons
         }
       }
   // particle IDs copied wholesale (particle.f90:173-177)
-  if (o->ndim == 6) {
+  if (o->ndim == 6 && mode != PUSH_MOM) {
     const size_t n = (size_t)o->np * (nye - nys + 1) * o->nsp;
 #pragma omp parallel for
     for (long long k = 0; k < (long long)n; ++k) gp[(size_t)k * 6 + 5] = up[(size_t)k * 6 + 5];
@@ -838,6 +853,70 @@ int energy(Orc2D* o, const double* up, const double* uf, const int* np2, double*
   return ORC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// mom_calc__nvt  (2d/common/mom_calc.f90:164-249)
+// mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp): number density, velocity and diagonal
+// of u v at the half-integer nodes, linear (area) weights, single-thread order.
+// ---------------------------------------------------------------------------
+size_t imom(const Orc2D* o, int l, int i, int j, int isp) {
+  const size_t nxm = (size_t)(o->nxge - o->nxgs + 3), nym = (size_t)(o->nye - o->nys + 3);
+  return (size_t)(l - 1) + 7 * ((size_t)(i - (o->nxgs - 1)) + nxm * ((size_t)(j - (o->nys - 1)) + nym * (size_t)(isp - 1)));
+}
+
+int mom_nvt(Orc2D* o, double* mom, const double* up, const int* np2) {
+  const size_t n = 7 * (size_t)(o->nxge - o->nxgs + 3) * (o->nye - o->nys + 3) * o->nsp;
+  std::fill(mom, mom + n, 0.0);
+  const double d_delx = 1.0 / o->delx, c = o->c;
+  for (int isp = 1; isp <= o->nsp; ++isp)
+    for (int j = o->nys; j <= o->nye; ++j)
+      for (int ii = 1; ii <= np2[o->inp2(j, isp)]; ++ii) {
+        const double x = up[o->iup(1, ii, j, isp)], y = up[o->iup(2, ii, j, isp)];
+        const double u1 = up[o->iup(3, ii, j, isp)], u2 = up[o->iup(4, ii, j, isp)], u3 = up[o->iup(5, ii, j, isp)];
+        const int ih = (int)(x * d_delx - 0.5);  // Fortran int(): truncation toward zero
+        const int jh = (int)(y * d_delx - 0.5);
+        if (ih < o->nxgs - 1 || ih > o->nxge || jh < o->nys - 1 || jh > o->nye) return ORC_OUT_OF_RANGE;
+        const double dx = x * d_delx - 0.5 - ih, dxm = 1. - dx;
+        const double dy = y * d_delx - 0.5 - jh, dym = 1. - dy;
+        const double gam = 1. / std::sqrt(1.0 + (+u1 * u1 + u2 * u2 + u3 * u3) / (c * c));
+        const double wx[2] = {dxm, dx}, wy[2] = {dym, dy};
+        const double pre[7] = {1.0, u1 * gam, u2 * gam, u3 * gam, u1 * u1 * gam, u2 * u2 * gam, u3 * u3 * gam};
+        for (int l = 1; l <= 7; ++l)
+          for (int b = 0; b < 2; ++b)
+            for (int a = 0; a < 2; ++a) {
+              double& m = mom[imom(o, l, ih + a, jh + b, isp)];
+              m = l == 1 ? m + wx[a] * wy[b] : m + pre[l - 1] * wx[a] * wy[b];
+            }
+      }
+  return ORC_OK;
+}
+
+// boundary_periodic__mom (2d/common/boundary_periodic.f90:571-636) with one rank (the
+// y exchanges are self-exchanges); boundary_reconnection__mom
+// (2d/proj/reconnection/boundary_reconnection.f90:582-647) folds the x ghosts onto the
+// adjacent wall columns instead of the periodic images.
+void bc_mom(Orc2D* o, double* mom) {
+  const int nxgs = o->nxgs, nxge = o->nxge, nys = o->nys, nye = o->nye;
+  for (int isp = 1; isp <= o->nsp; ++isp)
+    for (int j = nys - 1; j <= nye + 1; ++j)
+      for (int l = 1; l <= 7; ++l) {
+        if (o->bc_kind == BC_RECONNECTION) {
+          mom[imom(o, l, nxgs, j, isp)] = mom[imom(o, l, nxgs, j, isp)] + mom[imom(o, l, nxgs - 1, j, isp)];
+          mom[imom(o, l, nxge, j, isp)] = mom[imom(o, l, nxge, j, isp)] + mom[imom(o, l, nxge + 1, j, isp)];
+        } else {
+          mom[imom(o, l, nxgs, j, isp)] = mom[imom(o, l, nxgs, j, isp)] + mom[imom(o, l, nxge + 1, j, isp)];
+          mom[imom(o, l, nxge, j, isp)] = mom[imom(o, l, nxge, j, isp)] + mom[imom(o, l, nxgs - 1, j, isp)];
+        }
+      }
+  for (int isp = 1; isp <= o->nsp; ++isp) {
+    for (int i = nxgs - 1; i <= nxge + 1; ++i)
+      for (int l = 1; l <= 7; ++l)
+        mom[imom(o, l, i, nye, isp)] = mom[imom(o, l, i, nye, isp)] + mom[imom(o, l, i, nys - 1, isp)];
+    for (int i = nxgs - 1; i <= nxge + 1; ++i)
+      for (int l = 1; l <= 7; ++l)
+        mom[imom(o, l, i, nys, isp)] = mom[imom(o, l, i, nys, isp)] + mom[imom(o, l, i, nye + 1, isp)];
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -898,8 +977,16 @@ int orc2d_particle_solv(void* h, double* gp, const double* up, const double* uf,
 }
 int orc2d_particle_solv_vay(void* h, double* gp, const double* up, const double* uf, const int* cumcnt, int nxs,
                             int nxe) {
-  return particle_solv((Orc2D*)h, gp, up, uf, cumcnt, nxs, nxe, true);
+  return particle_solv((Orc2D*)h, gp, up, uf, cumcnt, nxs, nxe, PUSH_VAY);
 }
+int orc2d_mom_calc_accl(void* h, double* gp, const double* up, const double* uf, const int* cumcnt, int nxs,
+                        int nxe) {
+  return particle_solv((Orc2D*)h, gp, up, uf, cumcnt, nxs, nxe, PUSH_MOM);
+}
+int orc2d_mom_calc_nvt(void* h, double* mom, const double* up, const int* np2) {
+  return mom_nvt((Orc2D*)h, mom, up, np2);
+}
+int orc2d_bc_mom(void* h, double* mom) { bc_mom((Orc2D*)h, mom); return 0; }
 int orc2d_ele_cur(void* h, double* uj, const double* up, const double* gp, const int* cumcnt, int nxs, int nxe) {
   return ele_cur((Orc2D*)h, uj, up, gp, cumcnt, nxs, nxe);
 }

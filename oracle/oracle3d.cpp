@@ -15,6 +15,9 @@
 //   boundary_periodic__particle_x/_yz/dfield/curre/phi
 //                             3d/common/boundary_periodic.f90:68-1099
 //   energy_history sums       3d/proj/weibel/app.f90:509-577
+//   particle__solv_vay        3d/common/particle.f90:236-419
+//   mom_calc__accl / __nvt    3d/common/mom_calc.f90:49-332
+//   boundary_periodic__mom    3d/common/boundary_periodic.f90:1102-1235
 //
 // Parity status: UNPINNED (no golden vectors in the reference for this path;
 // no Fortran compiler or MPI in this image).  It is checked against physical
@@ -117,8 +120,14 @@ inline void vay_update(double fac1, double fac2, double c, double bpx, double bp
   *gam_out = 1.0 / gam;
 }
 
+// mode: PUSH_BORIS = particle__solv, PUSH_VAY = particle__solv_vay, PUSH_MOM = mom_calc__accl
+// (3d/common/mom_calc.f90:49-216: the same gather and rotation at half the time step,
+// mom_calc__init halves delt at :36; positions copied, no move, IDs untouched).
+enum { PUSH_BORIS = 0, PUSH_VAY = 1, PUSH_MOM = 2 };
+
 int particle_solv(Orc3D* o, double* gp, const double* up, const double* uf, const int* cumcnt, int nxs, int nxe,
-                  bool vay = false) {
+                  int mode = PUSH_BORIS) {
+  const bool vay = mode == PUSH_VAY;
   const int nys = o->nys, nye = o->nye, nzs = o->nzs, nze = o->nze;
   const int tw = nxe - nxs + 3, th = nye - nys + 3, td = nze - nzs + 3;  // tmpf(6, nxs-1:nxe+1, nys-1:nye+1, nzs-1:nze+1)
   std::vector<double> tmpf((size_t)6 * tw * th * td);
@@ -140,7 +149,7 @@ int particle_solv(Orc3D* o, double* gp, const double* up, const double* uf, cons
         T(5, i, j, k) = 5e-1 * (+U(5, i, j, k) + U(5, i, j + 1, k));
         T(6, i, j, k) = 5e-1 * (+U(6, i, j, k) + U(6, i, j, k + 1));
       }
-  const double d_delx = o->d_delx, delt = o->delt, c = o->c;
+  const double d_delx = o->d_delx, delt = mode == PUSH_MOM ? o->delt * 5e-1 : o->delt, c = o->c;
 #pragma omp parallel for
   for (int k = nzs; k <= nze; ++k)
     for (int j = nys; j <= nye; ++j)
@@ -199,6 +208,12 @@ int particle_solv(Orc3D* o, double* gp, const double* up, const double* uf, cons
             g[o->iup(4, ii, j, k, isp)] = uvm1 + fac1 * epx;
             g[o->iup(5, ii, j, k, isp)] = uvm2 + fac1 * epy;
             g[o->iup(6, ii, j, k, isp)] = uvm3 + fac1 * epz;
+            if (mode == PUSH_MOM) {  // mom_calc.f90:204-209
+              g[o->iup(1, ii, j, k, isp)] = up[o->iup(1, ii, j, k, isp)];
+              g[o->iup(2, ii, j, k, isp)] = up[o->iup(2, ii, j, k, isp)];
+              g[o->iup(3, ii, j, k, isp)] = up[o->iup(3, ii, j, k, isp)];
+              continue;
+            }
             const double g4 = g[o->iup(4, ii, j, k, isp)], g5 = g[o->iup(5, ii, j, k, isp)], g6 = g[o->iup(6, ii, j, k, isp)];
             gam = 1e0 / std::sqrt(1e0 + (+g4 * g4 + g5 * g5 + g6 * g6) / (c * c));
             g[o->iup(1, ii, j, k, isp)] = up[o->iup(1, ii, j, k, isp)] + g4 * delt * gam;
@@ -206,7 +221,7 @@ int particle_solv(Orc3D* o, double* gp, const double* up, const double* uf, cons
             g[o->iup(3, ii, j, k, isp)] = up[o->iup(3, ii, j, k, isp)] + g6 * delt * gam;
           }
         }
-  if (o->ndim == 7) {
+  if (o->ndim == 7 && mode != PUSH_MOM) {
     for (int isp = 1; isp <= o->nsp; ++isp)
       for (int k = nzs; k <= nze; ++k)
         for (int j = nys; j <= nye; ++j)
@@ -932,6 +947,82 @@ int energy(Orc3D* o, const double* up, const double* uf, const int* np2, double*
   return ORC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// mom_calc__nvt  (3d/common/mom_calc.f90:219-332)
+// mom(7, nxgs-1:nxge+1, nys-1:nye+1, nzs-1:nze+1, nsp); floor() for the node index and
+// the offset taken without d_delx, as the 3D reference writes them (:242-251).
+// ---------------------------------------------------------------------------
+size_t imom(const Orc3D* o, int l, int i, int j, int k, int isp) {
+  const size_t nxm = (size_t)(o->nxge - o->nxgs + 3), nym = (size_t)(o->nye - o->nys + 3),
+               nzm = (size_t)(o->nze - o->nzs + 3);
+  return (size_t)(l - 1) +
+         7 * ((size_t)(i - (o->nxgs - 1)) +
+              nxm * ((size_t)(j - (o->nys - 1)) + nym * ((size_t)(k - (o->nzs - 1)) + nzm * (size_t)(isp - 1))));
+}
+
+int mom_nvt(Orc3D* o, double* mom, const double* up, const int* np2) {
+  const size_t n = 7 * (size_t)(o->nxge - o->nxgs + 3) * (o->nye - o->nys + 3) * (o->nze - o->nzs + 3) * o->nsp;
+  std::fill(mom, mom + n, 0.0);
+  const double d_delx = 1e0 / o->delx, c = o->c;
+  for (int isp = 1; isp <= o->nsp; ++isp)
+    for (int k = o->nzs; k <= o->nze; ++k)
+      for (int j = o->nys; j <= o->nye; ++j)
+        for (int ii = 1; ii <= np2[o->inp2(j, k, isp)]; ++ii) {
+          const double x = up[o->iup(1, ii, j, k, isp)], y = up[o->iup(2, ii, j, k, isp)],
+                       z = up[o->iup(3, ii, j, k, isp)];
+          const double u1 = up[o->iup(4, ii, j, k, isp)], u2 = up[o->iup(5, ii, j, k, isp)],
+                       u3 = up[o->iup(6, ii, j, k, isp)];
+          const int ih = (int)std::floor(x * d_delx - 5e-1);
+          const int jh = (int)std::floor(y * d_delx - 5e-1);
+          const int kh = (int)std::floor(z * d_delx - 5e-1);
+          if (ih < o->nxgs - 1 || ih > o->nxge || jh < o->nys - 1 || jh > o->nye || kh < o->nzs - 1 || kh > o->nze)
+            return ORC_OUT_OF_RANGE;
+          const double dx = x - 5e-1 - ih, dxm = 1e0 - dx;
+          const double dy = y - 5e-1 - jh, dym = 1e0 - dy;
+          const double dz = z - 5e-1 - kh, dzm = 1e0 - dz;
+          const double gam = 1e0 / std::sqrt(1e0 + (+u1 * u1 + u2 * u2 + u3 * u3) / (c * c));
+          const double wx[2] = {dxm, dx}, wy[2] = {dym, dy}, wz[2] = {dzm, dz};
+          const double pre[7] = {1.0, u1 * gam, u2 * gam, u3 * gam, u1 * u1 * gam, u2 * u2 * gam, u3 * u3 * gam};
+          for (int l = 1; l <= 7; ++l)
+            for (int cz = 0; cz < 2; ++cz)
+              for (int b = 0; b < 2; ++b)
+                for (int a = 0; a < 2; ++a) {
+                  double& m = mom[imom(o, l, ih + a, jh + b, kh + cz, isp)];
+                  m = l == 1 ? m + wx[a] * wy[b] * wz[cz] : m + pre[l - 1] * wx[a] * wy[b] * wz[cz];
+                }
+        }
+  return ORC_OK;
+}
+
+// boundary_periodic__mom (3d/common/boundary_periodic.f90:1102-1235), one rank: x images,
+// then the y self-exchange over every z layer, then the z self-exchange over the interior
+// y rows.
+void bc_mom(Orc3D* o, double* mom) {
+  const int nxgs = o->nxgs, nxge = o->nxge, nys = o->nys, nye = o->nye, nzs = o->nzs, nze = o->nze;
+  auto M = [&](int l, int i, int j, int k, int isp) -> double& { return mom[imom(o, l, i, j, k, isp)]; };
+  for (int isp = 1; isp <= o->nsp; ++isp)
+    for (int k = nzs - 1; k <= nze + 1; ++k)
+      for (int j = nys - 1; j <= nye + 1; ++j)
+        for (int l = 1; l <= 7; ++l) {
+          M(l, nxgs, j, k, isp) = M(l, nxgs, j, k, isp) + M(l, nxge + 1, j, k, isp);
+          M(l, nxge, j, k, isp) = M(l, nxge, j, k, isp) + M(l, nxgs - 1, j, k, isp);
+        }
+  for (int isp = 1; isp <= o->nsp; ++isp) {
+    for (int k = nzs - 1; k <= nze + 1; ++k)
+      for (int i = nxgs - 1; i <= nxge + 1; ++i)
+        for (int l = 1; l <= 7; ++l) M(l, i, nye, k, isp) = M(l, i, nye, k, isp) + M(l, i, nys - 1, k, isp);
+    for (int k = nzs - 1; k <= nze + 1; ++k)
+      for (int i = nxgs - 1; i <= nxge + 1; ++i)
+        for (int l = 1; l <= 7; ++l) M(l, i, nys, k, isp) = M(l, i, nys, k, isp) + M(l, i, nye + 1, k, isp);
+    for (int j = nys; j <= nye; ++j)
+      for (int i = nxgs - 1; i <= nxge + 1; ++i)
+        for (int l = 1; l <= 7; ++l) M(l, i, j, nze, isp) = M(l, i, j, nze, isp) + M(l, i, j, nzs - 1, isp);
+    for (int j = nys; j <= nye; ++j)
+      for (int i = nxgs - 1; i <= nxge + 1; ++i)
+        for (int l = 1; l <= 7; ++l) M(l, i, j, nzs, isp) = M(l, i, j, nzs, isp) + M(l, i, j, nze + 1, isp);
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -983,7 +1074,18 @@ int orc3d_particle_solv(void* h, double* gp, const double* up, const double* uf,
 }
 int orc3d_particle_solv_vay(void* h, double* gp, const double* up, const double* uf, const int* cumcnt, int nxs,
                             int nxe) {
-  return particle_solv((Orc3D*)h, gp, up, uf, cumcnt, nxs, nxe, true);
+  return particle_solv((Orc3D*)h, gp, up, uf, cumcnt, nxs, nxe, PUSH_VAY);
+}
+int orc3d_mom_calc_accl(void* h, double* gp, const double* up, const double* uf, const int* cumcnt, int nxs,
+                        int nxe) {
+  return particle_solv((Orc3D*)h, gp, up, uf, cumcnt, nxs, nxe, PUSH_MOM);
+}
+int orc3d_mom_calc_nvt(void* h, double* mom, const double* up, const int* np2) {
+  return mom_nvt((Orc3D*)h, mom, up, np2);
+}
+int orc3d_bc_mom(void* h, double* mom) {
+  bc_mom((Orc3D*)h, mom);
+  return 0;
 }
 int orc3d_ele_cur(void* h, double* uj, const double* up, const double* gp, const int* cumcnt, int nxs, int nxe) {
   return ele_cur((Orc3D*)h, uj, up, gp, cumcnt, nxs, nxe);

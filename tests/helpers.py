@@ -268,3 +268,68 @@ def literal_particle_yz(up, np2, p):
                     row[:, n2 + m] = arr[iii + m]
                 np2[j - nys, k - nzs, isp] = n2 + cnt
     return np2
+
+
+def literal_moments2d(p, gp, np2, bc="periodic"):
+    """mom_calc__nvt + bc__mom (2d/common/mom_calc.f90:164-249,
+    2d/common/boundary_periodic.f90:571-636) in numpy, independent of the oracle's
+    loops: np.add.at per node offset, then the ghost folds.  Summation order differs
+    from the reference's, so agreement is to round-off."""
+    nxm, nym = p.nx + 2, p.ny + 2
+    mom = np.zeros((7, nxm, nym, p.nsp))
+    for isp in range(p.nsp):
+        for jj in range(p.ny):
+            n = np2[jj, isp]
+            x = gp[0, :n, jj, isp] / p.delx
+            y = gp[1, :n, jj, isp] / p.delx
+            u = gp[2:5, :n, jj, isp]
+            ih = np.trunc(x - 0.5).astype(int)
+            jh = np.trunc(y - 0.5).astype(int)
+            dx, dy = x - 0.5 - ih, y - 0.5 - jh
+            gam = 1.0 / np.sqrt(1.0 + (u * u).sum(0) / (p.c * p.c))
+            pre = [np.ones(n), u[0] * gam, u[1] * gam, u[2] * gam, u[0] ** 2 * gam, u[1] ** 2 * gam, u[2] ** 2 * gam]
+            for a, wx in ((0, 1.0 - dx), (1, dx)):
+                for b, wy in ((0, 1.0 - dy), (1, dy)):
+                    for l in range(7):
+                        np.add.at(mom[l, :, :, isp], (ih + a - (p.nxgs - 1), jh + b - (p.nygs - 1)), pre[l] * wx * wy)
+    if bc == "reconnection":
+        mom[:, 1] += mom[:, 0]
+        mom[:, nxm - 2] += mom[:, nxm - 1]
+    else:
+        mom[:, 1] += mom[:, nxm - 1]
+        mom[:, nxm - 2] += mom[:, 0]
+    mom[:, :, nym - 2] += mom[:, :, 0]
+    mom[:, :, 1] += mom[:, :, nym - 1]
+    return mom
+
+
+def literal_moments3d(p, gp, np2):
+    """mom_calc__nvt + bc__mom in 3D (3d/common/mom_calc.f90:219-332,
+    3d/common/boundary_periodic.f90:1102-1235) in numpy."""
+    nxm, nym, nzm = p.nx + 2, p.ny + 2, p.nz + 2
+    mom = np.zeros((7, nxm, nym, nzm, p.nsp))
+    for isp in range(p.nsp):
+        for kk in range(p.nz):
+            for jj in range(p.ny):
+                n = np2[jj, kk, isp]
+                r = gp[0:3, :n, jj, kk, isp]
+                u = gp[3:6, :n, jj, kk, isp]
+                h = np.floor(r / p.delx - 0.5).astype(int)
+                d = r - 0.5 - h
+                gam = 1.0 / np.sqrt(1.0 + (u * u).sum(0) / (p.c * p.c))
+                pre = [np.ones(n), u[0] * gam, u[1] * gam, u[2] * gam, u[0] ** 2 * gam, u[1] ** 2 * gam,
+                       u[2] ** 2 * gam]
+                for a in (0, 1):
+                    for b in (0, 1):
+                        for cz in (0, 1):
+                            w = (d[0] if a else 1 - d[0]) * (d[1] if b else 1 - d[1]) * (d[2] if cz else 1 - d[2])
+                            idx = (h[0] + a - (p.nxgs - 1), h[1] + b - (p.nygs - 1), h[2] + cz - (p.nzgs - 1))
+                            for l in range(7):
+                                np.add.at(mom[l, :, :, :, isp], idx, pre[l] * w)
+    mom[:, 1] += mom[:, nxm - 1]
+    mom[:, nxm - 2] += mom[:, 0]
+    mom[:, :, nym - 2] += mom[:, :, 0]
+    mom[:, :, 1] += mom[:, :, nym - 1]
+    mom[:, :, 1:nym - 1, nzm - 2] += mom[:, :, 1:nym - 1, 0]
+    mom[:, :, 1:nym - 1, 1] += mom[:, :, 1:nym - 1, nzm - 1]
+    return mom

@@ -387,3 +387,107 @@ def test_exact_step_matches_golden_fixture(gpu_lib):
     assert_particles(out.up, out.np2, ref["up1"], ref["np21"])
     np.testing.assert_array_equal(out.cumcnt, ref["cumcnt1"])
     assert_field(out.uf, ref["uf1"], REL)
+
+
+# ---- moments: mom_calc__accl, mom_calc__nvt, bc__mom (2d/proj/weibel/app.f90:121-123) ----
+
+def _valid_rows(a, np2, comps):
+    for isp in range(a.shape[3]):
+        for jj in range(a.shape[2]):
+            yield a[comps, :np2[jj, isp], jj, isp]
+
+
+@pytest.mark.parametrize("precision,rel", [("fp64_exact", 0.0), ("fp64", REL)])
+def test_mom_calc_accl_parity(gpu_lib, precision, rel):
+    """The half-step push into gp: positions copied, momenta within the tolerance."""
+    p, st = perturbed_case(seed=51, u_the=0.2)
+    st.uf[:3] *= 40.0
+    g = make_gpu(p, precision, gpu_lib)
+    g.put_state(st)
+    g.mom_calc__accl()
+    gp_gpu, np2, _ = g.get_particles(1)
+    ref = st.copy()
+    assert make_oracle(p).mom_calc_accl(ref.gp, ref.up, ref.uf, ref.cumcnt) == 0
+    np.testing.assert_array_equal(np2, ref.np2)
+    for a, b in zip(_valid_rows(gp_gpu, np2, slice(0, 5)), _valid_rows(ref.gp, ref.np2, slice(0, 5))):
+        if rel == 0.0:
+            np.testing.assert_array_equal(a, b)
+        else:
+            np.testing.assert_allclose(a, b, rtol=0, atol=rel * max(np.abs(b).max(initial=0.0), 1e-300))
+
+
+@pytest.mark.parametrize("bc", ["periodic", "reconnection"])
+@pytest.mark.parametrize("precision,rel", [("fp64_exact", 0.0), ("fp64", REL)])
+def test_moments_parity(gpu_lib, precision, rel, bc):
+    """mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp) including the ghost nodes: bit-exact in the
+    exact build (the node gather keeps the single-thread summation order), 1e-12 otherwise."""
+    p, st = perturbed_case(seed=52, u_the=0.2, bc=bc)
+    g = make_gpu(p, precision, gpu_lib)
+    g.put_state(st)
+    mom = g.moments()
+    up_after, np2_after, _ = g.get_particles(0)
+    rc, ref = make_oracle(p).moments(st.copy())
+    assert rc == 0
+    assert_field(mom, ref, rel)
+    assert_particles(up_after, np2_after, st.up, st.np2)  # the state is not modified
+
+
+def test_mom_calc_nvt_stages_and_source(gpu_lib):
+    """The three stages called one by one, and mom_calc__nvt on up, match the oracle."""
+    p, st = perturbed_case(seed=53, u_the=0.2)
+    g = make_gpu(p, "fp64_exact", gpu_lib)
+    g.put_state(st)
+    o = make_oracle(p)
+    g.mom_calc__nvt(from_gp=False)
+    a = g.get_mom()
+    ref = np.zeros(o.mom_shape(), order="F")
+    assert o.mom_calc_nvt(ref, st.up, st.np2) == 0
+    np.testing.assert_array_equal(a, ref)
+    g.bc__mom()
+    assert o.bc_mom(ref) == 0
+    np.testing.assert_array_equal(g.get_mom(), ref)
+
+
+def test_mom_calc_nvt_on_pushed_and_displaced_particles(gpu_lib):
+    """mom_calc__nvt only needs each particle's 2 x 2 node stencil to lie within the 3 x 3
+    nodes around its bucket cell: gp straight after particle__solv (moved < 1/2 cell) gives
+    the oracle's moments bit for bit; a particle displaced further is reported (out of
+    range) instead of being dropped."""
+    from wumingpic_gb300._lib import WpicError
+    p, st = perturbed_case(seed=54, u_the=0.3)
+    g = make_gpu(p, "fp64_exact", gpu_lib)
+    g.put_state(st)
+    g.particle__solv()
+    gp, np2, cc = g.get_particles(1)
+    g.mom_calc__nvt(from_gp=True)
+    o = make_oracle(p)
+    ref = np.zeros(o.mom_shape(), order="F")
+    assert o.mom_calc_nvt(ref, gp, np2) == 0
+    np.testing.assert_array_equal(g.get_mom(), ref)
+    k = cc[5, 1, 0]  # first particle of cell 5 in row 1
+    gp[0, k, 1, 0] += 1.6
+    g.put_particles(1, gp, np2)
+    with pytest.raises(WpicError) as e:
+        g.mom_calc__nvt(from_gp=True)
+    assert e.value.status == _lib.OUT_OF_RANGE
+    g.moments()  # the context stays usable
+
+
+@pytest.mark.parametrize("bc", ["periodic", "reconnection"])
+def test_moments_mixed_against_oracle(gpu_lib, bc):
+    """Mixed path: FP32 half-step push and FP32 tile sums against the FP64 oracle run on the
+    same (FP32-stored) particles: within 2e-5 of each moment's largest magnitude."""
+    p, st = perturbed_case(seed=55, nx=32, ny=32, ppc=8, u_the=0.2, bc=bc)
+    g = make_gpu(p, "mixed", gpu_lib)
+    g.put_state(st)
+    mom = g.moments()
+    cur = g.get_state()
+    cur.uf[...] = st.uf
+    rc, ref = make_oracle(p).moments(cur)
+    assert rc == 0
+    for l in range(7):
+        for isp in range(p.nsp):
+            scale = np.abs(ref[l, :, :, isp]).max()
+            np.testing.assert_allclose(mom[l, :, :, isp], ref[l, :, :, isp], rtol=0, atol=2e-5 * scale)
+    after = g.get_state()
+    np.testing.assert_array_equal(after.up, cur.up)

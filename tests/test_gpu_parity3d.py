@@ -242,3 +242,38 @@ def test_device_loader_3d(gpu_lib):
     assert g.num_particles() == p.n_particles
     e = g.energy()
     assert np.isfinite(e).all() and e[1] > 0
+
+
+@pytest.mark.parametrize("precision,rel", [("fp64_exact", 0.0), ("fp64", REL)])
+def test_mom_calc_accl_parity_3d(gpu_lib, precision, rel):
+    p, st = perturbed_case(seed=51, u_the=0.2)
+    st.uf[:3] *= 40.0
+    g = make_gpu(p, precision, gpu_lib)
+    g.put_state(st)
+    g.mom_calc__accl()
+    gp_gpu, np2, _ = g.get_particles(1)
+    ref = st.copy()
+    assert make_oracle(p).mom_calc_accl(ref.gp, ref.up, ref.uf, ref.cumcnt) == 0
+    np.testing.assert_array_equal(np2, ref.np2)
+    for a, b in zip(rows(gp_gpu, np2), rows(ref.gp, ref.np2)):
+        if rel == 0.0:
+            np.testing.assert_array_equal(a[:6], b[:6])
+        else:
+            np.testing.assert_allclose(a[:6], b[:6], rtol=0, atol=rel * max(np.abs(b[:6]).max(initial=0.0), 1e-300))
+
+
+@pytest.mark.parametrize("precision,rel", [("fp64_exact", 0.0), ("fp64", REL)])
+def test_moments_parity_3d(gpu_lib, precision, rel):
+    p, st = perturbed_case(seed=52, u_the=0.2)
+    g = make_gpu(p, precision, gpu_lib)
+    g.put_state(st)
+    mom = g.moments()
+    rc, ref = make_oracle(p).moments(st.copy())
+    assert rc == 0
+    assert_field(mom, ref, rel)
+    o = make_oracle(p)
+    g.mom_calc__nvt(from_gp=False)
+    g.bc__mom()
+    ref2 = np.zeros(o.mom_shape(), order="F")
+    assert o.mom_calc_nvt(ref2, st.up, st.np2) == 0 and o.bc_mom(ref2) == 0
+    assert_field(g.get_mom(), ref2, rel)

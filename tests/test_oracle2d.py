@@ -7,7 +7,8 @@ import numpy as np
 import pytest
 
 from oracle.oracle import Oracle2D
-from tests.helpers import closed_form_plan, continuity_residual, literal_particle_y, small_case, small_plasma
+from tests.helpers import (closed_form_plan, continuity_residual, literal_moments2d, literal_particle_y, small_case,
+                           small_plasma)
 from wumingpic_gb300.loader import load_weibel2d
 
 
@@ -275,3 +276,41 @@ def test_vay_keeps_relativistic_exb_drift_force_free():
         np.testing.assert_allclose(st.gp[3:5, :n, 0, isp], 0.0, atol=1e-12 * ux)
     n = st.np2[0, 1]
     assert np.abs(gb[2:5, :n, 0, 1] - st.up[2:5, :n, 0, 1]).max() > 1e-5 * ux
+
+
+@pytest.mark.parametrize("bc", ["periodic", "reconnection"])
+def test_moments_match_numpy_restatement(bc):
+    """mom_calc__accl -> mom_calc__nvt -> bc__mom (2d/proj/weibel/app.f90:121-123) against an
+    independent numpy restatement of the deposit and the ghost folds."""
+    p, st = small_case(seed=23, u_the=0.2, bc=bc)
+    rng = np.random.default_rng(23)
+    st.uf[...] = 0.02 * rng.standard_normal(st.uf.shape)
+    o = make_oracle(p)
+    rc, mom = o.moments(st)
+    assert rc == 0
+    ref = literal_moments2d(p, st.gp, st.np2, bc=bc)
+    scale = np.abs(ref).max(axis=(1, 2, 3), keepdims=True)
+    np.testing.assert_allclose(mom, ref, rtol=0, atol=1e-13 * scale.max())
+    # particle number: the linear weights of each particle sum to one over the interior nodes
+    for isp in range(p.nsp):
+        n = mom[0, 1:p.nx + 1, 1:p.ny + 1, isp].sum()
+        if bc == "periodic":
+            np.testing.assert_allclose(n, st.np2[:, isp].sum(), rtol=1e-12)
+
+
+def test_mom_calc_accl_is_a_half_step_in_pure_e():
+    """With B = 0 the half-step push gives u + (q/m)(dt/2) E and leaves the positions."""
+    p, st = small_case(seed=29, u_the=0.2)
+    q, r = p.charges()
+    e = (0.05, -0.02, 0.03)
+    _uniform_fields(st.uf, (0.0, 0.0, 0.0), e)
+    o = make_oracle(p)
+    assert o.mom_calc_accl(st.gp, st.up, st.uf, st.cumcnt) == 0
+    for isp in range(p.nsp):
+        for jj in range(p.ny):
+            n = st.np2[jj, isp]
+            np.testing.assert_array_equal(st.gp[0:2, :n, jj, isp], st.up[0:2, :n, jj, isp])
+            for k in range(3):
+                np.testing.assert_allclose(st.gp[2 + k, :n, jj, isp],
+                                           st.up[2 + k, :n, jj, isp] + q[isp] / r[isp] * 0.5 * p.delt * e[k],
+                                           rtol=1e-13, atol=1e-16)

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from oracle.oracle import Oracle3D
-from tests.helpers import continuity_residual3d, literal_particle_yz, small_case3d
+from tests.helpers import continuity_residual3d, literal_moments3d, literal_particle_yz, small_case3d
 
 
 def make_oracle3d(p, **kw):
@@ -224,3 +224,18 @@ def test_vay_equals_boris_in_pure_e_3d():
                 n = st.np2[jj, kk, isp]
                 np.testing.assert_allclose(st.gp[:6, :n, jj, kk, isp], gb[:6, :n, jj, kk, isp],
                                            rtol=1e-13, atol=1e-15)
+
+
+def test_moments_match_numpy_restatement_3d():
+    p, st = small_case3d(seed=23, u_the=0.2)
+    rng = np.random.default_rng(23)
+    core = 0.02 * rng.standard_normal((6, p.nx, p.ny, p.nz))
+    st.uf[...] = np.pad(core, ((0, 0), (2, 2), (2, 2), (2, 2)), mode="wrap")
+    o = make_oracle3d(p)
+    rc, mom = o.moments(st)
+    assert rc == 0
+    ref = literal_moments3d(p, st.gp, st.np2)
+    np.testing.assert_allclose(mom, ref, rtol=0, atol=1e-13 * np.abs(ref).max())
+    for isp in range(p.nsp):
+        n = mom[0, 1:p.nx + 1, 1:p.ny + 1, 1:p.nz + 1, isp].sum()
+        np.testing.assert_allclose(n, st.np2[:, :, isp].sum(), rtol=1e-12)

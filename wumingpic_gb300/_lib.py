@@ -80,6 +80,12 @@ def lib():
             getattr(L, n).argtypes = [vp, vp]
         L.wpic_set_pusher.argtypes = [vp, i]
         L.wpic3d_set_pusher.argtypes = [vp, i]
+        for pre in ("wpic", "wpic3d"):
+            getattr(L, pre + "_mom_calc_accl").argtypes = [vp]
+            getattr(L, pre + "_mom_calc_nvt").argtypes = [vp, i]
+            getattr(L, pre + "_bc_mom").argtypes = [vp]
+            getattr(L, pre + "_get_mom").argtypes = [vp, vp]
+            getattr(L, pre + "_moments").argtypes = [vp, vp]
         for n in ("wpic_particle_solv", "wpic_particle_solv_vay", "wpic_field_fdtd_i", "wpic_ele_cur",
                   "wpic_bc_particle_x",
                   "wpic_bc_particle_y", "wpic_sort_bucket", "wpic_synchronize"):

@@ -58,6 +58,7 @@ struct wpic_ctx {
   std::vector<int> h_np2;
   double mix_vmax = 0.0;  // largest contribution of one particle to one node of the deposit
   int pusher = WPIC_PUSH_BORIS;  // the push of the fused step
+  double* mom = nullptr;         // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp), allocated on first use
 };
 
 namespace {
@@ -868,6 +869,67 @@ int wpic_energy(wpic_ctx* c, double* out) {
   out[nsp] = h[2] / (8 * c->d.ph.pi);
   out[nsp + 1] = h[3] / (8 * c->d.ph.pi);
   return WPIC_OK;
+}
+
+namespace {
+size_t mom_count(const wpic_ctx* c) { return 7 * (size_t)(c->d.g.nx + 2) * (c->d.g.ny + 2) * c->d.ph.nsp; }
+
+int ensure_mom(wpic_ctx* c) {
+  if (c->mom) return WPIC_OK;
+  return dalloc(c, &c->mom, mom_count(c));
+}
+
+int copy_mom(wpic_ctx* c, double* out) {
+  if (!out) return WPIC_OK;
+  CK(cudaMemcpyAsync(out, c->mom, mom_count(c) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return WPIC_OK;
+}
+}  // namespace
+
+int wpic_mom_calc_accl(wpic_ctx* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;
+  FP(mom_accl2d, c->d, c->stream);
+  return finish(c);
+}
+
+int wpic_mom_calc_nvt(wpic_ctx* c, int from_gp) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed || (from_gp != 0 && from_gp != 1)) return WPIC_BAD_ARGUMENT;
+  int st = ensure_mom(c);
+  if (st) return st;
+  FP(mom_nvt2d, c->d, from_gp ? c->d.B : c->d.A, c->mom, c->stream);
+  return finish(c);
+}
+
+int wpic_bc_mom(wpic_ctx* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!c->mom) return WPIC_BAD_ARGUMENT;
+  bc_mom2d(c->d, c->mom, c->stream);
+  return finish(c);
+}
+
+int wpic_get_mom(wpic_ctx* c, double* mom) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!c->mom || !mom) return WPIC_BAD_ARGUMENT;
+  int st = copy_mom(c, mom);
+  if (st) return st;
+  return finish(c);
+}
+
+int wpic_moments(wpic_ctx* c, double* mom) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  int st = ensure_mom(c);
+  if (st) return st;
+  if (c->mixed) {
+    mix_moments2d(c->d, c->mom, c->stream);
+  } else {
+    FP(mom_accl2d, c->d, c->stream);
+    FP(mom_nvt2d, c->d, c->d.B, c->mom, c->stream);
+    bc_mom2d(c->d, c->mom, c->stream);
+  }
+  if ((st = copy_mom(c, mom))) return st;
+  return finish(c);
 }
 
 int wpic_cg_control(wpic_ctx* c, const int* fixed3, int ite_max) {

@@ -24,6 +24,7 @@ struct wpic_ctx3d {
   double* staging = nullptr;
   size_t staging_bytes = 0;
   int pusher = WPIC_PUSH_BORIS;  // the push of the fused step
+  double* mom = nullptr;         // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nzs-1:nze+1, nsp), on first use
 };
 
 namespace {
@@ -437,6 +438,62 @@ int wpic3d_energy(wpic_ctx3d* c, double* out) {
   out[nsp] = h[2];
   out[nsp + 1] = h[3];
   return WPIC_OK;
+}
+
+namespace {
+size_t mom_count3(const wpic_ctx3d* c) {
+  return 7 * (size_t)(c->d.g.nx + 2) * (c->d.g.ny + 2) * (c->d.g.nz + 2) * c->d.ph.nsp;
+}
+int ensure_mom3(wpic_ctx3d* c) {
+  if (c->mom) return WPIC_OK;
+  return dalloc3(c, &c->mom, mom_count3(c));
+}
+int copy_mom3(wpic_ctx3d* c, double* out) {
+  if (!out) return WPIC_OK;
+  CK3(cudaMemcpyAsync(out, c->mom, mom_count3(c) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return WPIC_OK;
+}
+}  // namespace
+
+int wpic3d_mom_calc_accl(wpic_ctx3d* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  FP3(mom_accl3d, c->d, c->stream);
+  return finish3(c);
+}
+
+int wpic3d_mom_calc_nvt(wpic_ctx3d* c, int from_gp) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (from_gp != 0 && from_gp != 1) return WPIC_BAD_ARGUMENT;
+  int st = ensure_mom3(c);
+  if (st) return st;
+  FP3(mom_nvt3d, c->d, from_gp ? c->d.B : c->d.A, c->mom, c->stream);
+  return finish3(c);
+}
+
+int wpic3d_bc_mom(wpic_ctx3d* c) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!c->mom) return WPIC_BAD_ARGUMENT;
+  bc_mom3d(c->d, c->mom, c->stream);
+  return finish3(c);
+}
+
+int wpic3d_get_mom(wpic_ctx3d* c, double* mom) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!c->mom || !mom) return WPIC_BAD_ARGUMENT;
+  int st = copy_mom3(c, mom);
+  if (st) return st;
+  return finish3(c);
+}
+
+int wpic3d_moments(wpic_ctx3d* c, double* mom) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  int st = ensure_mom3(c);
+  if (st) return st;
+  FP3(mom_accl3d, c->d, c->stream);
+  FP3(mom_nvt3d, c->d, c->d.B, c->mom, c->stream);
+  bc_mom3d(c->d, c->mom, c->stream);
+  if ((st = copy_mom3(c, mom))) return st;
+  return finish3(c);
 }
 
 int wpic3d_cg_control(wpic_ctx3d* c, const int* fixed3, int ite_max) {

@@ -42,8 +42,12 @@ __device__ __forceinline__ double vay_update(double fac1, double fac2, double c,
   return 1.0 / gam;
 }
 
-template <bool VAY>
+// MODE: PUSH_BORIS = particle__solv, PUSH_VAY = particle__solv_vay, PUSH_MOM = mom_calc__accl
+// (2d/common/mom_calc.f90:48-161: the same gather and Boris rotation with the time step
+// halved by mom_calc__init (:36); positions copied, no move, IDs not written).
+template <int MODE>
 __global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
+  constexpr bool VAY = MODE == PUSH_VAY;
   const Grid2D g = d.g;
   const int c0 = blockIdx.x * PUSH_TW;
   const int jj = blockIdx.y, isp = blockIdx.z;
@@ -69,7 +73,7 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
   for (int idx = threadIdx.x; idx <= nc; idx += blockDim.x) scc[idx] = d.cc[(size_t)row * (g.nx + 1) + c0 + idx];
   __syncthreads();
 
-  const double dxi = d.ph.p_d_delx, delt = d.ph.delt, c = d.ph.c;
+  const double dxi = d.ph.p_d_delx, delt = MODE == PUSH_MOM ? d.ph.delt * 0.5 : d.ph.delt, c = d.ph.c;
   const double fac1 = d.ph.q[isp] / d.ph.r[isp] * 0.5 * delt;
   const double txxx = fac1 * fac1;
   const double fac2 = d.ph.q[isp] * delt / d.ph.r[isp];
@@ -128,6 +132,14 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
     const double g3 = uvm1 + fac1 * epx;
     const double g4 = uvm2 + fac1 * epy;
     const double g5 = uvm3 + fac1 * epz;
+    if (MODE == PUSH_MOM) {
+      d.B.x[k] = x;
+      d.B.y[k] = y;
+      d.B.ux[k] = g3;
+      d.B.uy[k] = g4;
+      d.B.uz[k] = g5;
+      continue;
+    }
     gam = 1.0 / sqrt(1.0 + (+g3 * g3 + g4 * g4 + g5 * g5) / (c * c));
     d.B.ux[k] = g3;
     d.B.uy[k] = g4;
@@ -140,12 +152,83 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
 
 void push2d(const Dev2D& d, cudaStream_t s) {
   dim3 grid((d.g.nx + PUSH_TW - 1) / PUSH_TW, d.g.ny, d.ph.nsp);
-  k_push2d<false><<<grid, PUSH_THREADS, 0, s>>>(d);
+  k_push2d<PUSH_BORIS><<<grid, PUSH_THREADS, 0, s>>>(d);
 }
 
 void push_vay2d(const Dev2D& d, cudaStream_t s) {
   dim3 grid((d.g.nx + PUSH_TW - 1) / PUSH_TW, d.g.ny, d.ph.nsp);
-  k_push2d<true><<<grid, PUSH_THREADS, 0, s>>>(d);
+  k_push2d<PUSH_VAY><<<grid, PUSH_THREADS, 0, s>>>(d);
+}
+
+void mom_accl2d(const Dev2D& d, cudaStream_t s) {
+  dim3 grid((d.g.nx + PUSH_TW - 1) / PUSH_TW, d.g.ny, d.ph.nsp);
+  k_push2d<PUSH_MOM><<<grid, PUSH_THREADS, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// mom_calc__nvt  (2d/common/mom_calc.f90:164-249)
+// One thread per node (I, J) of mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp).  A node takes
+// contributions only from particles of cells I-1..I+1 in rows J-1..J+1; the thread walks
+// those rows in ascending j and, within a row, the three cells' particles in storage
+// order, so every node is the single-thread reference's sum (0 + c1) + c2 + ... .  The
+// cells come from cumcnt, so the particles must be bucket-sorted (up after sort__bucket,
+// or gp after mom_calc__accl); a particle outside the 2x2 node stencil of its cell is
+// reported as out of range instead of being dropped.
+// ---------------------------------------------------------------------------
+constexpr int MOM_TX = 128;
+
+__global__ void __launch_bounds__(MOM_TX) k_mom_nvt2d(Dev2D d, Parts64 P, double* mom) {
+  const Grid2D g = d.g;
+  const int nxm = g.nx + 2;
+  const int in = blockIdx.x * MOM_TX + threadIdx.x, jn = blockIdx.y, isp = blockIdx.z;
+  if (in >= nxm) return;
+  const int I = g.nxgs - 1 + in, J = g.nygs - 1 + jn;
+  const double d_delx = d.ph.d_delx, c = d.ph.c;
+  double acc[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  bool bad = false;
+  for (int dj = -1; dj <= 1; ++dj) {
+    const int jj = jn - 1 + dj;  // particle row J + dj
+    if (jj < 0 || jj >= g.ny) continue;
+    const int row = isp * g.ny + jj;
+    const int* ccr = d.cc + (size_t)row * (g.nx + 1);
+    const int c_lo = max(in - 2, 0), c_hi = min(in, g.nx - 1);  // cells I-1..I+1
+    if (c_lo > c_hi) continue;
+    const int s0 = ccr[c_lo], s1 = ccr[c_hi + 1];
+    // the cell with the node's own index is checked by this thread (row J only)
+    const int own0 = (dj == 0 && in >= 1 && in <= g.nx) ? ccr[in - 1] : 0;
+    const int own1 = (dj == 0 && in >= 1 && in <= g.nx) ? ccr[in] : 0;
+    const size_t rbase = (size_t)row * d.cap;
+    for (int s = s0; s < s1; ++s) {
+      const size_t k = rbase + s;
+      const double x = P.x[k], y = P.y[k];
+      const int ih = (int)(x * d_delx - 0.5);
+      const int jh = (int)(y * d_delx - 0.5);
+      if (s >= own0 && s < own1 && (ih < I - 1 || ih > I || jh < J - 1 || jh > J)) bad = true;
+      const int a = I - ih, b = J - jh;
+      if (a < 0 || a > 1 || b < 0 || b > 1) continue;
+      const double dx = x * d_delx - 0.5 - ih, dxm = 1. - dx;
+      const double dy = y * d_delx - 0.5 - jh, dym = 1. - dy;
+      const double wx = a ? dx : dxm, wy = b ? dy : dym;
+      const double u1 = P.ux[k], u2 = P.uy[k], u3 = P.uz[k];
+      const double gam = 1. / sqrt(1.0 + (+u1 * u1 + u2 * u2 + u3 * u3) / (c * c));
+      acc[0] = acc[0] + wx * wy;
+      acc[1] = acc[1] + u1 * gam * wx * wy;
+      acc[2] = acc[2] + u2 * gam * wx * wy;
+      acc[3] = acc[3] + u3 * gam * wx * wy;
+      acc[4] = acc[4] + u1 * u1 * gam * wx * wy;
+      acc[5] = acc[5] + u2 * u2 * gam * wx * wy;
+      acc[6] = acc[6] + u3 * u3 * gam * wx * wy;
+    }
+  }
+  if (bad) atomicOr(d.err, EB_OUT_OF_RANGE);
+  double* o = mom + 7 * ((size_t)in + (size_t)nxm * ((size_t)jn + (size_t)(g.ny + 2) * isp));
+#pragma unroll
+  for (int l = 0; l < 7; ++l) o[l] = acc[l];
+}
+
+void mom_nvt2d(const Dev2D& d, const Parts64& P, double* mom, cudaStream_t s) {
+  dim3 grid((d.g.nx + 2 + MOM_TX - 1) / MOM_TX, d.g.ny + 2, d.ph.nsp);
+  k_mom_nvt2d<<<grid, MOM_TX, 0, s>>>(d, P, mom);
 }
 
 // ---------------------------------------------------------------------------

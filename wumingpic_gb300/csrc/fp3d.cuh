@@ -15,8 +15,11 @@ __device__ __forceinline__ size_t f3(const Grid3D& g, int fi, int fj, int fk) { 
 // shared memory (particle.f90:75-92); each particle then gathers 27 points per
 // component in the reference's nesting order.
 // ---------------------------------------------------------------------------
-template <bool VAY>
+// MODE PUSH_MOM is mom_calc__accl (3d/common/mom_calc.f90:49-216): the same gather and
+// rotation at half the time step (mom_calc__init, :36), positions copied, no move.
+template <int MODE>
 __global__ void __launch_bounds__(PUSH_THREADS) k_push3d(Dev3D d) {
+  constexpr bool VAY = MODE == PUSH_VAY;
   const Grid3D g = d.g;
   // blockIdx.x = x tile + tiles per row * (row of the species), blockIdx.y = species
   const int ntx = (g.nx + PUSH_TW - 1) / PUSH_TW;
@@ -46,7 +49,7 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push3d(Dev3D d) {
   for (int idx = threadIdx.x; idx <= nc; idx += blockDim.x) scc[idx] = d.cc[(size_t)row * (g.nx + 1) + c0 + idx];
   __syncthreads();
 
-  const double dxi = d.ph.p_d_delx, delt = d.ph.delt, c = d.ph.c;
+  const double dxi = d.ph.p_d_delx, delt = MODE == PUSH_MOM ? d.ph.delt * 5e-1 : d.ph.delt, c = d.ph.c;
   const double fac1 = d.ph.q[isp] / d.ph.r[isp] * 5e-1 * delt;
   const double txxx = fac1 * fac1;
   const double fac2 = d.ph.q[isp] * delt / d.ph.r[isp];
@@ -110,6 +113,15 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push3d(Dev3D d) {
     const double g4 = uvm1 + fac1 * epx;
     const double g5 = uvm2 + fac1 * epy;
     const double g6 = uvm3 + fac1 * epz;
+    if (MODE == PUSH_MOM) {
+      d.B.x[k] = x;
+      d.B.y[k] = y;
+      d.B.z[k] = z;
+      d.B.ux[k] = g4;
+      d.B.uy[k] = g5;
+      d.B.uz[k] = g6;
+      continue;
+    }
     gam = 1e0 / sqrt(1e0 + (+g4 * g4 + g5 * g5 + g6 * g6) / (c * c));
     d.B.ux[k] = g4;
     d.B.uy[k] = g5;
@@ -123,12 +135,92 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push3d(Dev3D d) {
 
 void push3d(const Dev3D& d, cudaStream_t s) {
   dim3 grid(((d.g.nx + PUSH_TW - 1) / PUSH_TW) * d.g.ny * d.g.nz, d.ph.nsp);
-  k_push3d<false><<<grid, PUSH_THREADS, 0, s>>>(d);
+  k_push3d<PUSH_BORIS><<<grid, PUSH_THREADS, 0, s>>>(d);
 }
 
 void push_vay3d(const Dev3D& d, cudaStream_t s) {
   dim3 grid(((d.g.nx + PUSH_TW - 1) / PUSH_TW) * d.g.ny * d.g.nz, d.ph.nsp);
-  k_push3d<true><<<grid, PUSH_THREADS, 0, s>>>(d);
+  k_push3d<PUSH_VAY><<<grid, PUSH_THREADS, 0, s>>>(d);
+}
+
+void mom_accl3d(const Dev3D& d, cudaStream_t s) {
+  dim3 grid(((d.g.nx + PUSH_TW - 1) / PUSH_TW) * d.g.ny * d.g.nz, d.ph.nsp);
+  k_push3d<PUSH_MOM><<<grid, PUSH_THREADS, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// mom_calc__nvt  (3d/common/mom_calc.f90:219-332)
+// One thread per node (I, J, K) of mom(7, nxgs-1:nxge+1, nys-1:nye+1, nzs-1:nze+1, nsp);
+// it walks the particle rows (j, k) of K-1..K+1 and J-1..J+1 in the reference's loop
+// order (k outer) and, within a row, cells I-1..I+1 in storage order, so each node is the
+// single-thread reference's sum.  Node index floor(x/dx - 0.5) and offset x - 0.5 - ih as
+// the 3D reference writes them; bucket-sorted particles required, as in 2D.
+// ---------------------------------------------------------------------------
+constexpr int MOM3_TX = 128;
+
+__global__ void __launch_bounds__(MOM3_TX) k_mom_nvt3d(Dev3D d, Parts3D P, double* mom) {
+  const Grid3D g = d.g;
+  const int nxm = g.nx + 2, nym = g.ny + 2, nzm = g.nz + 2;
+  const int nbx = (nxm + MOM3_TX - 1) / MOM3_TX;
+  const int in = (blockIdx.x % nbx) * MOM3_TX + threadIdx.x, jn = blockIdx.x / nbx;
+  const int kn = blockIdx.y, isp = blockIdx.z;
+  if (in >= nxm) return;
+  const int I = g.nxgs - 1 + in, J = g.nygs - 1 + jn, K = g.nzgs - 1 + kn;
+  const double d_delx = d.ph.d_delx, c = d.ph.c;
+  double acc[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  bool bad = false;
+  const int c_lo = max(in - 2, 0), c_hi = min(in, g.nx - 1);  // cells I-1..I+1
+  if (c_lo <= c_hi) {
+    for (int dk = -1; dk <= 1; ++dk) {
+      const int kk = kn - 1 + dk;
+      if (kk < 0 || kk >= g.nz) continue;
+      for (int dj = -1; dj <= 1; ++dj) {
+        const int jj = jn - 1 + dj;
+        if (jj < 0 || jj >= g.ny) continue;
+        const int row = (isp * g.nz + kk) * g.ny + jj;
+        const int* ccr = d.cc + (size_t)row * (g.nx + 1);
+        const int s0 = ccr[c_lo], s1 = ccr[c_hi + 1];
+        const bool own_row = dj == 0 && dk == 0 && in >= 1 && in <= g.nx;
+        const int own0 = own_row ? ccr[in - 1] : 0, own1 = own_row ? ccr[in] : 0;
+        const size_t rbase = (size_t)row * d.cap;
+        for (int s = s0; s < s1; ++s) {
+          const size_t k = rbase + s;
+          const double x = P.x[k], y = P.y[k], z = P.z[k];
+          const int ih = (int)floor(x * d_delx - 5e-1);
+          const int jh = (int)floor(y * d_delx - 5e-1);
+          const int kh = (int)floor(z * d_delx - 5e-1);
+          if (s >= own0 && s < own1 &&
+              (ih < I - 1 || ih > I || jh < J - 1 || jh > J || kh < K - 1 || kh > K))
+            bad = true;
+          const int a = I - ih, b = J - jh, e = K - kh;
+          if (a < 0 || a > 1 || b < 0 || b > 1 || e < 0 || e > 1) continue;
+          const double dx = x - 5e-1 - ih, dxm = 1e0 - dx;
+          const double dy = y - 5e-1 - jh, dym = 1e0 - dy;
+          const double dz = z - 5e-1 - kh, dzm = 1e0 - dz;
+          const double wx = a ? dx : dxm, wy = b ? dy : dym, wz = e ? dz : dzm;
+          const double u1 = P.ux[k], u2 = P.uy[k], u3 = P.uz[k];
+          const double gam = 1e0 / sqrt(1e0 + (+u1 * u1 + u2 * u2 + u3 * u3) / (c * c));
+          acc[0] = acc[0] + wx * wy * wz;
+          acc[1] = acc[1] + u1 * gam * wx * wy * wz;
+          acc[2] = acc[2] + u2 * gam * wx * wy * wz;
+          acc[3] = acc[3] + u3 * gam * wx * wy * wz;
+          acc[4] = acc[4] + u1 * u1 * gam * wx * wy * wz;
+          acc[5] = acc[5] + u2 * u2 * gam * wx * wy * wz;
+          acc[6] = acc[6] + u3 * u3 * gam * wx * wy * wz;
+        }
+      }
+    }
+  }
+  if (bad) atomicOr(d.err, EB_OUT_OF_RANGE);
+  double* o = mom + 7 * ((size_t)in + (size_t)nxm * ((size_t)jn + (size_t)nym * ((size_t)kn + (size_t)nzm * isp)));
+#pragma unroll
+  for (int l = 0; l < 7; ++l) o[l] = acc[l];
+}
+
+void mom_nvt3d(const Dev3D& d, const Parts3D& P, double* mom, cudaStream_t s) {
+  const int nbx = (d.g.nx + 2 + MOM3_TX - 1) / MOM3_TX;
+  dim3 grid(nbx * (d.g.ny + 2), d.g.nz + 2, d.ph.nsp);
+  k_mom_nvt3d<<<grid, MOM3_TX, 0, s>>>(d, P, mom);
 }
 
 // ---------------------------------------------------------------------------

@@ -572,4 +572,52 @@ void load_weibel3d_ppc(const Dev3D& d, int ppc, unsigned long long seed, double 
   k_load_weibel3d<<<d.g.ny * d.g.nz, 256, 0, s>>>(d, ppc, seed, drift, drift_axis, u_thi, u_the);
 }
 
+// ---------------------------------------------------------------------------
+// boundary_periodic__mom  (3d/common/boundary_periodic.f90:1102-1235), one rank:
+// x images over every (j, k); the y self-exchange over every z layer; the z
+// self-exchange over the interior y rows.  Three launches, in that order.
+// ---------------------------------------------------------------------------
+__global__ void k_mom3_fold_x(Dev3D d, double* mom) {
+  const Grid3D g = d.g;
+  const long long nxm = g.nx + 2;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (l, jn, kn, isp)
+  if (t >= 7LL * (g.ny + 2) * (g.nz + 2) * d.ph.nsp) return;
+  const int l = (int)(t % 7);
+  double* m = mom + (t / 7) * nxm * 7 + l;
+  m[7] = m[7] + m[7 * (size_t)(g.nx + 1)];
+  m[7 * (size_t)g.nx] = m[7 * (size_t)g.nx] + m[0];
+}
+
+__global__ void k_mom3_fold_y(Dev3D d, double* mom) {
+  const Grid3D g = d.g;
+  const size_t rowst = 7 * (size_t)(g.nx + 2);               // stride of jn
+  const size_t plane = rowst * (size_t)(g.ny + 2);           // stride of kn
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;       // (l, in)
+  if (t >= (int)rowst) return;
+  const int kn = blockIdx.y, isp = blockIdx.z;
+  double* m = mom + ((size_t)isp * (g.nz + 2) + kn) * plane + t;
+  m[rowst * g.ny] = m[rowst * g.ny] + m[0];
+  m[rowst] = m[rowst] + m[rowst * (g.ny + 1)];
+}
+
+__global__ void k_mom3_fold_z(Dev3D d, double* mom) {
+  const Grid3D g = d.g;
+  const size_t rowst = 7 * (size_t)(g.nx + 2);
+  const size_t plane = rowst * (size_t)(g.ny + 2);
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (l, in)
+  if (t >= (int)rowst) return;
+  const int jn = 1 + blockIdx.y, isp = blockIdx.z;      // interior rows nys..nye
+  double* m = mom + (size_t)isp * (g.nz + 2) * plane + jn * rowst + t;
+  m[plane * g.nz] = m[plane * g.nz] + m[0];
+  m[plane] = m[plane] + m[plane * (g.nz + 1)];
+}
+
+void bc_mom3d(const Dev3D& d, double* mom, cudaStream_t s) {
+  const long long nxt = 7LL * (d.g.ny + 2) * (d.g.nz + 2) * d.ph.nsp;
+  const int rowst = 7 * (d.g.nx + 2);
+  k_mom3_fold_x<<<(unsigned)((nxt + 255) / 256), 256, 0, s>>>(d, mom);
+  k_mom3_fold_y<<<dim3((rowst + 255) / 256, d.g.nz + 2, d.ph.nsp), 256, 0, s>>>(d, mom);
+  k_mom3_fold_z<<<dim3((rowst + 255) / 256, d.g.ny, d.ph.nsp), 256, 0, s>>>(d, mom);
+}
+
 }  // namespace wpic

@@ -57,6 +57,47 @@ void curre_fold2d(const Dev2D& d, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
+// boundary_periodic__mom (2d/common/boundary_periodic.f90:571-636, one rank: the y
+// exchanges are self-exchanges) and boundary_reconnection__mom
+// (2d/proj/reconnection/boundary_reconnection.f90:582-647, x ghosts folded onto the wall
+// columns).  mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp); the x fold first over every row,
+// then the y fold over every column, each thread doing its two statements in order.
+// ---------------------------------------------------------------------------
+__global__ void k_mom_fold_x(Dev2D d, double* mom) {
+  const Grid2D g = d.g;
+  const int nxm = g.nx + 2, nym = g.ny + 2;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (l, jn, isp)
+  if (t >= 7 * nym * d.ph.nsp) return;
+  const int l = t % 7, r = t / 7;  // r = jn + nym * isp
+  double* m = mom + (size_t)r * nxm * 7 + l;
+  if (d.ph.bc == BC_RECONNECTION) {
+    m[7 * 1] = m[7 * 1] + m[0];
+    m[7 * (size_t)g.nx] = m[7 * (size_t)g.nx] + m[7 * (size_t)(g.nx + 1)];
+  } else {
+    m[7 * 1] = m[7 * 1] + m[7 * (size_t)(g.nx + 1)];
+    m[7 * (size_t)g.nx] = m[7 * (size_t)g.nx] + m[0];
+  }
+}
+
+__global__ void k_mom_fold_y(Dev2D d, double* mom) {
+  const Grid2D g = d.g;
+  const int nxm = g.nx + 2, nym = g.ny + 2;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (l, in) of one species
+  const int isp = blockIdx.y;
+  if (t >= 7 * nxm) return;
+  const size_t col = 7 * (size_t)nxm;  // stride of one node row
+  double* m = mom + (size_t)isp * nym * col + t;
+  m[col * g.ny] = m[col * g.ny] + m[0];
+  m[col] = m[col] + m[col * (g.ny + 1)];
+}
+
+void bc_mom2d(const Dev2D& d, double* mom, cudaStream_t s) {
+  const int nx_threads = 7 * (d.g.ny + 2) * d.ph.nsp;
+  k_mom_fold_x<<<(nx_threads + 255) / 256, 256, 0, s>>>(d, mom);
+  k_mom_fold_y<<<dim3((7 * (d.g.nx + 2) + 255) / 256, d.ph.nsp), 256, 0, s>>>(d, mom);
+}
+
+// ---------------------------------------------------------------------------
 // boundary_*__dfield (2d/common/boundary_periodic.f90:251-354;
 // 2d/proj/reconnection/boundary_reconnection.f90:254-361): two-deep ghosts of df.
 // ---------------------------------------------------------------------------

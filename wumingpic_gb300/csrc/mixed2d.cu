@@ -925,6 +925,136 @@ void mix_energy2d(const Dev2D& d, cudaStream_t s) {
   fast::energy_fields_fin2d(d, s);
 }
 
+// ---------------------------------------------------------------------------
+// mom_calc__accl + mom_calc__nvt (2d/common/mom_calc.f90:48-249) on the column layout:
+// one CTA per (tile, species), thread c walks the column of cell c.  The half-step Boris
+// push of mom_calc__accl (time step halved by mom_calc__init, :36) runs in FP32 on the
+// cell-centred fields; the seven moments of the particle go into the thread's registers
+// over the 3 x 3 nodes its cell can reach (node ih = floor(x/dx - 0.5) is cell i - 1 or i),
+// then into the tile's 18 x 18 node patch (FP32 shared atomics) and once per node into the
+// FP64 global moments.  The state is not modified (the reference writes gp, which the next
+// step overwrites).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(MIX_TC) k_mix_mom(Dev2D d, double* mom) {
+  __shared__ __align__(16) float4 sfa[TT * TT];  // (Bx, By, Bz, Ex) at cell centres, local cells -1..16
+  __shared__ __align__(8) float2 sfb[TT * TT];   // (Ey, Ez)
+  __shared__ float macc[7][TT][TT];              // node patch: local node xl = node index - 16 tx
+  const Mix2D& m = d.m;
+  const Grid2D g = d.g;
+  const int tile = blockIdx.x, isp = blockIdx.y;
+  const int tx = tile % m.ntx, ty = tile / m.ntx;
+  const int c = threadIdx.x;
+  for (int k = c; k < TT * TT; k += MIX_TC) {
+    const int r = k / TT, cc = k % TT;  // local cell (cc - 1, r - 1), field index + 2
+    const int fi = tx * MIX_TS + cc + 1, fj = ty * MIX_TS + r + 1;
+    const double* U = d.uf + (size_t)fj * g.fp + fi;
+#define UF(comp, di, dj) U[(size_t)(comp) * g.fplane + (size_t)(dj) * g.fp + (di)]
+    sfa[k] = make_float4((float)(0.5 * (UF(0, 0, 0) + UF(0, 0, 1))), (float)(0.5 * (UF(1, 0, 0) + UF(1, 1, 0))),
+                         (float)(0.25 * (UF(2, 0, 0) + UF(2, 1, 0) + UF(2, 0, 1) + UF(2, 1, 1))),
+                         (float)(0.5 * (UF(3, 0, 0) + UF(3, 1, 0))));
+    sfb[k] = make_float2((float)(0.5 * (UF(4, 0, 0) + UF(4, 0, 1))), (float)UF(5, 0, 0));
+#undef UF
+  }
+  for (int k = c; k < 7 * TT * TT; k += MIX_TC) (&macc[0][0][0])[k] = 0.f;
+  __syncthreads();
+
+  const int bin = tile * d.ph.nsp + isp;
+  const int n = m.cnt[bin * MIX_TC + c];
+  const float* col = mix_slot(m, bin, 0, c);
+  const double hdt = d.ph.delt * 0.5;
+  const float fac1 = (float)(d.ph.q[isp] / d.ph.r[isp] * 0.5 * hdt);
+  const float fac2 = (float)(d.ph.q[isp] * hdt / d.ph.r[isp]);
+  const float txxx = fac1 * fac1;
+  const float cl = m.k_c, ic2 = m.k_ic2;
+  const int lx = c & (MIX_TS - 1), ly = c >> 4;
+  const int f0 = ly * TT + lx;
+  float acc[7][3][3];
+#pragma unroll
+  for (int l = 0; l < 7; ++l)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) acc[l][b][a] = 0.f;
+  for (int k = 0; k < n; ++k) {
+    const float* o = col + (size_t)k * MIX_PL;
+    const float ox = o[MIX_OX], oy = o[MIX_OY];
+    const float ux0 = o[MIX_UX], uy0 = o[MIX_UY], uz0 = o[MIX_UZ];
+    const float sx0 = 0.5f * (1.f - ox) * (1.f - ox), sx1 = 0.75f - (ox - 0.5f) * (ox - 0.5f), sx2 = 0.5f * ox * ox;
+    const float sy0 = 0.5f * (1.f - oy) * (1.f - oy), sy1 = 0.75f - (oy - 0.5f) * (oy - 0.5f), sy2 = 0.5f * oy * oy;
+    float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int jy = 0; jy < 3; ++jy) {
+      const float wy = jy == 0 ? sy0 : (jy == 1 ? sy1 : sy2);
+#pragma unroll
+      for (int jx = 0; jx < 3; ++jx) {
+        const float w = wy * (jx == 0 ? sx0 : (jx == 1 ? sx1 : sx2));
+        const float4 a = sfa[f0 + jy * TT + jx];
+        const float2 b = sfb[f0 + jy * TT + jx];
+        f[0] = fmaf(w, a.x, f[0]);
+        f[1] = fmaf(w, a.y, f[1]);
+        f[2] = fmaf(w, a.z, f[2]);
+        f[3] = fmaf(w, a.w, f[3]);
+        f[4] = fmaf(w, b.x, f[4]);
+        f[5] = fmaf(w, b.y, f[5]);
+      }
+    }
+    const float bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
+    float u1 = ux0 + fac1 * epx, u2 = uy0 + fac1 * epy, u3 = uz0 + fac1 * epz;
+    const float g2 = cl * cl + u1 * u1 + u2 * u2 + u3 * u3;
+    const float igam = rsqrtf(g2);
+    const float gm = g2 * igam;
+    const float fac1r = fac1 * igam;
+    const float fac2r = __fdividef(fac2, gm + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
+    const float u4 = u1 + fac1r * (u2 * bpz - u3 * bpy);
+    const float u5 = u2 + fac1r * (u3 * bpx - u1 * bpz);
+    const float u6 = u3 + fac1r * (u1 * bpy - u2 * bpx);
+    u1 = u1 + fac2r * (u5 * bpz - u6 * bpy);
+    u2 = u2 + fac2r * (u6 * bpx - u4 * bpz);
+    u3 = u3 + fac2r * (u4 * bpy - u5 * bpx);
+    const float ux = u1 + fac1 * epx, uy = u2 + fac1 * epy, uz = u3 + fac1 * epz;
+    const float gam = rsqrtf(1.f + (ux * ux + uy * uy + uz * uz) * ic2);
+    // linear weights over nodes i-1, i, i+1 (and j-1, j, j+1)
+    const float hx = ox - 0.5f, hy = oy - 0.5f;
+    const float wx[3] = {hx < 0.f ? -hx : 0.f, hx < 0.f ? hx + 1.f : 1.f - hx, hx < 0.f ? 0.f : hx};
+    const float wy[3] = {hy < 0.f ? -hy : 0.f, hy < 0.f ? hy + 1.f : 1.f - hy, hy < 0.f ? 0.f : hy};
+    const float pre[7] = {1.f, ux * gam, uy * gam, uz * gam, ux * ux * gam, uy * uy * gam, uz * uz * gam};
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float w = wx[a] * wy[b];
+#pragma unroll
+        for (int l = 0; l < 7; ++l) acc[l][b][a] = fmaf(pre[l], w, acc[l][b][a]);
+      }
+  }
+  if (n > 0) {
+#pragma unroll
+    for (int l = 0; l < 7; ++l)
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) atomicAdd(&macc[l][ly + b][lx + a], acc[l][b][a]);
+  }
+  __syncthreads();
+  const int nxm = g.nx + 2, nym = g.ny + 2;
+  for (int k = c; k < TT * TT; k += MIX_TC) {
+    const int yl = k / TT, xl = k % TT;
+    const size_t in = (size_t)tx * MIX_TS + xl, jn = (size_t)ty * MIX_TS + yl;
+    double* out = mom + 7 * (in + (size_t)nxm * (jn + (size_t)nym * isp));
+#pragma unroll
+    for (int l = 0; l < 7; ++l) {
+      const float v = macc[l][yl][xl];
+      if (v != 0.f) atomicAdd(out + l, (double)v);
+    }
+  }
+}
+
+void mix_moments2d(const Dev2D& d, double* mom, cudaStream_t s) {
+  cudaMemsetAsync(mom, 0, sizeof(double) * 7 * (size_t)(d.g.nx + 2) * (d.g.ny + 2) * d.ph.nsp, s);
+  k_mix_mom<<<dim3(d.m.ntile, d.ph.nsp), MIX_TC, 0, s>>>(d, mom);
+  bc_mom2d(d, mom, s);
+}
+
 int mix_setup2d(const Dev2D& d, void* out) {
   typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,

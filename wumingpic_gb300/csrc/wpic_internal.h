@@ -36,6 +36,9 @@ enum ErrBit : int {
 
 enum Bc : int { BC_PERIODIC = 0, BC_RECONNECTION = 1 };
 
+// modes of the particle push kernels: particle__solv, particle__solv_vay, mom_calc__accl
+enum PushMode : int { PUSH_BORIS = 0, PUSH_VAY = 1, PUSH_MOM = 2 };
+
 struct Grid2D {
   int nx, ny;       // interior cells
   int nxgs, nygs;   // reference index of the first interior cell (nxgs, nys)
@@ -139,6 +142,8 @@ struct Dev2D {
 #define WPIC_DECLARE_FP_LAUNCHERS                                                          \
   void push2d(const Dev2D& d, cudaStream_t s);                                             \
   void push_vay2d(const Dev2D& d, cudaStream_t s);                                         \
+  void mom_accl2d(const Dev2D& d, cudaStream_t s);                                         \
+  void mom_nvt2d(const Dev2D& d, const Parts64& P, double* mom, cudaStream_t s);           \
   void deposit2d(const Dev2D& d, cudaStream_t s);                                          \
   void gkl2d(const Dev2D& d, cudaStream_t s);                                              \
   void cg_init2d(const Dev2D& d, cudaStream_t s);                                          \
@@ -155,6 +160,8 @@ namespace fast { WPIC_DECLARE_FP_LAUNCHERS }
 
 // ---- precision-independent kernels (integer work, copies, exact adds) ----
 void curre_fold2d(const Dev2D& d, cudaStream_t s);
+void bc_mom2d(const Dev2D& d, double* mom, cudaStream_t s);
+void mix_moments2d(const Dev2D& d, double* mom, cudaStream_t s);
 void dfield_ghost2d(const Dev2D& d, cudaStream_t s);
 void uf_add2d(const Dev2D& d, cudaStream_t s);
 void particle_x2d(const Dev2D& d, const Parts64& P, cudaStream_t s);
@@ -232,6 +239,8 @@ struct Dev3D {
 #define WPIC_DECLARE_FP3_LAUNCHERS                       \
   void push3d(const Dev3D& d, cudaStream_t s);           \
   void push_vay3d(const Dev3D& d, cudaStream_t s);       \
+  void mom_accl3d(const Dev3D& d, cudaStream_t s);       \
+  void mom_nvt3d(const Dev3D& d, const Parts3D& P, double* mom, cudaStream_t s); \
   void deposit3d(const Dev3D& d, cudaStream_t s);        \
   void gkl3d(const Dev3D& d, cudaStream_t s);            \
   void cg_init3d(const Dev3D& d, cudaStream_t s);        \
@@ -246,6 +255,7 @@ namespace exact { WPIC_DECLARE_FP3_LAUNCHERS }
 namespace fast { WPIC_DECLARE_FP3_LAUNCHERS }
 
 void curre_fold3d(const Dev3D& d, cudaStream_t s);
+void bc_mom3d(const Dev3D& d, double* mom, cudaStream_t s);
 void dfield_ghost3d(const Dev3D& d, cudaStream_t s);
 void uf_add3d(const Dev3D& d, cudaStream_t s);
 void particle_x3d(const Dev3D& d, const Parts3D& P, cudaStream_t s);

@@ -133,6 +133,34 @@ class Pic2D:
     def step(self, nsteps=1):
         check(lib().wpic_step(self._h, int(nsteps)), "step")
 
+    # ---- moments (mom_calc__accl, mom_calc__nvt, bc__mom) ----
+    def mom_shape(self):
+        """mom(7, nxgs-1:nxge+1, nys-1:nye+1[, nzs-1:nze+1], nsp)"""
+        return (7, self.p.nx + 2, self.p.ny + 2, self.p.nsp)
+
+    def mom_calc__accl(self):
+        check(lib().wpic_mom_calc_accl(self._h), "mom_calc__accl")
+
+    def mom_calc__nvt(self, from_gp=True):
+        check(lib().wpic_mom_calc_nvt(self._h, 1 if from_gp else 0), "mom_calc__nvt")
+
+    def bc__mom(self):
+        check(lib().wpic_bc_mom(self._h), "bc__mom")
+
+    def get_mom(self):
+        out = np.zeros(self.mom_shape(), order="F")
+        check(lib().wpic_get_mom(self._h, _ptr(out, np.float64)), "get_mom")
+        return out
+
+    def moments(self, to_host=True):
+        """accl + nvt + bc__mom; returns the host copy (or None with to_host=False)"""
+        if not to_host:
+            check(lib().wpic_moments(self._h, None), "moments")
+            return None
+        out = np.zeros(self.mom_shape(), order="F")
+        check(lib().wpic_moments(self._h, _ptr(out, np.float64)), "moments")
+        return out
+
     def energy(self):
         out = np.zeros(self.p.nsp + 2)
         check(lib().wpic_energy(self._h, _ptr(out, np.float64)), "energy")
