@@ -199,6 +199,25 @@ def time_path(p, precision, steps, warmup, rank, torch, dist, local):
     return g, npart, ms, stages, clocks
 
 
+def time_moments(g, torch, reps=3):
+    """mom_calc__accl + mom_calc__nvt + bc__mom on the device (wpic_moments with no host copy),
+    averaged over `reps` calls after one warm-up call, and one call with the copy to the host."""
+    stream = torch.cuda.current_stream()
+    g.moments(to_host=False)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        g.moments(to_host=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mom = g.moments(to_host=True)
+    host_ms = (time.perf_counter() - t0) * 1e3
+    return {"device_ms": e0.elapsed_time(e1) / reps, "with_host_copy_ms": host_ms,
+            "mom_bytes": int(mom.nbytes), "reps": reps}
+
+
 def time_path3d(steps, rank, torch, dist, world):
     """The 3D FP64 path on the 3D Weibel workload (256^3 cells, 16 ppc/species, m_i/m_e = 16,
     beams +-0.5c along x, u_th 0.05c), state resident in HBM, one warm-up step."""
@@ -226,11 +245,12 @@ def time_path3d(steps, rank, torch, dist, world):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     cg = [int(x) for x in g.cg_iters()]
+    moments = time_moments(g, torch, reps=2)
     g.close()
     return {"workload": f"3D Weibel 256^3 cells, 16 ppc/species, {npart} particles, drift +-0.5c along x, "
                         f"u_th 0.05c, m_i/m_e 16, c*dt/dx=0.5",
             "value": npart * world * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
-            "steps": steps, "warmup": 1, "dtype": "f64", "cg_iterations": cg}
+            "steps": steps, "warmup": 1, "dtype": "f64", "cg_iterations": cg, "moments": moments}
 
 
 def main():
@@ -276,6 +296,7 @@ def main():
                 "traffic": None, "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "bytes_per_particle": BYTES_MIX_PUSH, "launch_ms": per_launch}
     launches = int(sum(v[1] for v in stages.values()))
+    moments = time_moments(g, torch)
     e2e = None if args.no_e2e else measure_e2e(g, p)
     g.close()
 
@@ -302,6 +323,7 @@ def main():
         for k in fp64["kernels"].values():
             k["hbm_frac"] = k["hbm_gbs"] / hbm_peak
             k["fp64_pipe_frac"] = k["fp64_gflops"] / peak64
+        fp64["moments"] = time_moments(g64, torch)
         g64.close()
 
     # ---- 3D FP64 path: 256^3 cells, 16 ppc/species (the 3D Weibel configuration) ----
@@ -323,7 +345,7 @@ def main():
                 "path": "mixed: integer cell + FP32 offset, FP32 push/gather/deposition, FP64 fields and CG",
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks, "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()},
-                "fp64_path": fp64, "fp64_3d_path": fp64_3d}
+                "moments": moments, "fp64_path": fp64, "fp64_3d_path": fp64_3d}
         print(json.dumps(line), flush=True)
         if args.stages:
             for k, (t, n) in stages.items():

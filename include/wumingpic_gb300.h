@@ -227,6 +227,8 @@ int wpic3d_put_particles(wpic_ctx3d* ctx, int which, const double* up, const int
 int wpic3d_get_particles(wpic_ctx3d* ctx, int which, double* up, int* np2, int* cumcnt);
 int wpic3d_put_fields(wpic_ctx3d* ctx, const double* uf);
 int wpic3d_get_fields(wpic_ctx3d* ctx, double* uf);
+/* the CG warm start of field__fdtd_i (SAVEd df), for a restart that continues bit for bit */
+int wpic3d_put_df(wpic_ctx3d* ctx, const double* df);
 int wpic3d_get_df(wpic_ctx3d* ctx, double* df);   /* the SAVEd dB/dE of field__fdtd_i */
 int wpic3d_get_uj(wpic_ctx3d* ctx, double* uj);   /* the current of the last field__fdtd_i */
 /* particle__solv(gp, up, uf, cumcnt, nxs, nxe)       3d/common/particle.f90:52 */

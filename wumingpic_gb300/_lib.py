@@ -112,7 +112,7 @@ def lib():
         L.wpic3d_finalize.argtypes = [vp]
         L.wpic3d_put_particles.argtypes = [vp, i, vp, vp, vp]
         L.wpic3d_get_particles.argtypes = [vp, i, vp, vp, vp]
-        for n in ("wpic3d_put_fields", "wpic3d_get_fields", "wpic3d_get_df", "wpic3d_get_uj"):
+        for n in ("wpic3d_put_fields", "wpic3d_get_fields", "wpic3d_put_df", "wpic3d_get_df", "wpic3d_get_uj"):
             getattr(L, n).argtypes = [vp, vp]
         for n in ("wpic3d_particle_solv", "wpic3d_particle_solv_vay", "wpic3d_field_fdtd_i", "wpic3d_ele_cur",
                   "wpic3d_bc_particle_x",

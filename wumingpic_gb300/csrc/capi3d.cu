@@ -342,6 +342,7 @@ int wpic3d_get_particles(wpic_ctx3d* c, int which, double* up, int* np2, int* cu
 
 int wpic3d_put_fields(wpic_ctx3d* c, const double* uf) { return c ? put_field3(c, uf, c->d.uf, 6) : WPIC_NOT_INITIALISED; }
 int wpic3d_get_fields(wpic_ctx3d* c, double* uf) { return c ? get_field3(c, uf, c->d.uf, 6) : WPIC_NOT_INITIALISED; }
+int wpic3d_put_df(wpic_ctx3d* c, const double* df) { return c ? put_field3(c, df, c->d.df, 6) : WPIC_NOT_INITIALISED; }
 int wpic3d_get_df(wpic_ctx3d* c, double* df) { return c ? get_field3(c, df, c->d.df, 6) : WPIC_NOT_INITIALISED; }
 int wpic3d_get_uj(wpic_ctx3d* c, double* uj) { return c ? get_field3(c, uj, c->d.uj, 3) : WPIC_NOT_INITIALISED; }
 

@@ -1,5 +1,5 @@
 ! wpic_shim2d.f90 -- drop-in replacements for WumingPIC's 2D hot-path modules
-! (particle, field, sort, boundary_periodic) that forward to the GB300 library
+! (particle, field, sort, boundary_periodic, mom_calc) that forward to the GB300 library
 ! through ISO_C_BINDING.  Link these objects instead of the corresponding objects
 ! of libwuming2d_common.a; the drivers ({2d}/proj/*/app.f90) stay unchanged.
 !
@@ -55,6 +55,24 @@ module wpic_capi
        type(c_ptr), value :: ctx
        real(c_double), intent(inout) :: uf(*)
      end function wpic_get_fields
+     integer(c_int) function wpic_mom_calc_nvt(ctx, from_gp) bind(C, name="wpic_mom_calc_nvt")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: from_gp
+     end function wpic_mom_calc_nvt
+     integer(c_int) function wpic_get_mom(ctx, mom) bind(C, name="wpic_get_mom")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(inout) :: mom(*)
+     end function wpic_get_mom
+     integer(c_int) function wpic_mom_calc_accl(ctx) bind(C, name="wpic_mom_calc_accl")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic_mom_calc_accl
+     integer(c_int) function wpic_bc_mom(ctx) bind(C, name="wpic_bc_mom")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic_bc_mom
      integer(c_int) function wpic_call(ctx) bind(C)
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx
@@ -281,14 +299,45 @@ contains
     real(8), intent(inout) :: phi(*)
   end subroutine boundary_periodic__phi
 
-  ! moments stay on the host: the one-rank periodic fold of the moment array
+  ! the fold runs on the device copy of mom that mom_calc__nvt left there; the host array
+  ! is refreshed from it
   subroutine boundary_periodic__mom(mom)
-    real(8), intent(inout) :: mom(7, wpic_prm%nxgs-1:wpic_prm%nxge+1, wpic_prm%nys-1:wpic_prm%nye+1, wpic_prm%nsp)
-    integer :: gs, ge, ys, ye
-    gs = wpic_prm%nxgs; ge = wpic_prm%nxge; ys = wpic_prm%nys; ye = wpic_prm%nye
-    mom(:, gs, :, :) = mom(:, gs, :, :) + mom(:, ge+1, :, :)
-    mom(:, ge, :, :) = mom(:, ge, :, :) + mom(:, gs-1, :, :)
-    mom(:, :, ye, :) = mom(:, :, ye, :) + mom(:, :, ys-1, :)
-    mom(:, :, ys, :) = mom(:, :, ys, :) + mom(:, :, ye+1, :)
+    real(8), intent(inout) :: mom(*)
+    call wpic_check(wpic_bc_mom(wpic_ctx), 'bc__mom')
+    call wpic_check(wpic_get_mom(wpic_ctx, mom), 'get mom')
   end subroutine boundary_periodic__mom
 end module boundary_periodic
+
+
+! mom_calc (2d/common/mom_calc.f90) on the device: mom_calc__accl writes the device gp,
+! mom_calc__nvt deposits from it (the driver passes gp) and copies mom to the host.
+module mom_calc
+  use wpic_capi
+  implicit none
+  private
+  public :: mom_calc__init, mom_calc__accl, mom_calc__nvt
+contains
+  subroutine mom_calc__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nys_in,nye_in, &
+                            delx_in,delt_in,c_in,q_in,r_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in, nxgs_in, nxge_in, nygs_in, nyge_in, nys_in, nye_in
+    real(8), intent(in) :: delx_in, delt_in, c_in, q_in(nsp_in), r_in(nsp_in)
+  end subroutine mom_calc__init
+
+  subroutine mom_calc__accl(gp,up,uf,cumcnt,nxs,nxe)
+    integer, intent(in)  :: nxs, nxe
+    integer, intent(in)  :: cumcnt(*)
+    real(8), intent(in)  :: up(*), uf(*)
+    real(8), intent(out) :: gp(*)
+    call wpic_ensure_ctx()
+    call wpic_check(wpic_mom_calc_accl(wpic_ctx), 'mom_calc__accl')
+  end subroutine mom_calc__accl
+
+  subroutine mom_calc__nvt(mom,up,np2)
+    integer, intent(in)  :: np2(*)
+    real(8), intent(in)  :: up(*)
+    real(8), intent(out) :: mom(*)
+    call wpic_ensure_ctx()
+    call wpic_check(wpic_mom_calc_nvt(wpic_ctx, 1_c_int), 'mom_calc__nvt')
+    call wpic_check(wpic_get_mom(wpic_ctx, mom), 'get mom')
+  end subroutine mom_calc__nvt
+end module mom_calc

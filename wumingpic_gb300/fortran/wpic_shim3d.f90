@@ -1,5 +1,5 @@
 ! wpic_shim3d.f90 -- drop-in replacements for WumingPIC's 3D hot-path modules
-! (particle, field, sort, boundary_periodic) that forward to the GB300 library's
+! (particle, field, sort, boundary_periodic, mom_calc) that forward to the GB300 library's
 ! wpic3d_* entry points through ISO_C_BINDING.  Link these objects instead of the
 ! corresponding objects of libwuming3d_common.a; the drivers (3d/proj/*/app.f90)
 ! stay unchanged.  Coherence follows the 2D shim: the first particle__solv uploads
@@ -42,6 +42,24 @@ module wpic3d_capi
        type(c_ptr), value :: ctx
        real(c_double), intent(in) :: uf(*)
      end function wpic3d_put_fields
+     integer(c_int) function wpic3d_mom_calc_accl(ctx) bind(C, name="wpic3d_mom_calc_accl")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic3d_mom_calc_accl
+     integer(c_int) function wpic3d_mom_calc_nvt(ctx, from_gp) bind(C, name="wpic3d_mom_calc_nvt")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: from_gp
+     end function wpic3d_mom_calc_nvt
+     integer(c_int) function wpic3d_bc_mom(ctx) bind(C, name="wpic3d_bc_mom")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+     end function wpic3d_bc_mom
+     integer(c_int) function wpic3d_get_mom(ctx, mom) bind(C, name="wpic3d_get_mom")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(inout) :: mom(*)
+     end function wpic3d_get_mom
      integer(c_int) function wpic3d_get_fields(ctx, uf) bind(C, name="wpic3d_get_fields")
        import :: c_int, c_ptr, c_double
        type(c_ptr), value :: ctx
@@ -257,18 +275,44 @@ contains
     real(8), intent(inout) :: phi(*)
   end subroutine boundary_periodic__phi
 
-  ! moments stay on the host: the one-rank periodic fold of the moment array in x, y, z
+  ! the fold runs on the device copy of mom that mom_calc__nvt left there
   subroutine boundary_periodic__mom(mom)
-    real(8), intent(inout) :: mom(7, wpic3_prm%nxgs-1:wpic3_prm%nxge+1, wpic3_prm%nys-1:wpic3_prm%nye+1, &
-                                  wpic3_prm%nzs-1:wpic3_prm%nze+1, wpic3_prm%nsp)
-    integer :: gs, ge, ys, ye, zs, ze
-    gs = wpic3_prm%nxgs; ge = wpic3_prm%nxge; ys = wpic3_prm%nys; ye = wpic3_prm%nye
-    zs = wpic3_prm%nzs; ze = wpic3_prm%nze
-    mom(:, gs, :, :, :) = mom(:, gs, :, :, :) + mom(:, ge+1, :, :, :)
-    mom(:, ge, :, :, :) = mom(:, ge, :, :, :) + mom(:, gs-1, :, :, :)
-    mom(:, :, ye, :, :) = mom(:, :, ye, :, :) + mom(:, :, ys-1, :, :)
-    mom(:, :, ys, :, :) = mom(:, :, ys, :, :) + mom(:, :, ye+1, :, :)
-    mom(:, :, :, ze, :) = mom(:, :, :, ze, :) + mom(:, :, :, zs-1, :)
-    mom(:, :, :, zs, :) = mom(:, :, :, zs, :) + mom(:, :, :, ze+1, :)
+    real(8), intent(inout) :: mom(*)
+    call wpic3_check(wpic3d_bc_mom(wpic3_ctx), 'bc__mom')
+    call wpic3_check(wpic3d_get_mom(wpic3_ctx, mom), 'get mom')
   end subroutine boundary_periodic__mom
 end module boundary_periodic
+
+
+! mom_calc (3d/common/mom_calc.f90) on the device, as in the 2D shim
+module mom_calc
+  use wpic3d_capi
+  implicit none
+  private
+  public :: mom_calc__init, mom_calc__accl, mom_calc__nvt
+contains
+  subroutine mom_calc__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nzgs_in,nzge_in,nys_in,nye_in, &
+                            nzs_in,nze_in,delx_in,delt_in,c_in,q_in,r_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in, nxgs_in, nxge_in, nygs_in, nyge_in, nzgs_in, nzge_in
+    integer, intent(in) :: nys_in, nye_in, nzs_in, nze_in
+    real(8), intent(in) :: delx_in, delt_in, c_in, q_in(nsp_in), r_in(nsp_in)
+  end subroutine mom_calc__init
+
+  subroutine mom_calc__accl(gp,up,uf,cumcnt,nxs,nxe)
+    integer, intent(in)  :: nxs, nxe
+    integer, intent(in)  :: cumcnt(*)
+    real(8), intent(in)  :: up(*), uf(*)
+    real(8), intent(out) :: gp(*)
+    call wpic3_ensure_ctx()
+    call wpic3_check(wpic3d_mom_calc_accl(wpic3_ctx), 'mom_calc__accl')
+  end subroutine mom_calc__accl
+
+  subroutine mom_calc__nvt(mom,up,np2)
+    integer, intent(in)  :: np2(*)
+    real(8), intent(in)  :: up(*)
+    real(8), intent(out) :: mom(*)
+    call wpic3_ensure_ctx()
+    call wpic3_check(wpic3d_mom_calc_nvt(wpic3_ctx, 1_c_int), 'mom_calc__nvt')
+    call wpic3_check(wpic3d_get_mom(wpic3_ctx, mom), 'get mom')
+  end subroutine mom_calc__nvt
+end module mom_calc

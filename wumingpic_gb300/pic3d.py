@@ -100,6 +100,9 @@ class Pic3D:
         check(lib().wpic3d_get_df(self._h, _ptr(df, np.float64)), "get df")
         return df
 
+    def put_df(self, df):
+        check(lib().wpic3d_put_df(self._h, _ptr(np.asfortranarray(df), np.float64)), "put df")
+
     def get_uj(self):
         uj = np.zeros(self._fshape(3), order="F")
         check(lib().wpic3d_get_uj(self._h, _ptr(uj, np.float64)), "get uj")
