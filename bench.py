@@ -218,16 +218,17 @@ def time_moments(g, torch, reps=3):
             "mom_bytes": int(mom.nbytes), "reps": reps}
 
 
-def time_path3d(steps, rank, torch, dist, world):
-    """The 3D FP64 path on the 3D Weibel workload (256^3 cells, 16 ppc/species, m_i/m_e = 16,
-    beams +-0.5c along x, u_th 0.05c), state resident in HBM, one warm-up step."""
+def time_path3d(steps, rank, torch, dist, world, precision="fp64", n=256):
+    """The 3D path (FP64, or mixed: FP32 push and deposit on split positions) on the 3D
+    Weibel workload (256^3 cells, 16 ppc/species, m_i/m_e = 16, beams +-0.5c along x,
+    u_th 0.05c), state resident in HBM, one warm-up step."""
     from wumingpic_gb300.loader import Plasma3D
     from wumingpic_gb300.pic3d import Pic3D
-    p = Plasma3D(nx=256, ny=256, nz=256, ppc=16, mass_ratio=16.0, drift=0.5, drift_axis=0, u_the=0.05,
+    p = Plasma3D(nx=n, ny=n, nz=n, ppc=16, mass_ratio=16.0, drift=0.5, drift_axis=0, u_the=0.05,
                  seed=20261203 + 7919 * rank, np_slack=1.5)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    g = Pic3D(p, precision="fp64", stream=stream.cuda_stream)
+    g = Pic3D(p, precision=precision, stream=stream.cuda_stream)
     g.load_weibel()
     npart = g.num_particles()
     g.step(1)
@@ -247,10 +248,11 @@ def time_path3d(steps, rank, torch, dist, world):
     cg = [int(x) for x in g.cg_iters()]
     moments = time_moments(g, torch, reps=2)
     g.close()
-    return {"workload": f"3D Weibel 256^3 cells, 16 ppc/species, {npart} particles, drift +-0.5c along x, "
+    return {"workload": f"3D Weibel {n}^3 cells, 16 ppc/species, {npart} particles, drift +-0.5c along x, "
                         f"u_th 0.05c, m_i/m_e 16, c*dt/dx=0.5",
             "value": npart * world * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
-            "steps": steps, "warmup": 1, "dtype": "f64", "cg_iterations": cg, "moments": moments}
+            "steps": steps, "warmup": 1, "dtype": "f64" if precision == "fp64" else "f32+f64",
+            "cg_iterations": cg, "moments": moments}
 
 
 def main():
@@ -263,6 +265,11 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the FP64 path (0 = skip)")
     ap.add_argument("--fp64-3d-steps", type=int, default=2,
                     help="timed steps of the 3D FP64 path on the 256^3 x 16 ppc Weibel workload (0 = skip)")
+    ap.add_argument("--mixed-3d-steps", type=int, default=5,
+                    help="timed steps of the 3D mixed path on the 256^3 x 16 ppc Weibel workload (0 = skip)")
+    ap.add_argument("--grid3d", type=int, default=256, help="cells per edge of the 3D legs")
+    ap.add_argument("--only-3d", action="store_true",
+                    help="run only the 3D legs and print them (a profiling aid, not the bench line)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--stages", action="store_true", help="print the per-stage breakdown to stderr")
@@ -284,6 +291,18 @@ def main():
 
     p = config(args.config)
     hbm_peak, hbm_src = measured_hbm_peak()
+    if args.only_3d:
+        out = {}
+        if args.fp64_3d_steps > 0:
+            out["fp64_3d_path"] = time_path3d(args.fp64_3d_steps, rank, torch, dist, world, n=args.grid3d)
+        if args.mixed_3d_steps > 0:
+            out["mixed_3d_path"] = time_path3d(args.mixed_3d_steps, rank, torch, dist, world, precision="mixed",
+                                               n=args.grid3d)
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
 
     # ---- mixed path: the headline ----
     g, npart, ms, stages, clocks = time_path(p, "mixed", args.steps, args.warmup, rank, torch, dist, local)
@@ -329,7 +348,12 @@ def main():
     # ---- 3D FP64 path: 256^3 cells, 16 ppc/species (the 3D Weibel configuration) ----
     fp64_3d = None
     if args.fp64_3d_steps > 0:
-        fp64_3d = time_path3d(args.fp64_3d_steps, rank, torch, dist, world)
+        fp64_3d = time_path3d(args.fp64_3d_steps, rank, torch, dist, world, n=args.grid3d)
+    mixed_3d = None
+    if args.mixed_3d_steps > 0:
+        mixed_3d = time_path3d(args.mixed_3d_steps, rank, torch, dist, world, precision="mixed", n=args.grid3d)
+        if fp64_3d:
+            mixed_3d["mixed_over_fp64"] = mixed_3d["value"] / fp64_3d["value"]
 
     base = None
     if rank == 0 and not args.no_cpu:
@@ -345,7 +369,7 @@ def main():
                 "path": "mixed: integer cell + FP32 offset, FP32 push/gather/deposition, FP64 fields and CG",
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks, "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()},
-                "moments": moments, "fp64_path": fp64, "fp64_3d_path": fp64_3d}
+                "moments": moments, "fp64_path": fp64, "fp64_3d_path": fp64_3d, "mixed_3d_path": mixed_3d}
         print(json.dumps(line), flush=True)
         if args.stages:
             for k, (t, n) in stages.items():

@@ -1,0 +1,111 @@
+"""The mixed-precision 3D path (FP32 push and deposit on split positions, FP64 fields and
+bookkeeping) against the FP64 3D path as the oracle.
+
+Tolerances (stated per test):
+  * one step from the same state: positions within 1e-5 cell, momenta within 1e-5 of the
+    largest |u|, current within 1e-5 of the largest |J| (FP32 arithmetic);
+  * charge conservation |(rho1 - rho0) dx/dt + div J| <= 1e-6 of max |rho1 - rho0| dx/dt;
+  * twenty steps of a Weibel plasma: total energy and field energy within 1e-3 relative,
+    the particle bookkeeping (np2 totals) exact.
+"""
+import numpy as np
+import pytest
+
+from tests.helpers import rho3d, small_case3d
+
+pytestmark = pytest.mark.gpu
+
+
+def make(p, precision):
+    from wumingpic_gb300.pic3d import Pic3D
+    return Pic3D(p, precision=precision)
+
+
+def by_id(st):
+    """id -> (x, y, z, ux, uy, uz) over the valid slots"""
+    rows = []
+    for isp in range(st.np2.shape[2]):
+        for k in range(st.np2.shape[1]):
+            for j in range(st.np2.shape[0]):
+                n = st.np2[j, k, isp]
+                a = st.up[:, :n, j, k, isp]
+                rows.append(np.vstack([a[:6], a[6].view(np.int64)[None, :].astype(np.float64)]))
+    a = np.concatenate(rows, axis=1)
+    order = np.argsort(a[6])
+    return a[:, order]
+
+
+def perturbed(seed, nx=16, ny=16, nz=8, ppc=6):
+    p, st = small_case3d(nx=nx, ny=ny, nz=nz, ppc=ppc, seed=seed, u_the=0.2, np_slack=3.0)
+    rng = np.random.default_rng(seed)
+    core = 0.02 * rng.standard_normal((6, p.nx, p.ny, p.nz))
+    st.uf[...] = np.pad(core, ((0, 0), (2, 2), (2, 2), (2, 2)), mode="wrap")
+    return p, st
+
+
+def test_mixed3d_one_step_against_fp64(gpu_lib):
+    p, st = perturbed(71)
+    m = make(p, "mixed")
+    m.put_state(st)
+    m.step(1)
+    f = make(p, "fp64")
+    f.put_state(st)
+    f.step(1)
+    sm, sf = m.get_state(), f.get_state()
+    assert sm.np2.sum() == sf.np2.sum()
+    a, b = by_id(sm), by_id(sf)
+    np.testing.assert_array_equal(a[6], b[6])
+    np.testing.assert_allclose(a[:3], b[:3], rtol=0, atol=1e-5 * p.delx)
+    umax = np.abs(b[3:6]).max()
+    np.testing.assert_allclose(a[3:6], b[3:6], rtol=0, atol=1e-5 * umax)
+    jm, jf = m.get_uj(), f.get_uj()
+    np.testing.assert_allclose(jm, jf, rtol=0, atol=1e-5 * np.abs(jf).max())
+
+
+def test_mixed3d_charge_conservation(gpu_lib):
+    """Second step (positions already split-representable): the FP32 Esirkepov current
+    satisfies continuity against the FP64 charge density of the stored positions."""
+    p, st = perturbed(72)
+    q, _ = p.charges()
+    m = make(p, "mixed")
+    m.put_state(st)
+    m.step(1)
+    s0 = m.get_state()
+    m.step(1)
+    s1 = m.get_state()
+    r0 = rho3d(p, s0.up, s0.np2, q)
+    r1 = rho3d(p, s1.up, s1.np2, q)
+    J = m.get_uj()[:, 2:-2, 2:-2, 2:-2]
+    res = (r1 - r0) * p.delx / p.delt
+    for d in range(3):
+        res = res + (np.roll(J[d], -1, d) - J[d])
+    scale = np.abs(r1 - r0).max() * p.delx / p.delt
+    assert np.abs(res).max() <= 1e-6 * scale
+
+
+def test_mixed3d_weibel_steps_track_fp64(gpu_lib):
+    from wumingpic_gb300.loader import Plasma3D
+    p = Plasma3D(nx=16, ny=16, nz=16, ppc=8, drift=0.5, u_the=0.05, seed=73, np_slack=2.0)
+    m, f = make(p, "mixed"), make(p, "fp64")
+    m.load_weibel()
+    f.load_weibel()
+    for _ in range(20):
+        m.step(1)
+        f.step(1)
+    assert m.num_particles() == f.num_particles() == p.n_particles
+    em, ef = m.energy(), f.energy()
+    np.testing.assert_allclose(em.sum(), ef.sum(), rtol=1e-3)
+    np.testing.assert_allclose(em[-2:], ef[-2:], rtol=1e-3, atol=1e-6 * ef.sum())
+
+
+def test_mixed3d_rejects_staged_calls_and_odd_tiles(gpu_lib):
+    from wumingpic_gb300._lib import WpicError
+    p, st = perturbed(74)
+    m = make(p, "mixed")
+    with pytest.raises(WpicError):
+        m.particle__solv()
+    with pytest.raises(WpicError):
+        m.field__fdtd_i()
+    p2, _ = small_case3d(nx=12, ny=16, nz=8, ppc=2, seed=75)
+    with pytest.raises(WpicError):
+        make(p2, "mixed")

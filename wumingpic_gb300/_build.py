@@ -36,6 +36,7 @@ CUDA_UNITS = {
     "no_alloc.cu": [],
     "capi3d.cu": [],
     "kernels3d_common.cu": [],
+    "mixed3d.cu": [],
 }
 
 

@@ -25,6 +25,9 @@ struct wpic_ctx3d {
   size_t staging_bytes = 0;
   int pusher = WPIC_PUSH_BORIS;  // the push of the fused step
   double* mom = nullptr;         // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nzs-1:nze+1, nsp), on first use
+  bool mixed = false;            // FP32 push/deposit on split positions (fused step only)
+  Mix3Const mk{};
+  long long* ujx = nullptr;      // global fixed-point current of the mixed step
 };
 
 namespace {
@@ -143,7 +146,25 @@ void do_migrate_sort3(wpic_ctx3d* c) {
   cudaMemcpyAsync(c->d.np2, c->d.np2new, sizeof(int) * c->d.nrow, cudaMemcpyDeviceToDevice, c->stream);
 }
 
+// the mixed step: fused FP32 push + deposit into the fixed-point current, then the FP64
+// field solve and bookkeeping of the FP64 path
+int mixed_step3(wpic_ctx3d* c) {
+  mix3_push_deposit(c->d, c->mk, c->ujx, c->stream);
+  curre_fold3d(c->d, c->stream);
+  fast::gkl3d(c->d, c->stream);
+  int st = do_cg3(c);
+  if (st) return st;
+  dfield_ghost3d(c->d, c->stream);
+  fast::efield3d(c->d, c->stream);
+  dfield_ghost3d(c->d, c->stream);
+  uf_add3d(c->d, c->stream);
+  particle_x3d(c->d, c->d.B, c->stream);
+  do_migrate_sort3(c);
+  return WPIC_OK;
+}
+
 int one_step3(wpic_ctx3d* c) {
+  if (c->mixed) return mixed_step3(c);
   if (c->pusher == WPIC_PUSH_VAY) FP3(push_vay3d, c->d, c->stream);
   else FP3(push3d, c->d, c->stream);
   int st = do_field3(c);
@@ -186,7 +207,9 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
   if (p->ndim != 7 || p->nsp < 1 || p->nsp > 2 || nx < 4 || ny < 4 || nz < 4 || p->np < 1) return WPIC_BAD_ARGUMENT;
   if (p->nys != p->nygs || p->nye != p->nyge || p->nzs != p->nzgs || p->nze != p->nzge) return WPIC_BAD_ARGUMENT;
   if (!(p->delx > 0) || !(p->delt > 0) || !(p->c > 0)) return WPIC_BAD_ARGUMENT;
-  if (p->precision != WPIC_FP64 && p->precision != WPIC_FP64_EXACT) return WPIC_BAD_ARGUMENT;
+  if (p->precision != WPIC_FP64 && p->precision != WPIC_FP64_EXACT && p->precision != WPIC_MIXED)
+    return WPIC_BAD_ARGUMENT;
+  if (p->precision == WPIC_MIXED && !mix3_shape_ok(nx, ny, nz)) return WPIC_BAD_ARGUMENT;
   if ((double)nx * ny * nz > 2.0e9 || (double)p->nsp * ny * nz * p->np >= 2147483647.0) return WPIC_BAD_ARGUMENT;
   wpic_ctx3d* c = new wpic_ctx3d();
   c->prm = *p;
@@ -225,6 +248,29 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
   ph.d_delt = 1.0 / p->delt;
   d.cap = p->device_cap > 0 ? p->device_cap : p->np;
   d.nrow = p->nsp * ny * nz;
+  c->mixed = p->precision == WPIC_MIXED;
+  if (c->mixed) {
+    // FP32 constants of the split-position step, rounded once (the FP64 expressions of
+    // 3d/common/particle.f90:106-108 and 3d/common/field.f90:226)
+    Mix3Const& k = c->mk;
+    double vmax = 0.0;
+    for (int s = 0; s < 2; ++s) {
+      const bool on = s < p->nsp;
+      k.fac1[s] = on ? (float)(p->q[s] / p->r[s] * 0.5 * p->delt) : 0.f;
+      k.fac2[s] = on ? (float)(p->q[s] * p->delt / p->r[s]) : 0.f;
+      k.qdd[s] = on ? (float)(p->q[s] * p->delx * (1.0 / p->delt)) : 0.f;
+      if (on) vmax = std::max(vmax, std::fabs(p->q[s] * p->delx / p->delt));
+    }
+    vmax = std::max(vmax, 1e-30);
+    k.dtdx = (float)(p->delt / p->delx);
+    k.c = (float)p->c;
+    k.ic2 = (float)(1.0 / (p->c * p->c));
+    k.vmax = (float)(vmax * (1.0 + 1e-6));
+    // a contribution is at most |q| dx / dt; a node's sum over all particles at most slots times that
+    k.eA = std::ilogb(4194304.0 / (double)k.vmax);
+    const double slots = (double)d.nrow * (double)d.cap;
+    k.G = std::ilogb(4611686018427387904.0 / (slots * (double)k.vmax));
+  }
   d.nred = (int)std::min<size_t>(1216, (d.g.ncell + CG_THREADS_HOST - 1) / CG_THREADS_HOST);
   if (d.nred < 1) d.nred = 1;
   d.ite_max = 100;
@@ -247,7 +293,12 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
     if ((st = dalloc3(c, &d.uf, 6 * d.g.fvol)) || (st = dalloc3(c, &d.df, 6 * d.g.fvol)) ||
         (st = dalloc3(c, &d.uj, 3 * d.g.fvol)) || (st = dalloc3(c, &d.gkl, 3 * d.g.ncell)))
       break;
-    if ((st = dalloc3(c, &d.cellJ, (size_t)375 * d.g.ncell))) break;
+    if (c->mixed) {
+      if (mix3_setup() != 0) { st = WPIC_CUDA_ERROR; break; }
+      if ((st = dalloc3(c, &c->ujx, 3 * d.g.fvol))) break;
+    } else if ((st = dalloc3(c, &d.cellJ, (size_t)375 * d.g.ncell))) {
+      break;
+    }
     if ((st = dalloc3(c, &d.phi, 3 * d.g.ncell)) || (st = dalloc3(c, &d.p, 3 * d.g.ncell)) ||
         (st = dalloc3(c, &d.r, 3 * d.g.ncell)) || (st = dalloc3(c, &d.ap, 3 * d.g.ncell)) ||
         (st = dalloc3(c, &d.b, 3 * d.g.ncell)))
@@ -348,12 +399,14 @@ int wpic3d_get_uj(wpic_ctx3d* c, double* uj) { return c ? get_field3(c, uj, c->d
 
 int wpic3d_particle_solv(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
   FP3(push3d, c->d, c->stream);
   return finish3(c);
 }
 
 int wpic3d_particle_solv_vay(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
   FP3(push_vay3d, c->d, c->stream);
   return finish3(c);
 }
@@ -361,12 +414,14 @@ int wpic3d_particle_solv_vay(wpic_ctx3d* c) {
 int wpic3d_set_pusher(wpic_ctx3d* c, int pusher) {
   if (!c) return WPIC_NOT_INITIALISED;
   if (pusher != WPIC_PUSH_BORIS && pusher != WPIC_PUSH_VAY) return WPIC_BAD_ARGUMENT;
+  if (c->mixed && pusher != WPIC_PUSH_BORIS) return WPIC_BAD_ARGUMENT;
   c->pusher = pusher;
   return WPIC_OK;
 }
 
 int wpic3d_field_fdtd_i(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
   int st = do_field3(c);
   if (st) return st;
   return finish3(c);
@@ -375,6 +430,7 @@ int wpic3d_field_fdtd_i(wpic_ctx3d* c) {
 // ele_cur + bc__curre of field__fdtd_i (3d/common/field.f90:129-130), for parity checks
 int wpic3d_ele_cur(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
   FP3(deposit3d, c->d, c->stream);
   curre_fold3d(c->d, c->stream);
   return finish3(c);

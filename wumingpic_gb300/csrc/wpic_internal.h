@@ -254,6 +254,17 @@ struct Dev3D {
 namespace exact { WPIC_DECLARE_FP3_LAUNCHERS }
 namespace fast { WPIC_DECLARE_FP3_LAUNCHERS }
 
+// mixed-precision 3D: FP32 constants rounded once on the host, and the fixed-point exponents
+// (eA: largest tile scale keeping |v s1| < 2^22; G: global int64 scale 2^G)
+struct Mix3Const {
+  float fac1[2], fac2[2], qdd[2];
+  float dtdx, c, ic2, vmax;
+  int eA, G;
+};
+void mix3_push_deposit(const Dev3D& d, const Mix3Const& k, long long* ujx, cudaStream_t s);
+bool mix3_shape_ok(int nx, int ny, int nz);
+int mix3_setup();  // kernel attributes (dynamic shared memory); 0 on success
+
 void curre_fold3d(const Dev3D& d, cudaStream_t s);
 void bc_mom3d(const Dev3D& d, double* mom, cudaStream_t s);
 void dfield_ghost3d(const Dev3D& d, cudaStream_t s);

@@ -34,7 +34,7 @@ class Pic3D:
         prm.delx, prm.delt, prm.c, prm.gfac = plasma.delx, plasma.delt, plasma.c, plasma.gfac
         prm.q[0], prm.q[1] = q[0], q[1]
         prm.r[0], prm.r[1] = r[0], r[1]
-        prm.precision = {"fp64": _lib.FP64, "fp64_exact": _lib.FP64_EXACT}[precision]
+        prm.precision = {"fp64": _lib.FP64, "fp64_exact": _lib.FP64_EXACT, "mixed": _lib.MIXED}[precision]
         prm.device_cap = int(device_cap)
         self.precision = precision
         h = ctypes.c_void_p()
