@@ -109,3 +109,26 @@ def test_mixed3d_rejects_staged_calls_and_odd_tiles(gpu_lib):
     p2, _ = small_case3d(nx=12, ny=16, nz=8, ppc=2, seed=75)
     with pytest.raises(WpicError):
         make(p2, "mixed")
+
+
+def test_mixed3d_moments_against_oracle(gpu_lib):
+    """FP32 half-step push and FP32 node sums against the FP64 oracle on the same state:
+    within 2e-5 of each moment's largest magnitude; the state is not modified."""
+    from oracle.oracle import Oracle3D
+    p, st = perturbed(76)
+    m = make(p, "mixed")
+    m.put_state(st)
+    m.step(1)
+    cur = m.get_state()
+    mom = m.moments()
+    q, r = p.charges()
+    o = Oracle3D(nx=p.nx, ny=p.ny, nz=p.nz, np_cap=p.np_cap, q=q, r=r, delt=p.delt, delx=p.delx, c=p.c,
+                 gfac=p.gfac)
+    rc, ref = o.moments(cur.copy())
+    assert rc == 0
+    for l in range(7):
+        for isp in range(p.nsp):
+            scale = np.abs(ref[l, ..., isp]).max()
+            np.testing.assert_allclose(mom[l, ..., isp], ref[l, ..., isp], rtol=0, atol=2e-5 * scale)
+    after = m.get_state()
+    np.testing.assert_array_equal(after.up, cur.up)

@@ -546,9 +546,13 @@ int wpic3d_moments(wpic_ctx3d* c, double* mom) {
   if (!c) return WPIC_NOT_INITIALISED;
   int st = ensure_mom3(c);
   if (st) return st;
-  FP3(mom_accl3d, c->d, c->stream);
-  FP3(mom_nvt3d, c->d, c->d.B, c->mom, c->stream);
-  bc_mom3d(c->d, c->mom, c->stream);
+  if (c->mixed) {
+    mix3_moments(c->d, c->mk, c->mom, c->stream);
+  } else {
+    FP3(mom_accl3d, c->d, c->stream);
+    FP3(mom_nvt3d, c->d, c->d.B, c->mom, c->stream);
+    bc_mom3d(c->d, c->mom, c->stream);
+  }
   if ((st = copy_mom3(c, mom))) return st;
   return finish3(c);
 }

@@ -291,6 +291,139 @@ void mix3_push_deposit(const Dev3D& d, const Mix3Const& k, long long* ujx, cudaS
   k_mix3_fix<<<4 * 152, 256, 0, s>>>(d, ujx, std::ldexp(1.0, -k.G));
 }
 
+// ---------------------------------------------------------------------------
+// mom_calc__accl + mom_calc__nvt (3d/common/mom_calc.f90:49-332) for the mixed path: the
+// half-step push (time step halved by mom_calc__init, :36) in FP32 on split positions, then
+// the seven moments of each particle at its 2 x 2 x 2 half-integer nodes (node index
+// floor(x/dx - 0.5), cell - 1 or cell), summed in the tile's 10 x 10 x 6 node patch with FP32
+// shared atomics and added once per node into the FP64 moments.  The state is not modified.
+// ---------------------------------------------------------------------------
+constexpr int M3X = T3X + 2, M3Y = T3Y + 2, M3Z = T3Z + 2;  // nodes at cell offsets -1 .. T
+
+__global__ void __launch_bounds__(T3C, 2) k_mix3_mom(Dev3D d, Mix3Const k, double* mom) {
+  __shared__ float tf[6][F3Z][F3Y][F3X];
+  __shared__ float macc[7][M3Z][M3Y][M3X];
+  const Grid3D g = d.g;
+  const int ntx = g.nx / T3X, nty = g.ny / T3Y;
+  const int b = blockIdx.x;
+  const int cx0 = (b % ntx) * T3X, cy0 = ((b / ntx) % nty) * T3Y, cz0 = (b / (ntx * nty)) * T3Z;
+  const int t = threadIdx.x;
+  for (int idx = t; idx < F3X * F3Y * F3Z; idx += T3C) {
+    const int a = idx % F3X, bb = (idx / F3X) % F3Y, cc = idx / (F3X * F3Y);
+    const size_t f = fidx3(g, cx0 + a + 1, cy0 + bb + 1, cz0 + cc + 1);
+    const size_t V = g.fvol, I = 1, J = g.fp, K = g.fplane;
+    const double* U = d.uf;
+    tf[0][cc][bb][a] = (float)(2.5e-1 * (U[f] + U[f + J] + U[f + K] + U[f + J + K]));
+    tf[1][cc][bb][a] = (float)(2.5e-1 * (U[V + f] + U[V + f + I] + U[V + f + K] + U[V + f + I + K]));
+    tf[2][cc][bb][a] = (float)(2.5e-1 * (U[2 * V + f] + U[2 * V + f + I] + U[2 * V + f + J] + U[2 * V + f + I + J]));
+    tf[3][cc][bb][a] = (float)(5e-1 * (U[3 * V + f] + U[3 * V + f + I]));
+    tf[4][cc][bb][a] = (float)(5e-1 * (U[4 * V + f] + U[4 * V + f + J]));
+    tf[5][cc][bb][a] = (float)(5e-1 * (U[5 * V + f] + U[5 * V + f + K]));
+  }
+  for (int idx = t; idx < 7 * M3X * M3Y * M3Z; idx += T3C) (&macc[0][0][0][0])[idx] = 0.f;
+  __syncthreads();
+  const int lx = t % T3X, ly = (t / T3X) % T3Y, lz = t / (T3X * T3Y);
+  const int ci = cx0 + lx, cj = cy0 + ly, ck = cz0 + lz;
+  const double dxi = d.ph.p_d_delx;
+  const int ia = g.nxgs + ci, ja = g.nygs + cj, ka = g.nzgs + ck;
+  const float cl = k.c, ic2 = k.ic2;
+  for (int isp = 0; isp < d.ph.nsp; ++isp) {
+    const int row = (isp * g.nz + ck) * g.ny + cj;
+    const int* ccr = d.cc + (size_t)row * (g.nx + 1);
+    const int sb = ccr[ci], se = ccr[ci + 1];
+    const float fac1 = 0.5f * k.fac1[isp], fac2 = 0.5f * k.fac2[isp];  // half time step
+    const float txxx = fac1 * fac1;
+    const size_t rbase = (size_t)row * d.cap;
+    for (int s = sb; s < se; ++s) {
+      const size_t q = rbase + s;
+      float o[3] = {(float)(d.A.x[q] * dxi - (double)ia), (float)(d.A.y[q] * dxi - (double)ja),
+                    (float)(d.A.z[q] * dxi - (double)ka)};
+      float w[3][3];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        o[m] = fminf(fmaxf(o[m], 0.f), 0.99999994f);
+        w[m][0] = 0.5f * (1.f - o[m]) * (1.f - o[m]);
+        w[m][1] = 0.75f - (o[m] - 0.5f) * (o[m] - 0.5f);
+        w[m][2] = 0.5f * o[m] * o[m];
+      }
+      float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int c3 = 0; c3 < 3; ++c3)
+#pragma unroll
+        for (int b3 = 0; b3 < 3; ++b3) {
+          const float wzy = w[2][c3] * w[1][b3];
+#pragma unroll
+          for (int a3 = 0; a3 < 3; ++a3) {
+            const float wt = wzy * w[0][a3];
+#pragma unroll
+            for (int m = 0; m < 6; ++m) f[m] = fmaf(wt, tf[m][lz + c3][ly + b3][lx + a3], f[m]);
+          }
+        }
+      const float bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
+      float u1 = (float)d.A.ux[q] + fac1 * epx, u2 = (float)d.A.uy[q] + fac1 * epy, u3 = (float)d.A.uz[q] + fac1 * epz;
+      const float g2 = cl * cl + u1 * u1 + u2 * u2 + u3 * u3;
+      const float igam = rsqrtf(g2);
+      const float gm = g2 * igam;
+      const float fac1r = fac1 * igam;
+      const float fac2r = __fdividef(fac2, gm + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
+      const float u4 = u1 + fac1r * (u2 * bpz - u3 * bpy);
+      const float u5 = u2 + fac1r * (u3 * bpx - u1 * bpz);
+      const float u6 = u3 + fac1r * (u1 * bpy - u2 * bpx);
+      u1 = u1 + fac2r * (u5 * bpz - u6 * bpy);
+      u2 = u2 + fac2r * (u6 * bpx - u4 * bpz);
+      u3 = u3 + fac2r * (u4 * bpy - u5 * bpx);
+      const float ux = u1 + fac1 * epx, uy = u2 + fac1 * epy, uz = u3 + fac1 * epz;
+      const float gam = rsqrtf(1.f + (ux * ux + uy * uy + uz * uz) * ic2);
+      const float pre[7] = {1.f, ux * gam, uy * gam, uz * gam, ux * ux * gam, uy * uy * gam, uz * uz * gam};
+      // node index cell - 1 (offset < 1/2) or cell; local node coordinate = l + (0 or 1)
+      float wl[3][2];
+      int nb[3];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const float h = o[m] - 0.5f;
+        nb[m] = h < 0.f ? 0 : 1;
+        const float dd = h < 0.f ? h + 1.f : h;
+        wl[m][0] = 1.f - dd;
+        wl[m][1] = dd;
+      }
+#pragma unroll
+      for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+        for (int by = 0; by < 2; ++by)
+#pragma unroll
+          for (int ax = 0; ax < 2; ++ax) {
+            const float wt = wl[0][ax] * wl[1][by] * wl[2][cz];
+            const int xl = lx + nb[0] + ax, yl = ly + nb[1] + by, zl = lz + nb[2] + cz;
+#pragma unroll
+            for (int l = 0; l < 7; ++l) atomicAdd(&macc[l][zl][yl][xl], pre[l] * wt);
+          }
+    }
+    __syncthreads();
+    // the patch into the FP64 moments of this species: local node (xl, yl, zl) is node index
+    // (cx0 + xl, cy0 + yl, cz0 + zl) of mom(7, nxgs-1:nxge+1, nys-1:nye+1, nzs-1:nze+1, nsp)
+    const size_t nxm = g.nx + 2, nym = g.ny + 2, nzm = g.nz + 2;
+    for (int idx = t; idx < M3X * M3Y * M3Z; idx += T3C) {
+      const int xl = idx % M3X, yl = (idx / M3X) % M3Y, zl = idx / (M3X * M3Y);
+      double* out = mom + 7 * ((size_t)(cx0 + xl) +
+                               nxm * ((size_t)(cy0 + yl) + nym * ((size_t)(cz0 + zl) + nzm * isp)));
+#pragma unroll
+      for (int l = 0; l < 7; ++l) {
+        const float v = macc[l][zl][yl][xl];
+        if (v != 0.f) atomicAdd(out + l, (double)v);
+        macc[l][zl][yl][xl] = 0.f;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+void mix3_moments(const Dev3D& d, const Mix3Const& k, double* mom, cudaStream_t s) {
+  const int ntile = (d.g.nx / T3X) * (d.g.ny / T3Y) * (d.g.nz / T3Z);
+  cudaMemsetAsync(mom, 0, sizeof(double) * 7 * (size_t)(d.g.nx + 2) * (d.g.ny + 2) * (d.g.nz + 2) * d.ph.nsp, s);
+  k_mix3_mom<<<ntile, T3C, 0, s>>>(d, k, mom);
+  bc_mom3d(d, mom, s);
+}
+
 bool mix3_shape_ok(int nx, int ny, int nz) { return nx % T3X == 0 && ny % T3Y == 0 && nz % T3Z == 0; }
 
 int mix3_setup() {

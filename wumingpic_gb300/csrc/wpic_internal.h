@@ -264,6 +264,7 @@ struct Mix3Const {
 void mix3_push_deposit(const Dev3D& d, const Mix3Const& k, long long* ujx, cudaStream_t s);
 bool mix3_shape_ok(int nx, int ny, int nz);
 int mix3_setup();  // kernel attributes (dynamic shared memory); 0 on success
+void mix3_moments(const Dev3D& d, const Mix3Const& k, double* mom, cudaStream_t s);
 
 void curre_fold3d(const Dev3D& d, cudaStream_t s);
 void bc_mom3d(const Dev3D& d, double* mom, cudaStream_t s);
