@@ -49,6 +49,9 @@ extern "C" {
 #define WPIC_BC_PERIODIC 0     /* boundary_periodic (2d/common/boundary_periodic.f90) */
 #define WPIC_BC_RECONNECTION 1 /* boundary_reconnection: conducting walls in x
                                   (2d/proj/reconnection/boundary_reconnection.f90) */
+#define WPIC_BC_SHOCK 2        /* boundary_shock: reflecting wall at nxs, injection boundary at
+                                  nxe of the active window (2d/proj/shock/boundary_shock.f90);
+                                  FP64 paths */
 
 /* arithmetic of the particle and field kernels */
 #define WPIC_FP64 0       /* FP64, fused multiply-add allowed */
@@ -107,6 +110,15 @@ int wpic_particle_solv(wpic_ctx* ctx);
 int wpic_particle_solv_vay(wpic_ctx* ctx);
 /* which push the fused step (wpic_step) uses: WPIC_PUSH_BORIS (default) or WPIC_PUSH_VAY */
 int wpic_set_pusher(wpic_ctx* ctx, int pusher);
+/* the active x window nxs..nxe that the drivers pass to every module call; the shock
+ * driver widens it as its box expands (2d/proj/shock/app.f90:276-277, 615-625).  Default:
+ * the whole domain; walls only (FP64 paths).  Cells outside the window hold no particles
+ * and keep their fields. */
+int wpic_set_window(wpic_ctx* ctx, int nxs, int nxe);
+/* the upstream four-velocity u0 of boundary_shock__injection used by the fused step */
+int wpic_set_injection(wpic_ctx* ctx, double u0);
+/* boundary_shock__injection(gp,np2,nxs,nxe,u0)   2d/proj/shock/boundary_shock.f90:255 */
+int wpic_bc_injection(wpic_ctx* ctx, double u0);
 
 /* Moments (the driver's diagnostic block, 2d/proj/weibel/app.f90:121-123).  The device keeps
  * mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp) in the reference's layout: number density, the three

@@ -21,7 +21,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 
 OK, CG_NOT_CONVERGED, CAPACITY, OUT_OF_RANGE = 0, 1, 2, 3
-BC_PERIODIC, BC_RECONNECTION = 0, 1
+BC_PERIODIC, BC_RECONNECTION, BC_SHOCK = 0, 1, 2
 
 _lib = None
 
@@ -46,6 +46,7 @@ def lib():
         L.orc2d_mom_calc_accl.argtypes = [vp, dp, dp, dp, ip, i, i]
         L.orc2d_mom_calc_nvt.argtypes = [vp, dp, dp, ip]
         L.orc2d_bc_mom.argtypes = [vp, dp]
+        L.orc2d_bc_injection.argtypes = [vp, dp, ip, i, i, d]
         L.orc2d_ele_cur.argtypes = [vp, dp, dp, dp, ip, i, i]
         L.orc2d_bc_curre.argtypes = [vp, dp, i, i]
         L.orc2d_bc_dfield.argtypes = [vp, dp, i, i]
@@ -96,7 +97,8 @@ class Oracle2D:
         self.nxgs, self.nxge = nxgs, nxgs + nx - 1
         self.nygs, self.nyge = nygs, nygs + ny - 1
         self.nxs, self.nxe = self.nxgs, self.nxge
-        self.bc = BC_PERIODIC if bc == "periodic" else BC_RECONNECTION
+        self.bc = {"periodic": BC_PERIODIC, "reconnection": BC_RECONNECTION, "shock": BC_SHOCK}[bc]
+        self.u0 = 0.0  # upstream four-velocity of the shock injection boundary
         q = np.ascontiguousarray(q, dtype=np.float64)
         r = np.ascontiguousarray(r, dtype=np.float64)
         self._h = lib().orc2d_create(ndim, np_cap, nsp, self.nxgs, self.nxge, self.nygs, self.nyge, self.nygs,
@@ -163,6 +165,15 @@ class Oracle2D:
     def bc_mom(self, mom):
         return lib().orc2d_bc_mom(self._h, _p(mom, np.float64))
 
+    def set_window(self, nxs, nxe):
+        """the active x window nxs..nxe that the driver passes to every call (the shock
+        driver's expanding box, 2d/proj/shock/app.f90:276-277, 615-625)"""
+        self.nxs, self.nxe = int(nxs), int(nxe)
+
+    def bc_injection(self, up, np2, u0=None):
+        return lib().orc2d_bc_injection(self._h, _p(up, np.float64), _p(np2, np.int32), self.nxs, self.nxe,
+                                        self.u0 if u0 is None else u0)
+
     def moments(self, st):
         """The driver's diagnostic block (2d/proj/weibel/app.f90:121-123) on a State2D:
         mom_calc__accl into st.gp, mom_calc__nvt from st.gp, bc__mom.  Returns (status, mom)."""
@@ -213,6 +224,8 @@ class Oracle2D:
         rc = push(st.gp, st.up, st.uf, st.cumcnt)
         if self.bc == BC_RECONNECTION:
             rc = rc or self.bc_particle_x(st.gp, st.np2)
+        if self.bc == BC_SHOCK:  # 2d/proj/shock/app.f90:110-115
+            rc = rc or self.bc_injection(st.gp, st.np2)
         rc = rc or self.field_fdtd_i(st.uf, st.up, st.gp, st.cumcnt)
         if self.bc == BC_PERIODIC:
             rc = rc or self.bc_particle_x(st.gp, st.np2)

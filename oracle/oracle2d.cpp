@@ -16,6 +16,9 @@
 //                             2d/common/boundary_periodic.f90:61-568
 //   boundary_reconnection__particle_x/dfield/curre/phi (conducting walls in x)
 //                             2d/proj/reconnection/boundary_reconnection.f90:61-99,254-579
+//   boundary_shock__particle_x/injection/dfield/curre/phi/mom (reflecting wall at the left,
+//   the moving injection boundary at the right of the window nxs..nxe)
+//                             2d/proj/shock/boundary_shock.f90:62-100,255-693
 //   energy_history sums       2d/proj/weibel/app.f90:479-545
 //   particle__solv_vay        2d/common/particle.f90:182-315
 //   mom_calc__accl / __nvt    2d/common/mom_calc.f90:48-249
@@ -52,7 +55,7 @@
 namespace {
 
 enum { ORC_OK = 0, ORC_CG_NOT_CONVERGED = 1, ORC_CAPACITY = 2, ORC_OUT_OF_RANGE = 3 };
-enum { BC_PERIODIC = 0, BC_RECONNECTION = 1 };
+enum { BC_PERIODIC = 0, BC_RECONNECTION = 1, BC_SHOCK = 2 };
 
 struct Orc2D {
   int ndim, np, nsp, nxgs, nxge, nygs, nyge, nys, nye;
@@ -444,6 +447,10 @@ void bc_dfield(Orc2D* o, double* df, int nxs, int nxe) {
       df[o->iuf(1, nxs - 1, j)] = -df[o->iuf(1, nxs, j)];
       for (int k = 2; k <= 4; ++k) df[o->iuf(k, nxs - 1, j)] = df[o->iuf(k, nxs + 1, j)];
       for (int k = 5; k <= 6; ++k) df[o->iuf(k, nxs - 1, j)] = -df[o->iuf(k, nxs, j)];
+      if (o->bc_kind == BC_SHOCK) {  // boundary_shock.f90:399-405
+        for (int k = 1; k <= 6; ++k) df[o->iuf(k, nxe + 1, j)] = 0.0;
+        continue;
+      }
       df[o->iuf(1, nxe, j)] = -df[o->iuf(1, nxe - 1, j)];
       for (int k = 2; k <= 4; ++k) df[o->iuf(k, nxe + 1, j)] = df[o->iuf(k, nxe - 1, j)];
       for (int k = 5; k <= 6; ++k) df[o->iuf(k, nxe, j)] = -df[o->iuf(k, nxe - 1, j)];
@@ -466,12 +473,12 @@ void bc_phi(Orc2D* o, double* phi, int nxs, int nxe, int l) {
   } else if (l == 1) {
     for (int j = nys - 1; j <= nye + 1; ++j) {
       P(nxs - 1, j) = -P(nxs, j);
-      P(nxe + 1, j) = -P(nxe - 2, j);
+      P(nxe + 1, j) = o->bc_kind == BC_SHOCK ? 0.0 : -P(nxe - 2, j);  // boundary_shock.f90:605-611
     }
   } else {
     for (int j = nys - 1; j <= nye + 1; ++j) {
       P(nxs - 1, j) = P(nxs + 1, j);
-      P(nxe + 1, j) = P(nxe - 1, j);
+      P(nxe + 1, j) = o->bc_kind == BC_SHOCK ? 0.0 : P(nxe - 1, j);
     }
   }
 }
@@ -854,6 +861,35 @@ int energy(Orc2D* o, const double* up, const double* uf, const int* np2, double*
 }
 
 // ---------------------------------------------------------------------------
+// boundary_shock__injection  (2d/proj/shock/boundary_shock.f90:255-297): reflection at the
+// wall x = (nxs+1) dx, and at the injection boundary xend = nxe dx + v0 dt moving with the
+// upstream flow u0 (four-velocity), where u_x -> 2 u0 - u_x.  Default rounding.
+// ---------------------------------------------------------------------------
+int bc_injection(Orc2D* o, double* up, const int* np2, int nxs, int nxe, double u0) {
+  const int nys = o->nys, nye = o->nye;
+  const double delx = o->delx, c = o->c, delt = o->delt;
+  const double xend = nxe * delx + u0 / std::sqrt(1 + (u0 * u0) / (c * c)) * delt;
+  set_threads(o);
+  for (int isp = 1; isp <= o->nsp; ++isp) {
+#pragma omp parallel for
+    for (int j = nys; j <= nye; ++j)
+      for (int ii = 1; ii <= np2[o->inp2(j, isp)]; ++ii) {
+        double& x = up[o->iup(1, ii, j, isp)];
+        const int ipos = (int)(x / delx);
+        if (ipos < nxs + 1) {
+          x = +(double)(2.0f * (float)(nxs + 1)) * delx - x;
+          for (int d = 3; d <= 5; ++d) up[o->iup(d, ii, j, isp)] = -up[o->iup(d, ii, j, isp)];
+        } else if (x > xend) {
+          x = +2. * xend - x;
+          up[o->iup(3, ii, j, isp)] = +2. * u0 - up[o->iup(3, ii, j, isp)];
+          for (int d = 4; d <= 5; ++d) up[o->iup(d, ii, j, isp)] = -up[o->iup(d, ii, j, isp)];
+        }
+      }
+  }
+  return ORC_OK;
+}
+
+// ---------------------------------------------------------------------------
 // mom_calc__nvt  (2d/common/mom_calc.f90:164-249)
 // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp): number density, velocity and diagonal
 // of u v at the half-integer nodes, linear (area) weights, single-thread order.
@@ -899,7 +935,7 @@ void bc_mom(Orc2D* o, double* mom) {
   for (int isp = 1; isp <= o->nsp; ++isp)
     for (int j = nys - 1; j <= nye + 1; ++j)
       for (int l = 1; l <= 7; ++l) {
-        if (o->bc_kind == BC_RECONNECTION) {
+        if (o->bc_kind != BC_PERIODIC) {  // walls (reconnection, shock: boundary_shock.f90:628-693)
           mom[imom(o, l, nxgs, j, isp)] = mom[imom(o, l, nxgs, j, isp)] + mom[imom(o, l, nxgs - 1, j, isp)];
           mom[imom(o, l, nxge, j, isp)] = mom[imom(o, l, nxge, j, isp)] + mom[imom(o, l, nxge + 1, j, isp)];
         } else {
@@ -987,6 +1023,9 @@ int orc2d_mom_calc_nvt(void* h, double* mom, const double* up, const int* np2) {
   return mom_nvt((Orc2D*)h, mom, up, np2);
 }
 int orc2d_bc_mom(void* h, double* mom) { bc_mom((Orc2D*)h, mom); return 0; }
+int orc2d_bc_injection(void* h, double* up, const int* np2, int nxs, int nxe, double u0) {
+  return bc_injection((Orc2D*)h, up, np2, nxs, nxe, u0);
+}
 int orc2d_ele_cur(void* h, double* uj, const double* up, const double* gp, const int* cumcnt, int nxs, int nxe) {
   return ele_cur((Orc2D*)h, uj, up, gp, cumcnt, nxs, nxe);
 }

@@ -491,3 +491,89 @@ def test_moments_mixed_against_oracle(gpu_lib, bc):
             np.testing.assert_allclose(mom[l, :, :, isp], ref[l, :, :, isp], rtol=0, atol=2e-5 * scale)
     after = g.get_state()
     np.testing.assert_array_equal(after.up, cur.up)
+
+
+# ---- the shock boundary family (2d/proj/shock/boundary_shock.f90) on a window nxs..nxe ----
+
+def shock_setup(seed, nx=24, ny=8, window=16, ppc=5, u0=0.3):
+    p, st = small_case(nx=nx, ny=ny, ppc=ppc, seed=seed, bc="shock", window=window, u0=u0, u_the=0.1)
+    rng = np.random.default_rng(seed)
+    # small fields inside the window and its ghosts; the region beyond stays zero
+    st.uf[:, :window + 4, :] = 0.02 * rng.standard_normal((6, window + 4, ny + 4))
+    st.uf[:, :, :2] = st.uf[:, :, ny:ny + 2]
+    st.uf[:, :, ny + 2:] = st.uf[:, :, 2:4]
+    o = make_oracle(p)
+    o.set_window(p.nxgs, p.nxe)
+    o.u0 = p.u0
+    return p, st, o
+
+
+def assert_window_cumcnt(a, b, window):
+    np.testing.assert_array_equal(a[:window + 1], b[:window + 1])
+
+
+def test_shock_injection_parity(gpu_lib):
+    p, st, o = shock_setup(91)
+    g = make_gpu(p, "fp64_exact", gpu_lib)
+    g.put_state(st)
+    g.particle__solv()
+    g.bc__injection(p.u0)
+    gp_gpu, np2, _ = g.get_particles(1)
+    ref = st.copy()
+    assert o.particle_solv(ref.gp, ref.up, ref.uf, ref.cumcnt) == 0
+    assert o.bc_injection(ref.gp, ref.np2) == 0
+    assert_particles(gp_gpu, np2, ref.gp, ref.np2)
+
+
+def test_shock_one_step_exact(gpu_lib):
+    """The shock driver's step (particle__solv, bc__injection, field__fdtd_i with the shock
+    boundaries on the window, bc__particle_y, sort__bucket): particles bit-identical, cumcnt
+    bit-identical inside the window, fields within 1e-12 at equal CG counts."""
+    p, st, o = shock_setup(92)
+    g = make_gpu(p, "fp64_exact", gpu_lib)
+    g.put_state(st)
+    g.step(1)
+    o.cg_control(fixed=g.cg_iters())
+    ref = st.copy()
+    assert o.step(ref) == 0
+    out = g.get_state()
+    assert_particles(out.up, out.np2, ref.up, ref.np2)
+    assert_window_cumcnt(out.cumcnt, ref.cumcnt, p.window)
+    assert_field(out.uf, ref.uf, REL)
+
+
+@pytest.mark.parametrize("precision,rel", [("fp64_exact", 1e-10), ("fp64", 1e-10)])
+def test_shock_steps_with_expanding_window(gpu_lib, precision, rel):
+    """Four steps, the window widened by one (empty) cell as relocate() does, three more
+    steps.  relocate() keeps cumcnt of the new cell consistent (2d/proj/shock/app.f90:669);
+    the oracle's copy is updated the same way, the library keeps it itself."""
+    p, st, o = shock_setup(93)
+    g = make_gpu(p, precision, gpu_lib)
+    g.put_state(st)
+    ref = st.copy()
+    for k in range(7):
+        if k == 4:
+            g.set_window(p.nxgs, p.nxe + 1)
+            o.set_window(p.nxgs, p.nxe + 1)
+            ref.cumcnt[p.window + 1, :, :] = ref.cumcnt[p.window, :, :]
+        g.step(1)
+        o.cg_control(fixed=g.cg_iters())
+        assert o.step(ref) == 0
+    out = g.get_state()
+    np.testing.assert_array_equal(out.np2, ref.np2)
+    assert_window_cumcnt(out.cumcnt, ref.cumcnt, p.window + 1)
+    assert_particles(out.up, out.np2, ref.up, ref.np2, rel=rel)
+    assert_field(out.uf, ref.uf, rel)
+
+
+def test_shock_rejected_where_unsupported(gpu_lib):
+    from wumingpic_gb300._lib import WpicError
+    p, st, o = shock_setup(94, nx=32, ny=16)
+    with pytest.raises(WpicError):
+        make_gpu(p, "mixed", gpu_lib)
+    q, _ = small_case(nx=16, ny=12)
+    g = make_gpu(q, "fp64", gpu_lib)
+    with pytest.raises(WpicError):
+        g.set_window(q.nxgs, q.nxge - 2)  # periodic: the window is the whole domain
+    with pytest.raises(WpicError):
+        g.bc__injection(0.1)

@@ -314,3 +314,55 @@ def test_mom_calc_accl_is_a_half_step_in_pure_e():
                 np.testing.assert_allclose(st.gp[2 + k, :n, jj, isp],
                                            st.up[2 + k, :n, jj, isp] + q[isp] / r[isp] * 0.5 * p.delt * e[k],
                                            rtol=1e-13, atol=1e-16)
+
+
+def shock_oracle(p, window_cells):
+    o = make_oracle(p)
+    o.set_window(p.nxgs, p.nxgs + window_cells - 1)
+    o.u0 = p.u0
+    return o
+
+
+def test_shock_injection_reflects_at_both_ends():
+    """boundary_shock__injection: x below the wall (nxs+1) dx is mirrored with u reversed;
+    x beyond xend = nxe dx + v0 dt is mirrored about xend with u_x -> 2 u0 - u_x."""
+    p, st = small_case(nx=24, ny=8, ppc=4, seed=81, bc="shock", window=16, u0=0.3)
+    o = shock_oracle(p, 16)
+    nxs, nxe = p.nxgs, p.nxgs + 15
+    xend = nxe * p.delx + p.u0 / math.sqrt(1 + p.u0 ** 2 / p.c ** 2) * p.delt
+    gp = st.up.copy(order="F")
+    n = st.np2[0, 1]
+    gp[0, 0, 0, 1] = (nxs + 1) * p.delx - 0.25          # behind the wall
+    gp[0, 1, 0, 1] = xend + 0.1                          # beyond the injection boundary
+    u_before = gp[2:5, :n, 0, 1].copy()
+    assert o.bc_injection(gp, st.np2) == 0
+    assert gp[0, 0, 0, 1] == (nxs + 1) * p.delx + 0.25
+    np.testing.assert_array_equal(gp[2:5, 0, 0, 1], -u_before[:, 0])
+    np.testing.assert_allclose(gp[0, 1, 0, 1], xend - 0.1, rtol=0, atol=1e-12)
+    assert gp[2, 1, 0, 1] == 2 * p.u0 - u_before[0, 1]
+    np.testing.assert_array_equal(gp[3:5, 1, 0, 1], -u_before[1:, 1])
+    np.testing.assert_array_equal(gp[:, 2:n, 0, 1], st.up[:, 2:n, 0, 1])
+
+
+def test_shock_steps_stay_in_the_window():
+    """Five steps of the shock boundary in a 16-cell window of a 24-cell domain: particles stay
+    between the wall and the injection boundary, the count is conserved, the fields outside
+    the window (and its two ghost columns) are untouched, and the CG converges."""
+    p, st = small_case(nx=24, ny=8, ppc=4, seed=82, bc="shock", window=16, u0=0.3, u_the=0.1)
+    o = shock_oracle(p, 16)
+    uf0 = st.uf.copy()
+    n_before = st.np2.sum()
+    nxe = p.nxgs + 15
+    for _ in range(5):
+        assert o.step(st) == 0
+    assert st.np2.sum() == n_before
+    xend = nxe * p.delx + p.u0 / math.sqrt(1 + p.u0 ** 2 / p.c ** 2) * p.delt
+    for isp in range(p.nsp):
+        for j in range(p.ny):
+            x = st.up[0, :st.np2[j, isp], j, isp]
+            assert np.all(x >= (p.nxgs + 1) * p.delx) and np.all(x <= xend)
+    # field columns beyond nxe+2 (array index nxe+2 - (nxgs-2) + 1 ...) are never written
+    first_untouched = nxe + 3 - (p.nxgs - 2)
+    np.testing.assert_array_equal(st.uf[:, first_untouched:, :], uf0[:, first_untouched:, :])
+    assert np.abs(st.uf[:, :first_untouched, :]).max() > 0
+    assert all(0 < k < 100 for k in o.cg_iters())

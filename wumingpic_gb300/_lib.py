@@ -24,6 +24,7 @@ NOT_INITIALISED = 8
 
 BC_PERIODIC = 0
 BC_RECONNECTION = 1
+BC_SHOCK = 2
 FP64 = 0
 FP64_EXACT = 1
 MIXED = 2
@@ -79,6 +80,9 @@ def lib():
         for n in ("wpic_put_fields", "wpic_get_fields", "wpic_put_df", "wpic_get_df", "wpic_get_uj"):
             getattr(L, n).argtypes = [vp, vp]
         L.wpic_set_pusher.argtypes = [vp, i]
+        L.wpic_set_window.argtypes = [vp, i, i]
+        L.wpic_set_injection.argtypes = [vp, ctypes.c_double]
+        L.wpic_bc_injection.argtypes = [vp, ctypes.c_double]
         L.wpic3d_set_pusher.argtypes = [vp, i]
         for pre in ("wpic", "wpic3d"):
             getattr(L, pre + "_mom_calc_accl").argtypes = [vp]

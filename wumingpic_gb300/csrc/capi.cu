@@ -59,6 +59,7 @@ struct wpic_ctx {
   double mix_vmax = 0.0;  // largest contribution of one particle to one node of the deposit
   int pusher = WPIC_PUSH_BORIS;  // the push of the fused step
   double* mom = nullptr;         // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp), allocated on first use
+  double u0 = 0.0;               // shock: upstream four-velocity of the injection boundary
 };
 
 namespace {
@@ -384,9 +385,26 @@ int mixed_step(wpic_ctx* c) {
   return WPIC_OK;
 }
 
+// boundary_shock__injection's right end: xend = nxe dx + v0 dt in the reference's FP64
+// expression (2d/proj/shock/boundary_shock.f90:272)
+double shock_xend(const wpic_ctx* c, double u0) {
+  const double delx = c->d.ph.delx, cl = c->d.ph.c, delt = c->d.ph.delt;
+  const int nxe = c->d.g.nxgs + c->d.g.wx1;
+  return nxe * delx + u0 / std::sqrt(1 + (u0 * u0) / (cl * cl)) * delt;
+}
+
+void do_injection(wpic_ctx* c, double u0) {
+  stage_begin(c, SG_PBC);
+  injection2d(c->d, c->d.B, u0, shock_xend(c, u0), c->stream);
+  stage_end(c, SG_PBC, 1);
+}
+
 int one_step(wpic_ctx* c) {
   if (c->mixed) return mixed_step(c);
   do_push(c);
+  // the shock driver's order (2d/proj/shock/app.f90:110-115): injection before the field
+  // solve and no particle_x; the reconnection driver's: particle_x before the field solve
+  if (c->d.ph.bc == BC_SHOCK) do_injection(c, c->u0);
   if (c->d.ph.bc == BC_RECONNECTION) do_particle_x(c);
   int st = do_field(c);
   if (st) return st;
@@ -406,7 +424,9 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
   if (p->ndim != 6 || p->nsp < 1 || p->nsp > 2 || nx < 4 || ny < 4 || p->np < 1) return WPIC_BAD_ARGUMENT;
   if (p->nys != p->nygs || p->nye != p->nyge) return WPIC_BAD_ARGUMENT;  // one device holds the whole domain
   if (!(p->delx > 0) || !(p->delt > 0) || !(p->c > 0)) return WPIC_BAD_ARGUMENT;
-  if (p->bc_kind != WPIC_BC_PERIODIC && p->bc_kind != WPIC_BC_RECONNECTION) return WPIC_BAD_ARGUMENT;
+  if (p->bc_kind != WPIC_BC_PERIODIC && p->bc_kind != WPIC_BC_RECONNECTION && p->bc_kind != WPIC_BC_SHOCK)
+    return WPIC_BAD_ARGUMENT;
+  if (p->bc_kind == WPIC_BC_SHOCK && p->precision == WPIC_MIXED) return WPIC_BAD_ARGUMENT;
   if (p->precision != WPIC_FP64 && p->precision != WPIC_FP64_EXACT && p->precision != WPIC_MIXED)
     return WPIC_BAD_ARGUMENT;
   if (p->precision == WPIC_MIXED && (nx % MIX_TS != 0 || ny % MIX_TS != 0)) return WPIC_BAD_ARGUMENT;
@@ -421,6 +441,8 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
   d.g.fp = nx + 4;
   d.g.fplane = (nx + 4) * (ny + 4);
   d.g.ncell = nx * ny;
+  d.g.wx0 = 0;
+  d.g.wx1 = nx - 1;
   Phys& ph = d.ph;
   ph.delx = p->delx;
   ph.delt = p->delt;
@@ -791,6 +813,31 @@ int wpic_set_pusher(wpic_ctx* c, int pusher) {
   if (c->mixed && pusher != WPIC_PUSH_BORIS) return WPIC_BAD_ARGUMENT;
   c->pusher = pusher;
   return WPIC_OK;
+}
+
+int wpic_set_window(wpic_ctx* c, int nxs, int nxe) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  const int nxge = c->d.g.nxgs + c->d.g.nx - 1;
+  if (nxs < c->d.g.nxgs || nxe > nxge || nxe - nxs < 3) return WPIC_BAD_ARGUMENT;
+  const bool full = nxs == c->d.g.nxgs && nxe == nxge;
+  if (!full && (c->mixed || c->d.ph.bc == BC_PERIODIC)) return WPIC_BAD_ARGUMENT;
+  c->d.g.wx0 = nxs - c->d.g.nxgs;
+  c->d.g.wx1 = nxe - c->d.g.nxgs;
+  return WPIC_OK;
+}
+
+int wpic_set_injection(wpic_ctx* c, double u0) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!(u0 == u0)) return WPIC_BAD_ARGUMENT;
+  c->u0 = u0;
+  return WPIC_OK;
+}
+
+int wpic_bc_injection(wpic_ctx* c, double u0) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed || c->d.ph.bc != BC_SHOCK) return WPIC_BAD_ARGUMENT;
+  do_injection(c, u0);
+  return finish(c);
 }
 
 int wpic_field_fdtd_i(wpic_ctx* c) {

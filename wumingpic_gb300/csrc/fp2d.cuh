@@ -383,7 +383,7 @@ void deposit2d(const Dev2D& d, cudaStream_t s) {
 __global__ void k_gkl2d(Dev2D d) {
   const Grid2D g = d.g;
   const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
-  if (cx >= g.nx) return;
+  if (cx < g.wx0 || cx > g.wx1) return;  // the active window nxs..nxe
   const size_t f = (size_t)(cy + 2) * g.fp + (cx + 2);
   const size_t P = g.fplane;
   const double* uf = d.uf;
@@ -422,21 +422,31 @@ void gkl2d(const Dev2D& d, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 constexpr int CG_THREADS = 256;
 
-// phi(cx, cy) of component l with the boundary_*__phi ghost rules applied by
-// index arithmetic (periodic y; periodic or conducting-wall x).
+// The boundary_*__phi ghost rules as index arithmetic on the window nxs..nxe (cells wx0..wx1):
+// periodic y; x periodic, conducting walls (boundary_reconnection__phi,
+// 2d/proj/reconnection/boundary_reconnection.f90:505-579) or the shock's wall and zero
+// right end (boundary_shock__phi, 2d/proj/shock/boundary_shock.f90:551-625).  Returns the
+// source cell of (cx, cy) with the sign flag, or cx = -1 where the ghost value is zero.
 // The sign flip is an integer flag so that no FP64 compare is issued.
-__device__ __forceinline__ double phi_at(const double* v, const Grid2D& g, int bc, int l, int cx, int cy) {
+__device__ __forceinline__ void phi_src(const Grid2D& g, int bc, int l, int& cx, int& cy, bool& neg) {
   if (cy < 0) cy += g.ny; else if (cy >= g.ny) cy -= g.ny;
-  bool neg = false;
-  if (cx < 0) {
+  neg = false;
+  if (cx < g.wx0) {
     if (bc == BC_PERIODIC) cx += g.nx;
-    else if (l == 0) { cx = 0; neg = true; }
-    else cx = 1;
-  } else if (cx >= g.nx) {
+    else if (l == 0) { cx = g.wx0; neg = true; }
+    else cx = g.wx0 + 1;
+  } else if (cx > g.wx1) {
     if (bc == BC_PERIODIC) cx -= g.nx;
-    else if (l == 0) { cx = g.nx - 3; neg = true; }
-    else cx = g.nx - 2;
+    else if (bc == BC_SHOCK) cx = -1;
+    else if (l == 0) { cx = g.wx1 - 2; neg = true; }
+    else cx = g.wx1 - 1;
   }
+}
+
+__device__ __forceinline__ double phi_at(const double* v, const Grid2D& g, int bc, int l, int cx, int cy) {
+  bool neg;
+  phi_src(g, bc, l, cx, cy, neg);
+  if (cx < 0) return 0.0;
   const double val = v[(size_t)cy * g.nx + cx];
   return neg ? -val : val;
 }
@@ -463,16 +473,13 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_init(Dev2D d) {
   double sb = 0.0, sr = 0.0;
   for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS) {
     const int cy = c / g.nx, cx = c - cy * g.nx;
+    if (cx < g.wx0 || cx > g.wx1) continue;  // outside the window: not part of the system
     // db interior viewed as a [ny][nx] array with pitch fp
     const double* db = d.df + (size_t)l * g.fplane + 2 * (size_t)g.fp + 2;
     auto ph = [&](int x, int y) {
-      if (y < 0) y += g.ny; else if (y >= g.ny) y -= g.ny;
-      bool neg = false;
-      if (x < 0) {
-        if (d.ph.bc == BC_PERIODIC) x += g.nx; else if (l == 0) { x = 0; neg = true; } else x = 1;
-      } else if (x >= g.nx) {
-        if (d.ph.bc == BC_PERIODIC) x -= g.nx; else if (l == 0) { x = g.nx - 3; neg = true; } else x = g.nx - 2;
-      }
+      bool neg;
+      phi_src(g, d.ph.bc, l, x, y, neg);
+      if (x < 0) return 0.0;
       const double v = db[(size_t)y * g.fp + x];
       return neg ? -v : v;
     };
@@ -537,6 +544,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_ap(Dev2D d) {
   double s2 = 0.0;
   for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS) {
     const int cy = c / g.nx, cx = c - cy * g.nx;
+    if (cx < g.wx0 || cx > g.wx1) continue;
     const double pc = p[c];
     const double ap = -phi_at(p, g, bc, l, cx, cy - 1) - phi_at(p, g, bc, l, cx - 1, cy) + f4 * pc
                       - phi_at(p, g, bc, l, cx + 1, cy) - phi_at(p, g, bc, l, cx, cy + 1);
@@ -573,6 +581,8 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_update(Dev2D d) {
   const double av = d.cg[l].av;
   double s1 = 0.0;
   for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS) {
+    const int cx = c % g.nx;
+    if (cx < g.wx0 || cx > g.wx1) continue;
     d.phi[off + c] = d.phi[off + c] + av * d.p[off + c];
     const double r = d.r[off + c] - av * d.ap[off + c];
     d.r[off + c] = r;
@@ -616,8 +626,11 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_p(Dev2D d) {
   if (act != 1) return;
   const size_t off = (size_t)l * g.ncell;
   const double bv = d.cg[l].bv;
-  for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS)
+  for (int c = blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += gridDim.x * CG_THREADS) {
+    const int cx = c % g.nx;
+    if (cx < g.wx0 || cx > g.wx1) continue;
     d.p[off + c] = d.r[off + c] + bv * d.p[off + c];
+  }
 }
 
 __global__ void k_cg_settle(Dev2D d) {
@@ -647,6 +660,7 @@ __global__ void k_cg_store(Dev2D d) {
   const int l = blockIdx.y;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < g.ncell; c += gridDim.x * blockDim.x) {
     const int cy = c / g.nx, cx = c - cy * g.nx;
+    if (cx < g.wx0 || cx > g.wx1) continue;
     d.df[(size_t)l * g.fplane + (size_t)(cy + 2) * g.fp + cx + 2] = d.phi[(size_t)l * g.ncell + c];
   }
 }
@@ -658,7 +672,7 @@ void cg_store2d(const Dev2D& d, cudaStream_t s) { k_cg_store<<<dim3(d.nred, 3), 
 __global__ void k_efield2d(Dev2D d) {
   const Grid2D g = d.g;
   const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y;
-  if (cx >= g.nx) return;
+  if (cx < g.wx0 || cx > g.wx1) return;
   const size_t f = (size_t)(cy + 2) * g.fp + (cx + 2);
   const size_t P = g.fplane;
   const size_t E = f + 1, N = f + g.fp;

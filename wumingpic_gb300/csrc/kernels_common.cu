@@ -70,7 +70,7 @@ __global__ void k_mom_fold_x(Dev2D d, double* mom) {
   if (t >= 7 * nym * d.ph.nsp) return;
   const int l = t % 7, r = t / 7;  // r = jn + nym * isp
   double* m = mom + (size_t)r * nxm * 7 + l;
-  if (d.ph.bc == BC_RECONNECTION) {
+  if (d.ph.bc != BC_PERIODIC) {  // walls: reconnection and shock
     m[7 * 1] = m[7 * 1] + m[0];
     m[7 * (size_t)g.nx] = m[7 * (size_t)g.nx] + m[7 * (size_t)(g.nx + 1)];
   } else {
@@ -129,13 +129,19 @@ __global__ void k_dfield_x(Dev2D d) {
     for (int k = 0; k < 6; ++k) u[k][nx + 2] = u[k][2];
     for (int k = 0; k < 6; ++k) u[k][nx + 3] = u[k][3];
   } else {
-    // nxs-1 -> 1, nxs -> 2, nxs+1 -> 3, nxe-1 -> nx, nxe -> nx+1, nxe+1 -> nx+2
-    u[0][1] = -u[0][2];
-    for (int k = 1; k <= 3; ++k) u[k][1] = u[k][3];
-    for (int k = 4; k <= 5; ++k) u[k][1] = -u[k][2];
-    u[0][nx + 1] = -u[0][nx];
-    for (int k = 1; k <= 3; ++k) u[k][nx + 2] = u[k][nx];
-    for (int k = 4; k <= 5; ++k) u[k][nx + 1] = -u[k][nx];
+    // window nxs..nxe = cells wx0..wx1: nxs-1 -> a, nxs -> a+1, nxs+1 -> a+2 (a = wx0 + 1);
+    // nxe-1 -> e-1, nxe -> e, nxe+1 -> e+1 (e = wx1 + 2)
+    const int a = g.wx0 + 1, e = g.wx1 + 2;
+    u[0][a] = -u[0][a + 1];
+    for (int k = 1; k <= 3; ++k) u[k][a] = u[k][a + 2];
+    for (int k = 4; k <= 5; ++k) u[k][a] = -u[k][a + 1];
+    if (d.ph.bc == BC_SHOCK) {  // boundary_shock__dfield (2d/proj/shock/boundary_shock.f90:397-405)
+      for (int k = 0; k < 6; ++k) u[k][e + 1] = 0.0;
+    } else {
+      u[0][e] = -u[0][e - 1];
+      for (int k = 1; k <= 3; ++k) u[k][e + 1] = u[k][e - 1];
+      for (int k = 4; k <= 5; ++k) u[k][e] = -u[k][e - 1];
+    }
   }
 }
 
@@ -175,14 +181,14 @@ __global__ void k_particle_x(Dev2D d, Parts64 P) {
     else if (ipos >= nxge + 1) x = __dsub_rd(x, L);
     P.x[k] = x;
   } else {
-    const int nxs = g.nxgs, nxe = nxge;
+    const int nxs = g.nxgs + g.wx0, nxe = g.nxgs + g.wx1;  // the window; walls at nxs+1, nxe-1
     const int ipos = (int)(x / delx);
     bool flip = false;
     if (ipos < nxs + 1) {
-      x = (double)(2.0f * (float)(nxs + 1)) * delx - x;
+      x = __dsub_rn(__dmul_rn((double)(2.0f * (float)(nxs + 1)), delx), x);
       flip = true;
     } else if (ipos >= nxe - 1) {
-      x = (double)(2.0f * (float)(nxe - 1)) * delx - x;
+      x = __dsub_rn(__dmul_rn((double)(2.0f * (float)(nxe - 1)), delx), x);
       flip = true;
     }
     if (flip) {
@@ -197,6 +203,38 @@ __global__ void k_particle_x(Dev2D d, Parts64 P) {
 void particle_x2d(const Dev2D& d, const Parts64& P, cudaStream_t s) {
   dim3 grid((d.cap + 255) / 256, d.nrowjob);
   k_particle_x<<<grid, 256, 0, s>>>(d, P);
+}
+
+// boundary_shock__injection (2d/proj/shock/boundary_shock.f90:255-297): reflection at the
+// wall x = (nxs+1) dx with all momentum components reversed, and at the injection boundary
+// xend = nxe dx + v0 dt (computed on the host, as the reference does, in FP64) with
+// u_x -> 2 u0 - u_x; default rounding.
+__global__ void k_injection(Dev2D d, Parts64 P, double u0, double xend) {
+  const int row = blockIdx.y;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.np2[row]) return;
+  const size_t k = (size_t)row * d.cap + s;
+  const double delx = d.ph.delx;
+  const int nxs = d.g.nxgs + d.g.wx0;
+  const double x = P.x[k];
+  const int ipos = (int)(x / delx);
+  // products and differences rounded separately, as the reference evaluates them (no FMA)
+  if (ipos < nxs + 1) {
+    P.x[k] = __dsub_rn(__dmul_rn((double)(2.0f * (float)(nxs + 1)), delx), x);
+    P.ux[k] = -P.ux[k];
+    P.uy[k] = -P.uy[k];
+    P.uz[k] = -P.uz[k];
+  } else if (x > xend) {
+    P.x[k] = __dsub_rn(__dmul_rn(2., xend), x);
+    P.ux[k] = __dsub_rn(__dmul_rn(2., u0), P.ux[k]);
+    P.uy[k] = -P.uy[k];
+    P.uz[k] = -P.uz[k];
+  }
+}
+
+void injection2d(const Dev2D& d, const Parts64& P, double u0, double xend, cudaStream_t s) {
+  dim3 grid((d.cap + 255) / 256, d.nrowjob);
+  k_injection<<<grid, 256, 0, s>>>(d, P, u0, xend);
 }
 
 // ---------------------------------------------------------------------------

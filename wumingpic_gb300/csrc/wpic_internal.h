@@ -34,7 +34,7 @@ enum ErrBit : int {
   EB_CG = 8,
 };
 
-enum Bc : int { BC_PERIODIC = 0, BC_RECONNECTION = 1 };
+enum Bc : int { BC_PERIODIC = 0, BC_RECONNECTION = 1, BC_SHOCK = 2 };
 
 // modes of the particle push kernels: particle__solv, particle__solv_vay, mom_calc__accl
 enum PushMode : int { PUSH_BORIS = 0, PUSH_VAY = 1, PUSH_MOM = 2 };
@@ -45,6 +45,7 @@ struct Grid2D {
   int fp;           // field row pitch = nx + 4
   int fplane;       // (nx + 4) * (ny + 4)
   int ncell;        // nx * ny
+  int wx0, wx1;     // active x window nxs..nxe as interior cell indices (all cells unless set)
 };
 
 struct Phys {
@@ -165,6 +166,7 @@ void mix_moments2d(const Dev2D& d, double* mom, cudaStream_t s);
 void dfield_ghost2d(const Dev2D& d, cudaStream_t s);
 void uf_add2d(const Dev2D& d, cudaStream_t s);
 void particle_x2d(const Dev2D& d, const Parts64& P, cudaStream_t s);
+void injection2d(const Dev2D& d, const Parts64& P, double u0, double xend, cudaStream_t s);
 void migrate_scan2d(const Dev2D& d, const Parts64& P, cudaStream_t s);
 void migrate_plan2d(const Dev2D& d, cudaStream_t s);
 void sort_rank2d(const Dev2D& d, const Parts64& P, const int* slist, cudaStream_t s);

@@ -55,10 +55,17 @@ class Plasma2D:
     seed: int = 12345
     nxgs: int = 2
     nygs: int = 2
+    window: int = 0               # shock: cells of the active window nxs..nxe from nxgs (0 = all)
+    u0: float = 0.0               # shock: upstream four-velocity along x (the flow is -u0)
 
     @property
     def nxge(self):
         return self.nxgs + self.nx - 1
+
+    @property
+    def nxe(self):
+        """right end of the active window (the shock driver's nxe)"""
+        return self.nxgs + (self.window or self.nx) - 1
 
     @property
     def nyge(self):
@@ -113,7 +120,9 @@ def load_weibel2d(p: Plasma2D) -> State2D:
     nx, ny, n0 = p.nx, p.ny, p.ppc
     # cells that hold particles: all of them, or with conducting walls in x the
     # cells between the walls, [nxs+1, nxe-1) (2d/proj/reconnection/app.f90:418)
-    c_lo, c_hi = (0, nx) if p.bc == "periodic" else (1, nx - 2)
+    # (the shock driver's upstream plasma fills its window likewise, drifting at -u0 along x)
+    nw = p.window or nx
+    c_lo, c_hi = (0, nx) if p.bc == "periodic" else (1, nw - 2)
     npr = (c_hi - c_lo) * n0  # particles per row per species
     # positions: cell-major inside each row, uniform in the cell
     ix = np.repeat(np.arange(c_lo, c_hi), n0)                # (npr,)
@@ -131,6 +140,8 @@ def load_weibel2d(p: Plasma2D) -> State2D:
         if isp == 1 and p.drift != 0.0:
             sign = np.where(np.arange(npr) % 2 == 0, 1.0, -1.0)
             u[p.drift_axis] += p.drift * sign[:, None]
+        if p.u0 != 0.0:
+            u[0] -= p.u0
         st.up[2:5, :npr, :, isp] = u
     # ids: -pid bit-cast to real(8), pid = running index per species over rows
     for isp in range(p.nsp):

@@ -32,13 +32,17 @@ class Pic2D:
         prm.delx, prm.delt, prm.c, prm.gfac = plasma.delx, plasma.delt, plasma.c, plasma.gfac
         prm.q[0], prm.q[1] = q[0], q[1]
         prm.r[0], prm.r[1] = r[0], r[1]
-        prm.bc_kind = _lib.BC_PERIODIC if plasma.bc == "periodic" else _lib.BC_RECONNECTION
+        prm.bc_kind = {"periodic": _lib.BC_PERIODIC, "reconnection": _lib.BC_RECONNECTION,
+                       "shock": _lib.BC_SHOCK}[plasma.bc]
         prm.precision = {"fp64": _lib.FP64, "fp64_exact": _lib.FP64_EXACT, "mixed": _lib.MIXED}[precision]
         prm.device_cap = int(device_cap)
         self.precision = precision
         h = ctypes.c_void_p()
         check(lib().wpic_init_2d(ctypes.byref(h), ctypes.byref(prm), ctypes.c_void_p(stream or 0)), "wpic_init_2d")
         self._h = h
+        if plasma.bc == "shock":
+            self.set_window(plasma.nxgs, plasma.nxe)
+            self.set_injection(plasma.u0)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -107,6 +111,16 @@ class Pic2D:
     # ---- the module procedures ----
     def particle__solv(self):
         check(lib().wpic_particle_solv(self._h), "particle__solv")
+
+    def set_window(self, nxs, nxe):
+        """the active x window nxs..nxe (the shock driver's expanding box)"""
+        check(lib().wpic_set_window(self._h, int(nxs), int(nxe)), "set_window")
+
+    def set_injection(self, u0):
+        check(lib().wpic_set_injection(self._h, float(u0)), "set_injection")
+
+    def bc__injection(self, u0):
+        check(lib().wpic_bc_injection(self._h, float(u0)), "bc__injection")
 
     def particle__solv_vay(self):
         check(lib().wpic_particle_solv_vay(self._h), "particle__solv_vay")
