@@ -1,5 +1,6 @@
 ! wpic_shim2d.f90 -- drop-in replacements for WumingPIC's 2D hot-path modules
-! (particle, field, sort, boundary_periodic, mom_calc) that forward to the GB300 library
+! (particle, field, sort, boundary_periodic, boundary_reconnection, boundary_shock, mom_calc)
+! that forward to the GB300 library
 ! through ISO_C_BINDING.  Link these objects instead of the corresponding objects
 ! of libwuming2d_common.a; the drivers ({2d}/proj/*/app.f90) stay unchanged.
 !
@@ -65,6 +66,16 @@ module wpic_capi
        type(c_ptr), value :: ctx
        real(c_double), intent(inout) :: mom(*)
      end function wpic_get_mom
+     integer(c_int) function wpic_set_window(ctx, nxs, nxe) bind(C, name="wpic_set_window")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: nxs, nxe
+     end function wpic_set_window
+     integer(c_int) function wpic_bc_injection(ctx, u0) bind(C, name="wpic_bc_injection")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: u0
+     end function wpic_bc_injection
      integer(c_int) function wpic_mom_calc_accl(ctx) bind(C, name="wpic_mom_calc_accl")
        import :: c_int, c_ptr
        type(c_ptr), value :: ctx
@@ -83,6 +94,9 @@ module wpic_capi
   type(c_ptr), save :: wpic_ctx = c_null_ptr
   type(wpic_params), save :: wpic_prm
   logical, save :: wpic_uploaded = .false.
+  logical, save :: wpic_bc_set = .false.           ! a boundary module's __init chose the kind
+  logical, save :: wpic_upload_each_step = .false. ! drivers that edit up/uf/cumcnt between steps
+  integer, save :: wpic_win_s = -1, wpic_win_e = -1
   integer, save :: wpic_sync_every = 1, wpic_step_count = 0
 
   procedure(wpic_call), pointer :: p_solv => null(), p_fdtd => null(), p_bcx => null(), &
@@ -98,6 +112,42 @@ contains
        stop
     endif
   end subroutine wpic_check
+
+  ! The shock driver adds particles and sets upstream fields on the host between steps
+  ! (inject, relocate: 2d/proj/shock/app.f90:615-852); with upload on, every particle__solv
+  ! sends the host state to the device first.
+  subroutine wpic_shim_set_upload(flag)
+    logical, intent(in) :: flag
+    wpic_upload_each_step = flag
+  end subroutine wpic_shim_set_upload
+
+  ! the active window nxs..nxe that the driver passes to every module call
+  subroutine wpic_apply_window(nxs, nxe)
+    integer, intent(in) :: nxs, nxe
+    if (nxs /= wpic_win_s .or. nxe /= wpic_win_e) then
+       call wpic_check(wpic_set_window(wpic_ctx, int(nxs, c_int), int(nxe, c_int)), 'window')
+       wpic_win_s = nxs; wpic_win_e = nxe
+    endif
+  end subroutine wpic_apply_window
+
+  ! up, uf and cumcnt to the device; cumcnt beyond the window (stale in the drivers) is
+  ! completed with the row totals, which is what the library keeps there
+  subroutine wpic_upload_state(up, uf, cumcnt, nxe)
+    real(8), intent(in) :: up(*), uf(*)
+    integer, intent(in) :: cumcnt(wpic_prm%nxgs:wpic_prm%nxge+1,wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    integer, intent(in) :: nxe
+    integer(c_int) :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    integer(c_int) :: cc(wpic_prm%nxgs:wpic_prm%nxge+1,wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    integer :: i
+    cc(:,:,:) = cumcnt(:,:,:)
+    do i = nxe+2, wpic_prm%nxge+1
+       cc(i,:,:) = cumcnt(nxe+1,:,:)
+    enddo
+    np2(:,:) = cumcnt(nxe+1,:,:)
+    call wpic_check(wpic_put_particles(wpic_ctx, 0_c_int, up, np2, cc), 'put up')
+    call wpic_check(wpic_put_fields(wpic_ctx, uf), 'put uf')
+    wpic_uploaded = .true.
+  end subroutine wpic_upload_state
 
   subroutine wpic_shim_set_sync(n)
     integer, intent(in) :: n
@@ -164,7 +214,8 @@ contains
     wpic_prm%nys = nys_in; wpic_prm%nye = nye_in
     wpic_prm%delx = delx_in; wpic_prm%delt = delt_in; wpic_prm%c = c_in
     wpic_prm%q(1:nsp_in) = q_in; wpic_prm%r(1:nsp_in) = r_in
-    wpic_prm%bc_kind = 0; wpic_prm%precision = 0; wpic_prm%device_cap = 0
+    if (.not. wpic_bc_set) wpic_prm%bc_kind = 0
+    wpic_prm%precision = 0; wpic_prm%device_cap = 0
   end subroutine particle__init
 
   subroutine particle__solv(gp,up,uf,cumcnt,nxs,nxe)
@@ -172,14 +223,9 @@ contains
     integer, intent(in)  :: cumcnt(wpic_prm%nxgs:wpic_prm%nxge+1,wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
     real(8), intent(in)  :: up(*), uf(*)
     real(8), intent(out) :: gp(*)
-    integer(c_int) :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
     call wpic_ensure_ctx()
-    if (.not. wpic_uploaded) then
-       np2(:,:) = cumcnt(nxe+1,:,:)
-       call wpic_check(wpic_put_particles(wpic_ctx, 0_c_int, up, np2, cumcnt), 'put up')
-       call wpic_check(wpic_put_fields(wpic_ctx, uf), 'put uf')
-       wpic_uploaded = .true.
-    endif
+    call wpic_apply_window(nxs, nxe)
+    if (.not. wpic_uploaded .or. wpic_upload_each_step) call wpic_upload_state(up, uf, cumcnt, nxe)
     call wpic_check(p_solv(wpic_ctx), 'particle__solv')
   end subroutine particle__solv
 
@@ -188,14 +234,9 @@ contains
     integer, intent(in)  :: cumcnt(wpic_prm%nxgs:wpic_prm%nxge+1,wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
     real(8), intent(in)  :: up(*), uf(*)
     real(8), intent(out) :: gp(*)
-    integer(c_int) :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
     call wpic_ensure_ctx()
-    if (.not. wpic_uploaded) then
-       np2(:,:) = cumcnt(nxe+1,:,:)
-       call wpic_check(wpic_put_particles(wpic_ctx, 0_c_int, up, np2, cumcnt), 'put up')
-       call wpic_check(wpic_put_fields(wpic_ctx, uf), 'put uf')
-       wpic_uploaded = .true.
-    endif
+    call wpic_apply_window(nxs, nxe)
+    if (.not. wpic_uploaded .or. wpic_upload_each_step) call wpic_upload_state(up, uf, cumcnt, nxe)
     call wpic_check(p_solv_vay(wpic_ctx), 'particle__solv_vay')
   end subroutine particle__solv_vay
 end module particle
@@ -221,6 +262,7 @@ contains
     real(8), intent(in)    :: up(*), gp(*)
     real(8), intent(inout) :: uf(*)
     external :: set_boundary_dfield, set_boundary_curre, set_boundary_phi
+    call wpic_apply_window(nxs, nxe)
     call wpic_check(p_fdtd(wpic_ctx), 'field__fdtd_i')
     if (mod(wpic_step_count + 1, wpic_sync_every) == 0) then
        call wpic_check(wpic_get_fields(wpic_ctx, uf), 'get uf')
@@ -248,6 +290,7 @@ contains
     real(8), intent(in)    :: up(*)
     real(8), intent(out)   :: gp(*)
     integer(c_int) :: np2_dev(wpic_prm%nye-wpic_prm%nys+1, wpic_prm%nsp)
+    call wpic_apply_window(nxs, nxe)
     call wpic_check(p_sort(wpic_ctx), 'sort__bucket')
     wpic_step_count = wpic_step_count + 1
     if (mod(wpic_step_count, wpic_sync_every) == 0) then
@@ -341,3 +384,121 @@ contains
     call wpic_check(wpic_get_mom(wpic_ctx, mom), 'get mom')
   end subroutine mom_calc__nvt
 end module mom_calc
+
+
+! boundary_reconnection (2d/proj/reconnection/boundary_reconnection.f90): conducting walls in x
+module boundary_reconnection
+  use wpic_capi
+  implicit none
+  private
+  public :: boundary_reconnection__init, boundary_reconnection__dfield, boundary_reconnection__particle_x, &
+       boundary_reconnection__particle_y, boundary_reconnection__curre, boundary_reconnection__phi, &
+       boundary_reconnection__mom
+contains
+  subroutine boundary_reconnection__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nys_in,nye_in, &
+                                         nup_in,ndown_in,mnpi_in,mnpr_in,ncomw_in,nerr_in,nstat_in,delx_in,delt_in,c_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in, nxgs_in, nxge_in, nygs_in, nyge_in, nys_in, nye_in
+    integer, intent(in) :: nup_in, ndown_in, mnpi_in, mnpr_in, ncomw_in, nerr_in, nstat_in(:)
+    real(8), intent(in) :: delx_in, delt_in, c_in
+    wpic_prm%bc_kind = 1; wpic_bc_set = .true.
+  end subroutine boundary_reconnection__init
+
+  subroutine boundary_reconnection__particle_x(up,np2,nxs,nxe)
+    integer, intent(in)    :: nxs, nxe
+    real(8), intent(inout) :: up(*)
+    integer, intent(in)    :: np2(*)
+    call wpic_apply_window(nxs, nxe)
+    call wpic_check(p_bcx(wpic_ctx), 'bc__particle_x')
+  end subroutine boundary_reconnection__particle_x
+
+  subroutine boundary_reconnection__particle_y(up,np2)
+    real(8), intent(inout) :: up(*)
+    integer, intent(inout) :: np2(*)
+    call wpic_check(p_bcy(wpic_ctx), 'bc__particle_y')
+  end subroutine boundary_reconnection__particle_y
+
+  ! applied inside the library; present so that field__fdtd_i's arguments type-check
+  subroutine boundary_reconnection__dfield(df,nxs,nxe,nys,nye,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nxgs, nxge
+    real(8), intent(inout) :: df(*)
+  end subroutine boundary_reconnection__dfield
+  subroutine boundary_reconnection__curre(uj,nxs,nxe,nys,nye,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nxgs, nxge
+    real(8), intent(inout) :: uj(*)
+  end subroutine boundary_reconnection__curre
+  subroutine boundary_reconnection__phi(phi,nxs,nxe,nys,nye,l)
+    integer, intent(in)    :: nxs, nxe, nys, nye, l
+    real(8), intent(inout) :: phi(*)
+  end subroutine boundary_reconnection__phi
+
+  subroutine boundary_reconnection__mom(mom)
+    real(8), intent(inout) :: mom(*)
+    call wpic_check(wpic_bc_mom(wpic_ctx), 'bc__mom')
+    call wpic_check(wpic_get_mom(wpic_ctx, mom), 'get mom')
+  end subroutine boundary_reconnection__mom
+end module boundary_reconnection
+
+
+! boundary_shock (2d/proj/shock/boundary_shock.f90): reflecting wall at nxs, injection
+! boundary at nxe of the window.  The shock driver edits up, uf and cumcnt on the host
+! (inject, relocate), so its init switches the per-step upload on.
+module boundary_shock
+  use wpic_capi
+  implicit none
+  private
+  public :: boundary_shock__init, boundary_shock__dfield, boundary_shock__particle_x, &
+       boundary_shock__particle_y, boundary_shock__injection, boundary_shock__curre, boundary_shock__phi, &
+       boundary_shock__mom
+contains
+  subroutine boundary_shock__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nys_in,nye_in, &
+                                  nup_in,ndown_in,mnpi_in,mnpr_in,ncomw_in,nerr_in,nstat_in,delx_in,delt_in,c_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in, nxgs_in, nxge_in, nygs_in, nyge_in, nys_in, nye_in
+    integer, intent(in) :: nup_in, ndown_in, mnpi_in, mnpr_in, ncomw_in, nerr_in, nstat_in(:)
+    real(8), intent(in) :: delx_in, delt_in, c_in
+    wpic_prm%bc_kind = 2; wpic_bc_set = .true.
+    call wpic_shim_set_upload(.true.)
+  end subroutine boundary_shock__init
+
+  subroutine boundary_shock__particle_x(up,np2,nxs,nxe)
+    integer, intent(in)    :: nxs, nxe
+    real(8), intent(inout) :: up(*)
+    integer, intent(in)    :: np2(*)
+    call wpic_apply_window(nxs, nxe)
+    call wpic_check(p_bcx(wpic_ctx), 'bc__particle_x')
+  end subroutine boundary_shock__particle_x
+
+  subroutine boundary_shock__particle_y(up,np2)
+    real(8), intent(inout) :: up(*)
+    integer, intent(inout) :: np2(*)
+    call wpic_check(p_bcy(wpic_ctx), 'bc__particle_y')
+  end subroutine boundary_shock__particle_y
+
+  subroutine boundary_shock__injection(up,np2,nxs,nxe,u0)
+    integer, intent(in)    :: nxs, nxe
+    real(8), intent(inout) :: up(*)
+    integer, intent(in)    :: np2(*)
+    real(8), intent(in)    :: u0
+    call wpic_apply_window(nxs, nxe)
+    call wpic_check(wpic_bc_injection(wpic_ctx, real(u0, c_double)), 'bc__injection')
+  end subroutine boundary_shock__injection
+
+  ! applied inside the library; present so that field__fdtd_i's arguments type-check
+  subroutine boundary_shock__dfield(df,nxs,nxe,nys,nye,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nxgs, nxge
+    real(8), intent(inout) :: df(*)
+  end subroutine boundary_shock__dfield
+  subroutine boundary_shock__curre(uj,nxs,nxe,nys,nye,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nxgs, nxge
+    real(8), intent(inout) :: uj(*)
+  end subroutine boundary_shock__curre
+  subroutine boundary_shock__phi(phi,nxs,nxe,nys,nye,l)
+    integer, intent(in)    :: nxs, nxe, nys, nye, l
+    real(8), intent(inout) :: phi(*)
+  end subroutine boundary_shock__phi
+
+  subroutine boundary_shock__mom(mom)
+    real(8), intent(inout) :: mom(*)
+    call wpic_check(wpic_bc_mom(wpic_ctx), 'bc__mom')
+    call wpic_check(wpic_get_mom(wpic_ctx, mom), 'get mom')
+  end subroutine boundary_shock__mom
+end module boundary_shock
