@@ -443,12 +443,18 @@ __device__ __forceinline__ void phi_src(const Grid2D& g, int bc, int l, int& cx,
   }
 }
 
+// x or -x by flipping the sign bit with an integer XOR: the conditional negation would
+// otherwise cost an FP64 instruction, and the CG stencils are FP64-pipe bound (GB300 runs
+// FP64 at 1/64 of FP32)
+__device__ __forceinline__ double flip_sign(double x, bool neg) {
+  return __longlong_as_double(__double_as_longlong(x) ^ ((long long)neg << 63));
+}
+
 __device__ __forceinline__ double phi_at(const double* v, const Grid2D& g, int bc, int l, int cx, int cy) {
   bool neg;
   phi_src(g, bc, l, cx, cy, neg);
   if (cx < 0) return 0.0;
-  const double val = v[(size_t)cy * g.nx + cx];
-  return neg ? -val : val;
+  return flip_sign(v[(size_t)cy * g.nx + cx], neg);
 }
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -480,8 +486,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_init(Dev2D d) {
       bool neg;
       phi_src(g, d.ph.bc, l, x, y, neg);
       if (x < 0) return 0.0;
-      const double v = db[(size_t)y * g.fp + x];
-      return neg ? -v : v;
+      return flip_sign(db[(size_t)y * g.fp + x], neg);
     };
     const double pc = ph(cx, cy);
     const double b = f5 * d.gkl[off + c];
