@@ -46,3 +46,29 @@ def test_weibel_growth_rate_mixed_matches_fp64(gpu_lib):
     # total energy of the two runs tracks within 1 % through saturation
     tot64, totmx = e64.sum(axis=1), emx.sum(axis=1)
     np.testing.assert_allclose(totmx, tot64, rtol=1e-2)
+
+
+def test_weibel_growth_rate_mixed_matches_fp64_3d(gpu_lib):
+    """The 3D configuration's physics (beams +-0.5c along x, u_th 0.05c, m_i/m_e 16) on
+    32^3 cells: the mixed 3D path's magnetic growth rate within 1 % of the FP64 path's
+    from the same initial state, both saturating, total energies within 1 %."""
+    from wumingpic_gb300.loader import Plasma3D, load_weibel3d
+    from wumingpic_gb300.pic3d import Pic3D
+    p = Plasma3D(nx=32, ny=32, nz=32, ppc=16, mass_ratio=16.0, drift=0.5, drift_axis=0, u_the=0.05,
+                 seed=434343, np_slack=16.0)
+    st = load_weibel3d(p)
+    runs = {}
+    for precision in ("fp64", "mixed"):
+        g = Pic3D(p, precision=precision)
+        g.put_state(st)
+        runs[precision] = energy_history(g.step, g.energy, 800, 10, p.delt)
+        g.close()
+    t, e64 = runs["fp64"]
+    _, emx = runs["mixed"]
+    b64, bmx = e64[:, 3], emx[:, 3]
+    assert b64.max() > 1e2 * b64[1] and bmx.max() > 1e2 * bmx[1]
+    g64, win64, n64 = growth_rate(t, b64)
+    gmx, winmx, nmx = growth_rate(t, bmx)
+    assert n64 >= 5 and nmx >= 5
+    assert abs(gmx / g64 - 1.0) <= GROWTH_RATE_RTOL, (gmx, g64, win64, winmx)
+    np.testing.assert_allclose(emx.sum(axis=1), e64.sum(axis=1), rtol=1e-2)
