@@ -164,6 +164,19 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def rank_totals(ms, npart, dist, device):
+    """Whole-job figures of a replica run: the slowest rank's timed region (MAX over the
+    ranks) and the particles all ranks advanced (SUM); with no process group, the local ones."""
+    if not dist:
+        return float(ms), int(npart)
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    n = torch.tensor([int(npart)], dtype=torch.int64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(n.item())
+
+
 def time_path(p, precision, steps, warmup, rank, torch, dist, local):
     """Device-resident timing of `steps` fused steps on one context."""
     from wumingpic_gb300.pic2d import Pic2D
@@ -192,11 +205,8 @@ def time_path(p, precision, steps, warmup, rank, torch, dist, local):
     ms = e0.elapsed_time(e1)
     stages = g.stage_times()
     g.timing(False)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    return g, npart, ms, stages, clocks
+    ms, ntotal = rank_totals(ms, npart, dist, "cuda")
+    return g, ntotal, ms, stages, clocks
 
 
 def time_moments(g, torch, reps=3):
@@ -240,17 +250,13 @@ def time_path3d(steps, rank, torch, dist, world, precision="fp64", n=256):
     g.step(steps)
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, ntotal = rank_totals(e0.elapsed_time(e1), npart, dist, "cuda")
     cg = [int(x) for x in g.cg_iters()]
     moments = time_moments(g, torch, reps=2)
     g.close()
     return {"workload": f"3D Weibel {n}^3 cells, 16 ppc/species, {npart} particles, drift +-0.5c along x, "
                         f"u_th 0.05c, m_i/m_e 16, c*dt/dx=0.5",
-            "value": npart * world * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+            "value": ntotal * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
             "steps": steps, "warmup": 1, "dtype": "f64" if precision == "fp64" else "f32+f64",
             "cg_iterations": cg, "moments": moments}
 
@@ -306,24 +312,25 @@ def main():
 
     # ---- mixed path: the headline ----
     g, npart, ms, stages, clocks = time_path(p, "mixed", args.steps, args.warmup, rank, torch, dist, local)
-    value = npart * world * args.steps / (ms / 1e3)
+    value = npart * args.steps / (ms / 1e3)  # npart: all ranks' particles
     push_ms, push_n = stages["push"]
     per_launch = push_ms / max(1, push_n)
-    achieved = BYTES_MIX_PUSH * npart / (per_launch / 1e3) / 1e9
+    achieved = BYTES_MIX_PUSH * (npart / world) / (per_launch / 1e3) / 1e9  # one GPU's launch
     roofline = {"bound": "hbm", "kernel": "k_mix_push (fused push + deposit, mixed precision)",
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "traffic": None, "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "bytes_per_particle": BYTES_MIX_PUSH, "launch_ms": per_launch}
     launches = int(sum(v[1] for v in stages.values()))
     moments = time_moments(g, torch)
-    e2e = None if args.no_e2e else measure_e2e(g, p)
+    e2e = None if args.no_e2e else measure_e2e(g, p, dist)
     g.close()
 
     # ---- FP64 path on the same workload ----
     fp64 = None
     if args.fp64_steps > 0:
         g64, n64, ms64, st64, clk64 = time_path(p, "fp64", args.fp64_steps, 1, rank, torch, dist, local)
-        v64 = n64 * world * args.fp64_steps / (ms64 / 1e3)
+        v64 = n64 * args.fp64_steps / (ms64 / 1e3)
+        n64 = n64 // world  # one GPU's particles, for the per-launch kernel figures
         peak64 = _lib.fma_peak_gflops(True)
         dep_ms = st64["deposit"][0] / max(1, st64["deposit"][1] // 2)
         push64_ms = st64["push"][0] / max(1, st64["push"][1])
@@ -381,10 +388,11 @@ def main():
         dist.destroy_process_group()
 
 
-def measure_e2e(g, p):
+def measure_e2e(g, p, dist=None):
     """The same step through the C ABI with the reference-layout state in host memory:
     every step copies the state in (host -> device), runs the step and copies the new
-    state back (device -> host)."""
+    state back (device -> host).  With several ranks: all ranks' particles over the
+    slowest rank's time."""
     from wumingpic_gb300 import _lib
     st = g.get_state()
     pinned = []
@@ -406,7 +414,8 @@ def measure_e2e(g, p):
     dt = time.perf_counter() - t0
     for a in pinned:
         _lib.host_unregister(a)
-    n = int(st.np2.sum())
+    ms, n = rank_totals(dt * 1e3, int(st.np2.sum()), dist, "cuda")
+    dt = ms / 1e3
     bytes_state = st.up.nbytes + st.uf.nbytes + st.np2.nbytes + st.cumcnt.nbytes
     return {"value": n * steps / dt, "unit": UNIT, "h2d_bytes_per_step": int(bytes_state),
             "d2h_bytes_per_step": int(bytes_state), "steps": steps,
