@@ -162,6 +162,35 @@ int wpic_energy(wpic_ctx* ctx, double* out);
  * ite_max as in cgm (2d/common/field.f90:337).  cg_iters returns the last counts. */
 int wpic_cg_control(wpic_ctx* ctx, const int* fixed3, int ite_max);
 int wpic_cg_iters(wpic_ctx* ctx, int* out3);
+/* the CG stopping tolerance relative to ||b|| (the reference's 1e-6, field.f90:364) and the
+ * iteration limit (100, field.f90:427); a tight tolerance for gradient checks */
+int wpic_cg_tolerance(wpic_ctx* ctx, double rtol, int ite_max);
+
+/* Discrete adjoint of nsteps fused steps from the current state (FP64 paths, periodic, the
+ * Boris push): given lam_uf_final, the gradient of a scalar with respect to the fields after
+ * the last step (reference layout uf(6, nxgs-2:nxge+2, nys-2:nye+2)), returns its gradient with
+ * respect to the particles (lam_up0, layout of up with the ids in the id column) and the fields
+ * (lam_uf0) at the start.  States are kept every `every` steps and recomputed in between.
+ * The context is left in its state after the nsteps steps. */
+int wpic_adjoint(wpic_ctx* ctx, int nsteps, int every, const double* lam_uf_final, double* lam_up0,
+                 double* lam_uf0);
+/* wpic_adjoint in two halves.  record: nsteps steps from the current state, keeping the state
+ * at every segment start and at the end.  reverse: the gradients for the recorded run (may be
+ * called again with another lam_uf_final); leaves the recorded final state in the context. */
+int wpic_adjoint_record(wpic_ctx* ctx, int nsteps, int every);
+int wpic_adjoint_reverse(wpic_ctx* ctx, const double* lam_uf_final, double* lam_up0, double* lam_uf0);
+/* dot-product checks <L x, y> = <x, L^T y> of the adjoint's transposed field operators on
+ * random vectors (current fold, ghost copies, E update, RHS, cell-centre averaging): five
+ * relative differences.  Overwrites the context's fields. */
+int wpic_adjoint_selfcheck(wpic_ctx* ctx, double* out5);
+/* the push's field adjoint against a central difference of the push along a random field
+ * direction (step hstep), both projected on random particle adjoints: out2 = {difference,
+ * adjoint} */
+int wpic_adjoint_pushcheck(wpic_ctx* ctx, double hstep, double* out2);
+/* the deposit's adjoint against a central difference along random particle directions */
+int wpic_adjoint_depositcheck(wpic_ctx* ctx, double hstep, double* out2);
+/* the fields -> push -> deposit chain's adjoint against a central difference along random fields */
+int wpic_adjoint_chaincheck(wpic_ctx* ctx, double hstep, double* out2);
 
 /* Device-side seeded loader of a 2D Weibel plasma (no reference counterpart:
  * the reference loads on the host from an unseeded RNG, 2d/proj/weibel/app.f90:380-437). */

@@ -37,6 +37,7 @@ CUDA_UNITS = {
     "capi3d.cu": [],
     "kernels3d_common.cu": [],
     "mixed3d.cu": [],
+    "adjoint2d.cu": [],
 }
 
 

@@ -81,6 +81,14 @@ def lib():
             getattr(L, n).argtypes = [vp, vp]
         L.wpic_set_pusher.argtypes = [vp, i]
         L.wpic_set_window.argtypes = [vp, i, i]
+        L.wpic_cg_tolerance.argtypes = [vp, ctypes.c_double, i]
+        L.wpic_adjoint.argtypes = [vp, i, i, vp, vp, vp]
+        L.wpic_adjoint_record.argtypes = [vp, i, i]
+        L.wpic_adjoint_reverse.argtypes = [vp, vp, vp, vp]
+        L.wpic_adjoint_selfcheck.argtypes = [vp, vp]
+        L.wpic_adjoint_pushcheck.argtypes = [vp, ctypes.c_double, vp]
+        L.wpic_adjoint_depositcheck.argtypes = [vp, ctypes.c_double, vp]
+        L.wpic_adjoint_chaincheck.argtypes = [vp, ctypes.c_double, vp]
         L.wpic_set_injection.argtypes = [vp, ctypes.c_double]
         L.wpic_bc_injection.argtypes = [vp, ctypes.c_double]
         L.wpic3d_set_pusher.argtypes = [vp, i]

@@ -60,6 +60,19 @@ struct wpic_ctx {
   int pusher = WPIC_PUSH_BORIS;  // the push of the fused step
   double* mom = nullptr;         // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp), allocated on first use
   double u0 = 0.0;               // shock: upstream four-velocity of the injection boundary
+  // adjoint: adjoint particle arrays (sorted-state and pushed slots), field adjoints, the
+  // cell-centred fields and their adjoint, and the stored states of the reverse sweep
+  struct AdjState {
+    Parts64 A;
+    int *cc, *np2;
+    double *uf, *df;
+  };
+  bool adj_ready = false;
+  Parts64 lA{}, lB{};
+  double *luf = nullptr, *ldf = nullptr, *luj = nullptr, *lg = nullptr, *tmpc = nullptr, *ltmp = nullptr;
+  int* adj_cc = nullptr;  // the step's cell offsets, kept across the sort that gives the permutation
+  int adj_nsteps = 0, adj_every = 1;  // the recorded forward run (0: none)
+  std::vector<AdjState> adj_states;
 };
 
 namespace {
@@ -470,6 +483,7 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
   d.nred = (d.g.ncell + 255) / 256;
   if (d.nred > 1216) d.nred = 1216;
   d.ite_max = 100;
+  d.cg_rtol = 1e-6;  // field.f90:364
 
   int st = WPIC_OK;
   if (cuda_stream) {
@@ -787,6 +801,405 @@ static int get_field(wpic_ctx* c, double* ref, const double* src, int ncomp) {
   return finish(c);
 }
 
+// ---------------------------------------------------------------------------
+// adjoint of nsteps fused steps (FP64, periodic): states every `every` steps are kept; each
+// segment is recomputed forward with every step's state stored, then swept backwards with
+// the kernels of adjoint2d.cu.  The gradients are of the scalar whose gradient with respect
+// to the final fields is lam_uf_final (reference layout); they are returned with respect to
+// the particle state (same layout as wpic_get_particles: x, y, ux, uy, uz; the id column
+// carries the ids) and the fields at the start.  The context ends in its final state.
+// ---------------------------------------------------------------------------
+namespace {
+
+int adj_alloc_state(wpic_ctx* c, wpic_ctx::AdjState& S) {
+  const Dev2D& d = c->d;
+  const size_t slots = (size_t)d.nrowjob * d.cap;
+  int st;
+  if ((st = alloc_parts(c, &S.A, slots))) return st;
+  if ((st = dalloc(c, &S.cc, (size_t)d.nrowjob * (d.g.nx + 1)))) return st;
+  if ((st = dalloc(c, &S.np2, (size_t)d.nrowjob))) return st;
+  if ((st = dalloc(c, &S.uf, 6 * (size_t)d.g.fplane))) return st;
+  return dalloc(c, &S.df, 6 * (size_t)d.g.fplane);
+}
+
+void adj_copy_parts(const Parts64& from, const Parts64& to, size_t n, cudaStream_t s) {
+  cudaMemcpyAsync(to.x, from.x, n * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(to.y, from.y, n * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(to.ux, from.ux, n * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(to.uy, from.uy, n * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(to.uz, from.uz, n * 8, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(to.id, from.id, n * 8, cudaMemcpyDeviceToDevice, s);
+}
+
+void adj_save(wpic_ctx* c, const wpic_ctx::AdjState& S) {
+  Dev2D& d = c->d;
+  const size_t slots = (size_t)d.nrowjob * d.cap;
+  adj_copy_parts(d.A, S.A, slots, c->stream);
+  cudaMemcpyAsync(S.cc, d.cc, sizeof(int) * (size_t)d.nrowjob * (d.g.nx + 1), cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(S.np2, d.np2, sizeof(int) * (size_t)d.nrowjob, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(S.uf, d.uf, sizeof(double) * 6 * (size_t)d.g.fplane, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(S.df, d.df, sizeof(double) * 6 * (size_t)d.g.fplane, cudaMemcpyDeviceToDevice, c->stream);
+}
+
+void adj_load(wpic_ctx* c, const wpic_ctx::AdjState& S) {
+  Dev2D& d = c->d;
+  const size_t slots = (size_t)d.nrowjob * d.cap;
+  adj_copy_parts(S.A, d.A, slots, c->stream);
+  cudaMemcpyAsync(d.cc, S.cc, sizeof(int) * (size_t)d.nrowjob * (d.g.nx + 1), cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(d.np2, S.np2, sizeof(int) * (size_t)d.nrowjob, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(d.uf, S.uf, sizeof(double) * 6 * (size_t)d.g.fplane, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(d.df, S.df, sizeof(double) * 6 * (size_t)d.g.fplane, cudaMemcpyDeviceToDevice, c->stream);
+}
+
+int adj_prepare(wpic_ctx* c, int nstates) {
+  Dev2D& d = c->d;
+  int st;
+  if (!c->adj_ready) {
+    const size_t slots = (size_t)d.nrowjob * d.cap, P = d.g.fplane;
+    const size_t nt = 6 * (size_t)(d.g.nx + 2) * (d.g.ny + 2);
+    if ((st = alloc_parts(c, &c->lA, slots)) || (st = alloc_parts(c, &c->lB, slots))) return st;
+    if ((st = dalloc(c, &c->luf, 6 * P)) || (st = dalloc(c, &c->ldf, 6 * P)) || (st = dalloc(c, &c->luj, 3 * P)))
+      return st;
+    if ((st = dalloc(c, &c->lg, 3 * (size_t)d.g.ncell)) || (st = dalloc(c, &c->tmpc, nt)) ||
+        (st = dalloc(c, &c->ltmp, nt)) || (st = dalloc(c, &c->adj_cc, (size_t)d.nrowjob * (d.g.nx + 1))))
+      return st;
+    if ((st = ensure_C(c))) return st;
+    c->adj_ready = true;
+  }
+  while ((int)c->adj_states.size() < nstates) {
+    wpic_ctx::AdjState S{};
+    if ((st = adj_alloc_state(c, S))) return st;
+    c->adj_states.push_back(S);
+  }
+  return WPIC_OK;
+}
+
+void adj_zero_parts(const Parts64& P, size_t n, cudaStream_t s) {
+  cudaMemsetAsync(P.x, 0, n * 8, s);
+  cudaMemsetAsync(P.y, 0, n * 8, s);
+  cudaMemsetAsync(P.ux, 0, n * 8, s);
+  cudaMemsetAsync(P.uy, 0, n * 8, s);
+  cudaMemsetAsync(P.uz, 0, n * 8, s);
+}
+
+// one step backwards: d holds the state before the step; lA, luf hold the adjoints of the
+// state after it and return those of the state before it
+int adj_step(wpic_ctx* c) {
+  Dev2D& d = c->d;
+  const size_t slots = (size_t)d.nrowjob * d.cap;
+  fast::push2d(d, c->stream);                        // B: the pushed particles, before the wraps
+  adj_copy_parts(d.B, d.C, slots, c->stream);        // the bookkeeping on a copy gives the permutation
+  const size_t ccb = (size_t)d.nrowjob * (d.g.nx + 1) * sizeof(int);
+  cudaMemcpyAsync(c->adj_cc, d.cc, ccb, cudaMemcpyDeviceToDevice, c->stream);  // the sort rewrites cc
+  particle_x2d(d, d.C, c->stream);
+  migrate_scan2d(d, d.C, c->stream);
+  migrate_plan2d(d, c->stream);
+  sort_rank2d(d, d.C, d.slist, c->stream);
+  adj_zero_parts(c->lB, slots, c->stream);
+  adj_unsort(d, c->lA, c->lB, c->stream);
+  cudaMemcpyAsync(d.cc, c->adj_cc, ccb, cudaMemcpyDeviceToDevice, c->stream);  // the deposit and push read it
+  adj_zero_parts(c->lA, slots, c->stream);
+  adj_field(d, c->luf, c->ldf, c->luj, c->stream);
+  int st = do_cg(c);                                 // the adjoint solve: same symmetric operator
+  if (st) return st;
+  adj_field_after_cg(d, c->luf, c->lg, c->luj, c->stream);
+  adj_particles(d, c->luj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->stream);
+  return WPIC_OK;
+}
+
+}  // namespace
+
+// <L x, y> against <x, L^T y> for the transposed linear operators of the field part, with
+// random vectors: out[0] current fold, out[1] ghost copies, out[2] E update, out[3] RHS,
+// out[4] tmp averaging (relative differences).  Overwrites the context's fields.
+int wpic_adjoint_selfcheck(wpic_ctx* c, double* out) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed || c->d.ph.bc != BC_PERIODIC || !out) return WPIC_BAD_ARGUMENT;
+  Dev2D& d = c->d;
+  int st = adj_prepare(c, 0);
+  if (st) return st;
+  const size_t P = d.g.fplane, nc = d.g.ncell, nt = 6 * (size_t)(d.g.nx + 2) * (d.g.ny + 2);
+  double* dots = nullptr;
+  if ((st = dalloc(c, &dots, 8))) return st;
+  double h[8];
+  auto dot = [&](const double* a, const double* b, size_t n, int slot) { adj_dot(a, b, n, dots + slot, c->stream); };
+  // x in the scratch of the adjoint (luf/ldf/luj/lg: the inputs), y random, forward on d's buffers
+  // 0: fold.  x = uj (3P), L x = fold(uj); y = luj
+  cudaMemsetAsync(dots, 0, 8 * sizeof(double), c->stream);
+  adj_fill_rand(d.uj, 3 * P, 11, c->stream);
+  cudaMemcpyAsync(c->ldf, d.uj, 3 * P * 8, cudaMemcpyDeviceToDevice, c->stream);  // keep x
+  curre_fold2d(d, c->stream);
+  adj_fill_rand(c->luj, 3 * P, 12, c->stream);
+  dot(d.uj, c->luj, 3 * P, 0);
+  adj_field_fold_T(d, c->luj, c->stream);
+  dot(c->ldf, c->luj, 3 * P, 1);
+  // 1: ghost copies on 6 components.  x = df, L x = ghost(df); y = ldf
+  adj_fill_rand(d.df, 6 * P, 13, c->stream);
+  cudaMemcpyAsync(c->luf, d.df, 6 * P * 8, cudaMemcpyDeviceToDevice, c->stream);
+  dfield_ghost2d(d, c->stream);
+  adj_fill_rand(c->ldf, 6 * P, 14, c->stream);
+  dot(d.df, c->ldf, 6 * P, 2);
+  adj_field_ghost_T(d, c->ldf, c->stream);
+  dot(c->luf, c->ldf, 6 * P, 3);
+  CK(cudaMemcpyAsync(h, dots, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  out[0] = std::fabs(h[0] - h[1]) / std::fmax(std::fabs(h[0]), 1e-300);
+  out[1] = std::fabs(h[2] - h[3]) / std::fmax(std::fabs(h[2]), 1e-300);
+  // 2: E update.  x = (df0..2, uf, uj) random; L x = df3..5 interior; y on df3..5 interior
+  cudaMemsetAsync(dots, 0, 8 * sizeof(double), c->stream);
+  adj_fill_rand(d.df, 6 * P, 15, c->stream);
+  adj_fill_rand(d.uf, 6 * P, 16, c->stream);
+  adj_fill_rand(d.uj, 3 * P, 17, c->stream);
+  cudaMemsetAsync(d.df + 3 * P, 0, 3 * P * 8, c->stream);
+  fast::efield2d(d, c->stream);
+  adj_fill_rand(c->ldf, 6 * P, 18, c->stream);
+  adj_keep_interior(d, c->ldf + 3 * P, 3, c->stream);  // y: interior of df3..5 only
+  cudaMemsetAsync(c->ldf, 0, 3 * P * 8, c->stream);
+  dot(d.df + 3 * P, c->ldf + 3 * P, 3 * P, 0);
+  cudaMemsetAsync(c->luf, 0, 6 * P * 8, c->stream);
+  cudaMemsetAsync(c->luj, 0, 3 * P * 8, c->stream);
+  adj_field_efield_T(d, c->ldf, c->luf, c->luj, c->stream);
+  dot(d.df, c->ldf, 3 * P, 1);
+  dot(d.uf, c->luf, 6 * P, 1);
+  dot(d.uj, c->luj, 3 * P, 1);
+  // 3: RHS.  x = (uf, uj); L x = gkl; y = lg
+  adj_fill_rand(d.uf, 6 * P, 19, c->stream);
+  adj_fill_rand(d.uj, 3 * P, 20, c->stream);
+  fast::gkl2d(d, c->stream);
+  adj_fill_rand(c->lg, 3 * nc, 21, c->stream);
+  dot(d.gkl, c->lg, 3 * nc, 2);
+  cudaMemsetAsync(c->luf, 0, 6 * P * 8, c->stream);
+  cudaMemsetAsync(c->luj, 0, 3 * P * 8, c->stream);
+  adj_field_gkl_T(d, c->lg, c->luf, c->luj, c->stream);
+  dot(d.uf, c->luf, 6 * P, 3);
+  dot(d.uj, c->luj, 3 * P, 3);
+  // 4: tmp averaging.  x = uf; L x = tmp; y = ltmp
+  adj_fill_rand(d.uf, 6 * P, 22, c->stream);
+  adj_field_tmp(d, c->tmpc, c->stream);
+  adj_fill_rand(c->ltmp, nt, 23, c->stream);
+  dot(c->tmpc, c->ltmp, nt, 4);
+  cudaMemsetAsync(c->luf, 0, 6 * P * 8, c->stream);
+  adj_field_tmp_T(d, c->ltmp, c->luf, c->stream);
+  dot(d.uf, c->luf, 6 * P, 5);
+  CK(cudaMemcpyAsync(h, dots, 6 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  out[2] = std::fabs(h[0] - h[1]) / std::fmax(std::fabs(h[0]), 1e-300);
+  out[3] = std::fabs(h[2] - h[3]) / std::fmax(std::fabs(h[2]), 1e-300);
+  out[4] = std::fabs(h[4] - h[5]) / std::fmax(std::fabs(h[4]), 1e-300);
+  return finish(c);
+}
+
+// central difference of the push along a random field direction v, projected on a random lB,
+// against <v, (dB/duf)^T lB> from the adjoint kernels: out[0] the difference, out[1] the
+// adjoint.  Uses the context's particles and fields; the fields are restored.
+int wpic_adjoint_pushcheck(wpic_ctx* c, double hstep, double* out) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed || !out || !(hstep > 0)) return WPIC_BAD_ARGUMENT;
+  Dev2D& d = c->d;
+  int st = adj_prepare(c, 0);
+  if (st) return st;
+  const size_t P = d.g.fplane, slots = (size_t)d.nrowjob * d.cap;
+  double* dots = nullptr;
+  if ((st = dalloc(c, &dots, 4))) return st;
+  cudaMemsetAsync(dots, 0, 4 * sizeof(double), c->stream);
+  cudaMemcpyAsync(c->ldf, d.uf, 6 * P * 8, cudaMemcpyDeviceToDevice, c->stream);  // u
+  adj_fill_rand(c->luj, 3 * P, 31, c->stream);                                     // v (B components)
+  cudaMemsetAsync(c->luf, 0, 6 * P * 8, c->stream);
+  cudaMemcpyAsync(c->luf, c->luj, 3 * P * 8, cudaMemcpyDeviceToDevice, c->stream);
+  adj_fill_rand(c->luj, 3 * P, 37, c->stream);                                     // v (E components)
+  cudaMemcpyAsync(c->luf + 3 * P, c->luj, 3 * P * 8, cudaMemcpyDeviceToDevice, c->stream);
+  adj_fill_rand(c->lB.x, slots, 32, c->stream);
+  adj_fill_rand(c->lB.y, slots, 33, c->stream);
+  adj_fill_rand(c->lB.ux, slots, 34, c->stream);
+  adj_fill_rand(c->lB.uy, slots, 35, c->stream);
+  adj_fill_rand(c->lB.uz, slots, 36, c->stream);
+  adj_axpy(d.uf, c->ldf, c->luf, hstep, 6 * P, c->stream);
+  fast::push2d(d, c->stream);
+  adj_dot_parts(d, c->lB, d.B, 0.5 / hstep, dots, c->stream);
+  adj_axpy(d.uf, c->ldf, c->luf, -hstep, 6 * P, c->stream);
+  fast::push2d(d, c->stream);
+  adj_dot_parts(d, c->lB, d.B, -0.5 / hstep, dots, c->stream);
+  cudaMemcpyAsync(d.uf, c->ldf, 6 * P * 8, cudaMemcpyDeviceToDevice, c->stream);
+  // adjoint into ldf (zeroed): <v, ldf>
+  cudaMemsetAsync(c->ldf, 0, 6 * P * 8, c->stream);
+  adj_push_fields(d, c->lB, c->lA, c->tmpc, c->ltmp, c->ldf, c->stream);
+  adj_dot(c->luf, c->ldf, 6 * P, dots + 1, c->stream);
+  double h[2];
+  CK(cudaMemcpyAsync(h, dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  out[0] = h[0];
+  out[1] = h[1];
+  return finish(c);
+}
+
+// central difference of <lJ, J(A, B)> (J the raw deposit, B the push of the context's state)
+// along random directions of A's positions and B's positions and momenta, against the
+// deposit's adjoint: out2 = {difference, adjoint}.  The particles are restored.
+int wpic_adjoint_depositcheck(wpic_ctx* c, double hstep, double* out) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed || !out || !(hstep > 0)) return WPIC_BAD_ARGUMENT;
+  Dev2D& d = c->d;
+  int st = adj_prepare(c, 0);
+  if (st) return st;
+  const size_t P = d.g.fplane, slots = (size_t)d.nrowjob * d.cap;
+  Parts64 A0{}, B0{}, vA{}, vB{};
+  double* dots = nullptr;
+  if ((st = alloc_parts(c, &A0, slots)) || (st = alloc_parts(c, &B0, slots)) || (st = alloc_parts(c, &vA, slots)) ||
+      (st = alloc_parts(c, &vB, slots)) || (st = dalloc(c, &dots, 4)))
+    return st;
+  cudaMemsetAsync(dots, 0, 4 * sizeof(double), c->stream);
+  fast::push2d(d, c->stream);
+  adj_copy_parts(d.A, A0, slots, c->stream);
+  adj_copy_parts(d.B, B0, slots, c->stream);
+  double* va[2] = {vA.x, vA.y};
+  double* vb[5] = {vB.x, vB.y, vB.ux, vB.uy, vB.uz};
+  double* a_[2] = {d.A.x, d.A.y};
+  double* a0[2] = {A0.x, A0.y};
+  double* b_[5] = {d.B.x, d.B.y, d.B.ux, d.B.uy, d.B.uz};
+  double* b0[5] = {B0.x, B0.y, B0.ux, B0.uy, B0.uz};
+  for (int q = 0; q < 2; ++q) adj_fill_rand(va[q], slots, 41 + q, c->stream);
+  for (int q = 0; q < 5; ++q) adj_fill_rand(vb[q], slots, 43 + q, c->stream);
+  adj_fill_rand(c->luj, 3 * P, 48, c->stream);
+  for (int sgn = 1; sgn >= -1; sgn -= 2) {
+    for (int q = 0; q < 2; ++q) adj_axpy(a_[q], a0[q], va[q], sgn * hstep, slots, c->stream);
+    for (int q = 0; q < 5; ++q) adj_axpy(b_[q], b0[q], vb[q], sgn * hstep, slots, c->stream);
+    fast::deposit2d(d, c->stream);
+    adj_dot(d.uj, c->luj, 3 * P, dots + (sgn > 0 ? 0 : 1), c->stream);
+  }
+  adj_copy_parts(A0, d.A, slots, c->stream);
+  adj_copy_parts(B0, d.B, slots, c->stream);
+  adj_zero_parts(c->lA, slots, c->stream);
+  adj_zero_parts(c->lB, slots, c->stream);
+  adj_deposit_only(d, c->luj, c->lA, c->lB, c->stream);
+  double* la[2] = {c->lA.x, c->lA.y};
+  double* lb[5] = {c->lB.x, c->lB.y, c->lB.ux, c->lB.uy, c->lB.uz};
+  for (int q = 0; q < 2; ++q) adj_dot(va[q], la[q], slots, dots + 2, c->stream);
+  for (int q = 0; q < 5; ++q) adj_dot(vb[q], lb[q], slots, dots + 2, c->stream);
+  double h[3];
+  CK(cudaMemcpyAsync(h, dots, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  out[0] = (h[0] - h[1]) * 0.5 / hstep;
+  out[1] = h[2];
+  return finish(c);
+}
+
+// central difference of <lJ, J(A, push(A, uf))> along a random direction of the fields against
+// push_F^T deposit_B^T lJ: out2 = {difference, adjoint}.  The fields are restored.
+int wpic_adjoint_chaincheck(wpic_ctx* c, double hstep, double* out) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed || !out || !(hstep > 0)) return WPIC_BAD_ARGUMENT;
+  Dev2D& d = c->d;
+  int st = adj_prepare(c, 0);
+  if (st) return st;
+  const size_t P = d.g.fplane, slots = (size_t)d.nrowjob * d.cap;
+  double *dots = nullptr, *f0 = nullptr, *v = nullptr, *lj = nullptr;
+  if ((st = dalloc(c, &dots, 4)) || (st = dalloc(c, &f0, 6 * P)) || (st = dalloc(c, &v, 6 * P)) ||
+      (st = dalloc(c, &lj, 3 * P)))
+    return st;
+  cudaMemsetAsync(dots, 0, 4 * sizeof(double), c->stream);
+  cudaMemcpyAsync(f0, d.uf, 6 * P * 8, cudaMemcpyDeviceToDevice, c->stream);
+  adj_fill_rand(v, 6 * P, 51, c->stream);
+  adj_fill_rand(lj, 3 * P, 52, c->stream);
+  for (int sgn = 1; sgn >= -1; sgn -= 2) {
+    adj_axpy(d.uf, f0, v, sgn * hstep, 6 * P, c->stream);
+    fast::push2d(d, c->stream);
+    fast::deposit2d(d, c->stream);
+    adj_dot(d.uj, lj, 3 * P, dots + (sgn > 0 ? 0 : 1), c->stream);
+  }
+  cudaMemcpyAsync(d.uf, f0, 6 * P * 8, cudaMemcpyDeviceToDevice, c->stream);
+  fast::push2d(d, c->stream);
+  cudaMemsetAsync(c->luf, 0, 6 * P * 8, c->stream);
+  adj_zero_parts(c->lA, slots, c->stream);
+  adj_zero_parts(c->lB, slots, c->stream);
+  adj_particles(d, lj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->stream);
+  adj_dot(v, c->luf, 6 * P, dots + 2, c->stream);
+  double h[3];
+  CK(cudaMemcpyAsync(h, dots, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  out[0] = (h[0] - h[1]) * 0.5 / hstep;
+  out[1] = h[2];
+  return finish(c);
+}
+
+// Forward half of the adjoint: nsteps steps from the current state, keeping the particle and
+// field state at every segment start (every K steps) and at the end.
+int wpic_adjoint_record(wpic_ctx* c, int nsteps, int every) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed || c->d.ph.bc != BC_PERIODIC || c->pusher != WPIC_PUSH_BORIS || nsteps < 1 || every < 1)
+    return WPIC_BAD_ARGUMENT;
+  const int nseg = (nsteps + every - 1) / every;
+  c->adj_nsteps = 0;
+  int st = adj_prepare(c, nseg + every + 1);
+  if (st) return st;
+  for (int k = 0; k < nsteps; ++k) {
+    if (k % every == 0) adj_save(c, c->adj_states[k / every]);
+    if ((st = one_step(c))) return st;
+  }
+  adj_save(c, c->adj_states[nseg + every]);
+  if ((st = finish(c))) return st;
+  c->adj_nsteps = nsteps;
+  c->adj_every = every;
+  return WPIC_OK;
+}
+
+// Reverse half: given the gradient of a scalar with respect to the recorded final fields,
+// the gradients with respect to the recorded initial particles (reference layout of up, ids
+// in the last slot) and fields (layout of uf).  Each segment is recomputed from its start,
+// its step states kept, and the steps are reversed.  Leaves the recorded final state.
+int wpic_adjoint_reverse(wpic_ctx* c, const double* lam_uf_final, double* lam_up0, double* lam_uf0) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!lam_uf_final || !lam_up0 || !lam_uf0) return WPIC_BAD_ARGUMENT;
+  if (c->adj_nsteps < 1) return WPIC_BAD_ARGUMENT;  // nothing recorded
+  Dev2D& d = c->d;
+  const int nsteps = c->adj_nsteps, every = c->adj_every;
+  const int nseg = (nsteps + every - 1) / every;
+  int fixed_saved[3];
+  for (int l = 0; l < 3; ++l) fixed_saved[l] = c->cg_fixed[l];
+  auto ckpt = [&](int k) -> wpic_ctx::AdjState& { return c->adj_states[k]; };
+  auto step_state = [&](int k) -> wpic_ctx::AdjState& { return c->adj_states[nseg + k]; };
+  wpic_ctx::AdjState& fin = c->adj_states[nseg + every];
+  int st = put_field(c, lam_uf_final, c->luf, 6);  // the seed: the final fields' adjoint
+  if (st) return st;
+  adj_zero_parts(c->lA, (size_t)d.nrowjob * d.cap, c->stream);
+  for (int l = 0; l < 3; ++l) c->cg_fixed[l] = -1;  // adjoint solves: the tolerance rule
+  for (int seg = nseg - 1; seg >= 0; --seg) {
+    const int s0 = seg * every, s1 = std::min(nsteps, s0 + every);
+    adj_load(c, ckpt(seg));
+    for (int k = s0; k < s1; ++k) {
+      adj_save(c, step_state(k - s0));
+      if (k + 1 < s1 && (st = one_step(c))) break;
+    }
+    if (st) break;
+    for (int k = s1 - 1; k >= s0; --k) {
+      adj_load(c, step_state(k - s0));
+      if ((st = adj_step(c))) break;
+    }
+    if (st) break;
+    if ((st = finish(c))) break;
+  }
+  for (int l = 0; l < 3; ++l) c->cg_fixed[l] = fixed_saved[l];
+  if (st) return st;
+  // d holds the initial state: the particle gradient in its slot order, with its ids
+  const int ndim = c->prm.ndim, nph = c->prm.np;
+  const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
+  if ((st = ensure_staging(c, (size_t)d.nrowjob * row_bytes))) return st;
+  Parts64 G = c->lA;
+  G.id = d.A.id;
+  soa_to_aos2d(d, c->staging, ndim, nph, 0, d.nrowjob, G, c->stream);
+  CK(cudaMemcpyAsync(lam_up0, c->staging, (size_t)d.nrowjob * row_bytes, cudaMemcpyDeviceToHost, c->stream));
+  if ((st = finish(c))) return st;
+  if ((st = get_field(c, lam_uf0, c->luf, 6))) return st;
+  adj_load(c, fin);
+  return finish(c);
+}
+
+int wpic_adjoint(wpic_ctx* c, int nsteps, int every, const double* lam_uf_final, double* lam_up0,
+                 double* lam_uf0) {
+  if (!lam_uf_final || !lam_up0 || !lam_uf0) return WPIC_BAD_ARGUMENT;
+  int st = wpic_adjoint_record(c, nsteps, every);
+  return st ? st : wpic_adjoint_reverse(c, lam_uf_final, lam_up0, lam_uf0);
+}
+
 int wpic_put_fields(wpic_ctx* c, const double* uf) { return c ? put_field(c, uf, c->d.uf, 6) : WPIC_NOT_INITIALISED; }
 int wpic_get_fields(wpic_ctx* c, double* uf) { return c ? get_field(c, uf, c->d.uf, 6) : WPIC_NOT_INITIALISED; }
 int wpic_put_df(wpic_ctx* c, const double* df) { return c ? put_field(c, df, c->d.df, 6) : WPIC_NOT_INITIALISED; }
@@ -983,6 +1396,14 @@ int wpic_cg_control(wpic_ctx* c, const int* fixed3, int ite_max) {
   if (!c) return WPIC_NOT_INITIALISED;
   for (int l = 0; l < 3; ++l) c->cg_fixed[l] = fixed3 ? fixed3[l] : -1;
   c->d.ite_max = ite_max > 0 ? ite_max : 100;
+  return WPIC_OK;
+}
+
+int wpic_cg_tolerance(wpic_ctx* c, double rtol, int ite_max) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!(rtol > 0.0) || rtol >= 1.0 || ite_max < 1) return WPIC_BAD_ARGUMENT;
+  c->d.cg_rtol = rtol;
+  c->d.ite_max = ite_max;
   return WPIC_OK;
 }
 

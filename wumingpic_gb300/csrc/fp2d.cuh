@@ -526,7 +526,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_init_fin(Dev2D d) {
   if (threadIdx.x == 0) {
     CGState& st = d.cg[l];
     st.sum_g = sb;
-    st.eps = sqrt(sb) * 1e-6;
+    st.eps = sqrt(sb) * d.cg_rtol;
     st.sumr_g = sr;
     st.ite = 0;
     if (st.fixed >= 0) st.active = st.fixed > 0;

@@ -112,6 +112,61 @@ class Pic2D:
     def particle__solv(self):
         check(lib().wpic_particle_solv(self._h), "particle__solv")
 
+    def cg_tolerance(self, rtol, ite_max=1000):
+        """CG stopping tolerance relative to ||b|| (the reference's 1e-6) and iteration limit"""
+        check(lib().wpic_cg_tolerance(self._h, float(rtol), int(ite_max)), "cg_tolerance")
+
+    def adjoint(self, nsteps, every, lam_uf_final):
+        """Run nsteps steps from the current state and return the gradient of a scalar with
+        respect to the initial particles (layout of up) and fields (layout of uf), given its
+        gradient with respect to the final fields."""
+        p = self.p
+        lam_uf_final = np.asfortranarray(lam_uf_final, dtype=np.float64)
+        lup = np.zeros((p.ndim, p.np_cap, p.ny, p.nsp), order="F")
+        luf = np.zeros((6, p.nx + 4, p.ny + 4), order="F")
+        check(lib().wpic_adjoint(self._h, int(nsteps), int(every), _ptr(lam_uf_final, np.float64),
+                                 _ptr(lup, np.float64), _ptr(luf, np.float64)), "adjoint")
+        return lup, luf
+
+    def adjoint_record(self, nsteps, every):
+        """The forward half of ``adjoint``: run nsteps steps keeping the state every `every` steps."""
+        check(lib().wpic_adjoint_record(self._h, int(nsteps), int(every)), "adjoint_record")
+
+    def adjoint_reverse(self, lam_uf_final):
+        """The reverse half of ``adjoint`` for the recorded run: (lam_up0, lam_uf0)."""
+        p = self.p
+        lam_uf_final = np.asfortranarray(lam_uf_final, dtype=np.float64)
+        lup = np.zeros((p.ndim, p.np_cap, p.ny, p.nsp), order="F")
+        luf = np.zeros((6, p.nx + 4, p.ny + 4), order="F")
+        check(lib().wpic_adjoint_reverse(self._h, _ptr(lam_uf_final, np.float64), _ptr(lup, np.float64),
+                                         _ptr(luf, np.float64)), "adjoint_reverse")
+        return lup, luf
+
+    def adjoint_selfcheck(self):
+        """relative <L x, y> - <x, L^T y> of the adjoint's transposed field operators
+        (fold, ghost copies, E update, RHS, averaging); overwrites the fields"""
+        out = np.zeros(5)
+        check(lib().wpic_adjoint_selfcheck(self._h, _ptr(out, np.float64)), "adjoint_selfcheck")
+        return out
+
+    def adjoint_pushcheck(self, h=1e-6):
+        """(central difference, adjoint) of the push along a random field direction"""
+        out = np.zeros(2)
+        check(lib().wpic_adjoint_pushcheck(self._h, float(h), _ptr(out, np.float64)), "adjoint_pushcheck")
+        return out
+
+    def adjoint_depositcheck(self, h=1e-6):
+        """(central difference, adjoint) of the deposit along random particle directions"""
+        out = np.zeros(2)
+        check(lib().wpic_adjoint_depositcheck(self._h, float(h), _ptr(out, np.float64)), "adjoint_depositcheck")
+        return out
+
+    def adjoint_chaincheck(self, h=1e-6):
+        """(central difference, adjoint) of fields -> push -> deposit along random fields"""
+        out = np.zeros(2)
+        check(lib().wpic_adjoint_chaincheck(self._h, float(h), _ptr(out, np.float64)), "adjoint_chaincheck")
+        return out
+
     def set_window(self, nxs, nxe):
         """the active x window nxs..nxe (the shock driver's expanding box)"""
         check(lib().wpic_set_window(self._h, int(nxs), int(nxe)), "set_window")
