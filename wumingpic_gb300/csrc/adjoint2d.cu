@@ -14,11 +14,13 @@
 //   current fold -> its transpose: lJ
 //   deposit: lA(x, y) and lB(x, y, u) += dJ/d(.)^T lJ
 //   push:    lA += dB/dA^T lB, luf += dB/duf^T lB
-// The per-particle Jacobians of the push and the deposit are evaluated in forward mode with
-// dual numbers on the same expressions as the forward kernels; the linear field operators
-// are transposed by hand (the dot-product identity <L x, y> = <x, L^T y> is checked by
-// wpic_adjoint_selfcheck).  Scatters use FP64 atomics: the adjoint is not bitwise
-// reproducible, only to round-off.
+// The push and the deposit are differentiated per particle in reverse mode, by hand, on the
+// same expressions as the forward kernels (one backward sweep through the Boris rotation
+// and through the Esirkepov weights gives all input adjoints at a few times the primal
+// cost); the linear field operators are transposed by hand (the dot-product identity
+// <L x, y> = <x, L^T y> is checked by wpic_adjoint_selfcheck).  The push's field adjoints
+// are summed per cell inside each block and added to the nodes with FP64 atomics: the
+// adjoint is reproducible to round-off, not bitwise.
 #include <cmath>
 
 #include "common.cuh"
@@ -26,92 +28,6 @@
 namespace wpic {
 
 namespace {
-
-// ---- dual numbers: value and N partial derivatives ----
-template <int N>
-struct Dual {
-  double v;
-  double d[N];
-};
-
-template <int N>
-__device__ __forceinline__ Dual<N> dconst(double v) {
-  Dual<N> r;
-  r.v = v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = 0.0;
-  return r;
-}
-template <int N>
-__device__ __forceinline__ Dual<N> dvar(double v, int k) {
-  Dual<N> r = dconst<N>(v);
-  r.d[k] = 1.0;
-  return r;
-}
-template <int N>
-__device__ __forceinline__ Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) {
-  Dual<N> r;
-  r.v = a.v + b.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i];
-  return r;
-}
-template <int N>
-__device__ __forceinline__ Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) {
-  Dual<N> r;
-  r.v = a.v - b.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i];
-  return r;
-}
-template <int N>
-__device__ __forceinline__ Dual<N> operator-(const Dual<N>& a) {
-  Dual<N> r;
-  r.v = -a.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
-  return r;
-}
-template <int N>
-__device__ __forceinline__ Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
-  Dual<N> r;
-  r.v = a.v * b.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
-  return r;
-}
-template <int N>
-__device__ __forceinline__ Dual<N> operator*(double s, const Dual<N>& a) {
-  Dual<N> r;
-  r.v = s * a.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = s * a.d[i];
-  return r;
-}
-template <int N>
-__device__ __forceinline__ Dual<N> operator+(double s, const Dual<N>& a) {
-  Dual<N> r = a;
-  r.v = s + a.v;
-  return r;
-}
-template <int N>
-__device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
-  Dual<N> r;
-  const double ib = 1.0 / b.v;
-  r.v = a.v * ib;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
-  return r;
-}
-template <int N>
-__device__ __forceinline__ Dual<N> dsqrt(const Dual<N>& a) {
-  Dual<N> r;
-  r.v = sqrt(a.v);
-  const double h = 0.5 / r.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * h;
-  return r;
-}
 
 __device__ __forceinline__ int cell_of(const int* ccr, int nc, int s) {
   int lo = 0, hi = nc;
@@ -358,8 +274,15 @@ __global__ void k_adj_cg_result(Dev2D d, double* lg) {
   }
 }
 
-// ---- the deposit's Jacobian: inputs (x_old, y_old, x_new, y_new, ux', uy', uz') ----
-__global__ void k_adj_deposit(Dev2D d, const double* luj, Parts64 lA, Parts64 lB) {
+// ---- the deposit's adjoint: inputs (x_old, y_old, x_new, y_new, ux', uy', uz') ----
+// Forward (per particle, 2d/common/field.f90:189-316): shapes s0 (old position, 5-point
+// stencil around the old cell), S1 (new position, shifted by the cell change inc), ds = S1 - s0,
+//   Jx(i+1, j) = -qdd wy[j] sum_{i'<=i} ds_x[i'],   wy = s0_y + ds_y / 2,
+//   Jy(i, j+1) = -qdd wx[i] sum_{j'<=j} ds_y[j'],   wx = s0_x + ds_x / 2,
+//   Jz(i, j)   = q gvz (s0_x s0_y + ds_x s0_y / 2 + s0_x ds_y / 2 + ds_x ds_y / 3),
+// gvz = uz / sqrt(1 + u^2 / c^2).  Reverse: the adjoints of the 5-point shape arrays from
+// suffix sums of lJ, then through ds = S1 - s0, the shift and the quadratic spline.
+__global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj, Parts64 lA, Parts64 lB) {
   const Grid2D g = d.g;
   const int row = blockIdx.y;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -369,166 +292,266 @@ __global__ void k_adj_deposit(Dev2D d, const double* luj, Parts64 lA, Parts64 lB
   const int cx = cell_of(ccr, g.nx, s);
   const size_t k = (size_t)row * d.cap + s;
   const double d_delx = d.ph.d_delx, c = d.ph.c;
-  const double qdd = d.ph.q[isp] * d.ph.delx * d.ph.d_delt, fac = 1.0 / 3.0;
+  const double q = d.ph.q[isp];
+  const double qdd = q * d.ph.delx * d.ph.d_delt, fac = 1.0 / 3.0;
   const int iabs = g.nxgs + cx, jabs = g.nygs + jj;
-  using D7 = Dual<7>;
-  const D7 in[7] = {dvar<7>(d.A.x[k], 0), dvar<7>(d.A.y[k], 1), dvar<7>(d.B.x[k], 2), dvar<7>(d.B.y[k], 3),
-                    dvar<7>(d.B.ux[k], 4), dvar<7>(d.B.uy[k], 5), dvar<7>(d.B.uz[k], 6)};
-  D7 s0[2][5], ds[2][5];
+  const double pos0[2] = {d.A.x[k], d.A.y[k]};
+  const double pos1[2] = {d.B.x[k], d.B.y[k]};
+  double s0[2][5], ds[2][5], dh[2], dh1[2];
+  int inc[2];
 #pragma unroll
   for (int dim = 0; dim < 2; ++dim) {
-    const D7 dh = d_delx * in[dim] + dconst<7>(-0.5 - (double)(dim == 0 ? iabs : jabs));
-    s0[dim][0] = dconst<7>(0.0);
-    s0[dim][1] = 0.5 * ((0.5 + (-dh)) * (0.5 + (-dh)));
-    s0[dim][2] = 0.75 + (-(dh * dh));
-    s0[dim][3] = 0.5 * ((0.5 + dh) * (0.5 + dh));
-    s0[dim][4] = dconst<7>(0.0);
-    const double pnv = in[2 + dim].v;
-    const int i2 = (int)(pnv * d_delx);
-    const D7 dh1 = d_delx * in[2 + dim] + dconst<7>(-0.5 - (double)i2);
-    const int inc = i2 - (dim == 0 ? iabs : jabs);
-    const D7 s1_1 = 0.5 * ((0.5 + (-dh1)) * (0.5 + (-dh1)));
-    const D7 s1_2 = 0.75 + (-(dh1 * dh1));
-    const D7 s1_3 = 0.5 * ((0.5 + dh1) * (0.5 + dh1));
-    const int ainc = inc < 0 ? -inc : inc;
-    const double m1 = (double)(-(inc - ainc)) * 0.5, m2 = (double)(-ainc + 1), m3 = (double)(inc + ainc) * 0.5;
-    ds[dim][0] = m1 * s1_1 - s0[dim][0];
-    ds[dim][1] = m2 * s1_1 + m1 * s1_2 - s0[dim][1];
-    ds[dim][2] = m2 * s1_2 + m1 * s1_3 + m3 * s1_1 - s0[dim][2];
-    ds[dim][3] = m2 * s1_3 + m3 * s1_2 - s0[dim][3];
-    ds[dim][4] = m3 * s1_3 - s0[dim][4];
+    const double h = d_delx * pos0[dim] + (-0.5 - (double)(dim == 0 ? iabs : jabs));
+    dh[dim] = h;
+    s0[dim][0] = 0.0;
+    s0[dim][1] = 0.5 * ((0.5 - h) * (0.5 - h));
+    s0[dim][2] = 0.75 - h * h;
+    s0[dim][3] = 0.5 * ((0.5 + h) * (0.5 + h));
+    s0[dim][4] = 0.0;
+    const int i2 = (int)(pos1[dim] * d_delx);
+    const double h1 = d_delx * pos1[dim] + (-0.5 - (double)i2);
+    dh1[dim] = h1;
+    inc[dim] = i2 - (dim == 0 ? iabs : jabs);
+    const double a1 = 0.5 * ((0.5 - h1) * (0.5 - h1)), a2 = 0.75 - h1 * h1, a3 = 0.5 * ((0.5 + h1) * (0.5 + h1));
+    const int ai = inc[dim] < 0 ? -inc[dim] : inc[dim];
+    const double m1 = (double)(-(inc[dim] - ai)) * 0.5, m2 = (double)(-ai + 1), m3 = (double)(inc[dim] + ai) * 0.5;
+    ds[dim][0] = m1 * a1 - s0[dim][0];
+    ds[dim][1] = m2 * a1 + m1 * a2 - s0[dim][1];
+    ds[dim][2] = m2 * a2 + m1 * a3 + m3 * a1 - s0[dim][2];
+    ds[dim][3] = m2 * a3 + m3 * a2 - s0[dim][3];
+    ds[dim][4] = m3 * a3 - s0[dim][4];
   }
-  const D7 u2 = in[4] * in[4] + in[5] * in[5] + in[6] * in[6];
-  const D7 gvz = in[6] / dsqrt(1. + (1.0 / (c * c)) * u2);
-  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  const double ux = d.B.ux[k], uy = d.B.uy[k], uz = d.B.uz[k];
+  const double ic2 = 1.0 / (c * c);
+  const double gmi = 1.0 / sqrt(1. + ic2 * (ux * ux + uy * uy + uz * uz));
+  const double gvz = uz * gmi;
   const size_t P = g.fplane;
-  auto take = [&](const D7& v, int comp, int a, int b) {  // entry (a, b) of the cell -> node (cx+a, jj+b)
-    const double l = luj[(size_t)comp * P + (size_t)(jj + b) * g.fp + (cx + a)];
+  const double* L0 = luj + (size_t)jj * g.fp + cx;  // node (cx + a, jj + b) at L0[b * fp + a]
+  double gs0[2][5], gds[2][5];
 #pragma unroll
-    for (int i = 0; i < 7; ++i) acc[i] += l * v.d[i];
-  };
+  for (int dim = 0; dim < 2; ++dim)
 #pragma unroll
-  for (int jp = 0; jp < 5; ++jp) {
-    const D7 wy = s0[1][jp] + 0.5 * ds[1][jp];
-    D7 t = dconst<7>(0.0);
+    for (int i = 0; i < 5; ++i) gs0[dim][i] = gds[dim][i] = 0.0;
+  // Jx: nodes (i + 1, j), i = 0..3, j = 0..4
 #pragma unroll
-    for (int ip = 0; ip < 4; ++ip) {
-      t = t - qdd * (ds[0][ip] * wy);
-      take(t, 0, ip + 1, jp);
+  for (int j = 0; j < 5; ++j) {
+    const double wy = s0[1][j] + 0.5 * ds[1][j];
+    double suf = 0.0, gw = 0.0;
+#pragma unroll
+    for (int i = 3; i >= 0; --i) {
+      suf += L0[(size_t)j * g.fp + i + 1];  // sum_{i'' >= i} lJx(i'' + 1, j)
+      gds[0][i] += -qdd * wy * suf;
+      gw += ds[0][i] * suf;
     }
+    gw *= -qdd;
+    gs0[1][j] += gw;
+    gds[1][j] += 0.5 * gw;
+  }
+  // Jy: nodes (i, j + 1), i = 0..4, j = 0..3
+  const double* L1 = L0 + P;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const double wx = s0[0][i] + 0.5 * ds[0][i];
+    double suf = 0.0, gw = 0.0;
+#pragma unroll
+    for (int j = 3; j >= 0; --j) {
+      suf += L1[(size_t)(j + 1) * g.fp + i];
+      gds[1][j] += -qdd * wx * suf;
+      gw += ds[1][j] * suf;
+    }
+    gw *= -qdd;
+    gs0[0][i] += gw;
+    gds[0][i] += 0.5 * gw;
+  }
+  // Jz: nodes (i, j) = Qz (s0_x (x) Ay + ds_x (x) By), Ay = s0_y + ds_y / 2, By = s0_y / 2 + ds_y / 3
+  const double* L2 = L0 + 2 * P;
+  const double Qz = q * gvz;
+  double gAy[5] = {0, 0, 0, 0, 0}, gBy[5] = {0, 0, 0, 0, 0}, phiz = 0.0;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    double r1 = 0.0, r2 = 0.0;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      const double l = L2[(size_t)j * g.fp + i];
+      r1 += l * (s0[1][j] + 0.5 * ds[1][j]);
+      r2 += l * (0.5 * s0[1][j] + fac * ds[1][j]);
+      gAy[j] += l * s0[0][i];
+      gBy[j] += l * ds[0][i];
+    }
+    gs0[0][i] += Qz * r1;
+    gds[0][i] += Qz * r2;
+    phiz += s0[0][i] * r1 + ds[0][i] * r2;
   }
 #pragma unroll
-  for (int ip = 0; ip < 5; ++ip) {
-    const D7 wx = s0[0][ip] + 0.5 * ds[0][ip];
-    D7 t = dconst<7>(0.0);
-#pragma unroll
-    for (int jp = 0; jp < 4; ++jp) {
-      t = t - qdd * (ds[1][jp] * wx);
-      take(t, 1, ip, jp + 1);
-    }
+  for (int j = 0; j < 5; ++j) {
+    gs0[1][j] += Qz * (gAy[j] + 0.5 * gBy[j]);
+    gds[1][j] += Qz * (0.5 * gAy[j] + fac * gBy[j]);
   }
-  const D7 qg = d.ph.q[isp] * gvz;
+  // through ds = S1 - s0, the shift by inc and the splines
+  double gpos0[2], gpos1[2];
 #pragma unroll
-  for (int jp = 0; jp < 5; ++jp)
-#pragma unroll
-    for (int ip = 0; ip < 5; ++ip) {
-      const D7 v = qg * (s0[0][ip] * s0[1][jp] + 0.5 * (ds[0][ip] * s0[1][jp]) + 0.5 * (s0[0][ip] * ds[1][jp]) +
-                         fac * (ds[0][ip] * ds[1][jp]));
-      take(v, 2, ip, jp);
-    }
-  lA.x[k] += acc[0];
-  lA.y[k] += acc[1];
-  lB.x[k] += acc[2];
-  lB.y[k] += acc[3];
-  lB.ux[k] += acc[4];
-  lB.uy[k] += acc[5];
-  lB.uz[k] += acc[6];
+  for (int dim = 0; dim < 2; ++dim) {
+    const int ai = inc[dim] < 0 ? -inc[dim] : inc[dim];
+    const double m1 = (double)(-(inc[dim] - ai)) * 0.5, m2 = (double)(-ai + 1), m3 = (double)(inc[dim] + ai) * 0.5;
+    const double ga1 = m1 * gds[dim][0] + m2 * gds[dim][1] + m3 * gds[dim][2];
+    const double ga2 = m1 * gds[dim][1] + m2 * gds[dim][2] + m3 * gds[dim][3];
+    const double ga3 = m1 * gds[dim][2] + m2 * gds[dim][3] + m3 * gds[dim][4];
+    const double h1 = dh1[dim], h = dh[dim];
+    gpos1[dim] = d_delx * (-(0.5 - h1) * ga1 - 2.0 * h1 * ga2 + (0.5 + h1) * ga3);
+    const double g1 = gs0[dim][1] - gds[dim][1], g2 = gs0[dim][2] - gds[dim][2], g3 = gs0[dim][3] - gds[dim][3];
+    gpos0[dim] = d_delx * (-(0.5 - h) * g1 - 2.0 * h * g2 + (0.5 + h) * g3);
+  }
+  // gvz = uz / gamma
+  const double ggv = q * phiz;
+  const double t3 = gmi * gmi * gmi * ic2 * uz;
+  lA.x[k] += gpos0[0];
+  lA.y[k] += gpos0[1];
+  lB.x[k] += gpos1[0];
+  lB.y[k] += gpos1[1];
+  lB.ux[k] += ggv * (-t3 * ux);
+  lB.uy[k] += ggv * (-t3 * uy);
+  lB.uz[k] += ggv * (gmi - t3 * uz);
 }
 
-// ---- the push's Jacobian: inputs (ux, uy, uz, bpx, bpy, bpz, epx, epy, epz) ----
-__global__ void k_adj_push(Dev2D d, const double* tmp, Parts64 lA, Parts64 lB, double* ltmp) {
+// ---- the push's adjoint: inputs (x, y, ux, uy, uz) and the cell-centred fields tmp ----
+// Forward (2d/common/particle.f90:48-179): gather B, E at the old position (quadratic
+// splines on the cell-centred tmp), u1 = u + f1 E, gam = sqrt(c^2 + u1^2),
+// w = u1 + (f1 / gam) u1 x B, u2 = u1 + f2 / (gam + f1^2 B^2 / gam) w x B, u' = u2 + f1 E,
+// x' = x + dt u'_x / gamma', y' = y + dt u'_y / gamma'.  Reverse sweep through these lines;
+// the field adjoints (B, E at the particle) spread back over the 3 x 3 tmp nodes with the
+// same spline weights: summed per (cell, component, node) over the block's particles in
+// shared memory, then one FP64 atomic per (cell, component, node) of the block.
+constexpr int AP_T = 128;
+__global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const double* tmp, Parts64 lA, Parts64 lB,
+                                                   double* ltmp) {
+  __shared__ double slf[6][AP_T + 1];
+  __shared__ double sw[6][AP_T + 1];
   const Grid2D g = d.g;
   const int row = blockIdx.y;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= d.np2[row]) return;
+  const int s0b = blockIdx.x * AP_T;
+  const int np = d.np2[row];
+  if (s0b >= np) return;  // uniform across the block
+  const int tid = threadIdx.x;
+  const int s = s0b + tid;
   const int isp = row / g.ny, jj = row - isp * g.ny;
   const int* ccr = d.cc + (size_t)row * (g.nx + 1);
-  const int cx = cell_of(ccr, g.nx, s);
-  const size_t k = (size_t)row * d.cap + s;
   const int tw = g.nx + 2;
   const size_t n = (size_t)tw * (g.ny + 2);
-  const double dxi = d.ph.p_d_delx, delt = d.ph.delt, c = d.ph.c;
-  const double fac1 = d.ph.q[isp] / d.ph.r[isp] * 0.5 * delt;
-  const double txxx = fac1 * fac1;
-  const double fac2 = d.ph.q[isp] * delt / d.ph.r[isp];
-  const int iabs = g.nxgs + cx, jabs = g.nygs + jj;
-  const double x = d.A.x[k], y = d.A.y[k];
-  const double hx = x * dxi - 0.5 - (double)iabs, hy = y * dxi - 0.5 - (double)jabs;
-  const double sx[3] = {0.5 * (0.5 - hx) * (0.5 - hx), 0.75 - hx * hx, 0.5 * (0.5 + hx) * (0.5 + hx)};
-  const double sy[3] = {0.5 * (0.5 - hy) * (0.5 - hy), 0.75 - hy * hy, 0.5 * (0.5 + hy) * (0.5 + hy)};
-  const double dsx[3] = {-(0.5 - hx) * dxi, -2.0 * hx * dxi, (0.5 + hx) * dxi};
-  const double dsy[3] = {-(0.5 - hy) * dxi, -2.0 * hy * dxi, (0.5 + hy) * dxi};
-  // tmp node (a, b) of the particle's cell: local cell (cx - 1 + a, jj - 1 + b) -> index (cx + a, jj + b)
-  double fv[6], fdx[6], fdy[6];
+  if (s < np) {
+    const int cx = cell_of(ccr, g.nx, s);
+    const size_t k = (size_t)row * d.cap + s;
+    const double dxi = d.ph.p_d_delx, delt = d.ph.delt, c = d.ph.c;
+    const double fac1 = d.ph.q[isp] / d.ph.r[isp] * 0.5 * delt;
+    const double txxx = fac1 * fac1;
+    const double fac2 = d.ph.q[isp] * delt / d.ph.r[isp];
+    const int iabs = g.nxgs + cx, jabs = g.nygs + jj;
+    const double x = d.A.x[k], y = d.A.y[k];
+    const double hx = x * dxi - 0.5 - (double)iabs, hy = y * dxi - 0.5 - (double)jabs;
+    const double sx[3] = {0.5 * (0.5 - hx) * (0.5 - hx), 0.75 - hx * hx, 0.5 * (0.5 + hx) * (0.5 + hx)};
+    const double sy[3] = {0.5 * (0.5 - hy) * (0.5 - hy), 0.75 - hy * hy, 0.5 * (0.5 + hy) * (0.5 + hy)};
+    const double dsx[3] = {-(0.5 - hx) * dxi, -2.0 * hx * dxi, (0.5 + hx) * dxi};
+    const double dsy[3] = {-(0.5 - hy) * dxi, -2.0 * hy * dxi, (0.5 + hy) * dxi};
+    // tmp node (a, b) of the particle's cell: local cell (cx - 1 + a, jj - 1 + b) -> index (cx + a, jj + b)
+    double fv[6], fdx[6], fdy[6];
 #pragma unroll
-  for (int m = 0; m < 6; ++m) {
-    double v = 0.0, vx = 0.0, vy = 0.0;
+    for (int m = 0; m < 6; ++m) {
+      double v = 0.0, vx = 0.0, vy = 0.0;
 #pragma unroll
-    for (int b = 0; b < 3; ++b)
+      for (int b = 0; b < 3; ++b) {
+        double r = 0.0, rx = 0.0;
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const double t = tmp[(size_t)m * n + (size_t)(jj + b) * tw + (cx + a)];
-        v += t * sx[a] * sy[b];
-        vx += t * dsx[a] * sy[b];
-        vy += t * sx[a] * dsy[b];
+        for (int a = 0; a < 3; ++a) {
+          const double t = tmp[(size_t)m * n + (size_t)(jj + b) * tw + (cx + a)];
+          r += t * sx[a];
+          rx += t * dsx[a];
+        }
+        v += r * sy[b];
+        vx += rx * sy[b];
+        vy += r * dsy[b];
       }
-    fv[m] = v;
-    fdx[m] = vx;
-    fdy[m] = vy;
+      fv[m] = v;
+      fdx[m] = vx;
+      fdy[m] = vy;
+    }
+    const double B[3] = {fv[0], fv[1], fv[2]};
+    const double ux = d.A.ux[k], uy = d.A.uy[k], uz = d.A.uz[k];
+    // forward values
+    const double u1[3] = {ux + fac1 * fv[3], uy + fac1 * fv[4], uz + fac1 * fv[5]};
+    const double gam = sqrt(c * c + (u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2]));
+    const double igam = 1.0 / gam;
+    const double fac1r = fac1 * igam;
+    const double Bsq = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+    const double D = gam + txxx * (Bsq * igam);
+    const double fac2r = fac2 / D;
+    const double u1xB[3] = {u1[1] * B[2] - u1[2] * B[1], u1[2] * B[0] - u1[0] * B[2], u1[0] * B[1] - u1[1] * B[0]};
+    const double w[3] = {u1[0] + fac1r * u1xB[0], u1[1] + fac1r * u1xB[1], u1[2] + fac1r * u1xB[2]};
+    const double wxB[3] = {w[1] * B[2] - w[2] * B[1], w[2] * B[0] - w[0] * B[2], w[0] * B[1] - w[1] * B[0]};
+    const double gv[3] = {u1[0] + fac2r * wxB[0] + fac1 * fv[3], u1[1] + fac2r * wxB[1] + fac1 * fv[4],
+                          u1[2] + fac2r * wxB[2] + fac1 * fv[5]};
+    const double gi = 1.0 / sqrt(1.0 + (1.0 / (c * c)) * (gv[0] * gv[0] + gv[1] * gv[1] + gv[2] * gv[2]));
+    // reverse
+    const double lx = lB.x[k], ly = lB.y[k];
+    const double gib = delt * (lx * gv[0] + ly * gv[1]);
+    const double kk = gi * gi * gi * gib / (c * c);
+    double gb[3] = {lB.ux[k] + delt * gi * lx - kk * gv[0], lB.uy[k] + delt * gi * ly - kk * gv[1],
+                    lB.uz[k] - kk * gv[2]};  // adjoint of u' (= of u2)
+    double Eb[3] = {fac1 * gb[0], fac1 * gb[1], fac1 * gb[2]};
+    const double f2rb = gb[0] * wxB[0] + gb[1] * wxB[1] + gb[2] * wxB[2];
+    const double wb[3] = {fac2r * (B[1] * gb[2] - B[2] * gb[1]), fac2r * (B[2] * gb[0] - B[0] * gb[2]),
+                          fac2r * (B[0] * gb[1] - B[1] * gb[0])};
+    double Bb[3] = {fac2r * (gb[1] * w[2] - gb[2] * w[1]), fac2r * (gb[2] * w[0] - gb[0] * w[2]),
+                    fac2r * (gb[0] * w[1] - gb[1] * w[0])};
+    double u1b[3] = {gb[0] + wb[0] + fac1r * (B[1] * wb[2] - B[2] * wb[1]),
+                     gb[1] + wb[1] + fac1r * (B[2] * wb[0] - B[0] * wb[2]),
+                     gb[2] + wb[2] + fac1r * (B[0] * wb[1] - B[1] * wb[0])};
+    Bb[0] += fac1r * (wb[1] * u1[2] - wb[2] * u1[1]);
+    Bb[1] += fac1r * (wb[2] * u1[0] - wb[0] * u1[2]);
+    Bb[2] += fac1r * (wb[0] * u1[1] - wb[1] * u1[0]);
+    const double f1rb = wb[0] * u1xB[0] + wb[1] * u1xB[1] + wb[2] * u1xB[2];
+    const double Db = -(fac2r / D) * f2rb;
+    const double bsqb = Db * txxx * igam;
+    Bb[0] += 2.0 * bsqb * B[0];
+    Bb[1] += 2.0 * bsqb * B[1];
+    Bb[2] += 2.0 * bsqb * B[2];
+    const double igb = Db * txxx * Bsq + fac1 * f1rb;
+    const double gamb = Db - igam * igam * igb;
+    u1b[0] += gamb * igam * u1[0];
+    u1b[1] += gamb * igam * u1[1];
+    u1b[2] += gamb * igam * u1[2];
+    Eb[0] += fac1 * u1b[0];
+    Eb[1] += fac1 * u1b[1];
+    Eb[2] += fac1 * u1b[2];
+    const double lf[6] = {Bb[0], Bb[1], Bb[2], Eb[0], Eb[1], Eb[2]};
+    double lxa = lx, lya = ly;
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      lxa += lf[m] * fdx[m];
+      lya += lf[m] * fdy[m];
+      slf[m][tid] = lf[m];
+    }
+    lA.x[k] += lxa;
+    lA.y[k] += lya;
+    lA.ux[k] += u1b[0];
+    lA.uy[k] += u1b[1];
+    lA.uz[k] += u1b[2];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      sw[a][tid] = sx[a];
+      sw[3 + a][tid] = sy[a];
+    }
   }
-  using D9 = Dual<9>;
-  const D9 bpx = dvar<9>(fv[0], 3), bpy = dvar<9>(fv[1], 4), bpz = dvar<9>(fv[2], 5);
-  const D9 epx = dvar<9>(fv[3], 6), epy = dvar<9>(fv[4], 7), epz = dvar<9>(fv[5], 8);
-  D9 uvm1 = dvar<9>(d.A.ux[k], 0) + fac1 * epx;
-  D9 uvm2 = dvar<9>(d.A.uy[k], 1) + fac1 * epy;
-  D9 uvm3 = dvar<9>(d.A.uz[k], 2) + fac1 * epz;
-  const D9 gam = dsqrt(c * c + (uvm1 * uvm1 + uvm2 * uvm2 + uvm3 * uvm3));
-  const D9 igam = dconst<9>(1.0) / gam;
-  const D9 fac1r = fac1 * igam;
-  const D9 fac2r = dconst<9>(fac2) / (gam + txxx * ((bpx * bpx + bpy * bpy + bpz * bpz) * igam));
-  const D9 uvm4 = uvm1 + fac1r * (uvm2 * bpz - uvm3 * bpy);
-  const D9 uvm5 = uvm2 + fac1r * (uvm3 * bpx - uvm1 * bpz);
-  const D9 uvm6 = uvm3 + fac1r * (uvm1 * bpy - uvm2 * bpx);
-  uvm1 = uvm1 + fac2r * (uvm5 * bpz - uvm6 * bpy);
-  uvm2 = uvm2 + fac2r * (uvm6 * bpx - uvm4 * bpz);
-  uvm3 = uvm3 + fac2r * (uvm4 * bpy - uvm5 * bpx);
-  const D9 g3 = uvm1 + fac1 * epx, g4 = uvm2 + fac1 * epy, g5 = uvm3 + fac1 * epz;
-  const D9 gi = dconst<9>(1.0) / dsqrt(1.0 + (1.0 / (c * c)) * (g3 * g3 + g4 * g4 + g5 * g5));
-  const D9 mx = (delt * g3) * gi, my = (delt * g4) * gi;  // x' - x, y' - y
-  const double lx = lB.x[k], ly = lB.y[k], lux = lB.ux[k], luy = lB.uy[k], luz = lB.uz[k];
-  double lin[9];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) lin[i] = lx * mx.d[i] + ly * my.d[i] + lux * g3.d[i] + luy * g4.d[i] + luz * g5.d[i];
-  double lxa = lx, lya = ly;
-#pragma unroll
-  for (int m = 0; m < 6; ++m) {
-    lxa += lin[3 + m] * fdx[m];
-    lya += lin[3 + m] * fdy[m];
-  }
-  lA.x[k] += lxa;
-  lA.y[k] += lya;
-  lA.ux[k] += lin[0];
-  lA.uy[k] += lin[1];
-  lA.uz[k] += lin[2];
-#pragma unroll
-  for (int m = 0; m < 6; ++m) {
-    const double lf = lin[3 + m];
-    if (lf == 0.0) continue;
-#pragma unroll
-    for (int b = 0; b < 3; ++b)
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-        atomicAdd(ltmp + (size_t)m * n + (size_t)(jj + b) * tw + (cx + a), lf * sx[a] * sy[b]);
+  __syncthreads();
+  // per (cell, component, node) sums over the block's particles of each cell
+  const int last = min(s0b + AP_T, np) - 1;
+  const int c_first = cell_of(ccr, g.nx, s0b), c_last = cell_of(ccr, g.nx, last);
+  const int nent = (c_last - c_first + 1) * 54;
+  for (int e = tid; e < nent; e += AP_T) {
+    const int cc = c_first + e / 54, r = e - (e / 54) * 54;
+    const int m = r / 9, ab = r - m * 9, b = ab / 3, a = ab - b * 3;
+    const int p0 = max(ccr[cc], s0b) - s0b, p1 = min(ccr[cc + 1], last + 1) - s0b;
+    double acc = 0.0;
+    for (int p = p0; p < p1; ++p) acc += slf[m][p] * sw[a][p] * sw[3 + b][p];
+    if (acc != 0.0) atomicAdd(ltmp + (size_t)m * n + (size_t)(jj + b) * tw + (cc + a), acc);
   }
 }
 
