@@ -13,6 +13,7 @@ the FP64 path is timed beside it on the same workload.  Prints one JSON line.
 OpenMP over all host cores) on the same metric instead.
 """
 import argparse
+import dataclasses
 import json
 import os
 import subprocess
@@ -261,6 +262,41 @@ def time_path3d(steps, rank, torch, dist, world, precision="fp64", n=256):
             "cg_iterations": cg, "moments": moments}
 
 
+def time_adjoint(steps, every, rank, dist, n=512):
+    """The discrete adjoint on the 512^2 Weibel workload (32 ppc/species, drift 0.3c, u_th
+    0.05c, 64 Bz seed modes of amplitude ~1e-4): the gradient of the final magnetic energy
+    with respect to drift, u_th and the seed amplitudes through the checkpointed reverse
+    sweep, its cost against the plain FP64 forward of the same steps, and one central
+    difference (drift, h = 1e-6)."""
+    import numpy as np
+    from wumingpic_gb300.adjoint import FieldEnergyProblem, SeedModes
+    from wumingpic_gb300.loader import config_weibel2d
+    p = dataclasses.replace(config_weibel2d("cfg4", seed=20261204 + 7919 * rank), nx=n, ny=n)
+    modes = SeedModes.lowest(p.nx, p.ny, 64)
+    amps = 1e-4 * np.random.default_rng(3 + rank).standard_normal(modes.count)
+    prob = FieldEnergyProblem(p, steps, every, modes, which="B", cg_rtol=1e-13)
+    drift, u_th, h = 0.3, 0.05, 1e-6
+    prob.value(drift, u_th, amps)
+    t_fwd = prob.timings["forward"]
+    val = prob.forward(drift, u_th, amps)
+    g_drift, g_uth, g_amps = prob.backward()
+    t_rec, t_rev = prob.timings["record"], prob.timings["reverse"]
+    fd = (prob.value(drift + h, u_th, amps) - prob.value(drift - h, u_th, amps)) / (2 * h)
+    npart = prob.sim.num_particles()
+    prob.close()
+    fwd_ms, _ = rank_totals(t_fwd * 1e3, npart, dist, "cuda")
+    rec_ms, _ = rank_totals(t_rec * 1e3, npart, dist, "cuda")
+    rev_ms, _ = rank_totals(t_rev * 1e3, npart, dist, "cuda")
+    return {"workload": f"2D Weibel {n}^2 cells, 32 ppc/species ({npart} particles), drift +-0.3c, u_th 0.05c, "
+                        f"64 Bz seed modes; L = final magnetic energy after {steps} steps",
+            "steps": steps, "checkpoint_every": every, "dtype": "f64", "cg_rtol": 1e-13,
+            "forward_ms": fwd_ms, "record_ms": rec_ms, "reverse_ms": rev_ms,
+            "cost_over_forward": (rec_ms + rev_ms) / fwd_ms, "reverse_over_forward": rev_ms / fwd_ms, "L": val,
+            "grad": {"drift": g_drift, "u_th": g_uth, "amps_norm": float(np.linalg.norm(g_amps))},
+            "fd_check": {"param": "drift", "h": h, "fd": fd, "adjoint": g_drift,
+                         "rel_err": abs(g_drift - fd) / abs(fd) if fd else None}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -276,6 +312,11 @@ def main():
     ap.add_argument("--grid3d", type=int, default=256, help="cells per edge of the 3D legs")
     ap.add_argument("--only-3d", action="store_true",
                     help="run only the 3D legs and print them (a profiling aid, not the bench line)")
+    ap.add_argument("--adjoint-steps", type=int, default=200,
+                    help="steps of the adjoint leg on the 512^2 workload (0 = skip)")
+    ap.add_argument("--adjoint-every", type=int, default=20, help="checkpoint interval of the adjoint leg")
+    ap.add_argument("--adjoint-grid", type=int, default=512, help="cells per edge of the adjoint leg")
+    ap.add_argument("--only-adjoint", action="store_true", help="run the adjoint leg alone and print its JSON")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--stages", action="store_true", help="print the per-stage breakdown to stderr")
@@ -294,6 +335,14 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     from wumingpic_gb300 import _lib
+
+    if args.only_adjoint:
+        out = time_adjoint(args.adjoint_steps, args.adjoint_every, rank, dist, n=args.adjoint_grid)
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
 
     p = config(args.config)
     hbm_peak, hbm_src = measured_hbm_peak()
@@ -362,6 +411,10 @@ def main():
         if fp64_3d:
             mixed_3d["mixed_over_fp64"] = mixed_3d["value"] / fp64_3d["value"]
 
+    adjoint = None
+    if args.adjoint_steps > 0:
+        adjoint = time_adjoint(args.adjoint_steps, args.adjoint_every, rank, dist, n=args.adjoint_grid)
+
     base = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -376,7 +429,8 @@ def main():
                 "path": "mixed: integer cell + FP32 offset, FP32 push/gather/deposition, FP64 fields and CG",
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks, "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()},
-                "moments": moments, "fp64_path": fp64, "fp64_3d_path": fp64_3d, "mixed_3d_path": mixed_3d}
+                "moments": moments, "fp64_path": fp64, "fp64_3d_path": fp64_3d, "mixed_3d_path": mixed_3d,
+                "adjoint": adjoint}
         print(json.dumps(line), flush=True)
         if args.stages:
             for k, (t, n) in stages.items():

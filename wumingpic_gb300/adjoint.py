@@ -24,6 +24,7 @@ over the per-particle and per-cell adjoints:
 """
 import dataclasses
 import math
+import time
 
 import numpy as np
 
@@ -136,6 +137,7 @@ class FieldEnergyProblem:
         self.cg_rtol, self.cg_ite_max = cg_rtol, cg_ite_max
         self.sim = None
         self._init = None
+        self.timings = {}  # seconds of the last value / record / reverse calls (synchronous C calls)
 
     def close(self):
         if self.sim is not None:
@@ -164,14 +166,18 @@ class FieldEnergyProblem:
     def value(self, drift, u_th, amps=None):
         """L without recording (the forward alone, for finite differences and timing)."""
         g = self.load(drift, u_th, amps)
+        t0 = time.perf_counter()
         g.step(self.nsteps)
+        self.timings["forward"] = time.perf_counter() - t0
         return field_energy(g.get_fields(), self.which)[0]
 
     def forward(self, drift, u_th, amps=None):
         g = self.load(drift, u_th, amps)
         st = g.get_state()
         self._init = (float(drift), float(u_th), st.up[2:5].copy(), st.up[5].copy(), st.np2.copy())
+        t0 = time.perf_counter()
         g.adjoint_record(self.nsteps, self.every)
+        self.timings["record"] = time.perf_counter() - t0
         val, self._lam = field_energy(g.get_fields(), self.which)
         return val
 
@@ -179,7 +185,9 @@ class FieldEnergyProblem:
         if self._init is None:
             raise RuntimeError("backward before forward")
         drift, u_th, u0, ids, np2 = self._init
+        t0 = time.perf_counter()
         lup, luf = self.sim.adjoint_reverse(self._lam * scale)
+        self.timings["reverse"] = time.perf_counter() - t0
         valid, s, n = electron_parameters(u0, ids, np2, drift, u_th, self.p.drift_axis)
         lu = np.where(valid[None], lup[2:5, :, :, 1], 0.0)
         g_drift = float((s * lu[self.p.drift_axis]).sum())
