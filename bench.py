@@ -262,6 +262,48 @@ def time_path3d(steps, rank, torch, dist, world, precision="fp64", n=256):
             "cg_iterations": cg, "moments": moments}
 
 
+def time_reconnection(steps, rank, torch, dist, ny=4096, nx=2048):
+    """The reconnection configuration: a Harris sheet between conducting walls in x (2048
+    cells) and periodic in y (4096 cells; the reference's orientation), 32 ppc/species at
+    the sheet centre + 6 background, m_i/m_e 25, omega_ce/omega_pe 0.5, T_i/T_e 5, sheet
+    half-width 0.5 c/omega_pi, 10 % X-point perturbation.  Mixed and FP64 paths from the
+    same host-loaded state, each with one warm-up step and `steps` timed steps; energies
+    compared after the same number of steps."""
+    from wumingpic_gb300.loader import config_harris2d, load_harris2d
+    from wumingpic_gb300.pic2d import Pic2D
+    p = dataclasses.replace(config_harris2d("cfg3", seed=20261205 + 7919 * rank), nx=nx, ny=ny)
+    t0 = time.perf_counter()
+    st = load_harris2d(p)
+    load_s = time.perf_counter() - t0
+    out = {"workload": f"Harris sheet {ny} (periodic y) x {nx} (walls in x) cells, {p.ncs}+{p.nbg} ppc/species, "
+                       f"{p.n_particles} particles, m_i/m_e 25, wce/wpe 0.5, Ti/Te 5, c*dt/dx=0.5",
+           "host_load_s": load_s}
+    energies = {}
+    for precision in ("mixed", "fp64"):
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        g = Pic2D(p, precision=precision, stream=stream.cuda_stream)
+        g.put_state(st)
+        g.step(1)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.step(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms, ntotal = rank_totals(e0.elapsed_time(e1), g.num_particles(), dist, "cuda")
+        energies[precision] = g.energy()
+        out[precision] = {"value": ntotal * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+                          "steps": steps, "warmup": 1, "cg_iterations": [int(x) for x in g.cg_iters()]}
+        g.close()
+    em, ed = energies["mixed"], energies["fp64"]
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["energy_rel_diff_mixed_vs_fp64"] = [float(abs(a - b) / abs(b)) if b else None for a, b in zip(em, ed)]
+    return out
+
+
 def time_adjoint(steps, every, rank, dist, n=512):
     """The discrete adjoint on the 512^2 Weibel workload (32 ppc/species, drift 0.3c, u_th
     0.05c, 64 Bz seed modes of amplitude ~1e-4): the gradient of the final magnetic energy
@@ -283,6 +325,8 @@ def time_adjoint(steps, every, rank, dist, n=512):
     t_rec, t_rev = prob.timings["record"], prob.timings["reverse"]
     fd = (prob.value(drift + h, u_th, amps) - prob.value(drift - h, u_th, amps)) / (2 * h)
     npart = prob.sim.num_particles()
+    val_mixed = prob.value_mixed(drift, u_th, amps)
+    mix_ms, _ = rank_totals(prob.timings["forward_mixed"] * 1e3, npart, dist, "cuda")
     prob.close()
     fwd_ms, _ = rank_totals(t_fwd * 1e3, npart, dist, "cuda")
     rec_ms, _ = rank_totals(t_rec * 1e3, npart, dist, "cuda")
@@ -292,6 +336,8 @@ def time_adjoint(steps, every, rank, dist, n=512):
             "steps": steps, "checkpoint_every": every, "dtype": "f64", "cg_rtol": 1e-13,
             "forward_ms": fwd_ms, "record_ms": rec_ms, "reverse_ms": rev_ms,
             "cost_over_forward": (rec_ms + rev_ms) / fwd_ms, "reverse_over_forward": rev_ms / fwd_ms, "L": val,
+            "mixed_forward": {"L": val_mixed, "rel_diff_vs_fp64": abs(val_mixed - val) / abs(val),
+                              "forward_ms": mix_ms, "fp64_over_mixed_time": fwd_ms / mix_ms},
             "grad": {"drift": g_drift, "u_th": g_uth, "amps_norm": float(np.linalg.norm(g_amps))},
             "fd_check": {"param": "drift", "h": h, "fd": fd, "adjoint": g_drift,
                          "rel_err": abs(g_drift - fd) / abs(fd) if fd else None}}
@@ -317,6 +363,10 @@ def main():
     ap.add_argument("--adjoint-every", type=int, default=20, help="checkpoint interval of the adjoint leg")
     ap.add_argument("--adjoint-grid", type=int, default=512, help="cells per edge of the adjoint leg")
     ap.add_argument("--only-adjoint", action="store_true", help="run the adjoint leg alone and print its JSON")
+    ap.add_argument("--reconnection-steps", type=int, default=3,
+                    help="timed steps of each path on the Harris-sheet workload (0 = skip)")
+    ap.add_argument("--reconnection-grid", default="4096x2048", help="periodic y x walled x cells")
+    ap.add_argument("--only-reconnection", action="store_true", help="run the reconnection leg alone")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--stages", action="store_true", help="print the per-stage breakdown to stderr")
@@ -335,6 +385,15 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     from wumingpic_gb300 import _lib
+
+    rny, rnx = (int(v) for v in args.reconnection_grid.lower().split("x"))
+    if args.only_reconnection:
+        out = time_reconnection(args.reconnection_steps, rank, torch, dist, ny=rny, nx=rnx)
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
 
     if args.only_adjoint:
         out = time_adjoint(args.adjoint_steps, args.adjoint_every, rank, dist, n=args.adjoint_grid)
@@ -411,6 +470,10 @@ def main():
         if fp64_3d:
             mixed_3d["mixed_over_fp64"] = mixed_3d["value"] / fp64_3d["value"]
 
+    reconnection = None
+    if args.reconnection_steps > 0:
+        reconnection = time_reconnection(args.reconnection_steps, rank, torch, dist, ny=rny, nx=rnx)
+
     adjoint = None
     if args.adjoint_steps > 0:
         adjoint = time_adjoint(args.adjoint_steps, args.adjoint_every, rank, dist, n=args.adjoint_grid)
@@ -430,7 +493,7 @@ def main():
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks, "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()},
                 "moments": moments, "fp64_path": fp64, "fp64_3d_path": fp64_3d, "mixed_3d_path": mixed_3d,
-                "adjoint": adjoint}
+                "reconnection": reconnection, "adjoint": adjoint}
         print(json.dumps(line), flush=True)
         if args.stages:
             for k, (t, n) in stages.items():

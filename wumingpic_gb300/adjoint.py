@@ -140,9 +140,11 @@ class FieldEnergyProblem:
         self.timings = {}  # seconds of the last value / record / reverse calls (synchronous C calls)
 
     def close(self):
-        if self.sim is not None:
-            self.sim.close()
-            self.sim = None
+        for name in ("sim", "_mixed"):
+            g = getattr(self, name, None)
+            if g is not None:
+                g.close()
+                setattr(self, name, None)
 
     def _context(self):
         if self.sim is None:
@@ -169,6 +171,25 @@ class FieldEnergyProblem:
         t0 = time.perf_counter()
         g.step(self.nsteps)
         self.timings["forward"] = time.perf_counter() - t0
+        return field_energy(g.get_fields(), self.which)[0]
+
+    def value_mixed(self, drift, u_th, amps=None):
+        """L from the mixed-precision path (integer cell + FP32 offset, FP32 push and deposit,
+        FP64 fields) on the same plasma: the forward the FP64 adjoint is the reference for."""
+        if getattr(self, "_mixed", None) is None:
+            self._mixed = Pic2D(self.p, precision="mixed")
+            self._mixed.cg_tolerance(self.cg_rtol, self.cg_ite_max)
+        g = self._mixed
+        g.p = dataclasses.replace(self.p, drift=float(drift), u_the=float(u_th))
+        g.load_weibel()
+        if self.modes is not None and amps is not None and self.modes.count:
+            uf = g.get_fields()
+            core = np.zeros((6, self.p.nx, self.p.ny))
+            core[self.modes.comp] = self.modes.field(amps)
+            g.put_fields(uf + wrap_ghosts(core))
+        t0 = time.perf_counter()
+        g.step(self.nsteps)
+        self.timings["forward_mixed"] = time.perf_counter() - t0
         return field_energy(g.get_fields(), self.which)[0]
 
     def forward(self, drift, u_th, amps=None):

@@ -170,6 +170,146 @@ def config_weibel2d(size="small", seed=12345):
     return Plasma2D(nx=16, ny=12, ppc=4, drift=0.5, u_the=0.05, seed=seed)
 
 
+@dataclass
+class Harris2D(Plasma2D):
+    """The reconnection driver's Harris current sheet (2d/proj/reconnection/app.f90:260-346,
+    360-450): conducting walls in x, periodic in y, B_y = b0 tanh((x - x0) / lcs) with a
+    localised X-point perturbation of relative amplitude e1, density ncs sech^2 + nbg
+    particles per cell, drifting Maxwellians carrying the sheet current along z.
+
+    Derived as the driver does: Debye length = dx, v_te = sqrt(rtemp) c / (sqrt(1 + rtemp)
+    alpha) (pressure balance), v_ti = v_te sqrt(1 / r_i) / sqrt(rtemp), omega_pe = v_te /
+    (dx sqrt 2), omega_ce = omega_pe / alpha, q from n0 = nbg + ncs, b0 = r_i c / q_i
+    omega_ci, lcs in units of c / omega_pi.  Every row holds nbg (nx - 1) + int(2 ncs lcs)
+    particles per species: nbg (nx - 3) uniform between the walls, the rest the sheet."""
+    alpha: float = 2.0            # omega_pe / omega_ce
+    rtemp: float = 0.2            # T_e / T_i
+    lcs: float = 0.5              # sheet half-thickness in c / omega_pi
+    nbg: int = 6                  # background particles per cell per species
+    ncs: int = 32                 # sheet particles per cell per species at the centre
+    e1: float = 0.1               # X-point perturbation B1 / B0 (the driver's constant is 0.12)
+    bc: str = "reconnection"
+    drift: float = 0.0
+    u_the: float = 0.0
+
+    def __post_init__(self):
+        self.ppc = self.nbg + self.ncs  # n0 of the charge normalisation
+
+    def derived(self):
+        """(vte, vti, wpe, wpi, wge, wgi, q, b0, lcs in length units, x0, y0)"""
+        r = np.array([self.mass_ratio, 1.0])
+        c, dx = self.c, self.delx
+        vte = math.sqrt(self.rtemp) * c / (math.sqrt(1 + self.rtemp) * self.alpha)
+        vti = vte * math.sqrt(r[1] / r[0]) / math.sqrt(self.rtemp)
+        wpe = vte / dx / math.sqrt(2.0)
+        wpi = wpe * math.sqrt(r[1] / r[0])
+        wge = wpe / self.alpha
+        wgi = wge / self.mass_ratio
+        n0 = self.nbg + self.ncs
+        q = np.array([+math.sqrt(r[0] / (4 * PI * n0 / dx ** 2)) * wpi,
+                      -math.sqrt(r[1] / (4 * PI * n0 / dx ** 2)) * wpe])
+        b0 = r[0] * c / q[0] * wgi
+        lcs = self.lcs * c / wpi
+        x0 = 0.5 * (self.nxge + self.nxgs) * dx
+        y0 = 0.5 * (self.nyge - self.nygs) * dx
+        return dict(vte=vte, vti=vti, wpe=wpe, wpi=wpi, wge=wge, wgi=wgi, q=q, r=r, b0=b0, lcs=lcs, x0=x0, y0=y0)
+
+    def charges(self):
+        dv = self.derived()
+        return dv["q"], dv["r"]
+
+    @property
+    def n_row(self):
+        """particles per row per species (2d/proj/reconnection/app.f90:307, truncated)"""
+        return int(self.nbg * (self.nxge - self.nxgs) + self.ncs * 2 * self.derived()["lcs"])
+
+    @property
+    def np_cap(self):
+        return int(math.ceil(self.np_slack * self.n_row))
+
+    @property
+    def n_particles(self):
+        return self.n_row * self.ny * self.nsp
+
+
+def harris_fields(p: Harris2D, i, j):
+    """(bx, by) at the node (i dx, j dx) (2d/proj/reconnection/app.f90:375-378, 393-401)."""
+    dv = p.derived()
+    b0, lcs, x0, y0 = dv["b0"], dv["lcs"], dv["x0"], dv["y0"]
+    x, y = i * p.delx, j * p.delx
+    g = np.exp(-((x - x0) ** 2 + (y - y0) ** 2) / (2 * lcs) ** 2)
+    bx = +p.e1 * b0 * ((y - y0) / lcs) * g
+    by = b0 * np.tanh((x - x0) / lcs) - p.e1 * b0 * ((x - x0) / lcs) * g
+    return bx, by
+
+
+def harris_current(p: Harris2D, x, y):
+    """(jz, density) at particle positions (2d/proj/reconnection/app.f90:380-384)."""
+    dv = p.derived()
+    b0, lcs, x0, y0 = dv["b0"], dv["lcs"], dv["x0"], dv["y0"]
+    sech2 = np.cosh((x - x0) / lcs) ** (-2)
+    r2 = ((x - x0) ** 2 + (y - y0) ** 2) / (2 * lcs) ** 2
+    jz = b0 / (4 * PI * lcs) * sech2 - 2 * p.e1 * b0 / (4 * PI * lcs) * (1.0 - r2) * np.exp(-r2)
+    return jz, p.ncs * sech2 + p.nbg
+
+
+def load_harris2d(p: Harris2D) -> State2D:
+    """The Harris sheet of the reconnection driver (set_initial_condition,
+    2d/proj/reconnection/app.f90:360-450) from a seeded Philox stream, bucket-sorted as the
+    driver does after loading (app.f90:337-340)."""
+    rng = np.random.Generator(np.random.Philox(p.seed))
+    dv = p.derived()
+    st = empty_state2d(p)
+    nx, ny, dx = p.nx, p.ny, p.delx
+    n = p.n_row
+    ibg = p.nbg * (p.nxge - p.nxgs - 2)
+    jabs = (p.nygs + np.arange(ny))[:, None]
+    xs = np.empty((ny, n))
+    xs[:, :ibg] = (p.nxgs + 1) * dx + rng.random((ny, ibg)) * dx * (p.nxge - p.nxgs - 2)
+    r1 = (2.0 * rng.random((ny, n - ibg)) - 1.0) * math.tanh(0.5 * (p.nxge - p.nxgs - 2) * dx / dv["lcs"])
+    xs[:, ibg:] = dv["lcs"] * 0.5 * (np.log(1.0 + r1) - np.log(1.0 - r1)) + dv["x0"]
+    ys = jabs * dx + rng.random((ny, n)) * dx
+    # the driver's stable bucket sort by int(x) (ions and electrons share positions)
+    cell = np.trunc(xs).astype(np.int64) - p.nxgs
+    order = np.argsort(cell, axis=1, kind="stable")
+    xs = np.take_along_axis(xs, order, axis=1)
+    ys = np.take_along_axis(ys, order, axis=1)
+    cell = np.take_along_axis(cell, order, axis=1)
+    counts = np.bincount((np.arange(ny)[:, None] * nx + cell).ravel(), minlength=ny * nx).reshape(ny, nx)
+    cc = np.zeros((nx + 1, ny), np.int32)
+    cc[1:] = np.cumsum(counts, axis=1).T
+    jz, dens = harris_current(p, xs, ys)
+    f = (1.0 / ((1.0 + p.rtemp) * dv["q"][0]), p.rtemp / ((1.0 + p.rtemp) * dv["q"][1]))
+    sd = (dv["vti"] / math.sqrt(2.0), dv["vte"] / math.sqrt(2.0))
+    for isp in range(p.nsp):
+        st.up[0, :n, :, isp] = xs.T
+        st.up[1, :n, :, isp] = ys.T
+        u = rng.standard_normal((3, n, ny)) * sd[isp]
+        u[2] += (f[isp] * jz / dens).T
+        st.up[2:5, :n, :, isp] = u
+        pid = (np.arange(ny)[None, :] * n + np.arange(1, n + 1)[:, None]).astype(np.int64)
+        st.up[5, :n, :, isp] = (-pid).view(np.float64)
+        st.cumcnt[:, :, isp] = cc
+    st.np2[:, :] = n
+    i = np.arange(p.nxgs - 2, p.nxge + 3)[:, None]
+    j = np.arange(p.nygs - 2, p.nyge + 3)[None, :]
+    bx, by = harris_fields(p, i, j)
+    st.uf[0] = bx
+    st.uf[1] = by
+    st.gp[...] = st.up
+    return st
+
+
+def config_harris2d(size="small", seed=12345):
+    """'cfg3': 4096 x 2048 cells (2048 between the walls in x, 4096 periodic in y: the
+    reference's orientation), 32 ppc/species at the sheet centre + 6 background (0.2 n0),
+    m_i/m_e 25, omega_ce/omega_pe 0.5, T_i/T_e 5, sheet half-width 0.5 c/omega_pi, 10 %
+    perturbation; or a small case for tests."""
+    if size == "cfg3":
+        return Harris2D(nx=2048, ny=4096, ppc=38, mass_ratio=25.0, seed=seed, np_slack=1.25)
+    return Harris2D(nx=64, ny=48, ppc=20, mass_ratio=25.0, lcs=0.2, ncs=16, nbg=4, seed=seed, np_slack=1.5)
+
+
 # ---------------------------------------------------------------------------
 # 3D (3d/proj/weibel/app.f90 conventions: ndim = 7, (x, y, z, ux, uy, uz, id),
 # rows (j, k) of x-sorted particles, uf(6, nxgs-2:nxge+2, nys-2:nye+2, nzs-2:nze+2))
