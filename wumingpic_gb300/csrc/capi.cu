@@ -285,20 +285,20 @@ void do_migrate_sort(wpic_ctx* c) {
 }
 
 // Fixed-point scales of the mixed deposit for columns of at most maxdep slots.  One particle adds
-// at most vmax = max(|q| dx/dt, 2 |q| c) to a node; a thread flushes the sum of up to 16 particles
-// at once (|v s1| < 2^22 keeps the magic-number rounding exact), and at most 25 * nsp * maxdep
-// particles reach a node in one tile pass (|sum hi| < 2^30).  The current is rebuilt every step,
-// so the scales may change with the layout.
+// at most vmax = max(|q| dx/dt, 2 |q| c) to a node; a thread flushes the sum of up to MIX_FLUSH
+// particles at once (|v s1| <= 2^21 keeps the magic-number rounding exact), and at most
+// 25 * nsp * maxdep particles reach a node in one tile pass (|sum hi| < 2^30).  The current is
+// rebuilt every step, so the scales may change with the layout.
 int mix_set_scales(wpic_ctx* c, int maxdep) {
   Mix2D& m = c->d.m;
   const double vmax = c->mix_vmax;
   const int nsp = c->prm.nsp;
-  double s1 = std::ldexp(1.0, 17) / vmax;
+  double s1 = std::ldexp(1.0, 21) / (MIX_FLUSH * vmax);
   const double lim = std::ldexp(1.0, 30) / (25.0 * nsp * maxdep * vmax);
   if (lim < s1) s1 = lim;
   s1 = std::ldexp(1.0, (int)std::floor(std::log2(s1)));
-  // lo plane: each flush adds |lo| <= 2^14; a node takes at most 25 * ceil(nsp * maxdep / 16) flushes
-  const double nflush = 25.0 * std::ceil((double)nsp * maxdep / 16.0) + 25.0;
+  // lo plane: each flush adds |lo| <= 2^14; a node takes at most 25 * ceil(nsp * maxdep / MIX_FLUSH) flushes
+  const double nflush = 25.0 * std::ceil((double)nsp * maxdep / MIX_FLUSH) + 25.0;
   if (!(s1 > 0.0) || s1 > std::ldexp(1.0, 100) || nflush * 16384.0 >= std::ldexp(1.0, 31)) return WPIC_BAD_ARGUMENT;
   m.fx_s1 = (float)s1;
   m.fx_is1f = (float)(1.0 / s1);

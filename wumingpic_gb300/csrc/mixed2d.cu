@@ -12,7 +12,7 @@
 //  * each particle is pushed in place;
 //  * its Esirkepov current is added into the thread's registers, which hold
 //    the cell's full 5 x 5 x 3 stencil (every particle of the column shares the
-//    cell), and every 16 particles the registers are added into the tile's
+//    cell), and every MIX_FLUSH particles the registers are added into the tile's
 //    fixed-point current in shared memory (exact integer atomics);
 //  * the tile is added once into the global fixed-point current.
 // The periodic wraps of boundary_periodic__particle_x/_y are integer cell
@@ -41,7 +41,7 @@ constexpr int TT = MIX_TS + 2;      // cell-centred values per tile edge (cells 
 // Row pitch of the fixed-point current tile: the 32 lanes of a warp own cells of two
 // consecutive rows; a pitch of 16 (mod 32) words puts the two rows on disjoint banks.
 constexpr int JP = 48;
-constexpr int FLUSH_EVERY = 16;     // particles accumulated in registers between flushes
+constexpr int FLUSH_EVERY = MIX_FLUSH;  // particles accumulated in registers between flushes
 constexpr int PF = 8;               // particles in flight per push thread (shared-memory ring)
 constexpr int PF_BYTES = PF * 7 * MIX_TC * 4;  // the key plane is not prefetched
 constexpr unsigned long long kSpinLimit = 1ull << 22;  // a few seconds at most
@@ -379,16 +379,26 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
     float dsx[5], dsy[5];
     shape_diff5(ox, nx_, incx, dsx);
     shape_diff5(oy, ny_, incy, dsy);
+    // the old-position shapes are zero at offsets -2 and +2: those terms are left out (the
+    // results are the same, a signed zero aside, which the fixed-point sums do not see)
     const float s0x[5] = {0.f, sx0, sx1, sx2, 0.f};
     const float s0y[5] = {0.f, sy0, sy1, sy2, 0.f};
     const float qg = qs * uz * ig;  // q * vz
+    const float hq = -0.5f * qdd, hg = 0.5f * qg, tg = third * qg;
     float wyq[5], wxq[5], zy[5], vy[5];
 #pragma unroll
     for (int e = 0; e < 5; ++e) {
-      wyq[e] = -qdd * (s0y[e] + 0.5f * dsy[e]);
-      wxq[e] = -qdd * (s0x[e] + 0.5f * dsx[e]);
-      zy[e] = qg * (s0y[e] + 0.5f * dsy[e]);
-      vy[e] = qg * (0.5f * s0y[e] + third * dsy[e]);
+      if (e == 0 || e == 4) {
+        wyq[e] = hq * dsy[e];
+        wxq[e] = hq * dsx[e];
+        zy[e] = hg * dsy[e];
+        vy[e] = tg * dsy[e];
+      } else {
+        wyq[e] = -qdd * (s0y[e] + 0.5f * dsy[e]);
+        wxq[e] = -qdd * (s0x[e] + 0.5f * dsx[e]);
+        zy[e] = qg * (s0y[e] + 0.5f * dsy[e]);
+        vy[e] = qg * (0.5f * s0y[e] + third * dsy[e]);
+      }
     }
     float px = 0.f, py = 0.f;
 #pragma unroll
@@ -404,7 +414,10 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
 #pragma unroll
     for (int j = 0; j < 5; ++j)
 #pragma unroll
-      for (int i = 0; i < 5; ++i) acc.jz[j][i] = fmaf(s0x[i], zy[j], fmaf(dsx[i], vy[j], acc.jz[j][i]));
+      for (int i = 0; i < 5; ++i) {
+        const float t = fmaf(dsx[i], vy[j], acc.jz[j][i]);
+        acc.jz[j][i] = (i == 0 || i == 4) ? t : fmaf(s0x[i], zy[j], t);
+      }
     if (++since == FLUSH_EVERY) {
       cell_flush(acc, jhi, jlo, lx, ly, fs1, fis1, fs2);
       since = 0;
