@@ -66,6 +66,10 @@ struct wpic_ctx {
     Parts64 A;
     int *cc, *np2;
     double *uf, *df;
+    // states of a recomputed segment also keep the step's pushed particles and permutation
+    Parts64 B{};
+    int *map = nullptr, *np2new = nullptr;
+    bool has_step = false;
   };
   bool adj_ready = false;
   Parts64 lA{}, lB{};
@@ -841,6 +845,38 @@ void adj_save(wpic_ctx* c, const wpic_ctx::AdjState& S) {
   cudaMemcpyAsync(S.df, d.df, sizeof(double) * 6 * (size_t)d.g.fplane, cudaMemcpyDeviceToDevice, c->stream);
 }
 
+// the pushed particles and the permutation of one step, kept for its adjoint
+int adj_alloc_step(wpic_ctx* c, wpic_ctx::AdjState& S) {
+  if (S.map) return WPIC_OK;
+  const Dev2D& d = c->d;
+  const size_t slots = (size_t)d.nrowjob * d.cap;
+  int st;
+  if ((st = dalloc(c, &S.B.x, slots)) || (st = dalloc(c, &S.B.y, slots)) || (st = dalloc(c, &S.B.ux, slots)) ||
+      (st = dalloc(c, &S.B.uy, slots)) || (st = dalloc(c, &S.B.uz, slots)) || (st = dalloc(c, &S.np2new, d.nrowjob)))
+    return st;
+  return dalloc(c, &S.map, slots);
+}
+
+// one periodic step (one_step's order) that keeps B after the push and the sort's permutation
+int adj_forward_step(wpic_ctx* c, wpic_ctx::AdjState& S) {
+  Dev2D& d = c->d;
+  const size_t slots = (size_t)d.nrowjob * d.cap;
+  do_push(c);
+  for (int q = 0; q < 5; ++q) {
+    double* const from[5] = {d.B.x, d.B.y, d.B.ux, d.B.uy, d.B.uz};
+    double* const to[5] = {S.B.x, S.B.y, S.B.ux, S.B.uy, S.B.uz};
+    cudaMemcpyAsync(to[q], from[q], slots * 8, cudaMemcpyDeviceToDevice, c->stream);
+  }
+  int st = do_field(c);
+  if (st) return st;
+  do_particle_x(c);
+  do_migrate_sort(c);
+  cudaMemcpyAsync(S.map, d.map, slots * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(S.np2new, d.np2new, (size_t)d.nrowjob * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
+  S.has_step = true;
+  return WPIC_OK;
+}
+
 void adj_load(wpic_ctx* c, const wpic_ctx::AdjState& S) {
   Dev2D& d = c->d;
   const size_t slots = (size_t)d.nrowjob * d.cap;
@@ -884,9 +920,32 @@ void adj_zero_parts(const Parts64& P, size_t n, cudaStream_t s) {
 
 // one step backwards: d holds the state before the step; lA, luf hold the adjoints of the
 // state after it and return those of the state before it
-int adj_step(wpic_ctx* c) {
+int adj_step(wpic_ctx* c, const wpic_ctx::AdjState* S) {
   Dev2D& d = c->d;
   const size_t slots = (size_t)d.nrowjob * d.cap;
+  if (S && S->has_step) {
+    // B and the permutation kept by the recompute: the adjoint runs on them in place
+    const Parts64 B0 = d.B;
+    int* const map0 = d.map;
+    int* const np2new0 = d.np2new;
+    d.B = S->B;
+    d.B.id = B0.id;
+    d.map = S->map;
+    d.np2new = S->np2new;
+    adj_zero_parts(c->lB, slots, c->stream);
+    adj_unsort(d, c->lA, c->lB, c->stream);
+    adj_zero_parts(c->lA, slots, c->stream);
+    adj_field(d, c->luf, c->ldf, c->luj, c->stream);
+    int st = do_cg(c);
+    if (!st) {
+      adj_field_after_cg(d, c->luf, c->lg, c->luj, c->stream);
+      adj_particles(d, c->luj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->stream);
+    }
+    d.B = B0;
+    d.map = map0;
+    d.np2new = np2new0;
+    return st;
+  }
   fast::push2d(d, c->stream);                        // B: the pushed particles, before the wraps
   adj_copy_parts(d.B, d.C, slots, c->stream);        // the bookkeeping on a copy gives the permutation
   const size_t ccb = (size_t)d.nrowjob * (d.g.nx + 1) * sizeof(int);
@@ -1166,13 +1225,17 @@ int wpic_adjoint_reverse(wpic_ctx* c, const double* lam_uf_final, double* lam_up
     const int s0 = seg * every, s1 = std::min(nsteps, s0 + every);
     adj_load(c, ckpt(seg));
     for (int k = s0; k < s1; ++k) {
-      adj_save(c, step_state(k - s0));
-      if (k + 1 < s1 && (st = one_step(c))) break;
+      wpic_ctx::AdjState& S = step_state(k - s0);
+      adj_save(c, S);
+      S.has_step = false;
+      if (k + 1 < s1) {  // the segment's last step is pushed and sorted again by adj_step
+        if ((st = adj_alloc_step(c, S)) || (st = adj_forward_step(c, S))) break;
+      }
     }
     if (st) break;
     for (int k = s1 - 1; k >= s0; --k) {
       adj_load(c, step_state(k - s0));
-      if ((st = adj_step(c))) break;
+      if ((st = adj_step(c, &step_state(k - s0)))) break;
     }
     if (st) break;
     if ((st = finish(c))) break;

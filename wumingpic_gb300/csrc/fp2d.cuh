@@ -300,6 +300,52 @@ __global__ void __launch_bounds__(DEP_THREADS) k_deposit2d(Dev2D d) {
       }
       const double g3 = d.B.ux[k], g4 = d.B.uy[k], g5 = d.B.uz[k];
       const double gvz = g5 / sqrt(1. + (+g3 * g3 + g4 * g4 + g5 * g5) / (c * c));
+#if !WPIC_REF_ORDER
+      // The same sums in factored form (about 170 instead of 400 FP64 operations per particle):
+      // the weights q dx/dt (s0 + ds/2) and q vz (s0_y + ds_y/2), q vz (s0_y/2 + ds_y/3) once per
+      // row or column, pjz = s0_x (x) A_y + ds_x (x) B_y, and the zero entries of s0_x left out.
+      {
+        const double qg = qs * gvz;
+        double qwy[5], qwx[5], qay[5], qby[5];
+#pragma unroll
+        for (int e = 0; e < 5; ++e) {
+          const double wy = s0y[e] + 0.5 * dsy[e];
+          qwy[e] = qdd * wy;
+          qay[e] = qg * wy;
+          qby[e] = qg * (0.5 * s0y[e] + fac * dsy[e]);
+          qwx[e] = qdd * (s0x[e] + 0.5 * dsx[e]);
+        }
+#pragma unroll
+        for (int jp = 0; jp < 5; ++jp) {
+          double t = 0.0;
+#pragma unroll
+          for (int ip = 0; ip < 4; ++ip) {
+            t = fma(-dsx[ip], qwy[jp], t);
+            double* e = a + ((ip + 1) + 5 * jp) * DEP_THREADS;
+            *e += t;
+          }
+        }
+#pragma unroll
+        for (int ip = 0; ip < 5; ++ip) {
+          double t = 0.0;
+#pragma unroll
+          for (int jp = 0; jp < 4; ++jp) {
+            t = fma(-dsy[jp], qwx[ip], t);
+            double* e = a + (25 + ip + 5 * (jp + 1)) * DEP_THREADS;
+            *e += t;
+          }
+        }
+#pragma unroll
+        for (int jp = 0; jp < 5; ++jp)
+#pragma unroll
+          for (int ip = 0; ip < 5; ++ip) {
+            double v = dsx[ip] * qby[jp];
+            if (ip != 0 && ip != 4) v = fma(s0x[ip], qay[jp], v);
+            double* e = a + (50 + ip + 5 * jp) * DEP_THREADS;
+            *e += v;
+          }
+      }
+#else
       // pjx: prefix along x, pjtmp(ip+1,jp) = pjtmp(ip,jp) - q*delx/dt*ds_x(ip)*(s0_y(jp)+ds_y(jp)/2)
 #pragma unroll
       for (int jp = 0; jp < 5; ++jp) {
@@ -335,6 +381,7 @@ __global__ void __launch_bounds__(DEP_THREADS) k_deposit2d(Dev2D d) {
                           + fac * dsx[ip] * dsy[jp]);
         }
       }
+#endif
     }
   }
   const size_t cell = (size_t)jj * g.nx + cx;
