@@ -35,6 +35,10 @@ UNIT = "particle-updates/s"
 #  k_deposit2d (FP64 deposit): per particle read old x, y (16 B) + new x, y, ux, uy, uz (40 B)
 #    = 56 B, plus 600 B per cell for the cell's 5x5x3 current tile.
 BYTES_MIX_PUSH = 56
+# k_mix_push's measured DRAM traffic per particle: dram__bytes_read.sum + dram__bytes_write.sum of
+# one launch on the 2048^2 x 64 ppc workload (17.31 + 16.89 GB for 536,870,912 particles, one ncu
+# pass), scaled to the particles of a launch.
+TRAFFIC_MIX_PUSH_PER_PARTICLE = (17.31e9 + 16.89e9) / 536870912
 BYTES_PUSH_FP64 = 96
 BYTES_DEPOSIT_FP64 = 56
 BYTES_DEPOSIT_CELL = 600
@@ -426,7 +430,8 @@ def main():
     achieved = BYTES_MIX_PUSH * (npart / world) / (per_launch / 1e3) / 1e9  # one GPU's launch
     roofline = {"bound": "hbm", "kernel": "k_mix_push (fused push + deposit, mixed precision)",
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": None, "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "traffic": TRAFFIC_MIX_PUSH_PER_PARTICLE * (npart / world),
+                "traffic_unit": "bytes per launch (ncu dram read + write, 63.7 B per particle)", "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "bytes_per_particle": BYTES_MIX_PUSH, "launch_ms": per_launch}
     launches = int(sum(v[1] for v in stages.values()))
     moments = time_moments(g, torch)
