@@ -665,8 +665,9 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_put(Dev2D d, const double* aos, 
       const double a = rowp[w];
       float* o = col0 + (size_t)k * MIX_PL + ly * MIX_TS + lx;
       const int gx = tx * MIX_TS + lx;
-      if (comp == 0) o[MIX_OX] = (float)(a * dxi - (double)(g.nxgs + gx));
-      else if (comp == 1) o[MIX_OY] = (float)(a * dxi - (double)(g.nygs + gy));
+      // offsets in [0, 1): a position within 2^-25 cells below a face rounds up to 1 in FP32
+      if (comp == 0) o[MIX_OX] = fminf((float)(a * dxi - (double)(g.nxgs + gx)), 0.99999994f);
+      else if (comp == 1) o[MIX_OY] = fminf((float)(a * dxi - (double)(g.nygs + gy)), 0.99999994f);
       else if (comp == 2) o[MIX_UX] = (float)a;
       else if (comp == 3) o[MIX_UY] = (float)a;
       else if (comp == 4) o[MIX_UZ] = (float)a;
