@@ -110,6 +110,13 @@ struct CellCurrent {
   float jx[4][5], jy[4][5], jz[5][5];
 };
 
+// a0 += x0 y0, a1 += x1 y1 as one packed FP32x2 fused multiply-add (each lane rounds as fmaf)
+__device__ __forceinline__ void ffma2_into(float& a0, float& a1, float x0, float x1, float y0, float y1) {
+  const float2 r = __ffma2_rn(make_float2(x0, x1), make_float2(y0, y1), make_float2(a0, a1));
+  a0 = r.x;
+  a1 = r.y;
+}
+
 __device__ __forceinline__ void cell_zero(CellCurrent& a) {
 #pragma unroll
   for (int k = 0; k < 4; ++k)
@@ -280,12 +287,9 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
         const float w = wy * (jx == 0 ? sx0 : (jx == 1 ? sx1 : sx2));
         const float4 a = sfa[f0 + jy * TT + jx];
         const float2 b = sfb[f0 + jy * TT + jx];
-        f[0] = fmaf(w, a.x, f[0]);
-        f[1] = fmaf(w, a.y, f[1]);
-        f[2] = fmaf(w, a.z, f[2]);
-        f[3] = fmaf(w, a.w, f[3]);
-        f[4] = fmaf(w, b.x, f[4]);
-        f[5] = fmaf(w, b.y, f[5]);
+        ffma2_into(f[0], f[1], w, w, a.x, a.y);
+        ffma2_into(f[2], f[3], w, w, a.z, a.w);
+        ffma2_into(f[4], f[5], w, w, b.x, b.y);
       }
     }
     const float bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
@@ -400,24 +404,30 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
         vy[e] = qg * (0.5f * s0y[e] + third * dsy[e]);
       }
     }
+    // accumulators paired (0, 1), (2, 3) along the stencil row for packed FMAs; the s0_x terms of
+    // pair (0, 1) multiply s0_x[0] = 0, which changes nothing but the sign of a zero
     float px = 0.f, py = 0.f;
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
       px += dsx[kk];
       py += dsy[kk];
 #pragma unroll
-      for (int e = 0; e < 5; ++e) {
-        acc.jx[kk][e] = fmaf(px, wyq[e], acc.jx[kk][e]);
-        acc.jy[kk][e] = fmaf(py, wxq[e], acc.jy[kk][e]);
+      for (int e = 0; e < 4; e += 2) {
+        ffma2_into(acc.jx[kk][e], acc.jx[kk][e + 1], px, px, wyq[e], wyq[e + 1]);
+        ffma2_into(acc.jy[kk][e], acc.jy[kk][e + 1], py, py, wxq[e], wxq[e + 1]);
       }
+      acc.jx[kk][4] = fmaf(px, wyq[4], acc.jx[kk][4]);
+      acc.jy[kk][4] = fmaf(py, wxq[4], acc.jy[kk][4]);
     }
 #pragma unroll
-    for (int j = 0; j < 5; ++j)
-#pragma unroll
-      for (int i = 0; i < 5; ++i) {
-        const float t = fmaf(dsx[i], vy[j], acc.jz[j][i]);
-        acc.jz[j][i] = (i == 0 || i == 4) ? t : fmaf(s0x[i], zy[j], t);
-      }
+    for (int j = 0; j < 5; ++j) {
+      float* const z = acc.jz[j];
+      ffma2_into(z[0], z[1], dsx[0], dsx[1], vy[j], vy[j]);
+      ffma2_into(z[2], z[3], dsx[2], dsx[3], vy[j], vy[j]);
+      z[4] = fmaf(dsx[4], vy[j], z[4]);
+      ffma2_into(z[0], z[1], 0.f, s0x[1], zy[j], zy[j]);
+      ffma2_into(z[2], z[3], s0x[2], s0x[3], zy[j], zy[j]);
+    }
     if (++since == FLUSH_EVERY) {
       cell_flush(acc, jhi, jlo, lx, ly, fs1, fis1, fs2);
       since = 0;
