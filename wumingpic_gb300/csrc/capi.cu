@@ -76,6 +76,10 @@ struct wpic_ctx {
   double *luf = nullptr, *ldf = nullptr, *luj = nullptr, *lg = nullptr, *tmpc = nullptr, *ltmp = nullptr;
   int* adj_cc = nullptr;  // the step's cell offsets, kept across the sort that gives the permutation
   int adj_nsteps = 0, adj_every = 1;  // the recorded forward run (0: none)
+  // scratch of the adjoint's self-checks, allocated on first use
+  double* chk_dots = nullptr;
+  Parts64 chk_A0{}, chk_B0{}, chk_vA{}, chk_vB{};
+  double *chk_f0 = nullptr, *chk_v = nullptr, *chk_lj = nullptr;
   std::vector<AdjState> adj_states;
 };
 
@@ -910,6 +914,22 @@ int adj_prepare(wpic_ctx* c, int nstates) {
   return WPIC_OK;
 }
 
+// the self-checks' scratch: 8 dot-product slots, four particle sets, two field and one current array
+int chk_scratch(wpic_ctx* c, bool parts, bool fields) {
+  const Dev2D& d = c->d;
+  const size_t P = d.g.fplane, slots = (size_t)d.nrowjob * d.cap;
+  int st;
+  if (!c->chk_dots && (st = dalloc(c, &c->chk_dots, 8))) return st;
+  if (parts && !c->chk_A0.x &&
+      ((st = alloc_parts(c, &c->chk_A0, slots)) || (st = alloc_parts(c, &c->chk_B0, slots)) ||
+       (st = alloc_parts(c, &c->chk_vA, slots)) || (st = alloc_parts(c, &c->chk_vB, slots))))
+    return st;
+  if (fields && !c->chk_f0 &&
+      ((st = dalloc(c, &c->chk_f0, 6 * P)) || (st = dalloc(c, &c->chk_v, 6 * P)) || (st = dalloc(c, &c->chk_lj, 3 * P))))
+    return st;
+  return WPIC_OK;
+}
+
 void adj_zero_parts(const Parts64& P, size_t n, cudaStream_t s) {
   cudaMemsetAsync(P.x, 0, n * 8, s);
   cudaMemsetAsync(P.y, 0, n * 8, s);
@@ -978,8 +998,8 @@ int wpic_adjoint_selfcheck(wpic_ctx* c, double* out) {
   int st = adj_prepare(c, 0);
   if (st) return st;
   const size_t P = d.g.fplane, nc = d.g.ncell, nt = 6 * (size_t)(d.g.nx + 2) * (d.g.ny + 2);
-  double* dots = nullptr;
-  if ((st = dalloc(c, &dots, 8))) return st;
+  if ((st = chk_scratch(c, false, false))) return st;
+  double* const dots = c->chk_dots;
   double h[8];
   auto dot = [&](const double* a, const double* b, size_t n, int slot) { adj_dot(a, b, n, dots + slot, c->stream); };
   // x in the scratch of the adjoint (luf/ldf/luj/lg: the inputs), y random, forward on d's buffers
@@ -1058,8 +1078,8 @@ int wpic_adjoint_pushcheck(wpic_ctx* c, double hstep, double* out) {
   int st = adj_prepare(c, 0);
   if (st) return st;
   const size_t P = d.g.fplane, slots = (size_t)d.nrowjob * d.cap;
-  double* dots = nullptr;
-  if ((st = dalloc(c, &dots, 4))) return st;
+  if ((st = chk_scratch(c, false, false))) return st;
+  double* const dots = c->chk_dots;
   cudaMemsetAsync(dots, 0, 4 * sizeof(double), c->stream);
   cudaMemcpyAsync(c->ldf, d.uf, 6 * P * 8, cudaMemcpyDeviceToDevice, c->stream);  // u
   adj_fill_rand(c->luj, 3 * P, 31, c->stream);                                     // v (B components)
@@ -1101,11 +1121,9 @@ int wpic_adjoint_depositcheck(wpic_ctx* c, double hstep, double* out) {
   int st = adj_prepare(c, 0);
   if (st) return st;
   const size_t P = d.g.fplane, slots = (size_t)d.nrowjob * d.cap;
-  Parts64 A0{}, B0{}, vA{}, vB{};
-  double* dots = nullptr;
-  if ((st = alloc_parts(c, &A0, slots)) || (st = alloc_parts(c, &B0, slots)) || (st = alloc_parts(c, &vA, slots)) ||
-      (st = alloc_parts(c, &vB, slots)) || (st = dalloc(c, &dots, 4)))
-    return st;
+  if ((st = chk_scratch(c, true, false))) return st;
+  const Parts64 A0 = c->chk_A0, B0 = c->chk_B0, vA = c->chk_vA, vB = c->chk_vB;
+  double* const dots = c->chk_dots;
   cudaMemsetAsync(dots, 0, 4 * sizeof(double), c->stream);
   fast::push2d(d, c->stream);
   adj_copy_parts(d.A, A0, slots, c->stream);
@@ -1151,10 +1169,8 @@ int wpic_adjoint_chaincheck(wpic_ctx* c, double hstep, double* out) {
   int st = adj_prepare(c, 0);
   if (st) return st;
   const size_t P = d.g.fplane, slots = (size_t)d.nrowjob * d.cap;
-  double *dots = nullptr, *f0 = nullptr, *v = nullptr, *lj = nullptr;
-  if ((st = dalloc(c, &dots, 4)) || (st = dalloc(c, &f0, 6 * P)) || (st = dalloc(c, &v, 6 * P)) ||
-      (st = dalloc(c, &lj, 3 * P)))
-    return st;
+  if ((st = chk_scratch(c, false, true))) return st;
+  double *const dots = c->chk_dots, *const f0 = c->chk_f0, *const v = c->chk_v, *const lj = c->chk_lj;
   cudaMemsetAsync(dots, 0, 4 * sizeof(double), c->stream);
   cudaMemcpyAsync(f0, d.uf, 6 * P * 8, cudaMemcpyDeviceToDevice, c->stream);
   adj_fill_rand(v, 6 * P, 51, c->stream);
