@@ -226,9 +226,92 @@ __global__ void __launch_bounds__(MOM_TX) k_mom_nvt2d(Dev2D d, Parts64 P, double
   for (int l = 0; l < 7; ++l) o[l] = acc[l];
 }
 
+#if !WPIC_REF_ORDER
+// The FMA build sums the same moments without the reference's summation order (within 1e-12):
+// one thread per cell walks its particles once, each particle's seven moments added into the
+// cell's 3 x 3 node tile (the particle's 2 x 2 nodes start at node column cx or cx + 1 and row
+// jj or jj + 1), and a second kernel adds the nine tiles that touch each node.  The tiles of
+// one species at a time go to the deposit's cell buffer (63 of its 75 planes).
+constexpr int MOMC_T = 64;
+
+__global__ void __launch_bounds__(MOMC_T) k_mom_cell2d(Dev2D d, Parts64 P, int isp) {
+  extern __shared__ double macc[];  // [63][MOMC_T]: moment l of tile node (ta, tb) at l + 7 (ta + 3 tb)
+  const Grid2D g = d.g;
+  const int cx = blockIdx.x * MOMC_T + threadIdx.x, jj = blockIdx.y;
+  if (cx >= g.nx) return;
+  double* a = macc + threadIdx.x;
+#pragma unroll 7
+  for (int e = 0; e < 63; ++e) a[e * MOMC_T] = 0.0;
+  const double d_delx = d.ph.d_delx, c = d.ph.c, ic2 = 1.0 / (c * c);
+  const int row = isp * g.ny + jj;
+  const int* ccr = d.cc + (size_t)row * (g.nx + 1);
+  const int i0 = g.nxgs - 1 + cx, j0 = g.nygs - 1 + jj;  // indices of tile node (0, 0)
+  const size_t rbase = (size_t)row * d.cap;
+  bool bad = false;
+  for (int sl = ccr[cx]; sl < ccr[cx + 1]; ++sl) {
+    const size_t k = rbase + sl;
+    const double x = P.x[k], y = P.y[k];
+    const int ih = (int)(x * d_delx - 0.5), jh = (int)(y * d_delx - 0.5);
+    const int ta = ih - i0, tb = jh - j0;
+    if (ta < 0 || ta > 1 || tb < 0 || tb > 1) {
+      bad = true;
+      continue;
+    }
+    const double dx = x * d_delx - 0.5 - ih, dy = y * d_delx - 0.5 - jh;
+    const double u1 = P.ux[k], u2 = P.uy[k], u3 = P.uz[k];
+    const double gam = 1. / sqrt(1.0 + (u1 * u1 + u2 * u2 + u3 * u3) * ic2);
+    const double pre[7] = {1.0, u1 * gam, u2 * gam, u3 * gam, u1 * u1 * gam, u2 * u2 * gam, u3 * u3 * gam};
+    const double wx[2] = {1. - dx, dx}, wy[2] = {1. - dy, dy};
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int aa = 0; aa < 2; ++aa) {
+        const double w = wx[aa] * wy[b];
+        double* t = a + 7 * ((ta + aa) + 3 * (tb + b)) * MOMC_T;
+#pragma unroll
+        for (int l = 0; l < 7; ++l) t[l * MOMC_T] = fma(pre[l], w, t[l * MOMC_T]);
+      }
+  }
+  if (bad) atomicOr(d.err, EB_OUT_OF_RANGE);
+  const size_t cell = (size_t)jj * g.nx + cx;
+#pragma unroll 7
+  for (int e = 0; e < 63; ++e) d.cellJ[(size_t)e * g.ncell + cell] = a[e * MOMC_T];
+}
+
+// node (in, jn) of species isp: the tiles of cells in-2..in, jn-2..jn
+__global__ void k_mom_gather2d(Dev2D d, double* mom, int isp) {
+  const Grid2D g = d.g;
+  const int nxm = g.nx + 2;
+  const int in = blockIdx.x * blockDim.x + threadIdx.x, jn = blockIdx.y;
+  if (in >= nxm) return;
+  double acc[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int tb = 0; tb < 3; ++tb) {
+    const int jj = jn - tb;
+    if (jj < 0 || jj >= g.ny) continue;
+    for (int ta = 0; ta < 3; ++ta) {
+      const int cx = in - ta;
+      if (cx < 0 || cx >= g.nx) continue;
+      const size_t cell = (size_t)jj * g.nx + cx;
+#pragma unroll
+      for (int l = 0; l < 7; ++l) acc[l] += d.cellJ[(size_t)(l + 7 * (ta + 3 * tb)) * g.ncell + cell];
+    }
+  }
+  double* o = mom + 7 * ((size_t)in + (size_t)nxm * ((size_t)jn + (size_t)(g.ny + 2) * isp));
+#pragma unroll
+  for (int l = 0; l < 7; ++l) o[l] = acc[l];
+}
+#endif
+
 void mom_nvt2d(const Dev2D& d, const Parts64& P, double* mom, cudaStream_t s) {
+#if WPIC_REF_ORDER
   dim3 grid((d.g.nx + 2 + MOM_TX - 1) / MOM_TX, d.g.ny + 2, d.ph.nsp);
   k_mom_nvt2d<<<grid, MOM_TX, 0, s>>>(d, P, mom);
+#else
+  for (int isp = 0; isp < d.ph.nsp; ++isp) {
+    k_mom_cell2d<<<dim3((d.g.nx + MOMC_T - 1) / MOMC_T, d.g.ny), MOMC_T, 63 * MOMC_T * sizeof(double), s>>>(d, P, isp);
+    k_mom_gather2d<<<dim3((d.g.nx + 2 + 127) / 128, d.g.ny + 2), 128, 0, s>>>(d, mom, isp);
+  }
+#endif
 }
 
 // ---------------------------------------------------------------------------
