@@ -217,10 +217,97 @@ __global__ void __launch_bounds__(MOM3_TX) k_mom_nvt3d(Dev3D d, Parts3D P, doubl
   for (int l = 0; l < 7; ++l) o[l] = acc[l];
 }
 
+#if !WPIC_REF_ORDER
+// The FMA build, as in 2D: one thread per cell sums its particles' seven moments into the
+// cell's 3 x 3 x 3 node tile (189 values, the first of the deposit's 375 per cell), then a
+// per-node gather of the 27 tiles that touch each node; within 1e-12 of the reference order.
+constexpr int MOMC3_T = 32;
+
+__global__ void __launch_bounds__(MOMC3_T) k_mom_cell3d(Dev3D d, Parts3D P, int isp) {
+  extern __shared__ double macc3[];  // [189][MOMC3_T]: moment l of tile node (ta, tb, tc) at l + 7 (ta + 3 (tb + 3 tc))
+  const Grid3D g = d.g;
+  const int cx = blockIdx.x * MOMC3_T + threadIdx.x, jj = blockIdx.y, kk = blockIdx.z;
+  if (cx >= g.nx) return;
+  double* a = macc3 + threadIdx.x;
+  for (int e = 0; e < 189; ++e) a[e * MOMC3_T] = 0.0;
+  const double d_delx = d.ph.d_delx, c = d.ph.c, ic2 = 1.0 / (c * c);
+  const int row = (isp * g.nz + kk) * g.ny + jj;
+  const int* ccr = d.cc + (size_t)row * (g.nx + 1);
+  const int i0 = g.nxgs - 1 + cx, j0 = g.nygs - 1 + jj, k0 = g.nzgs - 1 + kk;
+  const size_t rbase = (size_t)row * d.cap;
+  bool bad = false;
+  for (int sl = ccr[cx]; sl < ccr[cx + 1]; ++sl) {
+    const size_t k = rbase + sl;
+    const double x = P.x[k], y = P.y[k], z = P.z[k];
+    const int ih = (int)floor(x * d_delx - 5e-1), jh = (int)floor(y * d_delx - 5e-1), kh = (int)floor(z * d_delx - 5e-1);
+    const int ta = ih - i0, tb = jh - j0, tc = kh - k0;
+    if (ta < 0 || ta > 1 || tb < 0 || tb > 1 || tc < 0 || tc > 1) {
+      bad = true;
+      continue;
+    }
+    const double dx = x - 5e-1 - ih, dy = y - 5e-1 - jh, dz = z - 5e-1 - kh;  // as the 3D reference writes them
+    const double u1 = P.ux[k], u2 = P.uy[k], u3 = P.uz[k];
+    const double gam = 1e0 / sqrt(1e0 + (u1 * u1 + u2 * u2 + u3 * u3) * ic2);
+    const double pre[7] = {1.0, u1 * gam, u2 * gam, u3 * gam, u1 * u1 * gam, u2 * u2 * gam, u3 * u3 * gam};
+    const double wx[2] = {1e0 - dx, dx}, wy[2] = {1e0 - dy, dy}, wz[2] = {1e0 - dz, dz};
+#pragma unroll
+    for (int e = 0; e < 2; ++e)
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        const double wyz = wy[b] * wz[e];
+#pragma unroll
+        for (int aa = 0; aa < 2; ++aa) {
+          const double w = wx[aa] * wyz;
+          double* t = a + 7 * ((ta + aa) + 3 * ((tb + b) + 3 * (tc + e))) * MOMC3_T;
+#pragma unroll
+          for (int l = 0; l < 7; ++l) t[l * MOMC3_T] = fma(pre[l], w, t[l * MOMC3_T]);
+        }
+      }
+  }
+  if (bad) atomicOr(d.err, EB_OUT_OF_RANGE);
+  double* out = d.cellJ + ((size_t)kk * g.ny * g.nx + (size_t)jj * g.nx + cx) * 189;
+  for (int e = 0; e < 189; ++e) out[e] = a[e * MOMC3_T];
+}
+
+__global__ void k_mom_gather3d(Dev3D d, double* mom, int isp) {
+  const Grid3D g = d.g;
+  const int nxm = g.nx + 2, nym = g.ny + 2, nzm = g.nz + 2;
+  const int in = blockIdx.x * blockDim.x + threadIdx.x, jn = blockIdx.y, kn = blockIdx.z;
+  if (in >= nxm) return;
+  double acc[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int tc = 0; tc < 3; ++tc) {
+    const int kk = kn - tc;
+    if (kk < 0 || kk >= g.nz) continue;
+    for (int tb = 0; tb < 3; ++tb) {
+      const int jj = jn - tb;
+      if (jj < 0 || jj >= g.ny) continue;
+      for (int ta = 0; ta < 3; ++ta) {
+        const int cx = in - ta;
+        if (cx < 0 || cx >= g.nx) continue;
+        const double* t = d.cellJ + ((size_t)kk * g.ny * g.nx + (size_t)jj * g.nx + cx) * 189 + 7 * (ta + 3 * (tb + 3 * tc));
+#pragma unroll
+        for (int l = 0; l < 7; ++l) acc[l] += t[l];
+      }
+    }
+  }
+  double* o = mom + 7 * ((size_t)in + (size_t)nxm * ((size_t)jn + (size_t)nym * ((size_t)kn + (size_t)nzm * isp)));
+#pragma unroll
+  for (int l = 0; l < 7; ++l) o[l] = acc[l];
+}
+#endif
+
 void mom_nvt3d(const Dev3D& d, const Parts3D& P, double* mom, cudaStream_t s) {
+#if WPIC_REF_ORDER
   const int nbx = (d.g.nx + 2 + MOM3_TX - 1) / MOM3_TX;
   dim3 grid(nbx * (d.g.ny + 2), d.g.nz + 2, d.ph.nsp);
   k_mom_nvt3d<<<grid, MOM3_TX, 0, s>>>(d, P, mom);
+#else
+  for (int isp = 0; isp < d.ph.nsp; ++isp) {
+    k_mom_cell3d<<<dim3((d.g.nx + MOMC3_T - 1) / MOMC3_T, d.g.ny, d.g.nz), MOMC3_T, 189 * MOMC3_T * sizeof(double),
+                   s>>>(d, P, isp);
+    k_mom_gather3d<<<dim3((d.g.nx + 2 + 127) / 128, d.g.ny + 2, d.g.nz + 2), 128, 0, s>>>(d, mom, isp);
+  }
+#endif
 }
 
 // ---------------------------------------------------------------------------
