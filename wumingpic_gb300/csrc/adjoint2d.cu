@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj,
   }
   const double ux = d.B.ux[k], uy = d.B.uy[k], uz = d.B.uz[k];
   const double ic2 = 1.0 / (c * c);
-  const double gmi = 1.0 / sqrt(1. + ic2 * (ux * ux + uy * uy + uz * uz));
+  const double gmi = rsqrt(1. + ic2 * (ux * ux + uy * uy + uz * uz));
   const double gvz = uz * gmi;
   const size_t P = g.fplane;
   const double* L0 = luj + (size_t)jj * g.fp + cx;  // node (cx + a, jj + b) at L0[b * fp + a]
@@ -477,22 +477,25 @@ __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const double* tmp, P
     const double ux = d.A.ux[k], uy = d.A.uy[k], uz = d.A.uz[k];
     // forward values
     const double u1[3] = {ux + fac1 * fv[3], uy + fac1 * fv[4], uz + fac1 * fv[5]};
-    const double gam = sqrt(c * c + (u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2]));
-    const double igam = 1.0 / gam;
+    const double gsq = c * c + (u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2]);
+    const double igam = rsqrt(gsq);
+    const double gam = gsq * igam;
     const double fac1r = fac1 * igam;
     const double Bsq = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
     const double D = gam + txxx * (Bsq * igam);
-    const double fac2r = fac2 / D;
+    const double iD = 1.0 / D;
+    const double fac2r = fac2 * iD;
     const double u1xB[3] = {u1[1] * B[2] - u1[2] * B[1], u1[2] * B[0] - u1[0] * B[2], u1[0] * B[1] - u1[1] * B[0]};
     const double w[3] = {u1[0] + fac1r * u1xB[0], u1[1] + fac1r * u1xB[1], u1[2] + fac1r * u1xB[2]};
     const double wxB[3] = {w[1] * B[2] - w[2] * B[1], w[2] * B[0] - w[0] * B[2], w[0] * B[1] - w[1] * B[0]};
     const double gv[3] = {u1[0] + fac2r * wxB[0] + fac1 * fv[3], u1[1] + fac2r * wxB[1] + fac1 * fv[4],
                           u1[2] + fac2r * wxB[2] + fac1 * fv[5]};
-    const double gi = 1.0 / sqrt(1.0 + (1.0 / (c * c)) * (gv[0] * gv[0] + gv[1] * gv[1] + gv[2] * gv[2]));
+    const double ic2 = 1.0 / (c * c);
+    const double gi = rsqrt(1.0 + ic2 * (gv[0] * gv[0] + gv[1] * gv[1] + gv[2] * gv[2]));
     // reverse
     const double lx = lB.x[k], ly = lB.y[k];
     const double gib = delt * (lx * gv[0] + ly * gv[1]);
-    const double kk = gi * gi * gi * gib / (c * c);
+    const double kk = gi * gi * gi * gib * ic2;
     double gb[3] = {lB.ux[k] + delt * gi * lx - kk * gv[0], lB.uy[k] + delt * gi * ly - kk * gv[1],
                     lB.uz[k] - kk * gv[2]};  // adjoint of u' (= of u2)
     double Eb[3] = {fac1 * gb[0], fac1 * gb[1], fac1 * gb[2]};
@@ -508,7 +511,7 @@ __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const double* tmp, P
     Bb[1] += fac1r * (wb[2] * u1[0] - wb[0] * u1[2]);
     Bb[2] += fac1r * (wb[0] * u1[1] - wb[1] * u1[0]);
     const double f1rb = wb[0] * u1xB[0] + wb[1] * u1xB[1] + wb[2] * u1xB[2];
-    const double Db = -(fac2r / D) * f2rb;
+    const double Db = -(fac2r * iD) * f2rb;
     const double bsqb = Db * txxx * igam;
     Bb[0] += 2.0 * bsqb * B[0];
     Bb[1] += 2.0 * bsqb * B[1];

@@ -77,6 +77,9 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
   const double fac1 = d.ph.q[isp] / d.ph.r[isp] * 0.5 * delt;
   const double txxx = fac1 * fac1;
   const double fac2 = d.ph.q[isp] * delt / d.ph.r[isp];
+#if !WPIC_REF_ORDER
+  const double ic2 = 1.0 / (c * c);
+#endif
   const int jabs = g.nygs + jj;
   const size_t rbase = (size_t)row * d.cap;
   const int s_end = scc[nc];
@@ -119,8 +122,16 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
     double uvm1 = d.A.ux[k] + fac1 * epx;
     double uvm2 = d.A.uy[k] + fac1 * epy;
     double uvm3 = d.A.uz[k] + fac1 * epz;
+#if WPIC_REF_ORDER
     double gam = sqrt(c * c + uvm1 * uvm1 + uvm2 * uvm2 + uvm3 * uvm3);
     const double igam = 1. / gam;
+#else
+    // FMA build: one reciprocal square root gives 1/gamma and gamma (the reference takes a
+    // square root and then divides); 1/c^2 once per thread
+    const double gsq = c * c + uvm1 * uvm1 + uvm2 * uvm2 + uvm3 * uvm3;
+    const double igam = rsqrt(gsq);
+    double gam = gsq * igam;
+#endif
     const double fac1r = fac1 * igam;
     const double fac2r = fac2 / (gam + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
     const double uvm4 = uvm1 + fac1r * (+uvm2 * bpz - uvm3 * bpy);
@@ -140,7 +151,11 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push2d(Dev2D d) {
       d.B.uz[k] = g5;
       continue;
     }
+#if WPIC_REF_ORDER
     gam = 1.0 / sqrt(1.0 + (+g3 * g3 + g4 * g4 + g5 * g5) / (c * c));
+#else
+    gam = rsqrt(1.0 + (g3 * g3 + g4 * g4 + g5 * g5) * ic2);
+#endif
     d.B.ux[k] = g3;
     d.B.uy[k] = g4;
     d.B.uz[k] = g5;
@@ -335,6 +350,9 @@ __global__ void __launch_bounds__(DEP_THREADS) k_deposit2d(Dev2D d) {
   for (int e = 0; e < 75; ++e) a[e * DEP_THREADS] = 0.0;
   const double d_delx = d.ph.d_delx, d_delt = d.ph.d_delt, delx = d.ph.delx, c = d.ph.c;
   const double fac = 1.0 / 3.0;
+#if !WPIC_REF_ORDER
+  const double ic2 = 1.0 / (c * c);
+#endif
   const int iabs = g.nxgs + cx, jabs = g.nygs + jj;
   for (int isp = 0; isp < d.ph.nsp; ++isp) {
     const int row = isp * g.ny + jj;
@@ -382,7 +400,11 @@ __global__ void __launch_bounds__(DEP_THREADS) k_deposit2d(Dev2D d) {
         ds[4] = s1_3 * smo_3 - s0[4];
       }
       const double g3 = d.B.ux[k], g4 = d.B.uy[k], g5 = d.B.uz[k];
+#if WPIC_REF_ORDER
       const double gvz = g5 / sqrt(1. + (+g3 * g3 + g4 * g4 + g5 * g5) / (c * c));
+#else
+      const double gvz = g5 * rsqrt(1. + (g3 * g3 + g4 * g4 + g5 * g5) * ic2);
+#endif
 #if !WPIC_REF_ORDER
       // The same sums in factored form (about 170 instead of 400 FP64 operations per particle):
       // the weights q dx/dt (s0 + ds/2) and q vz (s0_y + ds_y/2), q vz (s0_y/2 + ds_y/3) once per

@@ -53,6 +53,9 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push3d(Dev3D d) {
   const double fac1 = d.ph.q[isp] / d.ph.r[isp] * 5e-1 * delt;
   const double txxx = fac1 * fac1;
   const double fac2 = d.ph.q[isp] * delt / d.ph.r[isp];
+#if !WPIC_REF_ORDER
+  const double ic2 = 1.0 / (c * c);
+#endif
   const int jabs = g.nygs + jj, kabs = g.nzgs + kk;
   const size_t rbase = (size_t)row * d.cap;
   const int s_end = scc[nc];
@@ -100,8 +103,16 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push3d(Dev3D d) {
     double uvm1 = d.A.ux[k] + fac1 * epx;
     double uvm2 = d.A.uy[k] + fac1 * epy;
     double uvm3 = d.A.uz[k] + fac1 * epz;
+#if WPIC_REF_ORDER
     double gam = sqrt(c * c + uvm1 * uvm1 + uvm2 * uvm2 + uvm3 * uvm3);
     const double igam = 1e0 / gam;
+#else
+    // FMA build: one reciprocal square root gives 1/gamma and gamma (the reference takes a
+    // square root and then divides); 1/c^2 once per thread
+    const double gsq = c * c + uvm1 * uvm1 + uvm2 * uvm2 + uvm3 * uvm3;
+    const double igam = rsqrt(gsq);
+    double gam = gsq * igam;
+#endif
     const double fac1r = fac1 * igam;
     const double fac2r = fac2 / (gam + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
     const double uvm4 = uvm1 + fac1r * (+uvm2 * bpz - uvm3 * bpy);
@@ -122,7 +133,11 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push3d(Dev3D d) {
       d.B.uz[k] = g6;
       continue;
     }
+#if WPIC_REF_ORDER
     gam = 1e0 / sqrt(1e0 + (+g4 * g4 + g5 * g5 + g6 * g6) / (c * c));
+#else
+    gam = rsqrt(1e0 + (g4 * g4 + g5 * g5 + g6 * g6) * ic2);
+#endif
     d.B.ux[k] = g4;
     d.B.uy[k] = g5;
     d.B.uz[k] = g6;
