@@ -547,35 +547,32 @@ __global__ void __launch_bounds__(MIX_TC, 4) k_mix_arrive(Dev2D d) {
     return i < ARR_KEYS_SMEM ? skey[i][c] : __float_as_int(top[MIX_KEY - (ptrdiff_t)i * MIX_PL]);
   };
   for (int i0 = 0; ok && i0 < b; i0 += ARR_BATCH) {
-    const float* src[ARR_BATCH];
-    float* dst[ARR_BATCH];
-    bool on[ARR_BATCH];
+    int dl[ARR_BATCH];  // destination slot of arrival i0 + u, -1 past the last arrival
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u) {
       const int i = i0 + u;
-      on[u] = i < b;
-      src[u] = top;
-      dst[u] = col;
-      if (on[u]) {
+      dl[u] = -1;
+      if (i < b) {
         const int ki = key(i);
         int rank = 0;
         for (int l = 0; l < b; ++l) rank += key(l) < ki ? 1 : 0;
-        src[u] = top - (size_t)i * MIX_PL;
-        dst[u] = col + (size_t)(j + rank) * MIX_PL;
+        dl[u] = j + rank;
       }
     }
     float w[ARR_BATCH][7];
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u)
-      if (on[u]) {
+      if (dl[u] >= 0) {
+        const float* src = top - (size_t)(i0 + u) * MIX_PL;
 #pragma unroll
-        for (int a = 0; a < 7; ++a) w[u][a] = src[u][a * MIX_TC];
+        for (int a = 0; a < 7; ++a) w[u][a] = src[a * MIX_TC];
       }
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u)
-      if (on[u]) {
+      if (dl[u] >= 0) {
+        float* dst = col + (size_t)dl[u] * MIX_PL;
 #pragma unroll
-        for (int a = 0; a < 7; ++a) dst[u][a * MIX_TC] = w[u][a];
+        for (int a = 0; a < 7; ++a) dst[a * MIX_TC] = w[u][a];
       }
   }
   const int nn = ok ? j + b : j;
