@@ -255,8 +255,11 @@ typedef struct wpic_params3d {
   int nxgs, nxge, nygs, nyge, nzgs, nzge, nys, nye, nzs, nze;
   double delx, delt, c, gfac;
   double q[2], r[2];
-  int precision;            /* WPIC_FP64 or WPIC_FP64_EXACT */
+  int precision;            /* WPIC_FP64, WPIC_FP64_EXACT or WPIC_MIXED */
   int device_cap;           /* device particle slots per row per species; 0 = np */
+  int bc_kind;              /* WPIC_BC_PERIODIC (3d/common/boundary_periodic.f90) or WPIC_BC_RECONNECTION:
+                               conducting walls in x, 3d/proj/reconnection/boundary_reconnection.f90
+                               (FP64 paths) */
 } wpic_params3d;
 
 /* particle__init + field__init + sort__init + bc__init of a 3D run

@@ -62,6 +62,7 @@ def lib():
             L.orc3d_create.argtypes = [i] * 13 + [d, d, d, dp, dp, d]
             L.orc3d_destroy.argtypes = [vp]
             L.orc3d_set_threads.argtypes = [vp, i]
+            L.orc3d_set_bc.argtypes = [vp, i]
             L.orc3d_cg_control.argtypes = [vp, ip, i]
             L.orc3d_cg_iters.argtypes = [vp, ip]
             for n in ("orc3d_get_df", "orc3d_get_uj"):
@@ -73,6 +74,7 @@ def lib():
             L.orc3d_bc_mom.argtypes = [vp, dp]
             L.orc3d_ele_cur.argtypes = [vp, dp, dp, dp, ip, i, i]
             L.orc3d_bc_curre.argtypes = [vp, dp, i, i]
+            L.orc3d_bc_dfield.argtypes = [vp, dp, i, i]
             L.orc3d_field_fdtd_i.argtypes = [vp, dp, dp, dp, ip, i, i]
             L.orc3d_bc_particle_x.argtypes = [vp, dp, ip]
             L.orc3d_bc_particle_yz.argtypes = [vp, dp, ip]
@@ -235,10 +237,12 @@ class Oracle2D:
 
 
 class Oracle3D:
-    """3D oracle instance (periodic boundaries): the SAVEd module state of particle/field/sort/boundary."""
+    """3D oracle instance: the SAVEd module state of particle/field/sort/boundary; bc "periodic"
+    (3d/common/boundary_periodic.f90) or "reconnection" (conducting walls in x,
+    3d/proj/reconnection/boundary_reconnection.f90)."""
 
     def __init__(self, *, nx, ny, nz, np_cap, nsp=2, ndim=7, delx=1.0, delt=0.5, c=1.0, q, r, gfac=0.501,
-                 threads=1, nxgs=2, nygs=2, nzgs=2):
+                 threads=1, nxgs=2, nygs=2, nzgs=2, bc="periodic"):
         self.nx, self.ny, self.nz, self.np, self.nsp, self.ndim = nx, ny, nz, np_cap, nsp, ndim
         self.nxgs, self.nxge = nxgs, nxgs + nx - 1
         self.nygs, self.nyge = nygs, nygs + ny - 1
@@ -250,6 +254,8 @@ class Oracle3D:
                                      self.nzge, self.nygs, self.nyge, self.nzgs, self.nzge, delx, delt, c,
                                      _p(q, np.float64), _p(r, np.float64), gfac)
         lib().orc3d_set_threads(self._h, threads)
+        self.bc = bc
+        lib().orc3d_set_bc(self._h, {"periodic": 0, "reconnection": 1}[bc])
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -323,6 +329,9 @@ class Oracle3D:
     def bc_curre(self, uj):
         return lib().orc3d_bc_curre(self._h, _p(uj, np.float64), self.nxs, self.nxe)
 
+    def bc_dfield(self, df):
+        return lib().orc3d_bc_dfield(self._h, _p(df, np.float64), self.nxs, self.nxe)
+
     def field_fdtd_i(self, uf, up, gp, cumcnt):
         return lib().orc3d_field_fdtd_i(self._h, _p(uf, np.float64), _p(up, np.float64), _p(gp, np.float64),
                                         _p(cumcnt, np.int32), self.nxs, self.nxe)
@@ -345,11 +354,15 @@ class Oracle3D:
 
     def step(self, st, pusher="boris"):
         """One reference time step on a State3D, in the driver's call order
-        (3d/proj/weibel/app.f90:103-108); pusher="vay" calls particle__solv_vay."""
+        (3d/proj/weibel/app.f90:103-108; reconnection, particle_x before the field solve:
+        3d/proj/reconnection/app.f90:103-108); pusher="vay" calls particle__solv_vay."""
         push = self.particle_solv_vay if pusher == "vay" else self.particle_solv
         rc = push(st.gp, st.up, st.uf, st.cumcnt)
+        if self.bc == "reconnection":
+            rc = rc or self.bc_particle_x(st.gp, st.np2)
         rc = rc or self.field_fdtd_i(st.uf, st.up, st.gp, st.cumcnt)
-        rc = rc or self.bc_particle_x(st.gp, st.np2)
+        if self.bc == "periodic":
+            rc = rc or self.bc_particle_x(st.gp, st.np2)
         rc = rc or self.bc_particle_yz(st.gp, st.np2)
         rc = rc or self.sort_bucket(st.up, st.gp, st.cumcnt, st.np2)
         return rc

@@ -18,6 +18,9 @@
 //   particle__solv_vay        3d/common/particle.f90:236-419
 //   mom_calc__accl / __nvt    3d/common/mom_calc.f90:49-332
 //   boundary_periodic__mom    3d/common/boundary_periodic.f90:1102-1235
+//   boundary_reconnection__particle_x/dfield/curre/phi/mom (conducting walls in x; its
+//   particle_yz is boundary_periodic's)
+//                             3d/proj/reconnection/boundary_reconnection.f90:69-1255
 //
 // Parity status: UNPINNED (no golden vectors in the reference for this path;
 // no Fortran compiler or MPI in this image).  It is checked against physical
@@ -43,8 +46,11 @@ namespace {
 
 enum { ORC_OK = 0, ORC_CG_NOT_CONVERGED = 1, ORC_CAPACITY = 2, ORC_OUT_OF_RANGE = 3 };
 
+enum { BC3_PERIODIC = 0, BC3_WALLS = 1 };  // boundary_periodic / boundary_reconnection (3D)
+
 struct Orc3D {
   int ndim, np, nsp, nxgs, nxge, nygs, nyge, nzgs, nzge, nys, nye, nzs, nze;
+  int bc_kind = BC3_PERIODIC;  // conducting walls in x (3d/proj/reconnection/boundary_reconnection.f90)
   int nthreads;
   double delx, delt, c, gfac;
   std::vector<double> q, r;
@@ -454,7 +460,10 @@ void bc_curre(Orc3D* o, double* uj, int nxs, int nxe) {
       for (int i = nxs - 2; i <= nxe + 2; ++i)
         for (int l = 1; l <= 3; ++l) J(l, i, j, nzs - 1) = s[n++];
   }
-  // x: fold then refresh over the whole ghosted (j, k) range, one array statement after another
+  // x: fold then refresh over the whole ghosted (j, k) range, one array statement after another;
+  // boundary_reconnection__curre has no x stage
+  // (3d/proj/reconnection/boundary_reconnection.f90:689-978)
+  if (o->bc_kind == BC3_WALLS) return;
   const int jlo = nys - 2, jhi = nye + 2, klo = nzs - 2, khi = nze + 2;
   auto xstmt = [&](int dst, int src, bool add) {
     for (int k = klo; k <= khi; ++k)
@@ -512,6 +521,20 @@ void bc_dfield(Orc3D* o, double* df, int nxs, int nxe) {
   };
   zcopy(nze + 1, nze + 2, nzs, nzs + 1);
   zcopy(nzs - 2, nzs - 1, nze - 1, nze);
+  if (o->bc_kind == BC3_WALLS) {
+    // boundary_reconnection__dfield's walls (3d/proj/reconnection/boundary_reconnection.f90:674-683):
+    // Bx and (Ey, Ez) odd, (By, Bz, Ex) even, with the offsets of each wall; nxs-2 and nxe+2 untouched
+    for (int k = nzs - 2; k <= nze + 2; ++k)
+      for (int j = nys - 2; j <= nye + 2; ++j) {
+        D(1, nxs - 1, j, k) = -D(1, nxs, j, k);
+        for (int l = 2; l <= 4; ++l) D(l, nxs - 1, j, k) = D(l, nxs + 1, j, k);
+        for (int l = 5; l <= 6; ++l) D(l, nxs - 1, j, k) = -D(l, nxs, j, k);
+        D(1, nxe, j, k) = -D(1, nxe - 1, j, k);
+        for (int l = 2; l <= 4; ++l) D(l, nxe + 1, j, k) = D(l, nxe - 1, j, k);
+        for (int l = 5; l <= 6; ++l) D(l, nxe, j, k) = -D(l, nxe - 1, j, k);
+      }
+    return;
+  }
   auto xstmt = [&](int dst, int src) {
     for (int k = nzs - 2; k <= nze + 2; ++k)
       for (int j = nys - 2; j <= nye + 2; ++j)
@@ -526,7 +549,6 @@ void bc_dfield(Orc3D* o, double* df, int nxs, int nxe) {
 // boundary_periodic__phi (3d/common/boundary_periodic.f90:981-1099): 1-deep copies, y (k interior,
 // i interior), z (j = nys-1..nye+1, i interior), x (all j, k)
 void bc_phi(Orc3D* o, double* phi, int nxs, int nxe, int l) {
-  (void)l;
   const int nys = o->nys, nye = o->nye, nzs = o->nzs, nze = o->nze;
   const int pw = nxe - nxs + 3, ph = nye - nys + 3;
   auto P = [&](int i, int j, int k) -> double& {
@@ -556,6 +578,21 @@ void bc_phi(Orc3D* o, double* phi, int nxs, int nxe, int l) {
   n = 0;
   for (int j = nys - 1; j <= nye + 1; ++j)
     for (int i = nxs; i <= nxe; ++i) P(i, j, nzs - 1) = s[n++];
+  if (o->bc_kind == BC3_WALLS) {
+    // boundary_reconnection__phi (3d/proj/reconnection/boundary_reconnection.f90:1093-1117):
+    // component 1 odd about nxs and nxe-1, components 2 and 3 even about nxs and nxe
+    for (int k = nzs - 1; k <= nze + 1; ++k)
+      for (int j = nys - 1; j <= nye + 1; ++j) {
+        if (l == 1) {
+          P(nxs - 1, j, k) = -P(nxs, j, k);
+          P(nxe + 1, j, k) = -P(nxe - 2, j, k);
+        } else {
+          P(nxs - 1, j, k) = P(nxs + 1, j, k);
+          P(nxe + 1, j, k) = P(nxe - 1, j, k);
+        }
+      }
+    return;
+  }
   for (int k = nzs - 1; k <= nze + 1; ++k)
     for (int j = nys - 1; j <= nye + 1; ++j) P(nxs - 1, j, k) = P(nxe, j, k);
   for (int k = nzs - 1; k <= nze + 1; ++k)
@@ -732,6 +769,31 @@ int bc_particle_x(Orc3D* o, double* up, const int* np2) {
   const int nys = o->nys, nye = o->nye, nzs = o->nzs, nze = o->nze;
   const double d_delx = o->d_delx, delx = o->delx;
   set_threads(o);
+  if (o->bc_kind == BC3_WALLS) {
+    // boundary_reconnection__particle_x (3d/proj/reconnection/boundary_reconnection.f90:69-109):
+    // cell int(x / dx) below nxs+1 or from nxe-1 up reflects about that face, all three momentum
+    // components reversed; the driver passes nxs = nxgs, nxe = nxge
+    const int nxs = o->nxgs, nxe = o->nxge;
+    for (int isp = 1; isp <= o->nsp; ++isp) {
+#pragma omp parallel for
+      for (int k = nzs; k <= nze; ++k)
+        for (int j = nys; j <= nye; ++j)
+          for (int ii = 1; ii <= np2[o->inp2(j, k, isp)]; ++ii) {
+            double& x = up[o->iup(1, ii, j, k, isp)];
+            const int ipos = (int)(x / delx);
+            double face;
+            if (ipos < nxs + 1) face = 2.0 * (nxs + 1) * delx;
+            else if (ipos >= nxe - 1) face = 2.0 * (nxe - 1) * delx;
+            else continue;
+            x = face - x;
+            for (int d = 4; d <= 6; ++d) {
+              double& u = up[o->iup(d, ii, j, k, isp)];
+              u = -u;
+            }
+          }
+    }
+    return ORC_OK;
+  }
   for (int isp = 1; isp <= o->nsp; ++isp) {
 #pragma omp parallel for
     for (int k = nzs; k <= nze; ++k)
@@ -1004,8 +1066,13 @@ void bc_mom(Orc3D* o, double* mom) {
     for (int k = nzs - 1; k <= nze + 1; ++k)
       for (int j = nys - 1; j <= nye + 1; ++j)
         for (int l = 1; l <= 7; ++l) {
-          M(l, nxgs, j, k, isp) = M(l, nxgs, j, k, isp) + M(l, nxge + 1, j, k, isp);
-          M(l, nxge, j, k, isp) = M(l, nxge, j, k, isp) + M(l, nxgs - 1, j, k, isp);
+          if (o->bc_kind == BC3_WALLS) {  // boundary_reconnection__mom (:1134-1137): x ghosts onto the wall columns
+            M(l, nxgs, j, k, isp) = M(l, nxgs, j, k, isp) + M(l, nxgs - 1, j, k, isp);
+            M(l, nxge, j, k, isp) = M(l, nxge, j, k, isp) + M(l, nxge + 1, j, k, isp);
+          } else {
+            M(l, nxgs, j, k, isp) = M(l, nxgs, j, k, isp) + M(l, nxge + 1, j, k, isp);
+            M(l, nxge, j, k, isp) = M(l, nxge, j, k, isp) + M(l, nxgs - 1, j, k, isp);
+          }
         }
   for (int isp = 1; isp <= o->nsp; ++isp) {
     for (int k = nzs - 1; k <= nze + 1; ++k)
@@ -1052,6 +1119,7 @@ void* orc3d_create(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int 
   return o;
 }
 void orc3d_destroy(void* h) { delete (Orc3D*)h; }
+void orc3d_set_bc(void* h, int bc_kind) { ((Orc3D*)h)->bc_kind = bc_kind == BC3_WALLS ? BC3_WALLS : BC3_PERIODIC; }
 void orc3d_set_threads(void* h, int n) { ((Orc3D*)h)->nthreads = n > 0 ? n : 1; }
 void orc3d_cg_control(void* h, const int* fixed3, int ite_max) {
   Orc3D* o = (Orc3D*)h;
@@ -1091,6 +1159,7 @@ int orc3d_ele_cur(void* h, double* uj, const double* up, const double* gp, const
   return ele_cur((Orc3D*)h, uj, up, gp, cumcnt, nxs, nxe);
 }
 int orc3d_bc_curre(void* h, double* uj, int nxs, int nxe) { bc_curre((Orc3D*)h, uj, nxs, nxe); return 0; }
+int orc3d_bc_dfield(void* h, double* df, int nxs, int nxe) { bc_dfield((Orc3D*)h, df, nxs, nxe); return 0; }
 int orc3d_field_fdtd_i(void* h, double* uf, const double* up, const double* gp, const int* cumcnt, int nxs, int nxe) {
   return field_fdtd_i((Orc3D*)h, uf, up, gp, cumcnt, nxs, nxe);
 }

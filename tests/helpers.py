@@ -303,9 +303,10 @@ def literal_moments2d(p, gp, np2, bc="periodic"):
     return mom
 
 
-def literal_moments3d(p, gp, np2):
+def literal_moments3d(p, gp, np2, bc="periodic"):
     """mom_calc__nvt + bc__mom in 3D (3d/common/mom_calc.f90:219-332,
-    3d/common/boundary_periodic.f90:1102-1235) in numpy."""
+    3d/common/boundary_periodic.f90:1102-1235; with walls the x ghosts fold onto the wall
+    columns, 3d/proj/reconnection/boundary_reconnection.f90:1134-1137) in numpy."""
     nxm, nym, nzm = p.nx + 2, p.ny + 2, p.nz + 2
     mom = np.zeros((7, nxm, nym, nzm, p.nsp))
     for isp in range(p.nsp):
@@ -326,8 +327,12 @@ def literal_moments3d(p, gp, np2):
                             idx = (h[0] + a - (p.nxgs - 1), h[1] + b - (p.nygs - 1), h[2] + cz - (p.nzgs - 1))
                             for l in range(7):
                                 np.add.at(mom[l, :, :, :, isp], idx, pre[l] * w)
-    mom[:, 1] += mom[:, nxm - 1]
-    mom[:, nxm - 2] += mom[:, 0]
+    if bc == "periodic":
+        mom[:, 1] += mom[:, nxm - 1]
+        mom[:, nxm - 2] += mom[:, 0]
+    else:
+        mom[:, 1] += mom[:, 0]
+        mom[:, nxm - 2] += mom[:, nxm - 1]
     mom[:, :, nym - 2] += mom[:, :, 0]
     mom[:, :, 1] += mom[:, :, nym - 1]
     mom[:, :, 1:nym - 1, nzm - 2] += mom[:, :, 1:nym - 1, 0]

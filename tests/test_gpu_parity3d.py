@@ -22,7 +22,7 @@ REL = 1e-12
 def make_oracle(p):
     q, r = p.charges()
     return Oracle3D(nx=p.nx, ny=p.ny, nz=p.nz, np_cap=p.np_cap, q=q, r=r, delt=p.delt, delx=p.delx, c=p.c,
-                    gfac=p.gfac)
+                    gfac=p.gfac, bc=getattr(p, "bc", "periodic"))
 
 
 def make_gpu(p, precision, gpu_lib):
@@ -277,3 +277,71 @@ def test_moments_parity_3d(gpu_lib, precision, rel):
     ref2 = np.zeros(o.mom_shape(), order="F")
     assert o.mom_calc_nvt(ref2, st.up, st.np2) == 0 and o.bc_mom(ref2) == 0
     assert_field(g.get_mom(), ref2, rel)
+
+
+# ---- conducting walls in x (3d/proj/reconnection/boundary_reconnection.f90) ----
+
+def walls_case(seed, **kw):
+    kw.setdefault("u_the", 0.3)
+    return perturbed_case(seed=seed, nx=10, ny=6, nz=5, ppc=4, bc="reconnection", **kw)
+
+
+def test_walls_steps_exact_3d(gpu_lib):
+    """The reconnection driver's step in the exact build: one step bit-exact on particles
+    (permutation, np2, cumcnt included), fields 1e-12; the next step 1e-12 (pushed by those
+    fields); every particle between the walls."""
+    p, st = walls_case(71)
+    for steps, rel in ((1, 0.0), (2, 1e-12)):
+        g = make_gpu(p, "fp64_exact", gpu_lib)
+        g.put_state(st)
+        o = make_oracle(p)
+        ref = st.copy()
+        for _ in range(steps):
+            g.step(1)
+            o.cg_control(fixed=g.cg_iters())
+            assert o.step(ref) == 0
+        out = g.get_state()
+        assert_particles(out.up, out.np2, ref.up, ref.np2, rel)
+        np.testing.assert_array_equal(out.cumcnt, ref.cumcnt)
+        assert_field(out.uf, ref.uf, 1e-12)
+        for a in rows(out.up, out.np2):
+            assert a[0].min(initial=1e9) >= (p.nxgs + 1) * p.delx and a[0].max(initial=-1e9) < (p.nxge - 1) * p.delx
+        g.close()
+
+
+def test_walls_steps_fp64_3d(gpu_lib):
+    p, st = walls_case(72)
+    g = make_gpu(p, "fp64", gpu_lib)
+    g.put_state(st)
+    o = make_oracle(p)
+    ref = st.copy()
+    for _ in range(6):
+        g.step(1)
+        o.cg_control(fixed=g.cg_iters())
+        assert o.step(ref) == 0
+    out = g.get_state()
+    np.testing.assert_array_equal(out.np2, ref.np2)
+    np.testing.assert_array_equal(out.cumcnt, ref.cumcnt)
+    assert_particles(out.up, out.np2, ref.up, ref.np2, rel=1e-10)
+    assert_field(out.uf, ref.uf, 1e-10)
+    g.close()
+
+
+@pytest.mark.parametrize("precision,rel", [("fp64_exact", 0.0), ("fp64", REL)])
+def test_walls_moments_3d(gpu_lib, precision, rel):
+    p, st = walls_case(73)
+    g = make_gpu(p, precision, gpu_lib)
+    g.put_state(st)
+    mom = g.moments()
+    rc, ref = make_oracle(p).moments(st.copy())
+    assert rc == 0
+    assert_field(mom, ref, rel)
+    g.close()
+
+
+def test_walls_rejected_on_the_mixed_path_3d(gpu_lib):
+    from wumingpic_gb300._lib import WpicError
+    p, st = small_case3d(nx=16, ny=16, nz=8, ppc=2, seed=74, bc="reconnection")
+    with pytest.raises(WpicError):
+        make_gpu(p, "mixed", gpu_lib)
+

@@ -239,3 +239,96 @@ def test_moments_match_numpy_restatement_3d():
     for isp in range(p.nsp):
         n = mom[0, 1:p.nx + 1, 1:p.ny + 1, 1:p.nz + 1, isp].sum()
         np.testing.assert_allclose(n, st.np2[:, :, isp].sum(), rtol=1e-12)
+
+
+# ---- conducting walls in x (3d/proj/reconnection/boundary_reconnection.f90) ----
+
+def walls_case(seed, **kw):
+    kw.setdefault("u_the", 0.2)
+    return small_case3d(nx=8, ny=5, nz=4, ppc=4, seed=seed, bc="reconnection", **kw)
+
+
+def test_walls_steps_conserve_charge_3d():
+    """The reconnection driver's order (3d/proj/reconnection/app.f90:103-108): push, reflection
+    at the walls, field solve, y/z migration, sort.  Charge is conserved to round-off, no
+    particle is lost and all stay between the walls."""
+    p, st = walls_case(31, u_the=0.3)
+    q, _ = p.charges()
+    o = make_oracle3d(p, bc="reconnection")
+    for _ in range(4):
+        up0 = st.up.copy(order="F")
+        assert o.particle_solv(st.gp, st.up, st.uf, st.cumcnt) == 0
+        assert o.bc_particle_x(st.gp, st.np2) == 0
+        assert o.field_fdtd_i(st.uf, st.up, st.gp, st.cumcnt) == 0
+        res, scale = continuity_residual3d(p, q, up0, st.gp, st.np2, o.get_uj())
+        assert res <= 1e-12 * scale, (res, scale)
+        assert o.bc_particle_yz(st.gp, st.np2) == 0
+        assert o.sort_bucket(st.up, st.gp, st.cumcnt, st.np2) == 0
+    assert st.np2.sum() == p.n_particles
+    for isp in range(p.nsp):
+        for kk in range(p.nz):
+            for jj in range(p.ny):
+                x = st.up[0, :st.np2[jj, kk, isp], jj, kk, isp]
+                assert x.min() >= (p.nxgs + 1) * p.delx and x.max() < (p.nxge - 1) * p.delx
+
+
+def test_walls_reflection_3d():
+    """boundary_reconnection__particle_x: x = 2 (nxs+1) dx - x below the left wall, 2 (nxe-1) dx - x
+    from the right one, all three momenta reversed (numpy restatement)."""
+    p, st = walls_case(32)
+    o = make_oracle3d(p, bc="reconnection")
+    rng = np.random.default_rng(32)
+    gp = st.up.copy(order="F")
+    n = st.np2[0, 0, 1]
+    gp[0, :n, 0, 0, 1] = rng.uniform(p.nxgs + 0.5, p.nxge + 0.5, n) * p.delx
+    ref = gp.copy(order="F")
+    x = ref[0, :n, 0, 0, 1]
+    cell = np.trunc(x / p.delx).astype(int)
+    lo, hi = cell < p.nxgs + 1, cell >= p.nxge - 1
+    x[lo] = 2.0 * (p.nxgs + 1) * p.delx - x[lo]
+    x[hi] = 2.0 * (p.nxge - 1) * p.delx - x[hi]
+    for d in (3, 4, 5):
+        u = ref[d, :n, 0, 0, 1]
+        u[lo | hi] = -u[lo | hi]
+    assert lo.any() and hi.any()
+    assert o.bc_particle_x(gp, st.np2) == 0
+    np.testing.assert_array_equal(gp, ref)
+
+
+def test_walls_dfield_rule_3d():
+    """boundary_reconnection__dfield: periodic ghost copies in y and z, then at the walls Bx and
+    (Ey, Ez) odd about nxs and nxe - 1/2, (By, Bz, Ex) even about nxs and nxe (numpy restatement)."""
+    p, st = walls_case(33)
+    o = make_oracle3d(p, bc="reconnection")
+    rng = np.random.default_rng(33)
+    df = np.asfortranarray(rng.standard_normal(st.uf.shape))
+    ref = df.copy(order="F")
+    o.bc_dfield(df)
+    nx, ny, nz = p.nx, p.ny, p.nz
+    # y then z ghost copies over the interior x columns (2..nx+1 in array indices)
+    xs = slice(2, nx + 2)
+    ref[:, xs, ny + 2, 2:nz + 2] = ref[:, xs, 2, 2:nz + 2]
+    ref[:, xs, ny + 3, 2:nz + 2] = ref[:, xs, 3, 2:nz + 2]
+    ref[:, xs, 0, 2:nz + 2] = ref[:, xs, ny, 2:nz + 2]
+    ref[:, xs, 1, 2:nz + 2] = ref[:, xs, ny + 1, 2:nz + 2]
+    ref[:, xs, :, nz + 2] = ref[:, xs, :, 2]
+    ref[:, xs, :, nz + 3] = ref[:, xs, :, 3]
+    ref[:, xs, :, 0] = ref[:, xs, :, nz]
+    ref[:, xs, :, 1] = ref[:, xs, :, nz + 1]
+    s, e = 2, nx + 1  # nxs, nxe
+    ref[0, s - 1] = -ref[0, s]
+    ref[1:4, s - 1] = ref[1:4, s + 1]
+    ref[4:6, s - 1] = -ref[4:6, s]
+    ref[0, e] = -ref[0, e - 1]
+    ref[1:4, e + 1] = ref[1:4, e - 1]
+    ref[4:6, e] = -ref[4:6, e - 1]
+    np.testing.assert_array_equal(df, ref)
+
+
+def test_walls_moments_3d():
+    p, st = walls_case(34)
+    o = make_oracle3d(p, bc="reconnection")
+    rc, mom = o.moments(st)
+    assert rc == 0
+    ref = literal_moments3d(p, st.gp, st.np2, bc="reconnection")
+    np.testing.assert_allclose(mom, ref, rtol=0, atol=1e-13 * np.abs(ref).max())

@@ -51,7 +51,7 @@ class WpicParams3D(ctypes.Structure):
         ("nys", ctypes.c_int), ("nye", ctypes.c_int), ("nzs", ctypes.c_int), ("nze", ctypes.c_int),
         ("delx", ctypes.c_double), ("delt", ctypes.c_double), ("c", ctypes.c_double), ("gfac", ctypes.c_double),
         ("q", ctypes.c_double * 2), ("r", ctypes.c_double * 2),
-        ("precision", ctypes.c_int), ("device_cap", ctypes.c_int),
+        ("precision", ctypes.c_int), ("device_cap", ctypes.c_int), ("bc_kind", ctypes.c_int),
     ]
 
 

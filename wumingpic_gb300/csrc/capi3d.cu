@@ -167,9 +167,13 @@ int one_step3(wpic_ctx3d* c) {
   if (c->mixed) return mixed_step3(c);
   if (c->pusher == WPIC_PUSH_VAY) FP3(push_vay3d, c->d, c->stream);
   else FP3(push3d, c->d, c->stream);
+  // the reconnection driver reflects at the walls before the field solve
+  // (3d/proj/reconnection/app.f90:103-108), the periodic one wraps after it
+  const bool walls = c->d.ph.bc == BC_RECONNECTION;
+  if (walls) particle_x3d(c->d, c->d.B, c->stream);
   int st = do_field3(c);
   if (st) return st;
-  particle_x3d(c->d, c->d.B, c->stream);
+  if (!walls) particle_x3d(c->d, c->d.B, c->stream);
   do_migrate_sort3(c);
   return WPIC_OK;
 }
@@ -210,6 +214,8 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
   if (p->precision != WPIC_FP64 && p->precision != WPIC_FP64_EXACT && p->precision != WPIC_MIXED)
     return WPIC_BAD_ARGUMENT;
   if (p->precision == WPIC_MIXED && !mix3_shape_ok(nx, ny, nz)) return WPIC_BAD_ARGUMENT;
+  if (p->bc_kind != WPIC_BC_PERIODIC && p->bc_kind != WPIC_BC_RECONNECTION) return WPIC_BAD_ARGUMENT;
+  if (p->bc_kind == WPIC_BC_RECONNECTION && (p->precision == WPIC_MIXED || nx < 6)) return WPIC_BAD_ARGUMENT;
   if ((double)nx * ny * nz > 2.0e9 || (double)p->nsp * ny * nz * p->np >= 2147483647.0) return WPIC_BAD_ARGUMENT;
   wpic_ctx3d* c = new wpic_ctx3d();
   c->prm = *p;
@@ -230,7 +236,7 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
   ph.c = p->c;
   ph.gfac = p->gfac;
   ph.nsp = p->nsp;
-  ph.bc = BC_PERIODIC;
+  ph.bc = p->bc_kind == WPIC_BC_RECONNECTION ? BC_RECONNECTION : BC_PERIODIC;
   for (int k = 0; k < 2; ++k) {
     ph.q[k] = k < p->nsp ? p->q[k] : 0.0;
     ph.r[k] = k < p->nsp ? p->r[k] : 1.0;

@@ -502,11 +502,24 @@ void gkl3d(const Dev3D& d, cudaStream_t s) { k_gkl3d<<<8 * 152, 256, 0, s>>>(d);
 // periodic ghosts (boundary_periodic__phi, 3d/common/boundary_periodic.f90:981-1099)
 // applied by index arithmetic.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double v3_at(const double* v, const Grid3D& g, int x, int y, int z) {
-  if (x < 0) x += g.nx; else if (x >= g.nx) x -= g.nx;
+// the value of component l at cell (x, y, z) one step outside the interior: periodic in y and z;
+// in x periodic, or at conducting walls (boundary_reconnection__phi,
+// 3d/proj/reconnection/boundary_reconnection.f90:1093-1117) component 1 odd about nxs and nxe-1,
+// components 2 and 3 even about nxs and nxe
+__device__ __forceinline__ double v3_at(const double* v, const Grid3D& g, int bc, int l, int x, int y, int z) {
   if (y < 0) y += g.ny; else if (y >= g.ny) y -= g.ny;
   if (z < 0) z += g.nz; else if (z >= g.nz) z -= g.nz;
-  return v[((size_t)z * g.ny + y) * g.nx + x];
+  bool neg = false;
+  if (x < 0) {
+    if (bc == BC_PERIODIC) x += g.nx;
+    else if (l == 0) { x = 0; neg = true; }
+    else x = 1;
+  } else if (x >= g.nx) {
+    if (bc == BC_PERIODIC) x -= g.nx;
+    else if (l == 0) { x = g.nx - 3; neg = true; }
+    else x = g.nx - 2;
+  }
+  return flip_sign(v[((size_t)z * g.ny + y) * g.nx + x], neg);
 }
 
 __device__ __forceinline__ void final_sums3(const Dev3D& d, int l, double* sh, double* out0, double* out1) {
@@ -529,11 +542,21 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg3_init(Dev3D d) {
   const double f4 = d.ph.f4, f5 = d.ph.f5;
   // phi = db(l) over the interior, viewed with periodic ghosts
   const double* db = d.df + (size_t)l * g.fvol;
+  const int bc = d.ph.bc;
   auto ph = [&](int x, int y, int z) {
-    if (x < 0) x += g.nx; else if (x >= g.nx) x -= g.nx;
     if (y < 0) y += g.ny; else if (y >= g.ny) y -= g.ny;
     if (z < 0) z += g.nz; else if (z >= g.nz) z -= g.nz;
-    return db[f3(g, x + 2, y + 2, z + 2)];
+    bool neg = false;
+    if (x < 0) {
+      if (bc == BC_PERIODIC) x += g.nx;
+      else if (l == 0) { x = 0; neg = true; }
+      else x = 1;
+    } else if (x >= g.nx) {
+      if (bc == BC_PERIODIC) x -= g.nx;
+      else if (l == 0) { x = g.nx - 3; neg = true; }
+      else x = g.nx - 2;
+    }
+    return flip_sign(db[f3(g, x + 2, y + 2, z + 2)], neg);
   };
   double sb = 0.0, sr = 0.0;
   for (size_t c = (size_t)blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += (size_t)gridDim.x * CG_THREADS) {
@@ -586,8 +609,10 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg3_ap(Dev3D d) {
   for (size_t c = (size_t)blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += (size_t)gridDim.x * CG_THREADS) {
     const int cx = (int)(c % g.nx), cy = (int)((c / g.nx) % g.ny), cz = (int)(c / ((size_t)g.nx * g.ny));
     const double pc = p[c];
-    const double ap = -v3_at(p, g, cx, cy, cz - 1) - v3_at(p, g, cx, cy - 1, cz) - v3_at(p, g, cx - 1, cy, cz) +
-                      f4 * pc - v3_at(p, g, cx + 1, cy, cz) - v3_at(p, g, cx, cy + 1, cz) - v3_at(p, g, cx, cy, cz + 1);
+    const int bc = d.ph.bc;
+    const double ap = -v3_at(p, g, bc, l, cx, cy, cz - 1) - v3_at(p, g, bc, l, cx, cy - 1, cz) -
+                      v3_at(p, g, bc, l, cx - 1, cy, cz) + f4 * pc - v3_at(p, g, bc, l, cx + 1, cy, cz) -
+                      v3_at(p, g, bc, l, cx, cy + 1, cz) - v3_at(p, g, bc, l, cx, cy, cz + 1);
     d.ap[off + c] = ap;
     s2 = s2 + pc * ap;
   }

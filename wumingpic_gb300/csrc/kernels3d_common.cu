@@ -108,7 +108,8 @@ void curre_fold3d(const Dev3D& d, cudaStream_t s) {
   k_curre3d_z<<<(g.fp * g.ny + 127) / 128, 128, 0, s>>>(d);
   k_curre3d_margin_y<<<(g.fp * g.nz + 127) / 128, 128, 0, s>>>(d);
   k_curre3d_margin_z<<<(g.fp * (g.ny + 2) + 127) / 128, 128, 0, s>>>(d);
-  k_curre3d_x<<<((g.ny + 4) * (g.nz + 4) + 127) / 128, 128, 0, s>>>(d);
+  // boundary_reconnection__curre has no x stage (3d/proj/reconnection/boundary_reconnection.f90:689-978)
+  if (d.ph.bc == BC_PERIODIC) k_curre3d_x<<<((g.ny + 4) * (g.nz + 4) + 127) / 128, 128, 0, s>>>(d);
 }
 
 // ---------------------------------------------------------------------------
@@ -130,7 +131,36 @@ __global__ void k_dfield3d(Dev3D d) {
   }
 }
 
-void dfield_ghost3d(const Dev3D& d, cudaStream_t s) { k_dfield3d<<<8 * 152, 256, 0, s>>>(d); }
+// boundary_reconnection__dfield (3d/proj/reconnection/boundary_reconnection.f90:466-686): the
+// periodic y and z copies over the interior x columns, then at the walls, for every (j, k)
+// including the ghosts, Bx and (Ey, Ez) odd -- column nxs-1 from nxs, column nxe (an interior
+// column) from nxe-1 -- and (By, Bz, Ex) even -- nxs-1 from nxs+1, nxe+1 from nxe-1; columns
+// nxs-2 and nxe+2 are left as they are.  Every value read is an interior-x value the rule does
+// not write, so one pass over the cells is the reference's sequence.
+__global__ void k_dfield3d_walls(Dev3D d) {
+  const Grid3D g = d.g;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < g.fvol; t += (size_t)gridDim.x * blockDim.x) {
+    const int fi = (int)(t % g.fp), fj = (int)((t / g.fp) % (g.ny + 4)), fk = (int)(t / g.fplane);
+    const bool yz_ghost = fj < 2 || fj >= g.ny + 2 || fk < 2 || fk >= g.nz + 2;
+    int sj = fj - 2, sk = fk - 2;
+    sj = sj < 0 ? sj + g.ny : (sj >= g.ny ? sj - g.ny : sj);
+    sk = sk < 0 ? sk + g.nz : (sk >= g.nz ? sk - g.nz : sk);
+    auto src = [&](int l, int si) { return d.df[(size_t)l * g.fvol + g3(g, si, sj + 2, sk + 2)]; };
+    for (int l = 0; l < 6; ++l) {
+      const bool odd = l == 0 || l == 4 || l == 5;
+      double* out = d.df + (size_t)l * g.fvol + t;
+      if (fi == 1) *out = odd ? -src(l, 2) : src(l, 3);
+      else if (fi == g.nx + 1 && odd) *out = -src(l, g.nx);
+      else if (fi == g.nx + 2 && !odd) *out = src(l, g.nx);
+      else if (fi >= 2 && fi <= g.nx + 1 && yz_ghost) *out = src(l, fi);
+    }
+  }
+}
+
+void dfield_ghost3d(const Dev3D& d, cudaStream_t s) {
+  if (d.ph.bc == BC_PERIODIC) k_dfield3d<<<8 * 152, 256, 0, s>>>(d);
+  else k_dfield3d_walls<<<8 * 152, 256, 0, s>>>(d);
+}
 
 // uf += df over the whole ghosted extent (3d/common/field.f90:196-205)
 __global__ void k_uf_add3d(Dev3D d) {
@@ -159,7 +189,34 @@ __global__ void k_particle_x3d(Dev3D d, Parts3D P) {  // one block per row
   }
 }
 
-void particle_x3d(const Dev3D& d, const Parts3D& P, cudaStream_t s) { k_particle_x3d<<<d.nrow, 256, 0, s>>>(d, P); }
+// boundary_reconnection__particle_x (3d/proj/reconnection/boundary_reconnection.f90:69-109): cell
+// int(x / dx) below nxs+1 or from nxe-1 on reflects about that face, 2 (nxs+1) dx - x or
+// 2 (nxe-1) dx - x, all three momentum components reversed; separately rounded as the reference
+__global__ void k_particle_x3d_walls(Dev3D d, Parts3D P) {  // one block per row
+  const int row = blockIdx.x;
+  const Grid3D g = d.g;
+  const int nxs = g.nxgs, nxe = g.nxgs + g.nx - 1;
+  const double delx = d.ph.delx;
+  const int n = d.np2[row];
+  for (int s = threadIdx.x; s < n; s += blockDim.x) {
+    const size_t k = (size_t)row * d.cap + s;
+    const double x = P.x[k];
+    const int ipos = (int)__ddiv_rn(x, delx);
+    double face;
+    if (ipos < nxs + 1) face = __dmul_rn(2.0 * (nxs + 1), delx);
+    else if (ipos >= nxe - 1) face = __dmul_rn(2.0 * (nxe - 1), delx);
+    else continue;
+    P.x[k] = __dsub_rn(face, x);
+    P.ux[k] = -P.ux[k];
+    P.uy[k] = -P.uy[k];
+    P.uz[k] = -P.uz[k];
+  }
+}
+
+void particle_x3d(const Dev3D& d, const Parts3D& P, cudaStream_t s) {
+  if (d.ph.bc == BC_PERIODIC) k_particle_x3d<<<d.nrow, 256, 0, s>>>(d, P);
+  else k_particle_x3d_walls<<<d.nrow, 256, 0, s>>>(d, P);
+}
 
 // ---------------------------------------------------------------------------
 // boundary_periodic__particle_yz (3d/common/boundary_periodic.f90:104-455), first phase:
@@ -584,8 +641,13 @@ __global__ void k_mom3_fold_x(Dev3D d, double* mom) {
   if (t >= 7LL * (g.ny + 2) * (g.nz + 2) * d.ph.nsp) return;
   const int l = (int)(t % 7);
   double* m = mom + (t / 7) * nxm * 7 + l;
-  m[7] = m[7] + m[7 * (size_t)(g.nx + 1)];
-  m[7 * (size_t)g.nx] = m[7 * (size_t)g.nx] + m[0];
+  if (d.ph.bc == BC_PERIODIC) {
+    m[7] = m[7] + m[7 * (size_t)(g.nx + 1)];
+    m[7 * (size_t)g.nx] = m[7 * (size_t)g.nx] + m[0];
+  } else {  // boundary_reconnection__mom (:1134-1137): the x ghosts onto the wall columns
+    m[7] = m[7] + m[0];
+    m[7 * (size_t)g.nx] = m[7 * (size_t)g.nx] + m[7 * (size_t)(g.nx + 1)];
+  }
 }
 
 __global__ void k_mom3_fold_y(Dev3D d, double* mom) {

@@ -13,7 +13,7 @@ module wpic3d_capi
      integer(c_int) :: ndim, np, nsp, nxgs, nxge, nygs, nyge, nzgs, nzge, nys, nye, nzs, nze
      real(c_double) :: delx, delt, c, gfac
      real(c_double) :: q(2), r(2)
-     integer(c_int) :: precision, device_cap
+     integer(c_int) :: precision, device_cap, bc_kind
   end type wpic_params3d
 
   interface
@@ -94,6 +94,7 @@ module wpic3d_capi
   type(c_ptr), save :: wpic3_ctx = c_null_ptr
   type(wpic_params3d), save :: wpic3_prm
   logical, save :: wpic3_uploaded = .false.
+  logical, save :: wpic3_bc_set = .false.  ! a boundary module's __init chose the kind
   integer, save :: wpic3_sync_every = 1, wpic3_step_count = 0
 
 contains
@@ -137,6 +138,7 @@ contains
     wpic3_prm%delx = delx_in; wpic3_prm%delt = delt_in; wpic3_prm%c = c_in
     wpic3_prm%q(1:nsp_in) = q_in; wpic3_prm%r(1:nsp_in) = r_in
     wpic3_prm%precision = 0; wpic3_prm%device_cap = 0
+    if (.not. wpic3_bc_set) wpic3_prm%bc_kind = 0
   end subroutine particle__init
 
   subroutine particle__solv(gp,up,uf,cumcnt,nxs,nxe)
@@ -282,6 +284,62 @@ contains
     call wpic3_check(wpic3d_get_mom(wpic3_ctx, mom), 'get mom')
   end subroutine boundary_periodic__mom
 end module boundary_periodic
+
+
+! boundary_reconnection (3d/proj/reconnection/boundary_reconnection.f90): conducting walls in x,
+! periodic in y and z.  Its init selects the wall rules of the library's boundary kernels; the
+! reflection runs in bc__particle_x, the other rules inside field__fdtd_i and bc__mom.
+module boundary_reconnection
+  use wpic3d_capi
+  implicit none
+  private
+  public :: boundary_reconnection__init, boundary_reconnection__dfield, boundary_reconnection__particle_x, &
+       boundary_reconnection__particle_yz, boundary_reconnection__curre, boundary_reconnection__phi, &
+       boundary_reconnection__mom
+contains
+  subroutine boundary_reconnection__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nzgs_in, &
+                                         nzge_in,nys_in,nye_in,nzs_in,nze_in,jup_in,jdown_in,kup_in,kdown_in, &
+                                         mnpi_in,mnpr_in,ncomw_in,nerr_in,nstat_in,delx_in,delt_in,c_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in
+    integer, intent(in) :: nxgs_in, nxge_in, nygs_in, nyge_in, nzgs_in, nzge_in, nys_in, nye_in, nzs_in, nze_in
+    integer, intent(in) :: jup_in, jdown_in, kup_in, kdown_in, mnpi_in, mnpr_in, ncomw_in, nerr_in, nstat_in(:)
+    real(8), intent(in) :: delx_in, delt_in, c_in
+    wpic3_prm%bc_kind = 1; wpic3_bc_set = .true.
+  end subroutine boundary_reconnection__init
+
+  subroutine boundary_reconnection__particle_x(up,np2,nxs,nxe)
+    integer, intent(in)    :: nxs, nxe
+    real(8), intent(inout) :: up(*)
+    integer, intent(in)    :: np2(*)
+    call wpic3_check(wpic3d_bc_particle_x(wpic3_ctx), 'bc__particle_x')
+  end subroutine boundary_reconnection__particle_x
+
+  subroutine boundary_reconnection__particle_yz(up,np2)
+    real(8), intent(inout) :: up(*)
+    integer, intent(inout) :: np2(*)
+    call wpic3_check(wpic3d_bc_particle_yz(wpic3_ctx), 'bc__particle_yz')
+  end subroutine boundary_reconnection__particle_yz
+
+  ! applied inside the library; present so that field__fdtd_i's arguments type-check
+  subroutine boundary_reconnection__dfield(df,nxs,nxe,nys,nye,nzs,nze,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nzs, nze, nxgs, nxge
+    real(8), intent(inout) :: df(*)
+  end subroutine boundary_reconnection__dfield
+  subroutine boundary_reconnection__curre(uj,nxs,nxe,nys,nye,nzs,nze,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nzs, nze, nxgs, nxge
+    real(8), intent(inout) :: uj(*)
+  end subroutine boundary_reconnection__curre
+  subroutine boundary_reconnection__phi(phi,nxs,nxe,nys,nye,nzs,nze,l)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nzs, nze, l
+    real(8), intent(inout) :: phi(*)
+  end subroutine boundary_reconnection__phi
+
+  subroutine boundary_reconnection__mom(mom)
+    real(8), intent(inout) :: mom(*)
+    call wpic3_check(wpic3d_bc_mom(wpic3_ctx), 'bc__mom')
+    call wpic3_check(wpic3d_get_mom(wpic3_ctx, mom), 'get mom')
+  end subroutine boundary_reconnection__mom
+end module boundary_reconnection
 
 
 ! mom_calc (3d/common/mom_calc.f90) on the device, as in the 2D shim

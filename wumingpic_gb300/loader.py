@@ -338,6 +338,7 @@ class Plasma3D:
     nxgs: int = 2
     nygs: int = 2
     nzgs: int = 2
+    bc: str = "periodic"          # or "reconnection": conducting walls in x (3d/proj/reconnection)
 
     @property
     def nxge(self):
@@ -366,7 +367,8 @@ class Plasma3D:
 
     @property
     def n_particles(self):
-        return self.nx * self.ny * self.nz * self.ppc * self.nsp
+        cells_x = self.nx if self.bc == "periodic" else self.nx - 3
+        return cells_x * self.ny * self.nz * self.ppc * self.nsp
 
 
 @dataclass
@@ -398,8 +400,10 @@ def load_weibel3d(p: Plasma3D) -> State3D:
     rng = np.random.Generator(np.random.Philox(p.seed))
     st = empty_state3d(p)
     nx, ny, nz, n0 = p.nx, p.ny, p.nz, p.ppc
-    npr = nx * n0
-    ix = np.repeat(np.arange(nx), n0)
+    # with conducting walls in x the plasma fills the cells between them, [nxs+1, nxe-1)
+    c_lo, c_hi = (0, nx) if p.bc == "periodic" else (1, nx - 2)
+    npr = (c_hi - c_lo) * n0
+    ix = np.repeat(np.arange(c_lo, c_hi), n0)
     rx = rng.random((nz, ny, npr))
     ry = rng.random((nz, ny, npr))
     rz = rng.random((nz, ny, npr))
@@ -422,7 +426,8 @@ def load_weibel3d(p: Plasma3D) -> State3D:
         pid = row[None, :, :] * npr + np.arange(1, npr + 1, dtype=np.int64)[:, None, None]
         st.up[6, :npr, :, :, isp] = (-pid).view(np.float64)
     st.np2[:, :, :] = npr
-    st.cumcnt[:, :, :, :] = (np.arange(nx + 1, dtype=np.int32) * n0)[:, None, None, None]
+    cc = (np.clip(np.arange(nx + 1), c_lo, c_hi) - c_lo).astype(np.int32) * n0
+    st.cumcnt[:, :, :, :] = cc[:, None, None, None]
     st.gp[...] = st.up
     return st
 

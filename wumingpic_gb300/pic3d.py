@@ -36,6 +36,7 @@ class Pic3D:
         prm.r[0], prm.r[1] = r[0], r[1]
         prm.precision = {"fp64": _lib.FP64, "fp64_exact": _lib.FP64_EXACT, "mixed": _lib.MIXED}[precision]
         prm.device_cap = int(device_cap)
+        prm.bc_kind = {"periodic": _lib.BC_PERIODIC, "reconnection": _lib.BC_RECONNECTION}[getattr(plasma, "bc", "periodic")]
         self.precision = precision
         h = ctypes.c_void_p()
         check(lib().wpic3d_init(ctypes.byref(h), ctypes.byref(prm), ctypes.c_void_p(stream or 0)), "wpic3d_init")
