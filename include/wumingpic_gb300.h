@@ -257,9 +257,9 @@ typedef struct wpic_params3d {
   double q[2], r[2];
   int precision;            /* WPIC_FP64, WPIC_FP64_EXACT or WPIC_MIXED */
   int device_cap;           /* device particle slots per row per species; 0 = np */
-  int bc_kind;              /* WPIC_BC_PERIODIC (3d/common/boundary_periodic.f90) or WPIC_BC_RECONNECTION:
-                               conducting walls in x, 3d/proj/reconnection/boundary_reconnection.f90
-                               (FP64 paths) */
+  int bc_kind;              /* WPIC_BC_PERIODIC (3d/common/boundary_periodic.f90), WPIC_BC_RECONNECTION:
+                               conducting walls in x, 3d/proj/reconnection/boundary_reconnection.f90,
+                               or WPIC_BC_SHOCK: 3d/proj/shock/boundary_shock.f90 (FP64 paths) */
 } wpic_params3d;
 
 /* particle__init + field__init + sort__init + bc__init of a 3D run
@@ -296,6 +296,13 @@ int wpic3d_ele_cur(wpic_ctx3d* ctx);
 int wpic3d_bc_particle_x(wpic_ctx3d* ctx);
 /* bc__particle_yz(gp, np2)                           3d/common/boundary_periodic.f90:104 */
 int wpic3d_bc_particle_yz(wpic_ctx3d* ctx);
+/* the shock run (bc_kind WPIC_BC_SHOCK, FP64 paths; 3d/proj/shock): the active x window nxs..nxe
+ * every module call receives (3d/proj/shock/app.f90:112-117, widened by relocate at :654), the
+ * injection boundary's upstream four-velocity u0 for wpic3d_step, and
+ * boundary_shock__injection(gp,np2,nxs,nxe,u0) (3d/proj/shock/boundary_shock.f90:424) on gp */
+int wpic3d_set_window(wpic_ctx3d* ctx, int nxs, int nxe);
+int wpic3d_set_injection(wpic_ctx3d* ctx, double u0);
+int wpic3d_bc_injection(wpic_ctx3d* ctx, double u0);
 /* sort__bucket(up, gp, cumcnt, np2, nxs, nxe)        3d/common/sort.f90:40 */
 int wpic3d_sort_bucket(wpic_ctx3d* ctx);
 /* the driver loop body (3d/proj/weibel/app.f90:103-108), nsteps times */

@@ -75,6 +75,7 @@ def lib():
             L.orc3d_ele_cur.argtypes = [vp, dp, dp, dp, ip, i, i]
             L.orc3d_bc_curre.argtypes = [vp, dp, i, i]
             L.orc3d_bc_dfield.argtypes = [vp, dp, i, i]
+            L.orc3d_bc_injection.argtypes = [vp, dp, ip, i, i, d]
             L.orc3d_field_fdtd_i.argtypes = [vp, dp, dp, dp, ip, i, i]
             L.orc3d_bc_particle_x.argtypes = [vp, dp, ip]
             L.orc3d_bc_particle_yz.argtypes = [vp, dp, ip]
@@ -255,7 +256,16 @@ class Oracle3D:
                                      _p(q, np.float64), _p(r, np.float64), gfac)
         lib().orc3d_set_threads(self._h, threads)
         self.bc = bc
-        lib().orc3d_set_bc(self._h, {"periodic": 0, "reconnection": 1}[bc])
+        self.u0 = 0.0
+        lib().orc3d_set_bc(self._h, {"periodic": 0, "reconnection": 1, "shock": 2}[bc])
+
+    def set_window(self, nxs, nxe):
+        """the active x window nxs..nxe the shock driver passes (3d/proj/shock/app.f90:112-117, 654)"""
+        self.nxs, self.nxe = int(nxs), int(nxe)
+
+    def bc_injection(self, up, np2, u0=None):
+        return lib().orc3d_bc_injection(self._h, _p(up, np.float64), _p(np2, np.int32), self.nxs, self.nxe,
+                                        self.u0 if u0 is None else u0)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -360,6 +370,8 @@ class Oracle3D:
         rc = push(st.gp, st.up, st.uf, st.cumcnt)
         if self.bc == "reconnection":
             rc = rc or self.bc_particle_x(st.gp, st.np2)
+        if self.bc == "shock":  # 3d/proj/shock/app.f90:112-117: injection, no particle_x
+            rc = rc or self.bc_injection(st.gp, st.np2)
         rc = rc or self.field_fdtd_i(st.uf, st.up, st.gp, st.cumcnt)
         if self.bc == "periodic":
             rc = rc or self.bc_particle_x(st.gp, st.np2)

@@ -21,6 +21,8 @@
 //   boundary_reconnection__particle_x/dfield/curre/phi/mom (conducting walls in x; its
 //   particle_yz is boundary_periodic's)
 //                             3d/proj/reconnection/boundary_reconnection.f90:69-1255
+//   boundary_shock__injection/dfield/curre/phi/mom (wall at nxs, open end at nxe of the window)
+//                             3d/proj/shock/boundary_shock.f90:424-1245
 //
 // Parity status: UNPINNED (no golden vectors in the reference for this path;
 // no Fortran compiler or MPI in this image).  It is checked against physical
@@ -46,7 +48,8 @@ namespace {
 
 enum { ORC_OK = 0, ORC_CG_NOT_CONVERGED = 1, ORC_CAPACITY = 2, ORC_OUT_OF_RANGE = 3 };
 
-enum { BC3_PERIODIC = 0, BC3_WALLS = 1 };  // boundary_periodic / boundary_reconnection (3D)
+// boundary_periodic / boundary_reconnection / boundary_shock (3D)
+enum { BC3_PERIODIC = 0, BC3_WALLS = 1, BC3_SHOCK = 2 };
 
 struct Orc3D {
   int ndim, np, nsp, nxgs, nxge, nygs, nyge, nzgs, nzge, nys, nye, nzs, nze;
@@ -463,7 +466,8 @@ void bc_curre(Orc3D* o, double* uj, int nxs, int nxe) {
   // x: fold then refresh over the whole ghosted (j, k) range, one array statement after another;
   // boundary_reconnection__curre has no x stage
   // (3d/proj/reconnection/boundary_reconnection.f90:689-978)
-  if (o->bc_kind == BC3_WALLS) return;
+  // (boundary_shock__curre likewise, 3d/proj/shock/boundary_shock.f90:690-974)
+  if (o->bc_kind != BC3_PERIODIC) return;
   const int jlo = nys - 2, jhi = nye + 2, klo = nzs - 2, khi = nze + 2;
   auto xstmt = [&](int dst, int src, bool add) {
     for (int k = klo; k <= khi; ++k)
@@ -521,6 +525,18 @@ void bc_dfield(Orc3D* o, double* df, int nxs, int nxe) {
   };
   zcopy(nze + 1, nze + 2, nzs, nzs + 1);
   zcopy(nzs - 2, nzs - 1, nze - 1, nze);
+  if (o->bc_kind == BC3_SHOCK) {
+    // boundary_shock__dfield (3d/proj/shock/boundary_shock.f90:675-684): the wall at nxs as the
+    // reconnection walls, every component zero in column nxe+1
+    for (int k = nzs - 2; k <= nze + 2; ++k)
+      for (int j = nys - 2; j <= nye + 2; ++j) {
+        D(1, nxs - 1, j, k) = -D(1, nxs, j, k);
+        for (int l = 2; l <= 4; ++l) D(l, nxs - 1, j, k) = D(l, nxs + 1, j, k);
+        for (int l = 5; l <= 6; ++l) D(l, nxs - 1, j, k) = -D(l, nxs, j, k);
+        for (int l = 1; l <= 6; ++l) D(l, nxe + 1, j, k) = 0.0;
+      }
+    return;
+  }
   if (o->bc_kind == BC3_WALLS) {
     // boundary_reconnection__dfield's walls (3d/proj/reconnection/boundary_reconnection.f90:674-683):
     // Bx and (Ey, Ez) odd, (By, Bz, Ex) even, with the offsets of each wall; nxs-2 and nxe+2 untouched
@@ -578,6 +594,15 @@ void bc_phi(Orc3D* o, double* phi, int nxs, int nxe, int l) {
   n = 0;
   for (int j = nys - 1; j <= nye + 1; ++j)
     for (int i = nxs; i <= nxe; ++i) P(i, j, nzs - 1) = s[n++];
+  if (o->bc_kind == BC3_SHOCK) {
+    // boundary_shock__phi (3d/proj/shock/boundary_shock.f90:1084-1107): the wall at nxs, zero at nxe+1
+    for (int k = nzs - 1; k <= nze + 1; ++k)
+      for (int j = nys - 1; j <= nye + 1; ++j) {
+        P(nxs - 1, j, k) = l == 1 ? -P(nxs, j, k) : P(nxs + 1, j, k);
+        P(nxe + 1, j, k) = 0.0;
+      }
+    return;
+  }
   if (o->bc_kind == BC3_WALLS) {
     // boundary_reconnection__phi (3d/proj/reconnection/boundary_reconnection.f90:1093-1117):
     // component 1 odd about nxs and nxe-1, components 2 and 3 even about nxs and nxe
@@ -805,6 +830,41 @@ int bc_particle_x(Orc3D* o, double* up, const int* np2) {
             x = x + (double)(o->nxge - o->nxgs + 1) * delx;
           else if (ipos >= o->nxge + 1)
             x = x - (double)(o->nxge - o->nxgs + 1) * delx;
+        }
+  }
+  return ORC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// boundary_shock__injection (3d/proj/shock/boundary_shock.f90:424-469): reflection at the wall
+// x = (nxs+1) dx, and at xend = nxe dx + v0 dt (v0 = u0 / sqrt(1 + u0^2/c^2)) with u_x -> 2 u0 - u_x
+// ---------------------------------------------------------------------------
+int bc_injection(Orc3D* o, double* up, const int* np2, int nxs, int nxe, double u0) {
+  const int nys = o->nys, nye = o->nye, nzs = o->nzs, nze = o->nze;
+  const double delx = o->delx, c = o->c, delt = o->delt, d_delx = o->d_delx;
+  const double xend = nxe * delx + u0 / std::sqrt(1.0 + (u0 * u0) / (c * c)) * delt;
+  set_threads(o);
+  for (int isp = 1; isp <= o->nsp; ++isp) {
+#pragma omp parallel for
+    for (int k = nzs; k <= nze; ++k)
+      for (int j = nys; j <= nye; ++j)
+        for (int ii = 1; ii <= np2[o->inp2(j, k, isp)]; ++ii) {
+          double& x = up[o->iup(1, ii, j, k, isp)];
+          double& ux = up[o->iup(4, ii, j, k, isp)];
+          double& uy = up[o->iup(5, ii, j, k, isp)];
+          double& uz = up[o->iup(6, ii, j, k, isp)];
+          const int ipos = (int)(x * d_delx);
+          if (ipos < nxs + 1) {
+            x = 2.0 * (nxs + 1) * delx - x;
+            ux = -ux;
+            uy = -uy;
+            uz = -uz;
+          } else if (x > xend) {
+            x = 2.0 * xend - x;
+            ux = 2.0 * u0 - ux;
+            uy = -uy;
+            uz = -uz;
+          }
         }
   }
   return ORC_OK;
@@ -1066,7 +1126,9 @@ void bc_mom(Orc3D* o, double* mom) {
     for (int k = nzs - 1; k <= nze + 1; ++k)
       for (int j = nys - 1; j <= nye + 1; ++j)
         for (int l = 1; l <= 7; ++l) {
-          if (o->bc_kind == BC3_WALLS) {  // boundary_reconnection__mom (:1134-1137): x ghosts onto the wall columns
+          if (o->bc_kind != BC3_PERIODIC) {  // boundary_reconnection__mom (:1134-1137), boundary_shock__mom
+                                             // (3d/proj/shock/boundary_shock.f90:1124-1127): x ghosts onto the
+                                             // edge columns
             M(l, nxgs, j, k, isp) = M(l, nxgs, j, k, isp) + M(l, nxgs - 1, j, k, isp);
             M(l, nxge, j, k, isp) = M(l, nxge, j, k, isp) + M(l, nxge + 1, j, k, isp);
           } else {
@@ -1119,7 +1181,12 @@ void* orc3d_create(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int 
   return o;
 }
 void orc3d_destroy(void* h) { delete (Orc3D*)h; }
-void orc3d_set_bc(void* h, int bc_kind) { ((Orc3D*)h)->bc_kind = bc_kind == BC3_WALLS ? BC3_WALLS : BC3_PERIODIC; }
+void orc3d_set_bc(void* h, int bc_kind) {
+  ((Orc3D*)h)->bc_kind = (bc_kind == BC3_WALLS || bc_kind == BC3_SHOCK) ? bc_kind : BC3_PERIODIC;
+}
+int orc3d_bc_injection(void* h, double* up, const int* np2, int nxs, int nxe, double u0) {
+  return bc_injection((Orc3D*)h, up, np2, nxs, nxe, u0);
+}
 void orc3d_set_threads(void* h, int n) { ((Orc3D*)h)->nthreads = n > 0 ? n : 1; }
 void orc3d_cg_control(void* h, const int* fixed3, int ite_max) {
   Orc3D* o = (Orc3D*)h;

@@ -345,3 +345,84 @@ def test_walls_rejected_on_the_mixed_path_3d(gpu_lib):
     with pytest.raises(WpicError):
         make_gpu(p, "mixed", gpu_lib)
 
+
+
+# ---- the shock boundary (3d/proj/shock/boundary_shock.f90) on a window nxs..nxe ----
+
+def shock_case(seed, **kw):
+    kw.setdefault("u_the", 0.1)
+    p, st = perturbed_case(seed=seed, nx=12, ny=6, nz=5, ppc=4, bc="shock", window=9, u0=0.2, **kw)
+    return p, st
+
+
+def shock_oracle(p):
+    o = make_oracle(p)
+    o.set_window(p.nxgs, p.nxe)
+    o.u0 = p.u0
+    return o
+
+
+def test_shock_injection_exact_3d(gpu_lib):
+    """boundary_shock__injection on pushed particles: bit-exact against the oracle."""
+    p, st = shock_case(81, u_the=0.4)
+    g = make_gpu(p, "fp64_exact", gpu_lib)
+    g.put_state(st)
+    g.particle__solv()
+    g.bc__injection(p.u0)
+    gp, np2, _ = g.get_particles(1)
+    o = shock_oracle(p)
+    ref = st.copy()
+    assert o.particle_solv(ref.gp, ref.up, ref.uf, ref.cumcnt) == 0
+    assert o.bc_injection(ref.gp, ref.np2) == 0
+    assert_particles(gp, np2, ref.gp, ref.np2)
+    g.close()
+
+
+def test_shock_steps_exact_3d(gpu_lib):
+    p, st = shock_case(82)
+    for steps, rel in ((1, 0.0), (2, 1e-12)):
+        g = make_gpu(p, "fp64_exact", gpu_lib)
+        g.put_state(st)
+        o = shock_oracle(p)
+        ref = st.copy()
+        for _ in range(steps):
+            g.step(1)
+            o.cg_control(fixed=g.cg_iters())
+            assert o.step(ref) == 0
+        out = g.get_state()
+        assert_particles(out.up, out.np2, ref.up, ref.np2, rel)
+        # the reference's sort writes cumcnt(nxs:nxe+1) only; beyond the window its copy is stale
+        np.testing.assert_array_equal(out.cumcnt[:p.window + 1], ref.cumcnt[:p.window + 1])
+        assert_field(out.uf, ref.uf, 1e-12)
+        g.close()
+
+
+def test_shock_steps_with_expanding_window_3d(gpu_lib):
+    """Three steps, the window widened by one (empty) cell as the driver's relocate() does
+    (3d/proj/shock/app.f90:654), three more; the oracle's cumcnt of the new cell follows the
+    row total as the driver keeps it."""
+    p, st = shock_case(83)
+    g = make_gpu(p, "fp64", gpu_lib)
+    g.put_state(st)
+    o = shock_oracle(p)
+    ref = st.copy()
+    for k in range(6):
+        if k == 3:
+            g.set_window(p.nxgs, p.nxe + 1)
+            o.set_window(p.nxgs, p.nxe + 1)
+            ref.cumcnt[p.window + 1, ...] = ref.cumcnt[p.window, ...]
+        g.step(1)
+        o.cg_control(fixed=g.cg_iters())
+        assert o.step(ref) == 0
+    out = g.get_state()
+    np.testing.assert_array_equal(out.np2, ref.np2)
+    assert_particles(out.up, out.np2, ref.up, ref.np2, rel=1e-10)
+    assert_field(out.uf, ref.uf, 1e-10)
+    g.close()
+
+
+def test_shock_rejected_on_the_mixed_path_3d(gpu_lib):
+    from wumingpic_gb300._lib import WpicError
+    p, st = small_case3d(nx=16, ny=16, nz=8, ppc=2, seed=84, bc="shock", window=12, u0=0.1)
+    with pytest.raises(WpicError):
+        make_gpu(p, "mixed", gpu_lib)

@@ -332,3 +332,93 @@ def test_walls_moments_3d():
     assert rc == 0
     ref = literal_moments3d(p, st.gp, st.np2, bc="reconnection")
     np.testing.assert_allclose(mom, ref, rtol=0, atol=1e-13 * np.abs(ref).max())
+
+
+# ---- the shock boundary (3d/proj/shock/boundary_shock.f90): wall at nxs, open end at nxe ----
+
+def shock_case(seed, **kw):
+    kw.setdefault("u_the", 0.1)
+    return small_case3d(nx=12, ny=5, nz=4, ppc=4, seed=seed, bc="shock", window=9, u0=0.2, **kw)
+
+
+def shock_oracle(p):
+    o = make_oracle3d(p, bc="shock")
+    o.set_window(p.nxgs, p.nxe)
+    o.u0 = p.u0
+    return o
+
+
+def test_shock_steps_conserve_charge_3d():
+    """The shock driver's order (3d/proj/shock/app.f90:112-117): push, injection, field solve,
+    y/z migration, sort, on the window; charge conserved to round-off, no particle lost, all
+    between the wall and the injection boundary."""
+    p, st = shock_case(41)
+    q, _ = p.charges()
+    o = shock_oracle(p)
+    for _ in range(4):
+        up0 = st.up.copy(order="F")
+        assert o.particle_solv(st.gp, st.up, st.uf, st.cumcnt) == 0
+        assert o.bc_injection(st.gp, st.np2) == 0
+        assert o.field_fdtd_i(st.uf, st.up, st.gp, st.cumcnt) == 0
+        res, scale = continuity_residual3d(p, q, up0, st.gp, st.np2, o.get_uj())
+        assert res <= 1e-12 * scale, (res, scale)
+        assert o.bc_particle_yz(st.gp, st.np2) == 0
+        assert o.sort_bucket(st.up, st.gp, st.cumcnt, st.np2) == 0
+    assert st.np2.sum() == p.n_particles
+    xend = p.nxe * p.delx + p.u0 / math.sqrt(1 + p.u0 ** 2 / p.c ** 2) * p.delt
+    for isp in range(p.nsp):
+        for kk in range(p.nz):
+            for jj in range(p.ny):
+                x = st.up[0, :st.np2[jj, kk, isp], jj, kk, isp]
+                assert x.min() >= (p.nxgs + 1) * p.delx and x.max() <= xend
+
+
+def test_shock_injection_3d():
+    """boundary_shock__injection: reflection at (nxs+1) dx with all momenta reversed, and at
+    xend = nxe dx + v0 dt with u_x -> 2 u0 - u_x, u_y and u_z reversed (numpy restatement)."""
+    p, st = shock_case(42)
+    o = shock_oracle(p)
+    rng = np.random.default_rng(42)
+    gp = st.up.copy(order="F")
+    n = st.np2[1, 2, 0]
+    xend = p.nxe * p.delx + p.u0 / math.sqrt(1.0 + (p.u0 * p.u0) / (p.c * p.c)) * p.delt
+    gp[0, :n, 1, 2, 0] = rng.uniform(p.nxgs + 0.05, xend + 0.9, n)
+    ref = gp.copy(order="F")
+    x, u = ref[0, :n, 1, 2, 0], ref[3:6, :n, 1, 2, 0]
+    lo = np.trunc(x / p.delx).astype(int) < p.nxgs + 1
+    hi = ~lo & (x > xend)
+    x[lo] = 2.0 * (p.nxgs + 1) * p.delx - x[lo]
+    u[:, lo] = -u[:, lo]
+    x[hi] = 2.0 * xend - x[hi]
+    u[0, hi] = 2.0 * p.u0 - u[0, hi]
+    u[1:, hi] = -u[1:, hi]
+    assert lo.any() and hi.any()
+    assert o.bc_injection(gp, st.np2) == 0
+    np.testing.assert_array_equal(gp, ref)
+
+
+def test_shock_dfield_rule_3d():
+    """boundary_shock__dfield: y and z copies over the window's columns, the wall rule at nxs,
+    zero in column nxe+1; columns beyond are left as they are (numpy restatement)."""
+    p, st = shock_case(43)
+    o = shock_oracle(p)
+    rng = np.random.default_rng(43)
+    df = np.asfortranarray(rng.standard_normal(st.uf.shape))
+    ref = df.copy(order="F")
+    o.bc_dfield(df)
+    ny, nz = p.ny, p.nz
+    s, e = 2, p.nxe - p.nxgs + 2  # array columns of nxs and nxe
+    xs = slice(s, e + 1)
+    ref[:, xs, ny + 2, 2:nz + 2] = ref[:, xs, 2, 2:nz + 2]
+    ref[:, xs, ny + 3, 2:nz + 2] = ref[:, xs, 3, 2:nz + 2]
+    ref[:, xs, 0, 2:nz + 2] = ref[:, xs, ny, 2:nz + 2]
+    ref[:, xs, 1, 2:nz + 2] = ref[:, xs, ny + 1, 2:nz + 2]
+    ref[:, xs, :, nz + 2] = ref[:, xs, :, 2]
+    ref[:, xs, :, nz + 3] = ref[:, xs, :, 3]
+    ref[:, xs, :, 0] = ref[:, xs, :, nz]
+    ref[:, xs, :, 1] = ref[:, xs, :, nz + 1]
+    ref[0, s - 1] = -ref[0, s]
+    ref[1:4, s - 1] = ref[1:4, s + 1]
+    ref[4:6, s - 1] = -ref[4:6, s]
+    ref[:, e + 1] = 0.0
+    np.testing.assert_array_equal(df, ref)

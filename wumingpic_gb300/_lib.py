@@ -92,6 +92,9 @@ def lib():
         L.wpic_set_injection.argtypes = [vp, ctypes.c_double]
         L.wpic_bc_injection.argtypes = [vp, ctypes.c_double]
         L.wpic3d_set_pusher.argtypes = [vp, i]
+        L.wpic3d_set_window.argtypes = [vp, i, i]
+        L.wpic3d_set_injection.argtypes = [vp, ctypes.c_double]
+        L.wpic3d_bc_injection.argtypes = [vp, ctypes.c_double]
         for pre in ("wpic", "wpic3d"):
             getattr(L, pre + "_mom_calc_accl").argtypes = [vp]
             getattr(L, pre + "_mom_calc_nvt").argtypes = [vp, i]

@@ -409,9 +409,7 @@ int mixed_step(wpic_ctx* c) {
 // boundary_shock__injection's right end: xend = nxe dx + v0 dt in the reference's FP64
 // expression (2d/proj/shock/boundary_shock.f90:272)
 double shock_xend(const wpic_ctx* c, double u0) {
-  const double delx = c->d.ph.delx, cl = c->d.ph.c, delt = c->d.ph.delt;
-  const int nxe = c->d.g.nxgs + c->d.g.wx1;
-  return nxe * delx + u0 / std::sqrt(1 + (u0 * u0) / (cl * cl)) * delt;
+  return shock_xend_value(c->d.g.nxgs + c->d.g.wx1, c->d.ph.delx, u0, c->d.ph.c, c->d.ph.delt);
 }
 
 void do_injection(wpic_ctx* c, double u0) {

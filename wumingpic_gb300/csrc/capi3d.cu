@@ -24,6 +24,7 @@ struct wpic_ctx3d {
   double* staging = nullptr;
   size_t staging_bytes = 0;
   int pusher = WPIC_PUSH_BORIS;  // the push of the fused step
+  double u0 = 0.0;               // shock runs: the upstream four-velocity of the injection boundary
   double* mom = nullptr;         // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nzs-1:nze+1, nsp), on first use
   bool mixed = false;            // FP32 push/deposit on split positions (fused step only)
   Mix3Const mk{};
@@ -163,17 +164,23 @@ int mixed_step3(wpic_ctx3d* c) {
   return WPIC_OK;
 }
 
+double shock_xend3(const wpic_ctx3d* c, double u0) {
+  return shock_xend_value(c->d.g.nxgs + c->d.g.wx1, c->d.ph.delx, u0, c->d.ph.c, c->d.ph.delt);
+}
+
 int one_step3(wpic_ctx3d* c) {
   if (c->mixed) return mixed_step3(c);
   if (c->pusher == WPIC_PUSH_VAY) FP3(push_vay3d, c->d, c->stream);
   else FP3(push3d, c->d, c->stream);
   // the reconnection driver reflects at the walls before the field solve
-  // (3d/proj/reconnection/app.f90:103-108), the periodic one wraps after it
-  const bool walls = c->d.ph.bc == BC_RECONNECTION;
-  if (walls) particle_x3d(c->d, c->d.B, c->stream);
+  // (3d/proj/reconnection/app.f90:103-108), the shock driver applies its injection boundary
+  // there and has no particle_x (3d/proj/shock/app.f90:112-117), the periodic one wraps after it
+  const int bc = c->d.ph.bc;
+  if (bc == BC_RECONNECTION) particle_x3d(c->d, c->d.B, c->stream);
+  if (bc == BC_SHOCK) injection3d(c->d, c->d.B, c->u0, shock_xend3(c, c->u0), c->stream);
   int st = do_field3(c);
   if (st) return st;
-  if (!walls) particle_x3d(c->d, c->d.B, c->stream);
+  if (bc == BC_PERIODIC) particle_x3d(c->d, c->d.B, c->stream);
   do_migrate_sort3(c);
   return WPIC_OK;
 }
@@ -214,8 +221,9 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
   if (p->precision != WPIC_FP64 && p->precision != WPIC_FP64_EXACT && p->precision != WPIC_MIXED)
     return WPIC_BAD_ARGUMENT;
   if (p->precision == WPIC_MIXED && !mix3_shape_ok(nx, ny, nz)) return WPIC_BAD_ARGUMENT;
-  if (p->bc_kind != WPIC_BC_PERIODIC && p->bc_kind != WPIC_BC_RECONNECTION) return WPIC_BAD_ARGUMENT;
-  if (p->bc_kind == WPIC_BC_RECONNECTION && (p->precision == WPIC_MIXED || nx < 6)) return WPIC_BAD_ARGUMENT;
+  if (p->bc_kind != WPIC_BC_PERIODIC && p->bc_kind != WPIC_BC_RECONNECTION && p->bc_kind != WPIC_BC_SHOCK)
+    return WPIC_BAD_ARGUMENT;
+  if (p->bc_kind != WPIC_BC_PERIODIC && (p->precision == WPIC_MIXED || nx < 6)) return WPIC_BAD_ARGUMENT;
   if ((double)nx * ny * nz > 2.0e9 || (double)p->nsp * ny * nz * p->np >= 2147483647.0) return WPIC_BAD_ARGUMENT;
   wpic_ctx3d* c = new wpic_ctx3d();
   c->prm = *p;
@@ -226,6 +234,8 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
   d.g.nxgs = p->nxgs;
   d.g.nygs = p->nygs;
   d.g.nzgs = p->nzgs;
+  d.g.wx0 = 0;
+  d.g.wx1 = nx - 1;
   d.g.fp = nx + 4;
   d.g.fplane = (size_t)(nx + 4) * (ny + 4);
   d.g.fvol = d.g.fplane * (nz + 4);
@@ -236,7 +246,7 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
   ph.c = p->c;
   ph.gfac = p->gfac;
   ph.nsp = p->nsp;
-  ph.bc = p->bc_kind == WPIC_BC_RECONNECTION ? BC_RECONNECTION : BC_PERIODIC;
+  ph.bc = p->bc_kind == WPIC_BC_RECONNECTION ? BC_RECONNECTION : p->bc_kind == WPIC_BC_SHOCK ? BC_SHOCK : BC_PERIODIC;
   for (int k = 0; k < 2; ++k) {
     ph.q[k] = k < p->nsp ? p->q[k] : 0.0;
     ph.r[k] = k < p->nsp ? p->r[k] : 1.0;
@@ -444,7 +454,33 @@ int wpic3d_ele_cur(wpic_ctx3d* c) {
 
 int wpic3d_bc_particle_x(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->d.ph.bc == BC_SHOCK) return WPIC_BAD_ARGUMENT;  // boundary_shock has no particle_x
   particle_x3d(c->d, c->d.B, c->stream);
+  return finish3(c);
+}
+
+int wpic3d_set_window(wpic_ctx3d* c, int nxs, int nxe) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  const int nxge = c->d.g.nxgs + c->d.g.nx - 1;
+  if (nxs < c->d.g.nxgs || nxe > nxge || nxe - nxs < 3) return WPIC_BAD_ARGUMENT;
+  const bool full = nxs == c->d.g.nxgs && nxe == nxge;
+  if (!full && c->d.ph.bc != BC_SHOCK) return WPIC_BAD_ARGUMENT;
+  c->d.g.wx0 = nxs - c->d.g.nxgs;
+  c->d.g.wx1 = nxe - c->d.g.nxgs;
+  return WPIC_OK;
+}
+
+int wpic3d_set_injection(wpic_ctx3d* c, double u0) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (!(u0 == u0)) return WPIC_BAD_ARGUMENT;
+  c->u0 = u0;
+  return WPIC_OK;
+}
+
+int wpic3d_bc_injection(wpic_ctx3d* c, double u0) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed || c->d.ph.bc != BC_SHOCK) return WPIC_BAD_ARGUMENT;
+  injection3d(c->d, c->d.B, u0, shock_xend3(c, u0), c->stream);
   return finish3(c);
 }
 

@@ -469,6 +469,7 @@ __global__ void k_gkl3d(Dev3D d) {
   const size_t ncell = g.ncell;
   for (size_t cid = (size_t)blockIdx.x * blockDim.x + threadIdx.x; cid < ncell; cid += (size_t)gridDim.x * blockDim.x) {
     const int cx = (int)(cid % g.nx), cy = (int)((cid / g.nx) % g.ny), cz = (int)(cid / ((size_t)g.nx * g.ny));
+    if (cx < g.wx0 || cx > g.wx1) continue;  // the active window nxs..nxe
     const size_t f = f3(g, cx + 2, cy + 2, cz + 2);
     const size_t V = g.fvol;
     const size_t W = f - 1, E = f + 1, S = f - g.fp, N = f + g.fp, B = f - g.fplane, T = f + g.fplane;
@@ -506,19 +507,28 @@ void gkl3d(const Dev3D& d, cudaStream_t s) { k_gkl3d<<<8 * 152, 256, 0, s>>>(d);
 // in x periodic, or at conducting walls (boundary_reconnection__phi,
 // 3d/proj/reconnection/boundary_reconnection.f90:1093-1117) component 1 odd about nxs and nxe-1,
 // components 2 and 3 even about nxs and nxe
-__device__ __forceinline__ double v3_at(const double* v, const Grid3D& g, int bc, int l, int x, int y, int z) {
+// Ghosts are taken at the edges of the active window nxs..nxe (cells wx0..wx1); beyond a shock
+// run's nxe the value is zero (boundary_shock__phi, 3d/proj/shock/boundary_shock.f90:1084-1107).
+// x0 = -1 marks that zero.
+__device__ __forceinline__ void phi3_src(const Grid3D& g, int bc, int l, int& x, int& y, int& z, bool& neg) {
   if (y < 0) y += g.ny; else if (y >= g.ny) y -= g.ny;
   if (z < 0) z += g.nz; else if (z >= g.nz) z -= g.nz;
-  bool neg = false;
-  if (x < 0) {
+  neg = false;
+  if (x < g.wx0) {
     if (bc == BC_PERIODIC) x += g.nx;
-    else if (l == 0) { x = 0; neg = true; }
-    else x = 1;
-  } else if (x >= g.nx) {
+    else if (l == 0) { x = g.wx0; neg = true; }
+    else x = g.wx0 + 1;
+  } else if (x > g.wx1) {
     if (bc == BC_PERIODIC) x -= g.nx;
-    else if (l == 0) { x = g.nx - 3; neg = true; }
-    else x = g.nx - 2;
+    else if (bc == BC_SHOCK) x = -1;
+    else if (l == 0) { x = g.wx1 - 2; neg = true; }
+    else x = g.wx1 - 1;
   }
+}
+__device__ __forceinline__ double v3_at(const double* v, const Grid3D& g, int bc, int l, int x, int y, int z) {
+  bool neg;
+  phi3_src(g, bc, l, x, y, z, neg);
+  if (x < 0) return 0.0;
   return flip_sign(v[((size_t)z * g.ny + y) * g.nx + x], neg);
 }
 
@@ -544,23 +554,15 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg3_init(Dev3D d) {
   const double* db = d.df + (size_t)l * g.fvol;
   const int bc = d.ph.bc;
   auto ph = [&](int x, int y, int z) {
-    if (y < 0) y += g.ny; else if (y >= g.ny) y -= g.ny;
-    if (z < 0) z += g.nz; else if (z >= g.nz) z -= g.nz;
-    bool neg = false;
-    if (x < 0) {
-      if (bc == BC_PERIODIC) x += g.nx;
-      else if (l == 0) { x = 0; neg = true; }
-      else x = 1;
-    } else if (x >= g.nx) {
-      if (bc == BC_PERIODIC) x -= g.nx;
-      else if (l == 0) { x = g.nx - 3; neg = true; }
-      else x = g.nx - 2;
-    }
+    bool neg;
+    phi3_src(g, bc, l, x, y, z, neg);
+    if (x < 0) return 0.0;
     return flip_sign(db[f3(g, x + 2, y + 2, z + 2)], neg);
   };
   double sb = 0.0, sr = 0.0;
   for (size_t c = (size_t)blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += (size_t)gridDim.x * CG_THREADS) {
     const int cx = (int)(c % g.nx), cy = (int)((c / g.nx) % g.ny), cz = (int)(c / ((size_t)g.nx * g.ny));
+    if (cx < g.wx0 || cx > g.wx1) continue;  // outside the active window: not part of the system
     const double pc = ph(cx, cy, cz);
     const double b = f5 * d.gkl[off + c];
     const double r = b + ph(cx, cy, cz - 1) + ph(cx, cy - 1, cz) + ph(cx - 1, cy, cz) - f4 * pc + ph(cx + 1, cy, cz) +
@@ -608,6 +610,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg3_ap(Dev3D d) {
   double s2 = 0.0;
   for (size_t c = (size_t)blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += (size_t)gridDim.x * CG_THREADS) {
     const int cx = (int)(c % g.nx), cy = (int)((c / g.nx) % g.ny), cz = (int)(c / ((size_t)g.nx * g.ny));
+    if (cx < g.wx0 || cx > g.wx1) continue;
     const double pc = p[c];
     const int bc = d.ph.bc;
     const double ap = -v3_at(p, g, bc, l, cx, cy, cz - 1) - v3_at(p, g, bc, l, cx, cy - 1, cz) -
@@ -645,6 +648,8 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg3_update(Dev3D d) {
   const double av = d.cg[l].av;
   double s1 = 0.0;
   for (size_t c = (size_t)blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += (size_t)gridDim.x * CG_THREADS) {
+    const int cx = (int)(c % g.nx);
+    if (cx < g.wx0 || cx > g.wx1) continue;
     d.phi[off + c] = d.phi[off + c] + av * d.p[off + c];
     const double r = d.r[off + c] - av * d.ap[off + c];
     d.r[off + c] = r;
@@ -685,8 +690,11 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg3_p(Dev3D d) {
   if (d.cg[l].active != 1) return;
   const size_t off = (size_t)l * g.ncell;
   const double bv = d.cg[l].bv;
-  for (size_t c = (size_t)blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += (size_t)gridDim.x * CG_THREADS)
+  for (size_t c = (size_t)blockIdx.x * CG_THREADS + threadIdx.x; c < g.ncell; c += (size_t)gridDim.x * CG_THREADS) {
+    const int cx = (int)(c % g.nx);
+    if (cx < g.wx0 || cx > g.wx1) continue;
     d.p[off + c] = d.r[off + c] + bv * d.p[off + c];
+  }
 }
 
 __global__ void k_cg3_settle(Dev3D d) {
@@ -700,6 +708,7 @@ __global__ void k_cg3_store(Dev3D d) {
     const int l = (int)(t / g.ncell);
     const size_t c = t - (size_t)l * g.ncell;
     const int cx = (int)(c % g.nx), cy = (int)((c / g.nx) % g.ny), cz = (int)(c / ((size_t)g.nx * g.ny));
+    if (cx < g.wx0 || cx > g.wx1) continue;
     d.df[(size_t)l * g.fvol + f3(g, cx + 2, cy + 2, cz + 2)] = d.phi[t];
   }
 }
@@ -729,6 +738,7 @@ __global__ void k_efield3d(Dev3D d) {
   const Grid3D g = d.g;
   for (size_t cid = (size_t)blockIdx.x * blockDim.x + threadIdx.x; cid < g.ncell; cid += (size_t)gridDim.x * blockDim.x) {
     const int cx = (int)(cid % g.nx), cy = (int)((cid / g.nx) % g.ny), cz = (int)(cid / ((size_t)g.nx * g.ny));
+    if (cx < g.wx0 || cx > g.wx1) continue;  // the active window nxs..nxe
     const size_t f = f3(g, cx + 2, cy + 2, cz + 2);
     const size_t V = g.fvol;
     const size_t E = f + 1, N = f + g.fp, T = f + g.fplane;

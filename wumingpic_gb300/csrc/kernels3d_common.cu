@@ -137,8 +137,13 @@ __global__ void k_dfield3d(Dev3D d) {
 // column) from nxe-1 -- and (By, Bz, Ex) even -- nxs-1 from nxs+1, nxe+1 from nxe-1; columns
 // nxs-2 and nxe+2 are left as they are.  Every value read is an interior-x value the rule does
 // not write, so one pass over the cells is the reference's sequence.
+// boundary_shock__dfield (3d/proj/shock/boundary_shock.f90:472-687) differs only at the right
+// end: every component zero in column nxe+1, column nxe kept.  Both act on the window
+// nxs..nxe (array columns wx0+2 .. wx1+2); the y and z copies cover the window's columns.
 __global__ void k_dfield3d_walls(Dev3D d) {
   const Grid3D g = d.g;
+  const bool shock = d.ph.bc == BC_SHOCK;
+  const int cs = g.wx0 + 2, ce = g.wx1 + 2;  // array columns of nxs and nxe
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < g.fvol; t += (size_t)gridDim.x * blockDim.x) {
     const int fi = (int)(t % g.fp), fj = (int)((t / g.fp) % (g.ny + 4)), fk = (int)(t / g.fplane);
     const bool yz_ghost = fj < 2 || fj >= g.ny + 2 || fk < 2 || fk >= g.nz + 2;
@@ -149,10 +154,11 @@ __global__ void k_dfield3d_walls(Dev3D d) {
     for (int l = 0; l < 6; ++l) {
       const bool odd = l == 0 || l == 4 || l == 5;
       double* out = d.df + (size_t)l * g.fvol + t;
-      if (fi == 1) *out = odd ? -src(l, 2) : src(l, 3);
-      else if (fi == g.nx + 1 && odd) *out = -src(l, g.nx);
-      else if (fi == g.nx + 2 && !odd) *out = src(l, g.nx);
-      else if (fi >= 2 && fi <= g.nx + 1 && yz_ghost) *out = src(l, fi);
+      if (fi == cs - 1) *out = odd ? -src(l, cs) : src(l, cs + 1);
+      else if (shock && fi == ce + 1) *out = 0.0;
+      else if (!shock && fi == ce && odd) *out = -src(l, ce - 1);
+      else if (!shock && fi == ce + 1 && !odd) *out = src(l, ce - 1);
+      else if (fi >= cs && fi <= ce && yz_ghost) *out = src(l, fi);
     }
   }
 }
@@ -211,6 +217,36 @@ __global__ void k_particle_x3d_walls(Dev3D d, Parts3D P) {  // one block per row
     P.uy[k] = -P.uy[k];
     P.uz[k] = -P.uz[k];
   }
+}
+
+// boundary_shock__injection (3d/proj/shock/boundary_shock.f90:424-469): cell int(x / dx) (the
+// product with 1/dx) below nxs+1 reflects about (nxs+1) dx with all momenta reversed; beyond
+// xend (computed on the host) x -> 2 xend - x, u_x -> 2 u0 - u_x, u_y and u_z reversed
+__global__ void k_injection3d(Dev3D d, Parts3D P, double u0, double xend) {  // one block per row
+  const int row = blockIdx.x;
+  const int nxs = d.g.nxgs + d.g.wx0;
+  const double delx = d.ph.delx;
+  const int n = d.np2[row];
+  for (int s = threadIdx.x; s < n; s += blockDim.x) {
+    const size_t k = (size_t)row * d.cap + s;
+    const double x = P.x[k];
+    const int ipos = (int)__dmul_rn(x, d.ph.p_d_delx);
+    if (ipos < nxs + 1) {
+      P.x[k] = __dsub_rn(__dmul_rn(2.0 * (nxs + 1), delx), x);
+      P.ux[k] = -P.ux[k];
+      P.uy[k] = -P.uy[k];
+      P.uz[k] = -P.uz[k];
+    } else if (x > xend) {
+      P.x[k] = __dsub_rn(__dmul_rn(2.0, xend), x);
+      P.ux[k] = __dsub_rn(__dmul_rn(2.0, u0), P.ux[k]);
+      P.uy[k] = -P.uy[k];
+      P.uz[k] = -P.uz[k];
+    }
+  }
+}
+
+void injection3d(const Dev3D& d, const Parts3D& P, double u0, double xend, cudaStream_t s) {
+  k_injection3d<<<d.nrow, 256, 0, s>>>(d, P, u0, xend);
 }
 
 void particle_x3d(const Dev3D& d, const Parts3D& P, cudaStream_t s) {

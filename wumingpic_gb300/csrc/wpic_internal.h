@@ -9,6 +9,7 @@
 //   cumcnt   [isp][jj][0..nx]  (cumcnt(nxgs+ii, j, isp))
 //   np2      [isp][jj]
 #pragma once
+#include <cmath>
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -221,9 +222,20 @@ void load_weibel2d_ppc(const Dev2D& d, int ppc, unsigned long long seed, double 
                        double u_thi, double u_the, cudaStream_t s);
 
 // ---- 3D FP64 path ----
+// boundary_shock__injection's right end, xend = nxe dx + v0 dt with v0 = u0 / sqrt(1 + u0^2/c^2)
+// (2d/proj/shock/boundary_shock.f90, 3d/proj/shock/boundary_shock.f90:437): every product and
+// sum rounded on its own, as the reference evaluates it (no contraction into an FMA)
+inline double shock_xend_value(int nxe, double delx, double u0, double c, double delt) {
+  volatile double a = nxe * delx;
+  volatile double v0 = u0 / std::sqrt(1 + (u0 * u0) / (c * c));
+  volatile double b = v0 * delt;
+  return a + b;
+}
+
 struct Grid3D {
   int nx, ny, nz;
   int nxgs, nygs, nzgs;
+  int wx0, wx1;    // the active x window nxs..nxe as local cells (0, nx - 1 unless a shock run)
   int fp;          // nx + 4: row pitch of a ghosted field
   size_t fplane;   // (nx + 4)(ny + 4)
   size_t fvol;     // (nx + 4)(ny + 4)(nz + 4): one component of a ghosted field
@@ -292,6 +304,7 @@ void mix3_moments(const Dev3D& d, const Mix3Const& k, double* mom, cudaStream_t 
 
 void curre_fold3d(const Dev3D& d, cudaStream_t s);
 void bc_mom3d(const Dev3D& d, double* mom, cudaStream_t s);
+void injection3d(const Dev3D& d, const Parts3D& P, double u0, double xend, cudaStream_t s);
 void dfield_ghost3d(const Dev3D& d, cudaStream_t s);
 void uf_add3d(const Dev3D& d, cudaStream_t s);
 void particle_x3d(const Dev3D& d, const Parts3D& P, cudaStream_t s);

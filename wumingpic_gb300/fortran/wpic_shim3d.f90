@@ -37,6 +37,16 @@ module wpic3d_capi
        real(c_double), intent(inout) :: up(*)
        integer(c_int), intent(inout) :: np2(*), cumcnt(*)
      end function wpic3d_get_particles
+     integer(c_int) function wpic3d_set_window(ctx, nxs, nxe) bind(C, name="wpic3d_set_window")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: nxs, nxe
+     end function wpic3d_set_window
+     integer(c_int) function wpic3d_bc_injection(ctx, u0) bind(C, name="wpic3d_bc_injection")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: u0
+     end function wpic3d_bc_injection
      integer(c_int) function wpic3d_put_fields(ctx, uf) bind(C, name="wpic3d_put_fields")
        import :: c_int, c_ptr, c_double
        type(c_ptr), value :: ctx
@@ -95,6 +105,8 @@ module wpic3d_capi
   type(wpic_params3d), save :: wpic3_prm
   logical, save :: wpic3_uploaded = .false.
   logical, save :: wpic3_bc_set = .false.  ! a boundary module's __init chose the kind
+  logical, save :: wpic3_upload_each_step = .false.  ! the shock driver edits up/uf/cumcnt between steps
+  integer, save :: wpic3_win_s = -huge(1), wpic3_win_e = -huge(1)
   integer, save :: wpic3_sync_every = 1, wpic3_step_count = 0
 
 contains
@@ -116,6 +128,37 @@ contains
   subroutine wpic3_ensure_ctx()
     if (.not. c_associated(wpic3_ctx)) call wpic3_check(wpic3d_init(wpic3_ctx, wpic3_prm, c_null_ptr), 'wpic3d_init')
   end subroutine wpic3_ensure_ctx
+
+  ! the active window nxs..nxe that the driver passes to every module call (a shock run widens it)
+  subroutine wpic3_apply_window(nxs, nxe)
+    integer, intent(in) :: nxs, nxe
+    call wpic3_ensure_ctx()
+    if (nxs /= wpic3_win_s .or. nxe /= wpic3_win_e) then
+       call wpic3_check(wpic3d_set_window(wpic3_ctx, int(nxs, c_int), int(nxe, c_int)), 'window')
+       wpic3_win_s = nxs; wpic3_win_e = nxe
+    endif
+  end subroutine wpic3_apply_window
+
+  ! up, uf and cumcnt to the device; cumcnt beyond the window (stale in the drivers) is completed
+  ! with the row totals, which is what the library keeps there
+  subroutine wpic3_upload_state(up, uf, cumcnt, nxe)
+    real(8), intent(in) :: up(*), uf(*)
+    integer, intent(in) :: cumcnt(wpic3_prm%nxgs:wpic3_prm%nxge+1,wpic3_prm%nys:wpic3_prm%nye, &
+                                  wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    integer, intent(in) :: nxe
+    integer(c_int) :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    integer(c_int) :: cc(wpic3_prm%nxgs:wpic3_prm%nxge+1,wpic3_prm%nys:wpic3_prm%nye, &
+                         wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    integer :: i
+    cc(:,:,:,:) = cumcnt(:,:,:,:)
+    do i = nxe+2, wpic3_prm%nxge+1
+       cc(i,:,:,:) = cumcnt(nxe+1,:,:,:)
+    enddo
+    np2(:,:,:) = cumcnt(nxe+1,:,:,:)
+    call wpic3_check(wpic3d_put_particles(wpic3_ctx, 0_c_int, up, np2, cc), 'put up')
+    call wpic3_check(wpic3d_put_fields(wpic3_ctx, uf), 'put uf')
+    wpic3_uploaded = .true.
+  end subroutine wpic3_upload_state
 
 end module wpic3d_capi
 
@@ -147,14 +190,8 @@ contains
                                    wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
     real(8), intent(in)  :: up(*), uf(*)
     real(8), intent(out) :: gp(*)
-    integer(c_int) :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
-    call wpic3_ensure_ctx()
-    if (.not. wpic3_uploaded) then
-       np2(:,:,:) = cumcnt(nxe+1,:,:,:)
-       call wpic3_check(wpic3d_put_particles(wpic3_ctx, 0_c_int, up, np2, cumcnt), 'put up')
-       call wpic3_check(wpic3d_put_fields(wpic3_ctx, uf), 'put uf')
-       wpic3_uploaded = .true.
-    endif
+    call wpic3_apply_window(nxs, nxe)
+    if (.not. wpic3_uploaded .or. wpic3_upload_each_step) call wpic3_upload_state(up, uf, cumcnt, nxe)
     call wpic3_check(wpic3d_particle_solv(wpic3_ctx), 'particle__solv')
   end subroutine particle__solv
 
@@ -164,14 +201,8 @@ contains
                                    wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
     real(8), intent(in)  :: up(*), uf(*)
     real(8), intent(out) :: gp(*)
-    integer(c_int) :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
-    call wpic3_ensure_ctx()
-    if (.not. wpic3_uploaded) then
-       np2(:,:,:) = cumcnt(nxe+1,:,:,:)
-       call wpic3_check(wpic3d_put_particles(wpic3_ctx, 0_c_int, up, np2, cumcnt), 'put up')
-       call wpic3_check(wpic3d_put_fields(wpic3_ctx, uf), 'put uf')
-       wpic3_uploaded = .true.
-    endif
+    call wpic3_apply_window(nxs, nxe)
+    if (.not. wpic3_uploaded .or. wpic3_upload_each_step) call wpic3_upload_state(up, uf, cumcnt, nxe)
     call wpic3_check(wpic3d_particle_solv_vay(wpic3_ctx), 'particle__solv_vay')
   end subroutine particle__solv_vay
 end module particle
@@ -198,6 +229,7 @@ contains
     real(8), intent(in)    :: up(*), gp(*)
     real(8), intent(inout) :: uf(*)
     external :: set_boundary_dfield, set_boundary_curre, set_boundary_phi
+    call wpic3_apply_window(nxs, nxe)
     call wpic3_check(wpic3d_field_fdtd_i(wpic3_ctx), 'field__fdtd_i')
     if (mod(wpic3_step_count + 1, wpic3_sync_every) == 0) then
        call wpic3_check(wpic3d_get_fields(wpic3_ctx, uf), 'get uf')
@@ -225,6 +257,7 @@ contains
     real(8), intent(in)    :: up(*)
     real(8), intent(out)   :: gp(*)
     integer(c_int) :: np2_dev(wpic3_prm%nye-wpic3_prm%nys+1, wpic3_prm%nze-wpic3_prm%nzs+1, wpic3_prm%nsp)
+    call wpic3_apply_window(nxs, nxe)
     call wpic3_check(wpic3d_sort_bucket(wpic3_ctx), 'sort__bucket')
     wpic3_step_count = wpic3_step_count + 1
     if (mod(wpic3_step_count, wpic3_sync_every) == 0) then
@@ -340,6 +373,64 @@ contains
     call wpic3_check(wpic3d_get_mom(wpic3_ctx, mom), 'get mom')
   end subroutine boundary_reconnection__mom
 end module boundary_reconnection
+
+
+! boundary_shock (3d/proj/shock/boundary_shock.f90): reflecting wall at nxs, injection boundary
+! at nxe of the window.  The shock driver edits up, uf and cumcnt on the host (inject, relocate,
+! 3d/proj/shock/app.f90:120-124), so its init switches the per-step upload on.
+module boundary_shock
+  use wpic3d_capi
+  implicit none
+  private
+  public :: boundary_shock__init, boundary_shock__dfield, boundary_shock__particle_yz, &
+       boundary_shock__injection, boundary_shock__curre, boundary_shock__phi, boundary_shock__mom
+contains
+  subroutine boundary_shock__init(ndim_in,np_in,nsp_in,nxgs_in,nxge_in,nygs_in,nyge_in,nzgs_in, &
+                                  nzge_in,nys_in,nye_in,nzs_in,nze_in,jup_in,jdown_in,kup_in,kdown_in, &
+                                  mnpi_in,mnpr_in,ncomw_in,nerr_in,nstat_in,delx_in,delt_in,c_in)
+    integer, intent(in) :: ndim_in, np_in, nsp_in
+    integer, intent(in) :: nxgs_in, nxge_in, nygs_in, nyge_in, nzgs_in, nzge_in, nys_in, nye_in, nzs_in, nze_in
+    integer, intent(in) :: jup_in, jdown_in, kup_in, kdown_in, mnpi_in, mnpr_in, ncomw_in, nerr_in, nstat_in(:)
+    real(8), intent(in) :: delx_in, delt_in, c_in
+    wpic3_prm%bc_kind = 2; wpic3_bc_set = .true.
+    wpic3_upload_each_step = .true.
+  end subroutine boundary_shock__init
+
+  subroutine boundary_shock__particle_yz(up,np2)
+    real(8), intent(inout) :: up(*)
+    integer, intent(inout) :: np2(*)
+    call wpic3_check(wpic3d_bc_particle_yz(wpic3_ctx), 'bc__particle_yz')
+  end subroutine boundary_shock__particle_yz
+
+  subroutine boundary_shock__injection(up,np2,nxs,nxe,u0)
+    integer, intent(in)    :: nxs, nxe
+    real(8), intent(inout) :: up(*)
+    integer, intent(in)    :: np2(*)
+    real(8), intent(in)    :: u0
+    call wpic3_apply_window(nxs, nxe)
+    call wpic3_check(wpic3d_bc_injection(wpic3_ctx, real(u0, c_double)), 'bc__injection')
+  end subroutine boundary_shock__injection
+
+  ! applied inside the library; present so that field__fdtd_i's arguments type-check
+  subroutine boundary_shock__dfield(df,nxs,nxe,nys,nye,nzs,nze,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nzs, nze, nxgs, nxge
+    real(8), intent(inout) :: df(*)
+  end subroutine boundary_shock__dfield
+  subroutine boundary_shock__curre(uj,nxs,nxe,nys,nye,nzs,nze,nxgs,nxge)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nzs, nze, nxgs, nxge
+    real(8), intent(inout) :: uj(*)
+  end subroutine boundary_shock__curre
+  subroutine boundary_shock__phi(phi,nxs,nxe,nys,nye,nzs,nze,l)
+    integer, intent(in)    :: nxs, nxe, nys, nye, nzs, nze, l
+    real(8), intent(inout) :: phi(*)
+  end subroutine boundary_shock__phi
+
+  subroutine boundary_shock__mom(mom)
+    real(8), intent(inout) :: mom(*)
+    call wpic3_check(wpic3d_bc_mom(wpic3_ctx), 'bc__mom')
+    call wpic3_check(wpic3d_get_mom(wpic3_ctx, mom), 'get mom')
+  end subroutine boundary_shock__mom
+end module boundary_shock
 
 
 ! mom_calc (3d/common/mom_calc.f90) on the device, as in the 2D shim

@@ -338,7 +338,10 @@ class Plasma3D:
     nxgs: int = 2
     nygs: int = 2
     nzgs: int = 2
-    bc: str = "periodic"          # or "reconnection": conducting walls in x (3d/proj/reconnection)
+    bc: str = "periodic"          # "reconnection": conducting walls in x (3d/proj/reconnection);
+                                  # "shock": wall at nxs, open end at nxe of the window (3d/proj/shock)
+    window: int = 0               # shock: cells of the active window nxs..nxe from nxgs (0 = all)
+    u0: float = 0.0               # shock: upstream four-velocity along x (the flow is -u0)
 
     @property
     def nxge(self):
@@ -367,8 +370,13 @@ class Plasma3D:
 
     @property
     def n_particles(self):
-        cells_x = self.nx if self.bc == "periodic" else self.nx - 3
+        cells_x = self.nx if self.bc == "periodic" else (self.window or self.nx) - 3
         return cells_x * self.ny * self.nz * self.ppc * self.nsp
+
+    @property
+    def nxe(self):
+        """right end of the active window (the shock driver's nxe)"""
+        return self.nxgs + (self.window or self.nx) - 1
 
 
 @dataclass
@@ -400,8 +408,10 @@ def load_weibel3d(p: Plasma3D) -> State3D:
     rng = np.random.Generator(np.random.Philox(p.seed))
     st = empty_state3d(p)
     nx, ny, nz, n0 = p.nx, p.ny, p.nz, p.ppc
-    # with conducting walls in x the plasma fills the cells between them, [nxs+1, nxe-1)
-    c_lo, c_hi = (0, nx) if p.bc == "periodic" else (1, nx - 2)
+    # with conducting walls in x the plasma fills the cells between them, [nxs+1, nxe-1); the shock
+    # driver's upstream plasma fills its window likewise, drifting at -u0 along x
+    nw = p.window or nx
+    c_lo, c_hi = (0, nx) if p.bc == "periodic" else (1, nw - 2)
     npr = (c_hi - c_lo) * n0
     ix = np.repeat(np.arange(c_lo, c_hi), n0)
     rx = rng.random((nz, ny, npr))
@@ -420,6 +430,8 @@ def load_weibel3d(p: Plasma3D) -> State3D:
         if isp == 1 and p.drift != 0.0:
             sign = np.where(np.arange(npr) % 2 == 0, 1.0, -1.0)
             u[p.drift_axis] += p.drift * sign[:, None, None]
+        if p.u0 != 0.0:
+            u[0] -= p.u0
         st.up[3:6, :npr, :, :, isp] = u
     for isp in range(p.nsp):
         row = (np.arange(ny)[:, None] + ny * np.arange(nz)[None, :]).astype(np.int64)  # (ny, nz)

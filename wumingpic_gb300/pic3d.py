@@ -36,11 +36,27 @@ class Pic3D:
         prm.r[0], prm.r[1] = r[0], r[1]
         prm.precision = {"fp64": _lib.FP64, "fp64_exact": _lib.FP64_EXACT, "mixed": _lib.MIXED}[precision]
         prm.device_cap = int(device_cap)
-        prm.bc_kind = {"periodic": _lib.BC_PERIODIC, "reconnection": _lib.BC_RECONNECTION}[getattr(plasma, "bc", "periodic")]
+        prm.bc_kind = {"periodic": _lib.BC_PERIODIC, "reconnection": _lib.BC_RECONNECTION,
+                       "shock": _lib.BC_SHOCK}[getattr(plasma, "bc", "periodic")]
         self.precision = precision
         h = ctypes.c_void_p()
         check(lib().wpic3d_init(ctypes.byref(h), ctypes.byref(prm), ctypes.c_void_p(stream or 0)), "wpic3d_init")
         self._h = h
+        if getattr(plasma, "bc", "periodic") == "shock":
+            self.set_window(plasma.nxgs, plasma.nxe)
+            self.set_injection(plasma.u0)
+
+    def set_window(self, nxs, nxe):
+        """the active x window nxs..nxe of a shock run (3d/proj/shock/app.f90:112-117, 654)"""
+        check(lib().wpic3d_set_window(self._h, int(nxs), int(nxe)), "set_window")
+
+    def set_injection(self, u0):
+        """the injection boundary's upstream four-velocity for step()"""
+        check(lib().wpic3d_set_injection(self._h, float(u0)), "set_injection")
+
+    def bc__injection(self, u0):
+        """boundary_shock__injection on gp (3d/proj/shock/boundary_shock.f90:424)"""
+        check(lib().wpic3d_bc_injection(self._h, float(u0)), "bc__injection")
 
     def close(self):
         if getattr(self, "_h", None):
