@@ -328,6 +328,12 @@ def time_adjoint(steps, every, rank, dist, n=512):
     g_drift, g_uth, g_amps = prob.backward()
     t_rec, t_rev = prob.timings["record"], prob.timings["reverse"]
     fd = (prob.value(drift + h, u_th, amps) - prob.value(drift - h, u_th, amps)) / (2 * h)
+    # the mixed-precision adjoint (FP32 reverse push and deposit) on the same recorded run
+    prob.sim.adjoint_precision("mixed")
+    prob.forward(drift, u_th, amps)
+    m_drift, m_uth, m_amps = prob.backward()
+    m_rec, m_rev = prob.timings["record"], prob.timings["reverse"]
+    prob.sim.adjoint_precision("fp64")
     npart = prob.sim.num_particles()
     val_mixed = prob.value_mixed(drift, u_th, amps)
     mix_ms, _ = rank_totals(prob.timings["forward_mixed"] * 1e3, npart, dist, "cuda")
@@ -335,6 +341,9 @@ def time_adjoint(steps, every, rank, dist, n=512):
     fwd_ms, _ = rank_totals(t_fwd * 1e3, npart, dist, "cuda")
     rec_ms, _ = rank_totals(t_rec * 1e3, npart, dist, "cuda")
     rev_ms, _ = rank_totals(t_rev * 1e3, npart, dist, "cuda")
+    m_rec_ms, _ = rank_totals(m_rec * 1e3, npart, dist, "cuda")
+    m_rev_ms, _ = rank_totals(m_rev * 1e3, npart, dist, "cuda")
+    rel = lambda a, b: abs(a - b) / abs(b) if b else None  # noqa: E731
     return {"workload": f"2D Weibel {n}^2 cells, 32 ppc/species ({npart} particles), drift +-0.3c, u_th 0.05c, "
                         f"64 Bz seed modes; L = final magnetic energy after {steps} steps",
             "steps": steps, "checkpoint_every": every, "dtype": "f64", "cg_rtol": 1e-13,
@@ -344,7 +353,15 @@ def time_adjoint(steps, every, rank, dist, n=512):
                               "forward_ms": mix_ms, "fp64_over_mixed_time": fwd_ms / mix_ms},
             "grad": {"drift": g_drift, "u_th": g_uth, "amps_norm": float(np.linalg.norm(g_amps))},
             "fd_check": {"param": "drift", "h": h, "fd": fd, "adjoint": g_drift,
-                         "rel_err": abs(g_drift - fd) / abs(fd) if fd else None}}
+                         "rel_err": abs(g_drift - fd) / abs(fd) if fd else None},
+            "mixed_adjoint": {"arithmetic": "FP32 reverse push and deposit per particle; FP64 trajectory, "
+                                            "field adjoint, adjoint CG and sums",
+                              "record_ms": m_rec_ms, "reverse_ms": m_rev_ms,
+                              "cost_over_forward": (m_rec_ms + m_rev_ms) / fwd_ms,
+                              "rel_diff_vs_fp64_adjoint": {
+                                  "drift": rel(m_drift, g_drift), "u_th": rel(m_uth, g_uth),
+                                  "amps": float(np.linalg.norm(m_amps - g_amps) / np.linalg.norm(g_amps))},
+                              "rel_err_vs_fd_drift": rel(m_drift, fd)}}
 
 
 def main():

@@ -178,6 +178,9 @@ int wpic_adjoint(wpic_ctx* ctx, int nsteps, int every, const double* lam_uf_fina
  * at every segment start and at the end.  reverse: the gradients for the recorded run (may be
  * called again with another lam_uf_final); leaves the recorded final state in the context. */
 int wpic_adjoint_record(wpic_ctx* ctx, int nsteps, int every);
+/* arithmetic of the reverse push and deposit sweeps: WPIC_FP64 (default) or WPIC_MIXED (FP32
+   per particle along the recorded FP64 trajectory; fields, adjoint CG and sums stay FP64) */
+int wpic_adjoint_precision(wpic_ctx* ctx, int precision);
 int wpic_adjoint_reverse(wpic_ctx* ctx, const double* lam_uf_final, double* lam_up0, double* lam_uf0);
 /* dot-product checks <L x, y> = <x, L^T y> of the adjoint's transposed field operators on
  * random vectors (current fold, ghost copies, E update, RHS, cell-centre averaging): five

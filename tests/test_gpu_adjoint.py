@@ -8,7 +8,9 @@ Tolerances (stated per test):
   * whole steps (1 and 4) along random field and particle directions: 1e-6 relative;
   * gradients of the field energy with respect to beam drift, thermal spread and
     seed-mode amplitudes through the checkpointed reverse sweep: 1e-5 relative;
-  * the checkpoint interval changes only the atomic summation order: 1e-12.
+  * the checkpoint interval changes only the atomic summation order: 1e-12;
+  * the mixed-precision adjoint (FP32 reverse push and deposit) against the FP64 adjoint:
+    1e-4 relative on the parameter gradients.
 The CG runs at a relative tolerance of 1e-13 so that finite differences resolve it.
 """
 import math
@@ -142,6 +144,23 @@ def test_parameter_gradients_vs_fd(gpu_lib, which):
         fd = (prob.value(drift, u_th, amps + da) - prob.value(drift, u_th, amps - da)) / 2e-8
         assert abs(g_amps[k] - fd) <= 1e-5 * abs(fd), (k, g_amps[k], fd)
     prob.close()
+
+
+@pytest.mark.parametrize("which", ["B", "EB"])
+def test_mixed_adjoint_vs_fp64_adjoint(gpu_lib, which):
+    """FP32 reverse push and deposit along the same recorded FP64 run: the parameter gradients
+    within 1e-4 relative of the FP64 adjoint's (the seed amplitudes as a vector norm)."""
+    prob, amps = small_problem(which=which)
+    drift, u_th = 0.3, 0.05
+    prob.forward(drift, u_th, amps)
+    g64 = prob.backward()
+    prob.sim.adjoint_precision("mixed")
+    prob.forward(drift, u_th, amps)
+    g32 = prob.backward()
+    prob.close()
+    for a, b in zip(g32[:2], g64[:2]):
+        assert abs(a - b) <= 1e-4 * abs(b), (a, b)
+    assert np.linalg.norm(g32[2] - g64[2]) <= 1e-4 * np.linalg.norm(g64[2])
 
 
 def test_torch_autograd(gpu_lib):

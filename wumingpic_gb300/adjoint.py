@@ -124,10 +124,12 @@ class FieldEnergyProblem:
 
     ``forward`` loads the plasma (device loader, seed of the plasma description),
     adds the seed modes, records the run and returns L; ``backward`` reverses the
-    recorded run and returns (dL/d drift, dL/d u_th, dL/d a)."""
+    recorded run and returns (dL/d drift, dL/d u_th, dL/d a).  With
+    ``adjoint_precision="mixed"`` the reverse push and deposit run in FP32 per particle
+    (the trajectory, the field adjoint, the adjoint CG and all sums stay FP64)."""
 
     def __init__(self, plasma, nsteps, every, modes: SeedModes = None, which="B", cg_rtol=1e-13,
-                 cg_ite_max=2000):
+                 cg_ite_max=2000, adjoint_precision="fp64"):
         if plasma.bc != "periodic":
             raise ValueError("the adjoint covers the periodic run")
         self.p = plasma
@@ -135,6 +137,7 @@ class FieldEnergyProblem:
         self.modes = modes
         self.which = which
         self.cg_rtol, self.cg_ite_max = cg_rtol, cg_ite_max
+        self.adjoint_precision = adjoint_precision  # "mixed": FP32 reverse push and deposit sweeps
         self.sim = None
         self._init = None
         self.timings = {}  # seconds of the last value / record / reverse calls (synchronous C calls)
@@ -150,6 +153,7 @@ class FieldEnergyProblem:
         if self.sim is None:
             self.sim = Pic2D(self.p, precision="fp64")
             self.sim.cg_tolerance(self.cg_rtol, self.cg_ite_max)
+            self.sim.adjoint_precision(self.adjoint_precision)
         return self.sim
 
     def load(self, drift, u_th, amps=None):

@@ -274,6 +274,10 @@ __global__ void k_adj_cg_result(Dev2D d, double* lg) {
   }
 }
 
+// reciprocal square root in the kernel's arithmetic type
+__device__ __forceinline__ double rsq(double v) { return rsqrt(v); }
+__device__ __forceinline__ float rsq(float v) { return rsqrtf(v); }
+
 // ---- the deposit's adjoint: inputs (x_old, y_old, x_new, y_new, ux', uy', uz') ----
 // Forward (per particle, 2d/common/field.f90:189-316): shapes s0 (old position, 5-point
 // stencil around the old cell), S1 (new position, shifted by the cell change inc), ds = S1 - s0,
@@ -282,6 +286,10 @@ __global__ void k_adj_cg_result(Dev2D d, double* lg) {
 //   Jz(i, j)   = q gvz (s0_x s0_y + ds_x s0_y / 2 + s0_x ds_y / 2 + ds_x ds_y / 3),
 // gvz = uz / sqrt(1 + u^2 / c^2).  Reverse: the adjoints of the 5-point shape arrays from
 // suffix sums of lJ, then through ds = S1 - s0, the shift and the quadratic spline.
+// R is the arithmetic type of the per-particle sweep: double, or float for the
+// mixed-precision adjoint.  The in-cell offsets and the cell indices come from the FP64
+// positions in FP64 either way; the particle adjoints are accumulated into FP64 arrays.
+template <typename R>
 __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj, Parts64 lA, Parts64 lB) {
   const Grid2D g = d.g;
   const int row = blockIdx.y;
@@ -291,90 +299,91 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj,
   const int* ccr = d.cc + (size_t)row * (g.nx + 1);
   const int cx = cell_of(ccr, g.nx, s);
   const size_t k = (size_t)row * d.cap + s;
-  const double d_delx = d.ph.d_delx, c = d.ph.c;
-  const double q = d.ph.q[isp];
-  const double qdd = q * d.ph.delx * d.ph.d_delt, fac = 1.0 / 3.0;
+  const double d_delx = d.ph.d_delx;
+  const R dxr = (R)d_delx, c = (R)d.ph.c, q = (R)d.ph.q[isp];
+  const R qdd = (R)(d.ph.q[isp] * d.ph.delx * d.ph.d_delt), fac = R(1) / R(3);
+  const R h5 = R(0.5), q34 = R(0.75);
   const int iabs = g.nxgs + cx, jabs = g.nygs + jj;
   const double pos0[2] = {d.A.x[k], d.A.y[k]};
   const double pos1[2] = {d.B.x[k], d.B.y[k]};
-  double s0[2][5], ds[2][5], dh[2], dh1[2];
+  R s0[2][5], ds[2][5], dh[2], dh1[2];
   int inc[2];
 #pragma unroll
   for (int dim = 0; dim < 2; ++dim) {
-    const double h = d_delx * pos0[dim] + (-0.5 - (double)(dim == 0 ? iabs : jabs));
+    const R h = (R)(d_delx * pos0[dim] + (-0.5 - (double)(dim == 0 ? iabs : jabs)));
     dh[dim] = h;
-    s0[dim][0] = 0.0;
-    s0[dim][1] = 0.5 * ((0.5 - h) * (0.5 - h));
-    s0[dim][2] = 0.75 - h * h;
-    s0[dim][3] = 0.5 * ((0.5 + h) * (0.5 + h));
-    s0[dim][4] = 0.0;
+    s0[dim][0] = R(0);
+    s0[dim][1] = h5 * ((h5 - h) * (h5 - h));
+    s0[dim][2] = q34 - h * h;
+    s0[dim][3] = h5 * ((h5 + h) * (h5 + h));
+    s0[dim][4] = R(0);
     const int i2 = (int)(pos1[dim] * d_delx);
-    const double h1 = d_delx * pos1[dim] + (-0.5 - (double)i2);
+    const R h1 = (R)(d_delx * pos1[dim] + (-0.5 - (double)i2));
     dh1[dim] = h1;
     inc[dim] = i2 - (dim == 0 ? iabs : jabs);
-    const double a1 = 0.5 * ((0.5 - h1) * (0.5 - h1)), a2 = 0.75 - h1 * h1, a3 = 0.5 * ((0.5 + h1) * (0.5 + h1));
+    const R a1 = h5 * ((h5 - h1) * (h5 - h1)), a2 = q34 - h1 * h1, a3 = h5 * ((h5 + h1) * (h5 + h1));
     const int ai = inc[dim] < 0 ? -inc[dim] : inc[dim];
-    const double m1 = (double)(-(inc[dim] - ai)) * 0.5, m2 = (double)(-ai + 1), m3 = (double)(inc[dim] + ai) * 0.5;
+    const R m1 = (R)(-(inc[dim] - ai)) * h5, m2 = (R)(-ai + 1), m3 = (R)(inc[dim] + ai) * h5;
     ds[dim][0] = m1 * a1 - s0[dim][0];
     ds[dim][1] = m2 * a1 + m1 * a2 - s0[dim][1];
     ds[dim][2] = m2 * a2 + m1 * a3 + m3 * a1 - s0[dim][2];
     ds[dim][3] = m2 * a3 + m3 * a2 - s0[dim][3];
     ds[dim][4] = m3 * a3 - s0[dim][4];
   }
-  const double ux = d.B.ux[k], uy = d.B.uy[k], uz = d.B.uz[k];
-  const double ic2 = 1.0 / (c * c);
-  const double gmi = rsqrt(1. + ic2 * (ux * ux + uy * uy + uz * uz));
-  const double gvz = uz * gmi;
+  const R ux = (R)d.B.ux[k], uy = (R)d.B.uy[k], uz = (R)d.B.uz[k];
+  const R ic2 = R(1) / (c * c);
+  const R gmi = rsq(R(1) + ic2 * (ux * ux + uy * uy + uz * uz));
+  const R gvz = uz * gmi;
   const size_t P = g.fplane;
   const double* L0 = luj + (size_t)jj * g.fp + cx;  // node (cx + a, jj + b) at L0[b * fp + a]
-  double gs0[2][5], gds[2][5];
+  R gs0[2][5], gds[2][5];
 #pragma unroll
   for (int dim = 0; dim < 2; ++dim)
 #pragma unroll
-    for (int i = 0; i < 5; ++i) gs0[dim][i] = gds[dim][i] = 0.0;
+    for (int i = 0; i < 5; ++i) gs0[dim][i] = gds[dim][i] = R(0);
   // Jx: nodes (i + 1, j), i = 0..3, j = 0..4
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
-    const double wy = s0[1][j] + 0.5 * ds[1][j];
-    double suf = 0.0, gw = 0.0;
+    const R wy = s0[1][j] + h5 * ds[1][j];
+    R suf = R(0), gw = R(0);
 #pragma unroll
     for (int i = 3; i >= 0; --i) {
-      suf += L0[(size_t)j * g.fp + i + 1];  // sum_{i'' >= i} lJx(i'' + 1, j)
+      suf += (R)L0[(size_t)j * g.fp + i + 1];  // sum_{i'' >= i} lJx(i'' + 1, j)
       gds[0][i] += -qdd * wy * suf;
       gw += ds[0][i] * suf;
     }
     gw *= -qdd;
     gs0[1][j] += gw;
-    gds[1][j] += 0.5 * gw;
+    gds[1][j] += h5 * gw;
   }
   // Jy: nodes (i, j + 1), i = 0..4, j = 0..3
   const double* L1 = L0 + P;
 #pragma unroll
   for (int i = 0; i < 5; ++i) {
-    const double wx = s0[0][i] + 0.5 * ds[0][i];
-    double suf = 0.0, gw = 0.0;
+    const R wx = s0[0][i] + h5 * ds[0][i];
+    R suf = R(0), gw = R(0);
 #pragma unroll
     for (int j = 3; j >= 0; --j) {
-      suf += L1[(size_t)(j + 1) * g.fp + i];
+      suf += (R)L1[(size_t)(j + 1) * g.fp + i];
       gds[1][j] += -qdd * wx * suf;
       gw += ds[1][j] * suf;
     }
     gw *= -qdd;
     gs0[0][i] += gw;
-    gds[0][i] += 0.5 * gw;
+    gds[0][i] += h5 * gw;
   }
   // Jz: nodes (i, j) = Qz (s0_x (x) Ay + ds_x (x) By), Ay = s0_y + ds_y / 2, By = s0_y / 2 + ds_y / 3
   const double* L2 = L0 + 2 * P;
-  const double Qz = q * gvz;
-  double gAy[5] = {0, 0, 0, 0, 0}, gBy[5] = {0, 0, 0, 0, 0}, phiz = 0.0;
+  const R Qz = q * gvz;
+  R gAy[5] = {R(0), R(0), R(0), R(0), R(0)}, gBy[5] = {R(0), R(0), R(0), R(0), R(0)}, phiz = R(0);
 #pragma unroll
   for (int i = 0; i < 5; ++i) {
-    double r1 = 0.0, r2 = 0.0;
+    R r1 = R(0), r2 = R(0);
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
-      const double l = L2[(size_t)j * g.fp + i];
-      r1 += l * (s0[1][j] + 0.5 * ds[1][j]);
-      r2 += l * (0.5 * s0[1][j] + fac * ds[1][j]);
+      const R l = (R)L2[(size_t)j * g.fp + i];
+      r1 += l * (s0[1][j] + h5 * ds[1][j]);
+      r2 += l * (h5 * s0[1][j] + fac * ds[1][j]);
       gAy[j] += l * s0[0][i];
       gBy[j] += l * ds[0][i];
     }
@@ -384,33 +393,33 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj,
   }
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
-    gs0[1][j] += Qz * (gAy[j] + 0.5 * gBy[j]);
-    gds[1][j] += Qz * (0.5 * gAy[j] + fac * gBy[j]);
+    gs0[1][j] += Qz * (gAy[j] + h5 * gBy[j]);
+    gds[1][j] += Qz * (h5 * gAy[j] + fac * gBy[j]);
   }
   // through ds = S1 - s0, the shift by inc and the splines
-  double gpos0[2], gpos1[2];
+  R gpos0[2], gpos1[2];
 #pragma unroll
   for (int dim = 0; dim < 2; ++dim) {
     const int ai = inc[dim] < 0 ? -inc[dim] : inc[dim];
-    const double m1 = (double)(-(inc[dim] - ai)) * 0.5, m2 = (double)(-ai + 1), m3 = (double)(inc[dim] + ai) * 0.5;
-    const double ga1 = m1 * gds[dim][0] + m2 * gds[dim][1] + m3 * gds[dim][2];
-    const double ga2 = m1 * gds[dim][1] + m2 * gds[dim][2] + m3 * gds[dim][3];
-    const double ga3 = m1 * gds[dim][2] + m2 * gds[dim][3] + m3 * gds[dim][4];
-    const double h1 = dh1[dim], h = dh[dim];
-    gpos1[dim] = d_delx * (-(0.5 - h1) * ga1 - 2.0 * h1 * ga2 + (0.5 + h1) * ga3);
-    const double g1 = gs0[dim][1] - gds[dim][1], g2 = gs0[dim][2] - gds[dim][2], g3 = gs0[dim][3] - gds[dim][3];
-    gpos0[dim] = d_delx * (-(0.5 - h) * g1 - 2.0 * h * g2 + (0.5 + h) * g3);
+    const R m1 = (R)(-(inc[dim] - ai)) * h5, m2 = (R)(-ai + 1), m3 = (R)(inc[dim] + ai) * h5;
+    const R ga1 = m1 * gds[dim][0] + m2 * gds[dim][1] + m3 * gds[dim][2];
+    const R ga2 = m1 * gds[dim][1] + m2 * gds[dim][2] + m3 * gds[dim][3];
+    const R ga3 = m1 * gds[dim][2] + m2 * gds[dim][3] + m3 * gds[dim][4];
+    const R h1 = dh1[dim], h = dh[dim];
+    gpos1[dim] = dxr * (-(h5 - h1) * ga1 - R(2) * h1 * ga2 + (h5 + h1) * ga3);
+    const R g1 = gs0[dim][1] - gds[dim][1], g2 = gs0[dim][2] - gds[dim][2], g3 = gs0[dim][3] - gds[dim][3];
+    gpos0[dim] = dxr * (-(h5 - h) * g1 - R(2) * h * g2 + (h5 + h) * g3);
   }
   // gvz = uz / gamma
-  const double ggv = q * phiz;
-  const double t3 = gmi * gmi * gmi * ic2 * uz;
-  lA.x[k] += gpos0[0];
-  lA.y[k] += gpos0[1];
-  lB.x[k] += gpos1[0];
-  lB.y[k] += gpos1[1];
-  lB.ux[k] += ggv * (-t3 * ux);
-  lB.uy[k] += ggv * (-t3 * uy);
-  lB.uz[k] += ggv * (gmi - t3 * uz);
+  const R ggv = q * phiz;
+  const R t3 = gmi * gmi * gmi * ic2 * uz;
+  lA.x[k] += (double)gpos0[0];
+  lA.y[k] += (double)gpos0[1];
+  lB.x[k] += (double)gpos1[0];
+  lB.y[k] += (double)gpos1[1];
+  lB.ux[k] += (double)(ggv * (-t3 * ux));
+  lB.uy[k] += (double)(ggv * (-t3 * uy));
+  lB.uz[k] += (double)(ggv * (gmi - t3 * uz));
 }
 
 // ---- the push's adjoint: inputs (x, y, ux, uy, uz) and the cell-centred fields tmp ----
@@ -420,12 +429,13 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj,
 // x' = x + dt u'_x / gamma', y' = y + dt u'_y / gamma'.  Reverse sweep through these lines;
 // the field adjoints (B, E at the particle) spread back over the 3 x 3 tmp nodes with the
 // same spline weights: summed per (cell, component, node) over the block's particles in
-// shared memory, then one FP64 atomic per (cell, component, node) of the block.
+// shared memory (in R), then one FP64 atomic per (cell, component, node) of the block.
 constexpr int AP_T = 128;
+template <typename R>
 __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const double* tmp, Parts64 lA, Parts64 lB,
                                                    double* ltmp) {
-  __shared__ double slf[6][AP_T + 1];
-  __shared__ double sw[6][AP_T + 1];
+  __shared__ R slf[6][AP_T + 1];
+  __shared__ R sw[6][AP_T + 1];
   const Grid2D g = d.g;
   const int row = blockIdx.y;
   const int s0b = blockIdx.x * AP_T;
@@ -440,28 +450,29 @@ __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const double* tmp, P
   if (s < np) {
     const int cx = cell_of(ccr, g.nx, s);
     const size_t k = (size_t)row * d.cap + s;
-    const double dxi = d.ph.p_d_delx, delt = d.ph.delt, c = d.ph.c;
-    const double fac1 = d.ph.q[isp] / d.ph.r[isp] * 0.5 * delt;
-    const double txxx = fac1 * fac1;
-    const double fac2 = d.ph.q[isp] * delt / d.ph.r[isp];
+    const double dxi64 = d.ph.p_d_delx;
+    const R dxi = (R)dxi64, delt = (R)d.ph.delt, c = (R)d.ph.c;
+    const R fac1 = (R)(d.ph.q[isp] / d.ph.r[isp] * 0.5 * d.ph.delt);
+    const R txxx = fac1 * fac1;
+    const R fac2 = (R)(d.ph.q[isp] * d.ph.delt / d.ph.r[isp]);
+    const R h5 = R(0.5), q34 = R(0.75), two = R(2);
     const int iabs = g.nxgs + cx, jabs = g.nygs + jj;
-    const double x = d.A.x[k], y = d.A.y[k];
-    const double hx = x * dxi - 0.5 - (double)iabs, hy = y * dxi - 0.5 - (double)jabs;
-    const double sx[3] = {0.5 * (0.5 - hx) * (0.5 - hx), 0.75 - hx * hx, 0.5 * (0.5 + hx) * (0.5 + hx)};
-    const double sy[3] = {0.5 * (0.5 - hy) * (0.5 - hy), 0.75 - hy * hy, 0.5 * (0.5 + hy) * (0.5 + hy)};
-    const double dsx[3] = {-(0.5 - hx) * dxi, -2.0 * hx * dxi, (0.5 + hx) * dxi};
-    const double dsy[3] = {-(0.5 - hy) * dxi, -2.0 * hy * dxi, (0.5 + hy) * dxi};
+    const R hx = (R)(d.A.x[k] * dxi64 - 0.5 - (double)iabs), hy = (R)(d.A.y[k] * dxi64 - 0.5 - (double)jabs);
+    const R sx[3] = {h5 * (h5 - hx) * (h5 - hx), q34 - hx * hx, h5 * (h5 + hx) * (h5 + hx)};
+    const R sy[3] = {h5 * (h5 - hy) * (h5 - hy), q34 - hy * hy, h5 * (h5 + hy) * (h5 + hy)};
+    const R dsx[3] = {-(h5 - hx) * dxi, -two * hx * dxi, (h5 + hx) * dxi};
+    const R dsy[3] = {-(h5 - hy) * dxi, -two * hy * dxi, (h5 + hy) * dxi};
     // tmp node (a, b) of the particle's cell: local cell (cx - 1 + a, jj - 1 + b) -> index (cx + a, jj + b)
-    double fv[6], fdx[6], fdy[6];
+    R fv[6], fdx[6], fdy[6];
 #pragma unroll
     for (int m = 0; m < 6; ++m) {
-      double v = 0.0, vx = 0.0, vy = 0.0;
+      R v = R(0), vx = R(0), vy = R(0);
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        double r = 0.0, rx = 0.0;
+        R r = R(0), rx = R(0);
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-          const double t = tmp[(size_t)m * n + (size_t)(jj + b) * tw + (cx + a)];
+          const R t = (R)tmp[(size_t)m * n + (size_t)(jj + b) * tw + (cx + a)];
           r += t * sx[a];
           rx += t * dsx[a];
         }
@@ -473,70 +484,71 @@ __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const double* tmp, P
       fdx[m] = vx;
       fdy[m] = vy;
     }
-    const double B[3] = {fv[0], fv[1], fv[2]};
-    const double ux = d.A.ux[k], uy = d.A.uy[k], uz = d.A.uz[k];
+    const R B[3] = {fv[0], fv[1], fv[2]};
+    const R ux = (R)d.A.ux[k], uy = (R)d.A.uy[k], uz = (R)d.A.uz[k];
     // forward values
-    const double u1[3] = {ux + fac1 * fv[3], uy + fac1 * fv[4], uz + fac1 * fv[5]};
-    const double gsq = c * c + (u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2]);
-    const double igam = rsqrt(gsq);
-    const double gam = gsq * igam;
-    const double fac1r = fac1 * igam;
-    const double Bsq = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
-    const double D = gam + txxx * (Bsq * igam);
-    const double iD = 1.0 / D;
-    const double fac2r = fac2 * iD;
-    const double u1xB[3] = {u1[1] * B[2] - u1[2] * B[1], u1[2] * B[0] - u1[0] * B[2], u1[0] * B[1] - u1[1] * B[0]};
-    const double w[3] = {u1[0] + fac1r * u1xB[0], u1[1] + fac1r * u1xB[1], u1[2] + fac1r * u1xB[2]};
-    const double wxB[3] = {w[1] * B[2] - w[2] * B[1], w[2] * B[0] - w[0] * B[2], w[0] * B[1] - w[1] * B[0]};
-    const double gv[3] = {u1[0] + fac2r * wxB[0] + fac1 * fv[3], u1[1] + fac2r * wxB[1] + fac1 * fv[4],
-                          u1[2] + fac2r * wxB[2] + fac1 * fv[5]};
-    const double ic2 = 1.0 / (c * c);
-    const double gi = rsqrt(1.0 + ic2 * (gv[0] * gv[0] + gv[1] * gv[1] + gv[2] * gv[2]));
+    const R u1[3] = {ux + fac1 * fv[3], uy + fac1 * fv[4], uz + fac1 * fv[5]};
+    const R gsq = c * c + (u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2]);
+    const R igam = rsq(gsq);
+    const R gam = gsq * igam;
+    const R fac1r = fac1 * igam;
+    const R Bsq = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+    const R D = gam + txxx * (Bsq * igam);
+    const R iD = R(1) / D;
+    const R fac2r = fac2 * iD;
+    const R u1xB[3] = {u1[1] * B[2] - u1[2] * B[1], u1[2] * B[0] - u1[0] * B[2], u1[0] * B[1] - u1[1] * B[0]};
+    const R w[3] = {u1[0] + fac1r * u1xB[0], u1[1] + fac1r * u1xB[1], u1[2] + fac1r * u1xB[2]};
+    const R wxB[3] = {w[1] * B[2] - w[2] * B[1], w[2] * B[0] - w[0] * B[2], w[0] * B[1] - w[1] * B[0]};
+    const R gv[3] = {u1[0] + fac2r * wxB[0] + fac1 * fv[3], u1[1] + fac2r * wxB[1] + fac1 * fv[4],
+                     u1[2] + fac2r * wxB[2] + fac1 * fv[5]};
+    const R ic2 = R(1) / (c * c);
+    const R gi = rsq(R(1) + ic2 * (gv[0] * gv[0] + gv[1] * gv[1] + gv[2] * gv[2]));
     // reverse
-    const double lx = lB.x[k], ly = lB.y[k];
-    const double gib = delt * (lx * gv[0] + ly * gv[1]);
-    const double kk = gi * gi * gi * gib * ic2;
-    double gb[3] = {lB.ux[k] + delt * gi * lx - kk * gv[0], lB.uy[k] + delt * gi * ly - kk * gv[1],
-                    lB.uz[k] - kk * gv[2]};  // adjoint of u' (= of u2)
-    double Eb[3] = {fac1 * gb[0], fac1 * gb[1], fac1 * gb[2]};
-    const double f2rb = gb[0] * wxB[0] + gb[1] * wxB[1] + gb[2] * wxB[2];
-    const double wb[3] = {fac2r * (B[1] * gb[2] - B[2] * gb[1]), fac2r * (B[2] * gb[0] - B[0] * gb[2]),
-                          fac2r * (B[0] * gb[1] - B[1] * gb[0])};
-    double Bb[3] = {fac2r * (gb[1] * w[2] - gb[2] * w[1]), fac2r * (gb[2] * w[0] - gb[0] * w[2]),
-                    fac2r * (gb[0] * w[1] - gb[1] * w[0])};
-    double u1b[3] = {gb[0] + wb[0] + fac1r * (B[1] * wb[2] - B[2] * wb[1]),
-                     gb[1] + wb[1] + fac1r * (B[2] * wb[0] - B[0] * wb[2]),
-                     gb[2] + wb[2] + fac1r * (B[0] * wb[1] - B[1] * wb[0])};
+    const R lx = (R)lB.x[k], ly = (R)lB.y[k];
+    const R gib = delt * (lx * gv[0] + ly * gv[1]);
+    const R kk = gi * gi * gi * gib * ic2;
+    R gb[3] = {(R)lB.ux[k] + delt * gi * lx - kk * gv[0], (R)lB.uy[k] + delt * gi * ly - kk * gv[1],
+               (R)lB.uz[k] - kk * gv[2]};  // adjoint of u' (= of u2)
+    R Eb[3] = {fac1 * gb[0], fac1 * gb[1], fac1 * gb[2]};
+    const R f2rb = gb[0] * wxB[0] + gb[1] * wxB[1] + gb[2] * wxB[2];
+    const R wb[3] = {fac2r * (B[1] * gb[2] - B[2] * gb[1]), fac2r * (B[2] * gb[0] - B[0] * gb[2]),
+                     fac2r * (B[0] * gb[1] - B[1] * gb[0])};
+    R Bb[3] = {fac2r * (gb[1] * w[2] - gb[2] * w[1]), fac2r * (gb[2] * w[0] - gb[0] * w[2]),
+               fac2r * (gb[0] * w[1] - gb[1] * w[0])};
+    R u1b[3] = {gb[0] + wb[0] + fac1r * (B[1] * wb[2] - B[2] * wb[1]),
+                gb[1] + wb[1] + fac1r * (B[2] * wb[0] - B[0] * wb[2]),
+                gb[2] + wb[2] + fac1r * (B[0] * wb[1] - B[1] * wb[0])};
     Bb[0] += fac1r * (wb[1] * u1[2] - wb[2] * u1[1]);
     Bb[1] += fac1r * (wb[2] * u1[0] - wb[0] * u1[2]);
     Bb[2] += fac1r * (wb[0] * u1[1] - wb[1] * u1[0]);
-    const double f1rb = wb[0] * u1xB[0] + wb[1] * u1xB[1] + wb[2] * u1xB[2];
-    const double Db = -(fac2r * iD) * f2rb;
-    const double bsqb = Db * txxx * igam;
-    Bb[0] += 2.0 * bsqb * B[0];
-    Bb[1] += 2.0 * bsqb * B[1];
-    Bb[2] += 2.0 * bsqb * B[2];
-    const double igb = Db * txxx * Bsq + fac1 * f1rb;
-    const double gamb = Db - igam * igam * igb;
+    const R f1rb = wb[0] * u1xB[0] + wb[1] * u1xB[1] + wb[2] * u1xB[2];
+    const R Db = -(fac2r * iD) * f2rb;
+    const R bsqb = Db * txxx * igam;
+    Bb[0] += two * bsqb * B[0];
+    Bb[1] += two * bsqb * B[1];
+    Bb[2] += two * bsqb * B[2];
+    const R igb = Db * txxx * Bsq + fac1 * f1rb;
+    const R gamb = Db - igam * igam * igb;
     u1b[0] += gamb * igam * u1[0];
     u1b[1] += gamb * igam * u1[1];
     u1b[2] += gamb * igam * u1[2];
     Eb[0] += fac1 * u1b[0];
     Eb[1] += fac1 * u1b[1];
     Eb[2] += fac1 * u1b[2];
-    const double lf[6] = {Bb[0], Bb[1], Bb[2], Eb[0], Eb[1], Eb[2]};
-    double lxa = lx, lya = ly;
+    const R lf[6] = {Bb[0], Bb[1], Bb[2], Eb[0], Eb[1], Eb[2]};
+    R lxa = R(0), lya = R(0);
 #pragma unroll
     for (int m = 0; m < 6; ++m) {
       lxa += lf[m] * fdx[m];
       lya += lf[m] * fdy[m];
       slf[m][tid] = lf[m];
     }
-    lA.x[k] += lxa;
-    lA.y[k] += lya;
-    lA.ux[k] += u1b[0];
-    lA.uy[k] += u1b[1];
-    lA.uz[k] += u1b[2];
+    // lA(x, y) = lB(x, y) + the gather's position derivative; the pass-through part in FP64
+    lA.x[k] += lB.x[k] + (double)lxa;
+    lA.y[k] += lB.y[k] + (double)lya;
+    lA.ux[k] += (double)u1b[0];
+    lA.uy[k] += (double)u1b[1];
+    lA.uz[k] += (double)u1b[2];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       sw[a][tid] = sx[a];
@@ -552,9 +564,9 @@ __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const double* tmp, P
     const int cc = c_first + e / 54, r = e - (e / 54) * 54;
     const int m = r / 9, ab = r - m * 9, b = ab / 3, a = ab - b * 3;
     const int p0 = max(ccr[cc], s0b) - s0b, p1 = min(ccr[cc + 1], last + 1) - s0b;
-    double acc = 0.0;
+    R acc = R(0);
     for (int p = p0; p < p1; ++p) acc += slf[m][p] * sw[a][p] * sw[3 + b][p];
-    if (acc != 0.0) atomicAdd(ltmp + (size_t)m * n + (size_t)(jj + b) * tw + (cc + a), acc);
+    if (acc != R(0)) atomicAdd(ltmp + (size_t)m * n + (size_t)(jj + b) * tw + (cc + a), (double)acc);
   }
 }
 
@@ -625,16 +637,23 @@ void adj_dot_parts(const Dev2D& d, const Parts64& L, const Parts64& P, double sc
 }
 // the push's field adjoint alone: luf += (dB/duf)^T lB (lA receives the particle part)
 void adj_push_fields(const Dev2D& d, const Parts64& lB, const Parts64& lA, double* tmp, double* ltmp, double* luf,
-                     cudaStream_t s) {
+                     bool fp32, cudaStream_t s) {
   const size_t n = (size_t)(d.g.nx + 2) * (d.g.ny + 2);
   k_adj_tmp<<<4 * 152, 256, 0, s>>>(d, tmp);
   cudaMemsetAsync(ltmp, 0, sizeof(double) * 6 * n, s);
-  k_adj_push<<<dim3((d.cap + 127) / 128, d.nrowjob), 128, 0, s>>>(d, tmp, lA, lB, ltmp);
+  if (fp32)
+    k_adj_push<float><<<dim3((d.cap + 127) / 128, d.nrowjob), 128, 0, s>>>(d, tmp, lA, lB, ltmp);
+  else
+    k_adj_push<double><<<dim3((d.cap + 127) / 128, d.nrowjob), 128, 0, s>>>(d, tmp, lA, lB, ltmp);
   k_adj_tmpT<<<4 * 152, 256, 0, s>>>(d, ltmp, luf);
 }
 
-void adj_deposit_only(const Dev2D& d, const double* luj, const Parts64& lA, const Parts64& lB, cudaStream_t s) {
-  k_adj_deposit<<<dim3((d.cap + 127) / 128, d.nrowjob), 128, 0, s>>>(d, luj, lA, lB);
+void adj_deposit_only(const Dev2D& d, const double* luj, const Parts64& lA, const Parts64& lB, bool fp32,
+                      cudaStream_t s) {
+  if (fp32)
+    k_adj_deposit<float><<<dim3((d.cap + 127) / 128, d.nrowjob), 128, 0, s>>>(d, luj, lA, lB);
+  else
+    k_adj_deposit<double><<<dim3((d.cap + 127) / 128, d.nrowjob), 128, 0, s>>>(d, luj, lA, lB);
 }
 
 // zero everything but the interior cells of ncomp field planes
@@ -657,14 +676,20 @@ void adj_unsort(const Dev2D& d, const Parts64& lA, const Parts64& lB, cudaStream
 }
 
 void adj_particles(const Dev2D& d, const double* luj, const Parts64& lA, const Parts64& lB, double* tmp,
-                   double* ltmp, double* luf, cudaStream_t s) {
+                   double* ltmp, double* luf, bool fp32, cudaStream_t s) {
   const Grid2D& g = d.g;
   const size_t n = (size_t)(g.nx + 2) * (g.ny + 2);
   dim3 grid((d.cap + 127) / 128, d.nrowjob);
-  k_adj_deposit<<<grid, 128, 0, s>>>(d, luj, lA, lB);
+  if (fp32)
+    k_adj_deposit<float><<<grid, 128, 0, s>>>(d, luj, lA, lB);
+  else
+    k_adj_deposit<double><<<grid, 128, 0, s>>>(d, luj, lA, lB);
   k_adj_tmp<<<4 * 152, 256, 0, s>>>(d, tmp);
   cudaMemsetAsync(ltmp, 0, sizeof(double) * 6 * n, s);
-  k_adj_push<<<grid, 128, 0, s>>>(d, tmp, lA, lB, ltmp);
+  if (fp32)
+    k_adj_push<float><<<grid, 128, 0, s>>>(d, tmp, lA, lB, ltmp);
+  else
+    k_adj_push<double><<<grid, 128, 0, s>>>(d, tmp, lA, lB, ltmp);
   k_adj_tmpT<<<4 * 152, 256, 0, s>>>(d, ltmp, luf);
 }
 

@@ -76,6 +76,7 @@ struct wpic_ctx {
   double *luf = nullptr, *ldf = nullptr, *luj = nullptr, *lg = nullptr, *tmpc = nullptr, *ltmp = nullptr;
   int* adj_cc = nullptr;  // the step's cell offsets, kept across the sort that gives the permutation
   int adj_nsteps = 0, adj_every = 1;  // the recorded forward run (0: none)
+  int adj_fp32 = 0;  // the reverse push and deposit sweeps in FP32 (fields, CG and sums in FP64)
   // scratch of the adjoint's self-checks, allocated on first use
   double* chk_dots = nullptr;
   Parts64 chk_A0{}, chk_B0{}, chk_vA{}, chk_vB{};
@@ -957,7 +958,7 @@ int adj_step(wpic_ctx* c, const wpic_ctx::AdjState* S) {
     int st = do_cg(c);
     if (!st) {
       adj_field_after_cg(d, c->luf, c->lg, c->luj, c->stream);
-      adj_particles(d, c->luj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->stream);
+      adj_particles(d, c->luj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->adj_fp32 != 0, c->stream);
     }
     d.B = B0;
     d.map = map0;
@@ -980,7 +981,7 @@ int adj_step(wpic_ctx* c, const wpic_ctx::AdjState* S) {
   int st = do_cg(c);                                 // the adjoint solve: same symmetric operator
   if (st) return st;
   adj_field_after_cg(d, c->luf, c->lg, c->luj, c->stream);
-  adj_particles(d, c->luj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->stream);
+  adj_particles(d, c->luj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->adj_fp32 != 0, c->stream);
   return WPIC_OK;
 }
 
@@ -1099,7 +1100,7 @@ int wpic_adjoint_pushcheck(wpic_ctx* c, double hstep, double* out) {
   cudaMemcpyAsync(d.uf, c->ldf, 6 * P * 8, cudaMemcpyDeviceToDevice, c->stream);
   // adjoint into ldf (zeroed): <v, ldf>
   cudaMemsetAsync(c->ldf, 0, 6 * P * 8, c->stream);
-  adj_push_fields(d, c->lB, c->lA, c->tmpc, c->ltmp, c->ldf, c->stream);
+  adj_push_fields(d, c->lB, c->lA, c->tmpc, c->ltmp, c->ldf, c->adj_fp32 != 0, c->stream);
   adj_dot(c->luf, c->ldf, 6 * P, dots + 1, c->stream);
   double h[2];
   CK(cudaMemcpyAsync(h, dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -1145,7 +1146,7 @@ int wpic_adjoint_depositcheck(wpic_ctx* c, double hstep, double* out) {
   adj_copy_parts(B0, d.B, slots, c->stream);
   adj_zero_parts(c->lA, slots, c->stream);
   adj_zero_parts(c->lB, slots, c->stream);
-  adj_deposit_only(d, c->luj, c->lA, c->lB, c->stream);
+  adj_deposit_only(d, c->luj, c->lA, c->lB, c->adj_fp32 != 0, c->stream);
   double* la[2] = {c->lA.x, c->lA.y};
   double* lb[5] = {c->lB.x, c->lB.y, c->lB.ux, c->lB.uy, c->lB.uz};
   for (int q = 0; q < 2; ++q) adj_dot(va[q], la[q], slots, dots + 2, c->stream);
@@ -1184,7 +1185,7 @@ int wpic_adjoint_chaincheck(wpic_ctx* c, double hstep, double* out) {
   cudaMemsetAsync(c->luf, 0, 6 * P * 8, c->stream);
   adj_zero_parts(c->lA, slots, c->stream);
   adj_zero_parts(c->lB, slots, c->stream);
-  adj_particles(d, lj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->stream);
+  adj_particles(d, lj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->adj_fp32 != 0, c->stream);
   adj_dot(v, c->luf, 6 * P, dots + 2, c->stream);
   double h[3];
   CK(cudaMemcpyAsync(h, dots, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -1192,6 +1193,16 @@ int wpic_adjoint_chaincheck(wpic_ctx* c, double hstep, double* out) {
   out[0] = (h[0] - h[1]) * 0.5 / hstep;
   out[1] = h[2];
   return finish(c);
+}
+
+// Arithmetic of the adjoint's per-particle sweeps: WPIC_FP64 (or WPIC_FP64_EXACT) for FP64,
+// WPIC_MIXED for FP32 push and deposit reverses along the recorded FP64 trajectory; the field
+// adjoint, the adjoint CG and every accumulation stay FP64.
+int wpic_adjoint_precision(wpic_ctx* c, int precision) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (precision != WPIC_FP64 && precision != WPIC_FP64_EXACT && precision != WPIC_MIXED) return WPIC_BAD_ARGUMENT;
+  c->adj_fp32 = precision == WPIC_MIXED;
+  return WPIC_OK;
 }
 
 // Forward half of the adjoint: nsteps steps from the current state, keeping the particle and

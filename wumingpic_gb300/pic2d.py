@@ -128,6 +128,13 @@ class Pic2D:
                                  _ptr(lup, np.float64), _ptr(luf, np.float64)), "adjoint")
         return lup, luf
 
+    def adjoint_precision(self, precision):
+        """Arithmetic of the reverse push and deposit sweeps: "fp64" (default) or "mixed"
+        (FP32 per particle along the recorded FP64 trajectory; fields, adjoint CG and all
+        accumulations in FP64)."""
+        code = {"fp64": _lib.FP64, "fp64_exact": _lib.FP64_EXACT, "mixed": _lib.MIXED}[precision]
+        check(lib().wpic_adjoint_precision(self._h, code), "adjoint_precision")
+
     def adjoint_record(self, nsteps, every):
         """The forward half of ``adjoint``: run nsteps steps keeping the state every `every` steps."""
         check(lib().wpic_adjoint_record(self._h, int(nsteps), int(every)), "adjoint_record")
