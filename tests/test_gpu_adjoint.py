@@ -119,6 +119,21 @@ def test_checkpoint_interval(gpu_lib):
         assert np.abs(lup[:5] - res[0][0][:5]).max() <= 1e-12 * np.abs(res[0][0][:5]).max()
 
 
+@pytest.mark.parametrize("every", [2, 5])
+def test_reverse_twice(gpu_lib, every):
+    """The record keeps its last segment's step states; a second reverse sweep of the same
+    record recomputes that segment and gives the same gradients."""
+    p, st = seeded_case(6)
+    g = sim(p, st)
+    g.adjoint_record(5, every)
+    _, lam = field_energy(g.get_fields(), "EB")
+    lup1, luf1 = g.adjoint_reverse(lam)
+    lup2, luf2 = g.adjoint_reverse(lam)
+    g.close()
+    assert np.abs(luf2 - luf1).max() <= 1e-12 * np.abs(luf1).max()
+    assert np.abs(lup2[:5] - lup1[:5]).max() <= 1e-12 * np.abs(lup1[:5]).max()
+
+
 def small_problem(nsteps=10, every=4, which="B"):
     p = Plasma2D(nx=32, ny=32, ppc=8, drift=0.3, u_the=0.05, seed=21)
     modes = SeedModes.lowest(p.nx, p.ny, 8)

@@ -287,10 +287,11 @@ __device__ __forceinline__ float rsq(float v) { return rsqrtf(v); }
 // gvz = uz / sqrt(1 + u^2 / c^2).  Reverse: the adjoints of the 5-point shape arrays from
 // suffix sums of lJ, then through ds = S1 - s0, the shift and the quadratic spline.
 // R is the arithmetic type of the per-particle sweep: double, or float for the
-// mixed-precision adjoint.  The in-cell offsets and the cell indices come from the FP64
-// positions in FP64 either way; the particle adjoints are accumulated into FP64 arrays.
+// mixed-precision adjoint (lJ then comes as an FP32 copy, made once per step, so that no
+// particle converts field values).  The in-cell offsets and the cell indices come from the
+// FP64 positions in FP64 either way; the particle adjoints are accumulated into FP64 arrays.
 template <typename R>
-__global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj, Parts64 lA, Parts64 lB) {
+__global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const R* luj, Parts64 lA, Parts64 lB) {
   const Grid2D g = d.g;
   const int row = blockIdx.y;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj,
   const R gmi = rsq(R(1) + ic2 * (ux * ux + uy * uy + uz * uz));
   const R gvz = uz * gmi;
   const size_t P = g.fplane;
-  const double* L0 = luj + (size_t)jj * g.fp + cx;  // node (cx + a, jj + b) at L0[b * fp + a]
+  const R* L0 = luj + (size_t)jj * g.fp + cx;  // node (cx + a, jj + b) at L0[b * fp + a]
   R gs0[2][5], gds[2][5];
 #pragma unroll
   for (int dim = 0; dim < 2; ++dim)
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj,
     R suf = R(0), gw = R(0);
 #pragma unroll
     for (int i = 3; i >= 0; --i) {
-      suf += (R)L0[(size_t)j * g.fp + i + 1];  // sum_{i'' >= i} lJx(i'' + 1, j)
+      suf += L0[(size_t)j * g.fp + i + 1];  // sum_{i'' >= i} lJx(i'' + 1, j)
       gds[0][i] += -qdd * wy * suf;
       gw += ds[0][i] * suf;
     }
@@ -357,14 +358,14 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj,
     gds[1][j] += h5 * gw;
   }
   // Jy: nodes (i, j + 1), i = 0..4, j = 0..3
-  const double* L1 = L0 + P;
+  const R* L1 = L0 + P;
 #pragma unroll
   for (int i = 0; i < 5; ++i) {
     const R wx = s0[0][i] + h5 * ds[0][i];
     R suf = R(0), gw = R(0);
 #pragma unroll
     for (int j = 3; j >= 0; --j) {
-      suf += (R)L1[(size_t)(j + 1) * g.fp + i];
+      suf += L1[(size_t)(j + 1) * g.fp + i];
       gds[1][j] += -qdd * wx * suf;
       gw += ds[1][j] * suf;
     }
@@ -373,7 +374,7 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj,
     gds[0][i] += h5 * gw;
   }
   // Jz: nodes (i, j) = Qz (s0_x (x) Ay + ds_x (x) By), Ay = s0_y + ds_y / 2, By = s0_y / 2 + ds_y / 3
-  const double* L2 = L0 + 2 * P;
+  const R* L2 = L0 + 2 * P;
   const R Qz = q * gvz;
   R gAy[5] = {R(0), R(0), R(0), R(0), R(0)}, gBy[5] = {R(0), R(0), R(0), R(0), R(0)}, phiz = R(0);
 #pragma unroll
@@ -381,7 +382,7 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj,
     R r1 = R(0), r2 = R(0);
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
-      const R l = (R)L2[(size_t)j * g.fp + i];
+      const R l = L2[(size_t)j * g.fp + i];
       r1 += l * (s0[1][j] + h5 * ds[1][j]);
       r2 += l * (h5 * s0[1][j] + fac * ds[1][j]);
       gAy[j] += l * s0[0][i];
@@ -430,9 +431,10 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const double* luj,
 // the field adjoints (B, E at the particle) spread back over the 3 x 3 tmp nodes with the
 // same spline weights: summed per (cell, component, node) over the block's particles in
 // shared memory (in R), then one FP64 atomic per (cell, component, node) of the block.
+// For R = float the cell-centred fields come as an FP32 copy made once per step.
 constexpr int AP_T = 128;
 template <typename R>
-__global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const double* tmp, Parts64 lA, Parts64 lB,
+__global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const R* tmp, Parts64 lA, Parts64 lB,
                                                    double* ltmp) {
   __shared__ R slf[6][AP_T + 1];
   __shared__ R sw[6][AP_T + 1];
@@ -472,7 +474,7 @@ __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const double* tmp, P
         R r = R(0), rx = R(0);
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-          const R t = (R)tmp[(size_t)m * n + (size_t)(jj + b) * tw + (cx + a)];
+          const R t = tmp[(size_t)m * n + (size_t)(jj + b) * tw + (cx + a)];
           r += t * sx[a];
           rx += t * dsx[a];
         }
@@ -635,25 +637,50 @@ void adj_axpy(double* dst, const double* x, const double* v, double h, size_t n,
 void adj_dot_parts(const Dev2D& d, const Parts64& L, const Parts64& P, double scale, double* out, cudaStream_t s) {
   k_dot_parts<<<dim3((d.cap + 255) / 256, d.nrowjob), 256, 0, s>>>(d, L, P, scale, out);
 }
+// FP32 copy of a field array for the FP32 sweeps
+__global__ void k_to_f32(const double* a, float* b, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+namespace {
+// the push's adjoint on the cell-centred fields tmp; f32 (null: FP64 sweep) holds 6 tmp planes
+void launch_adj_push(const Dev2D& d, double* tmp, const Parts64& lA, const Parts64& lB, double* ltmp, float* f32,
+                     cudaStream_t s) {
+  const size_t n = (size_t)(d.g.nx + 2) * (d.g.ny + 2);
+  dim3 grid((d.cap + 127) / 128, d.nrowjob);
+  if (f32) {
+    k_to_f32<<<4 * 152, 256, 0, s>>>(tmp, f32, 6 * n);
+    k_adj_push<float><<<grid, 128, 0, s>>>(d, f32, lA, lB, ltmp);
+  } else {
+    k_adj_push<double><<<grid, 128, 0, s>>>(d, tmp, lA, lB, ltmp);
+  }
+}
+void launch_adj_deposit(const Dev2D& d, const double* luj, const Parts64& lA, const Parts64& lB, float* f32,
+                        cudaStream_t s) {
+  dim3 grid((d.cap + 127) / 128, d.nrowjob);
+  if (f32) {
+    k_to_f32<<<4 * 152, 256, 0, s>>>(luj, f32, 3 * d.g.fplane);
+    k_adj_deposit<float><<<grid, 128, 0, s>>>(d, f32, lA, lB);
+  } else {
+    k_adj_deposit<double><<<grid, 128, 0, s>>>(d, luj, lA, lB);
+  }
+}
+}  // namespace
+
 // the push's field adjoint alone: luf += (dB/duf)^T lB (lA receives the particle part)
 void adj_push_fields(const Dev2D& d, const Parts64& lB, const Parts64& lA, double* tmp, double* ltmp, double* luf,
-                     bool fp32, cudaStream_t s) {
+                     float* f32, cudaStream_t s) {
   const size_t n = (size_t)(d.g.nx + 2) * (d.g.ny + 2);
   k_adj_tmp<<<4 * 152, 256, 0, s>>>(d, tmp);
   cudaMemsetAsync(ltmp, 0, sizeof(double) * 6 * n, s);
-  if (fp32)
-    k_adj_push<float><<<dim3((d.cap + 127) / 128, d.nrowjob), 128, 0, s>>>(d, tmp, lA, lB, ltmp);
-  else
-    k_adj_push<double><<<dim3((d.cap + 127) / 128, d.nrowjob), 128, 0, s>>>(d, tmp, lA, lB, ltmp);
+  launch_adj_push(d, tmp, lA, lB, ltmp, f32, s);
   k_adj_tmpT<<<4 * 152, 256, 0, s>>>(d, ltmp, luf);
 }
 
-void adj_deposit_only(const Dev2D& d, const double* luj, const Parts64& lA, const Parts64& lB, bool fp32,
+void adj_deposit_only(const Dev2D& d, const double* luj, const Parts64& lA, const Parts64& lB, float* f32,
                       cudaStream_t s) {
-  if (fp32)
-    k_adj_deposit<float><<<dim3((d.cap + 127) / 128, d.nrowjob), 128, 0, s>>>(d, luj, lA, lB);
-  else
-    k_adj_deposit<double><<<dim3((d.cap + 127) / 128, d.nrowjob), 128, 0, s>>>(d, luj, lA, lB);
+  launch_adj_deposit(d, luj, lA, lB, f32, s);
 }
 
 // zero everything but the interior cells of ncomp field planes
@@ -676,20 +703,12 @@ void adj_unsort(const Dev2D& d, const Parts64& lA, const Parts64& lB, cudaStream
 }
 
 void adj_particles(const Dev2D& d, const double* luj, const Parts64& lA, const Parts64& lB, double* tmp,
-                   double* ltmp, double* luf, bool fp32, cudaStream_t s) {
-  const Grid2D& g = d.g;
-  const size_t n = (size_t)(g.nx + 2) * (g.ny + 2);
-  dim3 grid((d.cap + 127) / 128, d.nrowjob);
-  if (fp32)
-    k_adj_deposit<float><<<grid, 128, 0, s>>>(d, luj, lA, lB);
-  else
-    k_adj_deposit<double><<<grid, 128, 0, s>>>(d, luj, lA, lB);
+                   double* ltmp, double* luf, float* f32, cudaStream_t s) {
+  const size_t n = (size_t)(d.g.nx + 2) * (d.g.ny + 2);
+  launch_adj_deposit(d, luj, lA, lB, f32, s);
   k_adj_tmp<<<4 * 152, 256, 0, s>>>(d, tmp);
   cudaMemsetAsync(ltmp, 0, sizeof(double) * 6 * n, s);
-  if (fp32)
-    k_adj_push<float><<<grid, 128, 0, s>>>(d, tmp, lA, lB, ltmp);
-  else
-    k_adj_push<double><<<grid, 128, 0, s>>>(d, tmp, lA, lB, ltmp);
+  launch_adj_push(d, tmp, lA, lB, ltmp, f32, s);
   k_adj_tmpT<<<4 * 152, 256, 0, s>>>(d, ltmp, luf);
 }
 

@@ -77,6 +77,8 @@ struct wpic_ctx {
   int* adj_cc = nullptr;  // the step's cell offsets, kept across the sort that gives the permutation
   int adj_nsteps = 0, adj_every = 1;  // the recorded forward run (0: none)
   int adj_fp32 = 0;  // the reverse push and deposit sweeps in FP32 (fields, CG and sums in FP64)
+  bool adj_last_kept = false;  // the step states hold the recorded run's last segment
+  float* adj_f32 = nullptr;     // FP32 copies of lJ / the cell-centred fields for the FP32 sweeps
   // scratch of the adjoint's self-checks, allocated on first use
   double* chk_dots = nullptr;
   Parts64 chk_A0{}, chk_B0{}, chk_vA{}, chk_vB{};
@@ -900,7 +902,8 @@ int adj_prepare(wpic_ctx* c, int nstates) {
     if ((st = dalloc(c, &c->luf, 6 * P)) || (st = dalloc(c, &c->ldf, 6 * P)) || (st = dalloc(c, &c->luj, 3 * P)))
       return st;
     if ((st = dalloc(c, &c->lg, 3 * (size_t)d.g.ncell)) || (st = dalloc(c, &c->tmpc, nt)) ||
-        (st = dalloc(c, &c->ltmp, nt)) || (st = dalloc(c, &c->adj_cc, (size_t)d.nrowjob * (d.g.nx + 1))))
+        (st = dalloc(c, &c->ltmp, nt)) || (st = dalloc(c, &c->adj_cc, (size_t)d.nrowjob * (d.g.nx + 1))) ||
+        (st = dalloc(c, &c->adj_f32, 6 * P)))
       return st;
     if ((st = ensure_C(c))) return st;
     c->adj_ready = true;
@@ -958,7 +961,7 @@ int adj_step(wpic_ctx* c, const wpic_ctx::AdjState* S) {
     int st = do_cg(c);
     if (!st) {
       adj_field_after_cg(d, c->luf, c->lg, c->luj, c->stream);
-      adj_particles(d, c->luj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->adj_fp32 != 0, c->stream);
+      adj_particles(d, c->luj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->adj_fp32 ? c->adj_f32 : nullptr, c->stream);
     }
     d.B = B0;
     d.map = map0;
@@ -981,7 +984,7 @@ int adj_step(wpic_ctx* c, const wpic_ctx::AdjState* S) {
   int st = do_cg(c);                                 // the adjoint solve: same symmetric operator
   if (st) return st;
   adj_field_after_cg(d, c->luf, c->lg, c->luj, c->stream);
-  adj_particles(d, c->luj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->adj_fp32 != 0, c->stream);
+  adj_particles(d, c->luj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->adj_fp32 ? c->adj_f32 : nullptr, c->stream);
   return WPIC_OK;
 }
 
@@ -1100,7 +1103,7 @@ int wpic_adjoint_pushcheck(wpic_ctx* c, double hstep, double* out) {
   cudaMemcpyAsync(d.uf, c->ldf, 6 * P * 8, cudaMemcpyDeviceToDevice, c->stream);
   // adjoint into ldf (zeroed): <v, ldf>
   cudaMemsetAsync(c->ldf, 0, 6 * P * 8, c->stream);
-  adj_push_fields(d, c->lB, c->lA, c->tmpc, c->ltmp, c->ldf, c->adj_fp32 != 0, c->stream);
+  adj_push_fields(d, c->lB, c->lA, c->tmpc, c->ltmp, c->ldf, c->adj_fp32 ? c->adj_f32 : nullptr, c->stream);
   adj_dot(c->luf, c->ldf, 6 * P, dots + 1, c->stream);
   double h[2];
   CK(cudaMemcpyAsync(h, dots, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -1146,7 +1149,7 @@ int wpic_adjoint_depositcheck(wpic_ctx* c, double hstep, double* out) {
   adj_copy_parts(B0, d.B, slots, c->stream);
   adj_zero_parts(c->lA, slots, c->stream);
   adj_zero_parts(c->lB, slots, c->stream);
-  adj_deposit_only(d, c->luj, c->lA, c->lB, c->adj_fp32 != 0, c->stream);
+  adj_deposit_only(d, c->luj, c->lA, c->lB, c->adj_fp32 ? c->adj_f32 : nullptr, c->stream);
   double* la[2] = {c->lA.x, c->lA.y};
   double* lb[5] = {c->lB.x, c->lB.y, c->lB.ux, c->lB.uy, c->lB.uz};
   for (int q = 0; q < 2; ++q) adj_dot(va[q], la[q], slots, dots + 2, c->stream);
@@ -1185,7 +1188,7 @@ int wpic_adjoint_chaincheck(wpic_ctx* c, double hstep, double* out) {
   cudaMemsetAsync(c->luf, 0, 6 * P * 8, c->stream);
   adj_zero_parts(c->lA, slots, c->stream);
   adj_zero_parts(c->lB, slots, c->stream);
-  adj_particles(d, lj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->adj_fp32 != 0, c->stream);
+  adj_particles(d, lj, c->lA, c->lB, c->tmpc, c->ltmp, c->luf, c->adj_fp32 ? c->adj_f32 : nullptr, c->stream);
   adj_dot(v, c->luf, 6 * P, dots + 2, c->stream);
   double h[3];
   CK(cudaMemcpyAsync(h, dots, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -1215,12 +1218,26 @@ int wpic_adjoint_record(wpic_ctx* c, int nsteps, int every) {
   c->adj_nsteps = 0;
   int st = adj_prepare(c, nseg + every + 1);
   if (st) return st;
+  // the last segment keeps its step states as it runs: the reverse sweep starts on it
+  // without recomputing it
+  const int last0 = (nseg - 1) * every;
+  c->adj_last_kept = false;
   for (int k = 0; k < nsteps; ++k) {
     if (k % every == 0) adj_save(c, c->adj_states[k / every]);
+    if (k >= last0) {
+      wpic_ctx::AdjState& S = c->adj_states[nseg + (k - last0)];
+      adj_save(c, S);
+      S.has_step = false;
+      if (k + 1 < nsteps) {  // the segment's last step is pushed and sorted again by adj_step
+        if ((st = adj_alloc_step(c, S)) || (st = adj_forward_step(c, S))) return st;
+        continue;
+      }
+    }
     if ((st = one_step(c))) return st;
   }
   adj_save(c, c->adj_states[nseg + every]);
   if ((st = finish(c))) return st;
+  c->adj_last_kept = true;
   c->adj_nsteps = nsteps;
   c->adj_every = every;
   return WPIC_OK;
@@ -1248,8 +1265,9 @@ int wpic_adjoint_reverse(wpic_ctx* c, const double* lam_uf_final, double* lam_up
   for (int l = 0; l < 3; ++l) c->cg_fixed[l] = -1;  // adjoint solves: the tolerance rule
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int s0 = seg * every, s1 = std::min(nsteps, s0 + every);
-    adj_load(c, ckpt(seg));
-    for (int k = s0; k < s1; ++k) {
+    const bool kept = seg == nseg - 1 && c->adj_last_kept;
+    if (!kept) adj_load(c, ckpt(seg));
+    for (int k = s0; k < s1 && !kept; ++k) {
       wpic_ctx::AdjState& S = step_state(k - s0);
       adj_save(c, S);
       S.has_step = false;
@@ -1264,6 +1282,7 @@ int wpic_adjoint_reverse(wpic_ctx* c, const double* lam_uf_final, double* lam_up
     }
     if (st) break;
     if ((st = finish(c))) break;
+    if (seg < nseg - 1) c->adj_last_kept = false;  // the step states now hold this segment
   }
   for (int l = 0; l < 3; ++l) c->cg_fixed[l] = fixed_saved[l];
   if (st) return st;

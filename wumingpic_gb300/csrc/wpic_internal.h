@@ -170,12 +170,13 @@ void dfield_ghost2d(const Dev2D& d, cudaStream_t s);
 void uf_add2d(const Dev2D& d, cudaStream_t s);
 void particle_x2d(const Dev2D& d, const Parts64& P, cudaStream_t s);
 void injection2d(const Dev2D& d, const Parts64& P, double u0, double xend, cudaStream_t s);
-// adjoint of the FP64 2D step (adjoint2d.cu); fp32: the per-particle sweeps in FP32
+// adjoint of the FP64 2D step (adjoint2d.cu); f32 (6 field planes of FP32 scratch, or null):
+// the per-particle sweeps in FP32
 void adj_field(const Dev2D& d, double* luf, double* ldf, double* luj, cudaStream_t s);
 void adj_field_after_cg(const Dev2D& d, double* luf, double* lg, double* luj, cudaStream_t s);
 void adj_unsort(const Dev2D& d, const Parts64& lA, const Parts64& lB, cudaStream_t s);
 void adj_particles(const Dev2D& d, const double* luj, const Parts64& lA, const Parts64& lB, double* tmp,
-                   double* ltmp, double* luf, bool fp32, cudaStream_t s);
+                   double* ltmp, double* luf, float* f32, cudaStream_t s);
 void adj_fill_rand(double* v, size_t n, unsigned seed, cudaStream_t s);
 void adj_field_fold_T(const Dev2D& d, double* luj, cudaStream_t s);
 void adj_field_ghost_T(const Dev2D& d, double* ldf, cudaStream_t s);
@@ -186,10 +187,10 @@ void adj_field_tmp_T(const Dev2D& d, const double* ltmp, double* luf, cudaStream
 void adj_keep_interior(const Dev2D& d, double* v, int ncomp, cudaStream_t s);
 void adj_axpy(double* dst, const double* x, const double* v, double h, size_t n, cudaStream_t s);
 void adj_dot_parts(const Dev2D& d, const Parts64& L, const Parts64& P, double scale, double* out, cudaStream_t s);
-void adj_deposit_only(const Dev2D& d, const double* luj, const Parts64& lA, const Parts64& lB, bool fp32,
+void adj_deposit_only(const Dev2D& d, const double* luj, const Parts64& lA, const Parts64& lB, float* f32,
                       cudaStream_t s);
 void adj_push_fields(const Dev2D& d, const Parts64& lB, const Parts64& lA, double* tmp, double* ltmp, double* luf,
-                     bool fp32, cudaStream_t s);
+                     float* f32, cudaStream_t s);
 void adj_dot(const double* a, const double* b, size_t n, double* out, cudaStream_t s);
 void migrate_scan2d(const Dev2D& d, const Parts64& P, cudaStream_t s);
 void migrate_plan2d(const Dev2D& d, cudaStream_t s);
