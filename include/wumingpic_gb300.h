@@ -65,7 +65,7 @@ extern "C" {
 
 /* the push of the fused step: particle__solv (Buneman-Boris) or particle__solv_vay */
 #define WPIC_PUSH_BORIS 0
-#define WPIC_PUSH_VAY 1   /* FP64 paths only */
+#define WPIC_PUSH_VAY 1   /* every path; the mixed paths run it inside their fused step */
 
 typedef struct wpic_ctx wpic_ctx;
 

@@ -2,8 +2,8 @@
 FP32 push/gather/deposition, FP64 fields), through the C ABI.
 
 Every result is stated as an error against the FP64 path:
-  * one step from the same state: momenta and positions within 1e-5 relative to
-    their scale, fields within 1e-4 of max|B, E|;
+  * one step from the same state (Boris and Vay pushers): momenta and positions within
+    1e-5 relative to their scale, fields within 1e-4 of max|B, E|;
   * charge conservation |d rho/dt + div J| <= 1e-6 of max |d rho/dt|, rho computed in
     FP64 from the exact stored positions;
   * bookkeeping exact: particle count and the set of IDs conserved, every
@@ -51,7 +51,8 @@ def test_put_get_round_trip(gpu_lib):
             np.testing.assert_allclose(out.up[2:5, :n, jj, isp], st.up[2:5, :n, jj, isp], rtol=2 ** -23, atol=1e-30)
 
 
-def test_one_step_against_fp64(gpu_lib):
+@pytest.mark.parametrize("pusher", ["boris", "vay"])
+def test_one_step_against_fp64(gpu_lib, pusher):
     p, st = small_case(nx=32, ny=32, ppc=8, seed=6)
     rng = np.random.default_rng(6)
     st.uf[...] = 0.02 * rng.standard_normal(st.uf.shape)
@@ -60,6 +61,8 @@ def test_one_step_against_fp64(gpu_lib):
     st.uf[:, :, :2] = st.uf[:, :, p.ny:p.ny + 2]
     st.uf[:, :, p.ny + 2:] = st.uf[:, :, 2:4]
     gm, gd = make(p, "mixed", gpu_lib), make(p, "fp64", gpu_lib)
+    gm.set_pusher(pusher)
+    gd.set_pusher(pusher)
     gm.put_state(st)
     gd.put_state(st)
     gm.step(1)

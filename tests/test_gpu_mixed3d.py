@@ -43,12 +43,15 @@ def perturbed(seed, nx=16, ny=16, nz=8, ppc=6):
     return p, st
 
 
-def test_mixed3d_one_step_against_fp64(gpu_lib):
+@pytest.mark.parametrize("pusher", ["boris", "vay"])
+def test_mixed3d_one_step_against_fp64(gpu_lib, pusher):
     p, st = perturbed(71)
     m = make(p, "mixed")
+    m.set_pusher(pusher)
     m.put_state(st)
     m.step(1)
     f = make(p, "fp64")
+    f.set_pusher(pusher)
     f.put_state(st)
     f.step(1)
     sm, sf = m.get_state(), f.get_state()

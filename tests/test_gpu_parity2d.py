@@ -119,11 +119,12 @@ def test_one_step_vay_exact_is_bit_exact_on_particles(gpu_lib):
     assert_field(out.uf, ref.uf, REL)
 
 
-def test_vay_is_rejected_on_the_mixed_path(gpu_lib):
+def test_vay_on_the_mixed_path_is_a_step_option(gpu_lib):
+    """The mixed path runs Vay inside its fused step (wpic_set_pusher); it has no separate
+    particle__solv_vay module call."""
     p, st = perturbed_case(seed=34, nx=16, ny=16)
     g = make_gpu(p, "mixed", gpu_lib)
-    with pytest.raises(RuntimeError):
-        g.set_pusher("vay")
+    g.set_pusher("vay")
     with pytest.raises(RuntimeError):
         g.particle__solv_vay()
 

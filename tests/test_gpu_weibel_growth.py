@@ -1,7 +1,8 @@
 """Weibel growth rate of the mixed-precision path against the FP64 path (GPU).
 
 The mixed path (integer cell + FP32 offset, FP32 push and deposition, FP64
-fields and CG) must reproduce the physics of the FP64 path: from the same
+fields and CG) must reproduce the physics of the FP64 path, with the Boris and
+(2D) the Vay pusher: from the same
 initial state, the exponential growth rate of the magnetic field energy in the
 linear phase of the Weibel instability agrees within 1 %, and both runs reach
 saturation (the nonlinear stage concentrates particles into current filaments,
@@ -20,22 +21,24 @@ pytestmark = pytest.mark.gpu
 GROWTH_RATE_RTOL = 0.01
 
 
-def _run(p, st, precision, nsteps):
+def _run(p, st, precision, nsteps, pusher="boris"):
     from wumingpic_gb300.pic2d import Pic2D
     g = Pic2D(p, precision=precision)
+    g.set_pusher(pusher)
     g.put_state(st)
     t, e = energy_history(g.step, g.energy, nsteps, 10, p.delt)
     g.close()
     return t, e
 
 
-def test_weibel_growth_rate_mixed_matches_fp64(gpu_lib):
+@pytest.mark.parametrize("pusher", ["boris", "vay"])
+def test_weibel_growth_rate_mixed_matches_fp64(gpu_lib, pusher):
     # counter-streaming electrons along z (+-0.5 c), filamentation in the x-y plane
     p = Plasma2D(nx=128, ny=128, ppc=16, drift=0.5, u_the=0.05, seed=424242, np_slack=5.0)
     st = load_weibel2d(p)
     nsteps = 1000
-    t, e64 = _run(p, st, "fp64", nsteps)
-    _, emx = _run(p, st, "mixed", nsteps)
+    t, e64 = _run(p, st, "fp64", nsteps, pusher)
+    _, emx = _run(p, st, "mixed", nsteps, pusher)
     b64, bmx = e64[:, 3], emx[:, 3]
     # saturation reached: the magnetic energy grew by orders of magnitude in both runs
     assert b64.max() > 1e3 * b64[1] and bmx.max() > 1e3 * bmx[1]

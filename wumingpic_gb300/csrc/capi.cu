@@ -382,7 +382,7 @@ int mix_grow(wpic_ctx* c) {
 int mixed_step(wpic_ctx* c) {
   Dev2D& d = c->d;
   stage_begin(c, SG_PUSH);
-  mix_push_deposit2d(d, c->tmap, c->stream);
+  mix_push_deposit2d(d, c->tmap, c->pusher == WPIC_PUSH_VAY, c->stream);
   stage_end(c, SG_PUSH, 1);
   // the arrivals join their columns right away, so the particle state is whole again before
   // the field solve (which does not read particles) can return an error
@@ -1330,7 +1330,6 @@ int wpic_particle_solv_vay(wpic_ctx* c) {
 int wpic_set_pusher(wpic_ctx* c, int pusher) {
   if (!c) return WPIC_NOT_INITIALISED;
   if (pusher != WPIC_PUSH_BORIS && pusher != WPIC_PUSH_VAY) return WPIC_BAD_ARGUMENT;
-  if (c->mixed && pusher != WPIC_PUSH_BORIS) return WPIC_BAD_ARGUMENT;
   c->pusher = pusher;
   return WPIC_OK;
 }

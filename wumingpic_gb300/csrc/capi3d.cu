@@ -150,7 +150,7 @@ void do_migrate_sort3(wpic_ctx3d* c) {
 // the mixed step: fused FP32 push + deposit into the fixed-point current, then the FP64
 // field solve and bookkeeping of the FP64 path
 int mixed_step3(wpic_ctx3d* c) {
-  mix3_push_deposit(c->d, c->mk, c->ujx, c->stream);
+  mix3_push_deposit(c->d, c->mk, c->ujx, c->pusher == WPIC_PUSH_VAY, c->stream);
   curre_fold3d(c->d, c->stream);
   fast::gkl3d(c->d, c->stream);
   int st = do_cg3(c);
@@ -430,7 +430,6 @@ int wpic3d_particle_solv_vay(wpic_ctx3d* c) {
 int wpic3d_set_pusher(wpic_ctx3d* c, int pusher) {
   if (!c) return WPIC_NOT_INITIALISED;
   if (pusher != WPIC_PUSH_BORIS && pusher != WPIC_PUSH_VAY) return WPIC_BAD_ARGUMENT;
-  if (c->mixed && pusher != WPIC_PUSH_BORIS) return WPIC_BAD_ARGUMENT;
   c->pusher = pusher;
   return WPIC_OK;
 }

@@ -171,6 +171,9 @@ __device__ __forceinline__ void write_pending(const PendingLeaver* pend, int c, 
 // ---------------------------------------------------------------------------
 // fused push + deposit, one CTA per tile, one thread per cell column
 // ---------------------------------------------------------------------------
+// VAY: the push of particle__solv_vay (2d/common/particle.f90:182-315) in place of the
+// Buneman-Boris rotation; gather, move and deposit are the same.
+template <bool VAY>
 __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d, const __grid_constant__ CUtensorMap tm) {
   // the TMA staging of uf is dead once the cell-centred values exist; its bytes then hold the
   // fixed-point current planes of the tile
@@ -293,23 +296,46 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
       }
     }
     const float bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
-    // Buneman-Boris (2d/common/particle.f90:133-155)
-    float u1 = ux + fac1 * epx, u2 = uy + fac1 * epy, u3 = uz + fac1 * epz;
-    const float g2 = cl * cl + u1 * u1 + u2 * u2 + u3 * u3;
-    const float igam = rsqrtf(g2);
-    const float gm = g2 * igam;
-    const float fac1r = fac1 * igam;
-    const float fac2r = __fdividef(fac2, gm + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
-    const float u4 = u1 + fac1r * (u2 * bpz - u3 * bpy);
-    const float u5 = u2 + fac1r * (u3 * bpx - u1 * bpz);
-    const float u6 = u3 + fac1r * (u1 * bpy - u2 * bpx);
-    u1 = u1 + fac2r * (u5 * bpz - u6 * bpy);
-    u2 = u2 + fac2r * (u6 * bpx - u4 * bpz);
-    u3 = u3 + fac2r * (u4 * bpy - u5 * bpx);
-    ux = u1 + fac1 * epx;
-    uy = u2 + fac1 * epy;
-    uz = u3 + fac1 * epz;
-    const float ig = rsqrtf(1.f + (ux * ux + uy * uy + uz * uz) * ic2);
+    float ig;
+    if constexpr (VAY) {
+      // Vay (2d/common/particle.f90:214-262): gamma of the old momentum, the full electric
+      // kick plus the half rotation, then the implicit rotation solved in closed form; the
+      // move uses the new gamma of that solution
+      const float fac1r = fac1 * rsqrtf(cl * cl + ux * ux + uy * uy + uz * uz);
+      const float u4 = ux + fac2 * epx + fac1r * (uy * bpz - uz * bpy);
+      const float u5 = uy + fac2 * epy + fac1r * (uz * bpx - ux * bpz);
+      const float u6 = uz + fac2 * epz + fac1r * (ux * bpy - uy * bpx);
+      const float icl = ic2 * cl;
+      const float tx = fac1 * bpx * icl, ty = fac1 * bpy * icl, tz = fac1 * bpz * icl;
+      const float tau2 = tx * tx + ty * ty + tz * tz;
+      const float ua = (u4 * tx + u5 * ty + u6 * tz) * icl;
+      const float sigma = 1.f + (u4 * u4 + u5 * u5 + u6 * u6) * ic2 - tau2;
+      const float gam2 = 0.5f * (sigma + sqrtf(sigma * sigma + 4.f * (tau2 + ua * ua)));
+      ig = rsqrtf(gam2);
+      const float gv = gam2 * ig;
+      const float t = __fdividef(1.f, tau2 + gam2);
+      ux = t * (gam2 * u4 + cl * ua * tx + gv * (u5 * tz - u6 * ty));
+      uy = t * (gam2 * u5 + cl * ua * ty + gv * (u6 * tx - u4 * tz));
+      uz = t * (gam2 * u6 + cl * ua * tz + gv * (u4 * ty - u5 * tx));
+    } else {
+      // Buneman-Boris (2d/common/particle.f90:133-155)
+      float u1 = ux + fac1 * epx, u2 = uy + fac1 * epy, u3 = uz + fac1 * epz;
+      const float g2 = cl * cl + u1 * u1 + u2 * u2 + u3 * u3;
+      const float igam = rsqrtf(g2);
+      const float gm = g2 * igam;
+      const float fac1r = fac1 * igam;
+      const float fac2r = __fdividef(fac2, gm + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
+      const float u4 = u1 + fac1r * (u2 * bpz - u3 * bpy);
+      const float u5 = u2 + fac1r * (u3 * bpx - u1 * bpz);
+      const float u6 = u3 + fac1r * (u1 * bpy - u2 * bpx);
+      u1 = u1 + fac2r * (u5 * bpz - u6 * bpy);
+      u2 = u2 + fac2r * (u6 * bpx - u4 * bpz);
+      u3 = u3 + fac2r * (u4 * bpy - u5 * bpx);
+      ux = u1 + fac1 * epx;
+      uy = u2 + fac1 * epy;
+      uz = u3 + fac1 * epz;
+      ig = rsqrtf(1.f + (ux * ux + uy * uy + uz * uz) * ic2);
+    }
     // move in cell units; |displacement| < 1 cell, so the new cell is one of -1, 0, +1
     float nx_ = ox + ux * dtdx * ig, ny_ = oy + uy * dtdx * ig;
     int incx = 0, incy = 0;
@@ -458,9 +484,12 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
   }
 }
 
-void mix_push_deposit2d(const Dev2D& d, const void* tmap, cudaStream_t s) {
+void mix_push_deposit2d(const Dev2D& d, const void* tmap, bool vay, cudaStream_t s) {
   cudaMemsetAsync(d.m.ujx, 0, sizeof(unsigned long long) * 3 * (size_t)d.g.fplane, s);
-  k_mix_push<<<d.m.ntile, MP_THREADS, PUSH_DYN_BYTES, s>>>(d, *(const CUtensorMap*)tmap);
+  if (vay)
+    k_mix_push<true><<<d.m.ntile, MP_THREADS, PUSH_DYN_BYTES, s>>>(d, *(const CUtensorMap*)tmap);
+  else
+    k_mix_push<false><<<d.m.ntile, MP_THREADS, PUSH_DYN_BYTES, s>>>(d, *(const CUtensorMap*)tmap);
 }
 
 // fixed point -> FP64 current over the whole ghosted extent
@@ -1061,7 +1090,10 @@ int mix_setup2d(const Dev2D& d, void* out) {
                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return -2;
-  if (cudaFuncSetAttribute(k_mix_push, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH_DYN_BYTES) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_mix_push<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH_DYN_BYTES) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_mix_push<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH_DYN_BYTES) !=
+          cudaSuccess)
     return -3;
 
   return 0;

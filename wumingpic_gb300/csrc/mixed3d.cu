@@ -65,6 +65,9 @@ __device__ __forceinline__ void split_move(float p, float& on, int& inc, int* er
 
 }  // namespace
 
+// VAY: the push of particle__solv_vay (3d/common/particle.f90:236-419) in place of the
+// Buneman-Boris rotation; gather, move and deposit are the same.
+template <bool VAY>
 __global__ void __launch_bounds__(T3C, 2) k_mix3_step(Dev3D d, Mix3Const k, long long* ujx) {
   __shared__ float tf[6][F3Z][F3Y][F3X];
   __shared__ int jhi[3][J3Z][J3Y][J3X];
@@ -180,21 +183,45 @@ __global__ void __launch_bounds__(T3C, 2) k_mix3_step(Dev3D d, Mix3Const k, long
         }
       }
     const float bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
-    // Buneman-Boris (3d/common/particle.f90:182-205)
-    float u1 = ux0 + fac1 * epx, u2 = uy0 + fac1 * epy, u3 = uz0 + fac1 * epz;
-    const float g2 = cl * cl + u1 * u1 + u2 * u2 + u3 * u3;
-    const float igam = rsqrtf(g2);
-    const float gm = g2 * igam;
-    const float fac1r = fac1 * igam;
-    const float fac2r = __fdividef(fac2, gm + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
-    const float u4 = u1 + fac1r * (u2 * bpz - u3 * bpy);
-    const float u5 = u2 + fac1r * (u3 * bpx - u1 * bpz);
-    const float u6 = u3 + fac1r * (u1 * bpy - u2 * bpx);
-    u1 = u1 + fac2r * (u5 * bpz - u6 * bpy);
-    u2 = u2 + fac2r * (u6 * bpx - u4 * bpz);
-    u3 = u3 + fac2r * (u4 * bpy - u5 * bpx);
-    const float ux = u1 + fac1 * epx, uy = u2 + fac1 * epy, uz = u3 + fac1 * epz;
-    const float ig = rsqrtf(1.f + (ux * ux + uy * uy + uz * uz) * ic2);
+    float ux, uy, uz, ig;
+    if constexpr (VAY) {
+      // Vay: gamma of the old momentum, the full electric kick plus the half rotation, then
+      // the implicit rotation solved in closed form; the move uses that solution's gamma
+      const float fac1r = fac1 * rsqrtf(cl * cl + ux0 * ux0 + uy0 * uy0 + uz0 * uz0);
+      const float u4 = ux0 + fac2 * epx + fac1r * (uy0 * bpz - uz0 * bpy);
+      const float u5 = uy0 + fac2 * epy + fac1r * (uz0 * bpx - ux0 * bpz);
+      const float u6 = uz0 + fac2 * epz + fac1r * (ux0 * bpy - uy0 * bpx);
+      const float icl = ic2 * cl;
+      const float tx = fac1 * bpx * icl, ty = fac1 * bpy * icl, tz = fac1 * bpz * icl;
+      const float tau2 = tx * tx + ty * ty + tz * tz;
+      const float ua = (u4 * tx + u5 * ty + u6 * tz) * icl;
+      const float sigma = 1.f + (u4 * u4 + u5 * u5 + u6 * u6) * ic2 - tau2;
+      const float gam2 = 0.5f * (sigma + sqrtf(sigma * sigma + 4.f * (tau2 + ua * ua)));
+      ig = rsqrtf(gam2);
+      const float gv = gam2 * ig;
+      const float t = __fdividef(1.f, tau2 + gam2);
+      ux = t * (gam2 * u4 + cl * ua * tx + gv * (u5 * tz - u6 * ty));
+      uy = t * (gam2 * u5 + cl * ua * ty + gv * (u6 * tx - u4 * tz));
+      uz = t * (gam2 * u6 + cl * ua * tz + gv * (u4 * ty - u5 * tx));
+    } else {
+      // Buneman-Boris (3d/common/particle.f90:182-205)
+      float u1 = ux0 + fac1 * epx, u2 = uy0 + fac1 * epy, u3 = uz0 + fac1 * epz;
+      const float g2 = cl * cl + u1 * u1 + u2 * u2 + u3 * u3;
+      const float igam = rsqrtf(g2);
+      const float gm = g2 * igam;
+      const float fac1r = fac1 * igam;
+      const float fac2r = __fdividef(fac2, gm + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
+      const float u4 = u1 + fac1r * (u2 * bpz - u3 * bpy);
+      const float u5 = u2 + fac1r * (u3 * bpx - u1 * bpz);
+      const float u6 = u3 + fac1r * (u1 * bpy - u2 * bpx);
+      u1 = u1 + fac2r * (u5 * bpz - u6 * bpy);
+      u2 = u2 + fac2r * (u6 * bpx - u4 * bpz);
+      u3 = u3 + fac2r * (u4 * bpy - u5 * bpx);
+      ux = u1 + fac1 * epx;
+      uy = u2 + fac1 * epy;
+      uz = u3 + fac1 * epz;
+      ig = rsqrtf(1.f + (ux * ux + uy * uy + uz * uz) * ic2);
+    }
     const float dsp = dtdx * ig;
     float on[3];
     int inc[3];
@@ -285,9 +312,12 @@ __global__ void k_mix3_fix(Dev3D d, long long* ujx, double scale) {
   }
 }
 
-void mix3_push_deposit(const Dev3D& d, const Mix3Const& k, long long* ujx, cudaStream_t s) {
+void mix3_push_deposit(const Dev3D& d, const Mix3Const& k, long long* ujx, bool vay, cudaStream_t s) {
   const int ntile = (d.g.nx / T3X) * (d.g.ny / T3Y) * (d.g.nz / T3Z);
-  k_mix3_step<<<ntile, T3C, RING_BYTES, s>>>(d, k, ujx);
+  if (vay)
+    k_mix3_step<true><<<ntile, T3C, RING_BYTES, s>>>(d, k, ujx);
+  else
+    k_mix3_step<false><<<ntile, T3C, RING_BYTES, s>>>(d, k, ujx);
   k_mix3_fix<<<4 * 152, 256, 0, s>>>(d, ujx, std::ldexp(1.0, -k.G));
 }
 
@@ -427,7 +457,10 @@ void mix3_moments(const Dev3D& d, const Mix3Const& k, double* mom, cudaStream_t 
 bool mix3_shape_ok(int nx, int ny, int nz) { return nx % T3X == 0 && ny % T3Y == 0 && nz % T3Z == 0; }
 
 int mix3_setup() {
-  return cudaFuncSetAttribute(k_mix3_step, cudaFuncAttributeMaxDynamicSharedMemorySize, RING_BYTES) == cudaSuccess
+  return cudaFuncSetAttribute(k_mix3_step<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, RING_BYTES) ==
+                     cudaSuccess &&
+                 cudaFuncSetAttribute(k_mix3_step<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, RING_BYTES) ==
+                     cudaSuccess
              ? 0
              : -1;
 }

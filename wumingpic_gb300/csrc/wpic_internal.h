@@ -209,7 +209,7 @@ int mix_setup2d(const Dev2D& d, void* tmap_out);  // CUtensorMap of uf for the T
 void mix_relayout2d(const Dev2D& d, const float* from_P, const long long* from_boff, cudaStream_t s);
 // initial slots per column for a column of n particles (with the room the first pushes need)
 int mix_initial_depth(double n, double c_dt_dx);
-void mix_push_deposit2d(const Dev2D& d, const void* tmap, cudaStream_t s);
+void mix_push_deposit2d(const Dev2D& d, const void* tmap, bool vay, cudaStream_t s);
 void mix_curre_refresh2d(const Dev2D& d, cudaStream_t s);
 void mix_migrate2d(const Dev2D& d, cudaStream_t s);
 void mix_put2d(const Dev2D& d, const double* aos, int ndim, int np_host, int isp, int ty0, int nty, cudaStream_t s);
@@ -299,7 +299,7 @@ struct Mix3Const {
   float dtdx, c, ic2, vmax;
   int eA, G;
 };
-void mix3_push_deposit(const Dev3D& d, const Mix3Const& k, long long* ujx, cudaStream_t s);
+void mix3_push_deposit(const Dev3D& d, const Mix3Const& k, long long* ujx, bool vay, cudaStream_t s);
 bool mix3_shape_ok(int nx, int ny, int nz);
 int mix3_setup();  // kernel attributes (dynamic shared memory); 0 on success
 void mix3_moments(const Dev3D& d, const Mix3Const& k, double* mom, cudaStream_t s);
