@@ -101,6 +101,58 @@ def test_mixed3d_weibel_steps_track_fp64(gpu_lib):
     np.testing.assert_allclose(em[-2:], ef[-2:], rtol=1e-3, atol=1e-6 * ef.sum())
 
 
+def walls_perturbed(seed):
+    """The reconnection driver's walls in x (particles loaded between them), hot enough that
+    particles reach the walls within a few steps, perturbed fields."""
+    p, st = small_case3d(nx=16, ny=16, nz=8, ppc=6, seed=seed, u_the=0.3, np_slack=3.0, bc="reconnection")
+    rng = np.random.default_rng(seed)
+    core = 0.02 * rng.standard_normal((6, p.nx, p.ny, p.nz))
+    st.uf[...] = np.pad(core, ((0, 0), (2, 2), (2, 2), (2, 2)), mode="wrap")
+    return p, st
+
+
+def between_walls(p, st):
+    a = by_id(st)
+    return a[0].min() >= (p.nxgs + 1) * p.delx and a[0].max() < (p.nxge - 1) * p.delx
+
+
+def test_mixed3d_walls_one_step_against_fp64(gpu_lib):
+    """Walls on the mixed 3D path: the reflection inside the fused push, before the deposit,
+    as the reconnection driver orders particle_x; one step against the FP64 walls path."""
+    p, st = walls_perturbed(76)
+    m = make(p, "mixed")
+    m.put_state(st)
+    m.step(1)
+    f = make(p, "fp64")
+    f.put_state(st)
+    f.step(1)
+    sm, sf = m.get_state(), f.get_state()
+    assert sm.np2.sum() == sf.np2.sum() == st.np2.sum()
+    a, b = by_id(sm), by_id(sf)
+    np.testing.assert_array_equal(a[6], b[6])
+    np.testing.assert_allclose(a[:3], b[:3], rtol=0, atol=1e-5 * p.delx)
+    umax = np.abs(b[3:6]).max()
+    np.testing.assert_allclose(a[3:6], b[3:6], rtol=0, atol=1e-5 * umax)
+    jm, jf = m.get_uj(), f.get_uj()
+    np.testing.assert_allclose(jm, jf, rtol=0, atol=1e-5 * np.abs(jf).max())
+    assert between_walls(p, sm)
+
+
+def test_mixed3d_walls_steps_track_fp64(gpu_lib):
+    p, st = walls_perturbed(77)
+    m, f = make(p, "mixed"), make(p, "fp64")
+    m.put_state(st)
+    f.put_state(st)
+    for _ in range(10):
+        m.step(1)
+        f.step(1)
+    assert m.num_particles() == f.num_particles() == st.np2.sum()
+    em, ef = m.energy(), f.energy()
+    np.testing.assert_allclose(em.sum(), ef.sum(), rtol=1e-4)
+    np.testing.assert_allclose(em, ef, rtol=1e-3, atol=1e-6 * ef.sum())
+    assert between_walls(p, m.get_state())
+
+
 def test_mixed3d_rejects_staged_calls_and_odd_tiles(gpu_lib):
     from wumingpic_gb300._lib import WpicError
     p, st = perturbed(74)

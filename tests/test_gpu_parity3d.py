@@ -339,13 +339,6 @@ def test_walls_moments_3d(gpu_lib, precision, rel):
     g.close()
 
 
-def test_walls_rejected_on_the_mixed_path_3d(gpu_lib):
-    from wumingpic_gb300._lib import WpicError
-    p, st = small_case3d(nx=16, ny=16, nz=8, ppc=2, seed=74, bc="reconnection")
-    with pytest.raises(WpicError):
-        make_gpu(p, "mixed", gpu_lib)
-
-
 
 # ---- the shock boundary (3d/proj/shock/boundary_shock.f90) on a window nxs..nxe ----
 

@@ -159,7 +159,8 @@ int mixed_step3(wpic_ctx3d* c) {
   fast::efield3d(c->d, c->stream);
   dfield_ghost3d(c->d, c->stream);
   uf_add3d(c->d, c->stream);
-  particle_x3d(c->d, c->d.B, c->stream);
+  // periodic wrap in x after the field solve; the walls reflected inside the push kernel
+  if (c->d.ph.bc == BC_PERIODIC) particle_x3d(c->d, c->d.B, c->stream);
   do_migrate_sort3(c);
   return WPIC_OK;
 }
@@ -223,7 +224,8 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
   if (p->precision == WPIC_MIXED && !mix3_shape_ok(nx, ny, nz)) return WPIC_BAD_ARGUMENT;
   if (p->bc_kind != WPIC_BC_PERIODIC && p->bc_kind != WPIC_BC_RECONNECTION && p->bc_kind != WPIC_BC_SHOCK)
     return WPIC_BAD_ARGUMENT;
-  if (p->bc_kind != WPIC_BC_PERIODIC && (p->precision == WPIC_MIXED || nx < 6)) return WPIC_BAD_ARGUMENT;
+  if (p->bc_kind != WPIC_BC_PERIODIC && nx < 6) return WPIC_BAD_ARGUMENT;
+  if (p->bc_kind == WPIC_BC_SHOCK && p->precision == WPIC_MIXED) return WPIC_BAD_ARGUMENT;
   if ((double)nx * ny * nz > 2.0e9 || (double)p->nsp * ny * nz * p->np >= 2147483647.0) return WPIC_BAD_ARGUMENT;
   wpic_ctx3d* c = new wpic_ctx3d();
   c->prm = *p;

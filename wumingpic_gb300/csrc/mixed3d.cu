@@ -228,6 +228,27 @@ __global__ void __launch_bounds__(T3C, 2) k_mix3_step(Dev3D d, Mix3Const k, long
     split_move(o[0] + ux * dsp, on[0], inc[0], d.err);
     split_move(o[1] + uy * dsp, on[1], inc[1], d.err);
     split_move(o[2] + uz * dsp, on[2], inc[2], d.err);
+    if (d.ph.bc == BC_RECONNECTION) {
+      // the reconnection driver's particle_x before the deposit (3d/proj/reconnection/app.f90:103-108):
+      // reflection about the walls at cells 1 and nx-2 of the grid (nxs+1 and nxe-1), all three
+      // momentum components reversed (3d/proj/reconnection/boundary_reconnection.f90:69-101)
+      const int gxn = ci + inc[0];
+      float X = (float)gxn + on[0];
+      bool flip = false;
+      if (gxn < 1) { X = 2.f - X; flip = true; }
+      else if (gxn >= g.nx - 2) { X = 2.f * (float)(g.nx - 2) - X; flip = true; }
+      if (flip) {
+        ux = -ux; uy = -uy; uz = -uz;
+        const float fX = floorf(X);
+        on[0] = X - fX;
+        inc[0] = (int)fX - ci;
+        if (on[0] >= 1.f) { on[0] = 0.f; inc[0] += 1; }
+        if (inc[0] < -1 || inc[0] > 1) {
+          atomicOr(d.err, EB_MOVED_TOO_FAR);
+          inc[0] = max(-1, min(1, inc[0]));
+        }
+      }
+    }
     d.B.x[q] = ((double)(ia + inc[0]) + (double)on[0]) * dx;
     d.B.y[q] = ((double)(ja + inc[1]) + (double)on[1]) * dx;
     d.B.z[q] = ((double)(ka + inc[2]) + (double)on[2]) * dx;
