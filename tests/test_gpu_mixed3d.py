@@ -153,6 +153,40 @@ def test_mixed3d_walls_steps_track_fp64(gpu_lib):
     assert between_walls(p, m.get_state())
 
 
+def shock_perturbed(seed):
+    """The shock driver's window (12 of 16 cells) with its injection boundary, u0 = 0.2."""
+    p, st = small_case3d(nx=16, ny=8, nz=8, ppc=6, seed=seed, u_the=0.1, np_slack=3.0, bc="shock",
+                         window=12, u0=0.2)
+    rng = np.random.default_rng(seed)
+    core = 0.02 * rng.standard_normal((6, p.nx, p.ny, p.nz))
+    st.uf[...] = np.pad(core, ((0, 0), (2, 2), (2, 2), (2, 2)), mode="wrap")
+    return p, st
+
+
+@pytest.mark.parametrize("nsteps", [1, 6])
+def test_mixed3d_shock_against_fp64(gpu_lib, nsteps):
+    """The shock boundary on the mixed 3D path: the wall reflection and the injection
+    boundary inside the fused push, before the deposit, as the shock driver orders them;
+    particles within 1e-5 (one step) / 1e-4 (six steps) of the FP64 shock path."""
+    p, st = shock_perturbed(78)
+    m, f = make(p, "mixed"), make(p, "fp64")
+    m.put_state(st)
+    f.put_state(st)
+    m.step(nsteps)
+    f.step(nsteps)
+    sm, sf = m.get_state(), f.get_state()
+    assert sm.np2.sum() == sf.np2.sum() == st.np2.sum()
+    a, b = by_id(sm), by_id(sf)
+    np.testing.assert_array_equal(a[6], b[6])
+    tol = 1e-5 if nsteps == 1 else 1e-4
+    np.testing.assert_allclose(a[:3], b[:3], rtol=0, atol=tol * p.delx)
+    umax = np.abs(b[3:6]).max()
+    np.testing.assert_allclose(a[3:6], b[3:6], rtol=0, atol=tol * umax)
+    assert a[0].min() >= (p.nxgs + 1) * p.delx and a[0].max() <= (p.nxgs + p.window) * p.delx + p.delx
+    em, ef = m.energy(), f.energy()
+    np.testing.assert_allclose(em, ef, rtol=1e-3, atol=1e-6 * ef.sum())
+
+
 def test_mixed3d_rejects_staged_calls_and_odd_tiles(gpu_lib):
     from wumingpic_gb300._lib import WpicError
     p, st = perturbed(74)

@@ -149,7 +149,13 @@ void do_migrate_sort3(wpic_ctx3d* c) {
 
 // the mixed step: fused FP32 push + deposit into the fixed-point current, then the FP64
 // field solve and bookkeeping of the FP64 path
+double shock_xend3(const wpic_ctx3d* c, double u0);
+
 int mixed_step3(wpic_ctx3d* c) {
+  if (c->d.ph.bc == BC_SHOCK) {  // the injection boundary inside the push kernel, in cells from nxgs
+    c->mk.xend = (float)(shock_xend3(c, c->u0) * c->d.ph.d_delx - (double)c->d.g.nxgs);
+    c->mk.u0 = (float)c->u0;
+  }
   mix3_push_deposit(c->d, c->mk, c->ujx, c->pusher == WPIC_PUSH_VAY, c->stream);
   curre_fold3d(c->d, c->stream);
   fast::gkl3d(c->d, c->stream);
@@ -159,7 +165,8 @@ int mixed_step3(wpic_ctx3d* c) {
   fast::efield3d(c->d, c->stream);
   dfield_ghost3d(c->d, c->stream);
   uf_add3d(c->d, c->stream);
-  // periodic wrap in x after the field solve; the walls reflected inside the push kernel
+  // periodic wrap in x after the field solve; walls and the shock boundary acted inside the
+  // push kernel
   if (c->d.ph.bc == BC_PERIODIC) particle_x3d(c->d, c->d.B, c->stream);
   do_migrate_sort3(c);
   return WPIC_OK;
@@ -225,7 +232,6 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
   if (p->bc_kind != WPIC_BC_PERIODIC && p->bc_kind != WPIC_BC_RECONNECTION && p->bc_kind != WPIC_BC_SHOCK)
     return WPIC_BAD_ARGUMENT;
   if (p->bc_kind != WPIC_BC_PERIODIC && nx < 6) return WPIC_BAD_ARGUMENT;
-  if (p->bc_kind == WPIC_BC_SHOCK && p->precision == WPIC_MIXED) return WPIC_BAD_ARGUMENT;
   if ((double)nx * ny * nz > 2.0e9 || (double)p->nsp * ny * nz * p->np >= 2147483647.0) return WPIC_BAD_ARGUMENT;
   wpic_ctx3d* c = new wpic_ctx3d();
   c->prm = *p;

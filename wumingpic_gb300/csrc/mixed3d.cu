@@ -228,17 +228,33 @@ __global__ void __launch_bounds__(T3C, 2) k_mix3_step(Dev3D d, Mix3Const k, long
     split_move(o[0] + ux * dsp, on[0], inc[0], d.err);
     split_move(o[1] + uy * dsp, on[1], inc[1], d.err);
     split_move(o[2] + uz * dsp, on[2], inc[2], d.err);
-    if (d.ph.bc == BC_RECONNECTION) {
-      // the reconnection driver's particle_x before the deposit (3d/proj/reconnection/app.f90:103-108):
-      // reflection about the walls at cells 1 and nx-2 of the grid (nxs+1 and nxe-1), all three
-      // momentum components reversed (3d/proj/reconnection/boundary_reconnection.f90:69-101)
+    if (d.ph.bc != BC_PERIODIC) {
+      // the x boundary before the deposit, in the drivers' order.  Reconnection: particle_x
+      // (3d/proj/reconnection/app.f90:103-108), reflection about the walls at cells 1 and
+      // nx-2 of the grid (nxs+1 and nxe-1), all three momentum components reversed
+      // (3d/proj/reconnection/boundary_reconnection.f90:69-101).  Shock: boundary_shock__injection
+      // (3d/proj/shock/app.f90:112-113, boundary_shock.f90:424-469), reflection about cell wx0 + 1
+      // of the window with the momenta reversed, and beyond xend x -> 2 xend - x,
+      // u_x -> 2 u0 - u_x, u_y and u_z reversed.
       const int gxn = ci + inc[0];
       float X = (float)gxn + on[0];
       bool flip = false;
-      if (gxn < 1) { X = 2.f - X; flip = true; }
-      else if (gxn >= g.nx - 2) { X = 2.f * (float)(g.nx - 2) - X; flip = true; }
+      if (d.ph.bc == BC_RECONNECTION) {
+        if (gxn < 1) { X = 2.f - X; flip = true; }
+        else if (gxn >= g.nx - 2) { X = 2.f * (float)(g.nx - 2) - X; flip = true; }
+        if (flip) { ux = -ux; uy = -uy; uz = -uz; }
+      } else {
+        if (gxn < g.wx0 + 1) {
+          X = 2.f * (float)(g.wx0 + 1) - X;
+          ux = -ux; uy = -uy; uz = -uz;
+          flip = true;
+        } else if (X > k.xend) {
+          X = 2.f * k.xend - X;
+          ux = 2.f * k.u0 - ux; uy = -uy; uz = -uz;
+          flip = true;
+        }
+      }
       if (flip) {
-        ux = -ux; uy = -uy; uz = -uz;
         const float fX = floorf(X);
         on[0] = X - fX;
         inc[0] = (int)fX - ci;

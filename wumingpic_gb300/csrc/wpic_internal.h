@@ -298,6 +298,7 @@ struct Mix3Const {
   float fac1[2], fac2[2], qdd[2];
   float dtdx, c, ic2, vmax;
   int eA, G;
+  float xend, u0;  // shock: the injection boundary in cells from nxgs, and u0 (set every step)
 };
 void mix3_push_deposit(const Dev3D& d, const Mix3Const& k, long long* ujx, bool vay, cudaStream_t s);
 bool mix3_shape_ok(int nx, int ny, int nz);
