@@ -183,3 +183,33 @@ def test_mixed_path_is_bitwise_reproducible(gpu_lib):
     np.testing.assert_array_equal(a.up.view(np.int64), b.up.view(np.int64))
     np.testing.assert_array_equal(a.uf.view(np.int64), b.uf.view(np.int64))
     np.testing.assert_array_equal(ea, eb)
+
+
+@pytest.mark.parametrize("nsteps", [1, 6])
+def test_shock_window_against_fp64(gpu_lib, nsteps):
+    """The shock boundary on the mixed 2D path: the wall reflection at nxs + 1 and the
+    injection boundary at xend inside the fused push, before the deposit (the shock driver
+    calls bc__injection before field__fdtd_i); particles within 1e-5 (one step) / 1e-4 (six
+    steps) of the FP64 shock path, energies within 1e-3."""
+    p, st = small_case(nx=32, ny=16, ppc=8, seed=79, bc="shock", window=24, u0=0.2, u_the=0.1)
+    rng = np.random.default_rng(79)
+    st.uf[...] = np.pad(0.02 * rng.standard_normal((6, p.nx, p.ny)), ((0, 0), (2, 2), (2, 2)), mode="wrap")
+    gm, gd = make(p, "mixed", gpu_lib), make(p, "fp64", gpu_lib)
+    gm.put_state(st)
+    gd.put_state(st)
+    gm.step(nsteps)
+    gd.step(nsteps)
+    a, b = gm.get_state(), gd.get_state()
+    assert a.np2.sum() == b.np2.sum() == st.np2.sum()
+    pa, pb = by_id(a, p), by_id(b, p)
+    assert pa.keys() == pb.keys()
+    xa = np.array([pa[k] for k in sorted(pa)])
+    xb = np.array([pb[k] for k in sorted(pb)])
+    tol = 1e-5 if nsteps == 1 else 1e-4
+    np.testing.assert_allclose(xa[:, :2], xb[:, :2], rtol=0, atol=tol * p.delx)
+    uscale = np.abs(xb[:, 2:]).max()
+    np.testing.assert_allclose(xa[:, 2:], xb[:, 2:], rtol=0, atol=tol * uscale)
+    assert xa[:, 0].min() >= (p.nxgs + 1) * p.delx and xa[:, 0].max() <= (p.nxe + 1) * p.delx
+    em, ed = gm.energy(), gd.energy()
+    np.testing.assert_allclose(em, ed, rtol=1e-3, atol=1e-6 * ed.sum())
+

@@ -570,8 +570,10 @@ def test_shock_steps_with_expanding_window(gpu_lib, precision, rel):
 def test_shock_rejected_where_unsupported(gpu_lib):
     from wumingpic_gb300._lib import WpicError
     p, st, o = shock_setup(94, nx=32, ny=16)
+    g = make_gpu(p, "mixed", gpu_lib)  # the mixed path: inside its fused step only
     with pytest.raises(WpicError):
-        make_gpu(p, "mixed", gpu_lib)
+        g.bc__injection(p.u0)
+    g.close()
     q, _ = small_case(nx=16, ny=12)
     g = make_gpu(q, "fp64", gpu_lib)
     with pytest.raises(WpicError):

@@ -379,8 +379,14 @@ int mix_grow(wpic_ctx* c) {
   return any ? mix_set_layout(c, dep, true) : WPIC_OK;
 }
 
+double shock_xend(const wpic_ctx* c, double u0);
+
 int mixed_step(wpic_ctx* c) {
   Dev2D& d = c->d;
+  if (d.ph.bc == BC_SHOCK) {  // the injection boundary inside the push kernel, in cells from nxgs
+    d.m.k_xend = (float)(shock_xend(c, c->u0) * d.ph.d_delx - (double)d.g.nxgs);
+    d.m.k_u0 = (float)c->u0;
+  }
   stage_begin(c, SG_PUSH);
   mix_push_deposit2d(d, c->tmap, c->pusher == WPIC_PUSH_VAY, c->stream);
   stage_end(c, SG_PUSH, 1);
@@ -448,7 +454,6 @@ int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
   if (!(p->delx > 0) || !(p->delt > 0) || !(p->c > 0)) return WPIC_BAD_ARGUMENT;
   if (p->bc_kind != WPIC_BC_PERIODIC && p->bc_kind != WPIC_BC_RECONNECTION && p->bc_kind != WPIC_BC_SHOCK)
     return WPIC_BAD_ARGUMENT;
-  if (p->bc_kind == WPIC_BC_SHOCK && p->precision == WPIC_MIXED) return WPIC_BAD_ARGUMENT;
   if (p->precision != WPIC_FP64 && p->precision != WPIC_FP64_EXACT && p->precision != WPIC_MIXED)
     return WPIC_BAD_ARGUMENT;
   if (p->precision == WPIC_MIXED && (nx % MIX_TS != 0 || ny % MIX_TS != 0)) return WPIC_BAD_ARGUMENT;
@@ -1339,7 +1344,7 @@ int wpic_set_window(wpic_ctx* c, int nxs, int nxe) {
   const int nxge = c->d.g.nxgs + c->d.g.nx - 1;
   if (nxs < c->d.g.nxgs || nxe > nxge || nxe - nxs < 3) return WPIC_BAD_ARGUMENT;
   const bool full = nxs == c->d.g.nxgs && nxe == nxge;
-  if (!full && (c->mixed || c->d.ph.bc == BC_PERIODIC)) return WPIC_BAD_ARGUMENT;
+  if (!full && (c->d.ph.bc == BC_PERIODIC || (c->mixed && c->d.ph.bc != BC_SHOCK))) return WPIC_BAD_ARGUMENT;
   c->d.g.wx0 = nxs - c->d.g.nxgs;
   c->d.g.wx1 = nxe - c->d.g.nxgs;
   return WPIC_OK;

@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
   const float cl = m.k_c;
   const float ic2 = m.k_ic2;
   const float third = 1.0f / 3.0f;
-  const bool walls = d.ph.bc == BC_RECONNECTION;
+  const bool walls = d.ph.bc != BC_PERIODIC;  // reconnection walls or the shock window: no x wrap
   const int f0 = ly * TT + lx;  // this cell's 3 x 3 centred-field stencil starts here in sfa / sfb
   CellCurrent acc;
   cell_zero(acc);
@@ -353,14 +353,26 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
     if (walls) {
       // reflection about the walls at global cells 1 and nx-2 (nxs+1 and nxe-1 in reference indices),
       // all three momentum components reversed (2d/proj/reconnection/boundary_reconnection.f90:79-91)
+      // the shock window instead: reflection about cell wx0 + 1 with the momenta reversed, and
+      // beyond xend x -> 2 xend - x, u_x -> 2 u0 - u_x, u_y and u_z reversed
+      // (boundary_shock__injection, 2d/proj/shock/boundary_shock.f90:255-297)
       const int gx0 = tx * MIX_TS + lx;
       const int gxn = gx0 + incx;
       float X = (float)gxn + nx_;
+      const bool shock = d.ph.bc == BC_SHOCK;
+      const int lo_wall = shock ? g.wx0 + 1 : 1;
       bool flip = false;
-      if (gxn < 1) { X = 2.f - X; flip = true; }
-      else if (gxn >= g.nx - 2) { X = 2.f * (float)(g.nx - 2) - X; flip = true; }
+      if (gxn < lo_wall) {
+        X = 2.f * (float)lo_wall - X;
+        ux = -ux;
+        flip = true;
+      } else if (shock ? X > m.k_xend : gxn >= g.nx - 2) {
+        X = (shock ? 2.f * m.k_xend : 2.f * (float)(g.nx - 2)) - X;
+        ux = shock ? 2.f * m.k_u0 - ux : -ux;
+        flip = true;
+      }
       if (flip) {
-        ux = -ux; uy = -uy; uz = -uz;
+        uy = -uy; uz = -uz;
         const float fX = floorf(X);
         nx_ = X - fX;
         incx = (int)fX - gx0;

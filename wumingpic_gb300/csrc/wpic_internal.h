@@ -93,6 +93,7 @@ struct Mix2D {
   // per species q/r dt/2, q dt/r, q dx/dt, q; then dt/dx, c, 1/c^2
   float k_fac1[2], k_fac2[2], k_qdd[2], k_q[2];
   float k_dtdx, k_c, k_ic2;
+  float k_xend, k_u0;  // shock: the injection end in cells from nxgs, and u0 (set every step)
   int ntx, nty, ntile, nbin;
   float* P;            // particle layers, MIX_PL words each
   long long* boff;     // [nbin] first layer of each bin
