@@ -112,8 +112,8 @@ int wpic_particle_solv_vay(wpic_ctx* ctx);
 int wpic_set_pusher(wpic_ctx* ctx, int pusher);
 /* the active x window nxs..nxe that the drivers pass to every module call; the shock
  * driver widens it as its box expands (2d/proj/shock/app.f90:276-277, 615-625).  Default:
- * the whole domain; walls only (FP64 paths).  Cells outside the window hold no particles
- * and keep their fields. */
+ * the whole domain; non-periodic contexts only (on the mixed path, shock only).  Cells
+ * outside the window hold no particles and keep their fields. */
 int wpic_set_window(wpic_ctx* ctx, int nxs, int nxe);
 /* the upstream four-velocity u0 of boundary_shock__injection used by the fused step */
 int wpic_set_injection(wpic_ctx* ctx, double u0);
