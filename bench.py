@@ -118,54 +118,108 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(name, threads=None, budget_s=20.0):
-    """Oracle (C++ restatement of the reference, OpenMP) on a bounded sample of the
-    workload: same physics and particles per cell, a 256 x 256 grid, as many steps as
-    fit in about budget_s seconds."""
-    from oracle.oracle import Oracle2D
-    from wumingpic_gb300.loader import Plasma2D, load_weibel2d
-    full = config(name)
-    p = Plasma2D(nx=256, ny=256, ppc=full.ppc, drift=full.drift, u_the=full.u_the, seed=full.seed, np_slack=1.25)
-    st = load_weibel2d(p)
+def host_mem_available():
+    """MemAvailable of this host in bytes (Linux), or None."""
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return None
+
+
+def oracle_grid(full):
+    """The workload's grid if the oracle's state fits this host's memory (up and gp in the
+    reference layout plus the migration buffers: about 2.6 x the up array), else the largest
+    square grid of the same physics and particles per cell that does, and whether it is the
+    full grid."""
+    per_cell = full.np_slack * full.ppc * full.nsp * 6 * 8 * 2.6 / 2  # bytes per cell
+    avail = host_mem_available()
+    n = full.nx
+    while avail is not None and n > 64 and n * n * per_cell * 2 > 0.85 * avail:
+        n //= 2
+    return n, n == full.nx
+
+
+def oracle_state(full, n):
+    """Oracle instance and reference-layout state of the workload's physics on n x n cells,
+    written by the oracle's row-parallel loader (seeded counter hash)."""
+    import ctypes
+    import numpy as np
+    from oracle.oracle import Oracle2D, lib as orc_lib
+    from wumingpic_gb300.loader import Plasma2D, empty_state2d
+    p = Plasma2D(nx=n, ny=n, ppc=full.ppc, drift=full.drift, u_the=full.u_the, seed=full.seed,
+                 np_slack=full.np_slack)
+    st = empty_state2d(p)
+    L = orc_lib()
+    L.orc2d_load_weibel.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 7 + [
+        ctypes.c_double, ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_ulonglong]
+    sd = np.array([p.u_thi, p.u_the])
+    rc = L.orc2d_load_weibel(st.up.ctypes.data, st.cumcnt.ctypes.data, st.np2.ctypes.data, p.nx, p.ny, p.np_cap,
+                             p.nsp, p.ppc, p.nxgs, p.nygs, p.delx, sd.ctypes.data, p.drift, p.drift_axis, p.seed)
+    if rc:
+        raise RuntimeError(f"oracle loader status {rc}")
     q, r = p.charges()
-    threads = threads or os.cpu_count() or 1
+    threads = len(os.sched_getaffinity(0))
     o = Oracle2D(nx=p.nx, ny=p.ny, np_cap=p.np_cap, q=q, r=r, delt=p.delt, gfac=p.gfac, threads=threads)
+    return p, st, o, threads
+
+
+def cpu_baseline(name, budget_s=15.0):
+    """The oracle (C++ restatement of the reference, OpenMP over all host cores) on the
+    workload itself when the host holds it: one untimed step (first touch of the state),
+    then steps until about budget_s seconds have passed."""
+    full = config(name)
+    n, whole = oracle_grid(full)
+    p, st, o, threads = oracle_state(full, n)
+    rc = o.step(st)
+    if rc:
+        raise RuntimeError(f"oracle status {rc}")
     t0 = time.perf_counter()
     steps = 0
-    while True:
+    while steps == 0 or (time.perf_counter() - t0 < budget_s and steps < 50):
         rc = o.step(st)
         if rc:
             raise RuntimeError(f"oracle status {rc}")
         steps += 1
-        if time.perf_counter() - t0 > budget_s or steps >= 200:
-            break
     dt = time.perf_counter() - t0
     return {"value": p.n_particles * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{steps} steps of {p.nx}x{p.ny} cells x {p.ppc} ppc/species ({p.n_particles} particles), "
-                      f"same physics as the workload, {dt:.1f} s, OpenMP threads = host cores"}
+            "sample": f"{steps} steps of {p.nx}^2 x {p.ppc} ppc/sp, {'the workload' if whole else 'reduced grid'}"}
 
 
 def run_reference(args):
-    """The reference arm: the CPU restatement of the reference's step on the host cores."""
+    """The reference arm: the oracle (the CPU restatement of the reference's step, OpenMP over
+    all host cores) runs the workload's own steps: W untimed, then K timed, each one full step
+    of the whole grid.  Rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     name = args.config
     full = config(name)
-    cores = os.cpu_count() or 1
-    vals, base = [], None
-    for k in range(args.warmup + args.steps):
-        b = cpu_baseline(name, threads=cores, budget_s=max(2.0, 90.0 / max(1, args.warmup + args.steps)))
-        if k >= args.warmup:
-            vals.append(b["value"])
-            base = b
-    v = sum(vals) / len(vals)
-    base["value"] = v
+    n, whole = oracle_grid(full)
+    t0 = time.perf_counter()
+    p, st, o, threads = oracle_state(full, n)
+    load_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        if o.step(st):
+            raise RuntimeError("oracle step failed")
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        if o.step(st):
+            raise RuntimeError("oracle step failed")
+    dt = time.perf_counter() - t0
+    v = p.n_particles * args.steps / dt
+    cfg = workload_desc(p, name if whole else f"{name} on a reduced {n}x{n} grid (host memory)")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": full.n_particles / v * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_desc(full, name), "impl": "reference", "cpu_baseline": base,
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full steps of {p.nx}^2 x {p.ppc} ppc/sp after {args.warmup}"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "host_load_s": load_s}
     print(json.dumps(line), flush=True)
 
 
@@ -308,6 +362,40 @@ def time_reconnection(steps, rank, torch, dist, ny=4096, nx=2048):
     return out
 
 
+def time_growth_check(steps, rank, dist, n=512, every=10):
+    """The metric's accuracy qualifier on the workload's physics: drift +-0.3c, u_th 0.1c,
+    64 ppc/species, on n x n cells (the largest grid whose FP64 run saturates within about a
+    minute).  Mixed and FP64 paths run the same `steps` from the same host-loaded state with
+    energy_history every `every` steps (2d/proj/weibel/app.f90:479-545); the growth rate is
+    the linear-phase fit of the magnetic energy (wumingpic_gb300.diagnostics.growth_rate)."""
+    import numpy as np
+    from wumingpic_gb300.diagnostics import energy_history, growth_rate
+    from wumingpic_gb300.loader import Plasma2D, load_weibel2d
+    from wumingpic_gb300.pic2d import Pic2D
+    p = Plasma2D(nx=n, ny=n, ppc=64, drift=0.3, u_the=0.1, seed=20261211 + 7919 * rank, np_slack=3.0)
+    st = load_weibel2d(p)
+    runs, secs = {}, {}
+    for precision in ("mixed", "fp64"):
+        g = Pic2D(p, precision=precision)
+        g.put_state(st)
+        t0 = time.perf_counter()
+        runs[precision] = energy_history(g.step, g.energy, steps, every, p.delt)
+        secs[precision] = time.perf_counter() - t0
+        g.close()
+    t, em = runs["mixed"]
+    _, ed = runs["fp64"]
+    gm, wm, nm = growth_rate(t, em[:, 3])
+    gd, wd, nd = growth_rate(t, ed[:, 3])
+    tot_m, tot_d = em.sum(axis=1), ed.sum(axis=1)
+    return {"workload": f"2D Weibel {n}^2 cells, 64 ppc/species ({p.n_particles} particles), drift +-0.3c, "
+                        f"u_th 0.1c, {steps} steps, energy every {every}",
+            "growth_rate_mixed": gm, "growth_rate_fp64": gd, "growth_rate_rel_err": abs(gm / gd - 1.0),
+            "fit_window_mixed": wm, "fit_window_fp64": wd, "fit_points": [nm, nd],
+            "b_energy_growth": float(ed[:, 3].max() / ed[1, 3]),
+            "energy_max_rel_diff": float(np.max(np.abs(tot_m - tot_d) / np.abs(tot_d))),
+            "run_s": secs}
+
+
 def time_adjoint(steps, every, rank, dist, n=512):
     """The discrete adjoint on the 512^2 Weibel workload (32 ppc/species, drift 0.3c, u_th
     0.05c, 64 Bz seed modes of amplitude ~1e-4): the gradient of the final magnetic energy
@@ -388,6 +476,9 @@ def main():
                     help="timed steps of each path on the Harris-sheet workload (0 = skip)")
     ap.add_argument("--reconnection-grid", default="4096x2048", help="periodic y x walled x cells")
     ap.add_argument("--only-reconnection", action="store_true", help="run the reconnection leg alone")
+    ap.add_argument("--growth-steps", type=int, default=1200,
+                    help="steps of the growth-rate check (mixed against FP64, the workload's physics; 0 = skip)")
+    ap.add_argument("--growth-grid", type=int, default=512, help="cells per edge of the growth-rate check")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--stages", action="store_true", help="print the per-stage breakdown to stderr")
@@ -500,6 +591,10 @@ def main():
     if args.adjoint_steps > 0:
         adjoint = time_adjoint(args.adjoint_steps, args.adjoint_every, rank, dist, n=args.adjoint_grid)
 
+    growth = None
+    if args.growth_steps > 0:
+        growth = time_growth_check(args.growth_steps, rank, dist, n=args.growth_grid)
+
     base = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -515,7 +610,8 @@ def main():
                 "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clocks, "stages_ms_per_step": {k: v[0] / args.steps for k, v in stages.items()},
                 "moments": moments, "fp64_path": fp64, "fp64_3d_path": fp64_3d, "mixed_3d_path": mixed_3d,
-                "reconnection": reconnection, "adjoint": adjoint}
+                "reconnection": reconnection, "adjoint": adjoint, "growth_check": growth}
+        line["summary"] = summary(line)  # last, so that the tail of the line carries it
         print(json.dumps(line), flush=True)
         if args.stages:
             for k, (t, n) in stages.items():
@@ -525,6 +621,43 @@ def main():
                     print(f"fp64  {k:16s} {t:10.3f} ms/step", file=sys.stderr)
     if dist:
         dist.destroy_process_group()
+
+
+def summary(line):
+    """The legs' headline figures in a few hundred characters."""
+    def r(x, n=4):
+        return None if x is None else float(f"{x:.{n}g}")
+    out = {}
+    f = line.get("fp64_path")
+    if f:
+        k = f["kernels"]
+        out["fp64_2d"] = {"value": r(f["value"]), "ms_per_step": r(f["ms_per_step"]),
+                          "mixed_over_fp64": r(f["mixed_over_fp64"]), "fp64_fma_peak_gflops": r(f["fp64_fma_peak_gflops"]),
+                          "k_push2d": {"fp64_pipe_frac": r(k["k_push2d"]["fp64_pipe_frac"], 3),
+                                       "hbm_frac": r(k["k_push2d"]["hbm_frac"], 3)},
+                          "k_deposit2d": {"fp64_pipe_frac": r(k["k_deposit2d"]["fp64_pipe_frac"], 3),
+                                          "hbm_frac": r(k["k_deposit2d"]["hbm_frac"], 3)}}
+    for key, name in (("mixed_3d_path", "mixed_3d"), ("fp64_3d_path", "fp64_3d")):
+        v = line.get(key)
+        if v:
+            out[name] = {"value": r(v["value"]), "ms_per_step": r(v["ms_per_step"])}
+            if "mixed_over_fp64" in v:
+                out[name]["mixed_over_fp64"] = r(v["mixed_over_fp64"])
+    rc = line.get("reconnection")
+    if rc:
+        out["reconnection"] = {"mixed": r(rc["mixed"]["value"]), "fp64": r(rc["fp64"]["value"]),
+                               "mixed_over_fp64": r(rc["mixed_over_fp64"])}
+    a = line.get("adjoint")
+    if a:
+        out["adjoint"] = {"cost_over_forward": r(a["cost_over_forward"], 3), "fd_rel_err": r(a["fd_check"]["rel_err"], 3)}
+        if "mixed_adjoint" in a:
+            out["adjoint"]["mixed_cost_over_mixed_forward"] = r(a["mixed_adjoint"].get("cost_over_mixed_forward"), 3)
+    gc = line.get("growth_check")
+    if gc:
+        out["growth_check"] = {"growth_rate_rel_err": r(gc["growth_rate_rel_err"], 3),
+                               "energy_max_rel_diff": r(gc["energy_max_rel_diff"], 3),
+                               "grid": gc["workload"].split(" cells")[0].replace("2D Weibel ", "")}
+    return out
 
 
 def measure_e2e(g, p, dist=None):
@@ -555,10 +688,12 @@ def measure_e2e(g, p, dist=None):
         _lib.host_unregister(a)
     ms, n = rank_totals(dt * 1e3, int(st.np2.sum()), dist, "cuda")
     dt = ms / 1e3
-    bytes_state = st.up.nbytes + st.uf.nbytes + st.np2.nbytes + st.cumcnt.nbytes
+    # what crosses the link: each row's valid prefix of up (np2 particles of ndim words), uf,
+    # cumcnt and np2 (wpic_put_particles / wpic_get_particles copy the valid prefixes only)
+    bytes_state = int(st.np2.sum()) * p.ndim * 8 + st.uf.nbytes + st.np2.nbytes + st.cumcnt.nbytes
     return {"value": n * steps / dt, "unit": UNIT, "h2d_bytes_per_step": int(bytes_state),
             "d2h_bytes_per_step": int(bytes_state), "steps": steps,
-            "note": "reference-layout host arrays (page-locked with wpic_host_register), full state in "
+            "note": "reference-layout host arrays (page-locked with wpic_host_register), the valid state in "
                     "and out every step"}
 
 

@@ -43,6 +43,9 @@ extern "C" {
 #define WPIC_BAD_ARGUMENT 6
 #define WPIC_CUDA_ERROR 7
 #define WPIC_NOT_INITIALISED 8
+#define WPIC_STAGING_TIMEOUT 9  /* a bulk copy into shared memory did not complete within the kernel's
+                                   bounded wait; the copy may have been left in flight, so finalise
+                                   the context instead of stepping it again */
 
 /* boundary kinds: replace the procedure arguments of field__fdtd_i
  * (2d/common/field.f90:66-89) and the driver's choice of boundary module */
@@ -233,7 +236,10 @@ int wpic_host_unregister(void* ptr);
  * ny * nsp > WPIC_NOALLOC_MAX_ROWS are refused with WPIC_BAD_ARGUMENT.  All calls
  * share the array, so calls that overlap on the GPU race.  The first call on each
  * device looks up the array's device address; make that first call before any
- * stream capture. */
+ * stream capture.  The address is kept for the life of the process: after a
+ * cudaDeviceReset the library's device code is loaded again in a new context, where
+ * the array may lie elsewhere, so do not call this entry point after resetting a
+ * device. */
 #define WPIC_NOALLOC_MAX_ROWS 8192
 int wpic_energy_noalloc(const double* up, const int* np2, const double* uf, int ndim, int np, int nx, int ny,
                         int nsp, const double* r, double c, double* out, void* stream);

@@ -22,16 +22,19 @@ def make(p, precision):
 
 
 def by_id(st):
-    """id -> (x, y, z, ux, uy, uz) over the valid slots"""
-    rows = []
+    """(species, id) -> (x, y, z, ux, uy, uz, id) over the valid slots.  The ids count within a
+    species (ions and electrons share them), and the two paths order a row's particles
+    differently (cell columns against the bucket sort), so rows are matched by species and id."""
+    rows, sp = [], []
     for isp in range(st.np2.shape[2]):
         for k in range(st.np2.shape[1]):
             for j in range(st.np2.shape[0]):
                 n = st.np2[j, k, isp]
                 a = st.up[:, :n, j, k, isp]
                 rows.append(np.vstack([a[:6], a[6].view(np.int64)[None, :].astype(np.float64)]))
+                sp.append(np.full(n, isp))
     a = np.concatenate(rows, axis=1)
-    order = np.argsort(a[6])
+    order = np.lexsort((a[6], np.concatenate(sp)))
     return a[:, order]
 
 

@@ -21,6 +21,7 @@ NONFINITE = 5
 BAD_ARGUMENT = 6
 CUDA_ERROR = 7
 NOT_INITIALISED = 8
+STAGING_TIMEOUT = 9
 
 BC_PERIODIC = 0
 BC_RECONNECTION = 1

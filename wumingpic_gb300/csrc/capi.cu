@@ -153,6 +153,7 @@ int finish(wpic_ctx* c) {
   stage_collect(c);
   const int bits = *c->h_err;
   if (bits) cudaMemsetAsync(c->d.err, 0, sizeof(int), c->stream);
+  if (bits & EB_STAGING_TIMEOUT) return WPIC_STAGING_TIMEOUT;
   if (bits & EB_MOVED_TOO_FAR) return WPIC_MOVED_TOO_FAR;
   if (bits & EB_OUT_OF_RANGE) return WPIC_OUT_OF_RANGE;
   if (bits & EB_CAPACITY) return WPIC_CAPACITY;
@@ -1623,6 +1624,7 @@ const char* wpic_status_string(int s) {
     case WPIC_BAD_ARGUMENT: return "bad argument";
     case WPIC_CUDA_ERROR: return "CUDA error";
     case WPIC_NOT_INITIALISED: return "context not initialised";
+    case WPIC_STAGING_TIMEOUT: return "bulk copy into shared memory timed out (finalise the context)";
     default: return "unknown status";
   }
 }

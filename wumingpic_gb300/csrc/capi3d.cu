@@ -28,7 +28,12 @@ struct wpic_ctx3d {
   double* mom = nullptr;         // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nzs-1:nze+1, nsp), on first use
   bool mixed = false;            // FP32 push/deposit on split positions (fused step only)
   Mix3Const mk{};
-  long long* ujx = nullptr;      // global fixed-point current of the mixed step
+  alignas(128) unsigned char tmap[128];  // CUtensorMap of uf (mixed path TMA tile loads)
+  // mixed path: the particle layers (reallocated when bins grow) and the host copy of the layout
+  float* mixP = nullptr;
+  std::vector<int> h_dep;
+  int* h_grow = nullptr;         // pinned mirror of the grow flag
+  double mix_vmax = 0.0;         // largest contribution of one particle to one node of the deposit
 };
 
 namespace {
@@ -76,6 +81,7 @@ int finish3(wpic_ctx3d* c) {
   if (e != cudaSuccess) return cuda_status3(e);
   const int bits = *c->h_err;
   if (bits) cudaMemsetAsync(c->d.err, 0, sizeof(int), c->stream);
+  if (bits & EB_STAGING_TIMEOUT) return WPIC_STAGING_TIMEOUT;
   if (bits & EB_MOVED_TOO_FAR) return WPIC_MOVED_TOO_FAR;
   if (bits & EB_OUT_OF_RANGE) return WPIC_OUT_OF_RANGE;
   if (bits & EB_CAPACITY) return WPIC_CAPACITY;
@@ -147,28 +153,118 @@ void do_migrate_sort3(wpic_ctx3d* c) {
   cudaMemcpyAsync(c->d.np2, c->d.np2new, sizeof(int) * c->d.nrow, cudaMemcpyDeviceToDevice, c->stream);
 }
 
-// the mixed step: fused FP32 push + deposit into the fixed-point current, then the FP64
-// field solve and bookkeeping of the FP64 path
+// Fixed-point scales of the mixed deposit for columns of at most maxdep slots.  One particle adds
+// at most vmax = max |q| dx/dt to a node; a thread flushes the sum of up to 32 particles at once
+// (|v s1| <= 2^21 keeps the magic-number rounding exact), at most 125 * nsp * maxdep particles
+// reach a node in one tile pass (|sum hi| < 2^30), and each of them adds at most 2^14 to the low
+// plane.  The current is rebuilt every step, so the scales may change with the layout.
+int mix3_set_scales(wpic_ctx3d* c, int maxdep) {
+  Mix3D& m = c->d.m;
+  const double vmax = c->mix_vmax;
+  const double reach = 125.0 * c->prm.nsp * maxdep;
+  double s1 = std::ldexp(1.0, 21) / (32.0 * vmax);
+  const double lim = std::ldexp(1.0, 30) / (reach * vmax);
+  if (lim < s1) s1 = lim;
+  s1 = std::ldexp(1.0, (int)std::floor(std::log2(s1)));
+  if (!(s1 > 0.0) || s1 > std::ldexp(1.0, 100) || (reach + 27.0) * 16384.0 >= std::ldexp(1.0, 31))
+    return WPIC_CAPACITY;
+  m.fx_s1 = (float)s1;
+  m.fx_is1f = (float)(1.0 / s1);
+  m.fx_s2 = (float)(s1 * 32768.0);
+  m.fx_is2 = 1.0 / (s1 * 32768.0);
+  return WPIC_OK;
+}
+
+// Lays the mixed-path bins out with the given depths.  keep = true copies the columns of the
+// current layout (counts unchanged); otherwise the new layout starts empty.
+int mix3_set_layout(wpic_ctx3d* c, const std::vector<int>& dep, bool keep) {
+  Mix3D& m = c->d.m;
+  std::vector<long long> off(m.nbin);
+  long long layers = 0;
+  int maxdep = 1;
+  for (int b = 0; b < m.nbin; ++b) {
+    if (dep[b] < 1 || dep[b] > MIX_MAX_DEPTH) return WPIC_CAPACITY;
+    off[b] = layers;
+    layers += dep[b];
+    maxdep = std::max(maxdep, dep[b]);
+  }
+  if (int st = mix3_set_scales(c, maxdep)) return st;
+  if (!keep && c->mixP) {
+    CK3(cudaStreamSynchronize(c->stream));
+    cudaFree(c->mixP);
+    c->mixP = nullptr;
+  }
+  float* np_ = nullptr;
+  CK3(cudaMalloc(&np_, (size_t)layers * M3_PL * sizeof(float)));
+  long long* old_off = nullptr;
+  const float* old_P = c->mixP;
+  if (keep && old_P) {
+    CK3(cudaMalloc(&old_off, sizeof(long long) * m.nbin));
+    CK3(cudaMemcpyAsync(old_off, m.boff, sizeof(long long) * m.nbin, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  CK3(cudaMemcpyAsync(m.boff, off.data(), sizeof(long long) * m.nbin, cudaMemcpyHostToDevice, c->stream));
+  CK3(cudaMemcpyAsync(m.bdep, dep.data(), sizeof(int) * m.nbin, cudaMemcpyHostToDevice, c->stream));
+  m.P = np_;
+  if (keep && old_P) mix3_relayout(c->d, old_P, old_off, c->stream);
+  CK3(cudaStreamSynchronize(c->stream));  // host vectors and the old buffers are released below
+  if (old_off) cudaFree(old_off);
+  if (keep && old_P) cudaFree(c->mixP);
+  c->mixP = np_;
+  c->h_dep = dep;
+  return WPIC_OK;
+}
+
+// grows the bins whose columns came within 1/8 of full in the last step to 1.5 x their need
+int mix3_grow(wpic_ctx3d* c) {
+  Mix3D& m = c->d.m;
+  std::vector<int> need(m.nbin);
+  CK3(cudaMemcpyAsync(need.data(), m.bneed, sizeof(int) * m.nbin, cudaMemcpyDeviceToHost, c->stream));
+  CK3(cudaMemsetAsync(m.grow, 0, sizeof(int), c->stream));
+  CK3(cudaStreamSynchronize(c->stream));
+  *c->h_grow = 0;
+  std::vector<int> dep = c->h_dep;
+  bool any = false;
+  for (int b = 0; b < m.nbin; ++b)
+    if (8LL * need[b] > 7LL * dep[b]) {
+      const long long nd = ((long long)std::ceil(1.5 * need[b] + 8.0) + 7) & ~7LL;
+      dep[b] = (int)(nd > MIX_MAX_DEPTH ? MIX_MAX_DEPTH : nd);
+      any = true;
+    }
+  return any ? mix3_set_layout(c, dep, true) : WPIC_OK;
+}
+
 double shock_xend3(const wpic_ctx3d* c, double u0);
 
+// the mixed step: fused FP32 push + deposit + compaction, the arrivals, then the FP64 field solve
 int mixed_step3(wpic_ctx3d* c) {
-  if (c->d.ph.bc == BC_SHOCK) {  // the injection boundary inside the push kernel, in cells from nxgs
-    c->mk.xend = (float)(shock_xend3(c, c->u0) * c->d.ph.d_delx - (double)c->d.g.nxgs);
+  Dev3D& d = c->d;
+  if (d.ph.bc == BC_SHOCK) {  // the injection end in cells from nxgs, split into cell + FP32 fraction
+    const double xe = shock_xend3(c, c->u0) * d.ph.d_delx - (double)d.g.nxgs;
+    const double fl = std::floor(xe);
+    c->mk.xend_cell = (int)fl;
+    c->mk.xend_frac = (float)(xe - fl);
+    if (c->mk.xend_frac >= 1.f) {
+      c->mk.xend_frac = 0.f;
+      c->mk.xend_cell += 1;
+    }
     c->mk.u0 = (float)c->u0;
   }
-  mix3_push_deposit(c->d, c->mk, c->ujx, c->pusher == WPIC_PUSH_VAY, c->stream);
-  curre_fold3d(c->d, c->stream);
-  fast::gkl3d(c->d, c->stream);
+  mix3_push(d, c->mk, c->tmap, c->pusher == WPIC_PUSH_VAY, c->stream);
+  // the arrivals join their columns right away, so the particle state is whole again before the
+  // field solve (which does not read particles) can return an error
+  mix3_arrive(d, c->stream);
+  CK3(cudaMemcpyAsync(c->h_grow, d.m.grow, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  mix3_fix(d, c->stream);
+  curre_fold3d(d, c->stream);
+  fast::gkl3d(d, c->stream);
   int st = do_cg3(c);
   if (st) return st;
-  dfield_ghost3d(c->d, c->stream);
-  fast::efield3d(c->d, c->stream);
-  dfield_ghost3d(c->d, c->stream);
-  uf_add3d(c->d, c->stream);
-  // periodic wrap in x after the field solve; walls and the shock boundary acted inside the
-  // push kernel
-  if (c->d.ph.bc == BC_PERIODIC) particle_x3d(c->d, c->d.B, c->stream);
-  do_migrate_sort3(c);
+  dfield_ghost3d(d, c->stream);
+  fast::efield3d(d, c->stream);
+  dfield_ghost3d(d, c->stream);
+  uf_add3d(d, c->stream);
+  // the CG's host checks synchronised the stream, so the grow flag of this step is in h_grow
+  if (*c->h_grow) return mix3_grow(c);
   return WPIC_OK;
 }
 
@@ -285,15 +381,17 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
       k.qdd[s] = on ? (float)(p->q[s] * p->delx * (1.0 / p->delt)) : 0.f;
       if (on) vmax = std::max(vmax, std::fabs(p->q[s] * p->delx / p->delt));
     }
-    vmax = std::max(vmax, 1e-30);
     k.dtdx = (float)(p->delt / p->delx);
     k.c = (float)p->c;
     k.ic2 = (float)(1.0 / (p->c * p->c));
-    k.vmax = (float)(vmax * (1.0 + 1e-6));
-    // a contribution is at most |q| dx / dt; a node's sum over all particles at most slots times that
-    k.eA = std::ilogb(4194304.0 / (double)k.vmax);
-    const double slots = (double)d.nrow * (double)d.cap;
-    k.G = std::ilogb(4611686018427387904.0 / (slots * (double)k.vmax));
+    // a contribution to one node is at most |q| dx / dt (the Esirkepov weights are at most 1)
+    c->mix_vmax = std::max(vmax, 1e-300) * (1.0 + 1e-6);
+    Mix3D& m = d.m;
+    m.ntx = nx / M3_TX;
+    m.nty = ny / M3_TY;
+    m.ntz = nz / M3_TZ;
+    m.ntile = m.ntx * m.nty * m.ntz;
+    m.nbin = m.ntile * p->nsp;
   }
   d.nred = (int)std::min<size_t>(1216, (d.g.ncell + CG_THREADS_HOST - 1) / CG_THREADS_HOST);
   if (d.nred < 1) d.nred = 1;
@@ -307,10 +405,11 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
     }
     c->own_stream = true;
   }
-  const size_t slots = (size_t)d.nrow * d.cap;
+  // the mixed path keeps its particles in the bins: no FP64 particle arrays or migration scratch
+  const size_t slots = c->mixed ? 0 : (size_t)d.nrow * d.cap;
   int st = WPIC_OK;
   do {
-    if ((st = alloc_parts3(c, &d.A, slots)) || (st = alloc_parts3(c, &d.B, slots))) break;
+    if (!c->mixed && ((st = alloc_parts3(c, &d.A, slots)) || (st = alloc_parts3(c, &d.B, slots)))) break;
     if ((st = dalloc3(c, &d.cc, (size_t)d.nrow * (nx + 1))) || (st = dalloc3(c, &d.np2, d.nrow)) ||
         (st = dalloc3(c, &d.np2new, d.nrow)))
       break;
@@ -318,8 +417,18 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
         (st = dalloc3(c, &d.uj, 3 * d.g.fvol)) || (st = dalloc3(c, &d.gkl, 3 * d.g.ncell)))
       break;
     if (c->mixed) {
-      if (mix3_setup() != 0) { st = WPIC_CUDA_ERROR; break; }
-      if ((st = dalloc3(c, &c->ujx, 3 * d.g.fvol))) break;
+      Mix3D& m = d.m;
+      if ((st = dalloc3(c, &m.boff, (size_t)m.nbin)) || (st = dalloc3(c, &m.bdep, (size_t)m.nbin)) ||
+          (st = dalloc3(c, &m.cnt, (size_t)m.nbin * M3_TC)) || (st = dalloc3(c, &m.ccnt, (size_t)m.nbin * M3_TC)) ||
+          (st = dalloc3(c, &m.acnt, (size_t)m.nbin * M3_TC)) || (st = dalloc3(c, &m.bneed, (size_t)m.nbin)) ||
+          (st = dalloc3(c, &m.grow, 1)) || (st = dalloc3(c, &m.ujx, 3 * d.g.fvol)))
+        break;
+      if (cudaMallocHost(&c->h_grow, sizeof(int)) != cudaSuccess) { st = WPIC_CUDA_ERROR; break; }
+      *c->h_grow = 0;
+      if (mix3_setup(d, c->tmap) != 0) { st = WPIC_CUDA_ERROR; break; }
+      // an empty layout of shallow columns: wpic3d_put_particles and wpic3d_load_weibel lay the
+      // bins out for the particles they bring
+      if ((st = mix3_set_layout(c, std::vector<int>(m.nbin, 8), false))) break;
     } else if ((st = dalloc3(c, &d.cellJ, (size_t)375 * d.g.ncell))) {
       break;
     }
@@ -330,9 +439,10 @@ int wpic3d_init(wpic_ctx3d** out, const wpic_params3d* p, void* cuda_stream) {
     if ((st = dalloc3(c, &d.partials, (size_t)3 * d.nred * 2)) || (st = dalloc3(c, &d.cg, 3)) ||
         (st = dalloc3(c, &d.err, 1)) || (st = dalloc3(c, &d.red_out, 8)))
       break;
-    if ((st = dalloc3(c, &d.mig, slots)) || (st = dalloc3(c, &d.glist, slots)) ||
-        (st = dalloc3(c, &d.gcnt, (size_t)d.nrow * 8)) || (st = dalloc3(c, &d.goff, (size_t)d.nrow * 8)) ||
-        (st = dalloc3(c, &d.tlist, slots)) || (st = dalloc3(c, &d.slist, slots)) || (st = dalloc3(c, &d.map, slots)))
+    if (!c->mixed &&
+        ((st = dalloc3(c, &d.mig, slots)) || (st = dalloc3(c, &d.glist, slots)) ||
+         (st = dalloc3(c, &d.gcnt, (size_t)d.nrow * 8)) || (st = dalloc3(c, &d.goff, (size_t)d.nrow * 8)) ||
+         (st = dalloc3(c, &d.tlist, slots)) || (st = dalloc3(c, &d.slist, slots)) || (st = dalloc3(c, &d.map, slots))))
       break;
     if (cudaMallocHost(&c->h_cg, 3 * sizeof(CGState)) != cudaSuccess) { st = WPIC_CUDA_ERROR; break; }
     if (cudaMallocHost(&c->h_err, sizeof(int)) != cudaSuccess) { st = WPIC_CUDA_ERROR; break; }
@@ -352,6 +462,8 @@ int wpic3d_finalize(wpic_ctx3d* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (void* p : c->allocs) cudaFree(p);
   if (c->staging) cudaFree(c->staging);
+  if (c->mixP) cudaFree(c->mixP);
+  if (c->h_grow) cudaFreeHost(c->h_grow);
   if (c->h_cg) cudaFreeHost(c->h_cg);
   if (c->h_err) cudaFreeHost(c->h_err);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -373,10 +485,41 @@ int wpic3d_put_particles(wpic_ctx3d* c, int which, const double* up, const int* 
         if (cc[i + 1] < cc[i]) return WPIC_BAD_ARGUMENT;
     }
   }
+  if (c->mixed && which != 0) return WPIC_BAD_ARGUMENT;
   CK3(cudaMemcpyAsync(d.np2, np2, sizeof(int) * d.nrow, cudaMemcpyHostToDevice, c->stream));
   if (which == 0)
     CK3(cudaMemcpyAsync(d.cc, cumcnt, sizeof(int) * (size_t)d.nrow * (nx + 1), cudaMemcpyHostToDevice, c->stream));
   const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
+  if (c->mixed) {
+    // lay the bins out for these particles unless every bin already has the room: each bin's
+    // depth from its fullest cell, kept while every bin keeps 40 % of its depth free
+    Mix3D& m = d.m;
+    mix3_binmax(d, c->stream);
+    std::vector<int> mx(m.nbin);
+    CK3(cudaMemcpyAsync(mx.data(), m.bneed, sizeof(int) * m.nbin, cudaMemcpyDeviceToHost, c->stream));
+    CK3(cudaStreamSynchronize(c->stream));
+    const double cdx = c->prm.c * c->prm.delt / c->prm.delx;
+    std::vector<int> dep(m.nbin);
+    bool fits = (int)c->h_dep.size() == m.nbin;
+    for (int b = 0; b < m.nbin; ++b) {
+      dep[b] = mix3_initial_depth(mx[b], cdx);
+      if (fits && 5LL * mx[b] > 3LL * c->h_dep[b]) fits = false;
+    }
+    int st = fits ? WPIC_OK : mix3_set_layout(c, dep, false);
+    if (st) return st;
+    CK3(cudaMemsetAsync(m.acnt, 0, sizeof(int) * (size_t)m.nbin * M3_TC, c->stream));
+    // one chunk = the 4 ny rows of species isp and z layers 4 tz .. 4 tz + 3 (contiguous in up)
+    const size_t chunk_rows = (size_t)M3_TZ * d.g.ny;
+    if ((st = ensure_staging3(c, chunk_rows * row_bytes))) return st;
+    for (int isp = 0; isp < c->prm.nsp; ++isp)
+      for (int tz = 0; tz < m.ntz; ++tz) {
+        const size_t r0 = ((size_t)isp * d.g.nz + (size_t)tz * M3_TZ) * d.g.ny;
+        CK3(cudaMemcpyAsync(c->staging, up + r0 * ndim * nph, chunk_rows * row_bytes, cudaMemcpyHostToDevice,
+                            c->stream));
+        mix3_put(d, c->staging, ndim, nph, isp, tz, c->stream);
+      }
+    return finish3(c);
+  }
   size_t rows_per = ((size_t)1 << 30) / row_bytes;
   if (rows_per < 1) rows_per = 1;
   if (rows_per > (size_t)d.nrow) rows_per = d.nrow;
@@ -396,6 +539,31 @@ int wpic3d_get_particles(wpic_ctx3d* c, int which, double* up, int* np2, int* cu
   if (!up || (which != 0 && which != 1)) return WPIC_BAD_ARGUMENT;
   Dev3D& d = c->d;
   const int nx = d.g.nx, ndim = c->prm.ndim, nph = c->prm.np;
+  if (c->mixed) {
+    if (which != 0) return WPIC_BAD_ARGUMENT;
+    mix3_count_rows(d, c->stream);
+    std::vector<int> h(d.nrow);
+    CK3(cudaMemcpyAsync(h.data(), d.np2, sizeof(int) * d.nrow, cudaMemcpyDeviceToHost, c->stream));
+    if (cumcnt)
+      CK3(cudaMemcpyAsync(cumcnt, d.cc, sizeof(int) * (size_t)d.nrow * (nx + 1), cudaMemcpyDeviceToHost, c->stream));
+    CK3(cudaStreamSynchronize(c->stream));
+    for (int r = 0; r < d.nrow; ++r)
+      if (h[r] > nph) return WPIC_CAPACITY;
+    if (np2) std::copy(h.begin(), h.end(), np2);
+    const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
+    const size_t chunk_rows = (size_t)M3_TZ * d.g.ny;
+    int st = ensure_staging3(c, chunk_rows * row_bytes);
+    if (st) return st;
+    for (int isp = 0; isp < c->prm.nsp; ++isp)
+      for (int tz = 0; tz < d.m.ntz; ++tz) {
+        const size_t r0 = ((size_t)isp * d.g.nz + (size_t)tz * M3_TZ) * d.g.ny;
+        CK3(cudaMemsetAsync(c->staging, 0, chunk_rows * row_bytes, c->stream));
+        mix3_get(d, c->staging, ndim, nph, isp, tz, c->stream);
+        CK3(cudaMemcpyAsync(up + r0 * ndim * nph, c->staging, chunk_rows * row_bytes, cudaMemcpyDeviceToHost,
+                            c->stream));
+      }
+    return finish3(c);
+  }
   if (np2) CK3(cudaMemcpyAsync(np2, d.np2, sizeof(int) * d.nrow, cudaMemcpyDeviceToHost, c->stream));
   if (cumcnt && which == 0)
     CK3(cudaMemcpyAsync(cumcnt, d.cc, sizeof(int) * (size_t)d.nrow * (nx + 1), cudaMemcpyDeviceToHost, c->stream));
@@ -461,6 +629,7 @@ int wpic3d_ele_cur(wpic_ctx3d* c) {
 
 int wpic3d_bc_particle_x(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
   if (c->d.ph.bc == BC_SHOCK) return WPIC_BAD_ARGUMENT;  // boundary_shock has no particle_x
   particle_x3d(c->d, c->d.B, c->stream);
   return finish3(c);
@@ -494,6 +663,7 @@ int wpic3d_bc_injection(wpic_ctx3d* c, double u0) {
 // bc__particle_yz on gp (B) in place: the post-migration order is gathered through map = slist
 int wpic3d_bc_particle_yz(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
   Dev3D& d = c->d;
   migrate_scan3d(d, d.B, c->stream);
   migrate_plan3d(d, c->stream);
@@ -514,6 +684,7 @@ int wpic3d_bc_particle_yz(wpic_ctx3d* c) {
 // sort__bucket: gp (B) -> up (A) with cumcnt
 int wpic3d_sort_bucket(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
   Dev3D& d = c->d;
   sort_rank3d(d, d.B, nullptr, c->stream);
   gather3d(d, d.B, d.A, d.map, d.np2, c->stream);
@@ -534,7 +705,8 @@ int wpic3d_step(wpic_ctx3d* c, int nsteps) {
 int wpic3d_energy(wpic_ctx3d* c, double* out) {
   if (!c) return WPIC_NOT_INITIALISED;
   if (!out) return WPIC_BAD_ARGUMENT;
-  FP3(energy3d, c->d, c->stream);
+  if (c->mixed) mix3_energy(c->d, c->stream);
+  else FP3(energy3d, c->d, c->stream);
   double h[4];
   CK3(cudaMemcpyAsync(h, c->d.red_out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   int st = finish3(c);
@@ -563,13 +735,14 @@ int copy_mom3(wpic_ctx3d* c, double* out) {
 
 int wpic3d_mom_calc_accl(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path computes moments with wpic3d_moments
   FP3(mom_accl3d, c->d, c->stream);
   return finish3(c);
 }
 
 int wpic3d_mom_calc_nvt(wpic_ctx3d* c, int from_gp) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (from_gp != 0 && from_gp != 1) return WPIC_BAD_ARGUMENT;
+  if (c->mixed || (from_gp != 0 && from_gp != 1)) return WPIC_BAD_ARGUMENT;
   int st = ensure_mom3(c);
   if (st) return st;
   FP3(mom_nvt3d, c->d, from_gp ? c->d.B : c->d.A, c->mom, c->stream);
@@ -596,7 +769,7 @@ int wpic3d_moments(wpic_ctx3d* c, double* mom) {
   int st = ensure_mom3(c);
   if (st) return st;
   if (c->mixed) {
-    mix3_moments(c->d, c->mk, c->mom, c->stream);
+    mix3_moments(c->d, c->mk, c->mom, c->stream);  // from the bins: no gp is written
   } else {
     FP3(mom_accl3d, c->d, c->stream);
     FP3(mom_nvt3d, c->d, c->d.B, c->mom, c->stream);
@@ -625,8 +798,16 @@ int wpic3d_load_weibel(wpic_ctx3d* c, int ppc, uint64_t seed, double drift, int 
   if (!c) return WPIC_NOT_INITIALISED;
   Dev3D& d = c->d;
   if (drift_axis < 0 || drift_axis > 2 || ppc < 1) return WPIC_BAD_ARGUMENT;
-  if ((long long)ppc * d.g.nx > d.cap) return WPIC_CAPACITY;
-  load_weibel3d_ppc(d, ppc, seed, drift, drift_axis, u_thi, u_the, c->stream);
+  if (c->mixed) {
+    const int dep = mix3_initial_depth(ppc, c->prm.c * c->prm.delt / c->prm.delx);
+    int st = mix3_set_layout(c, std::vector<int>(d.m.nbin, dep), false);
+    if (st) return st;
+    CK3(cudaMemsetAsync(d.m.acnt, 0, sizeof(int) * (size_t)d.m.nbin * M3_TC, c->stream));
+    mix3_load_weibel(d, ppc, seed, drift, drift_axis, u_thi, u_the, c->stream);
+  } else {
+    if ((long long)ppc * d.g.nx > d.cap) return WPIC_CAPACITY;
+    load_weibel3d_ppc(d, ppc, seed, drift, drift_axis, u_thi, u_the, c->stream);
+  }
   CK3(cudaMemsetAsync(d.uf, 0, 6 * d.g.fvol * sizeof(double), c->stream));
   CK3(cudaMemsetAsync(d.df, 0, 6 * d.g.fvol * sizeof(double), c->stream));
   CK3(cudaMemsetAsync(d.uj, 0, 3 * d.g.fvol * sizeof(double), c->stream));
@@ -635,8 +816,10 @@ int wpic3d_load_weibel(wpic_ctx3d* c, int ppc, uint64_t seed, double drift, int 
 
 long long wpic3d_num_particles(wpic_ctx3d* c) {
   if (!c) return -1;
-  std::vector<int> h(c->d.nrow);
-  if (cudaMemcpyAsync(h.data(), c->d.np2, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+  const bool mx = c->mixed;
+  std::vector<int> h(mx ? (size_t)c->d.m.nbin * M3_TC : (size_t)c->d.nrow);
+  if (cudaMemcpyAsync(h.data(), mx ? c->d.m.cnt : c->d.np2, sizeof(int) * h.size(), cudaMemcpyDeviceToHost,
+                      c->stream) != cudaSuccess)
     return -1;
   cudaStreamSynchronize(c->stream);
   long long n = 0;

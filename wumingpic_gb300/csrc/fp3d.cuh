@@ -829,6 +829,11 @@ __global__ void __launch_bounds__(CG_THREADS) k_energy3d_fin(Dev3D d) {
 void energy3d(const Dev3D& d, cudaStream_t s) {
   cudaMemsetAsync(d.partials, 0, sizeof(double) * 2 * 3 * (size_t)d.nred, s);
   k_energy3d_kin<<<dim3(d.nred, d.ph.nsp), CG_THREADS, 0, s>>>(d);
+  energy_fields_fin3d(d, s);
+}
+
+// the field sums and the final reduction, after the kinetic partials are in place
+void energy_fields_fin3d(const Dev3D& d, cudaStream_t s) {
   k_energy3d_fld<<<d.nred, CG_THREADS, 0, s>>>(d);
   k_energy3d_fin<<<1, CG_THREADS, 0, s>>>(d);
 }

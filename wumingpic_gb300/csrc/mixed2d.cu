@@ -231,9 +231,11 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
     mbar_expect_tx(&bar, (unsigned)(6 * TW * TW * sizeof(double)));
     tma_load_3d(&suf[0][0][0], &tm, tx * MIX_TS, ty * MIX_TS, 0, &bar);
   }
-  if (!mbar_wait_bounded(&bar)) {
-    atomicOr(d.err, EB_OUT_OF_RANGE);
-    mbar_wait_bounded(&bar);  // second bounded wait for the copy in flight
+  // every thread waits (bounded) for the tile; the CTA gives up together if any wait ran out
+  const bool staged = mbar_wait_bounded(&bar);
+  if (!__syncthreads_and(staged)) {
+    if (threadIdx.x == 0) atomicOr(d.err, EB_STAGING_TIMEOUT);
+    if (!staged) mbar_wait_bounded(&bar);  // second bounded wait for the copy in flight
     cp_async_wait<0>();
     return;
   }
@@ -880,11 +882,11 @@ __global__ void k_mix_load(Dev2D d, int ppc, unsigned long long seed, double dri
                            double u_the) {
   const Mix2D& m = d.m;
   const Grid2D g = d.g;
-  const int bin = blockIdx.y;
+  const int bin = blockIdx.x;
   const int nsp = d.ph.nsp;
   const int tile = bin / nsp, isp = bin - tile * nsp;
   const int tx = tile % m.ntx, ty = tile / m.ntx;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;  // = kk * 256 + c
+  const int s = blockIdx.y * blockDim.x + threadIdx.x;  // = kk * 256 + c
   const int c = s % MIX_TC, kk = s / MIX_TC;
   const int dep = m.bdep[bin];
   if (kk == 0) m.cnt[bin * MIX_TC + c] = ppc < dep ? ppc : dep;
@@ -918,7 +920,7 @@ __global__ void k_mix_load(Dev2D d, int ppc, unsigned long long seed, double dri
 
 void mix_load_weibel2d(const Dev2D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
                        double u_thi, double u_the, cudaStream_t s) {
-  dim3 grid((MIX_TC * ppc + 255) / 256, d.m.nbin);
+  dim3 grid(d.m.nbin, (MIX_TC * ppc + 255) / 256);  // bins on x (the y extent is limited to 65535)
   k_mix_load<<<grid, 256, 0, s>>>(d, ppc, seed, drift, drift_axis, u_thi, u_the);
 }
 

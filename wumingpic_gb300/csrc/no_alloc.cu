@@ -35,6 +35,9 @@ void* g_scratch_addr[kMaxDevices] = {};
 std::mutex g_setup_mutex;
 
 // Device address of the scratch array for the current device, looked up once per device.
+// The cached address belongs to the context that was current at the look-up: after a
+// cudaDeviceReset the module is loaded again in a new context and the array may move, so
+// the entry point is not for use after a device reset (the header says so).
 int scratch_address(double** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return WPIC_CUDA_ERROR;

@@ -33,6 +33,9 @@ enum ErrBit : int {
   EB_OUT_OF_RANGE = 2,
   EB_MOVED_TOO_FAR = 4,
   EB_CG = 8,
+  // a bulk (TMA) copy into shared memory did not complete within the kernel's wait limit;
+  // the copy may still be in flight when the CTA returns, so the context is finished
+  EB_STAGING_TIMEOUT = 16,
 };
 
 enum Bc : int { BC_PERIODIC = 0, BC_RECONNECTION = 1, BC_SHOCK = 2 };
@@ -250,6 +253,42 @@ struct Parts3D {
   long long* id;
 };
 
+// ---- mixed-precision particle storage (3D) ----
+// The 2D scheme in three dimensions: bins of one 8 x 8 x 4-cell tile and one species,
+// bin = tile * nsp + isp, tile = (tz * nty + ty) * ntx + tx.  Inside a bin every cell
+// c = (lz * 8 + ly) * 8 + lx owns a column of bdep[bin] slots; slot (k, c) lies in layer
+// boff[bin] + k.  Position = the column's cell plus three FP32 offsets in [0, 1); momenta FP32;
+// 64-bit id; each 256-slot layer holds nine 32-bit planes (ox, oy, oz, ux, uy, uz, id low word,
+// id high word, arrival key) one after another.  The push compacts each column in place and
+// writes the particles that change cell to the top of their new column; the arrival kernel moves
+// them, in key order, to just above the stayers; bins grow when their columns come close to full.
+constexpr int M3_TX = 8, M3_TY = 8, M3_TZ = 4;
+constexpr int M3_TC = M3_TX * M3_TY * M3_TZ;  // cells per tile = threads of the tile kernels
+constexpr int M3_OX = 0, M3_OY = M3_TC, M3_OZ = 2 * M3_TC, M3_UX = 3 * M3_TC, M3_UY = 4 * M3_TC,
+              M3_UZ = 5 * M3_TC, M3_IDLO = 6 * M3_TC, M3_IDHI = 7 * M3_TC, M3_KEY = 8 * M3_TC;
+constexpr int M3_PL = 9 * M3_TC;  // 32-bit words per layer
+
+struct Mix3D {
+  // fixed-point current: v = hi / s1 + lo / s2 (int32 planes in shared memory), global sums in
+  // units of 1 / s2 (int64)
+  float fx_s1, fx_s2, fx_is1f;
+  double fx_is2;
+  int ntx, nty, ntz, ntile, nbin;
+  float* P;            // particle layers, M3_PL words each
+  long long* boff;     // [nbin] first layer of each bin
+  int* bdep;           // [nbin] slots per cell column
+  int* cnt;            // [nbin][256] particles per column (the push's input count)
+  int* ccnt;           // [nbin][256] stayers after the push's compaction
+  int* acnt;           // [nbin][256] arrivals written by the push (zero between steps)
+  int* bneed;          // [nbin] largest count + 2 x arrivals over a bin's columns in the last step
+  int* grow;           // nonzero when some bin's need passed 7/8 of its depth
+  unsigned long long* ujx;  // [3][fvol] current in fixed point (units 1/fx_s2), summed exactly
+};
+
+__device__ inline float* mix3_slot(const Mix3D& m, int bin, int k, int c) {
+  return m.P + ((size_t)m.boff[bin] + k) * M3_PL + c;
+}
+
 struct Dev3D {
   Grid3D g;
   Phys ph;
@@ -273,6 +312,7 @@ struct Dev3D {
   int *tlist, *slist, *map;
   int* err;
   double* red_out;
+  Mix3D m;          // the mixed path's particle bins (the FP64 particle arrays are then unused)
 };
 
 #define WPIC_DECLARE_FP3_LAUNCHERS                       \
@@ -288,22 +328,38 @@ struct Dev3D {
   void cg_iter_p3d(const Dev3D& d, cudaStream_t s);      \
   void cg_store3d(const Dev3D& d, cudaStream_t s);       \
   void efield3d(const Dev3D& d, cudaStream_t s);         \
-  void energy3d(const Dev3D& d, cudaStream_t s);
+  void energy3d(const Dev3D& d, cudaStream_t s);          \
+  void energy_fields_fin3d(const Dev3D& d, cudaStream_t s);
 
 namespace exact { WPIC_DECLARE_FP3_LAUNCHERS }
 namespace fast { WPIC_DECLARE_FP3_LAUNCHERS }
 
-// mixed-precision 3D: FP32 constants rounded once on the host, and the fixed-point exponents
-// (eA: largest tile scale keeping |v s1| < 2^22; G: global int64 scale 2^G)
+// mixed-precision 3D: FP32 constants rounded once on the host; the shock's injection end split
+// into an integer cell and an FP32 fraction (cells from nxgs), and u0 (set every step)
 struct Mix3Const {
   float fac1[2], fac2[2], qdd[2];
-  float dtdx, c, ic2, vmax;
-  int eA, G;
-  float xend, u0;  // shock: the injection boundary in cells from nxgs, and u0 (set every step)
+  float dtdx, c, ic2;
+  int xend_cell;
+  float xend_frac, u0;
 };
-void mix3_push_deposit(const Dev3D& d, const Mix3Const& k, long long* ujx, bool vay, cudaStream_t s);
 bool mix3_shape_ok(int nx, int ny, int nz);
-int mix3_setup();  // kernel attributes (dynamic shared memory); 0 on success
+// CUtensorMap of uf for the tile loads, kernel attributes; 0 on success
+int mix3_setup(const Dev3D& d, void* tmap_out);
+// the fused FP32 push + deposit + column compaction (ujx cleared first)
+void mix3_push(const Dev3D& d, const Mix3Const& k, const void* tmap, bool vay, cudaStream_t s);
+void mix3_arrive(const Dev3D& d, cudaStream_t s);
+void mix3_fix(const Dev3D& d, cudaStream_t s);  // uj = ujx / s2 over the ghosted extent
+void mix3_relayout(const Dev3D& d, const float* from_P, const long long* from_boff, cudaStream_t s);
+int mix3_initial_depth(double n, double c_dt_dx);
+void mix3_binmax(const Dev3D& d, cudaStream_t s);        // bneed[bin] = largest cell count in d.cc
+void mix3_count_rows(const Dev3D& d, cudaStream_t s);    // cumcnt and np2 of the reference layout
+// reference layout <-> bins for the rows of species isp and z layers 4 tz .. 4 tz + 3 (aos holds
+// those 4 ny rows, np_host slots each)
+void mix3_put(const Dev3D& d, const double* aos, int ndim, int np_host, int isp, int tz, cudaStream_t s);
+void mix3_get(const Dev3D& d, double* aos, int ndim, int np_host, int isp, int tz, cudaStream_t s);
+void mix3_load_weibel(const Dev3D& d, int ppc, unsigned long long seed, double drift, int drift_axis,
+                      double u_thi, double u_the, cudaStream_t s);
+void mix3_energy(const Dev3D& d, cudaStream_t s);
 void mix3_moments(const Dev3D& d, const Mix3Const& k, double* mom, cudaStream_t s);
 
 void curre_fold3d(const Dev3D& d, cudaStream_t s);

@@ -87,7 +87,8 @@ class Pic3D:
             st = empty_state3d(self.p)
         check(lib().wpic3d_get_particles(self._h, 0, _ptr(st.up, np.float64), _ptr(st.np2, np.int32),
                                          _ptr(st.cumcnt, np.int32)), "get up")
-        check(lib().wpic3d_get_particles(self._h, 1, _ptr(st.gp, np.float64), None, None), "get gp")
+        if self.precision != "mixed":  # the mixed path keeps no gp
+            check(lib().wpic3d_get_particles(self._h, 1, _ptr(st.gp, np.float64), None, None), "get gp")
         check(lib().wpic3d_get_fields(self._h, _ptr(st.uf, np.float64)), "get uf")
         return st
 
