@@ -82,7 +82,7 @@ struct Parts64 {
 // (the host re-lays out the bins) when its columns come close to full.
 constexpr int MIX_TS = 16;
 constexpr int MIX_TC = MIX_TS * MIX_TS;
-constexpr int MIX_FLUSH = 32;  // particles a push thread sums in registers between fixed-point flushes
+constexpr int MIX_FLUSH = 64;  // particles a push thread sums in registers between fixed-point flushes
 constexpr int MIX_MAX_DEPTH = 32767;  // slot indices fit the 16-bit field of the arrival key
 constexpr int MIX_OX = 0, MIX_OY = MIX_TC, MIX_UX = 2 * MIX_TC, MIX_UY = 3 * MIX_TC, MIX_UZ = 4 * MIX_TC;
 constexpr int MIX_IDLO = 5 * MIX_TC, MIX_IDHI = 6 * MIX_TC, MIX_KEY = 7 * MIX_TC;
