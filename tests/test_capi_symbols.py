@@ -43,3 +43,13 @@ def test_status_strings_without_gpu():
     assert b"capacity" in lib.wpic_status_string(2)
     lib.wpic_num_stages.restype = ctypes.c_int
     assert lib.wpic_num_stages() >= 5
+    assert b"finalise" in lib.wpic_status_string(9)
+
+
+def test_c_driver_builds_and_links_without_gpu():
+    """The C program that drives the header in the Weibel driver's order compiles against the
+    header, links against the library and answers a wrong command line before any device call."""
+    import subprocess
+    exe = _build.build_driver()
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "usage" in r.stderr

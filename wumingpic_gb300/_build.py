@@ -4,7 +4,9 @@ Both are plain compiler invocations run in parallel (no cmake, no setuptools):
   * wumingpic_gb300/_build/libwumingpic_gb300.so  -- the sm_103a kernels and the C ABI
     declared in include/wumingpic_gb300.h (nvcc, one -gencode);
   * oracle/_build/liboracle.so                    -- the CPU restatement used as checker
-    (g++ -ffp-contract=off -frounding-math, OpenMP).
+    (g++ -ffp-contract=off -frounding-math, OpenMP);
+  * wumingpic_gb300/_build/wpic_driver2d           -- a C program that calls the C ABI in the
+    2D Weibel driver's order (gcc, linked against the library).
 Object files are rebuilt only when a source or header is newer.
 """
 import glob
@@ -96,6 +98,20 @@ def build_library(verbose=False, extra=()):
     return LIB_PATH
 
 
+DRIVER_SRC = os.path.join(PKG, "driver", "wpic_driver2d.c")
+DRIVER_BIN = os.path.join(LIB_DIR, "wpic_driver2d")
+
+
+def build_driver():
+    """The C driver program, linked against the built library (run path next to it)."""
+    hdr = os.path.join(ROOT, "include", "wumingpic_gb300.h")
+    if _newer(DRIVER_BIN, [DRIVER_SRC, hdr, LIB_PATH]):
+        cmd = [os.environ.get("CC", "gcc"), "-O2", "-std=c11", "-I", os.path.join(ROOT, "include"), DRIVER_SRC,
+               "-L", LIB_DIR, "-lwumingpic_gb300", "-Wl,-rpath,$ORIGIN", "-lm", "-o", DRIVER_BIN]
+        _run_parallel([cmd])
+    return DRIVER_BIN
+
+
 def build_oracle():
     out_dir = os.path.join(ORACLE_DIR, "_build")
     os.makedirs(out_dir, exist_ok=True)
@@ -121,6 +137,7 @@ def build_all(verbose=False):
     t = threading.Thread(target=_o)
     t.start()
     build_library(verbose=verbose)
+    build_driver()
     t.join()
     if err:
         raise err[0]

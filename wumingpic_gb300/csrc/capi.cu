@@ -283,10 +283,12 @@ int ensure_C(wpic_ctx* c) {
   return WPIC_OK;
 }
 
-// fused migration + bucket sort: B (post-push, post-x-boundary) -> A sorted
-void do_migrate_sort(wpic_ctx* c) {
+// fused migration + bucket sort: B (post-push, post-x-boundary) -> A sorted; wrapx: the periodic
+// particle_x in the same pass over the particles as the first phase of particle_y
+void do_migrate_sort(wpic_ctx* c, bool wrapx = false) {
   stage_begin(c, SG_PBC);
-  migrate_scan2d(c->d, c->d.B, c->stream);
+  if (wrapx) wrapx_migrate_scan2d(c->d, c->d.B, c->stream);
+  else migrate_scan2d(c->d, c->d.B, c->stream);
   migrate_plan2d(c->d, c->stream);
   stage_end(c, SG_PBC, 2);
   stage_begin(c, SG_SORT);
@@ -437,8 +439,8 @@ int one_step(wpic_ctx* c) {
   if (c->d.ph.bc == BC_RECONNECTION) do_particle_x(c);
   int st = do_field(c);
   if (st) return st;
-  if (c->d.ph.bc == BC_PERIODIC) do_particle_x(c);
-  do_migrate_sort(c);
+  // periodic: particle_x (2d/common/boundary_periodic.f90:61-96) with particle_y's scan
+  do_migrate_sort(c, c->d.ph.bc == BC_PERIODIC);
   return WPIC_OK;
 }
 
@@ -880,8 +882,7 @@ int adj_forward_step(wpic_ctx* c, wpic_ctx::AdjState& S) {
   }
   int st = do_field(c);
   if (st) return st;
-  do_particle_x(c);
-  do_migrate_sort(c);
+  do_migrate_sort(c, true);  // periodic: particle_x with particle_y's scan
   cudaMemcpyAsync(S.map, d.map, slots * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(S.np2new, d.np2new, (size_t)d.nrowjob * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
   S.has_step = true;
@@ -978,8 +979,7 @@ int adj_step(wpic_ctx* c, const wpic_ctx::AdjState* S) {
   adj_copy_parts(d.B, d.C, slots, c->stream);        // the bookkeeping on a copy gives the permutation
   const size_t ccb = (size_t)d.nrowjob * (d.g.nx + 1) * sizeof(int);
   cudaMemcpyAsync(c->adj_cc, d.cc, ccb, cudaMemcpyDeviceToDevice, c->stream);  // the sort rewrites cc
-  particle_x2d(d, d.C, c->stream);
-  migrate_scan2d(d, d.C, c->stream);
+  wrapx_migrate_scan2d(d, d.C, c->stream);
   migrate_plan2d(d, c->stream);
   sort_rank2d(d, d.C, d.slist, c->stream);
   adj_zero_parts(c->lB, slots, c->stream);

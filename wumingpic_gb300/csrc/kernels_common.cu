@@ -2,6 +2,8 @@
 // and copies), particle boundaries (round-toward-minus-infinity arithmetic as
 // in the reference), particle migration between bucket rows, the bucket sort,
 // gathers, layout conversions and the device-side synthetic loader.
+#include <cstring>
+
 #include "common.cuh"
 
 namespace wpic {
@@ -165,7 +167,62 @@ void uf_add2d(const Dev2D& d, cudaStream_t s) { k_uf_add<<<4 * 152, 256, 0, s>>>
 //  reconnection: boundary_reconnection__particle_x (boundary_reconnection.f90:61-99),
 //                reflection at x walls, all three momentum components reversed
 // ---------------------------------------------------------------------------
-__global__ void k_particle_x(Dev2D d, Parts64 P) {
+// The periodic wrap: ipos = int(x/dx) rounded down is below nxgs exactly when x < nxgs dx and at
+// or above nxge + 1 exactly when x >= (nxge + 1) dx (directed rounding is monotone and the bounds
+// are integers).  A particle farther than 1e-12 of the domain's extent from both edges cannot
+// wrap and is left alone without the FP64 division (GB300 runs FP64 at 1/64 of FP32); the others
+// take the reference's arithmetic.
+//
+// The test itself uses no FP64 instruction: GB300 issues about two FP64 operations per clock per
+// SM, so even compares and conversions of a double cost milliseconds over 5e8 particles.  For
+// positive doubles the order of the IEEE bit patterns, read as 64-bit integers, is the order of
+// the numbers, so the bounds are compared as integers (interior_bits); a bound that is not
+// positive disables the shortcut (every particle then takes the exact path).
+struct InteriorBits {
+  long long lo, hi;  // a value v with lo < bits(v) < hi lies strictly inside the bounds
+};
+
+__host__ __device__ inline InteriorBits interior_bits(double lo, double hi) {
+  const double m = (fabs(lo) + fabs(hi)) * 1e-12;
+  InteriorBits b;
+  const double a = lo + m, c = hi - m;
+  if (a > 0.0 && c > a) {
+#ifdef __CUDA_ARCH__
+    b.lo = __double_as_longlong(a);
+    b.hi = __double_as_longlong(c);
+#else
+    memcpy(&b.lo, &a, 8);
+    memcpy(&b.hi, &c, 8);
+#endif
+  } else {
+    b.lo = 0x7fffffffffffffffLL;  // nothing is inside
+    b.hi = 0;
+  }
+  return b;
+}
+
+__device__ __forceinline__ bool inside(double v, const InteriorBits& b) {
+  const long long bits = __double_as_longlong(v);
+  return bits > b.lo && bits < b.hi;
+}
+
+InteriorBits x_interior(const Grid2D& g, double delx) {
+  return interior_bits((double)g.nxgs * delx, (double)(g.nxgs + g.nx) * delx);
+}
+
+__device__ __forceinline__ double wrap_x_periodic(double x, const Grid2D& g, double delx, const InteriorBits& xin,
+                                                  bool* changed) {
+  const int nxge = g.nxgs + g.nx - 1;
+  *changed = false;
+  if (inside(x, xin)) return x;
+  const int ipos = (int)__ddiv_rd(x, delx);
+  const double L = __dmul_rd((double)g.nx, delx);
+  if (ipos < g.nxgs) { *changed = true; return __dadd_rd(x, L); }
+  if (ipos >= nxge + 1) { *changed = true; return __dsub_rd(x, L); }
+  return x;
+}
+
+__global__ void k_particle_x(Dev2D d, Parts64 P, InteriorBits xin) {
   const int row = blockIdx.y;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= d.np2[row]) return;
@@ -173,13 +230,10 @@ __global__ void k_particle_x(Dev2D d, Parts64 P) {
   const Grid2D g = d.g;
   const double delx = d.ph.delx;
   double x = P.x[k];
-  const int nxge = g.nxgs + g.nx - 1;
   if (d.ph.bc == BC_PERIODIC) {
-    const int ipos = (int)__ddiv_rd(x, delx);
-    const double L = __dmul_rd((double)g.nx, delx);
-    if (ipos < g.nxgs) x = __dadd_rd(x, L);
-    else if (ipos >= nxge + 1) x = __dsub_rd(x, L);
-    P.x[k] = x;
+    bool changed;
+    x = wrap_x_periodic(x, g, delx, xin, &changed);
+    if (changed) P.x[k] = x;
   } else {
     const int nxs = g.nxgs + g.wx0, nxe = g.nxgs + g.wx1;  // the window; walls at nxs+1, nxe-1
     const int ipos = (int)(x / delx);
@@ -202,7 +256,7 @@ __global__ void k_particle_x(Dev2D d, Parts64 P) {
 
 void particle_x2d(const Dev2D& d, const Parts64& P, cudaStream_t s) {
   dim3 grid((d.cap + 255) / 256, d.nrowjob);
-  k_particle_x<<<grid, 256, 0, s>>>(d, P);
+  k_particle_x<<<grid, 256, 0, s>>>(d, P, x_interior(d.g, d.ph.delx));
 }
 
 // boundary_shock__injection (2d/proj/shock/boundary_shock.f90:255-297): reflection at the
@@ -246,7 +300,10 @@ void injection2d(const Dev2D& d, const Parts64& P, double u0, double xend, cudaS
 // ---------------------------------------------------------------------------
 constexpr int MIG_THREADS = 256;
 
-__global__ void __launch_bounds__(MIG_THREADS) k_migrate_scan(Dev2D d, Parts64 P) {
+// WRAPX: the periodic boundary_periodic__particle_x of the same particle first (the driver calls
+// it right before particle_y), so that one pass over the row does both
+template <bool WRAPX>
+__global__ void __launch_bounds__(MIG_THREADS) k_migrate_scan(Dev2D d, Parts64 P, InteriorBits xin) {
   const Grid2D g = d.g;
   const int row = blockIdx.x;
   const int jj = row % g.ny;
@@ -256,6 +313,9 @@ __global__ void __launch_bounds__(MIG_THREADS) k_migrate_scan(Dev2D d, Parts64 P
   const size_t rb = (size_t)row * d.cap;
   const double delx = d.ph.delx;
   const double L = __dmul_rd((double)g.ny, delx);
+  // jpos = int(y/dx) rounded down differs from j exactly when y < j dx or y >= (j + 1) dx; farther
+  // than 1e-12 of the row's extent from both bounds the division is not needed
+  const InteriorBits yin = interior_bits((double)j * delx, (double)(j + 1) * delx);
   __shared__ int wu[MIG_THREADS / 32], wd[MIG_THREADS / 32];
   __shared__ int base_u, base_d;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -265,8 +325,13 @@ __global__ void __launch_bounds__(MIG_THREADS) k_migrate_scan(Dev2D d, Parts64 P
     const int s = c0 + threadIdx.x;
     int dir = 0;
     if (s < n) {
+      if (WRAPX) {
+        bool changed;
+        const double x = wrap_x_periodic(P.x[rb + s], g, delx, xin, &changed);
+        if (changed) P.x[rb + s] = x;
+      }
       double y = P.y[rb + s];
-      const int jpos = (int)__ddiv_rd(y, delx);
+      const int jpos = inside(y, yin) ? j : (int)__ddiv_rd(y, delx);
       if (jpos != j) {
         if (jpos == j + 1) dir = 1;
         else if (jpos == j - 1) dir = 2;
@@ -310,7 +375,11 @@ __global__ void __launch_bounds__(MIG_THREADS) k_migrate_scan(Dev2D d, Parts64 P
 }
 
 void migrate_scan2d(const Dev2D& d, const Parts64& P, cudaStream_t s) {
-  k_migrate_scan<<<d.nrowjob, MIG_THREADS, 0, s>>>(d, P);
+  k_migrate_scan<false><<<d.nrowjob, MIG_THREADS, 0, s>>>(d, P, x_interior(d.g, d.ph.delx));
+}
+
+void wrapx_migrate_scan2d(const Dev2D& d, const Parts64& P, cudaStream_t s) {
+  k_migrate_scan<true><<<d.nrowjob, MIG_THREADS, 0, s>>>(d, P, x_interior(d.g, d.ph.delx));
 }
 
 // ---------------------------------------------------------------------------
@@ -466,9 +535,118 @@ __global__ void __launch_bounds__(32) k_sort_rank(Dev2D d, Parts64 P, const int*
   }
 }
 
+// The same stable counting sort with SW warps per row: warp w takes the w-th contiguous chunk of
+// the input sequence.  Pass 1: per-warp cell histograms in shared memory (the cells kept in
+// tlist); pass 2: per cell, the exclusive prefix over the warps plus the row's exclusive prefix
+// over the cells (cumcnt); pass 3: every warp ranks its chunk in order from its own offsets, so
+// the result is the single-warp sort's permutation.
+constexpr int SW = 8;
+constexpr int SORT_SMEM_MAX = 96 * 1024;
+
+// int(x) (truncation) of a double by integer operations on its bits, for 0 <= x < 2^30; other
+// values take the FP64 conversion.  Equal to (int)x wherever it answers.
+__device__ __forceinline__ int trunc_double(double x) {
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  if (b >= 0 && e < 30) {
+    if (e < 0) return 0;
+    const long long m = (b & 0x000fffffffffffffLL) | 0x0010000000000000LL;
+    return (int)(m >> (52 - e));
+  }
+  return (int)x;
+}
+
+__global__ void __launch_bounds__(SW * 32) k_sort_rank_mw(Dev2D d, Parts64 P, const int* slist, const int* counts) {
+  extern __shared__ int sh[];  // hist[SW][nx + 1], then tot[nx + 1]
+  const Grid2D g = d.g;
+  const int nx = g.nx, pitch = nx + 1;
+  int* const tot = sh + SW * pitch;
+  const int row = blockIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int n = counts[row];
+  const size_t rb = (size_t)row * d.cap;
+  for (int k = threadIdx.x; k < SW * pitch; k += SW * 32) sh[k] = 0;
+  __syncthreads();
+  const int chunk = ((n + SW - 1) / SW + 31) & ~31;
+  const int t_lo = w * chunk, t_hi = min(n, t_lo + chunk);
+  int* const hw = sh + w * pitch;
+  for (int t = t_lo + lane; t < t_hi; t += 32) {
+    const int src = slist ? slist[rb + t] : (int)(rb + t);
+    int cell = trunc_double(P.x[src]) - g.nxgs;
+    if (cell < 0 || cell >= nx) {
+      atomicOr(d.err, EB_OUT_OF_RANGE);
+      cell = cell < 0 ? 0 : nx - 1;
+    }
+    d.tlist[rb + t] = cell;
+    atomicAdd(&hw[cell], 1);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nx; k += SW * 32) {
+    int acc = 0;
+#pragma unroll
+    for (int q = 0; q < SW; ++q) {
+      const int v = sh[q * pitch + k];
+      sh[q * pitch + k] = acc;
+      acc += v;
+    }
+    tot[k] = acc;
+  }
+  __syncthreads();
+  int* ccr = d.cc + (size_t)row * (nx + 1);
+  if (w == 0) {
+    int carry = 0;
+    for (int k0 = 0; k0 < nx; k0 += 32) {
+      const int k = k0 + lane;
+      const int v = k < nx ? tot[k] : 0;
+      int incl = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (k < nx) {
+        tot[k] = incl - v + carry;
+        ccr[k] = incl - v + carry;
+      }
+      carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) ccr[nx] = carry;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nx; k += SW * 32) {
+    const int base = tot[k];
+#pragma unroll
+    for (int q = 0; q < SW; ++q) sh[q * pitch + k] += base;
+  }
+  __syncthreads();
+  const unsigned lt = lanemask_lt();
+  for (int t0 = t_lo; t0 < t_hi; t0 += 32) {
+    const int t = t0 + lane;
+    const bool act = t < t_hi;
+    int src = 0, cell = -1 - lane;
+    if (act) {
+      src = slist ? slist[rb + t] : (int)(rb + t);
+      cell = d.tlist[rb + t];
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, cell);
+    int base = 0;
+    if (act) base = hw[cell];
+    __syncwarp();
+    if (act && lane == __ffs(peers) - 1) hw[cell] = base + __popc(peers);
+    __syncwarp();
+    if (act) d.map[rb + base + __popc(peers & lt)] = src;
+  }
+}
+
 void sort_rank2d(const Dev2D& d, const Parts64& P, const int* slist, cudaStream_t s) {
   const int* counts = slist ? d.np2new : d.np2;
-  k_sort_rank<<<d.nrowjob, 32, (d.g.nx + 1) * sizeof(int), s>>>(d, P, slist, counts);
+  const size_t smem = (size_t)(SW + 1) * (d.g.nx + 1) * sizeof(int);
+  if (smem <= (size_t)SORT_SMEM_MAX) {
+    cudaFuncSetAttribute(k_sort_rank_mw, cudaFuncAttributeMaxDynamicSharedMemorySize, SORT_SMEM_MAX);
+    k_sort_rank_mw<<<d.nrowjob, SW * 32, smem, s>>>(d, P, slist, counts);
+  } else {
+    k_sort_rank<<<d.nrowjob, 32, (d.g.nx + 1) * sizeof(int), s>>>(d, P, slist, counts);
+  }
 }
 
 // dst[row][pos] = src[map[row][pos]] for pos < counts[row]

@@ -197,6 +197,8 @@ void adj_push_fields(const Dev2D& d, const Parts64& lB, const Parts64& lA, doubl
                      float* f32, cudaStream_t s);
 void adj_dot(const double* a, const double* b, size_t n, double* out, cudaStream_t s);
 void migrate_scan2d(const Dev2D& d, const Parts64& P, cudaStream_t s);
+// boundary_periodic__particle_x and the first phase of particle_y in one pass (periodic runs)
+void wrapx_migrate_scan2d(const Dev2D& d, const Parts64& P, cudaStream_t s);
 void migrate_plan2d(const Dev2D& d, cudaStream_t s);
 void sort_rank2d(const Dev2D& d, const Parts64& P, const int* slist, cudaStream_t s);
 void gather2d(const Dev2D& d, const Parts64& src, const Parts64& dst, const int* map, const int* counts,

@@ -5,11 +5,17 @@
 ! of libwuming2d_common.a; the drivers ({2d}/proj/*/app.f90) stay unchanged.
 !
 ! Coherence: the first particle__solv uploads the host state (up, uf, cumcnt;
-! np2 = cumcnt(nxe+1,:,:)).  Afterwards the device state is authoritative; with
-! the default sync interval of 1 the host arrays are refreshed every step (uf at
-! the end of field__fdtd_i, up/np2/cumcnt at the end of sort__bucket) so that
-! the drivers' I/O and diagnostics read current values.  A driver that knows its
-! output interval may call wpic_shim_set_sync(n) to refresh only every n steps.
+! np2 = cumcnt(nxe+1,:,:)).  Afterwards the device state is authoritative and the
+! host arrays are refreshed only where the drivers read them: on entry to
+! mom_calc__accl (the diagnostic block: mom_calc__accl, mom_calc__nvt, bc__mom,
+! io__mom and energy_history read up, uf, cumcnt and np2; np2 is handed back in
+! mom_calc__nvt) and in the I/O routines io__ptcl, io__orb, io__mom and io__output,
+! which this file's wuming2d module wraps (2d/proj/weibel/app.f90:108-125, 571).
+! io__input marks the host state as the newer one, so the next call uploads it.
+! Between those points no particle or field array crosses the host link.
+! wpic_shim_set_sync(n) (n >= 1) refreshes the host arrays every n steps instead,
+! for drivers that read them elsewhere; the shock driver, which edits the host state
+! every step, gets n = 1 and an upload every step from boundary_shock__init.
 !
 ! The three boundary routines that field__fdtd_i receives as procedure arguments
 ! are accepted and ignored: the library applies the boundary of the kind chosen
@@ -97,7 +103,9 @@ module wpic_capi
   logical, save :: wpic_bc_set = .false.           ! a boundary module's __init chose the kind
   logical, save :: wpic_upload_each_step = .false. ! drivers that edit up/uf/cumcnt between steps
   integer, save :: wpic_win_s = -1, wpic_win_e = -1
-  integer, save :: wpic_sync_every = 1, wpic_step_count = 0
+  integer, save :: wpic_sync_every = 0, wpic_step_count = 0  ! 0: refresh at the read points only
+  integer, save :: wpic_synced_at = -1      ! step count of the host arrays' last refresh
+  integer(c_int), allocatable, save :: wpic_np2_dev(:,:), wpic_cc_dev(:,:,:)
 
   procedure(wpic_call), pointer :: p_solv => null(), p_fdtd => null(), p_bcx => null(), &
        p_bcy => null(), p_sort => null(), p_solv_vay => null()
@@ -151,8 +159,43 @@ contains
 
   subroutine wpic_shim_set_sync(n)
     integer, intent(in) :: n
-    wpic_sync_every = max(1, n)
+    wpic_sync_every = max(0, n)
   end subroutine wpic_shim_set_sync
+
+  ! The host arrays brought up to date with the device (once per step): the sorted state up,
+  ! uf, and, when present, np2 and cumcnt.  Before the first upload the host is the newer side
+  ! and nothing is copied.
+  subroutine wpic_sync_host(up, uf, np2, cumcnt)
+    real(8), intent(inout) :: up(*), uf(*)
+    integer, intent(inout), optional :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    integer, intent(inout), optional :: cumcnt(wpic_prm%nxgs:wpic_prm%nxge+1,wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    if (.not. wpic_uploaded) return
+    if (.not. allocated(wpic_np2_dev)) then
+       allocate(wpic_np2_dev(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp))
+       allocate(wpic_cc_dev(wpic_prm%nxgs:wpic_prm%nxge+1,wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp))
+    endif
+    if (wpic_synced_at /= wpic_step_count) then
+       call wpic_check(wpic_get_particles(wpic_ctx, 0_c_int, up, wpic_np2_dev, wpic_cc_dev), 'get up')
+       call wpic_check(wpic_get_fields(wpic_ctx, uf), 'get uf')
+       wpic_synced_at = wpic_step_count
+    endif
+    if (present(np2)) np2(:,:) = wpic_np2_dev(:,:)
+    if (present(cumcnt)) cumcnt(:,:,:) = wpic_cc_dev(:,:,:)
+  end subroutine wpic_sync_host
+
+  ! uf alone brought up to date (io__mom receives uf only)
+  subroutine wpic_sync_fields(uf)
+    real(8), intent(inout) :: uf(*)
+    if (.not. wpic_uploaded) return
+    if (wpic_synced_at /= wpic_step_count) call wpic_check(wpic_get_fields(wpic_ctx, uf), 'get uf')
+  end subroutine wpic_sync_fields
+
+  ! np2 of the last refresh (mom_calc__nvt receives np2 after mom_calc__accl refreshed up)
+  subroutine wpic_sync_np2(np2)
+    integer, intent(inout) :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    if (wpic_uploaded .and. allocated(wpic_np2_dev) .and. wpic_synced_at == wpic_step_count) &
+         np2(:,:) = wpic_np2_dev(:,:)
+  end subroutine wpic_sync_np2
 
   subroutine wpic_bind_procedures()
     interface
@@ -264,8 +307,9 @@ contains
     external :: set_boundary_dfield, set_boundary_curre, set_boundary_phi
     call wpic_apply_window(nxs, nxe)
     call wpic_check(p_fdtd(wpic_ctx), 'field__fdtd_i')
-    if (mod(wpic_step_count + 1, wpic_sync_every) == 0) then
-       call wpic_check(wpic_get_fields(wpic_ctx, uf), 'get uf')
+    if (wpic_sync_every > 0) then
+       if (mod(wpic_step_count + 1, wpic_sync_every) == 0) &
+            call wpic_check(wpic_get_fields(wpic_ctx, uf), 'get uf')
     endif
   end subroutine field__fdtd_i
 end module field
@@ -286,17 +330,33 @@ contains
   subroutine sort__bucket(gp,up,cumcnt,np2,nxs,nxe)
     integer, intent(in)    :: nxs, nxe
     integer, intent(inout) :: np2(wpic_prm%nye-wpic_prm%nys+1, wpic_prm%nsp)
-    integer, intent(out)   :: cumcnt(*)
+    integer, intent(inout) :: cumcnt(*)
     real(8), intent(in)    :: up(*)
-    real(8), intent(out)   :: gp(*)
+    real(8), intent(inout) :: gp(*)
     integer(c_int) :: np2_dev(wpic_prm%nye-wpic_prm%nys+1, wpic_prm%nsp)
+    call wpic_ensure_ctx()
     call wpic_apply_window(nxs, nxe)
-    call wpic_check(p_sort(wpic_ctx), 'sort__bucket')
-    wpic_step_count = wpic_step_count + 1
-    if (mod(wpic_step_count, wpic_sync_every) == 0) then
-       ! the sorted state ('gp' dummy = the driver's up) with its np2 and cumcnt
+    if (.not. wpic_uploaded) then
+       ! the restart path (2d/proj/weibel/app.f90:351-352): io__input filled the host 'up' (this
+       ! routine's up dummy) and np2; they are sorted on the device and handed back, and the next
+       ! particle__solv uploads the whole host state
+       np2_dev(:,:) = np2(:,:)
+       ! (cumcnt is not read for the gp state; np2 stands in for it)
+       call wpic_check(wpic_put_particles(wpic_ctx, 1_c_int, up, np2_dev, np2_dev), 'put gp')
+       call wpic_check(p_sort(wpic_ctx), 'sort__bucket')
        call wpic_check(wpic_get_particles(wpic_ctx, 0_c_int, gp, np2_dev, cumcnt), 'get up')
        np2(:,:) = np2_dev(:,:)
+       return
+    endif
+    call wpic_check(p_sort(wpic_ctx), 'sort__bucket')
+    wpic_step_count = wpic_step_count + 1
+    if (wpic_sync_every > 0) then
+       if (mod(wpic_step_count, wpic_sync_every) == 0) then
+          ! the sorted state ('gp' dummy = the driver's up) with its np2 and cumcnt
+          call wpic_check(wpic_get_particles(wpic_ctx, 0_c_int, gp, np2_dev, cumcnt), 'get up')
+          np2(:,:) = np2_dev(:,:)
+          wpic_synced_at = wpic_step_count
+       endif
     endif
   end subroutine sort__bucket
 end module sort
@@ -366,20 +426,25 @@ contains
     real(8), intent(in) :: delx_in, delt_in, c_in, q_in(nsp_in), r_in(nsp_in)
   end subroutine mom_calc__init
 
+  ! the start of every driver's diagnostic block: the host up, uf and cumcnt are refreshed here
+  ! (intent(in) in the reference; the drivers pass their own arrays)
   subroutine mom_calc__accl(gp,up,uf,cumcnt,nxs,nxe)
-    integer, intent(in)  :: nxs, nxe
-    integer, intent(in)  :: cumcnt(*)
-    real(8), intent(in)  :: up(*), uf(*)
-    real(8), intent(out) :: gp(*)
+    integer, intent(in)    :: nxs, nxe
+    integer, intent(inout) :: cumcnt(wpic_prm%nxgs:wpic_prm%nxge+1,wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    real(8), intent(inout) :: up(*), uf(*)
+    real(8), intent(out)   :: gp(*)
     call wpic_ensure_ctx()
+    call wpic_sync_host(up, uf, cumcnt=cumcnt)
     call wpic_check(wpic_mom_calc_accl(wpic_ctx), 'mom_calc__accl')
   end subroutine mom_calc__accl
 
+  ! np2 comes back with the state refreshed in mom_calc__accl (energy_history reads it next)
   subroutine mom_calc__nvt(mom,up,np2)
-    integer, intent(in)  :: np2(*)
-    real(8), intent(in)  :: up(*)
-    real(8), intent(out) :: mom(*)
+    integer, intent(inout) :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    real(8), intent(in)    :: up(*)
+    real(8), intent(out)   :: mom(*)
     call wpic_ensure_ctx()
+    call wpic_sync_np2(np2)
     call wpic_check(wpic_mom_calc_nvt(wpic_ctx, 1_c_int), 'mom_calc__nvt')
     call wpic_check(wpic_get_mom(wpic_ctx, mom), 'get mom')
   end subroutine mom_calc__nvt
@@ -457,6 +522,7 @@ contains
     real(8), intent(in) :: delx_in, delt_in, c_in
     wpic_prm%bc_kind = 2; wpic_bc_set = .true.
     call wpic_shim_set_upload(.true.)
+    call wpic_shim_set_sync(1)
   end subroutine boundary_shock__init
 
   subroutine boundary_shock__particle_x(up,np2,nxs,nxe)
@@ -502,3 +568,77 @@ contains
     call wpic_check(wpic_get_mom(wpic_ctx, mom), 'get mom')
   end subroutine boundary_shock__mom
 end module boundary_shock
+
+
+! The I/O routines that read the host state (paraio, 2d/common/paraio.f90:93-741, the drivers'
+! io__* through wuming2d) refresh it from the device first; io__input marks the host state as
+! the newer one, so the next particle__solv or sort__bucket uploads it.
+module wpic_io
+  use wpic_capi
+  use paraio
+  implicit none
+  private
+  public :: io__input, io__output, io__mom, io__ptcl, io__orb
+contains
+  subroutine io__input(up,uf,np2,nxs,nxe,it,filename)
+    real(8), intent(out)         :: up(*), uf(*)
+    integer, intent(out)         :: np2(*), nxs, nxe, it
+    character(len=*), intent(in) :: filename
+    call paraio__input(up, uf, np2, nxs, nxe, it, filename)
+    wpic_uploaded = .false.
+  end subroutine io__input
+
+  subroutine io__output(up,uf,np2,nxs,nxe,it,filename)
+    real(8), intent(inout)       :: up(*), uf(*)
+    integer, intent(inout)       :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    integer, intent(in)          :: nxs, nxe, it
+    character(len=*), intent(in) :: filename
+    call wpic_sync_host(up, uf, np2=np2)
+    call paraio__output(up, uf, np2, nxs, nxe, it, filename)
+  end subroutine io__output
+
+  subroutine io__mom(mom,uf,it)
+    real(8), intent(inout) :: mom(*), uf(*)
+    integer, intent(in)    :: it
+    call wpic_sync_fields(uf)
+    call paraio__mom(mom, uf, it)
+  end subroutine io__mom
+
+  subroutine io__ptcl(up,uf,np2,it)
+    real(8), intent(inout) :: up(*), uf(*)
+    integer, intent(inout) :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    integer, intent(in)    :: it
+    call wpic_sync_host(up, uf, np2=np2)
+    call paraio__ptcl(up, uf, np2, it)
+  end subroutine io__ptcl
+
+  subroutine io__orb(up,uf,np2,it)
+    real(8), intent(inout) :: up(*), uf(*)
+    integer, intent(inout) :: np2(wpic_prm%nys:wpic_prm%nye,wpic_prm%nsp)
+    integer, intent(in)    :: it
+    call wpic_sync_host(up, uf, np2=np2)
+    call paraio__orb(up, uf, np2, it)
+  end subroutine io__orb
+end module wpic_io
+
+
+! wuming2d (2d/common/wuming2d.f90) with the paraio I/O routines of the drivers' calls routed
+! through wpic_io; everything else it exports is unchanged
+module wuming2d
+  use json_module
+  use jsonio
+  use mpiio
+  use field
+  use particle
+  use mom_calc
+  use sort
+  use mpi_set
+  use fio
+  use h5io
+  use paraio, &
+       & io__init     => paraio__init,     &
+       & io__finalize => paraio__finalize, &
+       & io__param    => paraio__param
+  use wpic_io
+  implicit none
+end module wuming2d

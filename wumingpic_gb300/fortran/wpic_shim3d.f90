@@ -4,7 +4,11 @@
 ! corresponding objects of libwuming3d_common.a; the drivers (3d/proj/*/app.f90)
 ! stay unchanged.  Coherence follows the 2D shim: the first particle__solv uploads
 ! the host state, the device state is authoritative afterwards, and the host arrays
-! are refreshed every wpic3d_shim_set_sync(n) steps (default: every step).
+! are refreshed only where the drivers read them -- on entry to mom_calc__accl (np2
+! handed back in mom_calc__nvt) and in io__ptcl, io__orb, io__mom and io__output, which
+! this file's wuming3d module wraps (3d/proj/weibel/app.f90 loop and diagnostic block);
+! io__input makes the host the newer side.  wpic3d_shim_set_sync(n) (n >= 1) adds a
+! refresh every n steps; the shock driver gets n = 1 from boundary_shock__init.
 module wpic3d_capi
   use iso_c_binding
   implicit none
@@ -107,7 +111,9 @@ module wpic3d_capi
   logical, save :: wpic3_bc_set = .false.  ! a boundary module's __init chose the kind
   logical, save :: wpic3_upload_each_step = .false.  ! the shock driver edits up/uf/cumcnt between steps
   integer, save :: wpic3_win_s = -huge(1), wpic3_win_e = -huge(1)
-  integer, save :: wpic3_sync_every = 1, wpic3_step_count = 0
+  integer, save :: wpic3_sync_every = 0, wpic3_step_count = 0  ! 0: refresh at the read points only
+  integer, save :: wpic3_synced_at = -1      ! step count of the host arrays' last refresh
+  integer(c_int), allocatable, save :: wpic3_np2_dev(:,:,:), wpic3_cc_dev(:,:,:,:)
 
 contains
 
@@ -122,8 +128,42 @@ contains
 
   subroutine wpic3d_shim_set_sync(n)
     integer, intent(in) :: n
-    wpic3_sync_every = max(1, n)
+    wpic3_sync_every = max(0, n)
   end subroutine wpic3d_shim_set_sync
+
+  ! the host arrays brought up to date with the device (once per step): up, uf and, when
+  ! present, np2 and cumcnt; before the first upload the host is the newer side
+  subroutine wpic3_sync_host(up, uf, np2, cumcnt)
+    real(8), intent(inout) :: up(*), uf(*)
+    integer, intent(inout), optional :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    integer, intent(inout), optional :: cumcnt(wpic3_prm%nxgs:wpic3_prm%nxge+1,wpic3_prm%nys:wpic3_prm%nye, &
+                                               wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    if (.not. wpic3_uploaded) return
+    if (.not. allocated(wpic3_np2_dev)) then
+       allocate(wpic3_np2_dev(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp))
+       allocate(wpic3_cc_dev(wpic3_prm%nxgs:wpic3_prm%nxge+1,wpic3_prm%nys:wpic3_prm%nye, &
+                             wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp))
+    endif
+    if (wpic3_synced_at /= wpic3_step_count) then
+       call wpic3_check(wpic3d_get_particles(wpic3_ctx, 0_c_int, up, wpic3_np2_dev, wpic3_cc_dev), 'get up')
+       call wpic3_check(wpic3d_get_fields(wpic3_ctx, uf), 'get uf')
+       wpic3_synced_at = wpic3_step_count
+    endif
+    if (present(np2)) np2(:,:,:) = wpic3_np2_dev(:,:,:)
+    if (present(cumcnt)) cumcnt(:,:,:,:) = wpic3_cc_dev(:,:,:,:)
+  end subroutine wpic3_sync_host
+
+  subroutine wpic3_sync_fields(uf)
+    real(8), intent(inout) :: uf(*)
+    if (.not. wpic3_uploaded) return
+    if (wpic3_synced_at /= wpic3_step_count) call wpic3_check(wpic3d_get_fields(wpic3_ctx, uf), 'get uf')
+  end subroutine wpic3_sync_fields
+
+  subroutine wpic3_sync_np2(np2)
+    integer, intent(inout) :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    if (wpic3_uploaded .and. allocated(wpic3_np2_dev) .and. wpic3_synced_at == wpic3_step_count) &
+         np2(:,:,:) = wpic3_np2_dev(:,:,:)
+  end subroutine wpic3_sync_np2
 
   subroutine wpic3_ensure_ctx()
     if (.not. c_associated(wpic3_ctx)) call wpic3_check(wpic3d_init(wpic3_ctx, wpic3_prm, c_null_ptr), 'wpic3d_init')
@@ -231,8 +271,9 @@ contains
     external :: set_boundary_dfield, set_boundary_curre, set_boundary_phi
     call wpic3_apply_window(nxs, nxe)
     call wpic3_check(wpic3d_field_fdtd_i(wpic3_ctx), 'field__fdtd_i')
-    if (mod(wpic3_step_count + 1, wpic3_sync_every) == 0) then
-       call wpic3_check(wpic3d_get_fields(wpic3_ctx, uf), 'get uf')
+    if (wpic3_sync_every > 0) then
+       if (mod(wpic3_step_count + 1, wpic3_sync_every) == 0) &
+            call wpic3_check(wpic3d_get_fields(wpic3_ctx, uf), 'get uf')
     endif
   end subroutine field__fdtd_i
 end module field
@@ -253,16 +294,30 @@ contains
   subroutine sort__bucket(gp,up,cumcnt,np2,nxs,nxe)
     integer, intent(in)    :: nxs, nxe
     integer, intent(inout) :: np2(wpic3_prm%nye-wpic3_prm%nys+1, wpic3_prm%nze-wpic3_prm%nzs+1, wpic3_prm%nsp)
-    integer, intent(out)   :: cumcnt(*)
+    integer, intent(inout) :: cumcnt(*)
     real(8), intent(in)    :: up(*)
-    real(8), intent(out)   :: gp(*)
+    real(8), intent(inout) :: gp(*)
     integer(c_int) :: np2_dev(wpic3_prm%nye-wpic3_prm%nys+1, wpic3_prm%nze-wpic3_prm%nzs+1, wpic3_prm%nsp)
     call wpic3_apply_window(nxs, nxe)
-    call wpic3_check(wpic3d_sort_bucket(wpic3_ctx), 'sort__bucket')
-    wpic3_step_count = wpic3_step_count + 1
-    if (mod(wpic3_step_count, wpic3_sync_every) == 0) then
+    if (.not. wpic3_uploaded) then
+       ! the restart path: io__input filled the host state; it is sorted on the device and handed
+       ! back, and the next particle__solv uploads the whole host state (cumcnt is not read for
+       ! the gp state; np2 stands in for it)
+       np2_dev(:,:,:) = np2(:,:,:)
+       call wpic3_check(wpic3d_put_particles(wpic3_ctx, 1_c_int, up, np2_dev, np2_dev), 'put gp')
+       call wpic3_check(wpic3d_sort_bucket(wpic3_ctx), 'sort__bucket')
        call wpic3_check(wpic3d_get_particles(wpic3_ctx, 0_c_int, gp, np2_dev, cumcnt), 'get up')
        np2(:,:,:) = np2_dev(:,:,:)
+       return
+    endif
+    call wpic3_check(wpic3d_sort_bucket(wpic3_ctx), 'sort__bucket')
+    wpic3_step_count = wpic3_step_count + 1
+    if (wpic3_sync_every > 0) then
+       if (mod(wpic3_step_count, wpic3_sync_every) == 0) then
+          call wpic3_check(wpic3d_get_particles(wpic3_ctx, 0_c_int, gp, np2_dev, cumcnt), 'get up')
+          np2(:,:,:) = np2_dev(:,:,:)
+          wpic3_synced_at = wpic3_step_count
+       endif
     endif
   end subroutine sort__bucket
 end module sort
@@ -394,6 +449,7 @@ contains
     real(8), intent(in) :: delx_in, delt_in, c_in
     wpic3_prm%bc_kind = 2; wpic3_bc_set = .true.
     wpic3_upload_each_step = .true.
+    call wpic3d_shim_set_sync(1)
   end subroutine boundary_shock__init
 
   subroutine boundary_shock__particle_yz(up,np2)
@@ -447,21 +503,96 @@ contains
     real(8), intent(in) :: delx_in, delt_in, c_in, q_in(nsp_in), r_in(nsp_in)
   end subroutine mom_calc__init
 
+  ! the start of every driver's diagnostic block: the host up, uf and cumcnt are refreshed here
   subroutine mom_calc__accl(gp,up,uf,cumcnt,nxs,nxe)
-    integer, intent(in)  :: nxs, nxe
-    integer, intent(in)  :: cumcnt(*)
-    real(8), intent(in)  :: up(*), uf(*)
-    real(8), intent(out) :: gp(*)
+    integer, intent(in)    :: nxs, nxe
+    integer, intent(inout) :: cumcnt(wpic3_prm%nxgs:wpic3_prm%nxge+1,wpic3_prm%nys:wpic3_prm%nye, &
+                                     wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    real(8), intent(inout) :: up(*), uf(*)
+    real(8), intent(out)   :: gp(*)
     call wpic3_ensure_ctx()
+    call wpic3_sync_host(up, uf, cumcnt=cumcnt)
     call wpic3_check(wpic3d_mom_calc_accl(wpic3_ctx), 'mom_calc__accl')
   end subroutine mom_calc__accl
 
+  ! np2 comes back with the state refreshed in mom_calc__accl (energy_history reads it next)
   subroutine mom_calc__nvt(mom,up,np2)
-    integer, intent(in)  :: np2(*)
-    real(8), intent(in)  :: up(*)
-    real(8), intent(out) :: mom(*)
+    integer, intent(inout) :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    real(8), intent(in)    :: up(*)
+    real(8), intent(out)   :: mom(*)
     call wpic3_ensure_ctx()
+    call wpic3_sync_np2(np2)
     call wpic3_check(wpic3d_mom_calc_nvt(wpic3_ctx, 1_c_int), 'mom_calc__nvt')
     call wpic3_check(wpic3d_get_mom(wpic3_ctx, mom), 'get mom')
   end subroutine mom_calc__nvt
 end module mom_calc
+
+
+! The paraio routines that read the host state (3d/common/paraio.f90:102-866, the drivers' io__*
+! through wuming3d) refresh it from the device first; io__input makes the host the newer side.
+module wpic3_io
+  use wpic3d_capi
+  use paraio
+  implicit none
+  private
+  public :: io__input, io__output, io__mom, io__ptcl, io__orb
+contains
+  subroutine io__input(up,uf,np2,nxs,nxe,it,filename)
+    real(8), intent(out)         :: up(*), uf(*)
+    integer, intent(out)         :: np2(*), nxs, nxe, it
+    character(len=*), intent(in) :: filename
+    call paraio__input(up, uf, np2, nxs, nxe, it, filename)
+    wpic3_uploaded = .false.
+  end subroutine io__input
+
+  subroutine io__output(up,uf,np2,nxs,nxe,it,filename)
+    real(8), intent(inout)       :: up(*), uf(*)
+    integer, intent(inout)       :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    integer, intent(in)          :: nxs, nxe, it
+    character(len=*), intent(in) :: filename
+    call wpic3_sync_host(up, uf, np2=np2)
+    call paraio__output(up, uf, np2, nxs, nxe, it, filename)
+  end subroutine io__output
+
+  subroutine io__mom(mom,uf,it)
+    real(8), intent(inout) :: mom(*), uf(*)
+    integer, intent(in)    :: it
+    call wpic3_sync_fields(uf)
+    call paraio__mom(mom, uf, it)
+  end subroutine io__mom
+
+  subroutine io__ptcl(up,uf,np2,it)
+    real(8), intent(inout) :: up(*), uf(*)
+    integer, intent(inout) :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    integer, intent(in)    :: it
+    call wpic3_sync_host(up, uf, np2=np2)
+    call paraio__ptcl(up, uf, np2, it)
+  end subroutine io__ptcl
+
+  subroutine io__orb(up,uf,np2,it)
+    real(8), intent(inout) :: up(*), uf(*)
+    integer, intent(inout) :: np2(wpic3_prm%nys:wpic3_prm%nye,wpic3_prm%nzs:wpic3_prm%nze,wpic3_prm%nsp)
+    integer, intent(in)    :: it
+    call wpic3_sync_host(up, uf, np2=np2)
+    call paraio__orb(up, uf, np2, it)
+  end subroutine io__orb
+end module wpic3_io
+
+
+! wuming3d (3d/common/wuming3d.f90) with the drivers' io__* routed through wpic3_io
+module wuming3d
+  use json_module
+  use jsonio
+  use mpiio
+  use field
+  use particle
+  use mom_calc
+  use sort
+  use mpi_set
+  use paraio, &
+       & io__init     => paraio__init,     &
+       & io__finalize => paraio__finalize, &
+       & io__param    => paraio__param
+  use wpic3_io
+  implicit none
+end module wuming3d
