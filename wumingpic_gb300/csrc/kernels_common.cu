@@ -182,6 +182,18 @@ struct InteriorBits {
   long long lo, hi;  // a value v with lo < bits(v) < hi lies strictly inside the bounds
 };
 
+// lo < bits(v) < hi with 32-bit compares of the high and low words (the common case, a high
+// word strictly between the bounds' high words, needs only the first test)
+__device__ __forceinline__ bool inside_words(double v, const InteriorBits& b) {
+  const int vh = __double2hiint(v);
+  const int lh = (int)(b.lo >> 32), hh = (int)(b.hi >> 32);
+  if (vh > lh && vh < hh) return true;
+  const unsigned vl = (unsigned)__double2loint(v);
+  const bool above = vh > lh || (vh == lh && vl > (unsigned)b.lo);
+  const bool below = vh < hh || (vh == hh && vl < (unsigned)b.hi);
+  return above && below;
+}
+
 __host__ __device__ inline InteriorBits interior_bits(double lo, double hi) {
   const double m = (fabs(lo) + fabs(hi)) * 1e-12;
   InteriorBits b;
@@ -201,21 +213,60 @@ __host__ __device__ inline InteriorBits interior_bits(double lo, double hi) {
   return b;
 }
 
-__device__ __forceinline__ bool inside(double v, const InteriorBits& b) {
-  const long long bits = __double_as_longlong(v);
-  return bits > b.lo && bits < b.hi;
+__device__ __forceinline__ bool inside(double v, const InteriorBits& b) { return inside_words(v, b); }
+
+// Row bounds k dx for k = j - 1 .. j + 2 as bit patterns, when every one of those products is an
+// exact double (dx = 1, or any dx whose products with these integers do not round; checked with an
+// FMA) and the lowest is not negative.  Then for a non-negative y, int(y/dx) rounded down equals
+// j - 1, j or j + 1 exactly when the bits of y lie in [b[0], b[1]), [b[1], b[2]) or [b[2], b[3]),
+// which integer compares of the 32-bit words decide without an FP64 instruction.
+struct RowBounds {
+  long long b[4];
+  bool exact;
+};
+
+__device__ __forceinline__ RowBounds row_bounds(int j, double delx) {
+  RowBounds r;
+  r.exact = true;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double kk = (double)(j - 1 + k);
+    const double p = kk * delx;
+    if (fma(kk, delx, -p) != 0.0 || p < 0.0) r.exact = false;
+    r.b[k] = __double_as_longlong(p);
+  }
+  return r;
+}
+
+// a < b for the bit patterns of two non-negative doubles (a may be any double), by 32-bit words
+__device__ __forceinline__ bool bits_less(double v, long long b) {
+  const int vh = __double2hiint(v), bh = (int)(b >> 32);
+  if (vh != bh) return vh < bh;
+  return (unsigned)__double2loint(v) < (unsigned)b;
+}
+
+// jpos - j in {-1, 0, 1} from the exact bounds, or 2 when y lies outside [b[0], b[3])
+__device__ __forceinline__ int row_step(double y, const RowBounds& r) {
+  if (bits_less(y, r.b[1])) return bits_less(y, r.b[0]) ? 2 : -1;
+  if (bits_less(y, r.b[2])) return 0;
+  return bits_less(y, r.b[3]) ? 1 : 2;
 }
 
 InteriorBits x_interior(const Grid2D& g, double delx) {
   return interior_bits((double)g.nxgs * delx, (double)(g.nxgs + g.nx) * delx);
 }
 
+// The exact paths are separate, non-inlined functions: inlined, the compiler turns the rare branch
+// into predicated FP64 instructions that every particle then pays for.
+__device__ __noinline__ int floor_div_rd(double v, double delx) { return (int)__ddiv_rd(v, delx); }
+__device__ __noinline__ int trunc_fp64(double v) { return (int)v; }
+
 __device__ __forceinline__ double wrap_x_periodic(double x, const Grid2D& g, double delx, const InteriorBits& xin,
                                                   bool* changed) {
   const int nxge = g.nxgs + g.nx - 1;
   *changed = false;
   if (inside(x, xin)) return x;
-  const int ipos = (int)__ddiv_rd(x, delx);
+  const int ipos = floor_div_rd(x, delx);
   const double L = __dmul_rd((double)g.nx, delx);
   if (ipos < g.nxgs) { *changed = true; return __dadd_rd(x, L); }
   if (ipos >= nxge + 1) { *changed = true; return __dsub_rd(x, L); }
@@ -299,6 +350,7 @@ void injection2d(const Dev2D& d, const Parts64& P, double u0, double xend, cudaS
 // (species, row).
 // ---------------------------------------------------------------------------
 constexpr int MIG_THREADS = 256;
+constexpr int MIG_PER = 4;  // consecutive slots per thread in k_migrate_scan
 
 // WRAPX: the periodic boundary_periodic__particle_x of the same particle first (the driver calls
 // it right before particle_y), so that one pass over the row does both
@@ -316,57 +368,86 @@ __global__ void __launch_bounds__(MIG_THREADS) k_migrate_scan(Dev2D d, Parts64 P
   // jpos = int(y/dx) rounded down differs from j exactly when y < j dx or y >= (j + 1) dx; farther
   // than 1e-12 of the row's extent from both bounds the division is not needed
   const InteriorBits yin = interior_bits((double)j * delx, (double)(j + 1) * delx);
-  __shared__ int wu[MIG_THREADS / 32], wd[MIG_THREADS / 32];
-  __shared__ int base_u, base_d;
+  const RowBounds yb = row_bounds(j, delx);
+  // a chunk of MIG_THREADS * MIG_PER slots per iteration, slot c0 + q MIG_THREADS + thread
+  // (coalesced loads, MIG_PER of them in flight per thread); the movers' list positions come from
+  // the ballots of each sub-chunk q and the counts of the preceding warps (double-buffered: one
+  // barrier per chunk)
+  __shared__ int wu[2][MIG_PER][MIG_THREADS / 32], wd[2][MIG_PER][MIG_THREADS / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) base_u = base_d = 0;
-  __syncthreads();
-  for (int c0 = 0; c0 < n; c0 += MIG_THREADS) {
-    const int s = c0 + threadIdx.x;
-    int dir = 0;
-    if (s < n) {
-      if (WRAPX) {
+  const unsigned lt = lanemask_lt();
+  int base_u = 0, base_d = 0;  // movers of the chunks before (the same in every thread)
+  int par = 0;
+  for (int c0 = 0; c0 < n; c0 += MIG_THREADS * MIG_PER, par ^= 1) {
+    int dir[MIG_PER];
+    double y[MIG_PER];
+#pragma unroll
+    for (int q = 0; q < MIG_PER; ++q) {
+      const int s = c0 + q * MIG_THREADS + threadIdx.x;
+      y[q] = s < n ? P.y[rb + s] : 0.0;
+    }
+    if (WRAPX) {
+      double x[MIG_PER];
+#pragma unroll
+      for (int q = 0; q < MIG_PER; ++q) {
+        const int s = c0 + q * MIG_THREADS + threadIdx.x;
+        x[q] = s < n ? P.x[rb + s] : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < MIG_PER; ++q) {
+        const int s = c0 + q * MIG_THREADS + threadIdx.x;
+        if (s >= n) continue;
         bool changed;
-        const double x = wrap_x_periodic(P.x[rb + s], g, delx, xin, &changed);
-        if (changed) P.x[rb + s] = x;
+        const double xn = wrap_x_periodic(x[q], g, delx, xin, &changed);
+        if (changed) P.x[rb + s] = xn;
       }
-      double y = P.y[rb + s];
-      const int jpos = inside(y, yin) ? j : (int)__ddiv_rd(y, delx);
-      if (jpos != j) {
-        if (jpos == j + 1) dir = 1;
-        else if (jpos == j - 1) dir = 2;
-        else atomicOr(d.err, EB_MOVED_TOO_FAR);
-        if (dir != 0) {
-          if (jpos <= g.nygs - 1) y = __dadd_rd(y, L);
-          else if (jpos >= nyge + 1) y = __dsub_rd(y, L);
-          P.y[rb + s] = y;
+    }
+    unsigned bu[MIG_PER], bd[MIG_PER];
+#pragma unroll
+    for (int q = 0; q < MIG_PER; ++q) {
+      const int s = c0 + q * MIG_THREADS + threadIdx.x;
+      dir[q] = 0;
+      if (s < n) {
+        int jpos = j;
+        if (!inside(y[q], yin)) {
+          const int st = yb.exact ? row_step(y[q], yb) : 2;
+          jpos = st != 2 ? j + st : floor_div_rd(y[q], delx);
         }
+        if (jpos != j) {
+          if (jpos == j + 1) dir[q] = 1;
+          else if (jpos == j - 1) dir[q] = 2;
+          else atomicOr(d.err, EB_MOVED_TOO_FAR);
+          if (dir[q] != 0) {
+            double yn = y[q];
+            if (jpos <= g.nygs - 1) yn = __dadd_rd(yn, L);
+            else if (jpos >= nyge + 1) yn = __dsub_rd(yn, L);
+            P.y[rb + s] = yn;
+          }
+        }
+        d.mig[rb + s] = (int8_t)dir[q];
       }
-      d.mig[rb + s] = (int8_t)dir;
-    }
-    const unsigned bu = __ballot_sync(0xffffffffu, dir == 1);
-    const unsigned bd = __ballot_sync(0xffffffffu, dir == 2);
-    if (lane == 0) {
-      wu[warp] = __popc(bu);
-      wd[warp] = __popc(bd);
+      bu[q] = __ballot_sync(0xffffffffu, dir[q] == 1);
+      bd[q] = __ballot_sync(0xffffffffu, dir[q] == 2);
+      if (lane == 0) {
+        wu[par][q][warp] = __popc(bu[q]);
+        wd[par][q][warp] = __popc(bd[q]);
+      }
     }
     __syncthreads();
-    int ou = base_u, od = base_d;
-    for (int w = 0; w < warp; ++w) {
-      ou += wu[w];
-      od += wd[w];
-    }
-    const unsigned lt = lanemask_lt();
-    if (dir == 1) d.ulist[rb + ou + __popc(bu & lt)] = s;
-    if (dir == 2) d.dlist[rb + od + __popc(bd & lt)] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < MIG_PER; ++q) {
+      int ou = base_u + __popc(bu[q] & lt), od = base_d + __popc(bd[q] & lt);
+#pragma unroll
       for (int w = 0; w < MIG_THREADS / 32; ++w) {
-        base_u += wu[w];
-        base_d += wd[w];
+        const int a = wu[par][q][w], b = wd[par][q][w];
+        if (w < warp) { ou += a; od += b; }
+        base_u += a;
+        base_d += b;
       }
+      const int s = c0 + q * MIG_THREADS + threadIdx.x;
+      if (dir[q] == 1) d.ulist[rb + ou] = s;
+      if (dir[q] == 2) d.dlist[rb + od] = s;
     }
-    __syncthreads();
   }
   if (threadIdx.x == 0) {
     d.nup[row] = base_u;
@@ -395,14 +476,19 @@ void wrapx_migrate_scan2d(const Dev2D& d, const Parts64& P, cudaStream_t s) {
 //   b >= h : hole m <- arrival m ; slot n+k <- arrival h+k
 //   b <  h : hole m (m < b) <- arrival m ; holes m >= b below n' = n-(h-b) <- the
 //            non-hole slots of [n', n) in descending order ; the row ends at n'.
-// One warp per (species, row) writes slist[t] = source slot of post-migration slot t.
+// One CTA of PW warps per (species, row) writes slist[t] = source slot of post-migration slot t:
+// warp 0 lists the tail stayers (b < h), every warp counts the holes of its chunk of [0, nn), and
+// with the counts of the chunks before it knows each hole's rank m; lanes take 4 consecutive slots.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(32) k_migrate_plan(Dev2D d) {
+constexpr int PW = 8;
+
+__global__ void __launch_bounds__(PW * 32) k_migrate_plan(Dev2D d) {
   const Grid2D g = d.g;
   const int row = blockIdx.x;
   const int isp = row / g.ny, jj = row - isp * g.ny;
   const int rowS = isp * g.ny;
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ int hcnt[PW];
   const size_t cap = d.cap;
   const int n = d.np2[row];
   const int h = d.nup[row] + d.ndown[row];
@@ -424,13 +510,13 @@ __global__ void __launch_bounds__(32) k_migrate_plan(Dev2D d) {
   const int b = c1 + c2;
   int nn = n - h + b;
   if (nn > (int)cap) {
-    if (lane == 0) atomicOr(d.err, EB_CAPACITY);
+    if (threadIdx.x == 0) atomicOr(d.err, EB_CAPACITY);
     nn = (int)cap;
   }
-  if (lane == 0) d.np2new[row] = nn;
+  if (threadIdx.x == 0) d.np2new[row] = nn;
   const size_t rb = (size_t)row * cap;
   const unsigned lt = lanemask_lt();
-  if (b < h) {
+  if (b < h && w == 0) {
     int k = 0;
     for (int t0 = n - 1; t0 >= nn; t0 -= 32) {
       const int t = t0 - lane;
@@ -440,29 +526,55 @@ __global__ void __launch_bounds__(32) k_migrate_plan(Dev2D d) {
       k += __popc(bal);
     }
   }
-  __syncwarp();
+  constexpr int PER = 4 * 32;  // slots per warp iteration
+  const int cs = ((nn + PW - 1) / PW + PER - 1) / PER * PER;
+  const int lo = w * cs, hi = min(nn, lo + cs);
+  auto is_hole = [&](int t) { return t < hi && t < n && d.mig[rb + t] != 0; };
+  int cnt = 0;
+  for (int t4 = lo + 4 * lane; t4 < hi; t4 += PER)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) cnt += is_hole(t4 + q) ? 1 : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if (lane == 0) hcnt[w] = cnt;
+  __syncthreads();  // the chunk counts, and warp 0's tail list, are visible to every warp
   int m0 = 0;
-  for (int t0 = 0; t0 < nn; t0 += 32) {
-    const int t = t0 + lane;
-    const bool act = t < nn;
-    const bool hole = act && t < n && d.mig[rb + t] != 0;
-    const unsigned hb = __ballot_sync(0xffffffffu, hole);
-    const int m = m0 + __popc(hb & lt);
-    if (act) {
-      int src;
+  for (int q = 0; q < w; ++q) m0 += hcnt[q];
+  for (int base = lo; base < hi; base += PER) {
+    const int t4 = base + 4 * lane;
+    bool hole[4];
+    int c = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      hole[q] = is_hole(t4 + q);
+      c += hole[q] ? 1 : 0;
+    }
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int m = m0 + incl - c;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int t = t4 + q;
+      if (t >= hi) continue;
+      int src = 0;
       int a = -1;  // arrival index
       if (t >= n) a = h + (t - n);
-      else if (!hole) src = (int)(rb + t);
+      else if (!hole[q]) src = (int)(rb + t);
       else if (m < b) a = m;
       else src = (int)(rb + d.tlist[rb + (m - b)]);
+      if (hole[q]) ++m;
       if (a >= 0) src = a < c1 ? (int)((size_t)r1 * cap + l1[a]) : (int)((size_t)r2 * cap + l2[a - c1]);
       d.slist[rb + t] = src;
     }
-    m0 += __popc(hb);
+    m0 += __shfl_sync(0xffffffffu, incl, 31);
   }
 }
 
-void migrate_plan2d(const Dev2D& d, cudaStream_t s) { k_migrate_plan<<<d.nrowjob, 32, 0, s>>>(d); }
+void migrate_plan2d(const Dev2D& d, cudaStream_t s) { k_migrate_plan<<<d.nrowjob, PW * 32, 0, s>>>(d); }
 
 // ---------------------------------------------------------------------------
 // sort__bucket (2d/common/sort.f90:36-82): stable counting sort of each row by
@@ -546,14 +658,16 @@ constexpr int SORT_SMEM_MAX = 96 * 1024;
 // int(x) (truncation) of a double by integer operations on its bits, for 0 <= x < 2^30; other
 // values take the FP64 conversion.  Equal to (int)x wherever it answers.
 __device__ __forceinline__ int trunc_double(double x) {
-  const long long b = __double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7ff) - 1023;
-  if (b >= 0 && e < 30) {
+  const int hi = __double2hiint(x);
+  const int e = ((hi >> 20) & 0x7ff) - 1023;
+  if (hi >= 0 && e < 30) {
     if (e < 0) return 0;
-    const long long m = (b & 0x000fffffffffffffLL) | 0x0010000000000000LL;
-    return (int)(m >> (52 - e));
+    const unsigned mh = ((unsigned)hi & 0xfffffu) | 0x100000u;  // implicit bit + top 20 mantissa bits
+    if (e <= 20) return (int)(mh >> (20 - e));
+    const unsigned lo = (unsigned)__double2loint(x);
+    return (int)((mh << (e - 20)) | (lo >> (52 - e)));
   }
-  return (int)x;
+  return trunc_fp64(x);
 }
 
 __global__ void __launch_bounds__(SW * 32) k_sort_rank_mw(Dev2D d, Parts64 P, const int* slist, const int* counts) {
