@@ -425,6 +425,19 @@ def time_adjoint(steps, every, rank, dist, n=512):
     npart = prob.sim.num_particles()
     val_mixed = prob.value_mixed(drift, u_th, amps)
     mix_ms, _ = rank_totals(prob.timings["forward_mixed"] * 1e3, npart, dist, "cuda")
+    # the mixed forward's own sensitivity: central differences at a step where its FP32 rounding
+    # (about 1e-7 of L) is far below the difference it resolves, beside the same differences of
+    # the FP64 forward (their gap is the h^2 truncation, common to both)
+    # (steps h and h/2, Richardson-extrapolated to remove the h^2 truncation)
+    hm = 1e-3
+
+    def cd(f, h):
+        return (f(drift + h, u_th, amps) - f(drift - h, u_th, amps)) / (2 * h)
+
+    fd_mixed_h, fd_mixed_h2 = cd(prob.value_mixed, hm), cd(prob.value_mixed, hm / 2)
+    fd_fp64_h, fd_fp64_h2 = cd(prob.value, hm), cd(prob.value, hm / 2)
+    fd_mixed = (4 * fd_mixed_h2 - fd_mixed_h) / 3
+    fd_fp64_hm = (4 * fd_fp64_h2 - fd_fp64_h) / 3
     prob.close()
     fwd_ms, _ = rank_totals(t_fwd * 1e3, npart, dist, "cuda")
     rec_ms, _ = rank_totals(t_rec * 1e3, npart, dist, "cuda")
@@ -435,10 +448,18 @@ def time_adjoint(steps, every, rank, dist, n=512):
     return {"workload": f"2D Weibel {n}^2 cells, 32 ppc/species ({npart} particles), drift +-0.3c, u_th 0.05c, "
                         f"64 Bz seed modes; L = final magnetic energy after {steps} steps",
             "steps": steps, "checkpoint_every": every, "dtype": "f64", "cg_rtol": 1e-13,
+            "gradient_of": "L of the FP64 forward: both adjoints reverse the recorded FP64 trajectory",
             "forward_ms": fwd_ms, "record_ms": rec_ms, "reverse_ms": rev_ms,
-            "cost_over_forward": (rec_ms + rev_ms) / fwd_ms, "reverse_over_forward": rev_ms / fwd_ms, "L": val,
+            "cost_over_forward": (rec_ms + rev_ms) / fwd_ms, "reverse_over_forward": rev_ms / fwd_ms,
+            "cost_over_mixed_forward": (rec_ms + rev_ms) / mix_ms, "L": val,
             "mixed_forward": {"L": val_mixed, "rel_diff_vs_fp64": abs(val_mixed - val) / abs(val),
-                              "forward_ms": mix_ms, "fp64_over_mixed_time": fwd_ms / mix_ms},
+                              "forward_ms": mix_ms, "fp64_over_mixed_time": fwd_ms / mix_ms,
+                              "fd_drift": {"h": [hm, hm / 2], "richardson": True,
+                                           "fd_mixed": fd_mixed, "fd_fp64": fd_fp64_hm,
+                                           "fd_mixed_h": fd_mixed_h, "fd_fp64_h": fd_fp64_h,
+                                           "mixed_fd_vs_fp64_fd": rel(fd_mixed, fd_fp64_hm),
+                                           "mixed_adjoint_vs_mixed_fd": rel(m_drift, fd_mixed),
+                                           "fp64_adjoint_vs_mixed_fd": rel(g_drift, fd_mixed)}},
             "grad": {"drift": g_drift, "u_th": g_uth, "amps_norm": float(np.linalg.norm(g_amps))},
             "fd_check": {"param": "drift", "h": h, "fd": fd, "adjoint": g_drift,
                          "rel_err": abs(g_drift - fd) / abs(fd) if fd else None},
@@ -446,6 +467,7 @@ def time_adjoint(steps, every, rank, dist, n=512):
                                             "field adjoint, adjoint CG and sums",
                               "record_ms": m_rec_ms, "reverse_ms": m_rev_ms,
                               "cost_over_forward": (m_rec_ms + m_rev_ms) / fwd_ms,
+                              "cost_over_mixed_forward": (m_rec_ms + m_rev_ms) / mix_ms,
                               "rel_diff_vs_fp64_adjoint": {
                                   "drift": rel(m_drift, g_drift), "u_th": rel(m_uth, g_uth),
                                   "amps": float(np.linalg.norm(m_amps - g_amps) / np.linalg.norm(g_amps))},

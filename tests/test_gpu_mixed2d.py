@@ -213,3 +213,61 @@ def test_shock_window_against_fp64(gpu_lib, nsteps):
     em, ed = gm.energy(), gd.energy()
     np.testing.assert_allclose(em, ed, rtol=1e-3, atol=1e-6 * ed.sum())
 
+
+
+def _shock_pair(p, st, gpu_lib, steps, widen_at=None):
+    gm, gd = make(p, "mixed", gpu_lib), make(p, "fp64", gpu_lib)
+    gm.put_state(st)
+    gd.put_state(st)
+    nxe = p.nxe
+    for it in range(steps):
+        if widen_at is not None and it == widen_at:
+            # the driver's relocate() widens the window by an empty cell (2d/proj/shock/app.f90:615-625)
+            nxe += 1
+            gm.set_window(p.nxgs, nxe)
+            gd.set_window(p.nxgs, nxe)
+        gm.step(1)
+        gd.step(1)
+    return gm, gd, nxe
+
+
+def _compare_shock(p, st, gm, gd, tol, nxe):
+    a, b = gm.get_state(), gd.get_state()
+    assert a.np2.sum() == b.np2.sum() == st.np2.sum()
+    pa, pb = by_id(a, p), by_id(b, p)
+    assert pa.keys() == pb.keys()
+    xa = np.array([pa[k] for k in sorted(pa)])
+    xb = np.array([pb[k] for k in sorted(pb)])
+    np.testing.assert_allclose(xa[:, :2], xb[:, :2], rtol=0, atol=tol * p.delx)
+    uscale = np.abs(xb[:, 2:]).max()
+    np.testing.assert_allclose(xa[:, 2:], xb[:, 2:], rtol=0, atol=tol * uscale)
+    assert xa[:, 0].min() >= (p.nxgs + 1) * p.delx and xa[:, 0].max() <= (nxe + 1) * p.delx
+    em, ed = gm.energy(), gd.energy()
+    np.testing.assert_allclose(em, ed, rtol=1e-3, atol=1e-6 * ed.sum())
+
+
+def test_shock_expanding_window_against_fp64(gpu_lib):
+    """The window widened by one cell between steps on a mixed context, as the shock driver's
+    relocate() does: xend and the wall follow the window; six steps within 1e-4 of the FP64
+    shock path with the same widening."""
+    p, st = small_case(nx=32, ny=16, ppc=8, seed=81, bc="shock", window=24, u0=0.2, u_the=0.1)
+    rng = np.random.default_rng(81)
+    st.uf[...] = np.pad(0.02 * rng.standard_normal((6, p.nx, p.ny)), ((0, 0), (2, 2), (2, 2)), mode="wrap")
+    gm, gd, nxe = _shock_pair(p, st, gpu_lib, 6, widen_at=3)
+    _compare_shock(p, st, gm, gd, 1e-4, nxe)
+
+
+@pytest.mark.parametrize("nsteps", [1, 8])
+def test_shock_far_window_against_fp64(gpu_lib, nsteps):
+    """A window of 4100 cells with the plasma streaming hot towards the injection end (u0 < 0:
+    drift +0.2c, u_th 0.3c): the particles reflected there, near x = 4100 cells, keep the split
+    representation's precision (the mirror image is formed from the integer cells and the FP32
+    offsets separately), within 1e-5 (one step) / 1e-4 (eight steps) of the FP64 path."""
+    p, st = small_case(nx=4112, ny=16, ppc=2, seed=83, bc="shock", window=4100, u0=-0.2, u_the=0.3)
+    gm, gd, nxe = _shock_pair(p, st, gpu_lib, nsteps)
+    _compare_shock(p, st, gm, gd, 1e-5 if nsteps == 1 else 1e-4, nxe)
+    if nsteps > 1:  # particles crossed the loaded plasma's edge into the cells before xend
+        b = gd.get_state()
+        far = sum(int((b.up[0, :b.np2[j, s], j, s] >= (p.nxgs + p.window - 2) * p.delx).sum())
+                  for s in range(p.nsp) for j in range(p.ny))
+        assert far > 0

@@ -224,3 +224,31 @@ def test_mixed3d_moments_against_oracle(gpu_lib):
             np.testing.assert_allclose(mom[l, ..., isp], ref[l, ..., isp], rtol=0, atol=2e-5 * scale)
     after = m.get_state()
     np.testing.assert_array_equal(after.up, cur.up)
+
+
+def test_mixed3d_shock_expanding_window_against_fp64(gpu_lib):
+    """The window widened by one cell after three steps on a mixed 3D context, as the shock
+    driver's relocate() does (3d/proj/shock/app.f90:654); six steps within 1e-4 of the FP64
+    shock path with the same widening, energies within 1e-3."""
+    p, st = shock_perturbed(80)
+    m, f = make(p, "mixed"), make(p, "fp64")
+    m.put_state(st)
+    f.put_state(st)
+    nxe = p.nxe
+    for it in range(6):
+        if it == 3:
+            nxe += 1
+            m.set_window(p.nxgs, nxe)
+            f.set_window(p.nxgs, nxe)
+        m.step(1)
+        f.step(1)
+    sm, sf = m.get_state(), f.get_state()
+    assert sm.np2.sum() == sf.np2.sum() == st.np2.sum()
+    a, b = by_id(sm), by_id(sf)
+    np.testing.assert_array_equal(a[6], b[6])
+    np.testing.assert_allclose(a[:3], b[:3], rtol=0, atol=1e-4 * p.delx)
+    umax = np.abs(b[3:6]).max()
+    np.testing.assert_allclose(a[3:6], b[3:6], rtol=0, atol=1e-4 * umax)
+    assert a[0].min() >= (p.nxgs + 1) * p.delx and a[0].max() <= (nxe + 1) * p.delx
+    em, ef = m.energy(), f.energy()
+    np.testing.assert_allclose(em, ef, rtol=1e-3, atol=1e-6 * ef.sum())

@@ -387,7 +387,14 @@ double shock_xend(const wpic_ctx* c, double u0);
 int mixed_step(wpic_ctx* c) {
   Dev2D& d = c->d;
   if (d.ph.bc == BC_SHOCK) {  // the injection boundary inside the push kernel, in cells from nxgs
-    d.m.k_xend = (float)(shock_xend(c, c->u0) * d.ph.d_delx - (double)d.g.nxgs);
+    const double xe = shock_xend(c, c->u0) * d.ph.d_delx - (double)d.g.nxgs;
+    const double fl = std::floor(xe);
+    d.m.k_xend_cell = (int)fl;
+    d.m.k_xend_frac = (float)(xe - fl);
+    if (d.m.k_xend_frac >= 1.f) {
+      d.m.k_xend_frac = 0.f;
+      d.m.k_xend_cell += 1;
+    }
     d.m.k_u0 = (float)c->u0;
   }
   stage_begin(c, SG_PUSH);

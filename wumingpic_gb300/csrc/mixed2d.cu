@@ -101,6 +101,16 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Mirror image X' = 2 W - X of the position X = cell + off about W = wc + wf (wf in [0, 1)), in
+// split form: the integer parts cancel exactly and only the fractions are rounded.
+__device__ __forceinline__ void reflect_split(int& cell, float& off, int wc, float wf) {
+  const float r = (wf - off) + wf;  // in (-1, 2)
+  const float fr = floorf(r);
+  cell = 2 * wc - cell + (int)fr;
+  off = r - fr;
+  if (off >= 1.f) { off = 0.f; cell += 1; }
+}
+
 // direction code d = (dy + 1) * 3 + (dx + 1) of a move (4 = same cell) -> group index 0..7
 __device__ __forceinline__ int dir_group(int d) { return d < 4 ? d : d - 1; }
 
@@ -358,27 +368,26 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
       // the shock window instead: reflection about cell wx0 + 1 with the momenta reversed, and
       // beyond xend x -> 2 xend - x, u_x -> 2 u0 - u_x, u_y and u_z reversed
       // (boundary_shock__injection, 2d/proj/shock/boundary_shock.f90:255-297)
+      // the mirror image X' = 2 W - X in split form (cell + offset): the integer parts cancel
+      // exactly and only the offsets round, so a reflected particle keeps the offset's precision
       const int gx0 = tx * MIX_TS + lx;
-      const int gxn = gx0 + incx;
-      float X = (float)gxn + nx_;
+      int gxn = gx0 + incx;
       const bool shock = d.ph.bc == BC_SHOCK;
       const int lo_wall = shock ? g.wx0 + 1 : 1;
       bool flip = false;
       if (gxn < lo_wall) {
-        X = 2.f * (float)lo_wall - X;
+        reflect_split(gxn, nx_, lo_wall, 0.f);
         ux = -ux;
         flip = true;
-      } else if (shock ? X > m.k_xend : gxn >= g.nx - 2) {
-        X = (shock ? 2.f * m.k_xend : 2.f * (float)(g.nx - 2)) - X;
+      } else if (shock ? (gxn > m.k_xend_cell || (gxn == m.k_xend_cell && nx_ > m.k_xend_frac)) : gxn >= g.nx - 2) {
+        if (shock) reflect_split(gxn, nx_, m.k_xend_cell, m.k_xend_frac);
+        else reflect_split(gxn, nx_, g.nx - 2, 0.f);
         ux = shock ? 2.f * m.k_u0 - ux : -ux;
         flip = true;
       }
       if (flip) {
         uy = -uy; uz = -uz;
-        const float fX = floorf(X);
-        nx_ = X - fX;
-        incx = (int)fX - gx0;
-        if (nx_ >= 1.f) { nx_ = 0.f; incx += 1; }
+        incx = gxn - gx0;
         if (incx < -1 || incx > 1) {
           atomicOr(d.err, EB_MOVED_TOO_FAR);
           incx = max(-1, min(1, incx));

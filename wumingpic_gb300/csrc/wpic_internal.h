@@ -96,7 +96,9 @@ struct Mix2D {
   // per species q/r dt/2, q dt/r, q dx/dt, q; then dt/dx, c, 1/c^2
   float k_fac1[2], k_fac2[2], k_qdd[2], k_q[2];
   float k_dtdx, k_c, k_ic2;
-  float k_xend, k_u0;  // shock: the injection end in cells from nxgs, and u0 (set every step)
+  int k_xend_cell;     // shock: the injection end in cells from nxgs as an integer cell and an FP32
+  float k_xend_frac;   // fraction in [0, 1), and u0 (set every step)
+  float k_u0;
   int ntx, nty, ntile, nbin;
   float* P;            // particle layers, MIX_PL words each
   long long* boff;     // [nbin] first layer of each bin
