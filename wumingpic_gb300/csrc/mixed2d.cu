@@ -50,6 +50,11 @@ constexpr unsigned long long kSpinLimit = 1ull << 22;  // a few seconds at most
 #ifndef WPIC_MIX_MINB
 #define WPIC_MIX_MINB 2
 #endif
+// 1: the push with a register current for the particles that stay in their cell and a per-warp
+// queue for the ones that leave (k_mix_push2); 0: the full-stencil register push (k_mix_push)
+#ifndef WPIC_MIX_PUSH2
+#define WPIC_MIX_PUSH2 1
+#endif
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -507,12 +512,459 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
   }
 }
 
+// ---------------------------------------------------------------------------
+// The push with the register current for the particles that stay in their cell only
+// (WPIC_MIX_PUSH2): a stayer's Esirkepov support is its cell's 3 x 3 nodes, so 21 registers
+// hold it (2 x 3 x-edges, 3 x 2 y-edges, 3 x 3 z-nodes); a particle that changes cell (about 1 in
+// 10 per step) joins its warp's queue and 32 of them are deposited at a time, one lane each,
+// straight into the tile's fixed-point current.  With the smaller stencil and shared memory laid
+// out for it (the TMA staging area becomes the queue and the pending leavers once the
+// cell-centred fields exist), three CTAs of 256 threads share an SM.
+// ---------------------------------------------------------------------------
+constexpr int PF2 = 4;                           // particles in flight per thread
+constexpr int LQ2 = 64;                          // leaver queue entries per warp
+constexpr int LQ2W = 6;                          // ox, oy, new ox, new oy, q vz, packed (inc, species, cell)
+constexpr int LQ2_BYTES = (MP_THREADS / 32) * LQ2W * LQ2 * 4;
+constexpr int PEND2_BYTES = 9 * MP_THREADS * 4;  // per thread: new column (packed) + the 8 words
+constexpr int STAGE2_BYTES = 6 * TW * TW * 8;
+constexpr int A2_BYTES = (STAGE2_BYTES > LQ2_BYTES + PEND2_BYTES ? STAGE2_BYTES : LQ2_BYTES + PEND2_BYTES);
+constexpr int OFF2_J = (A2_BYTES + 127) / 128 * 128;
+constexpr int OFF2_SFA = OFF2_J + 2 * 3 * TW * TW * 4;
+constexpr int OFF2_SFB = OFF2_SFA + TT * TT * 16;
+constexpr int OFF2_RING = OFF2_SFB + TT * TT * 8;
+constexpr int PUSH2_SMEM = OFF2_RING + PF2 * 7 * MIX_TC * 4;
+static_assert(OFF2_SFA % 16 == 0 && OFF2_RING % 16 == 0, "shared-memory alignment");
+
+// Esirkepov current of one cell-leaver on the 5 x 5 stencil of its old cell (lx, ly), each value
+// added to the tile's fixed-point planes (pitch TW); the same arithmetic as the register path
+__device__ __forceinline__ void deposit_leaver2(float ox, float oy, float px_, float py_, int incx, int incy,
+                                                int lx, int ly, float qdd, float qg, int* jhi, int* jlo, float s1,
+                                                float is1, float s2) {
+  const float third = 1.0f / 3.0f;
+  float dsx[5], dsy[5];
+  shape_diff5(ox, px_, incx, dsx);
+  shape_diff5(oy, py_, incy, dsy);
+  const float sx0 = 0.5f * (1.f - ox) * (1.f - ox), sx1 = 0.75f - (ox - 0.5f) * (ox - 0.5f), sx2 = 0.5f * ox * ox;
+  const float sy0 = 0.5f * (1.f - oy) * (1.f - oy), sy1 = 0.75f - (oy - 0.5f) * (oy - 0.5f), sy2 = 0.5f * oy * oy;
+  const float s0x[5] = {0.f, sx0, sx1, sx2, 0.f};
+  const float s0y[5] = {0.f, sy0, sy1, sy2, 0.f};
+  const float hq = -0.5f * qdd, hg = 0.5f * qg, tg = third * qg;
+  float wyq[5], wxq[5], zy[5], vy[5];
+#pragma unroll
+  for (int e = 0; e < 5; ++e) {
+    if (e == 0 || e == 4) {
+      wyq[e] = hq * dsy[e];
+      wxq[e] = hq * dsx[e];
+      zy[e] = hg * dsy[e];
+      vy[e] = tg * dsy[e];
+    } else {
+      wyq[e] = -qdd * (s0y[e] + 0.5f * dsy[e]);
+      wxq[e] = -qdd * (s0x[e] + 0.5f * dsx[e]);
+      zy[e] = qg * (s0y[e] + 0.5f * dsy[e]);
+      vy[e] = qg * (0.5f * s0y[e] + third * dsy[e]);
+    }
+  }
+  float px = 0.f, py = 0.f;
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk) {
+    px += dsx[kk];
+    py += dsy[kk];
+#pragma unroll
+    for (int e = 0; e < 5; ++e) {
+      const float vx = px * wyq[e], vyv = py * wxq[e];
+      if (vx != 0.f) {
+        const int w = (0 * TW + ly + e) * TW + lx + kk + 1;
+        fx_add(jhi + w, jlo + w, vx, s1, is1, s2);
+      }
+      if (vyv != 0.f) {
+        const int w = (1 * TW + ly + kk + 1) * TW + lx + e;
+        fx_add(jhi + w, jlo + w, vyv, s1, is1, s2);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 5; ++j)
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const float v = dsx[i] * vy[j] + s0x[i] * zy[j];
+      if (v != 0.f) {
+        const int w = (2 * TW + ly + j) * TW + lx + i;
+        fx_add(jhi + w, jlo + w, v, s1, is1, s2);
+      }
+    }
+}
+
+struct StayCurrent {
+  float jx[2][3], jy[2][3], jz[3][3];
+};
+
+__device__ __forceinline__ void stay_zero(StayCurrent& a) {
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+#pragma unroll
+    for (int e = 0; e < 3; ++e) a.jx[k][e] = a.jy[k][e] = 0.f;
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) a.jz[j][i] = 0.f;
+}
+
+// x-edge (k, e) of the register stencil at patch node (lx + k + 2, ly + e + 1); y-edge (k, e) at
+// (lx + e + 1, ly + k + 2); z (j, i) at (lx + i + 1, ly + j + 1)
+__device__ __forceinline__ void stay_flush(StayCurrent& a, int* jhi, int* jlo, int lx, int ly, float s1, float is1,
+                                           float s2) {
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const int wx = (0 * TW + ly + e + 1) * TW + lx + k + 2;
+      const int wy = (1 * TW + ly + k + 2) * TW + lx + e + 1;
+      fx_add(jhi + wx, jlo + wx, a.jx[k][e], s1, is1, s2);
+      fx_add(jhi + wy, jlo + wy, a.jy[k][e], s1, is1, s2);
+    }
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const int w = (2 * TW + ly + j + 1) * TW + lx + i + 1;
+      fx_add(jhi + w, jlo + w, a.jz[j][i], s1, is1, s2);
+    }
+  stay_zero(a);
+}
+
+template <bool VAY>
+__global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __grid_constant__ CUtensorMap tm) {
+  extern __shared__ __align__(128) unsigned char smem2[];
+  double(*suf)[TW][TW] = reinterpret_cast<double(*)[TW][TW]>(smem2);
+  float* const lqueue = reinterpret_cast<float*>(smem2);               // [warp][LQ2W][LQ2], after staging
+  float* const pend = reinterpret_cast<float*>(smem2 + LQ2_BYTES);      // [9][256], after staging
+  int* const jhi = reinterpret_cast<int*>(smem2 + OFF2_J);             // [3][TW][TW]
+  int* const jlo = jhi + 3 * TW * TW;
+  float4* const sfa = reinterpret_cast<float4*>(smem2 + OFF2_SFA);     // (Bx, By, Bz, Ex) at cell centres
+  float2* const sfb = reinterpret_cast<float2*>(smem2 + OFF2_SFB);     // (Ey, Ez)
+  float* const ring = reinterpret_cast<float*>(smem2 + OFF2_RING);     // [PF2][7][256]
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ int nb_bin[2][9], nb_dep[2][9];
+  __shared__ long long nb_off[2][9];
+  const Mix2D& m = d.m;
+  const int tile = blockIdx.x;
+  const int tx = tile % m.ntx, ty = tile / m.ntx;
+  const Grid2D g = d.g;
+  const int c = threadIdx.x;
+  const int lane = c & 31;
+  const int nsp = d.ph.nsp;
+  const int bin0 = tile * nsp;
+  const int n0 = m.cnt[bin0 * MIX_TC + c];
+  const int ntot = n0 + (nsp > 1 ? m.cnt[(bin0 + 1) * MIX_TC + c] : 0);
+  if (c < 2 * 9) {
+    const int s = c / 9, q = c % 9;
+    int ntx_ = tx + q % 3 - 1, nty_ = ty + q / 3 - 1;
+    if (ntx_ < 0) ntx_ += m.ntx; else if (ntx_ >= m.ntx) ntx_ -= m.ntx;
+    if (nty_ < 0) nty_ += m.nty; else if (nty_ >= m.nty) nty_ -= m.nty;
+    const int b = (nty_ * m.ntx + ntx_) * nsp + (s < nsp ? s : 0);
+    nb_bin[s][q] = b;
+    nb_dep[s][q] = m.bdep[b];
+    nb_off[s][q] = m.boff[b];
+  }
+  float* const col0 = mix_slot(m, bin0, 0, c);
+  float* const col1 = mix_slot(m, bin0 + (nsp > 1 ? 1 : 0), 0, c) - (size_t)n0 * MIX_PL;
+  auto issue = [&](int t) {
+    if (t < ntot) {
+      const float* src = (t < n0 ? col0 : col1) + (size_t)t * MIX_PL;
+      float* dst = ring + (t & (PF2 - 1)) * 7 * MIX_TC + c;
+#pragma unroll
+      for (int a = 0; a < 7; ++a) cp_async4(dst + a * MIX_TC, src + a * MIX_TC);
+    }
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int t = 0; t < PF2; ++t) issue(t);
+  if (c == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (c == 0) {
+    mbar_expect_tx(&bar, (unsigned)STAGE2_BYTES);
+    tma_load_3d(&suf[0][0][0], &tm, tx * MIX_TS, ty * MIX_TS, 0, &bar);
+  }
+  // every thread waits (bounded) for the tile; the CTA gives up together if any wait ran out
+  const bool staged = mbar_wait_bounded(&bar);
+  if (!__syncthreads_and(staged)) {
+    if (c == 0) atomicOr(d.err, EB_STAGING_TIMEOUT);
+    if (!staged) mbar_wait_bounded(&bar);
+    cp_async_wait<0>();
+    return;
+  }
+  for (int k = c; k < TT * TT; k += MP_THREADS) {
+    const int r = k / TT + 1, cc = k % TT + 1;
+    sfa[k] = make_float4((float)(0.5 * (suf[0][r][cc] + suf[0][r + 1][cc])),
+                         (float)(0.5 * (suf[1][r][cc] + suf[1][r][cc + 1])),
+                         (float)(0.25 * (suf[2][r][cc] + suf[2][r][cc + 1] + suf[2][r + 1][cc] + suf[2][r + 1][cc + 1])),
+                         (float)(0.5 * (suf[3][r][cc] + suf[3][r][cc + 1])));
+    sfb[k] = make_float2((float)(0.5 * (suf[4][r][cc] + suf[4][r + 1][cc])), (float)suf[5][r][cc]);
+  }
+  for (int k = c; k < 2 * 3 * TW * TW; k += MP_THREADS) jhi[k] = 0;
+  __syncthreads();  // the staging area is free from here on (queue and pending leavers)
+  const float fs1 = m.fx_s1, fs2 = m.fx_s2, fis1 = m.fx_is1f;
+  const int lx = c & (MIX_TS - 1), ly = c >> 4;
+  const float dtdx = m.k_dtdx;
+  const float cl = m.k_c;
+  const float ic2 = m.k_ic2;
+  const float third = 1.0f / 3.0f;
+  const bool walls = d.ph.bc != BC_PERIODIC;
+  const int f0 = ly * TT + lx;
+  StayCurrent acc;
+  stay_zero(acc);
+  float* const myq = lqueue + (c >> 5) * LQ2W * LQ2;
+  int qhead = 0, qtail = 0;  // the warp's leaver queue (warp-uniform)
+  auto drain = [&](int cnt) {
+    if (lane < cnt) {
+      const int e = (qhead + lane) & (LQ2 - 1);
+      const int pk = __float_as_int(myq[5 * LQ2 + e]);
+      const int cc = pk >> 8;
+      deposit_leaver2(myq[0 * LQ2 + e], myq[1 * LQ2 + e], myq[2 * LQ2 + e], myq[3 * LQ2 + e], (pk & 3) - 1,
+                      ((pk >> 2) & 3) - 1, cc & (MIX_TS - 1), cc >> 4, (pk >> 4) & 1 ? m.k_qdd[1] : m.k_qdd[0],
+                      myq[4 * LQ2 + e], jhi, jlo, fs1, fis1, fs2);
+    }
+    qhead += cnt;
+    __syncwarp();
+  };
+  // the pending leaver of this thread (its slot in the new column returned by the last iteration's
+  // atomic): arrival number pos goes to slot depth - 1 - pos
+  auto place = [&](int pos) {
+    const int dst = __float_as_int(pend[8 * MP_THREADS + c]);
+    const int q = dst & 15, s = (dst >> 4) & 1, dlc = dst >> 8;
+    const int dep = nb_dep[s][q];
+    if (pos >= dep) {
+      atomicOr(d.err, EB_CAPACITY);
+      return;
+    }
+    float* io = m.P + ((size_t)nb_off[s][q] + dep - 1 - pos) * MIX_PL + dlc;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) io[a * MIX_TC] = pend[a * MP_THREADS + c];
+  };
+  int j0 = 0, j1 = 0;
+  int ppos = -1;
+  int tw = ntot;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) tw = max(tw, __shfl_xor_sync(0xffffffffu, tw, o));
+  for (int t = 0; t < tw; ++t) {
+    cp_async_wait<PF2 - 1>();
+    if (ppos >= 0) place(ppos);
+    ppos = -1;
+    bool leaves = false;
+    float lq0 = 0.f, lq1 = 0.f, lq2 = 0.f, lq3 = 0.f, lq4 = 0.f;
+    int lpk = 0;
+    if (t < ntot) {
+      const bool sp1 = t >= n0;
+      const int k = sp1 ? t - n0 : t;
+      const float* pb = ring + (t & (PF2 - 1)) * 7 * MIX_TC + c;
+      const float ox = pb[MIX_OX], oy = pb[MIX_OY];
+      float ux = pb[MIX_UX], uy = pb[MIX_UY], uz = pb[MIX_UZ];
+      const float idlo = pb[MIX_IDLO], idhi = pb[MIX_IDHI];
+      const float fac1 = sp1 ? m.k_fac1[1] : m.k_fac1[0];
+      const float fac2 = sp1 ? m.k_fac2[1] : m.k_fac2[0];
+      const float qdd = sp1 ? m.k_qdd[1] : m.k_qdd[0];
+      const float qs = sp1 ? m.k_q[1] : m.k_q[0];
+      const float txxx = fac1 * fac1;
+      const float sx0 = 0.5f * (1.f - ox) * (1.f - ox), sx1 = 0.75f - (ox - 0.5f) * (ox - 0.5f), sx2 = 0.5f * ox * ox;
+      const float sy0 = 0.5f * (1.f - oy) * (1.f - oy), sy1 = 0.75f - (oy - 0.5f) * (oy - 0.5f), sy2 = 0.5f * oy * oy;
+      float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int jy = 0; jy < 3; ++jy) {
+        const float wy = jy == 0 ? sy0 : (jy == 1 ? sy1 : sy2);
+#pragma unroll
+        for (int jx = 0; jx < 3; ++jx) {
+          const float w = wy * (jx == 0 ? sx0 : (jx == 1 ? sx1 : sx2));
+          const float4 a = sfa[f0 + jy * TT + jx];
+          const float2 b = sfb[f0 + jy * TT + jx];
+          ffma2_into(f[0], f[1], w, w, a.x, a.y);
+          ffma2_into(f[2], f[3], w, w, a.z, a.w);
+          ffma2_into(f[4], f[5], w, w, b.x, b.y);
+        }
+      }
+      const float bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
+      float ig;
+      if constexpr (VAY) {
+        const float fac1r = fac1 * rsqrtf(cl * cl + ux * ux + uy * uy + uz * uz);
+        const float u4 = ux + fac2 * epx + fac1r * (uy * bpz - uz * bpy);
+        const float u5 = uy + fac2 * epy + fac1r * (uz * bpx - ux * bpz);
+        const float u6 = uz + fac2 * epz + fac1r * (ux * bpy - uy * bpx);
+        const float icl = ic2 * cl;
+        const float tx_ = fac1 * bpx * icl, ty_ = fac1 * bpy * icl, tz_ = fac1 * bpz * icl;
+        const float tau2 = tx_ * tx_ + ty_ * ty_ + tz_ * tz_;
+        const float ua = (u4 * tx_ + u5 * ty_ + u6 * tz_) * icl;
+        const float sigma = 1.f + (u4 * u4 + u5 * u5 + u6 * u6) * ic2 - tau2;
+        const float gam2 = 0.5f * (sigma + sqrtf(sigma * sigma + 4.f * (tau2 + ua * ua)));
+        ig = rsqrtf(gam2);
+        const float gv = gam2 * ig;
+        const float tt = __fdividef(1.f, tau2 + gam2);
+        ux = tt * (gam2 * u4 + cl * ua * tx_ + gv * (u5 * tz_ - u6 * ty_));
+        uy = tt * (gam2 * u5 + cl * ua * ty_ + gv * (u6 * tx_ - u4 * tz_));
+        uz = tt * (gam2 * u6 + cl * ua * tz_ + gv * (u4 * ty_ - u5 * tx_));
+      } else {
+        float u1 = ux + fac1 * epx, u2 = uy + fac1 * epy, u3 = uz + fac1 * epz;
+        const float g2 = cl * cl + u1 * u1 + u2 * u2 + u3 * u3;
+        const float igam = rsqrtf(g2);
+        const float gm = g2 * igam;
+        const float fac1r = fac1 * igam;
+        const float fac2r = __fdividef(fac2, gm + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
+        const float u4 = u1 + fac1r * (u2 * bpz - u3 * bpy);
+        const float u5 = u2 + fac1r * (u3 * bpx - u1 * bpz);
+        const float u6 = u3 + fac1r * (u1 * bpy - u2 * bpx);
+        u1 = u1 + fac2r * (u5 * bpz - u6 * bpy);
+        u2 = u2 + fac2r * (u6 * bpx - u4 * bpz);
+        u3 = u3 + fac2r * (u4 * bpy - u5 * bpx);
+        ux = u1 + fac1 * epx;
+        uy = u2 + fac1 * epy;
+        uz = u3 + fac1 * epz;
+        ig = rsqrtf(1.f + (ux * ux + uy * uy + uz * uz) * ic2);
+      }
+      float nx_ = ox + ux * dtdx * ig, ny_ = oy + uy * dtdx * ig;
+      int incx = 0, incy = 0;
+      if (nx_ >= 1.f) { nx_ -= 1.f; incx = 1; } else if (nx_ < 0.f) { nx_ += 1.f; incx = -1; }
+      if (ny_ >= 1.f) { ny_ -= 1.f; incy = 1; } else if (ny_ < 0.f) { ny_ += 1.f; incy = -1; }
+      if (nx_ >= 1.f) { nx_ = 0.f; incx += 1; }
+      if (ny_ >= 1.f) { ny_ = 0.f; incy += 1; }
+      if (nx_ < 0.f || nx_ >= 1.f || ny_ < 0.f || ny_ >= 1.f) {
+        atomicOr(d.err, EB_MOVED_TOO_FAR);
+        nx_ = fminf(fmaxf(nx_, 0.f), 0.99999994f);
+        ny_ = fminf(fmaxf(ny_, 0.f), 0.99999994f);
+      }
+      if (walls) {
+        const int gx0 = tx * MIX_TS + lx;
+        int gxn = gx0 + incx;
+        const bool shock = d.ph.bc == BC_SHOCK;
+        const int lo_wall = shock ? g.wx0 + 1 : 1;
+        bool flip = false;
+        if (gxn < lo_wall) {
+          reflect_split(gxn, nx_, lo_wall, 0.f);
+          ux = -ux;
+          flip = true;
+        } else if (shock ? (gxn > m.k_xend_cell || (gxn == m.k_xend_cell && nx_ > m.k_xend_frac)) : gxn >= g.nx - 2) {
+          if (shock) reflect_split(gxn, nx_, m.k_xend_cell, m.k_xend_frac);
+          else reflect_split(gxn, nx_, g.nx - 2, 0.f);
+          ux = shock ? 2.f * m.k_u0 - ux : -ux;
+          flip = true;
+        }
+        if (flip) {
+          uy = -uy; uz = -uz;
+          incx = gxn - gx0;
+          if (incx < -1 || incx > 1) {
+            atomicOr(d.err, EB_MOVED_TOO_FAR);
+            incx = max(-1, min(1, incx));
+          }
+        }
+      }
+      const float qg = qs * uz * ig;  // q * vz
+      leaves = (incx | incy) != 0;
+      if (leaves) {
+        const int nlx = lx + incx, nly = ly + incy;
+        const int q = ((nly >> 4) + 1) * 3 + ((nlx >> 4) + 1);
+        const int s = sp1 ? 1 : 0;
+        const int dlc = (nly & (MIX_TS - 1)) * MIX_TS + (nlx & (MIX_TS - 1));
+        ppos = atomicAdd(&m.acnt[nb_bin[s][q] * MIX_TC + dlc], 1);  // used in the next iteration
+        pend[0 * MP_THREADS + c] = nx_;
+        pend[1 * MP_THREADS + c] = ny_;
+        pend[2 * MP_THREADS + c] = ux;
+        pend[3 * MP_THREADS + c] = uy;
+        pend[4 * MP_THREADS + c] = uz;
+        pend[5 * MP_THREADS + c] = idlo;
+        pend[6 * MP_THREADS + c] = idhi;
+        pend[7 * MP_THREADS + c] = __int_as_float((dir_group((incy + 1) * 3 + (incx + 1)) << 16) | k);
+        pend[8 * MP_THREADS + c] = __int_as_float(q | (s << 4) | (dlc << 8));
+        lq0 = ox; lq1 = oy; lq2 = nx_; lq3 = ny_; lq4 = qg;
+        lpk = (incx + 1) | ((incy + 1) << 2) | ((sp1 ? 1 : 0) << 4) | (c << 8);
+      } else {
+        float* so = (sp1 ? col1 + (size_t)n0 * MIX_PL : col0) + (size_t)(sp1 ? j1 : j0) * MIX_PL;
+        so[MIX_OX] = nx_;
+        so[MIX_OY] = ny_;
+        so[MIX_UX] = ux;
+        so[MIX_UY] = uy;
+        so[MIX_UZ] = uz;
+        so[MIX_IDLO] = idlo;
+        so[MIX_IDHI] = idhi;
+        if (sp1) ++j1; else ++j0;
+        // Esirkepov on the cell's 3 x 3 nodes: the factored spline differences of a move inside
+        // the cell (2d/common/field.f90:223-298)
+        const float dlx = nx_ - ox, spx = ox + nx_, dly = ny_ - oy, spy = oy + ny_;
+        const float dsx[3] = {-0.5f * dlx * (2.f - spx), -dlx * (spx - 1.f), 0.5f * dlx * spx};
+        const float dsy[3] = {-0.5f * dly * (2.f - spy), -dly * (spy - 1.f), 0.5f * dly * spy};
+        const float s0x[3] = {sx0, sx1, sx2}, s0y[3] = {sy0, sy1, sy2};
+        const float px[2] = {dsx[0], dsx[0] + dsx[1]}, py[2] = {dsy[0], dsy[0] + dsy[1]};
+        float wyq[3], wxq[3], zy[3], vy[3];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          wyq[e] = -qdd * (s0y[e] + 0.5f * dsy[e]);
+          wxq[e] = -qdd * (s0x[e] + 0.5f * dsx[e]);
+          zy[e] = qg * (s0y[e] + 0.5f * dsy[e]);
+          vy[e] = qg * (0.5f * s0y[e] + third * dsy[e]);
+        }
+#pragma unroll
+        for (int kk = 0; kk < 2; ++kk)
+#pragma unroll
+          for (int e = 0; e < 3; ++e) {
+            acc.jx[kk][e] = fmaf(px[kk], wyq[e], acc.jx[kk][e]);
+            acc.jy[kk][e] = fmaf(py[kk], wxq[e], acc.jy[kk][e]);
+          }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          ffma2_into(acc.jz[j][0], acc.jz[j][1], dsx[0], dsx[1], vy[j], vy[j]);
+          acc.jz[j][2] = fmaf(dsx[2], vy[j], acc.jz[j][2]);
+          ffma2_into(acc.jz[j][0], acc.jz[j][1], s0x[0], s0x[1], zy[j], zy[j]);
+          acc.jz[j][2] = fmaf(s0x[2], zy[j], acc.jz[j][2]);
+        }
+      }
+    }
+    // leavers join the warp's queue; with 32 waiting they are deposited one per lane
+    const unsigned lm = __ballot_sync(0xffffffffu, leaves);
+    if (leaves) {
+      const int e = (qtail + __popc(lm & ((1u << lane) - 1u))) & (LQ2 - 1);
+      myq[0 * LQ2 + e] = lq0;
+      myq[1 * LQ2 + e] = lq1;
+      myq[2 * LQ2 + e] = lq2;
+      myq[3 * LQ2 + e] = lq3;
+      myq[4 * LQ2 + e] = lq4;
+      myq[5 * LQ2 + e] = __int_as_float(lpk);
+    }
+    qtail += __popc(lm);
+    __syncwarp();
+    if (qtail - qhead >= 32) drain(32);
+    if ((t & (FLUSH_EVERY - 1)) == FLUSH_EVERY - 1) stay_flush(acc, jhi, jlo, lx, ly, fs1, fis1, fs2);
+    issue(t + PF2);
+  }
+  cp_async_wait<0>();
+  if (ppos >= 0) place(ppos);
+  if (qtail > qhead) drain(qtail - qhead);
+  m.ccnt[bin0 * MIX_TC + c] = j0;
+  if (nsp > 1) m.ccnt[(bin0 + 1) * MIX_TC + c] = j1;
+  if (tw & (FLUSH_EVERY - 1)) stay_flush(acc, jhi, jlo, lx, ly, fs1, fis1, fs2);
+  __syncthreads();
+  for (int k = c; k < 3 * TW * TW; k += MP_THREADS) {
+    const int ih = jhi[k], il = jlo[k];
+    if ((ih | il) == 0) continue;
+    const long long v = (long long)ih * 32768LL + (long long)il;
+    const int comp = k / (TW * TW), r = (k / TW) % TW, cc = k % TW;
+    int gx = tx * MIX_TS + cc - 2, gy = ty * MIX_TS + r - 2;
+    if (gy < 0) gy += g.ny; else if (gy >= g.ny) gy -= g.ny;
+    if (!walls) {
+      if (gx < 0) gx += g.nx; else if (gx >= g.nx) gx -= g.nx;
+    }
+    atomicAdd(&m.ujx[(size_t)comp * g.fplane + (size_t)(gy + 2) * g.fp + gx + 2], (unsigned long long)v);
+  }
+}
+
 void mix_push_deposit2d(const Dev2D& d, const void* tmap, bool vay, cudaStream_t s) {
   cudaMemsetAsync(d.m.ujx, 0, sizeof(unsigned long long) * 3 * (size_t)d.g.fplane, s);
+#if WPIC_MIX_PUSH2
+  if (vay)
+    k_mix_push2<true><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, *(const CUtensorMap*)tmap);
+  else
+    k_mix_push2<false><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, *(const CUtensorMap*)tmap);
+#else
   if (vay)
     k_mix_push<true><<<d.m.ntile, MP_THREADS, PUSH_DYN_BYTES, s>>>(d, *(const CUtensorMap*)tmap);
   else
     k_mix_push<false><<<d.m.ntile, MP_THREADS, PUSH_DYN_BYTES, s>>>(d, *(const CUtensorMap*)tmap);
+#endif
 }
 
 // fixed point -> FP64 current over the whole ghosted extent
@@ -1116,6 +1568,10 @@ int mix_setup2d(const Dev2D& d, void* out) {
   if (cudaFuncSetAttribute(k_mix_push<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH_DYN_BYTES) !=
           cudaSuccess ||
       cudaFuncSetAttribute(k_mix_push<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH_DYN_BYTES) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_mix_push2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_mix_push2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
           cudaSuccess)
     return -3;
 
