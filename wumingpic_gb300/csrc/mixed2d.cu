@@ -43,7 +43,7 @@ constexpr int TT = MIX_TS + 2;      // cell-centred values per tile edge (cells 
 constexpr int JP = 48;
 constexpr int FLUSH_EVERY = MIX_FLUSH;  // particles accumulated in registers between flushes
 constexpr int PF = 8;               // particles in flight per push thread (shared-memory ring)
-constexpr int PF_BYTES = PF * 7 * MIX_TC * 4;  // the key plane is not prefetched
+constexpr int PF_BYTES = PF * 7 * MIX_TC * 4;  // the key word is not prefetched
 constexpr unsigned long long kSpinLimit = 1ull << 22;  // a few seconds at most
 // resident CTAs per SM asked of the push kernel; at 2 its 128 registers per thread still hold
 // the cell's whole current stencil without spilling
@@ -96,6 +96,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar) {
   return false;
 }
 
+// 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
 // 4-byte asynchronous global -> shared copy, completion tracked per thread by commit groups
 __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
@@ -180,7 +184,7 @@ __device__ __forceinline__ void write_pending(const PendingLeaver* pend, int c, 
   }
   float* io = pend->top[c] - (size_t)pos * MIX_PL;
 #pragma unroll
-  for (int a = 0; a < 8; ++a) io[a * MIX_TC] = pend->w[a][c];
+  for (int a = 0; a < 8; ++a) io[a] = pend->w[a][c];
 }
 
 // ---------------------------------------------------------------------------
@@ -234,7 +238,7 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
       const float* src = (t < n0 ? col0 : col1) + (size_t)t * MIX_PL;
       float* dst = pfbuf + (t & (PF - 1)) * 7 * MIX_TC + c;
 #pragma unroll
-      for (int a = 0; a < 7; ++a) cp_async4(dst + a * MIX_TC, src + a * MIX_TC);
+      for (int a = 0; a < 7; ++a) cp_async4(dst + a * MIX_TC, src + a);
     }
     cp_async_commit();
   };
@@ -286,10 +290,10 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
     cp_async_wait<PF - 1>();
     const bool sp1 = t >= n0;
     const int k = sp1 ? t - n0 : t;
-    const float* pb = pfbuf + (t & (PF - 1)) * 7 * MIX_TC + c;
-    const float ox = pb[MIX_OX], oy = pb[MIX_OY];
-    float ux = pb[MIX_UX], uy = pb[MIX_UY], uz = pb[MIX_UZ];
-    const float idlo = pb[MIX_IDLO], idhi = pb[MIX_IDHI];  // the id's two words, passed through
+    const float* pb = pfbuf + (t & (PF - 1)) * 7 * MIX_TC + c;  // word a of the slot at pb[a * 256]
+    const float ox = pb[MIX_OX * MIX_TC], oy = pb[MIX_OY * MIX_TC];
+    float ux = pb[MIX_UX * MIX_TC], uy = pb[MIX_UY * MIX_TC], uz = pb[MIX_UZ * MIX_TC];
+    const float idlo = pb[MIX_IDLO * MIX_TC], idhi = pb[MIX_IDHI * MIX_TC];  // the id's two words, passed through
     const float fac1 = sp1 ? m.k_fac1[1] : m.k_fac1[0];
     const float fac2 = sp1 ? m.k_fac2[1] : m.k_fac2[0];
     const float qdd = sp1 ? m.k_qdd[1] : m.k_qdd[0];
@@ -412,7 +416,7 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
       const int dlc = (nly & (MIX_TS - 1)) * MIX_TS + (nlx & (MIX_TS - 1));
       const int dep = nb_dep[s][q];
       ppos = atomicAdd(&m.acnt[nb_bin[s][q] * MIX_TC + dlc], 1);  // used in the next iteration
-      pend->top[c] = m.P + ((size_t)nb_off[s][q] + dep - 1) * MIX_PL + dlc;
+      pend->top[c] = m.P + ((size_t)nb_off[s][q] + dep - 1) * MIX_PL + (size_t)dlc * MIX_W;
       pend->dep[c] = dep;
       pend->w[0][c] = nx_;
       pend->w[1][c] = ny_;
@@ -525,14 +529,14 @@ constexpr int PF2 = 4;                           // particles in flight per thre
 constexpr int LQ2 = 64;                          // leaver queue entries per warp
 constexpr int LQ2W = 6;                          // ox, oy, new ox, new oy, q vz, packed (inc, species, cell)
 constexpr int LQ2_BYTES = (MP_THREADS / 32) * LQ2W * LQ2 * 4;
-constexpr int PEND2_BYTES = 9 * MP_THREADS * 4;  // per thread: new column (packed) + the 8 words
+constexpr int PEND2_BYTES = 9 * MP_THREADS * 4;  // per thread: the slot's 8 words + the new column (packed)
 constexpr int STAGE2_BYTES = 6 * TW * TW * 8;
 constexpr int A2_BYTES = (STAGE2_BYTES > LQ2_BYTES + PEND2_BYTES ? STAGE2_BYTES : LQ2_BYTES + PEND2_BYTES);
 constexpr int OFF2_J = (A2_BYTES + 127) / 128 * 128;
 constexpr int OFF2_SFA = OFF2_J + 2 * 3 * TW * TW * 4;
 constexpr int OFF2_SFB = OFF2_SFA + TT * TT * 16;
 constexpr int OFF2_RING = OFF2_SFB + TT * TT * 8;
-constexpr int PUSH2_SMEM = OFF2_RING + PF2 * 7 * MIX_TC * 4;
+constexpr int PUSH2_SMEM = OFF2_RING + PF2 * MIX_W * MIX_TC * 4;
 static_assert(OFF2_SFA % 16 == 0 && OFF2_RING % 16 == 0, "shared-memory alignment");
 
 // Esirkepov current of one cell-leaver on the 5 x 5 stencil of its old cell (lx, ly), each value
@@ -642,7 +646,7 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
   int* const jlo = jhi + 3 * TW * TW;
   float4* const sfa = reinterpret_cast<float4*>(smem2 + OFF2_SFA);     // (Bx, By, Bz, Ex) at cell centres
   float2* const sfb = reinterpret_cast<float2*>(smem2 + OFF2_SFB);     // (Ey, Ez)
-  float* const ring = reinterpret_cast<float*>(smem2 + OFF2_RING);     // [PF2][7][256]
+  float4* const ring = reinterpret_cast<float4*>(smem2 + OFF2_RING);   // [PF2][256] slots of 2 float4
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int nb_bin[2][9], nb_dep[2][9];
   __shared__ long long nb_off[2][9];
@@ -671,9 +675,9 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
   auto issue = [&](int t) {
     if (t < ntot) {
       const float* src = (t < n0 ? col0 : col1) + (size_t)t * MIX_PL;
-      float* dst = ring + (t & (PF2 - 1)) * 7 * MIX_TC + c;
-#pragma unroll
-      for (int a = 0; a < 7; ++a) cp_async4(dst + a * MIX_TC, src + a * MIX_TC);
+      float4* dst = ring + ((t & (PF2 - 1)) * MIX_TC + c) * 2;
+      cp_async16(dst, src);
+      cp_async16(dst + 1, src + 4);
     }
     cp_async_commit();
   };
@@ -729,17 +733,19 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
   };
   // the pending leaver of this thread (its slot in the new column returned by the last iteration's
   // atomic): arrival number pos goes to slot depth - 1 - pos
+  float4* const pend4 = reinterpret_cast<float4*>(pend);  // [256][2]: the slot's words
+  int* const pdst = reinterpret_cast<int*>(pend + 8 * MP_THREADS);  // [256]: the new column
   auto place = [&](int pos) {
-    const int dst = __float_as_int(pend[8 * MP_THREADS + c]);
+    const int dst = pdst[c];
     const int q = dst & 15, s = (dst >> 4) & 1, dlc = dst >> 8;
     const int dep = nb_dep[s][q];
     if (pos >= dep) {
       atomicOr(d.err, EB_CAPACITY);
       return;
     }
-    float* io = m.P + ((size_t)nb_off[s][q] + dep - 1 - pos) * MIX_PL + dlc;
-#pragma unroll
-    for (int a = 0; a < 8; ++a) io[a * MIX_TC] = pend[a * MP_THREADS + c];
+    float4* io = reinterpret_cast<float4*>(m.P + (((size_t)nb_off[s][q] + dep - 1 - pos) * MIX_TC + dlc) * MIX_W);
+    io[0] = pend4[2 * c];
+    io[1] = pend4[2 * c + 1];
   };
   int j0 = 0, j1 = 0;
   int ppos = -1;
@@ -756,10 +762,10 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
     if (t < ntot) {
       const bool sp1 = t >= n0;
       const int k = sp1 ? t - n0 : t;
-      const float* pb = ring + (t & (PF2 - 1)) * 7 * MIX_TC + c;
-      const float ox = pb[MIX_OX], oy = pb[MIX_OY];
-      float ux = pb[MIX_UX], uy = pb[MIX_UY], uz = pb[MIX_UZ];
-      const float idlo = pb[MIX_IDLO], idhi = pb[MIX_IDHI];
+      const float4 pa = ring[((t & (PF2 - 1)) * MIX_TC + c) * 2], pb = ring[((t & (PF2 - 1)) * MIX_TC + c) * 2 + 1];
+      const float ox = pa.x, oy = pa.y;
+      float ux = pa.z, uy = pa.w, uz = pb.x;
+      const float idlo = pb.y, idhi = pb.z;
       const float fac1 = sp1 ? m.k_fac1[1] : m.k_fac1[0];
       const float fac2 = sp1 ? m.k_fac2[1] : m.k_fac2[0];
       const float qdd = sp1 ? m.k_qdd[1] : m.k_qdd[0];
@@ -862,26 +868,16 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
         const int s = sp1 ? 1 : 0;
         const int dlc = (nly & (MIX_TS - 1)) * MIX_TS + (nlx & (MIX_TS - 1));
         ppos = atomicAdd(&m.acnt[nb_bin[s][q] * MIX_TC + dlc], 1);  // used in the next iteration
-        pend[0 * MP_THREADS + c] = nx_;
-        pend[1 * MP_THREADS + c] = ny_;
-        pend[2 * MP_THREADS + c] = ux;
-        pend[3 * MP_THREADS + c] = uy;
-        pend[4 * MP_THREADS + c] = uz;
-        pend[5 * MP_THREADS + c] = idlo;
-        pend[6 * MP_THREADS + c] = idhi;
-        pend[7 * MP_THREADS + c] = __int_as_float((dir_group((incy + 1) * 3 + (incx + 1)) << 16) | k);
-        pend[8 * MP_THREADS + c] = __int_as_float(q | (s << 4) | (dlc << 8));
+        pend4[2 * c] = make_float4(nx_, ny_, ux, uy);
+        pend4[2 * c + 1] = make_float4(uz, idlo, idhi, __int_as_float((dir_group((incy + 1) * 3 + (incx + 1)) << 16) | k));
+        pdst[c] = q | (s << 4) | (dlc << 8);
         lq0 = ox; lq1 = oy; lq2 = nx_; lq3 = ny_; lq4 = qg;
         lpk = (incx + 1) | ((incy + 1) << 2) | ((sp1 ? 1 : 0) << 4) | (c << 8);
       } else {
-        float* so = (sp1 ? col1 + (size_t)n0 * MIX_PL : col0) + (size_t)(sp1 ? j1 : j0) * MIX_PL;
-        so[MIX_OX] = nx_;
-        so[MIX_OY] = ny_;
-        so[MIX_UX] = ux;
-        so[MIX_UY] = uy;
-        so[MIX_UZ] = uz;
-        so[MIX_IDLO] = idlo;
-        so[MIX_IDHI] = idhi;
+        float4* so = reinterpret_cast<float4*>((sp1 ? col1 + (size_t)n0 * MIX_PL : col0) +
+                                               (size_t)(sp1 ? j1 : j0) * MIX_PL);
+        so[0] = make_float4(nx_, ny_, ux, uy);
+        so[1] = make_float4(uz, idlo, idhi, 0.f);  // a stayer's key word is not read
         if (sp1) ++j1; else ++j0;
         // Esirkepov on the cell's 3 x 3 nodes: the factored spline differences of a move inside
         // the cell (2d/common/field.f90:223-298)
@@ -1069,14 +1065,14 @@ __global__ void __launch_bounds__(MIX_TC, 4) k_mix_arrive(Dev2D d) {
       if (dl[u] >= 0) {
         const float* src = top - (size_t)(i0 + u) * MIX_PL;
 #pragma unroll
-        for (int a = 0; a < 7; ++a) w[u][a] = src[a * MIX_TC];
+        for (int a = 0; a < 7; ++a) w[u][a] = src[a];
       }
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u)
       if (dl[u] >= 0) {
         float* dst = col + (size_t)dl[u] * MIX_PL;
 #pragma unroll
-        for (int a = 0; a < 7; ++a) dst[a * MIX_TC] = w[u][a];
+        for (int a = 0; a < 7; ++a) dst[a] = w[u][a];
       }
   }
   const int nn = ok ? j + b : j;
@@ -1102,14 +1098,13 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_relayout(Dev2D d, const float* f
   const Mix2D& m = d.m;
   const int bin = blockIdx.x, c = threadIdx.x;
   const int n = m.cnt[bin * MIX_TC + c];
-  const float* src = from_P + (size_t)from_boff[bin] * MIX_PL + c;
-  float* dst = mix_slot(m, bin, 0, c);
+  const float4* src = reinterpret_cast<const float4*>(from_P + ((size_t)from_boff[bin] * MIX_TC + c) * MIX_W);
+  float4* dst = reinterpret_cast<float4*>(mix_slot(m, bin, 0, c));
   for (int k = 0; k < n; ++k) {
-    float w[7];
-#pragma unroll
-    for (int a = 0; a < 7; ++a) w[a] = src[(size_t)k * MIX_PL + a * MIX_TC];
-#pragma unroll
-    for (int a = 0; a < 7; ++a) dst[(size_t)k * MIX_PL + a * MIX_TC] = w[a];
+    const size_t o = (size_t)k * (MIX_PL / 4);
+    const float4 a = src[o], b = src[o + 1];
+    dst[o] = a;
+    dst[o + 1] = b;
   }
 }
 
@@ -1174,7 +1169,7 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_put(Dev2D d, const double* aos, 
       const int k = p - scc[ly][lx];
       if (k >= dep || comp > 5) continue;
       const double a = rowp[w];
-      float* o = col0 + (size_t)k * MIX_PL + ly * MIX_TS + lx;
+      float* o = col0 + (size_t)k * MIX_PL + (ly * MIX_TS + lx) * MIX_W;
       const int gx = tx * MIX_TS + lx;
       // offsets in [0, 1): a position within 2^-25 cells below a face rounds up to 1 in FP32
       if (comp == 0) o[MIX_OX] = fminf((float)(a * dxi - (double)(g.nxgs + gx)), 0.99999994f);
@@ -1198,7 +1193,7 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_put(Dev2D d, const double* aos, 
           if (scc[ly][lx + step] <= p) lx += step;
         const int k = p - scc[ly][lx];
         if (k >= dep) continue;
-        float* o = col0 + (size_t)k * MIX_PL + ly * MIX_TS + lx;
+        float* o = col0 + (size_t)k * MIX_PL + (ly * MIX_TS + lx) * MIX_W;
         o[MIX_IDLO] = 0.f;
         o[MIX_IDHI] = 0.f;
       }
@@ -1310,7 +1305,7 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_get(Dev2D d, double* aos, int nd
       for (int step = 8; step > 0; step >>= 1)
         if (scc[ly][lx + step] <= p) lx += step;
       const int k = p - scc[ly][lx];
-      const float* o = col0 + (size_t)k * MIX_PL + ly * MIX_TS + lx;
+      const float* o = col0 + (size_t)k * MIX_PL + (ly * MIX_TS + lx) * MIX_W;
       const int gx = tx * MIX_TS + lx;
       double v;
       if (comp == 0) v = ((double)(g.nxgs + gx) + (double)o[MIX_OX]) * dx;

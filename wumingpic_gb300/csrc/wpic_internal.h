@@ -73,9 +73,8 @@ struct Parts64 {
 // tile = ty * ntx + tx.  Inside a bin every cell owns a column of bdep[bin] slots:
 // slot (k, c) for cell c = ly * 16 + lx lies in layer boff[bin] + k, so the cell of a particle
 // is implicit.  Position = that cell plus an FP32 offset in [0, 1) per dimension; momenta FP32;
-// 64-bit id.  Each 256-slot layer stores its components one after another as 32-bit planes
-// (ox, oy, ux, uy, uz, id low word, id high word, arrival key), so one address per slot reaches
-// every component through fixed offsets while a warp still reads 128 contiguous bytes.
+// 64-bit id.  Each 256-slot layer holds the slots of the tile's cells in order, a slot being the
+// particle's 8 words (below), so a warp's 32 cells are 1 KB of contiguous memory.
 // A push compacts each column in place (stayers to the bottom) and writes the particles that
 // change cell to the top of their new cell's column, from slot bdep - 1 downwards; the arrival
 // kernel then moves them, in key order, to just above the stayers.  The depth of a bin grows
@@ -84,9 +83,14 @@ constexpr int MIX_TS = 16;
 constexpr int MIX_TC = MIX_TS * MIX_TS;
 constexpr int MIX_FLUSH = 64;  // particles a push thread sums in registers between fixed-point flushes
 constexpr int MIX_MAX_DEPTH = 32767;  // slot indices fit the 16-bit field of the arrival key
-constexpr int MIX_OX = 0, MIX_OY = MIX_TC, MIX_UX = 2 * MIX_TC, MIX_UY = 3 * MIX_TC, MIX_UZ = 4 * MIX_TC;
-constexpr int MIX_IDLO = 5 * MIX_TC, MIX_IDHI = 6 * MIX_TC, MIX_KEY = 7 * MIX_TC;
-constexpr int MIX_PL = 8 * MIX_TC;   // 32-bit words per layer
+// A slot is 8 consecutive 32-bit words (32 bytes): ox, oy, ux, uy, uz, id low, id high, arrival key.
+// Slot (k, c) of a bin lies at word ((boff + k) * 256 + c) * 8, so a warp reading slot k of 32
+// neighbouring cells reads 1 KB contiguously, and a thread moves a particle with two 16-byte
+// accesses.
+constexpr int MIX_W = 8;             // 32-bit words per slot
+constexpr int MIX_OX = 0, MIX_OY = 1, MIX_UX = 2, MIX_UY = 3, MIX_UZ = 4;
+constexpr int MIX_IDLO = 5, MIX_IDHI = 6, MIX_KEY = 7;
+constexpr int MIX_PL = MIX_W * MIX_TC;  // 32-bit words per layer
 
 struct Mix2D {
   // fixed-point current accumulation of the push: v = hi / s1 + lo / s2 with int32 hi, lo
@@ -111,9 +115,9 @@ struct Mix2D {
   unsigned long long* ujx;  // [3][ny+4][nx+4] current in fixed point (units 1/fx_s2), summed exactly
 };
 
-// word of slot (k, c) of bin `bin` in the first plane; the other components at + MIX_OY ... + MIX_KEY
+// first word of slot (k, c) of bin `bin`; the components at + MIX_OX ... + MIX_KEY
 __device__ inline float* mix_slot(const Mix2D& m, int bin, int k, int c) {
-  return m.P + ((size_t)m.boff[bin] + k) * MIX_PL + c;
+  return m.P + (((size_t)m.boff[bin] + k) * MIX_TC + c) * MIX_W;
 }
 
 struct CGState {
