@@ -31,6 +31,7 @@ struct wpic_ctx3d {
   alignas(128) unsigned char tmap[128];  // CUtensorMap of uf (mixed path TMA tile loads)
   // mixed path: the particle layers (reallocated when bins grow) and the host copy of the layout
   float* mixP = nullptr;
+  int* mixK = nullptr;           // the arrival keys of the layout (one per slot)
   std::vector<int> h_dep;
   int* h_grow = nullptr;         // pinned mirror of the grow flag
   double mix_vmax = 0.0;         // largest contribution of one particle to one node of the deposit
@@ -194,6 +195,12 @@ int mix3_set_layout(wpic_ctx3d* c, const std::vector<int>& dep, bool keep) {
     cudaFree(c->mixP);
     c->mixP = nullptr;
   }
+  // the keys only pass from a push to the arrival kernel: the old ones are not kept
+  CK3(cudaStreamSynchronize(c->stream));
+  if (c->mixK) cudaFree(c->mixK);
+  c->mixK = nullptr;
+  CK3(cudaMalloc(&c->mixK, (size_t)layers * M3_TC * sizeof(int)));
+  m.K = c->mixK;
   float* np_ = nullptr;
   CK3(cudaMalloc(&np_, (size_t)layers * M3_PL * sizeof(float)));
   long long* old_off = nullptr;
@@ -463,6 +470,7 @@ int wpic3d_finalize(wpic_ctx3d* c) {
   for (void* p : c->allocs) cudaFree(p);
   if (c->staging) cudaFree(c->staging);
   if (c->mixP) cudaFree(c->mixP);
+  if (c->mixK) cudaFree(c->mixK);
   if (c->h_grow) cudaFreeHost(c->h_grow);
   if (c->h_cg) cudaFreeHost(c->h_cg);
   if (c->h_err) cudaFreeHost(c->h_err);

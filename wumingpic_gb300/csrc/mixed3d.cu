@@ -48,7 +48,7 @@ constexpr int JX = TX + 4, JY = TY + 4, JZ = TZ + 4;
 constexpr int JN = JX * JY * JZ;
 constexpr int PATCH_BYTES = 2 * 3 * JN * 4;
 constexpr int PF = 4;  // particles in flight per thread (shared-memory ring)
-constexpr int RING_BYTES = PF * 8 * TC * 4;  // the key plane is not prefetched
+constexpr int RING_BYTES = PF * M3_W * TC * 4;
 constexpr int LQ = 64;                       // leaver queue entries per warp
 constexpr int LQW = 7;                       // 32-bit words per entry
 constexpr int LQ_BYTES = (TC / 32) * LQW * LQ * 4;
@@ -65,10 +65,12 @@ constexpr int OFF_SFB = OFF_SFA + FN * 16;
 constexpr int OFF_RING = OFF_SFB + FN * 8;
 constexpr int OFF_PEND = OFF_RING + RING_BYTES;
 
+// a leaver of the push waiting for its slot (one per thread): the slot's 8 words, its arrival key
+// and its new column (3 x 3 x 3 neighbourhood tile, species, cell)
 struct Pending3 {
-  float* top[TC];
-  int dep[TC];
-  float w[9][TC];
+  float4 w[TC][2];
+  int key[TC];
+  int dst[TC];
 };
 constexpr int PUSH_SMEM = OFF_PEND + (int)sizeof(Pending3);
 
@@ -105,8 +107,8 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* tm, in
       "l"(tm), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
       : "memory");
 }
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
@@ -239,16 +241,7 @@ __device__ __forceinline__ void cell3_flush(Cell3Current& a, int* jhi, int* jlo,
 // direction code d = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1) of a move (13 = same cell) -> group 0..25
 __device__ __forceinline__ int dir_group3(int d) { return d < 13 ? d : d - 1; }
 
-// arrival number pos of a column goes to slot depth - 1 - pos
-__device__ __forceinline__ void write_pending3(const Pending3* pend, int c, int pos, int* err) {
-  if (pos >= pend->dep[c]) {
-    atomicOr(err, EB_CAPACITY);
-    return;
-  }
-  float* io = pend->top[c] - (size_t)pos * M3_PL;
-#pragma unroll
-  for (int a = 0; a < 9; ++a) io[a * TC] = pend->w[a][c];
-}
+// __cvta helpers come before the kernel; write_pending3 is defined inside the kernel as a lambda
 
 }  // namespace
 
@@ -298,9 +291,9 @@ __global__ void __launch_bounds__(TC, 2) k_mix3_push(Dev3D d, Mix3Const k, const
   auto issue = [&](int t) {
     if (t < ntot) {
       const float* src = (t < n0 ? col0 : col1) + (size_t)t * M3_PL;
-      float* dst = ring + (t & (PF - 1)) * 8 * TC + c;
-#pragma unroll
-      for (int a = 0; a < 8; ++a) cp_async4(dst + a * TC, src + a * TC);
+      float* dst = ring + ((t & (PF - 1)) * TC + c) * M3_W;
+      cp_async16(dst, src);
+      cp_async16(dst + 4, src + 4);
     }
     cp_async_commit();
   };
@@ -364,6 +357,22 @@ __global__ void __launch_bounds__(TC, 2) k_mix3_push(Dev3D d, Mix3Const k, const
     qhead += cnt;
     __syncwarp();
   };
+  // the pending leaver of this thread (its slot returned by the last iteration's atomic): arrival
+  // number pos of a column goes to slot depth - 1 - pos, its key beside it in the key array
+  auto write_pending3 = [&](int pos) {
+    const int dst = pend->dst[c];
+    const int q = dst & 31, s = (dst >> 5) & 1, dlc = dst >> 8;
+    const int dep = nb_dep[s][q];
+    if (pos >= dep) {
+      atomicOr(d.err, EB_CAPACITY);
+      return;
+    }
+    const size_t slot = ((size_t)nb_off[s][q] + dep - 1 - pos) * TC + dlc;
+    float4* io = reinterpret_cast<float4*>(m.P + slot * M3_W);
+    io[0] = pend->w[c][0];
+    io[1] = pend->w[c][1];
+    m.K[slot] = pend->key[c];
+  };
   int j0 = 0, j1 = 0;  // stayers kept so far per species (compacted in place)
   int ppos = -1;       // arrival number of the pending leaver parked in shared memory, -1 if none
   int tw = ntot;       // iterations of this warp: the largest column of its lanes
@@ -378,10 +387,11 @@ __global__ void __launch_bounds__(TC, 2) k_mix3_push(Dev3D d, Mix3Const k, const
     if (t < ntot) {
       const bool sp1 = t >= n0;
       const int kk = sp1 ? t - n0 : t;
-      const float* pb = ring + (t & (PF - 1)) * 8 * TC + c;
-      const float o[3] = {pb[0 * TC], pb[1 * TC], pb[2 * TC]};
-      float ux = pb[3 * TC], uy = pb[4 * TC], uz = pb[5 * TC];
-      const float idlo = pb[6 * TC], idhi = pb[7 * TC];
+      const float4* pb = reinterpret_cast<const float4*>(ring + ((t & (PF - 1)) * TC + c) * M3_W);
+      const float4 pa = pb[0], pz = pb[1];
+      const float o[3] = {pa.x, pa.y, pa.z};
+      float ux = pa.w, uy = pz.x, uz = pz.y;
+      const float idlo = pz.z, idhi = pz.w;
       const float fac1 = sp1 ? k.fac1[1] : k.fac1[0];
       const float fac2 = sp1 ? k.fac2[1] : k.fac2[0];
       const float qdd = sp1 ? k.qdd[1] : k.qdd[0];
@@ -492,7 +502,7 @@ __global__ void __launch_bounds__(TC, 2) k_mix3_push(Dev3D d, Mix3Const k, const
       }
       leaver = (inc[0] | inc[1] | inc[2]) != 0;
       // the slot of the previous leaver has had a whole iteration to return
-      if (ppos >= 0) write_pending3(pend, c, ppos, d.err);
+      if (ppos >= 0) write_pending3(ppos);
       ppos = -1;
       if (leaver) {
         const int nlx = lx + inc[0], nly = ly + inc[1], nlz = lz + inc[2];
@@ -500,20 +510,11 @@ __global__ void __launch_bounds__(TC, 2) k_mix3_push(Dev3D d, Mix3Const k, const
         const int q = ((nlz >> 2) + 1) * 9 + ((nly >> 3) + 1) * 3 + ((nlx >> 3) + 1);
         const int s = sp1 ? 1 : 0;
         const int dlc = ((nlz & (TZ - 1)) * TY + (nly & (TY - 1))) * TX + (nlx & (TX - 1));
-        const int dep = nb_dep[s][q];
         ppos = atomicAdd(&m.acnt[nb_bin[s][q] * TC + dlc], 1);  // used in the next iteration
-        pend->top[c] = m.P + ((size_t)nb_off[s][q] + dep - 1) * M3_PL + dlc;
-        pend->dep[c] = dep;
-        pend->w[0][c] = on[0];
-        pend->w[1][c] = on[1];
-        pend->w[2][c] = on[2];
-        pend->w[3][c] = ux;
-        pend->w[4][c] = uy;
-        pend->w[5][c] = uz;
-        pend->w[6][c] = idlo;
-        pend->w[7][c] = idhi;
-        pend->w[8][c] =
-            __int_as_float((dir_group3((inc[2] + 1) * 9 + (inc[1] + 1) * 3 + (inc[0] + 1)) << 16) | kk);
+        pend->w[c][0] = make_float4(on[0], on[1], on[2], ux);
+        pend->w[c][1] = make_float4(uy, uz, idlo, idhi);
+        pend->key[c] = (dir_group3((inc[2] + 1) * 9 + (inc[1] + 1) * 3 + (inc[0] + 1)) << 16) | kk;
+        pend->dst[c] = q | (s << 5) | (dlc << 8);
 #pragma unroll
         for (int mm = 0; mm < 3; ++mm) {
           lo_[mm] = o[mm];
@@ -522,15 +523,10 @@ __global__ void __launch_bounds__(TC, 2) k_mix3_push(Dev3D d, Mix3Const k, const
         }
         lsp1 = sp1;
       } else {
-        float* so = (sp1 ? col1 + (size_t)n0 * M3_PL : col0) + (size_t)(sp1 ? j1 : j0) * M3_PL;
-        so[0 * TC] = on[0];
-        so[1 * TC] = on[1];
-        so[2 * TC] = on[2];
-        so[3 * TC] = ux;
-        so[4 * TC] = uy;
-        so[5 * TC] = uz;
-        so[6 * TC] = idlo;
-        so[7 * TC] = idhi;
+        float4* so = reinterpret_cast<float4*>((sp1 ? col1 + (size_t)n0 * M3_PL : col0) +
+                                               (size_t)(sp1 ? j1 : j0) * M3_PL);
+        so[0] = make_float4(on[0], on[1], on[2], ux);
+        so[1] = make_float4(uy, uz, idlo, idhi);
         if (sp1) ++j1; else ++j0;
         // ---- Esirkepov deposit of a particle that stays in its cell, into the registers ----
         // support: nodes -1, 0, 1 on every axis; ds from the factored difference
@@ -586,7 +582,7 @@ __global__ void __launch_bounds__(TC, 2) k_mix3_push(Dev3D d, Mix3Const k, const
     issue(t + PF);
   }
   cp_async_wait<0>();
-  if (ppos >= 0) write_pending3(pend, c, ppos, d.err);
+  if (ppos >= 0) write_pending3(ppos);
   if (qtail > qhead) drain(qtail - qhead);
   m.ccnt[bin0 * TC + c] = j0;
   if (nsp > 1) m.ccnt[(bin0 + 1) * TC + c] = j1;
@@ -650,11 +646,10 @@ __global__ void __launch_bounds__(TC, 4) k_mix3_arrive(Dev3D d) {
   if (b > dep) b = dep;
   float* const col = mix3_slot(m, bin, 0, c);
   const float* top = col + (size_t)(dep - 1) * M3_PL;  // arrival i in slot dep - 1 - i
+  const int* ktop = mix3_key(m, bin, dep - 1, c);
   const int ns = b < ARR_KEYS_SMEM ? b : ARR_KEYS_SMEM;
-  for (int i = 0; i < ns; ++i) skey[i][c] = __float_as_int(top[M3_KEY - (ptrdiff_t)i * M3_PL]);
-  auto key = [&](int i) {
-    return i < ARR_KEYS_SMEM ? skey[i][c] : __float_as_int(top[M3_KEY - (ptrdiff_t)i * M3_PL]);
-  };
+  for (int i = 0; i < ns; ++i) skey[i][c] = ktop[-(ptrdiff_t)i * TC];
+  auto key = [&](int i) { return i < ARR_KEYS_SMEM ? skey[i][c] : ktop[-(ptrdiff_t)i * TC]; };
   for (int i0 = 0; ok && i0 < b; i0 += ARR_BATCH) {
     int dl[ARR_BATCH];
 #pragma unroll
@@ -668,20 +663,20 @@ __global__ void __launch_bounds__(TC, 4) k_mix3_arrive(Dev3D d) {
         dl[u] = j + rank;
       }
     }
-    float w[ARR_BATCH][8];
+    float4 w[ARR_BATCH][2];
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u)
       if (dl[u] >= 0) {
-        const float* src = top - (size_t)(i0 + u) * M3_PL;
-#pragma unroll
-        for (int a = 0; a < 8; ++a) w[u][a] = src[a * TC];
+        const float4* src = reinterpret_cast<const float4*>(top - (size_t)(i0 + u) * M3_PL);
+        w[u][0] = src[0];
+        w[u][1] = src[1];
       }
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u)
       if (dl[u] >= 0) {
-        float* dst = col + (size_t)dl[u] * M3_PL;
-#pragma unroll
-        for (int a = 0; a < 8; ++a) dst[a * TC] = w[u][a];
+        float4* dst = reinterpret_cast<float4*>(col + (size_t)dl[u] * M3_PL);
+        dst[0] = w[u][0];
+        dst[1] = w[u][1];
       }
   }
   const int nn = ok ? j + b : j;
@@ -706,14 +701,13 @@ __global__ void __launch_bounds__(TC) k_mix3_relayout(Dev3D d, const float* from
   const Mix3D& m = d.m;
   const int bin = blockIdx.x, c = threadIdx.x;
   const int n = m.cnt[bin * TC + c];
-  const float* src = from_P + (size_t)from_boff[bin] * M3_PL + c;
-  float* dst = mix3_slot(m, bin, 0, c);
+  const float4* src = reinterpret_cast<const float4*>(from_P + ((size_t)from_boff[bin] * TC + c) * M3_W);
+  float4* dst = reinterpret_cast<float4*>(mix3_slot(m, bin, 0, c));
   for (int kk = 0; kk < n; ++kk) {
-    float w[8];
-#pragma unroll
-    for (int a = 0; a < 8; ++a) w[a] = src[(size_t)kk * M3_PL + a * TC];
-#pragma unroll
-    for (int a = 0; a < 8; ++a) dst[(size_t)kk * M3_PL + a * TC] = w[a];
+    const size_t o = (size_t)kk * (M3_PL / 4);
+    const float4 a = src[o], b = src[o + 1];
+    dst[o] = a;
+    dst[o + 1] = b;
   }
 }
 
@@ -778,7 +772,7 @@ __global__ void __launch_bounds__(TC) k_mix3_put(Dev3D d, const double* aos, int
       const int kq = p - scc[r][lx];
       if (kq >= dep || comp > 6) continue;
       const double a = rowp[w];
-      float* o = cl0 + (size_t)kq * M3_PL + r * TX + lx;
+      float* o = cl0 + (size_t)kq * M3_PL + (r * TX + lx) * M3_W;
       const int gx = tx * TX + lx;
       // offsets in [0, 1): a position within 2^-25 cells below a face rounds up to 1 in FP32
       if (comp == 0) o[M3_OX] = fminf((float)(a * dxi - (double)(g.nxgs + gx)), 0.99999994f);
@@ -897,7 +891,7 @@ __global__ void __launch_bounds__(TC) k_mix3_get(Dev3D d, double* aos, int ndim,
       for (int step = 4; step > 0; step >>= 1)
         if (scc[r][lx + step] <= p) lx += step;
       const int kq = p - scc[r][lx];
-      const float* o = cl0 + (size_t)kq * M3_PL + r * TX + lx;
+      const float* o = cl0 + (size_t)kq * M3_PL + (r * TX + lx) * M3_W;
       const int gx = tx * TX + lx;
       double v;
       if (comp == 0) v = ((double)(g.nxgs + gx) + (double)o[M3_OX]) * dx;

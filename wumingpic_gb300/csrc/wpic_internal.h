@@ -266,15 +266,16 @@ struct Parts3D {
 // bin = tile * nsp + isp, tile = (tz * nty + ty) * ntx + tx.  Inside a bin every cell
 // c = (lz * 8 + ly) * 8 + lx owns a column of bdep[bin] slots; slot (k, c) lies in layer
 // boff[bin] + k.  Position = the column's cell plus three FP32 offsets in [0, 1); momenta FP32;
-// 64-bit id; each 256-slot layer holds nine 32-bit planes (ox, oy, oz, ux, uy, uz, id low word,
-// id high word, arrival key) one after another.  The push compacts each column in place and
+// 64-bit id: a slot is 8 consecutive 32-bit words (ox, oy, oz, ux, uy, uz, id low word, id high
+// word), 32 bytes, the layer's 256 slots in cell order; the arrival key of a slot lies in a
+// separate array of one 32-bit word per slot.  The push compacts each column in place and
 // writes the particles that change cell to the top of their new column; the arrival kernel moves
 // them, in key order, to just above the stayers; bins grow when their columns come close to full.
 constexpr int M3_TX = 8, M3_TY = 8, M3_TZ = 4;
 constexpr int M3_TC = M3_TX * M3_TY * M3_TZ;  // cells per tile = threads of the tile kernels
-constexpr int M3_OX = 0, M3_OY = M3_TC, M3_OZ = 2 * M3_TC, M3_UX = 3 * M3_TC, M3_UY = 4 * M3_TC,
-              M3_UZ = 5 * M3_TC, M3_IDLO = 6 * M3_TC, M3_IDHI = 7 * M3_TC, M3_KEY = 8 * M3_TC;
-constexpr int M3_PL = 9 * M3_TC;  // 32-bit words per layer
+constexpr int M3_W = 8;  // 32-bit words per slot
+constexpr int M3_OX = 0, M3_OY = 1, M3_OZ = 2, M3_UX = 3, M3_UY = 4, M3_UZ = 5, M3_IDLO = 6, M3_IDHI = 7;
+constexpr int M3_PL = M3_W * M3_TC;  // 32-bit words per layer
 
 struct Mix3D {
   // fixed-point current: v = hi / s1 + lo / s2 (int32 planes in shared memory), global sums in
@@ -283,6 +284,7 @@ struct Mix3D {
   double fx_is2;
   int ntx, nty, ntz, ntile, nbin;
   float* P;            // particle layers, M3_PL words each
+  int* K;              // arrival keys, one per slot (M3_TC per layer)
   long long* boff;     // [nbin] first layer of each bin
   int* bdep;           // [nbin] slots per cell column
   int* cnt;            // [nbin][256] particles per column (the push's input count)
@@ -294,7 +296,10 @@ struct Mix3D {
 };
 
 __device__ inline float* mix3_slot(const Mix3D& m, int bin, int k, int c) {
-  return m.P + ((size_t)m.boff[bin] + k) * M3_PL + c;
+  return m.P + (((size_t)m.boff[bin] + k) * M3_TC + c) * M3_W;
+}
+__device__ inline int* mix3_key(const Mix3D& m, int bin, int k, int c) {
+  return m.K + ((size_t)m.boff[bin] + k) * M3_TC + c;
 }
 
 struct Dev3D {
