@@ -1015,11 +1015,10 @@ void mix_curre_refresh2d(const Dev2D& d, cudaStream_t s) {
 // records, per bin, count + 2 x arrivals of its fullest column, the room the next step may
 // need; past 7/8 of the depth the host grows the bin before the next push.
 // ---------------------------------------------------------------------------
-constexpr int ARR_KEYS_SMEM = 32;  // keys per cell staged in shared memory; more are read from global memory
+constexpr int ARR_KR = 8;     // keys per cell held in registers; more are read from global memory
 constexpr int ARR_BATCH = 4;
 
-__global__ void __launch_bounds__(MIX_TC, 4) k_mix_arrive(Dev2D d) {
-  __shared__ int skey[ARR_KEYS_SMEM][MIX_TC];
+__global__ void __launch_bounds__(MIX_TC) k_mix_arrive(Dev2D d) {
   __shared__ int wmax[MIX_TC / 32];
   const Mix2D& m = d.m;
   const int bin = blockIdx.x;
@@ -1035,45 +1034,51 @@ __global__ void __launch_bounds__(MIX_TC, 4) k_mix_arrive(Dev2D d) {
     atomicOr(d.err, EB_CAPACITY);
   }
   if (b > dep) b = dep;
+  const int bm = ok ? b : 0;  // arrivals moved
   float* const col = mix_slot(m, bin, 0, c);
   const float* top = col + (size_t)(dep - 1) * MIX_PL;  // arrival i in slot dep - 1 - i
-  const int ns = b < ARR_KEYS_SMEM ? b : ARR_KEYS_SMEM;
-  for (int i = 0; i < ns; ++i)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(&skey[i][c])),
-                 "l"(top - (size_t)i * MIX_PL + MIX_KEY)
-                 : "memory");
-  asm volatile("cp.async.commit_group;\n cp.async.wait_group 0;" ::: "memory");
-  auto key = [&](int i) {
-    return i < ARR_KEYS_SMEM ? skey[i][c] : __float_as_int(top[MIX_KEY - (ptrdiff_t)i * MIX_PL]);
+  auto key = [&](int i) { return __float_as_int(top[MIX_KEY - (ptrdiff_t)i * MIX_PL]); };
+  // the first ARR_KR keys in registers (all loads in flight together), the rest read as needed
+  int kr[ARR_KR];
+#pragma unroll
+  for (int i = 0; i < ARR_KR; ++i) kr[i] = i < bm ? key(i) : 0x7fffffff;
+  auto rank_of = [&](int ki) {
+    int r = 0;
+#pragma unroll
+    for (int l = 0; l < ARR_KR; ++l) r += kr[l] < ki ? 1 : 0;
+    for (int l = ARR_KR; l < bm; ++l) r += key(l) < ki ? 1 : 0;
+    return r;
   };
-  for (int i0 = 0; ok && i0 < b; i0 += ARR_BATCH) {
-    int dl[ARR_BATCH];  // destination slot of arrival i0 + u, -1 past the last arrival
+  auto move = [&](int i, int dst_slot, float4 (&w)[2]) {
+    const float4* src = reinterpret_cast<const float4*>(top - (size_t)i * MIX_PL);
+    w[0] = src[0];
+    w[1] = src[1];
+    (void)dst_slot;
+  };
+#pragma unroll
+  for (int h = 0; h < ARR_KR; h += ARR_BATCH) {
+    int dl[ARR_BATCH];
+    float4 w[ARR_BATCH][2];
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u) {
-      const int i = i0 + u;
-      dl[u] = -1;
-      if (i < b) {
-        const int ki = key(i);
-        int rank = 0;
-        for (int l = 0; l < b; ++l) rank += key(l) < ki ? 1 : 0;
-        dl[u] = j + rank;
-      }
+      dl[u] = h + u < bm ? j + rank_of(kr[h + u]) : -1;
+      if (dl[u] >= 0) move(h + u, dl[u], w[u]);
     }
-    float w[ARR_BATCH][7];
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u)
       if (dl[u] >= 0) {
-        const float* src = top - (size_t)(i0 + u) * MIX_PL;
-#pragma unroll
-        for (int a = 0; a < 7; ++a) w[u][a] = src[a];
+        float4* dst = reinterpret_cast<float4*>(col + (size_t)dl[u] * MIX_PL);
+        dst[0] = w[u][0];
+        dst[1] = w[u][1];
       }
-#pragma unroll
-    for (int u = 0; u < ARR_BATCH; ++u)
-      if (dl[u] >= 0) {
-        float* dst = col + (size_t)dl[u] * MIX_PL;
-#pragma unroll
-        for (int a = 0; a < 7; ++a) dst[a] = w[u][a];
-      }
+  }
+  for (int i = ARR_KR; i < bm; ++i) {
+    float4 w[2];
+    const int dl = j + rank_of(key(i));
+    move(i, dl, w);
+    float4* dst = reinterpret_cast<float4*>(col + (size_t)dl * MIX_PL);
+    dst[0] = w[0];
+    dst[1] = w[1];
   }
   const int nn = ok ? j + b : j;
   m.cnt[bin * MIX_TC + c] = nn;

@@ -625,11 +625,10 @@ void mix3_fix(const Dev3D& d, cudaStream_t s) { k_mix3_fix<<<8 * 152, 256, 0, s>
 // records per bin count + 2 x arrivals of its fullest column; past 7/8 of the depth the host
 // grows the bin before the next push.
 // ---------------------------------------------------------------------------
-constexpr int ARR_KEYS_SMEM = 24;
+constexpr int ARR_KR = 8;  // keys per cell held in registers; more are read from global memory
 constexpr int ARR_BATCH = 4;
 
-__global__ void __launch_bounds__(TC, 4) k_mix3_arrive(Dev3D d) {
-  __shared__ int skey[ARR_KEYS_SMEM][TC];
+__global__ void __launch_bounds__(TC) k_mix3_arrive(Dev3D d) {
   __shared__ int wmax[TC / 32];
   const Mix3D& m = d.m;
   const int bin = blockIdx.x;
@@ -644,33 +643,35 @@ __global__ void __launch_bounds__(TC, 4) k_mix3_arrive(Dev3D d) {
     atomicOr(d.err, EB_CAPACITY);
   }
   if (b > dep) b = dep;
+  const int bm = ok ? b : 0;  // arrivals moved
   float* const col = mix3_slot(m, bin, 0, c);
   const float* top = col + (size_t)(dep - 1) * M3_PL;  // arrival i in slot dep - 1 - i
   const int* ktop = mix3_key(m, bin, dep - 1, c);
-  const int ns = b < ARR_KEYS_SMEM ? b : ARR_KEYS_SMEM;
-  for (int i = 0; i < ns; ++i) skey[i][c] = ktop[-(ptrdiff_t)i * TC];
-  auto key = [&](int i) { return i < ARR_KEYS_SMEM ? skey[i][c] : ktop[-(ptrdiff_t)i * TC]; };
-  for (int i0 = 0; ok && i0 < b; i0 += ARR_BATCH) {
-    int dl[ARR_BATCH];
+  auto key = [&](int i) { return ktop[-(ptrdiff_t)i * TC]; };
+  // the first ARR_KR keys in registers (all loads in flight together), the rest read as needed
+  int kr[ARR_KR];
 #pragma unroll
-    for (int u = 0; u < ARR_BATCH; ++u) {
-      const int i = i0 + u;
-      dl[u] = -1;
-      if (i < b) {
-        const int ki = key(i);
-        int rank = 0;
-        for (int l = 0; l < b; ++l) rank += key(l) < ki ? 1 : 0;
-        dl[u] = j + rank;
-      }
-    }
+  for (int i = 0; i < ARR_KR; ++i) kr[i] = i < bm ? key(i) : 0x7fffffff;
+  auto rank_of = [&](int ki) {
+    int r = 0;
+#pragma unroll
+    for (int l = 0; l < ARR_KR; ++l) r += kr[l] < ki ? 1 : 0;
+    for (int l = ARR_KR; l < bm; ++l) r += key(l) < ki ? 1 : 0;
+    return r;
+  };
+#pragma unroll
+  for (int h = 0; h < ARR_KR; h += ARR_BATCH) {
+    int dl[ARR_BATCH];
     float4 w[ARR_BATCH][2];
 #pragma unroll
-    for (int u = 0; u < ARR_BATCH; ++u)
+    for (int u = 0; u < ARR_BATCH; ++u) {
+      dl[u] = h + u < bm ? j + rank_of(kr[h + u]) : -1;
       if (dl[u] >= 0) {
-        const float4* src = reinterpret_cast<const float4*>(top - (size_t)(i0 + u) * M3_PL);
+        const float4* src = reinterpret_cast<const float4*>(top - (size_t)(h + u) * M3_PL);
         w[u][0] = src[0];
         w[u][1] = src[1];
       }
+    }
 #pragma unroll
     for (int u = 0; u < ARR_BATCH; ++u)
       if (dl[u] >= 0) {
@@ -678,6 +679,14 @@ __global__ void __launch_bounds__(TC, 4) k_mix3_arrive(Dev3D d) {
         dst[0] = w[u][0];
         dst[1] = w[u][1];
       }
+  }
+  for (int i = ARR_KR; i < bm; ++i) {
+    const int dl = j + rank_of(key(i));
+    const float4* src = reinterpret_cast<const float4*>(top - (size_t)i * M3_PL);
+    const float4 w0 = src[0], w1 = src[1];
+    float4* dst = reinterpret_cast<float4*>(col + (size_t)dl * M3_PL);
+    dst[0] = w0;
+    dst[1] = w1;
   }
   const int nn = ok ? j + b : j;
   m.cnt[bin * TC + c] = nn;
