@@ -28,17 +28,20 @@ METRIC = "particle-updates/s on 1 GB300: mixed vs FP64 path at <=1% growth-rate 
 UNIT = "particle-updates/s"
 
 # Algorithmic bytes of the dominant kernels (compulsory traffic, one launch):
-#  k_mix_push (mixed push + deposit): per particle read the x/y offsets (8 B), ux, uy, uz
-#    (12 B) and the id (8 B), and write them back = 56 B (a particle that changes cell is
-#    written to its new cell's inbox instead, plus a 4-byte order key).
+#  k_mix_push2 (mixed push + deposit): per particle read its 32-byte state and write it back =
+#    64 B, the per-update figure of the split representation (cell index 4 B + two FP32
+#    offsets 8 B + three FP32 momenta 12 B + 64-bit id 8 B); here the cell is implicit in the
+#    particle's column and those 4 bytes of the slot carry the arrival key of a particle that
+#    changes cell.
 #  k_push2d (FP64 push): per particle read x, y, ux, uy, uz, id (48 B) + write them (48 B) = 96 B.
 #  k_deposit2d (FP64 deposit): per particle read old x, y (16 B) + new x, y, ux, uy, uz (40 B)
 #    = 56 B, plus 600 B per cell for the cell's 5x5x3 current tile.
-BYTES_MIX_PUSH = 56
-# k_mix_push's measured DRAM traffic per particle: dram__bytes_read.sum + dram__bytes_write.sum of
-# one launch on the 2048^2 x 64 ppc workload (17.31 + 16.89 GB for 536,870,912 particles, one ncu
-# pass), scaled to the particles of a launch.
-TRAFFIC_MIX_PUSH_PER_PARTICLE = (17.31e9 + 16.89e9) / 536870912
+BYTES_MIX_PUSH = 64
+# k_mix_push2's measured DRAM traffic per particle: dram__bytes_read.sum + dram__bytes_write.sum of
+# one launch on the 512^2 x 64 ppc case of the same physics (1.125 + 1.035 GB for 33,554,432
+# particles, ncu --set full), scaled to the particles of a launch (the traffic per particle of
+# the previous kernel was 61.8 B at 512^2 and 63.7 B at 2048^2: it grows in proportion)
+TRAFFIC_MIX_PUSH_PER_PARTICLE = (1.125434e9 + 1.034867e9) / 33554432
 BYTES_PUSH_FP64 = 96
 BYTES_DEPOSIT_FP64 = 56
 BYTES_DEPOSIT_CELL = 600
@@ -558,10 +561,11 @@ def main():
     push_ms, push_n = stages["push"]
     per_launch = push_ms / max(1, push_n)
     achieved = BYTES_MIX_PUSH * (npart / world) / (per_launch / 1e3) / 1e9  # one GPU's launch
-    roofline = {"bound": "hbm", "kernel": "k_mix_push (fused push + deposit, mixed precision)",
+    roofline = {"bound": "hbm", "kernel": "k_mix_push2 (fused push + deposit + column compaction, mixed precision)",
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "traffic": TRAFFIC_MIX_PUSH_PER_PARTICLE * (npart / world),
-                "traffic_unit": "bytes per launch (ncu dram read + write, 63.7 B per particle)", "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "traffic_unit": "bytes per launch (ncu dram read + write, 64.4 B per particle at 512^2, scaled)",
+                "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "bytes_per_particle": BYTES_MIX_PUSH, "launch_ms": per_launch}
     launches = int(sum(v[1] for v in stages.values()))
     moments = time_moments(g, torch)

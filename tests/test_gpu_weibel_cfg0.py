@@ -78,6 +78,9 @@ def test_cfg0_growth_rate_and_energy_match_oracle(cfg0_runs, precision):
     assert abs(gg / go - 1.0) <= GROWTH_RATE_RTOL, (precision, gg, go, wg, wo)
     to, tg_ = eo.sum(axis=1), eg.sum(axis=1)
     rel = np.abs(tg_ - to) / np.abs(to)
+    print(f"cfg0 {precision}: growth rate {gg:.6e} (oracle {go:.6e}, rel {abs(gg / go - 1.0):.2e}), "
+          f"total energy max rel diff {rel.max():.2e}, B growth x{bg.max() / bg[1]:.3g}, "
+          f"run {cfg0_runs[1][precision]:.1f} s, oracle {cfg0_runs[1]['oracle']:.1f} s")
     assert rel.max() <= ENERGY_RTOL, (precision, rel.max(), int(rel.argmax()))
 
 
@@ -87,6 +90,8 @@ def test_cfg0_fp64_first_steps_follow_oracle(cfg0_runs):
     runs, _ = cfg0_runs
     _, eo = runs["oracle"]
     _, eg = runs["fp64"]
+    worst = max(abs(eg[k, col] - eo[k, col]) / abs(eo[k, col]) for k in (1, 2) for col in range(eo.shape[1]))
+    print(f"cfg0 fp64 steps 10 and 20: energies within {worst:.2e} of the oracle")
     for k in (1, 2):
         for col in range(eo.shape[1]):
             assert abs(eg[k, col] - eo[k, col]) <= EARLY_RTOL * abs(eo[k, col]), (k, col, eg[k], eo[k])
