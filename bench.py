@@ -38,9 +38,10 @@ UNIT = "particle-updates/s"
 #    = 56 B, plus 600 B per cell for the cell's 5x5x3 current tile.
 BYTES_MIX_PUSH = 64
 # k_mix_push2's measured DRAM traffic per particle: dram__bytes_read.sum + dram__bytes_write.sum of
-# one launch on this 2048^2 x 64 ppc workload (18.331 + 17.326 GB for 536,870,912 particles, one
-# ncu pass), scaled to the particles of a launch (64.4 B per particle at 512^2)
-TRAFFIC_MIX_PUSH_PER_PARTICLE = (18330545408 + 17326184192) / 536870912
+# one launch on the 512^2 x 64 ppc case of the same physics (1.135 + 1.037 GB for 33,554,432
+# particles), scaled to the particles of a launch (an earlier build of the kernel moved 64.4 B per
+# particle at 512^2 and 66.4 B on the 2048^2 workload)
+TRAFFIC_MIX_PUSH_PER_PARTICLE = (1.135205e9 + 1.036641e9) / 33554432
 BYTES_PUSH_FP64 = 96
 BYTES_DEPOSIT_FP64 = 56
 BYTES_DEPOSIT_CELL = 600
@@ -563,7 +564,7 @@ def main():
     roofline = {"bound": "hbm", "kernel": "k_mix_push2 (fused push + deposit + column compaction, mixed precision)",
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "traffic": TRAFFIC_MIX_PUSH_PER_PARTICLE * (npart / world),
-                "traffic_unit": "bytes per launch (ncu dram read + write: 66.4 B per particle at 2048^2 x 64 ppc, scaled)",
+                "traffic_unit": "bytes per launch (ncu dram read + write: 64.7 B per particle at 512^2 x 64 ppc, scaled)",
                 "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "bytes_per_particle": BYTES_MIX_PUSH, "launch_ms": per_launch}
     launches = int(sum(v[1] for v in stages.values()))

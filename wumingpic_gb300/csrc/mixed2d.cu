@@ -520,16 +520,18 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
 // The push with the register current for the particles that stay in their cell only
 // (WPIC_MIX_PUSH2): a stayer's Esirkepov support is its cell's 3 x 3 nodes, so 21 registers
 // hold it (2 x 3 x-edges, 3 x 2 y-edges, 3 x 3 z-nodes); a particle that changes cell (about 1 in
-// 10 per step) joins its warp's queue and 32 of them are deposited at a time, one lane each,
-// straight into the tile's fixed-point current.  With the smaller stencil and shared memory laid
-// out for it (the TMA staging area becomes the queue and the pending leavers once the
-// cell-centred fields exist), three CTAs of 256 threads share an SM.
+// 10 per step) joins its warp's queue, and 32 of them at a time, one lane each, claim their
+// arrival slots, are deposited straight into the tile's fixed-point current and are written to
+// their new columns.  With the smaller stencil and shared memory laid out for it (the TMA
+// staging area becomes the queues and the per-thread staging slots once the cell-centred fields
+// exist), three CTAs of 256 threads share an SM.
 // ---------------------------------------------------------------------------
-constexpr int PF2 = 4;                           // particles in flight per thread
+constexpr int PF2 = 3;  // particles in flight per thread (as fast as four; the fourth slot's 8 KB holds the queues)
 constexpr int LQ2 = 64;                          // leaver queue entries per warp
-constexpr int LQ2W = 6;                          // ox, oy, new ox, new oy, q vz, packed (inc, species, cell)
-constexpr int LQ2_BYTES = (MP_THREADS / 32) * LQ2W * LQ2 * 4;
-constexpr int PEND2_BYTES = 9 * MP_THREADS * 4;  // per thread: the slot's 8 words + the new column (packed)
+constexpr int LQ2V = 3;                          // float4 per entry: (ox, oy, q vz, packed (inc, species, cell)),
+                                                 // then the new slot's two float4
+constexpr int LQ2_BYTES = (MP_THREADS / 32) * LQ2V * LQ2 * 16;
+constexpr int PEND2_BYTES = 8 * MP_THREADS * 4;  // per thread: a leaver's new slot, staged until its queue index is known
 constexpr int STAGE2_BYTES = 6 * TW * TW * 8;
 constexpr int A2_BYTES = (STAGE2_BYTES > LQ2_BYTES + PEND2_BYTES ? STAGE2_BYTES : LQ2_BYTES + PEND2_BYTES);
 constexpr int OFF2_J = (A2_BYTES + 127) / 128 * 128;
@@ -538,9 +540,14 @@ constexpr int OFF2_SFB = OFF2_SFA + TT * TT * 16;
 constexpr int OFF2_RING = OFF2_SFB + TT * TT * 8;
 constexpr int PUSH2_SMEM = OFF2_RING + PF2 * MIX_W * MIX_TC * 4;
 static_assert(OFF2_SFA % 16 == 0 && OFF2_RING % 16 == 0, "shared-memory alignment");
+// three CTAs per SM: 228 KB of shared memory per SM, 1 KB of it reserved per CTA, and the
+// kernel's static shared memory (under 512 bytes)
+static_assert(3 * (PUSH2_SMEM + 512 + 1024) <= 228 * 1024, "three CTAs of k_mix_push2 per SM");
 
 // Esirkepov current of one cell-leaver on the 5 x 5 stencil of its old cell (lx, ly), each value
-// added to the tile's fixed-point planes (pitch TW); the same arithmetic as the register path
+// added to the tile's fixed-point planes (pitch TW); the same arithmetic as the register path.
+// The three components are formed one after the other so that few weights are live at once
+// (the queue drain runs inside the particle loop, beside the register current).
 __device__ __forceinline__ void deposit_leaver2(float ox, float oy, float px_, float py_, int incx, int incy,
                                                 int lx, int ly, float qdd, float qg, int* jhi, int* jlo, float s1,
                                                 float is1, float s2) {
@@ -552,50 +559,58 @@ __device__ __forceinline__ void deposit_leaver2(float ox, float oy, float px_, f
   const float sy0 = 0.5f * (1.f - oy) * (1.f - oy), sy1 = 0.75f - (oy - 0.5f) * (oy - 0.5f), sy2 = 0.5f * oy * oy;
   const float s0x[5] = {0.f, sx0, sx1, sx2, 0.f};
   const float s0y[5] = {0.f, sy0, sy1, sy2, 0.f};
-  const float hq = -0.5f * qdd, hg = 0.5f * qg, tg = third * qg;
-  float wyq[5], wxq[5], zy[5], vy[5];
+  const float hq = -0.5f * qdd;
+  {  // jx on the x-edges (kk + 1, e)
+    float w[5];
 #pragma unroll
-  for (int e = 0; e < 5; ++e) {
-    if (e == 0 || e == 4) {
-      wyq[e] = hq * dsy[e];
-      wxq[e] = hq * dsx[e];
-      zy[e] = hg * dsy[e];
-      vy[e] = tg * dsy[e];
-    } else {
-      wyq[e] = -qdd * (s0y[e] + 0.5f * dsy[e]);
-      wxq[e] = -qdd * (s0x[e] + 0.5f * dsx[e]);
-      zy[e] = qg * (s0y[e] + 0.5f * dsy[e]);
-      vy[e] = qg * (0.5f * s0y[e] + third * dsy[e]);
-    }
-  }
-  float px = 0.f, py = 0.f;
+    for (int e = 0; e < 5; ++e) w[e] = (e == 0 || e == 4) ? hq * dsy[e] : -qdd * (s0y[e] + 0.5f * dsy[e]);
+    float px = 0.f;
 #pragma unroll
-  for (int kk = 0; kk < 4; ++kk) {
-    px += dsx[kk];
-    py += dsy[kk];
+    for (int kk = 0; kk < 4; ++kk) {
+      px += dsx[kk];
 #pragma unroll
-    for (int e = 0; e < 5; ++e) {
-      const float vx = px * wyq[e], vyv = py * wxq[e];
-      if (vx != 0.f) {
-        const int w = (0 * TW + ly + e) * TW + lx + kk + 1;
-        fx_add(jhi + w, jlo + w, vx, s1, is1, s2);
-      }
-      if (vyv != 0.f) {
-        const int w = (1 * TW + ly + kk + 1) * TW + lx + e;
-        fx_add(jhi + w, jlo + w, vyv, s1, is1, s2);
+      for (int e = 0; e < 5; ++e) {
+        const float v = px * w[e];
+        if (v != 0.f) {
+          const int a = (0 * TW + ly + e) * TW + lx + kk + 1;
+          fx_add(jhi + a, jlo + a, v, s1, is1, s2);
+        }
       }
     }
   }
+  {  // jy on the y-edges (e, kk + 1)
+    float w[5];
 #pragma unroll
-  for (int j = 0; j < 5; ++j)
+    for (int e = 0; e < 5; ++e) w[e] = (e == 0 || e == 4) ? hq * dsx[e] : -qdd * (s0x[e] + 0.5f * dsx[e]);
+    float py = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      py += dsy[kk];
+#pragma unroll
+      for (int e = 0; e < 5; ++e) {
+        const float v = py * w[e];
+        if (v != 0.f) {
+          const int a = (1 * TW + ly + kk + 1) * TW + lx + e;
+          fx_add(jhi + a, jlo + a, v, s1, is1, s2);
+        }
+      }
+    }
+  }
+  // jz on the nodes (i, j)
+  const float hg = 0.5f * qg, tg = third * qg;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    const float zy = (j == 0 || j == 4) ? hg * dsy[j] : qg * (s0y[j] + 0.5f * dsy[j]);
+    const float vy = (j == 0 || j == 4) ? tg * dsy[j] : qg * (0.5f * s0y[j] + third * dsy[j]);
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-      const float v = dsx[i] * vy[j] + s0x[i] * zy[j];
+      const float v = dsx[i] * vy + s0x[i] * zy;
       if (v != 0.f) {
-        const int w = (2 * TW + ly + j) * TW + lx + i;
-        fx_add(jhi + w, jlo + w, v, s1, is1, s2);
+        const int a = (2 * TW + ly + j) * TW + lx + i;
+        fx_add(jhi + a, jlo + a, v, s1, is1, s2);
       }
     }
+  }
 }
 
 struct StayCurrent {
@@ -640,8 +655,8 @@ template <bool VAY>
 __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __grid_constant__ CUtensorMap tm) {
   extern __shared__ __align__(128) unsigned char smem2[];
   double(*suf)[TW][TW] = reinterpret_cast<double(*)[TW][TW]>(smem2);
-  float* const lqueue = reinterpret_cast<float*>(smem2);               // [warp][LQ2W][LQ2], after staging
-  float* const pend = reinterpret_cast<float*>(smem2 + LQ2_BYTES);      // [9][256], after staging
+  float4* const lqueue = reinterpret_cast<float4*>(smem2);             // [warp][LQ2V][LQ2], after staging
+  float4* const pend4 = reinterpret_cast<float4*>(smem2 + LQ2_BYTES);  // [256][2], after staging
   int* const jhi = reinterpret_cast<int*>(smem2 + OFF2_J);             // [3][TW][TW]
   int* const jlo = jhi + 3 * TW * TW;
   float4* const sfa = reinterpret_cast<float4*>(smem2 + OFF2_SFA);     // (Bx, By, Bz, Ex) at cell centres
@@ -672,17 +687,18 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
   }
   float* const col0 = mix_slot(m, bin0, 0, c);
   float* const col1 = mix_slot(m, bin0 + (nsp > 1 ? 1 : 0), 0, c) - (size_t)n0 * MIX_PL;
-  auto issue = [&](int t) {
+  // particle t goes to ring slot t mod PF2 (rs, kept by the loop)
+  auto issue = [&](int t, int rs) {
     if (t < ntot) {
       const float* src = (t < n0 ? col0 : col1) + (size_t)t * MIX_PL;
-      float4* dst = ring + ((t & (PF2 - 1)) * MIX_TC + c) * 2;
+      float4* dst = ring + (rs * MIX_TC + c) * 2;
       cp_async16(dst, src);
       cp_async16(dst + 1, src + 4);
     }
     cp_async_commit();
   };
 #pragma unroll
-  for (int t = 0; t < PF2; ++t) issue(t);
+  for (int t = 0; t < PF2; ++t) issue(t, t);
   if (c == 0) mbar_init(&bar, 1);
   __syncthreads();
   if (c == 0) {
@@ -717,52 +733,53 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
   const int f0 = ly * TT + lx;
   StayCurrent acc;
   stay_zero(acc);
-  float* const myq = lqueue + (c >> 5) * LQ2W * LQ2;
+  float4* const myq = lqueue + (c >> 5) * LQ2V * LQ2;
   int qhead = 0, qtail = 0;  // the warp's leaver queue (warp-uniform)
+  // 32 leavers at a time, one per lane: claim the arrival slot (arrival number pos goes to slot
+  // depth - 1 - pos of the new column), deposit the current while the atomic is in flight, then
+  // write the slot (its key word holds the direction group and the index in the old column)
   auto drain = [&](int cnt) {
     if (lane < cnt) {
       const int e = (qhead + lane) & (LQ2 - 1);
-      const int pk = __float_as_int(myq[5 * LQ2 + e]);
-      const int cc = pk >> 8;
-      deposit_leaver2(myq[0 * LQ2 + e], myq[1 * LQ2 + e], myq[2 * LQ2 + e], myq[3 * LQ2 + e], (pk & 3) - 1,
-                      ((pk >> 2) & 3) - 1, cc & (MIX_TS - 1), cc >> 4, (pk >> 4) & 1 ? m.k_qdd[1] : m.k_qdd[0],
-                      myq[4 * LQ2 + e], jhi, jlo, fs1, fis1, fs2);
+      const float4 a = myq[e];
+      const int pk = __float_as_int(a.w);
+      const int incx = (pk & 3) - 1, incy = ((pk >> 2) & 3) - 1, s = (pk >> 4) & 1, cc = pk >> 8;
+      const int olx = cc & (MIX_TS - 1), oly = cc >> 4;
+      const int nlx = olx + incx, nly = oly + incy;
+      const int q = ((nly >> 4) + 1) * 3 + ((nlx >> 4) + 1);
+      const int dlc = (nly & (MIX_TS - 1)) * MIX_TS + (nlx & (MIX_TS - 1));
+      const int pos = atomicAdd(&m.acnt[nb_bin[s][q] * MIX_TC + dlc], 1);
+      {
+        const float4 b = myq[LQ2 + e];
+        deposit_leaver2(a.x, a.y, b.x, b.y, incx, incy, olx, oly, s ? m.k_qdd[1] : m.k_qdd[0], a.z, jhi, jlo, fs1,
+                        fis1, fs2);
+      }
+      const int dep = nb_dep[s][q];
+      if (pos >= dep) {
+        atomicOr(d.err, EB_CAPACITY);
+      } else {
+        float4* io = reinterpret_cast<float4*>(m.P + (((size_t)nb_off[s][q] + dep - 1 - pos) * MIX_TC + dlc) * MIX_W);
+        io[0] = myq[LQ2 + e];
+        io[1] = myq[2 * LQ2 + e];
+      }
     }
     qhead += cnt;
     __syncwarp();
   };
-  // the pending leaver of this thread (its slot in the new column returned by the last iteration's
-  // atomic): arrival number pos goes to slot depth - 1 - pos
-  float4* const pend4 = reinterpret_cast<float4*>(pend);  // [256][2]: the slot's words
-  int* const pdst = reinterpret_cast<int*>(pend + 8 * MP_THREADS);  // [256]: the new column
-  auto place = [&](int pos) {
-    const int dst = pdst[c];
-    const int q = dst & 15, s = (dst >> 4) & 1, dlc = dst >> 8;
-    const int dep = nb_dep[s][q];
-    if (pos >= dep) {
-      atomicOr(d.err, EB_CAPACITY);
-      return;
-    }
-    float4* io = reinterpret_cast<float4*>(m.P + (((size_t)nb_off[s][q] + dep - 1 - pos) * MIX_TC + dlc) * MIX_W);
-    io[0] = pend4[2 * c];
-    io[1] = pend4[2 * c + 1];
-  };
   int j0 = 0, j1 = 0;
-  int ppos = -1;
   int tw = ntot;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) tw = max(tw, __shfl_xor_sync(0xffffffffu, tw, o));
+  int rs = 0;
   for (int t = 0; t < tw; ++t) {
     cp_async_wait<PF2 - 1>();
-    if (ppos >= 0) place(ppos);
-    ppos = -1;
     bool leaves = false;
-    float lq0 = 0.f, lq1 = 0.f, lq2 = 0.f, lq3 = 0.f, lq4 = 0.f;
+    float lq0 = 0.f, lq1 = 0.f, lq2 = 0.f;
     int lpk = 0;
     if (t < ntot) {
       const bool sp1 = t >= n0;
       const int k = sp1 ? t - n0 : t;
-      const float4 pa = ring[((t & (PF2 - 1)) * MIX_TC + c) * 2], pb = ring[((t & (PF2 - 1)) * MIX_TC + c) * 2 + 1];
+      const float4 pa = ring[(rs * MIX_TC + c) * 2], pb = ring[(rs * MIX_TC + c) * 2 + 1];
       const float ox = pa.x, oy = pa.y;
       float ux = pa.z, uy = pa.w, uz = pb.x;
       const float idlo = pb.y, idhi = pb.z;
@@ -863,15 +880,9 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
       const float qg = qs * uz * ig;  // q * vz
       leaves = (incx | incy) != 0;
       if (leaves) {
-        const int nlx = lx + incx, nly = ly + incy;
-        const int q = ((nly >> 4) + 1) * 3 + ((nlx >> 4) + 1);
-        const int s = sp1 ? 1 : 0;
-        const int dlc = (nly & (MIX_TS - 1)) * MIX_TS + (nlx & (MIX_TS - 1));
-        ppos = atomicAdd(&m.acnt[nb_bin[s][q] * MIX_TC + dlc], 1);  // used in the next iteration
         pend4[2 * c] = make_float4(nx_, ny_, ux, uy);
         pend4[2 * c + 1] = make_float4(uz, idlo, idhi, __int_as_float((dir_group((incy + 1) * 3 + (incx + 1)) << 16) | k));
-        pdst[c] = q | (s << 4) | (dlc << 8);
-        lq0 = ox; lq1 = oy; lq2 = nx_; lq3 = ny_; lq4 = qg;
+        lq0 = ox; lq1 = oy; lq2 = qg;
         lpk = (incx + 1) | ((incy + 1) << 2) | ((sp1 ? 1 : 0) << 4) | (c << 8);
       } else {
         float4* so = reinterpret_cast<float4*>((sp1 ? col1 + (size_t)n0 * MIX_PL : col0) +
@@ -910,25 +921,22 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
         }
       }
     }
-    // leavers join the warp's queue; with 32 waiting they are deposited one per lane
+    // leavers join the warp's queue; with 32 waiting they are deposited and written one per lane
     const unsigned lm = __ballot_sync(0xffffffffu, leaves);
     if (leaves) {
       const int e = (qtail + __popc(lm & ((1u << lane) - 1u))) & (LQ2 - 1);
-      myq[0 * LQ2 + e] = lq0;
-      myq[1 * LQ2 + e] = lq1;
-      myq[2 * LQ2 + e] = lq2;
-      myq[3 * LQ2 + e] = lq3;
-      myq[4 * LQ2 + e] = lq4;
-      myq[5 * LQ2 + e] = __int_as_float(lpk);
+      myq[e] = make_float4(lq0, lq1, lq2, __int_as_float(lpk));
+      myq[LQ2 + e] = pend4[2 * c];
+      myq[2 * LQ2 + e] = pend4[2 * c + 1];
     }
     qtail += __popc(lm);
     __syncwarp();
     if (qtail - qhead >= 32) drain(32);
     if ((t & (FLUSH_EVERY - 1)) == FLUSH_EVERY - 1) stay_flush(acc, jhi, jlo, lx, ly, fs1, fis1, fs2);
-    issue(t + PF2);
+    issue(t + PF2, rs);
+    rs = rs == PF2 - 1 ? 0 : rs + 1;
   }
   cp_async_wait<0>();
-  if (ppos >= 0) place(ppos);
   if (qtail > qhead) drain(qtail - qhead);
   m.ccnt[bin0 * MIX_TC + c] = j0;
   if (nsp > 1) m.ccnt[(bin0 + 1) * MIX_TC + c] = j1;
