@@ -181,14 +181,18 @@ __device__ __forceinline__ void deposit_general(const float o[3], const float p[
     const int ea = (comp == 0 ? lx : comp == 1 ? ly : lz) + lo[comp] + 1;  // own axis: edge aw at ea + aw
     const int e1 = (t1 == 0 ? lx : ly) + lo[t1];
     const int e2 = (t2 == 1 ? ly : lz) + lo[t2];
-#pragma unroll
-    for (int kw = 0; kw < 4; ++kw) {
-      if (kw >= wd[t2]) continue;
+    // kw runs as a loop (the unrolled 4 x 4 x 3 sites per component made this function the
+    // largest part of the kernel's code, and the particle loop around it missed the
+    // instruction cache); s0w[t2][kw] and dsw[t2][kw] are selected, not indexed
+#pragma unroll 1
+    for (int kw = 0; kw < wd[t2]; ++kw) {
+      const float s0k = kw == 0 ? s0w[t2][0] : kw == 1 ? s0w[t2][1] : kw == 2 ? s0w[t2][2] : s0w[t2][3];
+      const float dsk = kw == 0 ? dsw[t2][0] : kw == 1 ? dsw[t2][1] : kw == 2 ? dsw[t2][2] : dsw[t2][3];
 #pragma unroll
       for (int jw = 0; jw < 4; ++jw) {
         if (jw >= wd[t1]) continue;
-        const float dstmp = ((s0w[t1][jw] + 0.5f * dsw[t1][jw]) * s0w[t2][kw] +
-                             (0.5f * s0w[t1][jw] + third * dsw[t1][jw]) * dsw[t2][kw]) * qdd;
+        const float dstmp = ((s0w[t1][jw] + 0.5f * dsw[t1][jw]) * s0k +
+                             (0.5f * s0w[t1][jw] + third * dsw[t1][jw]) * dsk) * qdd;
 #pragma unroll
         for (int aw = 0; aw < 3; ++aw) {
           if (aw >= wd[comp] - 1) continue;
