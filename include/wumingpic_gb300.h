@@ -107,9 +107,17 @@ int wpic_put_df(wpic_ctx* ctx, const double* df);
 int wpic_get_df(wpic_ctx* ctx, double* df);
 int wpic_get_uj(wpic_ctx* ctx, double* uj);
 
-/* particle__solv(gp, up, uf, cumcnt, nxs, nxe)      2d/common/particle.f90:48-179 */
+/* The drivers' staged calls.  On a WPIC_MIXED context they map onto the fused mixed step:
+ * particle__solv (or _vay) requests the push, field__fdtd_i runs the whole step (push, deposit,
+ * x boundary, cell-leavers into their columns, field solve), and bc__particle_x,
+ * bc__particle_y and sort__bucket find their work done; the Weibel order (push, field,
+ * particle_x) and the reconnection order (push, particle_x, field) are both accepted, and a
+ * shock context takes boundary_shock__injection's u0 between the push and the field solve.
+ * Out of order (a field solve without its push, a second push, particle_y or sort__bucket
+ * between push and field solve) they return WPIC_BAD_ARGUMENT.
+ * particle__solv(gp, up, uf, cumcnt, nxs, nxe)      2d/common/particle.f90:48-179 */
 int wpic_particle_solv(wpic_ctx* ctx);
-/* particle__solv_vay(gp,up,uf,cumcnt,nxs,nxe)  2d/common/particle.f90:182 (FP64 paths) */
+/* particle__solv_vay(gp,up,uf,cumcnt,nxs,nxe)  2d/common/particle.f90:182 */
 int wpic_particle_solv_vay(wpic_ctx* ctx);
 /* which push the fused step (wpic_step) uses: WPIC_PUSH_BORIS (default) or WPIC_PUSH_VAY */
 int wpic_set_pusher(wpic_ctx* ctx, int pusher);
@@ -125,7 +133,9 @@ int wpic_bc_injection(wpic_ctx* ctx, double u0);
 
 /* Moments (the driver's diagnostic block, 2d/proj/weibel/app.f90:121-123).  The device keeps
  * mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp) in the reference's layout: number density, the three
- * velocity components and the diagonal of u v at the half-integer nodes, per species.
+ * velocity components and the diagonal of u v at the half-integer nodes, per species.  On a
+ * mixed context mom_calc__nvt (from_gp = 1) computes the folded moments with the FP32
+ * half-step push, and mom_calc__accl and bc__mom have nothing left to do.
  * mom_calc__accl(gp,up,uf,cumcnt,nxs,nxe)   2d/common/mom_calc.f90:48   (FP64 paths): writes gp */
 int wpic_mom_calc_accl(wpic_ctx* ctx);
 /* mom_calc__nvt(mom,gp,np2)   2d/common/mom_calc.f90:164; from_gp = 1 reads gp (after
@@ -284,7 +294,11 @@ int wpic3d_get_fields(wpic_ctx3d* ctx, double* uf);
 int wpic3d_put_df(wpic_ctx3d* ctx, const double* df);
 int wpic3d_get_df(wpic_ctx3d* ctx, double* df);   /* the SAVEd dB/dE of field__fdtd_i */
 int wpic3d_get_uj(wpic_ctx3d* ctx, double* uj);   /* the current of the last field__fdtd_i */
-/* particle__solv(gp, up, uf, cumcnt, nxs, nxe)       3d/common/particle.f90:52 */
+/* The staged calls map onto the fused mixed step on a WPIC_MIXED context as in 2D:
+ * particle__solv (or _vay) requests the push, field__fdtd_i runs the step, bc__particle_x,
+ * bc__particle_yz and sort__bucket find their work done, boundary_shock__injection between
+ * the push and the field solve sets u0, mom_calc__nvt (from gp) computes the folded moments.
+ * particle__solv(gp, up, uf, cumcnt, nxs, nxe)       3d/common/particle.f90:52 */
 int wpic3d_particle_solv(wpic_ctx3d* ctx);
 /* particle__solv_vay(gp, up, uf, cumcnt, nxs, nxe)   3d/common/particle.f90:236 */
 int wpic3d_particle_solv_vay(wpic_ctx3d* ctx);

@@ -190,14 +190,22 @@ def test_mixed3d_shock_against_fp64(gpu_lib, nsteps):
     np.testing.assert_allclose(em, ef, rtol=1e-3, atol=1e-6 * ef.sum())
 
 
-def test_mixed3d_rejects_staged_calls_and_odd_tiles(gpu_lib):
+def test_mixed3d_rejects_out_of_order_staged_calls_and_odd_tiles(gpu_lib):
+    """A field solve without its push, a second push, and particle_yz or sort__bucket between
+    the push and the field solve are refused; so is a grid that is not a whole number of tiles."""
     from wumingpic_gb300._lib import WpicError
     p, st = perturbed(74)
     m = make(p, "mixed")
-    with pytest.raises(WpicError):
-        m.particle__solv()
+    m.put_state(st)
     with pytest.raises(WpicError):
         m.field__fdtd_i()
+    m.particle__solv()
+    for call in (m.particle__solv, m.bc__particle_yz, m.sort__bucket, lambda: m.step(1)):
+        with pytest.raises(WpicError):
+            call()
+    m.field__fdtd_i()
+    m.step(1)
+    m.close()
     p2, _ = small_case3d(nx=12, ny=16, nz=8, ppc=2, seed=75)
     with pytest.raises(WpicError):
         make(p2, "mixed")
@@ -252,3 +260,34 @@ def test_mixed3d_shock_expanding_window_against_fp64(gpu_lib):
     assert a[0].min() >= (p.nxgs + 1) * p.delx and a[0].max() <= (nxe + 1) * p.delx
     em, ef = m.energy(), f.energy()
     np.testing.assert_allclose(em, ef, rtol=1e-3, atol=1e-6 * ef.sum())
+
+
+def test_mixed3d_staged_calls_run_the_fused_step(gpu_lib):
+    """The 3D Weibel driver's call order (3d/proj/weibel/app.f90:103-108) on a mixed context:
+    particle__solv requests the push, field__fdtd_i runs the fused mixed step, particle_x,
+    particle_yz and sort__bucket find their work done.  Three steps equal wpic3d_step bit for
+    bit; the diagnostic block's calls give the mixed moments (1e-6 of each moment's largest
+    value: FP32 shared-memory sums whose order varies)."""
+    p, st = perturbed(74)
+    g, h = make(p, "mixed"), make(p, "mixed")
+    g.put_state(st)
+    h.put_state(st)
+    for _ in range(3):
+        g.particle__solv()
+        g.field__fdtd_i()
+        g.bc__particle_x()
+        g.bc__particle_yz()
+        g.sort__bucket()
+        h.step(1)
+    a, b = g.get_state(), h.get_state()
+    np.testing.assert_array_equal(a.np2, b.np2)
+    np.testing.assert_array_equal(a.uf, b.uf)
+    np.testing.assert_array_equal(by_id(a), by_id(b))
+    g.mom_calc__accl()
+    g.mom_calc__nvt()
+    g.bc__mom()
+    mg, mh = g.get_mom(), h.moments()
+    for q in range(7):
+        np.testing.assert_allclose(mg[q], mh[q], rtol=0, atol=1e-6 * np.abs(mh[q]).max())
+    g.close()
+    h.close()

@@ -58,6 +58,10 @@ struct wpic_ctx {
   std::vector<int> h_np2;
   double mix_vmax = 0.0;  // largest contribution of one particle to one node of the deposit
   int pusher = WPIC_PUSH_BORIS;  // the push of the fused step
+  // the drivers' staged calls on a mixed context: particle__solv asks for the push
+  // (mix_pending, with its pusher) and field__fdtd_i runs the fused mixed step
+  bool mix_pending = false;
+  int mix_pending_pusher = WPIC_PUSH_BORIS;
   double* mom = nullptr;         // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp), allocated on first use
   double u0 = 0.0;               // shock: upstream four-velocity of the injection boundary
   // adjoint: adjoint particle arrays (sorted-state and pushed slots), field adjoints, the
@@ -1326,16 +1330,43 @@ int wpic_put_df(wpic_ctx* c, const double* df) { return c ? put_field(c, df, c->
 int wpic_get_df(wpic_ctx* c, double* df) { return c ? get_field(c, df, c->d.df, 6) : WPIC_NOT_INITIALISED; }
 int wpic_get_uj(wpic_ctx* c, double* uj) { return c ? get_field(c, uj, c->d.uj, 3) : WPIC_NOT_INITIALISED; }
 
+namespace {
+// The staged calls on a mixed context.  The mixed step pushes, deposits, applies the x
+// boundary, moves the cell-leavers into their columns and solves the fields in one sequence
+// (mixed_step), so the drivers' calls map onto it: particle__solv asks for the push,
+// field__fdtd_i runs the whole step, and particle_x, particle_y and sort__bucket find their
+// work done.  Both driver orders are accepted (Weibel: push, field, particle_x; reconnection:
+// push, particle_x, field); the shock driver's injection call between the push and the field
+// solve sets the u0 the step uses.
+int mix_request_push(wpic_ctx* c, int pusher) {
+  if (c->mix_pending) return WPIC_BAD_ARGUMENT;  // a second push before the field solve
+  c->mix_pending = true;
+  c->mix_pending_pusher = pusher;
+  return WPIC_OK;
+}
+
+int mix_run_requested(wpic_ctx* c) {
+  if (!c->mix_pending) return WPIC_BAD_ARGUMENT;  // the field solve cannot run without its push
+  c->mix_pending = false;
+  const int saved = c->pusher;
+  c->pusher = c->mix_pending_pusher;
+  const int st = one_step(c);
+  c->pusher = saved;
+  const int st2 = finish(c);
+  return st ? st : st2;
+}
+}  // namespace
+
 int wpic_particle_solv(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) return mix_request_push(c, WPIC_PUSH_BORIS);
   do_push(c);
   return finish(c);
 }
 
 int wpic_particle_solv_vay(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) return mix_request_push(c, WPIC_PUSH_VAY);
   FP(push_vay2d, c->d, c->stream);
   return finish(c);
 }
@@ -1367,14 +1398,19 @@ int wpic_set_injection(wpic_ctx* c, double u0) {
 
 int wpic_bc_injection(wpic_ctx* c, double u0) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed || c->d.ph.bc != BC_SHOCK) return WPIC_BAD_ARGUMENT;
+  if (c->d.ph.bc != BC_SHOCK || !(u0 == u0)) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) {  // between the requested push and the field solve: the step's u0
+    if (!c->mix_pending) return WPIC_BAD_ARGUMENT;
+    c->u0 = u0;
+    return WPIC_OK;
+  }
   do_injection(c, u0);
   return finish(c);
 }
 
 int wpic_field_fdtd_i(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) return mix_run_requested(c);
   int st = do_field(c);
   int st2 = finish(c);
   return st ? st : st2;
@@ -1389,14 +1425,14 @@ int wpic_ele_cur(wpic_ctx* c) {
 
 int wpic_bc_particle_x(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) return WPIC_OK;  // inside the mixed step, before or after its field solve
   do_particle_x(c);
   return finish(c);
 }
 
 int wpic_bc_particle_y(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) return c->mix_pending ? WPIC_BAD_ARGUMENT : WPIC_OK;  // done by the mixed step
   int st = ensure_C(c);
   if (st) return st;
   Dev2D& d = c->d;
@@ -1414,7 +1450,7 @@ int wpic_bc_particle_y(wpic_ctx* c) {
 
 int wpic_sort_bucket(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) return c->mix_pending ? WPIC_BAD_ARGUMENT : WPIC_OK;  // done by the mixed step
   Dev2D& d = c->d;
   stage_begin(c, SG_SORT);
   sort_rank2d(d, d.B, nullptr, c->stream);
@@ -1425,6 +1461,7 @@ int wpic_sort_bucket(wpic_ctx* c) {
 
 int wpic_step(wpic_ctx* c, int nsteps) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mix_pending) return WPIC_BAD_ARGUMENT;  // a requested push waits for field__fdtd_i
   for (int it = 0; it < nsteps; ++it) {
     int st = one_step(c);
     int st2 = finish(c);
@@ -1465,25 +1502,32 @@ int copy_mom(wpic_ctx* c, double* out) {
 }
 }  // namespace
 
+// On a mixed context the diagnostic block's three calls map onto the mixed moments kernel,
+// which pushes the half step in FP32 without touching the particle state and folds the
+// ghost nodes: mom_calc__accl has nothing to write, mom_calc__nvt (after it, from gp)
+// computes the folded moments, bc__mom finds them folded.
 int wpic_mom_calc_accl(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) return c->mix_pending ? WPIC_BAD_ARGUMENT : WPIC_OK;
   FP(mom_accl2d, c->d, c->stream);
   return finish(c);
 }
 
 int wpic_mom_calc_nvt(wpic_ctx* c, int from_gp) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed || (from_gp != 0 && from_gp != 1)) return WPIC_BAD_ARGUMENT;
+  if (from_gp != 0 && from_gp != 1) return WPIC_BAD_ARGUMENT;
+  if (c->mixed && (from_gp != 1 || c->mix_pending)) return WPIC_BAD_ARGUMENT;
   int st = ensure_mom(c);
   if (st) return st;
-  FP(mom_nvt2d, c->d, from_gp ? c->d.B : c->d.A, c->mom, c->stream);
+  if (c->mixed) mix_moments2d(c->d, c->mom, c->stream);
+  else FP(mom_nvt2d, c->d, from_gp ? c->d.B : c->d.A, c->mom, c->stream);
   return finish(c);
 }
 
 int wpic_bc_mom(wpic_ctx* c) {
   if (!c) return WPIC_NOT_INITIALISED;
   if (!c->mom) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) return WPIC_OK;  // the mixed moments come folded
   bc_mom2d(c->d, c->mom, c->stream);
   return finish(c);
 }

@@ -26,7 +26,11 @@ struct wpic_ctx3d {
   int pusher = WPIC_PUSH_BORIS;  // the push of the fused step
   double u0 = 0.0;               // shock runs: the upstream four-velocity of the injection boundary
   double* mom = nullptr;         // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nzs-1:nze+1, nsp), on first use
-  bool mixed = false;            // FP32 push/deposit on split positions (fused step only)
+  bool mixed = false;            // FP32 push/deposit on split positions (the fused step)
+  // the drivers' staged calls on a mixed context: particle__solv asks for the push
+  // (mix_pending, with its pusher) and field__fdtd_i runs the fused mixed step
+  bool mix_pending = false;
+  int mix_pending_pusher = WPIC_PUSH_BORIS;
   Mix3Const mk{};
   alignas(128) unsigned char tmap[128];  // CUtensorMap of uf (mixed path TMA tile loads)
   // mixed path: the particle layers (reallocated when bins grow) and the host copy of the layout
@@ -597,16 +601,41 @@ int wpic3d_put_df(wpic_ctx3d* c, const double* df) { return c ? put_field3(c, df
 int wpic3d_get_df(wpic_ctx3d* c, double* df) { return c ? get_field3(c, df, c->d.df, 6) : WPIC_NOT_INITIALISED; }
 int wpic3d_get_uj(wpic_ctx3d* c, double* uj) { return c ? get_field3(c, uj, c->d.uj, 3) : WPIC_NOT_INITIALISED; }
 
+namespace {
+// The staged calls on a mixed context (the 3D counterpart of the 2D mapping): particle__solv
+// asks for the push, field__fdtd_i runs the fused mixed step (push, deposit, x boundary,
+// cell-leavers into their columns, field solve), particle_x, particle_yz and sort__bucket find
+// their work done; the shock driver's injection call between the push and the field solve
+// sets the step's u0.
+int mix3_request_push(wpic_ctx3d* c, int pusher) {
+  if (c->mix_pending) return WPIC_BAD_ARGUMENT;  // a second push before the field solve
+  c->mix_pending = true;
+  c->mix_pending_pusher = pusher;
+  return WPIC_OK;
+}
+
+int mix3_run_requested(wpic_ctx3d* c) {
+  if (!c->mix_pending) return WPIC_BAD_ARGUMENT;  // the field solve cannot run without its push
+  c->mix_pending = false;
+  const int saved = c->pusher;
+  c->pusher = c->mix_pending_pusher;
+  int st = one_step3(c);
+  c->pusher = saved;
+  const int st2 = finish3(c);
+  return st ? st : st2;
+}
+}  // namespace
+
 int wpic3d_particle_solv(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
+  if (c->mixed) return mix3_request_push(c, WPIC_PUSH_BORIS);
   FP3(push3d, c->d, c->stream);
   return finish3(c);
 }
 
 int wpic3d_particle_solv_vay(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
+  if (c->mixed) return mix3_request_push(c, WPIC_PUSH_VAY);
   FP3(push_vay3d, c->d, c->stream);
   return finish3(c);
 }
@@ -620,7 +649,7 @@ int wpic3d_set_pusher(wpic_ctx3d* c, int pusher) {
 
 int wpic3d_field_fdtd_i(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
+  if (c->mixed) return mix3_run_requested(c);
   int st = do_field3(c);
   if (st) return st;
   return finish3(c);
@@ -637,8 +666,8 @@ int wpic3d_ele_cur(wpic_ctx3d* c) {
 
 int wpic3d_bc_particle_x(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
   if (c->d.ph.bc == BC_SHOCK) return WPIC_BAD_ARGUMENT;  // boundary_shock has no particle_x
+  if (c->mixed) return WPIC_OK;  // inside the mixed step, before or after its field solve
   particle_x3d(c->d, c->d.B, c->stream);
   return finish3(c);
 }
@@ -663,7 +692,12 @@ int wpic3d_set_injection(wpic_ctx3d* c, double u0) {
 
 int wpic3d_bc_injection(wpic_ctx3d* c, double u0) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed || c->d.ph.bc != BC_SHOCK) return WPIC_BAD_ARGUMENT;
+  if (c->d.ph.bc != BC_SHOCK || !(u0 == u0)) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) {  // between the requested push and the field solve: the step's u0
+    if (!c->mix_pending) return WPIC_BAD_ARGUMENT;
+    c->u0 = u0;
+    return WPIC_OK;
+  }
   injection3d(c->d, c->d.B, u0, shock_xend3(c, u0), c->stream);
   return finish3(c);
 }
@@ -671,7 +705,7 @@ int wpic3d_bc_injection(wpic_ctx3d* c, double u0) {
 // bc__particle_yz on gp (B) in place: the post-migration order is gathered through map = slist
 int wpic3d_bc_particle_yz(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
+  if (c->mixed) return c->mix_pending ? WPIC_BAD_ARGUMENT : WPIC_OK;  // done by the mixed step
   Dev3D& d = c->d;
   migrate_scan3d(d, d.B, c->stream);
   migrate_plan3d(d, c->stream);
@@ -692,7 +726,7 @@ int wpic3d_bc_particle_yz(wpic_ctx3d* c) {
 // sort__bucket: gp (B) -> up (A) with cumcnt
 int wpic3d_sort_bucket(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path runs fused steps only
+  if (c->mixed) return c->mix_pending ? WPIC_BAD_ARGUMENT : WPIC_OK;  // done by the mixed step
   Dev3D& d = c->d;
   sort_rank3d(d, d.B, nullptr, c->stream);
   gather3d(d, d.B, d.A, d.map, d.np2, c->stream);
@@ -701,6 +735,7 @@ int wpic3d_sort_bucket(wpic_ctx3d* c) {
 
 int wpic3d_step(wpic_ctx3d* c, int nsteps) {
   if (!c) return WPIC_NOT_INITIALISED;
+  if (c->mix_pending) return WPIC_BAD_ARGUMENT;  // a requested push waits for field__fdtd_i
   for (int it = 0; it < nsteps; ++it) {
     int st = one_step3(c);
     if (st) return st;
@@ -741,25 +776,30 @@ int copy_mom3(wpic_ctx3d* c, double* out) {
 }
 }  // namespace
 
+// mixed context: mom_calc__nvt (from gp) computes the folded moments with the FP32 half-step
+// push, mom_calc__accl and bc__mom have nothing left to do
 int wpic3d_mom_calc_accl(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed) return WPIC_BAD_ARGUMENT;  // the mixed path computes moments with wpic3d_moments
+  if (c->mixed) return c->mix_pending ? WPIC_BAD_ARGUMENT : WPIC_OK;
   FP3(mom_accl3d, c->d, c->stream);
   return finish3(c);
 }
 
 int wpic3d_mom_calc_nvt(wpic_ctx3d* c, int from_gp) {
   if (!c) return WPIC_NOT_INITIALISED;
-  if (c->mixed || (from_gp != 0 && from_gp != 1)) return WPIC_BAD_ARGUMENT;
+  if (from_gp != 0 && from_gp != 1) return WPIC_BAD_ARGUMENT;
+  if (c->mixed && (from_gp != 1 || c->mix_pending)) return WPIC_BAD_ARGUMENT;
   int st = ensure_mom3(c);
   if (st) return st;
-  FP3(mom_nvt3d, c->d, from_gp ? c->d.B : c->d.A, c->mom, c->stream);
+  if (c->mixed) mix3_moments(c->d, c->mk, c->mom, c->stream);
+  else FP3(mom_nvt3d, c->d, from_gp ? c->d.B : c->d.A, c->mom, c->stream);
   return finish3(c);
 }
 
 int wpic3d_bc_mom(wpic_ctx3d* c) {
   if (!c) return WPIC_NOT_INITIALISED;
   if (!c->mom) return WPIC_BAD_ARGUMENT;
+  if (c->mixed) return WPIC_OK;  // the mixed moments come folded
   bc_mom3d(c->d, c->mom, c->stream);
   return finish3(c);
 }

@@ -9,12 +9,14 @@
  * those arrays, as the driver computes it (2d/proj/weibel/app.f90:479-545).  Between the
  * diagnostic steps no particle or field array crosses the host link.
  *
- * Usage: wpic_driver2d <in.bin> <out.bin> nx ny np nsteps intvl_mom
+ * Usage: wpic_driver2d <in.bin> <out.bin> nx ny np nsteps intvl_mom [precision]
+ * precision: 0 = WPIC_FP64 (default), 2 = WPIC_MIXED (the same calls run the fused mixed step;
+ * nx and ny multiples of 16).
  * in.bin: q[2], r[2] (doubles), then up(6, np, ny, 2), uf(6, nx+4, ny+4) (doubles),
  *         cumcnt(nx+1, ny, 2), np2(ny, 2) (int32), all in Fortran order.
  * out.bin: per diagnostic step: it (int32), up, np2, cumcnt, uf, mom(7, nx+2, ny+2, 2),
  *          energies (kinetic per species, E field, B field; doubles).
- * Grid: dx = 1, c dt/dx = 0.5, c = 1, gfac = 0.501, nxgs = nygs = 2, periodic, FP64 path.
+ * Grid: dx = 1, c dt/dx = 0.5, c = 1, gfac = 0.501, nxgs = nygs = 2, periodic.
  * Exit status 0 on success; a library status is printed with the call that returned it. */
 #include <math.h>
 #include <stdio.h>
@@ -62,10 +64,11 @@ static void energy_history(const double* up, const int* np2, const double* uf, i
 }
 
 int main(int argc, char** argv) {
-  if (argc != 8) {
-    fprintf(stderr, "usage: %s in.bin out.bin nx ny np nsteps intvl_mom\n", argv[0]);
+  if (argc != 8 && argc != 9) {
+    fprintf(stderr, "usage: %s in.bin out.bin nx ny np nsteps intvl_mom [precision]\n", argv[0]);
     return 1;
   }
+  const int precision = argc == 9 ? atoi(argv[8]) : WPIC_FP64;
   const int nx = atoi(argv[3]), ny = atoi(argv[4]), np = atoi(argv[5]);
   const int nsteps = atoi(argv[6]), intvl = atoi(argv[7]);
   if (nx < 4 || ny < 4 || np < 1 || nsteps < 1 || intvl < 1) return 1;
@@ -110,7 +113,7 @@ int main(int argc, char** argv) {
   prm.r[0] = r[0];
   prm.r[1] = r[1];
   prm.bc_kind = WPIC_BC_PERIODIC;
-  prm.precision = WPIC_FP64;
+  prm.precision = precision;
   wpic_ctx* ctx = NULL;
   CALL(wpic_init_2d(&ctx, &prm, NULL));
   /* the initial state crosses once (the shim's upload at the first particle__solv) */

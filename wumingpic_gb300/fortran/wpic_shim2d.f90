@@ -112,6 +112,20 @@ module wpic_capi
 
 contains
 
+  ! The arithmetic of the context, chosen without a driver change by the environment variable
+  ! WPIC_PRECISION: 'mixed' (WPIC_MIXED: the staged calls run the fused mixed step; the grid's
+  ! nx and ny, and nz in 3D, must be multiples of the tile edge), 'fp64_exact' (the reference's
+  ! operation order), anything else or unset: FP64.
+  integer(c_int) function wpic_env_precision()
+    character(len=32) :: val
+    integer :: n, stat
+    wpic_env_precision = 0
+    call get_environment_variable('WPIC_PRECISION', val, n, stat)
+    if (stat /= 0 .or. n < 1) return
+    if (val(1:n) == 'mixed') wpic_env_precision = 2
+    if (val(1:n) == 'fp64_exact') wpic_env_precision = 1
+  end function wpic_env_precision
+
   subroutine wpic_check(st, where)
     integer(c_int), intent(in) :: st
     character(len=*), intent(in) :: where
@@ -258,7 +272,7 @@ contains
     wpic_prm%delx = delx_in; wpic_prm%delt = delt_in; wpic_prm%c = c_in
     wpic_prm%q(1:nsp_in) = q_in; wpic_prm%r(1:nsp_in) = r_in
     if (.not. wpic_bc_set) wpic_prm%bc_kind = 0
-    wpic_prm%precision = 0; wpic_prm%device_cap = 0
+    wpic_prm%precision = wpic_env_precision(); wpic_prm%device_cap = 0
   end subroutine particle__init
 
   subroutine particle__solv(gp,up,uf,cumcnt,nxs,nxe)

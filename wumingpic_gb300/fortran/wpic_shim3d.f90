@@ -117,6 +117,21 @@ module wpic3d_capi
 
 contains
 
+  ! The arithmetic of the context, chosen without a driver change by the environment variable
+  ! WPIC_PRECISION: 'mixed' (WPIC_MIXED: the staged calls run the fused mixed step; the grid's
+  ! nx and ny, and nz in 3D, must be multiples of the tile edge), 'fp64_exact' (the reference's
+  ! operation order), anything else or unset: FP64.
+  integer(c_int) function wpic_env_precision()
+    character(len=32) :: val
+    integer :: n, stat
+    wpic_env_precision = 0
+    call get_environment_variable('WPIC_PRECISION', val, n, stat)
+    if (stat /= 0 .or. n < 1) return
+    if (val(1:n) == 'mixed') wpic_env_precision = 2
+    if (val(1:n) == 'fp64_exact') wpic_env_precision = 1
+  end function wpic_env_precision
+
+
   subroutine wpic3_check(st, where)
     integer(c_int), intent(in) :: st
     character(len=*), intent(in) :: where
@@ -220,7 +235,7 @@ contains
     wpic3_prm%nys = nys_in; wpic3_prm%nye = nye_in; wpic3_prm%nzs = nzs_in; wpic3_prm%nze = nze_in
     wpic3_prm%delx = delx_in; wpic3_prm%delt = delt_in; wpic3_prm%c = c_in
     wpic3_prm%q(1:nsp_in) = q_in; wpic3_prm%r(1:nsp_in) = r_in
-    wpic3_prm%precision = 0; wpic3_prm%device_cap = 0
+    wpic3_prm%precision = wpic_env_precision(); wpic3_prm%device_cap = 0
     if (.not. wpic3_bc_set) wpic3_prm%bc_kind = 0
   end subroutine particle__init
 
