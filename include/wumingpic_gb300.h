@@ -96,7 +96,9 @@ int wpic_finalize(wpic_ctx* ctx);
 /* State exchange in the reference layout.  which = 0: the sorted state 'up'
  * with its cumcnt; which = 1: the scratch/new state 'gp' (cumcnt ignored).
  * np2 is shared by both.  put validates np2 <= device capacity and the cumcnt
- * prefix sums. */
+ * prefix sums.  A mixed context keeps only the sorted state: put with which = 1 takes the
+ * unsorted rows of the restart path (io__input, before sort__bucket), sorts each row by x cell
+ * on the host and stores it as the sorted state. */
 int wpic_put_particles(wpic_ctx* ctx, int which, const double* up, const int* np2, const int* cumcnt);
 int wpic_get_particles(wpic_ctx* ctx, int which, double* up, int* np2, int* cumcnt);
 int wpic_put_fields(wpic_ctx* ctx, const double* uf);
@@ -285,7 +287,8 @@ typedef struct wpic_params3d {
    (3d/common/particle.f90:18, field.f90:22, sort.f90:18, boundary_periodic.f90:25) */
 int wpic3d_init(wpic_ctx3d** ctx, const wpic_params3d* p, void* cuda_stream);
 int wpic3d_finalize(wpic_ctx3d* ctx);
-/* which = 0: up (with cumcnt), 1: gp */
+/* which = 0: up (with cumcnt), 1: gp (on a mixed context: the unsorted rows of the restart
+ * path, sorted by x cell on the host into the sorted state) */
 int wpic3d_put_particles(wpic_ctx3d* ctx, int which, const double* up, const int* np2, const int* cumcnt);
 int wpic3d_get_particles(wpic_ctx3d* ctx, int which, double* up, int* np2, int* cumcnt);
 int wpic3d_put_fields(wpic_ctx3d* ctx, const double* uf);

@@ -51,6 +51,38 @@ def test_put_get_round_trip(gpu_lib):
             np.testing.assert_allclose(out.up[2:5, :n, jj, isp], st.up[2:5, :n, jj, isp], rtol=2 ** -23, atol=1e-30)
 
 
+def test_put_unsorted_rows_sorts_them(gpu_lib):
+    """The restart path on a mixed context: put with which = 1 (gp) takes rows whose particles
+    are in no particular order within the row, sorts them by x cell on the host and stores the
+    sorted state.  Against a put of the sorted rows: the same cumcnt and np2, the same particles
+    (matched by id), and after two steps the same fields to 1e-6 of their largest value (the
+    order within a cell changes the FP32 sums of the register current before each flush)."""
+    p, st = small_case(nx=32, ny=32, ppc=5, seed=14)
+    rng = np.random.default_rng(14)
+    up = np.array(st.up, order="F", copy=True)
+    for isp in range(p.nsp):
+        for jj in range(p.ny):
+            n = st.np2[jj, isp]
+            up[:, :n, jj, isp] = up[:, rng.permutation(n), jj, isp]
+    a, b = make(p, "mixed", gpu_lib), make(p, "mixed", gpu_lib)
+    a.put_state(st)
+    b.put_particles(1, up, st.np2)
+    b.put_fields(st.uf)
+    sa, sb = a.get_state(), b.get_state()
+    np.testing.assert_array_equal(sb.np2, sa.np2)
+    np.testing.assert_array_equal(sb.cumcnt, sa.cumcnt)
+    ia, ib = by_id(sa, p), by_id(sb, p)
+    assert ia.keys() == ib.keys()
+    for key in ia:
+        np.testing.assert_array_equal(ia[key], ib[key])
+    a.step(2)
+    b.step(2)
+    fa, fb = a.get_fields(), b.get_fields()
+    np.testing.assert_allclose(fb, fa, rtol=0, atol=1e-6 * np.abs(fa).max())
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("pusher", ["boris", "vay"])
 def test_one_step_against_fp64(gpu_lib, pusher):
     p, st = small_case(nx=32, ny=32, ppc=8, seed=6)

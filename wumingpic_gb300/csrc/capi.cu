@@ -660,7 +660,33 @@ int wpic_put_particles(wpic_ctx* c, int which, const double* up, const int* np2,
     }
     return WPIC_OK;
   };
-  if (c->mixed && which != 0) return WPIC_BAD_ARGUMENT;
+  if (c->mixed && which == 1) {
+    // the unsorted state of the restart path (io__input's up, before sort__bucket; the rows
+    // are right, the order within a row is not): each row is bucket-sorted on the host by
+    // its x cell i = int(x) as sort__bucket does (2d/common/sort.f90:60), stably, and put as
+    // the sorted state, which is all a mixed context keeps
+    std::vector<double> sorted((size_t)d.nrowjob * ndim * nph);
+    std::vector<int> cc((size_t)d.nrowjob * (nx + 1));
+    std::vector<int> cell(nph);
+    for (int r = 0; r < d.nrowjob; ++r) {
+      const double* row = up + (size_t)r * ndim * nph;
+      int* crow = cc.data() + (size_t)r * (nx + 1);
+      std::fill(crow, crow + nx + 1, 0);
+      for (int k = 0; k < np2[r]; ++k) {
+        const double x = row[(size_t)k * ndim];
+        int i = (x > -2147483648.0 && x < 2147483647.0) ? (int)x - d.g.nxgs : -1;
+        if (i < 0 || i >= nx) return WPIC_OUT_OF_RANGE;
+        cell[k] = i;
+        ++crow[i + 1];
+      }
+      for (int i = 0; i < nx; ++i) crow[i + 1] += crow[i];
+      std::vector<int> next(crow, crow + nx);
+      double* out = sorted.data() + (size_t)r * ndim * nph;
+      for (int k = 0; k < np2[r]; ++k)
+        std::copy(row + (size_t)k * ndim, row + (size_t)(k + 1) * ndim, out + (size_t)(next[cell[k]]++) * ndim);
+    }
+    return wpic_put_particles(c, 0, sorted.data(), np2, cc.data());
+  }
   if (!c->mixed) {
     const int st = check_cumcnt();
     if (st) return st;

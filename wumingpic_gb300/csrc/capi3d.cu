@@ -497,7 +497,33 @@ int wpic3d_put_particles(wpic_ctx3d* c, int which, const double* up, const int* 
         if (cc[i + 1] < cc[i]) return WPIC_BAD_ARGUMENT;
     }
   }
-  if (c->mixed && which != 0) return WPIC_BAD_ARGUMENT;
+  if (c->mixed && which == 1) {
+    // the unsorted state of the restart path (io__input's up, before sort__bucket; the rows
+    // are right, the order within a row is not): each row is bucket-sorted on the host by its
+    // x cell i = int(x) as sort__bucket does (3d/common/sort.f90:40-88), stably, and put as the
+    // sorted state, which is all a mixed context keeps
+    std::vector<double> sorted((size_t)d.nrow * ndim * nph);
+    std::vector<int> cc((size_t)d.nrow * (nx + 1));
+    std::vector<int> cell(nph);
+    for (int r = 0; r < d.nrow; ++r) {
+      const double* row = up + (size_t)r * ndim * nph;
+      int* crow = cc.data() + (size_t)r * (nx + 1);
+      std::fill(crow, crow + nx + 1, 0);
+      for (int q = 0; q < np2[r]; ++q) {
+        const double x = row[(size_t)q * ndim];
+        const int i = (x > -2147483648.0 && x < 2147483647.0) ? (int)x - d.g.nxgs : -1;
+        if (i < 0 || i >= nx) return WPIC_OUT_OF_RANGE;
+        cell[q] = i;
+        ++crow[i + 1];
+      }
+      for (int i = 0; i < nx; ++i) crow[i + 1] += crow[i];
+      std::vector<int> next(crow, crow + nx);
+      double* out = sorted.data() + (size_t)r * ndim * nph;
+      for (int q = 0; q < np2[r]; ++q)
+        std::copy(row + (size_t)q * ndim, row + (size_t)(q + 1) * ndim, out + (size_t)(next[cell[q]]++) * ndim);
+    }
+    return wpic3d_put_particles(c, 0, sorted.data(), np2, cc.data());
+  }
   CK3(cudaMemcpyAsync(d.np2, np2, sizeof(int) * d.nrow, cudaMemcpyHostToDevice, c->stream));
   if (which == 0)
     CK3(cudaMemcpyAsync(d.cc, cumcnt, sizeof(int) * (size_t)d.nrow * (nx + 1), cudaMemcpyHostToDevice, c->stream));
