@@ -120,13 +120,25 @@ def test_one_step_vay_exact_is_bit_exact_on_particles(gpu_lib):
 
 
 def test_vay_on_the_mixed_path_is_a_step_option(gpu_lib):
-    """The mixed path runs Vay inside its fused step (wpic_set_pusher); it has no separate
-    particle__solv_vay module call."""
+    """The mixed path runs Vay inside its fused step: wpic_set_pusher for wpic_step, or the
+    staged particle__solv_vay, which requests a Vay push that the following field__fdtd_i runs
+    (the two give the same state bit for bit)."""
     p, st = perturbed_case(seed=34, nx=16, ny=16)
     g = make_gpu(p, "mixed", gpu_lib)
+    g.put_state(st)
     g.set_pusher("vay")
-    with pytest.raises(RuntimeError):
-        g.particle__solv_vay()
+    g.step(1)
+    h = make_gpu(p, "mixed", gpu_lib)
+    h.put_state(st)
+    h.particle__solv_vay()
+    h.field__fdtd_i()
+    a, b = g.get_state(), h.get_state()
+    np.testing.assert_array_equal(a.np2, b.np2)
+    np.testing.assert_array_equal(a.uf, b.uf)
+    for isp in range(p.nsp):
+        for j in range(p.ny):
+            n = a.np2[j, isp]
+            np.testing.assert_array_equal(a.up[:, :n, j, isp], b.up[:, :n, j, isp])
 
 
 @pytest.mark.parametrize("precision,rel", [("fp64_exact", 0.0), ("fp64", REL)])
@@ -570,7 +582,7 @@ def test_shock_steps_with_expanding_window(gpu_lib, precision, rel):
 def test_shock_rejected_where_unsupported(gpu_lib):
     from wumingpic_gb300._lib import WpicError
     p, st, o = shock_setup(94, nx=32, ny=16)
-    g = make_gpu(p, "mixed", gpu_lib)  # the mixed path: inside its fused step only
+    g = make_gpu(p, "mixed", gpu_lib)  # the mixed path: only between a requested push and its field solve
     with pytest.raises(WpicError):
         g.bc__injection(p.u0)
     g.close()
@@ -580,3 +592,32 @@ def test_shock_rejected_where_unsupported(gpu_lib):
         g.set_window(q.nxgs, q.nxge - 2)  # periodic: the window is the whole domain
     with pytest.raises(WpicError):
         g.bc__injection(0.1)
+
+
+def test_shock_staged_calls_on_the_mixed_path(gpu_lib):
+    """The shock driver's order (2d/proj/shock/app.f90:110-115) on a mixed context:
+    particle__solv, boundary_shock__injection(u0), field__fdtd_i, particle_y, sort__bucket runs
+    the fused mixed step with that u0, the same state bit for bit as wpic_set_injection(u0) and
+    wpic_step."""
+    p, st, o = shock_setup(95, nx=32, ny=16)
+    g, h = make_gpu(p, "mixed", gpu_lib), make_gpu(p, "mixed", gpu_lib)
+    for x in (g, h):
+        x.put_state(st)
+        x.set_injection(0.0)
+    h.set_injection(p.u0)  # g receives p.u0 through its bc__injection calls only
+    for _ in range(3):
+        g.particle__solv()
+        g.bc__injection(p.u0)
+        g.field__fdtd_i()
+        g.bc__particle_y()
+        g.sort__bucket()
+        h.step(1)
+    a, b = g.get_state(), h.get_state()
+    np.testing.assert_array_equal(a.np2, b.np2)
+    np.testing.assert_array_equal(a.uf, b.uf)
+    for isp in range(p.nsp):
+        for j in range(p.ny):
+            n = a.np2[j, isp]
+            np.testing.assert_array_equal(a.up[:, :n, j, isp], b.up[:, :n, j, isp])
+    g.close()
+    h.close()

@@ -415,8 +415,8 @@ def test_shock_steps_with_expanding_window_3d(gpu_lib):
 
 
 def test_shock_injection_module_call_rejected_on_the_mixed_path_3d(gpu_lib):
-    """The mixed path applies the shock boundary inside its fused step; it has no separate
-    bc__injection module call."""
+    """The mixed path applies the shock boundary inside its fused step: bc__injection sets the
+    step's u0 between a requested push and its field solve, and is refused anywhere else."""
     from wumingpic_gb300._lib import WpicError
     p, st = small_case3d(nx=16, ny=16, nz=8, ppc=2, seed=84, bc="shock", window=12, u0=0.1)
     g = make_gpu(p, "mixed", gpu_lib)
