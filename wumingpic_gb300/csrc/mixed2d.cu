@@ -519,8 +519,8 @@ __global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d,
 // ---------------------------------------------------------------------------
 // The push with the register current for the particles that stay in their cell only
 // (WPIC_MIX_PUSH2): a stayer's Esirkepov support is its cell's 3 x 3 nodes, so 21 registers
-// hold it (2 x 3 x-edges, 3 x 2 y-edges, 3 x 3 z-nodes); a particle that changes cell (about 1 in
-// 10 per step) joins its warp's queue, and 32 of them at a time, one lane each, claim their
+// hold it (2 x 3 x-edges, 3 x 2 y-edges, 3 x 3 z-nodes); a particle that changes cell (4 in 100
+// per step on the 2D Weibel workload) joins its warp's queue, and 32 of them at a time, one lane each, claim their
 // arrival slots, are deposited straight into the tile's fixed-point current and are written to
 // their new columns.  With the smaller stencil and shared memory laid out for it (the TMA
 // staging area becomes the queues and the per-thread staging slots once the cell-centred fields
