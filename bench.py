@@ -47,9 +47,14 @@ BYTES_DEPOSIT_FP64 = 56
 BYTES_DEPOSIT_CELL = 600
 # FP64 floating-point operations per particle of the FP64 kernels, counted from the
 # reference's statements (2d/common/particle.f90:99-163, 2d/common/field.f90:224-298) with
-# each sqrt and divide counted as one operation
+# each sqrt and divide counted as one operation: `ref_fp64_gflops` is that count over the launch
+# time, a reference-equivalent rate (the FMA build's factored deposit executes fewer operations,
+# the push's FP64 sqrt and divides more)
 FLOP_PUSH_FP64 = 215
 FLOP_DEPOSIT_FP64 = 600
+# FP64 pipe utilisation of the same kernels measured by ncu (sm__inst_executed_pipe_fp64,
+# pct_of_peak_sustained_active) on one launch at 512^2 x 64 ppc: what bounds them
+FP64_PIPE_ACTIVE_NCU = {"k_push2d": 0.907, "k_deposit2d": 0.850}
 
 
 def config(name):
@@ -588,14 +593,15 @@ def main():
                     "k_deposit2d": {"launch_ms": dep_ms,
                                     "hbm_gbs": (BYTES_DEPOSIT_FP64 * n64 + BYTES_DEPOSIT_CELL * p.nx * p.ny)
                                     / (dep_ms / 1e3) / 1e9,
-                                    "fp64_gflops": FLOP_DEPOSIT_FP64 * n64 / (dep_ms / 1e3) / 1e9},
+                                    "ref_fp64_gflops": FLOP_DEPOSIT_FP64 * n64 / (dep_ms / 1e3) / 1e9},
                     "k_push2d": {"launch_ms": push64_ms,
                                  "hbm_gbs": BYTES_PUSH_FP64 * n64 / (push64_ms / 1e3) / 1e9,
-                                 "fp64_gflops": FLOP_PUSH_FP64 * n64 / (push64_ms / 1e3) / 1e9}},
+                                 "ref_fp64_gflops": FLOP_PUSH_FP64 * n64 / (push64_ms / 1e3) / 1e9}},
                 "stages_ms_per_step": {k: v[0] / args.fp64_steps for k, v in st64.items()}, "clocks": clk64}
-        for k in fp64["kernels"].values():
+        for name, k in fp64["kernels"].items():
             k["hbm_frac"] = k["hbm_gbs"] / hbm_peak
-            k["fp64_pipe_frac"] = k["fp64_gflops"] / peak64
+            k["ref_flops_over_fp64_peak"] = k["ref_fp64_gflops"] / peak64
+            k["fp64_pipe_active_ncu"] = FP64_PIPE_ACTIVE_NCU[name]
         fp64["moments"] = time_moments(g64, torch)
         g64.close()
 
@@ -659,9 +665,11 @@ def summary(line):
         k = f["kernels"]
         out["fp64_2d"] = {"value": r(f["value"]), "ms_per_step": r(f["ms_per_step"]),
                           "mixed_over_fp64": r(f["mixed_over_fp64"]), "fp64_fma_peak_gflops": r(f["fp64_fma_peak_gflops"]),
-                          "k_push2d": {"fp64_pipe_frac": r(k["k_push2d"]["fp64_pipe_frac"], 3),
+                          "k_push2d": {"fp64_pipe_active_ncu": FP64_PIPE_ACTIVE_NCU["k_push2d"],
+                                       "ref_flops_over_fp64_peak": r(k["k_push2d"]["ref_flops_over_fp64_peak"], 3),
                                        "hbm_frac": r(k["k_push2d"]["hbm_frac"], 3)},
-                          "k_deposit2d": {"fp64_pipe_frac": r(k["k_deposit2d"]["fp64_pipe_frac"], 3),
+                          "k_deposit2d": {"fp64_pipe_active_ncu": FP64_PIPE_ACTIVE_NCU["k_deposit2d"],
+                                          "ref_flops_over_fp64_peak": r(k["k_deposit2d"]["ref_flops_over_fp64_peak"], 3),
                                           "hbm_frac": r(k["k_deposit2d"]["hbm_frac"], 3)}}
     for key, name in (("mixed_3d_path", "mixed_3d"), ("fp64_3d_path", "fp64_3d")):
         v = line.get(key)
