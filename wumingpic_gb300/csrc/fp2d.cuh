@@ -406,9 +406,12 @@ __global__ void __launch_bounds__(DEP_THREADS) k_deposit2d(Dev2D d) {
       const double gvz = g5 * rsqrt(1. + (g3 * g3 + g4 * g4 + g5 * g5) * ic2);
 #endif
 #if !WPIC_REF_ORDER
-      // The same sums in factored form (about 170 instead of 400 FP64 operations per particle):
-      // the weights q dx/dt (s0 + ds/2) and q vz (s0_y + ds_y/2), q vz (s0_y/2 + ds_y/3) once per
-      // row or column, pjz = s0_x (x) A_y + ds_x (x) B_y, and the zero entries of s0_x left out.
+      // The same sums in factored form: the weights q dx/dt (s0 + ds/2) and q vz (s0_y + ds_y/2),
+      // q vz (s0_y/2 + ds_y/3) once per row or column; the prefix sums of ds_x and ds_y once per
+      // particle, so that every pjx / pjy entry is one fused multiply-add into its accumulator;
+      // pjz = s0_x (x) A_y + ds_x (x) B_y as two fused multiply-adds into the accumulator, the
+      // zero entries of s0_x left out.  About 190 FP64 instructions per particle; the pipe is
+      // the bound (GB300 issues FP64 at 1/64 of the FP32 rate).
       {
         const double qg = qs * gvz;
         double qwy[5], qwx[5], qay[5], qby[5];
@@ -420,34 +423,36 @@ __global__ void __launch_bounds__(DEP_THREADS) k_deposit2d(Dev2D d) {
           qby[e] = qg * (0.5 * s0y[e] + fac * dsy[e]);
           qwx[e] = qdd * (s0x[e] + 0.5 * dsx[e]);
         }
+        double px[4], py[4];
+        px[0] = dsx[0];
+        py[0] = dsy[0];
 #pragma unroll
-        for (int jp = 0; jp < 5; ++jp) {
-          double t = 0.0;
-#pragma unroll
-          for (int ip = 0; ip < 4; ++ip) {
-            t = fma(-dsx[ip], qwy[jp], t);
-            double* e = a + ((ip + 1) + 5 * jp) * DEP_THREADS;
-            *e += t;
-          }
-        }
-#pragma unroll
-        for (int ip = 0; ip < 5; ++ip) {
-          double t = 0.0;
-#pragma unroll
-          for (int jp = 0; jp < 4; ++jp) {
-            t = fma(-dsy[jp], qwx[ip], t);
-            double* e = a + (25 + ip + 5 * (jp + 1)) * DEP_THREADS;
-            *e += t;
-          }
+        for (int q = 1; q < 4; ++q) {
+          px[q] = px[q - 1] + dsx[q];
+          py[q] = py[q - 1] + dsy[q];
         }
 #pragma unroll
         for (int jp = 0; jp < 5; ++jp)
 #pragma unroll
+          for (int ip = 0; ip < 4; ++ip) {
+            double* e = a + ((ip + 1) + 5 * jp) * DEP_THREADS;
+            *e = fma(-px[ip], qwy[jp], *e);
+          }
+#pragma unroll
+        for (int ip = 0; ip < 5; ++ip)
+#pragma unroll
+          for (int jp = 0; jp < 4; ++jp) {
+            double* e = a + (25 + ip + 5 * (jp + 1)) * DEP_THREADS;
+            *e = fma(-py[jp], qwx[ip], *e);
+          }
+#pragma unroll
+        for (int jp = 0; jp < 5; ++jp)
+#pragma unroll
           for (int ip = 0; ip < 5; ++ip) {
-            double v = dsx[ip] * qby[jp];
-            if (ip != 0 && ip != 4) v = fma(s0x[ip], qay[jp], v);
             double* e = a + (50 + ip + 5 * jp) * DEP_THREADS;
-            *e += v;
+            double v = fma(dsx[ip], qby[jp], *e);
+            if (ip != 0 && ip != 4) v = fma(s0x[ip], qay[jp], v);
+            *e = v;
           }
       }
 #else
