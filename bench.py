@@ -54,7 +54,7 @@ FLOP_PUSH_FP64 = 215
 FLOP_DEPOSIT_FP64 = 600
 # FP64 pipe utilisation of the same kernels measured by ncu (sm__inst_executed_pipe_fp64,
 # pct_of_peak_sustained_active) on one launch at 512^2 x 64 ppc: what bounds them
-FP64_PIPE_ACTIVE_NCU = {"k_push2d": 0.907, "k_deposit2d": 0.850}
+FP64_PIPE_ACTIVE_NCU = {"k_push2d": 0.912, "k_deposit2d": 0.862}
 
 
 def config(name):
