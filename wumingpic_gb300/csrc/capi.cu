@@ -29,6 +29,7 @@ struct wpic_ctx {
   CGState* h_cg = nullptr;  // pinned mirror of the CG states
   int* h_err = nullptr;     // pinned mirror of the error word
   int cg_fixed[3] = {-1, -1, -1};
+  int cg_pred = 4;  // iterations enqueued before the first host check: the last solve's count
   int cg_iters[3] = {0, 0, 0};
   std::vector<void*> allocs;
   double* staging = nullptr;
@@ -240,18 +241,28 @@ int do_cg(wpic_ctx* c) {
     CK(cudaMemcpyAsync(&c->d.cg[l].fixed, &c->h_cg[l].fixed, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   FP(cg_init2d, c->d, c->stream);
   int launches = 2;
+  // The iterations run on device flags (a component that has converged returns at once), so
+  // the host only decides when to stop enqueueing: first as many iterations as the last solve
+  // took (the field changes little from step to step), then CG_CHECK_EVERY at a time.
+  int chunk = c->cg_pred;
   for (int guard = 0; guard < 100000; ++guard) {
-    CK(cudaMemcpyAsync(c->h_cg, c->d.cg, 3 * sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    if (!c->h_cg[0].active && !c->h_cg[1].active && !c->h_cg[2].active) break;
-    for (int k = 0; k < CG_CHECK_EVERY; ++k) {
+    for (int k = 0; k < chunk; ++k) {
       FP(cg_iter_ap2d, c->d, c->stream);
       FP(cg_iter_update2d, c->d, c->stream);
       FP(cg_iter_p2d, c->d, c->stream);
       launches += 6;
     }
+    CK(cudaMemcpyAsync(c->h_cg, c->d.cg, 3 * sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (!c->h_cg[0].active && !c->h_cg[1].active && !c->h_cg[2].active) break;
+    chunk = CG_CHECK_EVERY;
   }
-  for (int l = 0; l < 3; ++l) c->cg_iters[l] = c->h_cg[l].ite;
+  int most = 1;
+  for (int l = 0; l < 3; ++l) {
+    c->cg_iters[l] = c->h_cg[l].ite;
+    most = std::max(most, c->h_cg[l].ite);
+  }
+  c->cg_pred = std::min(most, 100);
   FP(cg_store2d, c->d, c->stream);
   stage_end(c, SG_CG, launches + 1);
   return WPIC_OK;

@@ -19,6 +19,7 @@ struct wpic_ctx3d {
   CGState* h_cg = nullptr;
   int* h_err = nullptr;
   int cg_fixed[3] = {-1, -1, -1};
+  int cg_pred = 4;  // iterations enqueued before the first host check: the last solve's count
   int cg_iters[3] = {0, 0, 0};
   std::vector<void*> allocs;
   double* staging = nullptr;
@@ -120,17 +121,26 @@ int do_cg3(wpic_ctx3d* c) {
   for (int l = 0; l < 3; ++l)
     CK3(cudaMemcpyAsync(&c->d.cg[l].fixed, &c->h_cg[l].fixed, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   FP3(cg_init3d, c->d, c->stream);
+  // the iterations run on device flags; the host enqueues the last solve's count first, then
+  // CG3_CHECK_EVERY at a time until every component has stopped
+  int chunk = c->cg_pred;
   for (int guard = 0; guard < 100000; ++guard) {
-    CK3(cudaMemcpyAsync(c->h_cg, c->d.cg, 3 * sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
-    CK3(cudaStreamSynchronize(c->stream));
-    if (!c->h_cg[0].active && !c->h_cg[1].active && !c->h_cg[2].active) break;
-    for (int k = 0; k < CG3_CHECK_EVERY; ++k) {
+    for (int k = 0; k < chunk; ++k) {
       FP3(cg_iter_ap3d, c->d, c->stream);
       FP3(cg_iter_update3d, c->d, c->stream);
       FP3(cg_iter_p3d, c->d, c->stream);
     }
+    CK3(cudaMemcpyAsync(c->h_cg, c->d.cg, 3 * sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
+    CK3(cudaStreamSynchronize(c->stream));
+    if (!c->h_cg[0].active && !c->h_cg[1].active && !c->h_cg[2].active) break;
+    chunk = CG3_CHECK_EVERY;
   }
-  for (int l = 0; l < 3; ++l) c->cg_iters[l] = c->h_cg[l].ite;
+  int most = 1;
+  for (int l = 0; l < 3; ++l) {
+    c->cg_iters[l] = c->h_cg[l].ite;
+    most = std::max(most, c->h_cg[l].ite);
+  }
+  c->cg_pred = std::min(most, 100);
   FP3(cg_store3d, c->d, c->stream);
   return WPIC_OK;
 }

@@ -651,7 +651,9 @@ __device__ __forceinline__ void stay_flush(StayCurrent& a, int* jhi, int* jlo, i
   stay_zero(a);
 }
 
-template <bool VAY>
+// WALLS: the reconnection or shock boundary in x (false: periodic, the boundary code left out of
+// the particle loop)
+template <bool VAY, bool WALLS>
 __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __grid_constant__ CUtensorMap tm) {
   extern __shared__ __align__(128) unsigned char smem2[];
   double(*suf)[TW][TW] = reinterpret_cast<double(*)[TW][TW]>(smem2);
@@ -729,7 +731,7 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
   const float cl = m.k_c;
   const float ic2 = m.k_ic2;
   const float third = 1.0f / 3.0f;
-  const bool walls = d.ph.bc != BC_PERIODIC;
+  constexpr bool walls = WALLS;
   const int f0 = ly * TT + lx;
   StayCurrent acc;
   stay_zero(acc);
@@ -959,10 +961,12 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
 void mix_push_deposit2d(const Dev2D& d, const void* tmap, bool vay, cudaStream_t s) {
   cudaMemsetAsync(d.m.ujx, 0, sizeof(unsigned long long) * 3 * (size_t)d.g.fplane, s);
 #if WPIC_MIX_PUSH2
-  if (vay)
-    k_mix_push2<true><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, *(const CUtensorMap*)tmap);
-  else
-    k_mix_push2<false><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, *(const CUtensorMap*)tmap);
+  const CUtensorMap& tm = *(const CUtensorMap*)tmap;
+  const bool walls = d.ph.bc != BC_PERIODIC;
+  if (vay && walls) k_mix_push2<true, true><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, tm);
+  else if (vay) k_mix_push2<true, false><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, tm);
+  else if (walls) k_mix_push2<false, true><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, tm);
+  else k_mix_push2<false, false><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, tm);
 #else
   if (vay)
     k_mix_push<true><<<d.m.ntile, MP_THREADS, PUSH_DYN_BYTES, s>>>(d, *(const CUtensorMap*)tmap);
@@ -1577,9 +1581,13 @@ int mix_setup2d(const Dev2D& d, void* out) {
           cudaSuccess ||
       cudaFuncSetAttribute(k_mix_push<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH_DYN_BYTES) !=
           cudaSuccess ||
-      cudaFuncSetAttribute(k_mix_push2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
+      cudaFuncSetAttribute(k_mix_push2<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
           cudaSuccess ||
-      cudaFuncSetAttribute(k_mix_push2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
+      cudaFuncSetAttribute(k_mix_push2<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_mix_push2<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_mix_push2<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
           cudaSuccess)
     return -3;
 
