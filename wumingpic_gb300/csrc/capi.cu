@@ -468,6 +468,22 @@ int one_step(wpic_ctx* c) {
 
 }  // namespace
 
+namespace {
+// The device address of a host array the GPU can read and write in place (page-locked and
+// mapped, as wpic_host_register makes it; on Grace the GPU reaches it over NVLink-C2C), or
+// null.  The mixed path's conversion kernels then read and write the host rows directly,
+// one pass over the link without staging copies.
+template <typename T>
+T* device_view(T* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, (const void*)p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost && a.devicePointer ? (T*)a.devicePointer : nullptr;
+}
+}  // namespace
+
 extern "C" {
 
 int wpic_init_2d(wpic_ctx** out, const wpic_params* p, void* cuda_stream) {
@@ -725,7 +741,8 @@ int wpic_put_particles(wpic_ctx* c, int which, const double* up, const int* np2,
       return WPIC_OK;
     };
     const int nchunk = c->prm.nsp * d.m.nty;
-    for (int k = 0; k < 2 && k < nchunk; ++k)
+    const double* dv = device_view(up);
+    for (int k = 0; k < 2 && k < nchunk && !dv; ++k)
       if ((st = copy_chunk(k))) return st;
     if ((st = check_cumcnt())) {
       sync_xfer(c);
@@ -749,6 +766,11 @@ int wpic_put_particles(wpic_ctx* c, int which, const double* up, const int* np2,
         if (fits && 5LL * mx[b] > 3LL * c->h_dep[b]) fits = false;
       }
       if (!fits && (st = mix_set_layout(c, dep, false))) return st;
+    }
+    if (dv) {  // the conversion kernels read the host rows in place
+      for (int isp = 0; isp < c->prm.nsp; ++isp)
+        mix_put2d(d, dv + (size_t)isp * d.g.ny * ndim * nph, ndim, nph, isp, 0, d.m.nty, c->stream);
+      return finish(c);
     }
     // one tile row (16 bucket rows) of one species per chunk: the valid prefix of each row is
     // copied into staging buffer k % 2 on the copy stream while the device converts chunk k - 1
@@ -798,6 +820,11 @@ int wpic_get_particles(wpic_ctx* c, int which, double* up, int* np2, int* cumcnt
     for (int r = 0; r < d.nrowjob; ++r)
       if (c->h_np2[r] > nph) return WPIC_CAPACITY;
     if (np2) std::copy(c->h_np2.begin(), c->h_np2.end(), np2);
+    if (double* dv = device_view(up)) {  // the kernels write the host rows in place
+      for (int isp = 0; isp < c->prm.nsp; ++isp)
+        mix_get2d(d, dv + (size_t)isp * d.g.ny * ndim * nph, ndim, nph, isp, 0, d.m.nty, c->stream);
+      return finish(c);
+    }
     const size_t row_bytes = (size_t)ndim * nph * sizeof(double);
     // chunk k is converted into staging buffer k % 2 while the copy stream moves chunk k - 1
     // to the host; only each row's valid prefix crosses the link
@@ -1674,7 +1701,7 @@ int wpic_num_stages(void) { return SG_COUNT; }
 
 int wpic_host_register(void* ptr, size_t bytes) {
   if (!ptr || !bytes) return WPIC_BAD_ARGUMENT;
-  return cuda_status(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  return cuda_status(cudaHostRegister(ptr, bytes, cudaHostRegisterMapped));
 }
 
 int wpic_host_unregister(void* ptr) {

@@ -1176,6 +1176,38 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_put(Dev2D d, const double* aos, 
     const long long nw = (long long)(scc[ly][MIX_TS] - first) * ndim;
     const double* rowp = aos + ((size_t)((ty - ty0) * MIX_TS + ly) * np_host + first) * ndim;
     const int gy = ty * MIX_TS + ly;
+    if (ndim == 6) {
+      // two words of a particle per thread ((x, y), (ux, uy) or (uz, id)): each warp reads 512
+      // contiguous bytes of the row with 16-byte loads -- whole lines, for a host array read in
+      // place over the host link -- and writes the matching part of the slot
+      const int n2 = (scc[ly][MIX_TS] - first) * 3;
+      for (int w2 = c; w2 < n2; w2 += MIX_TC) {
+        const int pl = w2 / 3, part = w2 - pl * 3;
+        const int p = first + pl;
+        int lx = 0;
+#pragma unroll
+        for (int step = 8; step > 0; step >>= 1)
+          if (scc[ly][lx + step] <= p) lx += step;
+        const int k = p - scc[ly][lx];
+        if (k >= dep) continue;
+        const double2 v = reinterpret_cast<const double2*>(rowp)[w2];
+        float* o = col0 + (size_t)k * MIX_PL + (ly * MIX_TS + lx) * MIX_W;
+        if (part == 0) {
+          const int gx = tx * MIX_TS + lx;
+          *reinterpret_cast<float2*>(o + MIX_OX) =
+              make_float2(fminf((float)(v.x * dxi - (double)(g.nxgs + gx)), 0.99999994f),
+                          fminf((float)(v.y * dxi - (double)(g.nygs + gy)), 0.99999994f));
+        } else if (part == 1) {
+          *reinterpret_cast<float2*>(o + MIX_UX) = make_float2((float)v.x, (float)v.y);
+        } else {
+          const long long id = __double_as_longlong(v.y);
+          *reinterpret_cast<float4*>(o + MIX_UZ) =
+              make_float4((float)v.x, __int_as_float((int)(unsigned)(id & 0xffffffffll)),
+                          __int_as_float((int)(unsigned)((unsigned long long)id >> 32)), 0.f);
+        }
+      }
+      continue;
+    }
     for (long long w = c; w < nw; w += MIX_TC) {
       const int pl = (int)(w / ndim), comp = (int)(w - (long long)pl * ndim);
       const int p = first + pl;
@@ -1314,6 +1346,37 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_get(Dev2D d, double* aos, int nd
     const long long nw = (long long)(last - first) * ndim;
     double* rowp = aos + ((size_t)((ty - ty0) * MIX_TS + ly) * np_host + (first > 0 ? first : 0)) * ndim;
     const int gy = ty * MIX_TS + ly;
+    if (ndim == 6) {
+      // two words of a particle per thread ((x, y), (ux, uy) or (uz, id)): each warp writes 512
+      // contiguous bytes of the row with 16-byte stores -- whole lines, for a host array written
+      // in place over the host link
+      const int n2 = (last - first) * 3;
+      for (int w2 = c; w2 < n2; w2 += MIX_TC) {
+        const int pl = w2 / 3, part = w2 - pl * 3;
+        const int p = first + pl;
+        int lx = 0;
+#pragma unroll
+        for (int step = 8; step > 0; step >>= 1)
+          if (scc[ly][lx + step] <= p) lx += step;
+        const int k = p - scc[ly][lx];
+        const float* o = col0 + (size_t)k * MIX_PL + (ly * MIX_TS + lx) * MIX_W;
+        double2 v;
+        if (part == 0) {
+          const float2 f = *reinterpret_cast<const float2*>(o + MIX_OX);
+          v = make_double2(((double)(g.nxgs + tx * MIX_TS + lx) + (double)f.x) * dx, ((double)(g.nygs + gy) + (double)f.y) * dx);
+        } else if (part == 1) {
+          const float2 f = *reinterpret_cast<const float2*>(o + MIX_UX);
+          v = make_double2((double)f.x, (double)f.y);
+        } else {
+          const float4 f = *reinterpret_cast<const float4*>(o + MIX_UZ);
+          const unsigned long long id = ((unsigned long long)(unsigned)__float_as_int(f.z) << 32) |
+                                        (unsigned)__float_as_int(f.y);
+          v = make_double2((double)f.x, __longlong_as_double((long long)id));
+        }
+        reinterpret_cast<double2*>(rowp)[w2] = v;
+      }
+      continue;
+    }
     for (long long w = c; w < nw; w += MIX_TC) {
       const int pl = (int)(w / ndim), comp = (int)(w - (long long)pl * ndim);
       const int p = first + pl;
