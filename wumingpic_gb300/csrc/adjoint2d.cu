@@ -342,36 +342,73 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const R* luj, Part
   for (int dim = 0; dim < 2; ++dim)
 #pragma unroll
     for (int i = 0; i < 5; ++i) gs0[dim][i] = gds[dim][i] = R(0);
-  // Jx: nodes (i + 1, j), i = 0..3, j = 0..4
+  // Jx: nodes (i + 1, j), i = 0..3, j = 0..4.  With Px the prefix sums of ds_x and
+  // Rx_i = sum_j wy_j lJx(i + 1, j): the adjoint of ds_x(i') is -qdd sum_{i >= i'} Rx_i, that of
+  // wy_j is -qdd sum_i Px_i lJx(i + 1, j) -- each lJx entry read once into two fused
+  // multiply-adds
+  const R wy[5] = {s0[1][0] + h5 * ds[1][0], s0[1][1] + h5 * ds[1][1], s0[1][2] + h5 * ds[1][2],
+                   s0[1][3] + h5 * ds[1][3], s0[1][4] + h5 * ds[1][4]};
+  const R wx[5] = {s0[0][0] + h5 * ds[0][0], s0[0][1] + h5 * ds[0][1], s0[0][2] + h5 * ds[0][2],
+                   s0[0][3] + h5 * ds[0][3], s0[0][4] + h5 * ds[0][4]};
+  {
+    R Px[4], Rx[4], gwy[5] = {R(0), R(0), R(0), R(0), R(0)};
+    Px[0] = ds[0][0];
 #pragma unroll
-  for (int j = 0; j < 5; ++j) {
-    const R wy = s0[1][j] + h5 * ds[1][j];
-    R suf = R(0), gw = R(0);
+    for (int q = 1; q < 4; ++q) Px[q] = Px[q - 1] + ds[0][q];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      R r = R(0);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        const R l = L0[(size_t)j * g.fp + i + 1];
+        r += wy[j] * l;
+        gwy[j] += Px[i] * l;
+      }
+      Rx[i] = r;
+    }
+    R suf = R(0);
 #pragma unroll
     for (int i = 3; i >= 0; --i) {
-      suf += L0[(size_t)j * g.fp + i + 1];  // sum_{i'' >= i} lJx(i'' + 1, j)
-      gds[0][i] += -qdd * wy * suf;
-      gw += ds[0][i] * suf;
+      suf += Rx[i];
+      gds[0][i] += -qdd * suf;
     }
-    gw *= -qdd;
-    gs0[1][j] += gw;
-    gds[1][j] += h5 * gw;
-  }
-  // Jy: nodes (i, j + 1), i = 0..4, j = 0..3
-  const R* L1 = L0 + P;
 #pragma unroll
-  for (int i = 0; i < 5; ++i) {
-    const R wx = s0[0][i] + h5 * ds[0][i];
-    R suf = R(0), gw = R(0);
+    for (int j = 0; j < 5; ++j) {
+      const R gw = -qdd * gwy[j];
+      gs0[1][j] += gw;
+      gds[1][j] += h5 * gw;
+    }
+  }
+  // Jy: nodes (i, j + 1), i = 0..4, j = 0..3, the same with the axes exchanged
+  const R* L1 = L0 + P;
+  {
+    R Py[4], Ry[4], gwx[5] = {R(0), R(0), R(0), R(0), R(0)};
+    Py[0] = ds[1][0];
+#pragma unroll
+    for (int q = 1; q < 4; ++q) Py[q] = Py[q - 1] + ds[1][q];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      R r = R(0);
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+        const R l = L1[(size_t)(j + 1) * g.fp + i];
+        r += wx[i] * l;
+        gwx[i] += Py[j] * l;
+      }
+      Ry[j] = r;
+    }
+    R suf = R(0);
 #pragma unroll
     for (int j = 3; j >= 0; --j) {
-      suf += L1[(size_t)(j + 1) * g.fp + i];
-      gds[1][j] += -qdd * wx * suf;
-      gw += ds[1][j] * suf;
+      suf += Ry[j];
+      gds[1][j] += -qdd * suf;
     }
-    gw *= -qdd;
-    gs0[0][i] += gw;
-    gds[0][i] += h5 * gw;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const R gw = -qdd * gwx[i];
+      gs0[0][i] += gw;
+      gds[0][i] += h5 * gw;
+    }
   }
   // Jz: nodes (i, j) = Qz (s0_x (x) Ay + ds_x (x) By), Ay = s0_y + ds_y / 2, By = s0_y / 2 + ds_y / 3
   const R* L2 = L0 + 2 * P;
@@ -385,7 +422,7 @@ __global__ void __launch_bounds__(128) k_adj_deposit(Dev2D d, const R* luj, Part
       const R l = L2[(size_t)j * g.fp + i];
       r1 += l * (s0[1][j] + h5 * ds[1][j]);
       r2 += l * (h5 * s0[1][j] + fac * ds[1][j]);
-      gAy[j] += l * s0[0][i];
+      if (i != 0 && i != 4) gAy[j] += l * s0[0][i];  // s0 is zero at the stencil's ends
       gBy[j] += l * ds[0][i];
     }
     gs0[0][i] += Qz * r1;
@@ -436,8 +473,10 @@ constexpr int AP_T = 128;
 template <typename R>
 __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const R* tmp, Parts64 lA, Parts64 lB,
                                                    double* ltmp) {
-  __shared__ R slf[6][AP_T + 1];
-  __shared__ R sw[6][AP_T + 1];
+  // per particle of the block: lf_m sy_b (the field adjoint times the y weight of node row b)
+  // and sx_a, so that each (cell, component, node) sum takes one fused multiply-add per particle
+  __shared__ R sq[18][AP_T + 1];
+  __shared__ R sxs[3][AP_T + 1];
   const Grid2D g = d.g;
   const int row = blockIdx.y;
   const int s0b = blockIdx.x * AP_T;
@@ -543,7 +582,8 @@ __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const R* tmp, Parts6
     for (int m = 0; m < 6; ++m) {
       lxa += lf[m] * fdx[m];
       lya += lf[m] * fdy[m];
-      slf[m][tid] = lf[m];
+#pragma unroll
+      for (int b = 0; b < 3; ++b) sq[m * 3 + b][tid] = lf[m] * sy[b];
     }
     // lA(x, y) = lB(x, y) + the gather's position derivative; the pass-through part in FP64
     lA.x[k] += lB.x[k] + (double)lxa;
@@ -552,10 +592,7 @@ __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const R* tmp, Parts6
     lA.uy[k] += (double)u1b[1];
     lA.uz[k] += (double)u1b[2];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      sw[a][tid] = sx[a];
-      sw[3 + a][tid] = sy[a];
-    }
+    for (int a = 0; a < 3; ++a) sxs[a][tid] = sx[a];
   }
   __syncthreads();
   // per (cell, component, node) sums over the block's particles of each cell
@@ -567,7 +604,7 @@ __global__ void __launch_bounds__(AP_T) k_adj_push(Dev2D d, const R* tmp, Parts6
     const int m = r / 9, ab = r - m * 9, b = ab / 3, a = ab - b * 3;
     const int p0 = max(ccr[cc], s0b) - s0b, p1 = min(ccr[cc + 1], last + 1) - s0b;
     R acc = R(0);
-    for (int p = p0; p < p1; ++p) acc += slf[m][p] * sw[a][p] * sw[3 + b][p];
+    for (int p = p0; p < p1; ++p) acc += sq[m * 3 + b][p] * sxs[a][p];
     if (acc != R(0)) atomicAdd(ltmp + (size_t)m * n + (size_t)(jj + b) * tw + (cc + a), (double)acc);
   }
 }

@@ -1036,7 +1036,7 @@ int adj_step(wpic_ctx* c, const wpic_ctx::AdjState* S) {
     d.B.id = B0.id;
     d.map = S->map;
     d.np2new = S->np2new;
-    adj_zero_parts(c->lB, slots, c->stream);
+    // the unsort writes every valid slot of lB (the step's permutation is a bijection)
     adj_unsort(d, c->lA, c->lB, c->stream);
     adj_zero_parts(c->lA, slots, c->stream);
     adj_field(d, c->luf, c->ldf, c->luj, c->stream);
@@ -1057,8 +1057,7 @@ int adj_step(wpic_ctx* c, const wpic_ctx::AdjState* S) {
   wrapx_migrate_scan2d(d, d.C, c->stream);
   migrate_plan2d(d, c->stream);
   sort_rank2d(d, d.C, d.slist, c->stream);
-  adj_zero_parts(c->lB, slots, c->stream);
-  adj_unsort(d, c->lA, c->lB, c->stream);
+  adj_unsort(d, c->lA, c->lB, c->stream);  // writes every valid slot of lB
   cudaMemcpyAsync(d.cc, c->adj_cc, ccb, cudaMemcpyDeviceToDevice, c->stream);  // the deposit and push read it
   adj_zero_parts(c->lA, slots, c->stream);
   adj_field(d, c->luf, c->ldf, c->luj, c->stream);
