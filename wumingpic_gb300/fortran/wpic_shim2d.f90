@@ -16,6 +16,10 @@
 ! wpic_shim_set_sync(n) (n >= 1) refreshes the host arrays every n steps instead,
 ! for drivers that read them elsewhere; the shock driver, which edits the host state
 ! every step, gets n = 1 and an upload every step from boundary_shock__init.
+! The environment variable WPIC_PRECISION chooses the arithmetic without a driver change:
+! 'mixed' runs the mixed-precision step (particle__solv requests the push, field__fdtd_i runs
+! the fused step, the boundary and sort calls find their work done), 'fp64_exact' the
+! reference-order FP64 build, anything else FP64.
 !
 ! The three boundary routines that field__fdtd_i receives as procedure arguments
 ! are accepted and ignored: the library applies the boundary of the kind chosen

@@ -9,6 +9,10 @@
 ! this file's wuming3d module wraps (3d/proj/weibel/app.f90 loop and diagnostic block);
 ! io__input makes the host the newer side.  wpic3d_shim_set_sync(n) (n >= 1) adds a
 ! refresh every n steps; the shock driver gets n = 1 from boundary_shock__init.
+! The environment variable WPIC_PRECISION chooses the arithmetic without a driver change:
+! 'mixed' runs the mixed-precision step (particle__solv requests the push, field__fdtd_i runs
+! the fused step, the boundary and sort calls find their work done), 'fp64_exact' the
+! reference-order FP64 build, anything else FP64.
 module wpic3d_capi
   use iso_c_binding
   implicit none
