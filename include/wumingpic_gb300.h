@@ -226,8 +226,9 @@ int wpic_num_stages(void);
  * register-only kernel; the compute roof the FP64 kernels are reported against. */
 int wpic_measure_fma_peak(int fp64, double* gflops);
 
-/* Page-lock (and release) a caller's host array, e.g. the reference-layout up/uf arrays,
- * so that wpic_put_* / wpic_get_* copy at full host-link bandwidth. */
+/* Page-lock and map (and release) a caller's host array, e.g. the reference-layout up/uf
+ * arrays, so that wpic_put_* / wpic_get_* move it at full host-link bandwidth; on a mixed 2D
+ * context the conversion kernels then read and write the registered particle array in place. */
 int wpic_host_register(void* ptr, size_t bytes);
 int wpic_host_unregister(void* ptr);
 
