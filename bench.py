@@ -453,10 +453,14 @@ def time_adjoint(steps, every, rank, dist, n=512):
     m_rec_ms, _ = rank_totals(m_rec * 1e3, npart, dist, "cuda")
     m_rev_ms, _ = rank_totals(m_rev * 1e3, npart, dist, "cuda")
     rel = lambda a, b: abs(a - b) / abs(b) if b else None  # noqa: E731
+    nfield = max(0, ((steps + every - 1) // every - 1) * every - 1)
     return {"workload": f"2D Weibel {n}^2 cells, 32 ppc/species ({npart} particles), drift +-0.3c, u_th 0.05c, "
                         f"64 Bz seed modes; L = final magnetic energy after {steps} steps",
             "steps": steps, "checkpoint_every": every, "dtype": "f64", "cg_rtol": 1e-13,
             "gradient_of": "L of the FP64 forward: both adjoints reverse the recorded FP64 trajectory",
+            "recompute": f"the last segment's step states kept by the record; the other segments pushed and "
+                         f"sorted again with the recorded fields replayed ({nfield} field states of "
+                         f"{12 * (n + 4) * (n + 4) * 8 / 2**20:.0f} MiB kept on the device)",
             "forward_ms": fwd_ms, "record_ms": rec_ms, "reverse_ms": rev_ms,
             "cost_over_forward": (rec_ms + rev_ms) / fwd_ms, "reverse_over_forward": rev_ms / fwd_ms,
             "cost_over_mixed_forward": (rec_ms + rev_ms) / mix_ms, "L": val,
@@ -725,10 +729,37 @@ def measure_e2e(g, p, dist=None):
     # what crosses the link: each row's valid prefix of up (np2 particles of ndim words), uf,
     # cumcnt and np2 (wpic_put_particles / wpic_get_particles copy the valid prefixes only)
     bytes_state = int(st.np2.sum()) * p.ndim * 8 + st.uf.nbytes + st.np2.nbytes + st.cumcnt.nbytes
+    link = measure_link()
+    ms_step = dt * 1e3 / steps
+    floor_ms = 1e3 * (bytes_state / (link["h2d_gbs"] * 1e9) + bytes_state / (link["d2h_gbs"] * 1e9))
+    link.update({"exchange_floor_ms_per_step": floor_ms, "e2e_ms_per_step": ms_step,
+                 "frac": floor_ms / ms_step})
     return {"value": n * steps / dt, "unit": UNIT, "h2d_bytes_per_step": int(bytes_state),
-            "d2h_bytes_per_step": int(bytes_state), "steps": steps,
+            "d2h_bytes_per_step": int(bytes_state), "steps": steps, "link": link,
             "note": "reference-layout host arrays (page-locked with wpic_host_register), the valid state in "
                     "and out every step"}
+
+
+def measure_link(nbytes=1 << 30, reps=3):
+    """The host link's copy bandwidth each way (one page-locked 1 GiB buffer, copy-engine
+    copies timed with CUDA events): the bound of the end-to-end exchange.  The conversion
+    kernels' in-place reads and writes of registered host memory reach the same figures."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    dbuf = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for key, dst, src in (("h2d_gbs", dbuf, h), ("d2h_gbs", h, dbuf)):
+        dst.copy_(src, non_blocking=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        out[key] = nbytes * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    del h, dbuf
+    return out
 
 
 if __name__ == "__main__":

@@ -196,6 +196,11 @@ int wpic_adjoint_record(wpic_ctx* ctx, int nsteps, int every);
 /* arithmetic of the reverse push and deposit sweeps: WPIC_FP64 (default) or WPIC_MIXED (FP32
    per particle along the recorded FP64 trajectory; fields, adjoint CG and sums stay FP64) */
 int wpic_adjoint_precision(wpic_ctx* ctx, int precision);
+/* keep (1, default) or not (0) the field state of every recorded step, 12 field planes of
+   doubles per step, when that fits in half of the free device memory: the reverse sweep's
+   recompute of a segment then pushes and sorts only, with the recorded fields replayed
+   (the same particle states as a full recompute, bit for bit).  Read by the next record. */
+int wpic_adjoint_keep_fields(wpic_ctx* ctx, int keep);
 int wpic_adjoint_reverse(wpic_ctx* ctx, const double* lam_uf_final, double* lam_up0, double* lam_uf0);
 /* dot-product checks <L x, y> = <x, L^T y> of the adjoint's transposed field operators on
  * random vectors (current fold, ghost copies, E update, RHS, cell-centre averaging): five

@@ -86,6 +86,7 @@ def lib():
         L.wpic_adjoint.argtypes = [vp, i, i, vp, vp, vp]
         L.wpic_adjoint_record.argtypes = [vp, i, i]
         L.wpic_adjoint_precision.argtypes = [vp, i]
+        L.wpic_adjoint_keep_fields.argtypes = [vp, i]
         L.wpic_adjoint_reverse.argtypes = [vp, vp, vp, vp]
         L.wpic_adjoint_selfcheck.argtypes = [vp, vp]
         L.wpic_adjoint_pushcheck.argtypes = [vp, ctypes.c_double, vp]

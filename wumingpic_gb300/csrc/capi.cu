@@ -83,6 +83,13 @@ struct wpic_ctx {
   int adj_nsteps = 0, adj_every = 1;  // the recorded forward run (0: none)
   int adj_fp32 = 0;  // the reverse push and deposit sweeps in FP32 (fields, CG and sums in FP64)
   bool adj_last_kept = false;  // the step states hold the recorded run's last segment
+  // the field state (uf, df) before each step j = 1 .. adj_nfield of the recorded run, slot
+  // j - 1: a recomputed segment then pushes and sorts only, its fields replayed from here
+  // instead of deposited and solved again
+  double* adj_fields = nullptr;
+  size_t adj_fields_slots = 0;  // states the buffer holds
+  int adj_nfield = 0;           // states of the recorded run in it
+  bool adj_keep_fields = true;  // wpic_adjoint_keep_fields
   float* adj_f32 = nullptr;     // FP32 copies of lJ / the cell-centred fields for the FP32 sweeps
   // scratch of the adjoint's self-checks, allocated on first use
   double* chk_dots = nullptr;
@@ -647,6 +654,7 @@ int wpic_finalize(wpic_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (void* p : c->allocs) cudaFree(p);
   if (c->mixP) cudaFree(c->mixP);
+  if (c->adj_fields) cudaFree(c->adj_fields);
   if (c->h_grow) cudaFreeHost(c->h_grow);
   for (int k = 0; k < 2; ++k)
     if (c->xfer[k]) cudaStreamSynchronize(c->xfer[k]);
@@ -945,8 +953,46 @@ int adj_alloc_step(wpic_ctx* c, wpic_ctx::AdjState& S) {
   return dalloc(c, &S.map, slots);
 }
 
-// one periodic step (one_step's order) that keeps B after the push and the sort's permutation
-int adj_forward_step(wpic_ctx* c, wpic_ctx::AdjState& S) {
+// The field store for n states (12 field planes each), when it fits in half of the free device
+// memory; otherwise no store (adj_nfield 0) and the segments are recomputed in full.
+int adj_field_store(wpic_ctx* c, int n) {
+  c->adj_nfield = 0;
+  if (n < 1 || !c->adj_keep_fields) return WPIC_OK;
+  const size_t per = 12 * (size_t)c->d.g.fplane;
+  if ((size_t)n > c->adj_fields_slots) {
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->adj_fields) cudaFree(c->adj_fields);
+    c->adj_fields = nullptr;
+    c->adj_fields_slots = 0;
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    if ((size_t)n * per * sizeof(double) > free_b / 2) return WPIC_OK;
+    void* v = nullptr;
+    if (cudaMalloc(&v, (size_t)n * per * sizeof(double)) != cudaSuccess) {
+      (void)cudaGetLastError();  // no store: the recompute runs the full step
+      return WPIC_OK;
+    }
+    c->adj_fields = (double*)v;
+    c->adj_fields_slots = n;
+  }
+  c->adj_nfield = n;
+  return WPIC_OK;
+}
+
+// the field state before step j (1 <= j <= adj_nfield) of the recorded run: into slot j - 1, or back
+void adj_field_slot(wpic_ctx* c, int j, bool save) {
+  Dev2D& d = c->d;
+  const size_t P6 = 6 * (size_t)d.g.fplane;
+  double* const f = c->adj_fields + (size_t)(j - 1) * 2 * P6;
+  const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+  cudaMemcpyAsync(save ? f : d.uf, save ? d.uf : f, P6 * sizeof(double), k, c->stream);
+  cudaMemcpyAsync(save ? f + P6 : d.df, save ? d.df : f + P6, P6 * sizeof(double), k, c->stream);
+}
+
+// one periodic step (one_step's order) that keeps B after the push and the sort's permutation;
+// replay > 0: the fields after the step are the stored state `replay` of the recorded run (the
+// same values the deposit and the solve gave then), so neither runs
+int adj_forward_step(wpic_ctx* c, wpic_ctx::AdjState& S, int replay = 0) {
   Dev2D& d = c->d;
   const size_t slots = (size_t)d.nrowjob * d.cap;
   do_push(c);
@@ -955,8 +1001,12 @@ int adj_forward_step(wpic_ctx* c, wpic_ctx::AdjState& S) {
     double* const to[5] = {S.B.x, S.B.y, S.B.ux, S.B.uy, S.B.uz};
     cudaMemcpyAsync(to[q], from[q], slots * 8, cudaMemcpyDeviceToDevice, c->stream);
   }
-  int st = do_field(c);
-  if (st) return st;
+  if (replay > 0) {
+    adj_field_slot(c, replay, false);
+  } else {
+    int st = do_field(c);
+    if (st) return st;
+  }
   do_migrate_sort(c, true);  // periodic: particle_x with particle_y's scan
   cudaMemcpyAsync(S.map, d.map, slots * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(S.np2new, d.np2new, (size_t)d.nrowjob * sizeof(int), cudaMemcpyDeviceToDevice, c->stream);
@@ -1288,6 +1338,13 @@ int wpic_adjoint_precision(wpic_ctx* c, int precision) {
   return WPIC_OK;
 }
 
+int wpic_adjoint_keep_fields(wpic_ctx* c, int keep) {
+  if (!c) return WPIC_NOT_INITIALISED;
+  if (keep != 0 && keep != 1) return WPIC_BAD_ARGUMENT;
+  c->adj_keep_fields = keep == 1;
+  return WPIC_OK;
+}
+
 // Forward half of the adjoint: nsteps steps from the current state, keeping the particle and
 // field state at every segment start (every K steps) and at the end.
 int wpic_adjoint_record(wpic_ctx* c, int nsteps, int every) {
@@ -1299,9 +1356,11 @@ int wpic_adjoint_record(wpic_ctx* c, int nsteps, int every) {
   int st = adj_prepare(c, nseg + every + 1);
   if (st) return st;
   // the last segment keeps its step states as it runs: the reverse sweep starts on it
-  // without recomputing it
+  // without recomputing it; the field state before each step 1 .. last0 - 1 goes to the
+  // field store (the other segments' recompute replays it)
   const int last0 = (nseg - 1) * every;
   c->adj_last_kept = false;
+  if ((st = adj_field_store(c, last0 - 1))) return st;
   for (int k = 0; k < nsteps; ++k) {
     if (k % every == 0) adj_save(c, c->adj_states[k / every]);
     if (k >= last0) {
@@ -1314,6 +1373,7 @@ int wpic_adjoint_record(wpic_ctx* c, int nsteps, int every) {
       }
     }
     if ((st = one_step(c))) return st;
+    if (k + 1 <= c->adj_nfield) adj_field_slot(c, k + 1, true);
   }
   adj_save(c, c->adj_states[nseg + every]);
   if ((st = finish(c))) return st;
@@ -1352,7 +1412,8 @@ int wpic_adjoint_reverse(wpic_ctx* c, const double* lam_uf_final, double* lam_up
       adj_save(c, S);
       S.has_step = false;
       if (k + 1 < s1) {  // the segment's last step is pushed and sorted again by adj_step
-        if ((st = adj_alloc_step(c, S)) || (st = adj_forward_step(c, S))) break;
+        const int replay = k + 1 <= c->adj_nfield ? k + 1 : 0;
+        if ((st = adj_alloc_step(c, S)) || (st = adj_forward_step(c, S, replay))) break;
       }
     }
     if (st) break;

@@ -135,6 +135,12 @@ class Pic2D:
         code = {"fp64": _lib.FP64, "fp64_exact": _lib.FP64_EXACT, "mixed": _lib.MIXED}[precision]
         check(lib().wpic_adjoint_precision(self._h, code), "adjoint_precision")
 
+    def adjoint_keep_fields(self, keep=True):
+        """Keep every recorded step's field state (default) so that the reverse sweep
+        recomputes a segment by pushing and sorting only; False recomputes the full steps.
+        Both give the same gradient bit for bit; read by the next adjoint_record."""
+        check(lib().wpic_adjoint_keep_fields(self._h, int(bool(keep))), "adjoint_keep_fields")
+
     def adjoint_record(self, nsteps, every):
         """The forward half of ``adjoint``: run nsteps steps keeping the state every `every` steps."""
         check(lib().wpic_adjoint_record(self._h, int(nsteps), int(every)), "adjoint_record")
