@@ -51,16 +51,25 @@ def test_put_get_round_trip(gpu_lib):
             np.testing.assert_allclose(out.up[2:5, :n, jj, isp], st.up[2:5, :n, jj, isp], rtol=2 ** -23, atol=1e-30)
 
 
-def test_put_get_in_place_through_registered_host_memory(gpu_lib):
+@pytest.mark.parametrize("off16", [0, 8])
+def test_put_get_in_place_through_registered_host_memory(gpu_lib, off16):
     """Host arrays page-locked with wpic_host_register are read and written in place by the
     conversion kernels (no staging copies): after two steps the same state as through ordinary
-    host arrays, bit for bit."""
+    host arrays, bit for bit.  The kernels move 16 bytes per access, so a particle array 8 bytes
+    off a 16-byte boundary (a view into a registered buffer) takes the staged copies instead,
+    with the same result."""
     from wumingpic_gb300 import _lib
     p, st = small_case(nx=32, ny=32, ppc=5, seed=24)
     a, b = make(p, "mixed", gpu_lib), make(p, "mixed", gpu_lib)
     a.put_state(st)
     reg = st.copy()
-    _lib.host_register(reg.up)
+    buf = np.zeros(reg.up.size + 2)
+    s0 = next(k for k in range(3) if (buf.ctypes.data + 8 * k) % 16 == off16)
+    view = buf[s0:s0 + reg.up.size].reshape(reg.up.shape, order="F")
+    view[...] = reg.up
+    assert view.ctypes.data % 16 == off16 and view.flags.f_contiguous
+    reg.up = view
+    _lib.host_register(buf)
     try:
         b.put_state(reg)
         a.step(2)
@@ -75,7 +84,7 @@ def test_put_get_in_place_through_registered_host_memory(gpu_lib):
                 n = sa.np2[jj, isp]
                 np.testing.assert_array_equal(sb.up[:, :n, jj, isp], sa.up[:, :n, jj, isp])
     finally:
-        _lib.host_unregister(reg.up)
+        _lib.host_unregister(buf)
     a.close()
     b.close()
 

@@ -479,7 +479,8 @@ namespace {
 // The device address of a host array the GPU can read and write in place (page-locked and
 // mapped, as wpic_host_register makes it; on Grace the GPU reaches it over NVLink-C2C), or
 // null.  The mixed path's conversion kernels then read and write the host rows directly,
-// one pass over the link without staging copies.
+// one pass over the link without staging copies.  They move 16 bytes per access, so an array
+// that is not 16-byte aligned takes the staged copies instead.
 template <typename T>
 T* device_view(T* p) {
   cudaPointerAttributes a{};
@@ -487,7 +488,8 @@ T* device_view(T* p) {
     (void)cudaGetLastError();
     return nullptr;
   }
-  return a.type == cudaMemoryTypeHost && a.devicePointer ? (T*)a.devicePointer : nullptr;
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer || ((size_t)a.devicePointer & 15)) return nullptr;
+  return (T*)a.devicePointer;
 }
 }  // namespace
 

@@ -1181,7 +1181,11 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_put(Dev2D d, const double* aos, 
       // contiguous bytes of the row with 16-byte loads -- whole lines, for a host array read in
       // place over the host link -- and writes the matching part of the slot
       const int n2 = (scc[ly][MIX_TS] - first) * 3;
-      for (int w2 = c; w2 < n2; w2 += MIX_TC) {
+      // each warp's 512 bytes start on a 128-byte line of the host array: w2 = 0 lies `skew`
+      // 16-byte units above a line start, so the loop starts that many units early
+      const int skew = (int)(((size_t)rowp >> 4) & 7);
+      for (int w2 = c - skew; w2 < n2; w2 += MIX_TC) {
+        if (w2 < 0) continue;
         const int pl = w2 / 3, part = w2 - pl * 3;
         const int p = first + pl;
         int lx = 0;
@@ -1351,7 +1355,9 @@ __global__ void __launch_bounds__(MIX_TC) k_mix_get(Dev2D d, double* aos, int nd
       // contiguous bytes of the row with 16-byte stores -- whole lines, for a host array written
       // in place over the host link
       const int n2 = (last - first) * 3;
-      for (int w2 = c; w2 < n2; w2 += MIX_TC) {
+      const int skew = (int)(((size_t)rowp >> 4) & 7);  // whole 128-byte lines per warp, as in k_mix_put
+      for (int w2 = c - skew; w2 < n2; w2 += MIX_TC) {
+        if (w2 < 0) continue;
         const int pl = w2 / 3, part = w2 - pl * 3;
         const int p = first + pl;
         int lx = 0;
