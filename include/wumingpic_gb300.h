@@ -62,9 +62,9 @@ extern "C" {
 #define WPIC_MIXED 2      /* positions as integer cell + FP32 offset, FP32 push / gather / deposition
                              weights, FP32 tile currents flushed into FP64 J, FP64 field solve.
                              Requires nx and ny to be multiples of 16; particles live in 16 x 16-cell
-                             tile bins whose capacity is np * 256 / nx slots per species.  Only the fused
-                             wpic_step, the state exchange (which = 0), the loader and the
-                             diagnostics are available in this mode. */
+                             tile bins whose capacity is np * 256 / nx slots per species.  The drivers'
+                             staged calls map onto the fused step (see wpic_particle_solv), and the
+                             state exchange keeps only the sorted state (see wpic_put_particles). */
 
 /* the push of the fused step: particle__solv (Buneman-Boris) or particle__solv_vay */
 #define WPIC_PUSH_BORIS 0
@@ -233,7 +233,8 @@ int wpic_measure_fma_peak(int fp64, double* gflops);
 
 /* Page-lock and map (and release) a caller's host array, e.g. the reference-layout up/uf
  * arrays, so that wpic_put_* / wpic_get_* move it at full host-link bandwidth; on a mixed 2D
- * context the conversion kernels then read and write the registered particle array in place. */
+ * context the conversion kernels then read and write the registered particle array in place
+ * (when it is 16-byte aligned, as malloc and Fortran allocations are; otherwise staged copies). */
 int wpic_host_register(void* ptr, size_t bytes);
 int wpic_host_unregister(void* ptr);
 
