@@ -199,7 +199,8 @@ int wpic_adjoint_precision(wpic_ctx* ctx, int precision);
 /* keep (1, default) or not (0) the field state of every recorded step, 12 field planes of
    doubles per step, when that fits in half of the free device memory: the reverse sweep's
    recompute of a segment then pushes and sorts only, with the recorded fields replayed
-   (the same particle states as a full recompute, bit for bit).  Read by the next record. */
+   (the same particle states as a full recompute, bit for bit).  Read by the next record;
+   0 also frees the store, after which a recorded run is recomputed in full. */
 int wpic_adjoint_keep_fields(wpic_ctx* ctx, int keep);
 int wpic_adjoint_reverse(wpic_ctx* ctx, const double* lam_uf_final, double* lam_up0, double* lam_uf0);
 /* dot-product checks <L x, y> = <x, L^T y> of the adjoint's transposed field operators on

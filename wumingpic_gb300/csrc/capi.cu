@@ -1344,6 +1344,13 @@ int wpic_adjoint_keep_fields(wpic_ctx* c, int keep) {
   if (!c) return WPIC_NOT_INITIALISED;
   if (keep != 0 && keep != 1) return WPIC_BAD_ARGUMENT;
   c->adj_keep_fields = keep == 1;
+  if (!keep && c->adj_fields) {  // give the store back; a recorded run is then recomputed in full
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaFree(c->adj_fields));
+    c->adj_fields = nullptr;
+    c->adj_fields_slots = 0;
+    c->adj_nfield = 0;
+  }
   return WPIC_OK;
 }
 
