@@ -716,11 +716,21 @@ def measure_e2e(g, p, dist=None):
     g.put_state(st)
     g.step(1)
     g.get_state(st)
+    # the three calls return after their work has finished (each synchronises its stream),
+    # so marks between them split the step into the exchange in, the step and the exchange out
+    split = [0.0, 0.0, 0.0]
     t0 = time.perf_counter()
     for _ in range(steps):
+        ta = time.perf_counter()
         g.put_state(st)
+        tb = time.perf_counter()
         g.step(1)
+        tc = time.perf_counter()
         g.get_state(st)
+        td = time.perf_counter()
+        split[0] += tb - ta
+        split[1] += tc - tb
+        split[2] += td - tc
     dt = time.perf_counter() - t0
     for a in pinned:
         _lib.host_unregister(a)
@@ -732,8 +742,11 @@ def measure_e2e(g, p, dist=None):
     link = measure_link()
     ms_step = dt * 1e3 / steps
     floor_ms = 1e3 * (bytes_state / (link["h2d_gbs"] * 1e9) + bytes_state / (link["d2h_gbs"] * 1e9))
+    put_s, step_s, get_s = (x / steps for x in split)
     link.update({"exchange_floor_ms_per_step": floor_ms, "e2e_ms_per_step": ms_step,
-                 "frac": floor_ms / ms_step})
+                 "frac": floor_ms / ms_step,
+                 "split_ms_per_step": {"put": put_s * 1e3, "step": step_s * 1e3, "get": get_s * 1e3},
+                 "put_gbs": bytes_state / put_s / 1e9, "get_gbs": bytes_state / get_s / 1e9})
     return {"value": n * steps / dt, "unit": UNIT, "h2d_bytes_per_step": int(bytes_state),
             "d2h_bytes_per_step": int(bytes_state), "steps": steps, "link": link,
             "note": "reference-layout host arrays (page-locked with wpic_host_register), the valid state in "
