@@ -38,23 +38,8 @@ namespace {
 constexpr int MP_THREADS = MIX_TC;  // one thread per cell of the tile
 constexpr int TW = MIX_TS + 4;      // staged field nodes per tile edge (cells -2 .. 17)
 constexpr int TT = MIX_TS + 2;      // cell-centred values per tile edge (cells -1 .. 16)
-// Row pitch of the fixed-point current tile: the 32 lanes of a warp own cells of two
-// consecutive rows; a pitch of 16 (mod 32) words puts the two rows on disjoint banks.
-constexpr int JP = 48;
 constexpr int FLUSH_EVERY = MIX_FLUSH;  // particles accumulated in registers between flushes
-constexpr int PF = 8;               // particles in flight per push thread (shared-memory ring)
-constexpr int PF_BYTES = PF * 7 * MIX_TC * 4;  // the key word is not prefetched
 constexpr unsigned long long kSpinLimit = 1ull << 22;  // a few seconds at most
-// resident CTAs per SM asked of the push kernel; at 2 its 128 registers per thread still hold
-// the cell's whole current stencil without spilling
-#ifndef WPIC_MIX_MINB
-#define WPIC_MIX_MINB 2
-#endif
-// 1: the push with a register current for the particles that stay in their cell and a per-warp
-// queue for the ones that leave (k_mix_push2); 0: the full-stencil register push (k_mix_push)
-#ifndef WPIC_MIX_PUSH2
-#define WPIC_MIX_PUSH2 1
-#endif
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -100,10 +85,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar) {
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
-// 4-byte asynchronous global -> shared copy, completion tracked per thread by commit groups
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
-}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
@@ -123,12 +104,6 @@ __device__ __forceinline__ void reflect_split(int& cell, float& off, int wc, flo
 // direction code d = (dy + 1) * 3 + (dx + 1) of a move (4 = same cell) -> group index 0..7
 __device__ __forceinline__ int dir_group(int d) { return d < 4 ? d : d - 1; }
 
-struct CellCurrent {
-  // the cell's stencil over node offsets -2..2: jx[k][j] at x node k+1, y node j;
-  // jy[k][i] at y node k+1, x node i; jz[j][i]
-  float jx[4][5], jy[4][5], jz[5][5];
-};
-
 // a0 += x0 y0, a1 += x1 y1 as one packed FP32x2 fused multiply-add (each lane rounds as fmaf)
 __device__ __forceinline__ void ffma2_into(float& a0, float& a1, float x0, float x1, float y0, float y1) {
   const float2 r = __ffma2_rn(make_float2(x0, x1), make_float2(y0, y1), make_float2(a0, a1));
@@ -136,389 +111,11 @@ __device__ __forceinline__ void ffma2_into(float& a0, float& a1, float x0, float
   a1 = r.y;
 }
 
-__device__ __forceinline__ void cell_zero(CellCurrent& a) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-#pragma unroll
-    for (int j = 0; j < 5; ++j) a.jx[k][j] = a.jy[k][j] = 0.f;
-#pragma unroll
-  for (int j = 0; j < 5; ++j)
-#pragma unroll
-    for (int i = 0; i < 5; ++i) a.jz[j][i] = 0.f;
-}
-
-// add the register stencil of cell (lx, ly) into the tile planes (plane origin = local cell -2)
-__device__ __forceinline__ void cell_flush(CellCurrent& a, int (*jhi)[TW][JP], int (*jlo)[TW][JP], int lx, int ly,
-                                           float s1, float is1, float s2) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-      fx_add(&jhi[0][ly + j][lx + k + 1], &jlo[0][ly + j][lx + k + 1], a.jx[k][j], s1, is1, s2);
-      fx_add(&jhi[1][ly + k + 1][lx + j], &jlo[1][ly + k + 1][lx + j], a.jy[k][j], s1, is1, s2);
-    }
-#pragma unroll
-  for (int j = 0; j < 5; ++j)
-#pragma unroll
-    for (int i = 0; i < 5; ++i) fx_add(&jhi[2][ly + j][lx + i], &jlo[2][ly + j][lx + i], a.jz[j][i], s1, is1, s2);
-  cell_zero(a);
-}
-
 }  // namespace
 
-// a leaver of the push waiting for its slot (one per thread): the top slot of its new column,
-// that column's depth, and the eight 32-bit words of the entry (five FP32 components, the id's
-// two words, the arrival key)
-struct PendingLeaver {
-  float* top[MP_THREADS];
-  int dep[MP_THREADS];
-  float w[8][MP_THREADS];
-};
-constexpr int PUSH_DYN_BYTES = PF_BYTES + (int)sizeof(PendingLeaver);
-
-// arrival number pos of a column goes to slot depth - 1 - pos
-__device__ __forceinline__ void write_pending(const PendingLeaver* pend, int c, int pos, int* err) {
-  if (pos >= pend->dep[c]) {
-    atomicOr(err, EB_CAPACITY);
-    return;
-  }
-  float* io = pend->top[c] - (size_t)pos * MIX_PL;
-#pragma unroll
-  for (int a = 0; a < 8; ++a) io[a] = pend->w[a][c];
-}
-
 // ---------------------------------------------------------------------------
-// fused push + deposit, one CTA per tile, one thread per cell column
-// ---------------------------------------------------------------------------
-// VAY: the push of particle__solv_vay (2d/common/particle.f90:182-315) in place of the
-// Buneman-Boris rotation; gather, move and deposit are the same.
-template <bool VAY>
-__global__ void __launch_bounds__(MP_THREADS, WPIC_MIX_MINB) k_mix_push(Dev2D d, const __grid_constant__ CUtensorMap tm) {
-  // the TMA staging of uf is dead once the cell-centred values exist; its bytes then hold the
-  // fixed-point current planes of the tile
-  __shared__ __align__(128) unsigned char sbuf[(6 * TW * TW * 8 > 2 * 3 * TW * JP * 4) ? 6 * TW * TW * 8
-                                                                                     : 2 * 3 * TW * JP * 4];
-  double(*suf)[TW][TW] = reinterpret_cast<double(*)[TW][TW]>(sbuf);
-  int(*jhi)[TW][JP] = reinterpret_cast<int(*)[TW][JP]>(sbuf);
-  int(*jlo)[TW][JP] = reinterpret_cast<int(*)[TW][JP]>(sbuf + 3 * TW * JP * 4);
-  __shared__ __align__(16) float4 sfa[TT * TT];  // (Bx, By, Bz, Ex) at cell centres
-  __shared__ __align__(8) float2 sfb[TT * TT];   // (Ey, Ez)
-  __shared__ __align__(8) unsigned long long bar;
-  // the 3 x 3 neighbourhood of tiles, per species: bin, first layer, depth
-  __shared__ int nb_bin[2][9], nb_dep[2][9];
-  __shared__ long long nb_off[2][9];
-  extern __shared__ __align__(16) float pfbuf[];  // [PF][7][256] prefetched slots
-  PendingLeaver* pend = reinterpret_cast<PendingLeaver*>(pfbuf + PF * 7 * MIX_TC);
-  const Mix2D& m = d.m;
-  const int tile = blockIdx.x;
-  const int tx = tile % m.ntx, ty = tile / m.ntx;
-  const Grid2D g = d.g;
-  const int c = threadIdx.x;
-  const int nsp = d.ph.nsp;
-  const int bin0 = tile * nsp;
-  const int n0 = m.cnt[bin0 * MIX_TC + c];
-  const int ntot = n0 + (nsp > 1 ? m.cnt[(bin0 + 1) * MIX_TC + c] : 0);
-  if (threadIdx.x < 2 * 9) {
-    const int s = threadIdx.x / 9, q = threadIdx.x % 9;
-    int ntx_ = tx + q % 3 - 1, nty_ = ty + q / 3 - 1;
-    if (ntx_ < 0) ntx_ += m.ntx; else if (ntx_ >= m.ntx) ntx_ -= m.ntx;
-    if (nty_ < 0) nty_ += m.nty; else if (nty_ >= m.nty) nty_ -= m.nty;
-    const int b = (nty_ * m.ntx + ntx_) * nsp + (s < nsp ? s : 0);
-    nb_bin[s][q] = b;
-    nb_dep[s][q] = m.bdep[b];
-    nb_off[s][q] = m.boff[b];
-  }
-  // slot of flattened item t (species 0 items first): col[t >= n0] + t layers
-  float* const col0 = mix_slot(m, bin0, 0, c);
-  float* const col1 = mix_slot(m, bin0 + (nsp > 1 ? 1 : 0), 0, c) - (size_t)n0 * MIX_PL;
-  // each thread streams its own column(s) through a ring of PF particles in shared memory
-  // (cp.async), so PF particle loads per thread are in flight
-  auto issue = [&](int t) {
-    if (t < ntot) {
-      const float* src = (t < n0 ? col0 : col1) + (size_t)t * MIX_PL;
-      float* dst = pfbuf + (t & (PF - 1)) * 7 * MIX_TC + c;
-#pragma unroll
-      for (int a = 0; a < 7; ++a) cp_async4(dst + a * MIX_TC, src + a);
-    }
-    cp_async_commit();
-  };
-#pragma unroll
-  for (int t = 0; t < PF; ++t) issue(t);
-  if (threadIdx.x == 0) mbar_init(&bar, 1);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    mbar_expect_tx(&bar, (unsigned)(6 * TW * TW * sizeof(double)));
-    tma_load_3d(&suf[0][0][0], &tm, tx * MIX_TS, ty * MIX_TS, 0, &bar);
-  }
-  // every thread waits (bounded) for the tile; the CTA gives up together if any wait ran out
-  const bool staged = mbar_wait_bounded(&bar);
-  if (!__syncthreads_and(staged)) {
-    if (threadIdx.x == 0) atomicOr(d.err, EB_STAGING_TIMEOUT);
-    if (!staged) mbar_wait_bounded(&bar);  // second bounded wait for the copy in flight
-    cp_async_wait<0>();
-    return;
-  }
-  // cell-centred fields for local cells -1..16 (2d/common/particle.f90:70-83), FP64 sums rounded to FP32
-  for (int k = threadIdx.x; k < TT * TT; k += MP_THREADS) {
-    const int r = k / TT + 1, cc = k % TT + 1;  // staged node of local cell (cc-2, r-2)
-    sfa[k] = make_float4((float)(0.5 * (suf[0][r][cc] + suf[0][r + 1][cc])),
-                         (float)(0.5 * (suf[1][r][cc] + suf[1][r][cc + 1])),
-                         (float)(0.25 * (suf[2][r][cc] + suf[2][r][cc + 1] + suf[2][r + 1][cc] + suf[2][r + 1][cc + 1])),
-                         (float)(0.5 * (suf[3][r][cc] + suf[3][r][cc + 1])));
-    sfb[k] = make_float2((float)(0.5 * (suf[4][r][cc] + suf[4][r + 1][cc])), (float)suf[5][r][cc]);
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k < 2 * 3 * TW * JP; k += MP_THREADS) (&jhi[0][0][0])[k] = 0;
-  __syncthreads();
-  const float fs1 = m.fx_s1, fs2 = m.fx_s2, fis1 = m.fx_is1f;
-
-  const int lx = c & (MIX_TS - 1), ly = c >> 4;
-  const float dtdx = m.k_dtdx;
-  const float cl = m.k_c;
-  const float ic2 = m.k_ic2;
-  const float third = 1.0f / 3.0f;
-  const bool walls = d.ph.bc != BC_PERIODIC;  // reconnection walls or the shock window: no x wrap
-  const int f0 = ly * TT + lx;  // this cell's 3 x 3 centred-field stencil starts here in sfa / sfb
-  CellCurrent acc;
-  cell_zero(acc);
-  int since = 0;
-  // the column is compacted in place: stayer number j goes to slot j (<= its old slot, whose
-  // contents were already read); leavers go to the top of their new cell's column
-  int j0 = 0, j1 = 0;
-  int ppos = -1;  // arrival number of the pending leaver parked in shared memory, -1 if none
-  for (int t = 0; t < ntot; ++t) {
-    cp_async_wait<PF - 1>();
-    const bool sp1 = t >= n0;
-    const int k = sp1 ? t - n0 : t;
-    const float* pb = pfbuf + (t & (PF - 1)) * 7 * MIX_TC + c;  // word a of the slot at pb[a * 256]
-    const float ox = pb[MIX_OX * MIX_TC], oy = pb[MIX_OY * MIX_TC];
-    float ux = pb[MIX_UX * MIX_TC], uy = pb[MIX_UY * MIX_TC], uz = pb[MIX_UZ * MIX_TC];
-    const float idlo = pb[MIX_IDLO * MIX_TC], idhi = pb[MIX_IDHI * MIX_TC];  // the id's two words, passed through
-    const float fac1 = sp1 ? m.k_fac1[1] : m.k_fac1[0];
-    const float fac2 = sp1 ? m.k_fac2[1] : m.k_fac2[0];
-    const float qdd = sp1 ? m.k_qdd[1] : m.k_qdd[0];
-    const float qs = sp1 ? m.k_q[1] : m.k_q[0];
-    const float txxx = fac1 * fac1;
-    // quadratic spline weights at the old position, offsets -1, 0, +1
-    const float sx0 = 0.5f * (1.f - ox) * (1.f - ox), sx1 = 0.75f - (ox - 0.5f) * (ox - 0.5f), sx2 = 0.5f * ox * ox;
-    const float sy0 = 0.5f * (1.f - oy) * (1.f - oy), sy1 = 0.75f - (oy - 0.5f) * (oy - 0.5f), sy2 = 0.5f * oy * oy;
-    float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-    for (int jy = 0; jy < 3; ++jy) {
-      const float wy = jy == 0 ? sy0 : (jy == 1 ? sy1 : sy2);
-#pragma unroll
-      for (int jx = 0; jx < 3; ++jx) {
-        const float w = wy * (jx == 0 ? sx0 : (jx == 1 ? sx1 : sx2));
-        const float4 a = sfa[f0 + jy * TT + jx];
-        const float2 b = sfb[f0 + jy * TT + jx];
-        ffma2_into(f[0], f[1], w, w, a.x, a.y);
-        ffma2_into(f[2], f[3], w, w, a.z, a.w);
-        ffma2_into(f[4], f[5], w, w, b.x, b.y);
-      }
-    }
-    const float bpx = f[0], bpy = f[1], bpz = f[2], epx = f[3], epy = f[4], epz = f[5];
-    float ig;
-    if constexpr (VAY) {
-      // Vay (2d/common/particle.f90:214-262): gamma of the old momentum, the full electric
-      // kick plus the half rotation, then the implicit rotation solved in closed form; the
-      // move uses the new gamma of that solution
-      const float fac1r = fac1 * rsqrtf(cl * cl + ux * ux + uy * uy + uz * uz);
-      const float u4 = ux + fac2 * epx + fac1r * (uy * bpz - uz * bpy);
-      const float u5 = uy + fac2 * epy + fac1r * (uz * bpx - ux * bpz);
-      const float u6 = uz + fac2 * epz + fac1r * (ux * bpy - uy * bpx);
-      const float icl = ic2 * cl;
-      const float tx = fac1 * bpx * icl, ty = fac1 * bpy * icl, tz = fac1 * bpz * icl;
-      const float tau2 = tx * tx + ty * ty + tz * tz;
-      const float ua = (u4 * tx + u5 * ty + u6 * tz) * icl;
-      const float sigma = 1.f + (u4 * u4 + u5 * u5 + u6 * u6) * ic2 - tau2;
-      const float gam2 = 0.5f * (sigma + sqrtf(sigma * sigma + 4.f * (tau2 + ua * ua)));
-      ig = rsqrtf(gam2);
-      const float gv = gam2 * ig;
-      const float t = __fdividef(1.f, tau2 + gam2);
-      ux = t * (gam2 * u4 + cl * ua * tx + gv * (u5 * tz - u6 * ty));
-      uy = t * (gam2 * u5 + cl * ua * ty + gv * (u6 * tx - u4 * tz));
-      uz = t * (gam2 * u6 + cl * ua * tz + gv * (u4 * ty - u5 * tx));
-    } else {
-      // Buneman-Boris (2d/common/particle.f90:133-155)
-      float u1 = ux + fac1 * epx, u2 = uy + fac1 * epy, u3 = uz + fac1 * epz;
-      const float g2 = cl * cl + u1 * u1 + u2 * u2 + u3 * u3;
-      const float igam = rsqrtf(g2);
-      const float gm = g2 * igam;
-      const float fac1r = fac1 * igam;
-      const float fac2r = __fdividef(fac2, gm + txxx * (bpx * bpx + bpy * bpy + bpz * bpz) * igam);
-      const float u4 = u1 + fac1r * (u2 * bpz - u3 * bpy);
-      const float u5 = u2 + fac1r * (u3 * bpx - u1 * bpz);
-      const float u6 = u3 + fac1r * (u1 * bpy - u2 * bpx);
-      u1 = u1 + fac2r * (u5 * bpz - u6 * bpy);
-      u2 = u2 + fac2r * (u6 * bpx - u4 * bpz);
-      u3 = u3 + fac2r * (u4 * bpy - u5 * bpx);
-      ux = u1 + fac1 * epx;
-      uy = u2 + fac1 * epy;
-      uz = u3 + fac1 * epz;
-      ig = rsqrtf(1.f + (ux * ux + uy * uy + uz * uz) * ic2);
-    }
-    // move in cell units; |displacement| < 1 cell, so the new cell is one of -1, 0, +1
-    float nx_ = ox + ux * dtdx * ig, ny_ = oy + uy * dtdx * ig;
-    int incx = 0, incy = 0;
-    if (nx_ >= 1.f) { nx_ -= 1.f; incx = 1; } else if (nx_ < 0.f) { nx_ += 1.f; incx = -1; }
-    if (ny_ >= 1.f) { ny_ -= 1.f; incy = 1; } else if (ny_ < 0.f) { ny_ += 1.f; incy = -1; }
-    // a step a hair below the cell's lower face: p + 1 rounds to 1, so the particle stays at
-    // offset 0 of the cell it came from (within 2^-25 of its true position)
-    if (nx_ >= 1.f) { nx_ = 0.f; incx += 1; }
-    if (ny_ >= 1.f) { ny_ = 0.f; incy += 1; }
-    if (nx_ < 0.f || nx_ >= 1.f || ny_ < 0.f || ny_ >= 1.f) {
-      atomicOr(d.err, EB_MOVED_TOO_FAR);  // moved a full cell or more (c dt >= dx)
-      nx_ = fminf(fmaxf(nx_, 0.f), 0.99999994f);
-      ny_ = fminf(fmaxf(ny_, 0.f), 0.99999994f);
-    }
-    if (walls) {
-      // reflection about the walls at global cells 1 and nx-2 (nxs+1 and nxe-1 in reference indices),
-      // all three momentum components reversed (2d/proj/reconnection/boundary_reconnection.f90:79-91)
-      // the shock window instead: reflection about cell wx0 + 1 with the momenta reversed, and
-      // beyond xend x -> 2 xend - x, u_x -> 2 u0 - u_x, u_y and u_z reversed
-      // (boundary_shock__injection, 2d/proj/shock/boundary_shock.f90:255-297)
-      // the mirror image X' = 2 W - X in split form (cell + offset): the integer parts cancel
-      // exactly and only the offsets round, so a reflected particle keeps the offset's precision
-      const int gx0 = tx * MIX_TS + lx;
-      int gxn = gx0 + incx;
-      const bool shock = d.ph.bc == BC_SHOCK;
-      const int lo_wall = shock ? g.wx0 + 1 : 1;
-      bool flip = false;
-      if (gxn < lo_wall) {
-        reflect_split(gxn, nx_, lo_wall, 0.f);
-        ux = -ux;
-        flip = true;
-      } else if (shock ? (gxn > m.k_xend_cell || (gxn == m.k_xend_cell && nx_ > m.k_xend_frac)) : gxn >= g.nx - 2) {
-        if (shock) reflect_split(gxn, nx_, m.k_xend_cell, m.k_xend_frac);
-        else reflect_split(gxn, nx_, g.nx - 2, 0.f);
-        ux = shock ? 2.f * m.k_u0 - ux : -ux;
-        flip = true;
-      }
-      if (flip) {
-        uy = -uy; uz = -uz;
-        incx = gxn - gx0;
-        if (incx < -1 || incx > 1) {
-          atomicOr(d.err, EB_MOVED_TOO_FAR);
-          incx = max(-1, min(1, incx));
-        }
-      }
-    }
-    const bool leaves = (incx | incy) != 0;
-    // the slot of the previous leaver has had a whole iteration to return
-    if (ppos >= 0) write_pending(pend, c, ppos, d.err);
-    ppos = -1;
-    if (leaves) {
-      // new cell, and its tile among the 3 x 3 neighbourhood (periodic in y; in x periodic, or
-      // inside the walls)
-      const int nlx = lx + incx, nly = ly + incy;
-      const int q = ((nly >> 4) + 1) * 3 + ((nlx >> 4) + 1);  // >> 4 of -1 is -1
-      const int s = sp1 ? 1 : 0;
-      const int dlc = (nly & (MIX_TS - 1)) * MIX_TS + (nlx & (MIX_TS - 1));
-      const int dep = nb_dep[s][q];
-      ppos = atomicAdd(&m.acnt[nb_bin[s][q] * MIX_TC + dlc], 1);  // used in the next iteration
-      pend->top[c] = m.P + ((size_t)nb_off[s][q] + dep - 1) * MIX_PL + (size_t)dlc * MIX_W;
-      pend->dep[c] = dep;
-      pend->w[0][c] = nx_;
-      pend->w[1][c] = ny_;
-      pend->w[2][c] = ux;
-      pend->w[3][c] = uy;
-      pend->w[4][c] = uz;
-      pend->w[5][c] = idlo;
-      pend->w[6][c] = idhi;
-      pend->w[7][c] = __int_as_float((dir_group((incy + 1) * 3 + (incx + 1)) << 16) | k);
-    } else {
-      float* so = (sp1 ? col1 + (size_t)n0 * MIX_PL : col0) + (size_t)(sp1 ? j1 : j0) * MIX_PL;
-      so[MIX_OX] = nx_;
-      so[MIX_OY] = ny_;
-      so[MIX_UX] = ux;
-      so[MIX_UY] = uy;
-      so[MIX_UZ] = uz;
-      so[MIX_IDLO] = idlo;
-      so[MIX_IDHI] = idhi;
-      if (sp1) ++j1; else ++j0;
-    }
-    // ---- Esirkepov deposition on the cell's full 5 x 5 stencil (2d/common/field.f90:223-298) ----
-    float dsx[5], dsy[5];
-    shape_diff5(ox, nx_, incx, dsx);
-    shape_diff5(oy, ny_, incy, dsy);
-    // the old-position shapes are zero at offsets -2 and +2: those terms are left out (the
-    // results are the same, a signed zero aside, which the fixed-point sums do not see)
-    const float s0x[5] = {0.f, sx0, sx1, sx2, 0.f};
-    const float s0y[5] = {0.f, sy0, sy1, sy2, 0.f};
-    const float qg = qs * uz * ig;  // q * vz
-    const float hq = -0.5f * qdd, hg = 0.5f * qg, tg = third * qg;
-    float wyq[5], wxq[5], zy[5], vy[5];
-#pragma unroll
-    for (int e = 0; e < 5; ++e) {
-      if (e == 0 || e == 4) {
-        wyq[e] = hq * dsy[e];
-        wxq[e] = hq * dsx[e];
-        zy[e] = hg * dsy[e];
-        vy[e] = tg * dsy[e];
-      } else {
-        wyq[e] = -qdd * (s0y[e] + 0.5f * dsy[e]);
-        wxq[e] = -qdd * (s0x[e] + 0.5f * dsx[e]);
-        zy[e] = qg * (s0y[e] + 0.5f * dsy[e]);
-        vy[e] = qg * (0.5f * s0y[e] + third * dsy[e]);
-      }
-    }
-    // accumulators paired (0, 1), (2, 3) along the stencil row for packed FMAs; the s0_x terms of
-    // pair (0, 1) multiply s0_x[0] = 0, which changes nothing but the sign of a zero
-    float px = 0.f, py = 0.f;
-#pragma unroll
-    for (int kk = 0; kk < 4; ++kk) {
-      px += dsx[kk];
-      py += dsy[kk];
-#pragma unroll
-      for (int e = 0; e < 4; e += 2) {
-        ffma2_into(acc.jx[kk][e], acc.jx[kk][e + 1], px, px, wyq[e], wyq[e + 1]);
-        ffma2_into(acc.jy[kk][e], acc.jy[kk][e + 1], py, py, wxq[e], wxq[e + 1]);
-      }
-      acc.jx[kk][4] = fmaf(px, wyq[4], acc.jx[kk][4]);
-      acc.jy[kk][4] = fmaf(py, wxq[4], acc.jy[kk][4]);
-    }
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-      float* const z = acc.jz[j];
-      ffma2_into(z[0], z[1], dsx[0], dsx[1], vy[j], vy[j]);
-      ffma2_into(z[2], z[3], dsx[2], dsx[3], vy[j], vy[j]);
-      z[4] = fmaf(dsx[4], vy[j], z[4]);
-      ffma2_into(z[0], z[1], 0.f, s0x[1], zy[j], zy[j]);
-      ffma2_into(z[2], z[3], s0x[2], s0x[3], zy[j], zy[j]);
-    }
-    if (++since == FLUSH_EVERY) {
-      cell_flush(acc, jhi, jlo, lx, ly, fs1, fis1, fs2);
-      since = 0;
-    }
-    issue(t + PF);
-  }
-  cp_async_wait<0>();
-  if (ppos >= 0) write_pending(pend, c, ppos, d.err);
-  m.ccnt[bin0 * MIX_TC + c] = j0;
-  if (nsp > 1) m.ccnt[(bin0 + 1) * MIX_TC + c] = j1;
-  if (since) cell_flush(acc, jhi, jlo, lx, ly, fs1, fis1, fs2);
-  __syncthreads();
-  // one flush of the tile into the global fixed-point current (exact 64-bit integer sums, so the
-  // result does not depend on the order of the tiles); nodes wrap periodically in y, and in x
-  // unless walls
-  for (int k = threadIdx.x; k < 3 * TW * TW; k += MP_THREADS) {
-    const int w = (k / TW) * JP + k % TW;
-    const int ih = (&jhi[0][0][0])[w], il = (&jlo[0][0][0])[w];
-    if ((ih | il) == 0) continue;
-    const long long v = (long long)ih * 32768LL + (long long)il;
-    const int comp = k / (TW * TW), r = (k / TW) % TW, cc = k % TW;
-    int gx = tx * MIX_TS + cc - 2, gy = ty * MIX_TS + r - 2;
-    if (gy < 0) gy += g.ny; else if (gy >= g.ny) gy -= g.ny;
-    if (!walls) {
-      if (gx < 0) gx += g.nx; else if (gx >= g.nx) gx -= g.nx;
-    }
-    atomicAdd(&m.ujx[(size_t)comp * g.fplane + (size_t)(gy + 2) * g.fp + gx + 2], (unsigned long long)v);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// The push with the register current for the particles that stay in their cell only
-// (WPIC_MIX_PUSH2): a stayer's Esirkepov support is its cell's 3 x 3 nodes, so 21 registers
+// The push with the register current for the particles that stay in their cell only:
+// a stayer's Esirkepov support is its cell's 3 x 3 nodes, so 21 registers
 // hold it (2 x 3 x-edges, 3 x 2 y-edges, 3 x 3 z-nodes); a particle that changes cell (4 in 100
 // per step on the 2D Weibel workload) joins its warp's queue, and 32 of them at a time, one lane each, claim their
 // arrival slots, are deposited straight into the tile's fixed-point current and are written to
@@ -960,19 +557,12 @@ __global__ void __launch_bounds__(MP_THREADS, 3) k_mix_push2(Dev2D d, const __gr
 
 void mix_push_deposit2d(const Dev2D& d, const void* tmap, bool vay, cudaStream_t s) {
   cudaMemsetAsync(d.m.ujx, 0, sizeof(unsigned long long) * 3 * (size_t)d.g.fplane, s);
-#if WPIC_MIX_PUSH2
   const CUtensorMap& tm = *(const CUtensorMap*)tmap;
   const bool walls = d.ph.bc != BC_PERIODIC;
   if (vay && walls) k_mix_push2<true, true><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, tm);
   else if (vay) k_mix_push2<true, false><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, tm);
   else if (walls) k_mix_push2<false, true><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, tm);
   else k_mix_push2<false, false><<<d.m.ntile, MP_THREADS, PUSH2_SMEM, s>>>(d, tm);
-#else
-  if (vay)
-    k_mix_push<true><<<d.m.ntile, MP_THREADS, PUSH_DYN_BYTES, s>>>(d, *(const CUtensorMap*)tmap);
-  else
-    k_mix_push<false><<<d.m.ntile, MP_THREADS, PUSH_DYN_BYTES, s>>>(d, *(const CUtensorMap*)tmap);
-#endif
 }
 
 // fixed point -> FP64 current over the whole ghosted extent
@@ -1646,11 +1236,7 @@ int mix_setup2d(const Dev2D& d, void* out) {
                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return -2;
-  if (cudaFuncSetAttribute(k_mix_push<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH_DYN_BYTES) !=
-          cudaSuccess ||
-      cudaFuncSetAttribute(k_mix_push<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH_DYN_BYTES) !=
-          cudaSuccess ||
-      cudaFuncSetAttribute(k_mix_push2<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
+  if (cudaFuncSetAttribute(k_mix_push2<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
           cudaSuccess ||
       cudaFuncSetAttribute(k_mix_push2<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PUSH2_SMEM) !=
           cudaSuccess ||
